@@ -1,0 +1,2 @@
+// forwarding header of the glm-subset shim (oracle build only)
+#include <glm/glm.hpp>

@@ -1,0 +1,213 @@
+// Reference renderer: replays a scene stream (skity_gb300/scene.py layout)
+// through the UNMODIFIED reference software backend -- Canvas::
+// MakeSoftwareCanvas(Bitmap*) (src/render/sw/sw_canvas.cc:146-156), Clear,
+// one DrawPath per draw, Flush -- and writes the premultiplied RGBA8 pixels.
+//
+// Built only from the reference sources by oracle/ref/Makefile into
+// oracle/_ref/ref_render. Test infrastructure: golden vectors and the oracle
+// pin come from here.
+//
+// usage: ref_render <scene.bin> <out.rgba> [first count] [--time]
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <skity/effect/mask_filter.hpp>
+#include <skity/effect/shader.hpp>
+#include <skity/graphic/bitmap.hpp>
+#include <skity/graphic/paint.hpp>
+#include <skity/graphic/path.hpp>
+#include <skity/render/canvas.hpp>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct PaintRec {
+  uint32_t style, cap, join, blend, fill_type;
+  int32_t gradient;
+  uint32_t blur_style;
+  float blur_radius;
+  float fill_color[4];
+  float stroke_color[4];
+  float stroke_width, miter;
+  uint32_t reserved[2];
+};
+static_assert(sizeof(PaintRec) == 80, "paint record layout");
+
+struct GradRec {
+  uint32_t type, tile_mode, stop_count, stop_start, has_offsets, reserved;
+  float p0[2], p1[2], radius[2];
+};
+static_assert(sizeof(GradRec) == 48, "gradient record layout");
+
+struct Scene {
+  uint32_t width = 0, height = 0, has_clear = 0;
+  float clear[4] = {0, 0, 0, 0};
+  std::vector<uint32_t> vo, po, wo;
+  std::vector<uint8_t> verbs;
+  std::vector<float> pts, wts;
+  std::vector<PaintRec> paints;
+  std::vector<GradRec> grads;
+  std::vector<float> stop_colors, stop_offsets;
+};
+
+template <typename T>
+void Take(const std::vector<char>& buf, size_t& o, std::vector<T>& dst,
+          size_t n) {
+  dst.resize(n);
+  if (n) std::memcpy(dst.data(), buf.data() + o, n * sizeof(T));
+  o += n * sizeof(T);
+}
+
+bool Load(const char* path, Scene* s) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  std::vector<char> buf((std::istreambuf_iterator<char>(f)),
+                        std::istreambuf_iterator<char>());
+  if (buf.size() < 80 || std::memcmp(buf.data(), "SKSC", 4) != 0) return false;
+  uint32_t hdr[7];
+  std::memcpy(hdr, buf.data() + 4, sizeof(hdr));
+  if (hdr[0] != 1) return false;
+  s->width = hdr[1];
+  s->height = hdr[2];
+  s->has_clear = hdr[3];
+  size_t o = 32;
+  std::memcpy(s->clear, buf.data() + o, 16);
+  o += 16;
+  uint32_t cnt[6];
+  std::memcpy(cnt, buf.data() + o, sizeof(cnt));
+  o += sizeof(cnt);
+  uint32_t nd = cnt[0];
+  Take(buf, o, s->vo, nd + 1);
+  Take(buf, o, s->po, nd + 1);
+  Take(buf, o, s->wo, nd + 1);
+  Take(buf, o, s->verbs, cnt[1]);
+  o += (4 - cnt[1] % 4) % 4;
+  Take(buf, o, s->pts, 2 * size_t(cnt[2]));
+  Take(buf, o, s->wts, cnt[3]);
+  Take(buf, o, s->paints, nd);
+  Take(buf, o, s->grads, cnt[4]);
+  Take(buf, o, s->stop_colors, 4 * size_t(cnt[5]));
+  Take(buf, o, s->stop_offsets, cnt[5]);
+  return o <= buf.size();
+}
+
+skity::Path BuildPath(const Scene& s, uint32_t d) {
+  skity::Path path;
+  const float* p = s.pts.data() + 2 * size_t(s.po[d]);
+  const float* w = s.wts.data() + s.wo[d];
+  for (uint32_t v = s.vo[d]; v < s.vo[d + 1]; ++v) {
+    switch (s.verbs[v]) {
+      case 0: path.MoveTo(p[0], p[1]); p += 2; break;
+      case 1: path.LineTo(p[0], p[1]); p += 2; break;
+      case 2: path.QuadTo(p[0], p[1], p[2], p[3]); p += 4; break;
+      case 3: path.ConicTo(p[0], p[1], p[2], p[3], *w++); p += 4; break;
+      case 4: path.CubicTo(p[0], p[1], p[2], p[3], p[4], p[5]); p += 6; break;
+      case 5: path.Close(); break;
+      default: break;
+    }
+  }
+  path.SetFillType(s.paints[d].fill_type == 1
+                       ? skity::Path::PathFillType::kEvenOdd
+                       : skity::Path::PathFillType::kWinding);
+  return path;
+}
+
+skity::Paint BuildPaint(const Scene& s, uint32_t d) {
+  const PaintRec& r = s.paints[d];
+  skity::Paint paint;
+  paint.SetStyle(static_cast<skity::Paint::Style>(r.style));
+  paint.SetStrokeCap(static_cast<skity::Paint::Cap>(r.cap));
+  paint.SetStrokeJoin(static_cast<skity::Paint::Join>(r.join));
+  paint.SetBlendMode(static_cast<skity::BlendMode>(r.blend));
+  paint.SetFillColor(r.fill_color[0], r.fill_color[1], r.fill_color[2],
+                     r.fill_color[3]);
+  paint.SetStrokeColor(r.stroke_color[0], r.stroke_color[1], r.stroke_color[2],
+                       r.stroke_color[3]);
+  paint.SetStrokeWidth(r.stroke_width);
+  paint.SetStrokeMiter(r.miter);
+  if (r.gradient >= 0) {
+    const GradRec& g = s.grads[r.gradient];
+    std::vector<skity::Vec4> colors(g.stop_count);
+    for (uint32_t i = 0; i < g.stop_count; ++i) {
+      const float* c = s.stop_colors.data() + 4 * size_t(g.stop_start + i);
+      colors[i] = skity::Vec4{c[0], c[1], c[2], c[3]};
+    }
+    const float* pos =
+        g.has_offsets ? s.stop_offsets.data() + g.stop_start : nullptr;
+    auto tile = static_cast<skity::TileMode>(g.tile_mode);
+    if (g.type == 1) {
+      skity::Point pts[2] = {skity::Point{g.p0[0], g.p0[1], 0, 1},
+                             skity::Point{g.p1[0], g.p1[1], 0, 1}};
+      paint.SetShader(skity::Shader::MakeLinear(pts, colors.data(), pos,
+                                                int(g.stop_count), tile));
+    } else if (g.type == 2) {
+      paint.SetShader(skity::Shader::MakeRadial(
+          skity::Point{g.p0[0], g.p0[1], 0, 1}, g.radius[0], colors.data(),
+          pos, int(g.stop_count), tile));
+    }
+  }
+  if (r.blur_style != 0) {
+    paint.SetMaskFilter(skity::MaskFilter::MakeBlur(
+        static_cast<skity::BlurStyle>(r.blur_style), r.blur_radius));
+  }
+  return paint;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::fprintf(stderr, "usage: %s scene.bin out.rgba [first count] [--time]\n",
+                 argv[0]);
+    return 2;
+  }
+  Scene s;
+  if (!Load(argv[1], &s)) {
+    std::fprintf(stderr, "cannot read scene %s\n", argv[1]);
+    return 2;
+  }
+  uint32_t first = 0, count = uint32_t(s.paints.size());
+  bool timed = false;
+  int pos = 3;
+  if (argc >= 5 && argv[3][0] != '-') {
+    first = uint32_t(std::strtoul(argv[3], nullptr, 10));
+    count = uint32_t(std::strtoul(argv[4], nullptr, 10));
+    pos = 5;
+  }
+  for (; pos < argc; ++pos) timed |= std::strcmp(argv[pos], "--time") == 0;
+  uint32_t last = std::min<uint32_t>(first + count, uint32_t(s.paints.size()));
+
+  // Inputs are built before the timed region (scene load is not timed).
+  std::vector<skity::Path> paths;
+  std::vector<skity::Paint> paints;
+  for (uint32_t d = first; d < last; ++d) {
+    paths.push_back(BuildPath(s, d));
+    paints.push_back(BuildPaint(s, d));
+  }
+  skity::Bitmap bitmap(s.width, s.height, skity::AlphaType::kPremul_AlphaType);
+  auto t0 = std::chrono::steady_clock::now();
+  auto canvas = skity::Canvas::MakeSoftwareCanvas(&bitmap);
+  if (!canvas) return 3;
+  if (s.has_clear) {
+    canvas->Clear(skity::Color4f{s.clear[0], s.clear[1], s.clear[2], s.clear[3]});
+  }
+  for (size_t i = 0; i < paths.size(); ++i) canvas->DrawPath(paths[i], paints[i]);
+  canvas->Flush();
+  auto t1 = std::chrono::steady_clock::now();
+  if (timed) {
+    std::printf("{\"seconds\": %.6f, \"draws\": %zu}\n",
+                std::chrono::duration<double>(t1 - t0).count(), paths.size());
+  }
+  std::ofstream out(argv[2], std::ios::binary);
+  for (uint32_t y = 0; y < s.height; ++y) {
+    out.write(reinterpret_cast<const char*>(bitmap.GetPixelAddr() +
+                                            size_t(y) * bitmap.RowBytes()),
+              std::streamsize(size_t(s.width) * 4));
+  }
+  return 0;
+}

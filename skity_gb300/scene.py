@@ -1,0 +1,451 @@
+"""Draw streams ("scenes") and the seeded synthetic scene generator.
+
+A scene is one canvas's worth of work in the form the C-ABI consumes: an
+optional ``Canvas::Clear`` colour followed by ``Canvas::DrawPath`` calls in
+order.  It is stored as flat little-endian arrays (plain pointers + sizes at
+the C boundary, see ``include/skity_cuda.h``):
+
+* ``verbs``   u8, skity ``Path::Verb`` values (kMove=0, kLine=1, kQuad=2,
+  kConic=3, kCubic=4, kClose=5; include/skity/graphic/path.hpp:45-60);
+* ``points``  f32 (x, y) pairs, one per verb point as ``Path::points_`` holds
+  them (include/skity/graphic/path.hpp:590);
+* ``weights`` f32 conic weights (``Path::conic_weights_``);
+* per draw: verb/point/weight offsets and one 80-byte paint record mirroring
+  ``skity::Paint`` (include/skity/graphic/paint.hpp:46-285);
+* gradient records (``Shader::MakeLinear`` / ``MakeRadial``,
+  src/effect/gradient_shader.cc:96-158) and their colour stops.
+
+The binary file layout (``Scene.to_bytes``) is read by the CPU oracle, by the
+reference-driver recipe and by the C-ABI batch entry point.
+
+Random numbers: SplitMix64-seeded xoshiro256**, one independent stream per
+path (seed, path index), vectorised over paths with numpy uint64 arithmetic,
+so a scene is bit-identical on every machine and numpy version.
+"""
+from __future__ import annotations
+
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Path::Verb
+MOVE, LINE, QUAD, CONIC, CUBIC, CLOSE = 0, 1, 2, 3, 4, 5
+VERB_POINTS = {MOVE: 1, LINE: 1, QUAD: 2, CONIC: 2, CUBIC: 3, CLOSE: 0}
+# Paint::Style / Cap / Join, BlendMode, Path::PathFillType, TileMode
+FILL, STROKE, STROKE_AND_FILL, STROKE_THEN_FILL = 0, 1, 2, 3
+BUTT, ROUND, SQUARE = 0, 1, 2
+MITER_JOIN, ROUND_JOIN, BEVEL_JOIN = 0, 1, 2
+BLEND_CLEAR, BLEND_SRC, BLEND_DST, BLEND_SRC_OVER = 0, 1, 2, 3
+WINDING, EVEN_ODD = 0, 1
+TILE_CLAMP, TILE_REPEAT, TILE_MIRROR, TILE_DECAL = 0, 1, 2, 3
+GRAD_LINEAR, GRAD_RADIAL = 1, 2
+BLUR_NONE, BLUR_NORMAL = 0, 1
+
+MAGIC = b"SKSC"
+VERSION = 1
+
+# paint record: 20 x 4 bytes (matches skity_cuda_paint in include/skity_cuda.h)
+PAINT_DTYPE = np.dtype([
+    ("style", "<u4"), ("cap", "<u4"), ("join", "<u4"), ("blend", "<u4"),
+    ("fill_type", "<u4"), ("gradient", "<i4"), ("blur_style", "<u4"),
+    ("blur_radius", "<f4"), ("fill_color", "<f4", 4), ("stroke_color", "<f4", 4),
+    ("stroke_width", "<f4"), ("miter", "<f4"), ("reserved", "<u4", 2)])
+assert PAINT_DTYPE.itemsize == 80
+# gradient record: 12 x 4 bytes (matches skity_cuda_gradient)
+GRADIENT_DTYPE = np.dtype([
+    ("type", "<u4"), ("tile_mode", "<u4"), ("stop_count", "<u4"),
+    ("stop_start", "<u4"), ("has_offsets", "<u4"), ("reserved", "<u4"),
+    ("p0", "<f4", 2), ("p1", "<f4", 2), ("radius", "<f4", 2)])
+assert GRADIENT_DTYPE.itemsize == 48
+
+
+def default_paint() -> np.ndarray:
+    """A ``skity::Paint()`` as constructed (paint.hpp:274-285): fill style,
+    butt cap, miter join, width 1, miter limit 4, opaque black, src-over."""
+    p = np.zeros((), PAINT_DTYPE)
+    p["blend"] = BLEND_SRC_OVER
+    p["gradient"] = -1
+    p["fill_color"] = (0.0, 0.0, 0.0, 1.0)
+    p["stroke_color"] = (0.0, 0.0, 0.0, 1.0)
+    p["stroke_width"] = 1.0
+    p["miter"] = 4.0
+    return p
+
+
+@dataclass
+class Scene:
+    width: int
+    height: int
+    clear: tuple | None = (1.0, 1.0, 1.0, 1.0)
+    verbs: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint8))
+    points: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.float32))
+    weights: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    verb_off: np.ndarray = field(default_factory=lambda: np.zeros(1, np.uint32))
+    point_off: np.ndarray = field(default_factory=lambda: np.zeros(1, np.uint32))
+    weight_off: np.ndarray = field(default_factory=lambda: np.zeros(1, np.uint32))
+    paints: np.ndarray = field(default_factory=lambda: np.zeros(0, PAINT_DTYPE))
+    gradients: np.ndarray = field(default_factory=lambda: np.zeros(0, GRADIENT_DTYPE))
+    stop_colors: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.float32))
+    stop_offsets: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+
+    @property
+    def n_draws(self) -> int:
+        return len(self.paints)
+
+    def to_bytes(self) -> bytes:
+        nd = self.n_draws
+        out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
+                                  1 if self.clear is not None else 0, 0, 0, 0)]
+        out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
+                              np.float32).tobytes())
+        out.append(struct.pack("<6I", nd, len(self.verbs), len(self.points),
+                               len(self.weights), len(self.gradients), len(self.stop_offsets)))
+        for a in (self.verb_off, self.point_off, self.weight_off):
+            assert len(a) == nd + 1
+            out.append(np.ascontiguousarray(a, np.uint32).tobytes())
+        vb = np.ascontiguousarray(self.verbs, np.uint8).tobytes()
+        out.append(vb + b"\0" * ((-len(vb)) % 4))
+        out.append(np.ascontiguousarray(self.points, np.float32).tobytes())
+        out.append(np.ascontiguousarray(self.weights, np.float32).tobytes())
+        out.append(np.ascontiguousarray(self.paints, PAINT_DTYPE).tobytes())
+        out.append(np.ascontiguousarray(self.gradients, GRADIENT_DTYPE).tobytes())
+        out.append(np.ascontiguousarray(self.stop_colors, np.float32).tobytes())
+        out.append(np.ascontiguousarray(self.stop_offsets, np.float32).tobytes())
+        return b"".join(out)
+
+    @staticmethod
+    def from_bytes(buf: bytes) -> "Scene":
+        if buf[:4] != MAGIC:
+            raise ValueError("not a scene stream")
+        ver, w, h, has_clear, _, _, _ = struct.unpack_from("<7I", buf, 4)
+        if ver != VERSION:
+            raise ValueError(f"scene version {ver}")
+        o = 32
+        clear = tuple(np.frombuffer(buf, np.float32, 4, o).tolist()); o += 16
+        nd, nv, npt, nw, ng, ns = struct.unpack_from("<6I", buf, o); o += 24
+
+        def take(dt, n, shape=None):
+            nonlocal o
+            a = np.frombuffer(buf, dt, n, o).copy()
+            o += a.nbytes
+            return a.reshape(shape) if shape else a
+        vo = take(np.uint32, nd + 1); po = take(np.uint32, nd + 1); wo = take(np.uint32, nd + 1)
+        verbs = take(np.uint8, nv); o += (-nv) % 4
+        pts = take(np.float32, 2 * npt, (npt, 2))
+        wts = take(np.float32, nw)
+        paints = take(PAINT_DTYPE, nd)
+        grads = take(GRADIENT_DTYPE, ng)
+        sc = take(np.float32, 4 * ns, (ns, 4))
+        so = take(np.float32, ns)
+        return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
+                     paints, grads, sc, so)
+
+    def subset(self, first: int, count: int) -> "Scene":
+        """Draws [first, first+count) of this scene, same canvas and clear."""
+        last = min(self.n_draws, first + count)
+        v0, v1 = int(self.verb_off[first]), int(self.verb_off[last])
+        p0, p1 = int(self.point_off[first]), int(self.point_off[last])
+        w0, w1 = int(self.weight_off[first]), int(self.weight_off[last])
+        paints = self.paints[first:last].copy()
+        used = sorted({int(g) for g in paints["gradient"] if g >= 0})
+        remap = {g: i for i, g in enumerate(used)}
+        grads = self.gradients[used].copy() if used else np.zeros(0, GRADIENT_DTYPE)
+        sc, so, start = [], [], 0
+        for i, g in enumerate(used):
+            s0, n = int(self.gradients[g]["stop_start"]), int(self.gradients[g]["stop_count"])
+            sc.append(self.stop_colors[s0:s0 + n]); so.append(self.stop_offsets[s0:s0 + n])
+            grads[i]["stop_start"] = start; start += n
+        for p in paints:
+            if p["gradient"] >= 0:
+                p["gradient"] = remap[int(p["gradient"])]
+        return Scene(self.width, self.height, self.clear,
+                     self.verbs[v0:v1].copy(), self.points[p0:p1].copy(),
+                     self.weights[w0:w1].copy(),
+                     (self.verb_off[first:last + 1] - v0).astype(np.uint32),
+                     (self.point_off[first:last + 1] - p0).astype(np.uint32),
+                     (self.weight_off[first:last + 1] - w0).astype(np.uint32),
+                     paints, grads,
+                     np.concatenate(sc) if sc else np.zeros((0, 4), np.float32),
+                     np.concatenate(so) if so else np.zeros(0, np.float32))
+
+
+class SceneBuilder:
+    """Appends Canvas::DrawPath calls to a Scene, the way skity::Path builds
+    its verb/point arrays (src/graphic/path.cc:494-569, 837-860)."""
+
+    def __init__(self, width: int, height: int, clear=(1.0, 1.0, 1.0, 1.0)):
+        self.width, self.height, self.clear = width, height, clear
+        self._verbs, self._pts, self._wts = [], [], []
+        self._vo, self._po, self._wo = [0], [0], [0]
+        self._paints, self._grads, self._sc, self._so = [], [], [], []
+        self._nv = self._np = self._nw = 0
+
+    def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
+                     tile_mode=TILE_CLAMP) -> int:
+        g = np.zeros((), GRADIENT_DTYPE)
+        g["type"], g["tile_mode"] = kind, tile_mode
+        colors = np.asarray(colors, np.float32).reshape(-1, 4)
+        g["stop_count"] = len(colors)
+        g["stop_start"] = sum(len(c) for c in self._sc)
+        g["has_offsets"] = 1 if offsets is not None else 0
+        g["p0"], g["p1"], g["radius"] = p0, p1, radius
+        self._grads.append(g)
+        self._sc.append(colors)
+        self._so.append(np.asarray(offsets if offsets is not None
+                                   else np.zeros(len(colors)), np.float32))
+        return len(self._grads) - 1
+
+    def draw_path(self, verbs, points, paint, weights=()):
+        verbs = np.asarray(verbs, np.uint8)
+        points = np.asarray(points, np.float32).reshape(-1, 2)
+        self._verbs.append(verbs); self._pts.append(points)
+        self._wts.append(np.asarray(weights, np.float32))
+        self._nv += len(verbs); self._np += len(points); self._nw += len(weights)
+        self._vo.append(self._nv); self._po.append(self._np); self._wo.append(self._nw)
+        self._paints.append(paint)
+
+    def build(self) -> Scene:
+        cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
+        return Scene(self.width, self.height, self.clear,
+                     cat(self._verbs, np.uint8, 0), cat(self._pts, np.float32, (0, 2)),
+                     cat(self._wts, np.float32, 0),
+                     np.asarray(self._vo, np.uint32), np.asarray(self._po, np.uint32),
+                     np.asarray(self._wo, np.uint32),
+                     np.array(self._paints, PAINT_DTYPE) if self._paints else np.zeros(0, PAINT_DTYPE),
+                     np.array(self._grads, GRADIENT_DTYPE) if self._grads else np.zeros(0, GRADIENT_DTYPE),
+                     cat(self._sc, np.float32, (0, 4)), cat(self._so, np.float32, 0))
+
+
+# ---------------------------------------------------------------------------
+# Seeded random streams: SplitMix64 -> xoshiro256**, vectorised over streams.
+# ---------------------------------------------------------------------------
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _rotl(x, k):
+    return (x << np.uint64(k)) | (x >> np.uint64(64 - k))
+
+
+def _splitmix64(x):
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    z = x
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x, z ^ (z >> np.uint64(31))
+
+
+def random_streams(seed: int, n_streams: int, n_draws: int) -> np.ndarray:
+    """(n_streams, n_draws) uint64: stream i is xoshiro256** seeded by a
+    SplitMix64 over (seed, i)."""
+    with np.errstate(over="ignore"):
+        x = (np.uint64(seed & 0xFFFFFFFFFFFFFFFF)
+             ^ (np.arange(n_streams, dtype=np.uint64) * np.uint64(0xD1B54A32D192ED03)))
+        s = []
+        for _ in range(4):
+            x, z = _splitmix64(x)
+            s.append(z)
+        s0, s1, s2, s3 = s
+        out = np.empty((n_streams, n_draws), np.uint64)
+        for k in range(n_draws):
+            out[:, k] = _rotl(s1 * np.uint64(5), 7) * np.uint64(9)
+            t = s1 << np.uint64(17)
+            s2 ^= s0; s3 ^= s1; s1 ^= s2; s0 ^= s3
+            s2 ^= t
+            s3 = _rotl(s3, 45)
+    return out
+
+
+def u01(u: np.ndarray) -> np.ndarray:
+    """uint64 -> float32 in [0,1): (u >> 40) * 2^-24 (exact in float32)."""
+    return ((u >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24))
+
+
+def uniform(u, lo, hi) -> np.ndarray:
+    return (np.float32(lo) + u01(u) * np.float32(hi - lo)).astype(np.float32)
+
+
+def randint(u, lo, hi) -> np.ndarray:
+    """Integer uniform on [lo, hi] inclusive (multiply-shift on the top 32 bits)."""
+    span = np.uint64(hi - lo + 1)
+    return (np.int64(lo) + ((u >> np.uint64(32)) * span >> np.uint64(32)).astype(np.int64))
+
+
+def loguniform(u, lo, hi) -> np.ndarray:
+    f = u01(u).astype(np.float64)
+    return np.exp(np.log(lo) + f * (np.log(hi) - np.log(lo)))
+
+
+def _color4f_from_rgb_bytes(r, g, b, a):
+    """Paint::SetColor(ARGB(255,r,g,b)) -> Color4fFromColor (c / 255.f) then
+    SetAlphaF(a) (src/graphic/paint.cc:77-101, src/graphic/color.cc:44-51)."""
+    f = np.float32(255.0)
+    return np.stack([np.asarray(r, np.float32) / f, np.asarray(g, np.float32) / f,
+                     np.asarray(b, np.float32) / f, np.asarray(a, np.float32)], -1)
+
+
+# ---------------------------------------------------------------------------
+# Workloads (the five benchmark configurations, seeded synthetic data)
+# ---------------------------------------------------------------------------
+SEED_BASE = 0x5EED0000
+_VERB_SLOTS = 7  # per verb: kind selector + up to 3 points
+
+
+def random_paths_scene(seed, width, height, n_paths, verbs_lo, verbs_hi,
+                       coord_lo=(0.0, 0.0), coord_hi=None, evenodd_frac=0.0,
+                       gradient_frac=0.0, stroke_frac=0.0, clear=(1.0, 1.0, 1.0, 1.0)) -> Scene:
+    """Random closed paths: MoveTo + n verbs (50% LineTo, 25% QuadTo,
+    25% CubicTo) + Close, control points uniform over [coord_lo, coord_hi]."""
+    if coord_hi is None:
+        coord_hi = (float(width), float(height))
+    base = 24
+    K = base + _VERB_SLOTS * verbs_hi
+    R = random_streams(seed, n_paths, K)
+    nverb = randint(R[:, 0], verbs_lo, verbs_hi)
+    fill_type = np.where(u01(R[:, 1]) < np.float32(evenodd_frac), EVEN_ODD, WINDING)
+    kind_u = u01(R[:, 2])
+    stroke = u01(R[:, 3]) < np.float32(stroke_frac)
+    width_s = uniform(R[:, 4], 1.0, 8.0)
+    cap = randint(R[:, 5], 0, 2)
+    join = randint(R[:, 6], 0, 2)
+    rgb = [randint(R[:, 7 + i], 0, 255) for i in range(3)]
+    alpha = uniform(R[:, 10], 0.3, 1.0)
+    colors = _color4f_from_rgb_bytes(*rgb, alpha)
+    grad_kind = np.where(kind_u < np.float32(1.0 - gradient_frac), 0,
+                         np.where(kind_u < np.float32(1.0 - gradient_frac / 2), GRAD_LINEAR, GRAD_RADIAL))
+    mx = uniform(R[:, 22], coord_lo[0], coord_hi[0])
+    my = uniform(R[:, 23], coord_lo[1], coord_hi[1])
+    vsel = u01(R[:, base::_VERB_SLOTS][:, :verbs_hi])
+    cx = [uniform(R[:, base + 1 + 2 * j::_VERB_SLOTS][:, :verbs_hi], coord_lo[0], coord_hi[0]) for j in range(3)]
+    cy = [uniform(R[:, base + 2 + 2 * j::_VERB_SLOTS][:, :verbs_hi], coord_lo[1], coord_hi[1]) for j in range(3)]
+
+    b = SceneBuilder(width, height, clear)
+    gradR = random_streams(seed ^ 0x6A09E667F3BCC908, n_paths, 48) if gradient_frac > 0 else None
+    for i in range(n_paths):
+        n = int(nverb[i])
+        sel = vsel[i, :n]
+        kinds = np.where(sel < 0.5, LINE, np.where(sel < 0.75, QUAD, CUBIC)).astype(np.uint8)
+        verbs = np.concatenate([[MOVE], kinds, [CLOSE]]).astype(np.uint8)
+        npts = np.where(kinds == LINE, 1, np.where(kinds == QUAD, 2, 3))
+        pts = [np.array([[mx[i], my[i]]], np.float32)]
+        for j in range(n):
+            k = int(npts[j])
+            pts.append(np.stack([[cx[t][i, j], cy[t][i, j]] for t in range(k)]).astype(np.float32))
+        pts = np.concatenate(pts)
+        p = default_paint()
+        p["fill_type"] = fill_type[i]
+        p["fill_color"] = colors[i]
+        p["stroke_color"] = colors[i]
+        if stroke[i]:
+            p["style"] = STROKE
+            p["stroke_width"] = width_s[i]
+            p["cap"] = cap[i]
+            p["join"] = join[i]
+        if grad_kind[i]:
+            g = gradR[i]
+            ns = int(randint(g[0], 2, 8))
+            offs = np.sort(u01(g[1:1 + ns]))
+            offs[0], offs[-1] = 0.0, 1.0
+            sc = np.stack([randint(g[10 + 4 * s + c], 0, 255) for s in range(ns) for c in range(4)]
+                          ).reshape(ns, 4).astype(np.float32) / np.float32(255.0)
+            lo, hi = pts.min(0), pts.max(0)
+            if grad_kind[i] == GRAD_LINEAR:
+                p0 = (uniform(g[42], lo[0], hi[0]), uniform(g[43], lo[1], hi[1]))
+                p1 = (uniform(g[44], lo[0], hi[0]), uniform(g[45], lo[1], hi[1]))
+                gi = b.add_gradient(GRAD_LINEAR, p0, p1, (0.0, 0.0), sc, offs)
+            else:
+                c = (uniform(g[42], lo[0], hi[0]), uniform(g[43], lo[1], hi[1]))
+                half_diag = np.float32(0.5) * np.float32(np.hypot(*(hi - lo).astype(np.float64)))
+                r = np.float32(uniform(g[44], 0.25, 1.0) * half_diag)
+                gi = b.add_gradient(GRAD_RADIAL, c, (0.0, 0.0), (r, 0.0), sc, offs)
+            p["gradient"] = gi
+        b.draw_path(verbs, pts, p)
+    return b.build()
+
+
+def config1(seed=SEED_BASE + 1, n_paths=1000) -> Scene:
+    """512x512, cleared white, 1,000 random filled paths of 3-32 verbs."""
+    return random_paths_scene(seed, 512, 512, n_paths, 3, 32)
+
+
+def config2(seed=SEED_BASE + 2, n_paths=20000, width=2048, height=2048) -> Scene:
+    """2048x2048, 20,000 paths of 3-64 verbs over [-64,2112]^2; 30% even-odd;
+    50% solid / 25% linear / 25% radial gradient; 20% stroked."""
+    return random_paths_scene(seed, width, height, n_paths, 3, 64,
+                              coord_lo=(-64.0, -64.0), coord_hi=(width + 64.0, height + 64.0),
+                              evenodd_frac=0.3, gradient_frac=0.5, stroke_frac=0.2)
+
+
+def config3(seed=SEED_BASE + 3, n_canvases=256, scale=1.0):
+    """256 canvases with log-uniform sides in [64,1024] and log-uniform
+    50-2,000 paths each, drawn as in config 1."""
+    R = random_streams(seed, n_canvases, 4)
+    out = []
+    for i in range(n_canvases):
+        w = int(round(float(loguniform(R[i, 0], 64, 1024))))
+        h = int(round(float(loguniform(R[i, 1], 64, 1024))))
+        n = max(1, int(round(float(loguniform(R[i, 2], 50, 2000)) * scale)))
+        out.append(random_paths_scene(int(R[i, 3]), w, h, n, 3, 32))
+    return out
+
+
+def config4(seed=SEED_BASE + 4, n_outlines=100000, width=4096, height=4096,
+            blur_frac=0.1) -> Scene:
+    """4096x4096 glyph-dense scene: closed cubic outlines (8-40 verbs total,
+    1-3 contours, inner contours smaller and wound the other way) scaled into
+    8-48 px boxes at uniform positions, even-odd fill, solid colours; a tenth
+    carry a kNormal blur mask filter with sigma ~ U[2,20] px, passed to
+    MaskFilter::MakeBlur as the radius (sigma - 0.5) / 0.57735
+    (src/effect/image_filter_base.hpp:32-41)."""
+    A = 40
+    K = 16 + 3 * A
+    R = random_streams(seed, n_outlines, K)
+    ncont = randint(R[:, 0], 1, 3)
+    m = randint(R[:, 1], 8, 40)
+    box = uniform(R[:, 2], 8.0, 48.0)
+    px = u01(R[:, 3]) * (np.float32(width) - box)
+    py = u01(R[:, 4]) * (np.float32(height) - box)
+    rgb = [randint(R[:, 5 + i], 0, 255) for i in range(3)]
+    alpha = uniform(R[:, 8], 0.3, 1.0)
+    colors = _color4f_from_rgb_bytes(*rgb, alpha)
+    blur = u01(R[:, 9]) < np.float32(blur_frac)
+    sigma = uniform(R[:, 10], 2.0, 20.0)
+    radius = ((sigma - np.float32(0.5)) / np.float32(0.57735)).astype(np.float32)
+    rj = uniform(R[:, 16:16 + A], 0.75, 1.0)
+    c1 = uniform(R[:, 16 + A:16 + 2 * A], 0.85, 1.15)
+    c2 = uniform(R[:, 16 + 2 * A:16 + 3 * A], 0.85, 1.15)
+    scales = np.array([1.0, 0.55, 0.3], np.float64)
+    b = SceneBuilder(width, height)
+    for i in range(n_outlines):
+        k = int(ncont[i]); per = max(3, int(m[i]) // k)
+        half = float(box[i]) * 0.5
+        cx, cy = float(px[i]) + half, float(py[i]) + half
+        verbs, pts, a0 = [], [], 0
+        for j in range(k):
+            rad = half * scales[j]
+            direction = 1.0 if j == 0 else -1.0
+            ang = direction * 2.0 * np.pi * np.arange(per + 1) / per
+            rr = rj[i, a0:a0 + per].astype(np.float64)
+            rr = np.concatenate([rr, rr[:1]])
+            ax = cx + rad * rr * np.cos(ang); ay = cy + rad * rr * np.sin(ang)
+            verbs.append(MOVE); pts.append((ax[0], ay[0]))
+            for s in range(per):
+                t1 = ang[s] + (ang[s + 1] - ang[s]) / 3.0
+                t2 = ang[s] + 2.0 * (ang[s + 1] - ang[s]) / 3.0
+                k1 = rad * float(c1[i, (a0 + s) % A]) * (rr[s] * 2 + rr[s + 1]) / 3.0
+                k2 = rad * float(c2[i, (a0 + s) % A]) * (rr[s] + 2 * rr[s + 1]) / 3.0
+                verbs.append(CUBIC)
+                pts += [(cx + k1 * np.cos(t1), cy + k1 * np.sin(t1)),
+                        (cx + k2 * np.cos(t2), cy + k2 * np.sin(t2)),
+                        (ax[s + 1], ay[s + 1])]
+            verbs.append(CLOSE)
+            a0 += per
+        p = default_paint()
+        p["fill_type"] = EVEN_ODD
+        p["fill_color"] = colors[i]
+        p["stroke_color"] = colors[i]
+        if blur[i]:
+            p["blur_style"] = BLUR_NORMAL
+            p["blur_radius"] = radius[i]
+        b.draw_path(np.asarray(verbs, np.uint8), np.asarray(pts, np.float32), p)
+    return b.build()
