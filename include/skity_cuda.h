@@ -1,0 +1,192 @@
+/*
+ * skity_cuda.h -- C ABI of the GB300 raster backend for Skity.
+ *
+ * This is the drop-in boundary for the reference's CPU software raster path:
+ *
+ *   Canvas::MakeSoftwareCanvas(Bitmap*)   include/skity/render/canvas.hpp:359,
+ *                                         src/render/sw/sw_canvas.cc:146-156
+ *   Canvas::Clear / DrawPath / Flush      include/skity/render/canvas.hpp:237-279
+ *
+ * It follows the conventions of the reference's C API (module/capi):
+ * opaque handles (module/capi/include/skity_c/skity_base.h:34), result codes
+ * (skity_base.h:48-56, extended here with device errors), extern "C"
+ * entry points that never throw.  Plain pointers and sizes only.
+ *
+ * Pixels are premultiplied RGBA8 rows (Bitmap(w, h, kPremul_AlphaType) with
+ * the default kRGBA colour type, include/skity/graphic/bitmap.hpp:28-30).
+ * Draw semantics are those of SWCanvas: results agree with the reference
+ * software backend (the oracle in oracle/ checks them).  The only observable
+ * difference is timing: the software canvas writes pixels during each draw,
+ * this canvas writes them back to the caller's bitmap at flush.
+ */
+#ifndef SKITY_CUDA_H
+#define SKITY_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define SKITY_CUDA_API __declspec(dllexport)
+#else
+#define SKITY_CUDA_API __attribute__((visibility("default")))
+#endif
+
+/* Result codes: 0 and -1..-5 mean what skity_result means
+ * (module/capi/include/skity_c/skity_base.h:48-56). */
+typedef enum skity_cuda_result {
+  SKITY_CUDA_SUCCESS = 0,
+  SKITY_CUDA_ERROR_INVALID_HANDLE = -1,
+  SKITY_CUDA_ERROR_INVALID_ARGUMENT = -2,
+  SKITY_CUDA_ERROR_INITIALIZATION_FAILED = -3,
+  SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY = -4,
+  SKITY_CUDA_ERROR_NOT_SUPPORTED = -5,
+  SKITY_CUDA_ERROR_DEVICE = -6,                 /* a CUDA call failed */
+  SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY = -7,   /* device budget exceeded */
+  SKITY_CUDA_ERROR_DEVICE_TIMEOUT = -8,         /* a bounded device wait expired */
+} skity_cuda_result;
+
+typedef struct skity_cuda_context_s* skity_cuda_context;
+typedef struct skity_cuda_canvas_s* skity_cuda_canvas;
+typedef struct skity_cuda_batch_s* skity_cuda_batch;
+
+/* Path::Verb (include/skity/graphic/path.hpp:45-60). */
+enum {
+  SKITY_CUDA_VERB_MOVE = 0,
+  SKITY_CUDA_VERB_LINE = 1,
+  SKITY_CUDA_VERB_QUAD = 2,
+  SKITY_CUDA_VERB_CONIC = 3,
+  SKITY_CUDA_VERB_CUBIC = 4,
+  SKITY_CUDA_VERB_CLOSE = 5,
+};
+
+/* A skity::Path as its storage holds it (path.hpp:590-596): verbs, points
+ * (x, y pairs) and conic weights, plus Path::PathFillType (0 kWinding,
+ * 1 kEvenOdd). */
+typedef struct skity_cuda_path {
+  const uint8_t* verbs;
+  uint32_t verb_count;
+  const float* points; /* 2 * point_count floats */
+  uint32_t point_count;
+  const float* conic_weights;
+  uint32_t conic_weight_count;
+  uint32_t fill_type;
+} skity_cuda_path;
+
+/* Shader::MakeLinear / MakeRadial (include/skity/effect/shader.hpp:88-109). */
+typedef struct skity_cuda_gradient {
+  uint32_t type;      /* 1 linear (p0 -> p1), 2 radial (centre p0, radius[0]) */
+  uint32_t tile_mode; /* TileMode: 0 clamp, 1 repeat, 2 mirror, 3 decal */
+  uint32_t stop_count;
+  uint32_t has_offsets; /* 0: stops evenly spaced (pos == nullptr) */
+  float p0[2];
+  float p1[2];
+  float radius[2];
+  const float* colors;  /* 4 * stop_count floats, unpremultiplied RGBA */
+  const float* offsets; /* stop_count floats when has_offsets */
+} skity_cuda_gradient;
+
+/* The skity::Paint state the raster path reads (paint.hpp:46-285).
+ * Colours are Color4f (unpremultiplied RGBA floats). */
+typedef struct skity_cuda_paint {
+  uint32_t style;      /* Paint::Style: fill, stroke, stroke-and-fill, stroke-then-fill */
+  uint32_t cap;        /* Paint::Cap: butt, round, square */
+  uint32_t join;       /* Paint::Join: miter, round, bevel */
+  uint32_t blend_mode; /* BlendMode (kSrcOver = 3) */
+  float fill_color[4];
+  float stroke_color[4];
+  float stroke_width;
+  float miter_limit;
+  const skity_cuda_gradient* shader; /* NULL: solid colour */
+  uint32_t blur_style;  /* 0: no mask filter; BlurStyle (kNormal = 1) */
+  float blur_radius;    /* MaskFilter::MakeBlur radius */
+} skity_cuda_paint;
+
+typedef struct skity_cuda_context_create_info {
+  uint32_t struct_size;       /* sizeof(skity_cuda_context_create_info) */
+  int32_t device;             /* CUDA device ordinal */
+  uint64_t device_memory_budget; /* bytes the context may hold; 0 = 16 GiB */
+} skity_cuda_context_create_info;
+
+/* Timings and work counts of the last flush / batch render. */
+typedef struct skity_cuda_stats {
+  double device_ms;       /* kernel time, CUDA events on the context stream */
+  double total_ms;        /* wall time of the call, uploads and readback included */
+  uint64_t draws;         /* DrawPath calls rendered */
+  uint64_t passes;        /* fill/stroke rasterisation passes */
+  uint64_t edges;         /* fixed-point edges built */
+  uint64_t spans;         /* coverage spans emitted inside the canvases */
+  uint64_t pixels;        /* canvas pixels written back */
+  uint64_t kernel_launches;
+  uint64_t retries;       /* scratch-capacity retries */
+} skity_cuda_stats;
+
+/* ---- context ------------------------------------------------------------ */
+SKITY_CUDA_API int32_t skity_cuda_context_create(
+    const skity_cuda_context_create_info* info, skity_cuda_context* out);
+SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx);
+/* Stats of the context's last flush or batch render. */
+SKITY_CUDA_API int32_t skity_cuda_context_get_stats(skity_cuda_context ctx,
+                                                    skity_cuda_stats* out);
+
+/* ---- canvas (Canvas::MakeSoftwareCanvas counterpart) --------------------
+ * Creates a canvas over a caller-owned premultiplied RGBA8 bitmap.  Like
+ * MakeSoftwareCanvas, a NULL bitmap or a zero width/height yields no canvas
+ * (SKITY_CUDA_ERROR_INVALID_ARGUMENT).  The bitmap must outlive the canvas;
+ * its pixels are read at the first draw after a flush and written at flush. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_create(skity_cuda_context ctx,
+                                                uint32_t width, uint32_t height,
+                                                void* pixels, size_t row_bytes,
+                                                skity_cuda_canvas* out);
+SKITY_CUDA_API void skity_cuda_canvas_destroy(skity_cuda_canvas canvas);
+/* Canvas::Clear(Color4f): DrawColor(color, kSrc) over the whole canvas. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas,
+                                               const float color[4]);
+/* Canvas::DrawPath(path, paint).  Path and paint data are copied; callers may
+ * reuse their buffers after the call. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
+                                                   const skity_cuda_path* path,
+                                                   const skity_cuda_paint* paint);
+/* Canvas::Flush: renders the recorded draws on the GPU and writes the
+ * bitmap's pixels. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas);
+
+/* ---- batched form -----------------------------------------------------------
+ * Many canvases rendered in one pipeline.  Each canvas is a scene stream
+ * (the flat draw-stream layout written by skity_gb300/scene.py: header,
+ * verb/point/weight offsets, verbs, points, weights, 80-byte paint records,
+ * 48-byte gradient records, stop colours and offsets).
+ *
+ * skity_cuda_render_streams: host streams in, host pixels out (each
+ * out_pixels[i] receives width*height*4 bytes).  The whole call -- upload,
+ * render, readback -- is timed in the stats. */
+SKITY_CUDA_API int32_t skity_cuda_render_streams(skity_cuda_context ctx,
+                                                 uint32_t count,
+                                                 const uint8_t* const* streams,
+                                                 const size_t* stream_bytes,
+                                                 uint8_t* const* out_pixels);
+
+/* Device-resident batches: the streams are parsed and uploaded once
+ * (skity_cuda_batch_create); each skity_cuda_batch_render re-renders every
+ * canvas from its clear colour with inputs already in device memory;
+ * skity_cuda_batch_read copies canvas i's pixels to host memory. */
+SKITY_CUDA_API int32_t skity_cuda_batch_create(skity_cuda_context ctx, uint32_t count,
+                                               const uint8_t* const* streams,
+                                               const size_t* stream_bytes,
+                                               skity_cuda_batch* out);
+SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch);
+SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
+                                             uint8_t* out_pixels);
+SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch);
+
+/* Library version string. */
+SKITY_CUDA_API const char* skity_cuda_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKITY_CUDA_H */

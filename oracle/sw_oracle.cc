@@ -1372,8 +1372,9 @@ static inline float RemapFloatTile(float t, int tile) {  // :21-32
   } else if (tile == 1) {
     t = t - std::floor(t);
   } else if (tile == 2) {
+    // float - 2 * std::floor(float * 0.5) - 1 evaluates in double
     float t1 = t - 1;
-    float t2 = t1 - 2 * (float)std::floor(t1 * 0.5) - 1;
+    float t2 = (float)((double)t1 - 2.0 * std::floor((double)t1 * 0.5) - 1.0);
     t = std::fabs(t2);
   }
   return t;

@@ -1,0 +1,115 @@
+"""ctypes binding of the C ABI in include/skity_cuda.h.
+
+The library must be built (skity_gb300.build.build()) and a CUDA device
+present; there is no CPU fallback: loading fails loudly otherwise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+SUCCESS = 0
+ERRORS = {
+    -1: "invalid handle", -2: "invalid argument", -3: "initialization failed",
+    -4: "out of host memory", -5: "not supported", -6: "device error",
+    -7: "out of device memory", -8: "device timeout",
+}
+
+
+class SkityCudaError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {ERRORS.get(code, code)} ({code})")
+        self.code = code
+
+
+class Path_(ctypes.Structure):
+    _fields_ = [("verbs", ctypes.c_void_p), ("verb_count", ctypes.c_uint32),
+                ("points", ctypes.c_void_p), ("point_count", ctypes.c_uint32),
+                ("conic_weights", ctypes.c_void_p), ("conic_weight_count", ctypes.c_uint32),
+                ("fill_type", ctypes.c_uint32)]
+
+
+class Gradient_(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("tile_mode", ctypes.c_uint32),
+                ("stop_count", ctypes.c_uint32), ("has_offsets", ctypes.c_uint32),
+                ("p0", ctypes.c_float * 2), ("p1", ctypes.c_float * 2),
+                ("radius", ctypes.c_float * 2), ("colors", ctypes.c_void_p),
+                ("offsets", ctypes.c_void_p)]
+
+
+class Paint_(ctypes.Structure):
+    _fields_ = [("style", ctypes.c_uint32), ("cap", ctypes.c_uint32), ("join", ctypes.c_uint32),
+                ("blend_mode", ctypes.c_uint32), ("fill_color", ctypes.c_float * 4),
+                ("stroke_color", ctypes.c_float * 4), ("stroke_width", ctypes.c_float),
+                ("miter_limit", ctypes.c_float), ("shader", ctypes.POINTER(Gradient_)),
+                ("blur_style", ctypes.c_uint32), ("blur_radius", ctypes.c_float)]
+
+
+class ContextInfo_(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("device", ctypes.c_int32),
+                ("device_memory_budget", ctypes.c_uint64)]
+
+
+class Stats_(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("draws", ctypes.c_uint64), ("passes", ctypes.c_uint64),
+                ("edges", ctypes.c_uint64), ("spans", ctypes.c_uint64),
+                ("pixels", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("retries", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every entry point declared in include/skity_cuda.h: name -> (restype, argtypes)
+_vp = ctypes.c_void_p
+SIGNATURES = {
+    "skity_cuda_version": (ctypes.c_char_p, []),
+    "skity_cuda_context_create": (ctypes.c_int32, [ctypes.POINTER(ContextInfo_), ctypes.POINTER(_vp)]),
+    "skity_cuda_context_destroy": (None, [_vp]),
+    "skity_cuda_context_get_stats": (ctypes.c_int32, [_vp, ctypes.POINTER(Stats_)]),
+    "skity_cuda_canvas_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                                  ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "skity_cuda_canvas_destroy": (None, [_vp]),
+    "skity_cuda_canvas_clear": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "skity_cuda_canvas_draw_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.POINTER(Paint_)]),
+    "skity_cuda_canvas_flush": (ctypes.c_int32, [_vp]),
+    "skity_cuda_render_streams": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
+                                                   ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
+    "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
+                                                 ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
+    "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
+    "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
+    "skity_cuda_batch_destroy": (None, [_vp]),
+}
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Loads libskity_cuda.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or _build.LIB
+    if not os.path.exists(p):
+        raise RuntimeError(f"skity_gb300 CUDA library not built ({p}); run skity_gb300.build.build()")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def check(code: int, what: str) -> None:
+    if code != SUCCESS:
+        raise SkityCudaError(code, what)

@@ -1,0 +1,327 @@
+"""Python mirror of the skity drawing interface over the C ABI.
+
+Names and argument meanings follow the reference's C++ API
+(include/skity/graphic/path.hpp, paint.hpp, effect/shader.hpp,
+effect/mask_filter.hpp, render/canvas.hpp) so tests read like the
+reference's own: ``Path().MoveTo(..).LineTo(..)``, ``Paint().SetColor(..)``,
+``Canvas.MakeCUDACanvas(bitmap)``, ``canvas.DrawPath(path, paint)``,
+``canvas.Flush()``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from . import scene as S
+
+Style = type("Style", (), {"kFill_Style": 0, "kStroke_Style": 1, "kStrokeAndFill_Style": 2,
+                           "kStrokeThenFill_Style": 3})
+Cap = type("Cap", (), {"kButt_Cap": 0, "kRound_Cap": 1, "kSquare_Cap": 2})
+Join = type("Join", (), {"kMiter_Join": 0, "kRound_Join": 1, "kBevel_Join": 2})
+PathFillType = type("PathFillType", (), {"kWinding": 0, "kEvenOdd": 1})
+BlendMode = type("BlendMode", (), {"kClear": 0, "kSrc": 1, "kDst": 2, "kSrcOver": 3})
+TileMode = type("TileMode", (), {"kClamp": 0, "kRepeat": 1, "kMirror": 2, "kDecal": 3})
+BlurStyle = type("BlurStyle", (), {"kNormal": 1, "kSolid": 2, "kOuter": 3, "kInner": 4})
+
+
+def ColorSetARGB(a, r, g, b) -> int:
+    return ((a & 0xFF) << 24) | ((r & 0xFF) << 16) | ((g & 0xFF) << 8) | (b & 0xFF)
+
+
+def Color4fFromColor(c: int) -> tuple:
+    """src/graphic/color.cc:44-51: each channel / 255.f (float32)."""
+    f = np.float32(255.0)
+    return tuple(float(np.float32(v) / f) for v in
+                 ((c >> 16) & 0xFF, (c >> 8) & 0xFF, c & 0xFF, (c >> 24) & 0xFF))
+
+
+class Path:
+    """skity::Path storage built with the same semantics as path.cc:494-569."""
+
+    def __init__(self):
+        self.verbs: list[int] = []
+        self.points: list[tuple] = []
+        self.weights: list[float] = []
+        self.fill_type = PathFillType.kWinding
+        self._last_move = ~0
+
+    def _inject(self):
+        if self._last_move < 0:
+            p = (0.0, 0.0) if not self.verbs else self.points[~self._last_move]
+            self.MoveTo(*p)
+
+    def MoveTo(self, x, y):
+        if self.verbs and self.verbs[-1] == S.MOVE:
+            self.points[-1] = (x, y)
+        else:
+            self._last_move = len(self.points)
+            self.verbs.append(S.MOVE)
+            self.points.append((x, y))
+        return self
+
+    def LineTo(self, x, y):
+        self._inject()
+        self.verbs.append(S.LINE)
+        self.points.append((x, y))
+        return self
+
+    def QuadTo(self, x1, y1, x2, y2):
+        self._inject()
+        self.verbs.append(S.QUAD)
+        self.points += [(x1, y1), (x2, y2)]
+        return self
+
+    def ConicTo(self, x1, y1, x2, y2, w):
+        if not w > 0:
+            return self.LineTo(x2, y2)
+        if np.isinf(w):
+            return self.LineTo(x1, y1).LineTo(x2, y2)
+        if w == 1.0:
+            return self.QuadTo(x1, y1, x2, y2)
+        self._inject()
+        self.verbs.append(S.CONIC)
+        self.weights.append(w)
+        self.points += [(x1, y1), (x2, y2)]
+        return self
+
+    def CubicTo(self, x1, y1, x2, y2, x3, y3):
+        self._inject()
+        self.verbs.append(S.CUBIC)
+        self.points += [(x1, y1), (x2, y2), (x3, y3)]
+        return self
+
+    def Close(self):
+        if self.verbs and self.verbs[-1] != S.CLOSE:
+            self.verbs.append(S.CLOSE)
+        if self._last_move >= 0:
+            self._last_move = ~self._last_move
+        return self
+
+    def AddRect(self, l, t, r, b):
+        """Path::AddRect(rect) with the default direction (CW, start 0)."""
+        return self.MoveTo(l, t).LineTo(r, t).LineTo(r, b).LineTo(l, b).Close()
+
+    def SetFillType(self, ft):
+        self.fill_type = ft
+        return self
+
+
+class Shader:
+    def __init__(self, kind, p0, p1, radius, colors, pos, tile):
+        self.kind, self.p0, self.p1, self.radius = kind, p0, p1, radius
+        self.colors = np.asarray(colors, np.float32).reshape(-1, 4)
+        self.pos = None if pos is None else np.asarray(pos, np.float32)
+        self.tile = tile
+
+    @staticmethod
+    def MakeLinear(pts, colors, pos, count, tile_mode=TileMode.kClamp):
+        if count < 2:
+            return None
+        return Shader(S.GRAD_LINEAR, pts[0], pts[1], (0.0, 0.0), colors[:count], pos, tile_mode)
+
+    @staticmethod
+    def MakeRadial(center, radius, colors, pos, count, tile_mode=TileMode.kClamp):
+        if count < 2 or radius < 0:
+            return None
+        return Shader(S.GRAD_RADIAL, center, (0.0, 0.0), (radius, 0.0), colors[:count], pos, tile_mode)
+
+
+class MaskFilter:
+    def __init__(self, style, radius):
+        self.style, self.radius = style, radius
+
+    @staticmethod
+    def MakeBlur(style, radius):
+        return None if radius <= 0 else MaskFilter(style, radius)
+
+
+class Paint:
+    def __init__(self):
+        self.rec = S.default_paint()
+        self.shader: Shader | None = None
+        self.mask_filter: MaskFilter | None = None
+
+    def SetStyle(self, s): self.rec["style"] = s; return self
+    def SetStrokeWidth(self, w): self.rec["stroke_width"] = w; return self
+    def SetStrokeMiter(self, m): self.rec["miter"] = m; return self
+    def SetStrokeCap(self, c): self.rec["cap"] = c; return self
+    def SetStrokeJoin(self, j): self.rec["join"] = j; return self
+    def SetBlendMode(self, m): self.rec["blend"] = m; return self
+    def SetShader(self, s): self.shader = s; return self
+    def SetMaskFilter(self, m): self.mask_filter = m; return self
+
+    def SetColor(self, c: int):
+        self.rec["fill_color"] = self.rec["stroke_color"] = Color4fFromColor(c)
+        return self
+
+    def SetFillColor(self, r, g, b, a): self.rec["fill_color"] = (r, g, b, a); return self
+    def SetStrokeColor(self, r, g, b, a): self.rec["stroke_color"] = (r, g, b, a); return self
+
+    def SetAlphaF(self, a):
+        a = float(np.clip(np.float32(a), 0, 1))
+        self.rec["fill_color"][3] = a
+        self.rec["stroke_color"][3] = a
+        return self
+
+
+class Context:
+    """One CUDA device context (skity_cuda_context)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self.lib = _lib.load()
+        info = _lib.ContextInfo_(ctypes.sizeof(_lib.ContextInfo_), device, budget_bytes)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.skity_cuda_context_create(ctypes.byref(info), ctypes.byref(h)),
+                   "skity_cuda_context_create")
+        self.handle = h
+
+    def stats(self) -> dict:
+        st = _lib.Stats_()
+        _lib.check(self.lib.skity_cuda_context_get_stats(self.handle, ctypes.byref(st)), "get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if self.handle:
+            self.lib.skity_cuda_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- batched form over scene streams
+    def render_streams(self, scenes: list) -> list:
+        bufs = [s.to_bytes() for s in scenes]
+        outs = [np.zeros((s.height, s.width, 4), np.uint8) for s in scenes]
+        n = len(bufs)
+        cbufs = [ctypes.create_string_buffer(b, len(b)) for b in bufs]
+        ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(c) for c in cbufs])
+        lens = (ctypes.c_size_t * n)(*[len(b) for b in bufs])
+        optr = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        _lib.check(self.lib.skity_cuda_render_streams(self.handle, n, ptrs, lens, optr),
+                   "skity_cuda_render_streams")
+        return outs
+
+
+class Batch:
+    """Device-resident batch of scene streams (skity_cuda_batch)."""
+
+    def __init__(self, ctx: Context, scenes: list):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.sizes = [(s.height, s.width) for s in scenes]
+        bufs = [s.to_bytes() for s in scenes]
+        n = len(bufs)
+        cbufs = [ctypes.create_string_buffer(b, len(b)) for b in bufs]
+        ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(c) for c in cbufs])
+        lens = (ctypes.c_size_t * n)(*[len(b) for b in bufs])
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.skity_cuda_batch_create(ctx.handle, n, ptrs, lens, ctypes.byref(h)),
+                   "skity_cuda_batch_create")
+        self.handle = h
+
+    def render(self) -> dict:
+        _lib.check(self.lib.skity_cuda_batch_render(self.handle), "skity_cuda_batch_render")
+        return self.ctx.stats()
+
+    def read(self, i: int, out: np.ndarray | None = None) -> np.ndarray:
+        h, w = self.sizes[i]
+        if out is None:
+            out = np.zeros((h, w, 4), np.uint8)
+        _lib.check(self.lib.skity_cuda_batch_read(self.handle, i, out.ctypes.data), "batch_read")
+        return out
+
+    def close(self):
+        if self.handle:
+            self.lib.skity_cuda_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Canvas:
+    """A CUDA canvas over a caller-owned premultiplied RGBA8 bitmap
+    (numpy array of shape (h, w, 4), uint8), created the way
+    Canvas::MakeSoftwareCanvas(Bitmap*) creates the software canvas."""
+
+    def __init__(self, ctx: Context, handle, bitmap: np.ndarray):
+        self.ctx, self.lib, self.handle, self.bitmap = ctx, ctx.lib, handle, bitmap
+
+    @staticmethod
+    def MakeCUDACanvas(ctx: Context, bitmap: np.ndarray | None):
+        """Returns None for a missing or empty bitmap, like MakeSoftwareCanvas."""
+        if bitmap is None or bitmap.size == 0:
+            return None
+        assert bitmap.dtype == np.uint8 and bitmap.ndim == 3 and bitmap.shape[2] == 4
+        assert bitmap.flags["C_CONTIGUOUS"]
+        h = ctypes.c_void_p()
+        rc = ctx.lib.skity_cuda_canvas_create(ctx.handle, bitmap.shape[1], bitmap.shape[0],
+                                              bitmap.ctypes.data, bitmap.strides[0], ctypes.byref(h))
+        if rc == -2:
+            return None
+        _lib.check(rc, "skity_cuda_canvas_create")
+        return Canvas(ctx, h, bitmap)
+
+    def Clear(self, color):
+        c4 = Color4fFromColor(color) if isinstance(color, int) else tuple(color)
+        arr = (ctypes.c_float * 4)(*c4)
+        _lib.check(self.lib.skity_cuda_canvas_clear(self.handle, arr), "skity_cuda_canvas_clear")
+
+    def DrawPath(self, path: Path, paint: Paint):
+        verbs = np.asarray(path.verbs, np.uint8)
+        pts = np.asarray(path.points, np.float32).reshape(-1, 2)
+        wts = np.asarray(path.weights, np.float32)
+        cp = _lib.Path_(verbs.ctypes.data if len(verbs) else None, len(verbs),
+                        pts.ctypes.data if len(pts) else None, len(pts),
+                        wts.ctypes.data if len(wts) else None, len(wts), path.fill_type)
+        r = paint.rec
+        cpaint = _lib.Paint_()
+        cpaint.style, cpaint.cap, cpaint.join, cpaint.blend_mode = (int(r["style"]), int(r["cap"]),
+                                                                    int(r["join"]), int(r["blend"]))
+        cpaint.fill_color[:] = [float(v) for v in r["fill_color"]]
+        cpaint.stroke_color[:] = [float(v) for v in r["stroke_color"]]
+        cpaint.stroke_width = float(r["stroke_width"])
+        cpaint.miter_limit = float(r["miter"])
+        keep = []
+        if paint.shader is not None:
+            s = paint.shader
+            colors = np.ascontiguousarray(s.colors, np.float32)
+            offs = None if s.pos is None else np.ascontiguousarray(s.pos, np.float32)
+            keep += [colors, offs]
+            g = _lib.Gradient_()
+            g.type, g.tile_mode, g.stop_count = s.kind, s.tile, len(colors)
+            g.has_offsets = 0 if offs is None else 1
+            g.p0[:] = list(s.p0)
+            g.p1[:] = list(s.p1)
+            g.radius[:] = list(s.radius)
+            g.colors = colors.ctypes.data
+            g.offsets = None if offs is None else offs.ctypes.data
+            keep.append(g)
+            cpaint.shader = ctypes.pointer(g)
+        if paint.mask_filter is not None:
+            cpaint.blur_style = paint.mask_filter.style
+            cpaint.blur_radius = paint.mask_filter.radius
+        _lib.check(self.lib.skity_cuda_canvas_draw_path(self.handle, ctypes.byref(cp),
+                                                        ctypes.byref(cpaint)),
+                   "skity_cuda_canvas_draw_path")
+
+    def Flush(self):
+        _lib.check(self.lib.skity_cuda_canvas_flush(self.handle), "skity_cuda_canvas_flush")
+
+    def close(self):
+        if self.handle:
+            self.lib.skity_cuda_canvas_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

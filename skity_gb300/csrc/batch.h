@@ -1,0 +1,555 @@
+// Host-side batch building for the raster pipeline (no CUDA runtime calls,
+// so the CPU execution of the pipeline in tests uses it too).
+//
+// A batch is a set of canvases, each with its draws in order.  Every
+// DrawPath becomes one or two rasterisation passes (fill / stroke, in
+// Paint::Style order, src/render/paint_order.hpp:12-31).  A draw with a
+// kNormal blur mask filter becomes a temp canvas holding the draw
+// (SWCanvas::HandleFilter, src/render/sw/sw_canvas.cc:797-826) plus an image
+// pass on the main canvas that samples the blurred temp
+// (ImageFilterBase::BlurBitmapToCanvas, src/effect/image_filter.cc:184-194).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <utility>
+#include <vector>
+
+#include "../../include/skity_cuda.h"
+#include "kernels.cuh"
+#include "stroke.cuh"
+
+namespace skc {
+
+// ---------------------------------------------------------------------------
+// scene stream records (layout of skity_gb300/scene.py)
+// ---------------------------------------------------------------------------
+struct PaintRec {
+  uint32_t style, cap, join, blend, fill_type;
+  int32_t gradient;
+  uint32_t blur_style;
+  float blur_radius;
+  float fill_color[4];
+  float stroke_color[4];
+  float stroke_width, miter;
+  uint32_t reserved[2];
+};
+static_assert(sizeof(PaintRec) == 80, "paint layout");
+struct GradRec {
+  uint32_t type, tile_mode, stop_count, stop_start, has_offsets, reserved;
+  float p0[2], p1[2], radius[2];
+};
+static_assert(sizeof(GradRec) == 48, "gradient layout");
+
+struct StreamView {
+  uint32_t width, height, has_clear;
+  float clear[4];
+  uint32_t nd, nv, np, nw, ng, ns;
+  const uint32_t *vo, *po, *wo;
+  const uint8_t* verbs;
+  const float *pts, *wts;
+  const PaintRec* paints;
+  const GradRec* grads;
+  const float *stop_colors, *stop_offsets;
+};
+
+// A draw the device code can take: the verb sequence of a skity::Path
+// (first verb kMove, a kMove after every kClose -- Path::LineTo/QuadTo/...
+// inject one, path.cc:1327-1339), point and weight counts that match the
+// verbs, finite coordinates inside the range the reference's 16.16 fixed
+// point represents (|v| <= 16384 leaves room for stroke and blur margins),
+// and sane paint parameters.
+constexpr float kMaxCoord = 16384.f;
+inline bool ValidPath(const uint8_t* verbs, uint32_t nv, const float* pts, uint32_t np,
+                      const float* w, uint32_t nw) {
+  uint64_t need_p = 0, need_w = 0;
+  bool need_move = true;
+  for (uint32_t i = 0; i < nv; ++i) {
+    uint8_t v = verbs[i];
+    if (v > kClose) return false;
+    if (v != kMove && v != kClose && need_move) return false;
+    if (v == kClose && need_move && i == 0) return false;
+    switch (v) {
+      case kMove: need_p += 1; need_move = false; break;
+      case kLine: need_p += 1; break;
+      case kQuad: need_p += 2; break;
+      case kConic: need_p += 2; need_w += 1; break;
+      case kCubic: need_p += 3; break;
+      case kClose: need_move = true; break;
+    }
+  }
+  if (need_p != np || need_w != nw) return false;
+  for (uint64_t i = 0; i < 2ull * np; ++i) {
+    float c = pts[i];
+    if (!(c >= -kMaxCoord && c <= kMaxCoord)) return false;
+  }
+  for (uint32_t i = 0; i < nw; ++i) {
+    if (std::isnan(w[i])) return false;
+  }
+  return true;
+}
+inline bool ValidPaint(uint32_t style, uint32_t cap, uint32_t join, float stroke_width, float miter,
+                       float blur_radius) {
+  if (style > 3 || cap > 2 || join > 2) return false;
+  if (!(stroke_width >= 0.f && stroke_width <= 4096.f)) return false;
+  if (!std::isfinite(miter)) return false;
+  if (!(blur_radius <= 1024.f) || std::isnan(blur_radius)) return false;
+  return true;
+}
+
+inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
+  if (!buf || len < 72 || std::memcmp(buf, "SKSC", 4) != 0) return false;
+  uint32_t hdr[7];
+  std::memcpy(hdr, buf + 4, sizeof hdr);
+  if (hdr[0] != 1) return false;
+  s->width = hdr[1];
+  s->height = hdr[2];
+  s->has_clear = hdr[3];
+  size_t o = 32;
+  std::memcpy(s->clear, buf + o, 16);
+  o += 16;
+  uint32_t cnt[6];
+  std::memcpy(cnt, buf + o, sizeof cnt);
+  o += sizeof cnt;
+  s->nd = cnt[0];
+  s->nv = cnt[1];
+  s->np = cnt[2];
+  s->nw = cnt[3];
+  s->ng = cnt[4];
+  s->ns = cnt[5];
+  auto at = [&](size_t bytes) -> const uint8_t* {
+    const uint8_t* p = buf + o;
+    o += bytes;
+    return p;
+  };
+  s->vo = (const uint32_t*)at(4 * (size_t)(s->nd + 1));
+  s->po = (const uint32_t*)at(4 * (size_t)(s->nd + 1));
+  s->wo = (const uint32_t*)at(4 * (size_t)(s->nd + 1));
+  s->verbs = at(s->nv);
+  o += (4 - s->nv % 4) % 4;
+  s->pts = (const float*)at(8 * (size_t)s->np);
+  s->wts = (const float*)at(4 * (size_t)s->nw);
+  s->paints = (const PaintRec*)at(sizeof(PaintRec) * s->nd);
+  s->grads = (const GradRec*)at(sizeof(GradRec) * s->ng);
+  s->stop_colors = (const float*)at(16 * (size_t)s->ns);
+  s->stop_offsets = (const float*)at(4 * (size_t)s->ns);
+  if (o > len) return false;
+  if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
+  for (uint32_t d = 0; d < s->nd; ++d) {
+    if (s->vo[d] > s->vo[d + 1] || s->vo[d + 1] > s->nv) return false;
+    if (s->po[d] > s->po[d + 1] || s->po[d + 1] > s->np) return false;
+    if (s->wo[d] > s->wo[d + 1] || s->wo[d + 1] > s->nw) return false;
+    if (s->paints[d].gradient >= (int32_t)s->ng) return false;
+    const PaintRec& pr = s->paints[d];
+    if (!ValidPaint(pr.style, pr.cap, pr.join, pr.stroke_width, pr.miter, pr.blur_radius))
+      return false;
+    if (!ValidPath(s->verbs + s->vo[d], s->vo[d + 1] - s->vo[d], s->pts + 2 * (size_t)s->po[d],
+                   s->po[d + 1] - s->po[d], s->wts + s->wo[d], s->wo[d + 1] - s->wo[d]))
+      return false;
+  }
+  for (uint32_t g = 0; g < s->ng; ++g) {
+    if ((uint64_t)s->grads[g].stop_start + s->grads[g].stop_count > s->ns) return false;
+    if (s->grads[g].stop_count > 4096 || s->grads[g].tile_mode > 3) return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// host-side brush setup (SWCanvas::GenerateBrush, sw_canvas.cc:727-795)
+// ---------------------------------------------------------------------------
+// PointsToUnit (sw_span_brush.cc:164-200) composed with device_to_local
+inline Mat4 PointsToUnitMat(const GradRec& g) {
+  if (g.type == 1) {
+    float sx = g.p0[0], sy = g.p0[1];
+    float ssx = g.p1[0] - sx, ssy = g.p1[1] - sy;
+    float length = std::sqrt(ssx * ssx + ssy * ssy);
+    float scale = length > 0 ? 1.0f / length : 0;
+    float ux = ssx * scale, uy = ssy * scale;
+    float sine = -uy, cosine = ux;
+    Mat4 rot;
+    rot.identity();
+    rot.e[0][0] = cosine;
+    rot.e[1][0] = -sine;
+    rot.e[0][1] = sine;
+    rot.e[1][1] = cosine;
+    return MatMul(MatMul(rot, MatScale(scale, scale)), MatTranslate(-sx, -sy));
+  }
+  float radius = g.radius[0];
+  float scale = radius > 0 ? 1.0f / radius : 0;
+  return MatMul(MatScale(scale, scale), MatTranslate(-g.p0[0], -g.p0[1]));
+}
+// Matrix::Invert of a translate-only CTM (matrix.cc:134-142, 242-266)
+inline Mat4 InvertTranslate(float tx, float ty) {
+  Mat4 m = MatTranslate(tx, ty);
+  if (m.is_identity()) {
+    m.identity();
+    return m;
+  }
+  Mat4 inv;
+  inv.identity();
+  inv.e[3][0] = -tx;
+  inv.e[3][1] = -ty;
+  return inv;
+}
+inline uint32_t SolidPM(const float c[4]) {
+  return ColorToPMColor(Color4fToColor(c[0], c[1], c[2], c[3]));
+}
+
+struct HostBatch {
+  std::vector<uint8_t> verbs;
+  std::vector<P> pts;
+  std::vector<float> weights;
+  std::vector<DrawDesc> draws;
+  std::vector<PassDesc> passes;
+  std::vector<Brush> brushes;
+  std::vector<CanvasDesc> canvases;
+  std::vector<float4> stop_colors;
+  std::vector<float> stop_offsets;
+  std::vector<uint32_t> main_canvases, temp_canvases;
+  uint64_t pixel_bytes = 0;
+  uint64_t draw_count = 0;
+  uint32_t max_temp_w = 0, max_temp_h = 0;
+
+  uint64_t AllocPixels(uint64_t bytes) {
+    uint64_t o = (pixel_bytes + 255) & ~uint64_t(255);
+    pixel_bytes = o + bytes;
+    return o;
+  }
+  uint32_t AddDraw(const uint8_t* v, uint32_t nv, const float* p, uint32_t np, const float* w,
+                   uint32_t nw) {
+    DrawDesc d;
+    d.v0 = (uint32_t)verbs.size();
+    d.nv = nv;
+    d.p0 = (uint32_t)pts.size();
+    d.np = np;
+    d.w0 = (uint32_t)weights.size();
+    d.nw = nw;
+    verbs.insert(verbs.end(), v, v + nv);
+    for (uint32_t i = 0; i < np; ++i) pts.push_back(mkP(p[2 * i], p[2 * i + 1]));
+    weights.insert(weights.end(), w, w + nw);
+    draws.push_back(d);
+    return (uint32_t)draws.size() - 1;
+  }
+};
+
+// Initial scratch capacities of a pass (counts that later overflow are
+// retried with the exact sizes the geometry kernel reports).
+inline void InitialCaps(const uint8_t* verbs, uint32_t nv, const float* pts, bool stroke,
+                        int32_t cap[13]) {
+  int64_t qv = 2, qp = 2;
+  uint32_t pi = 0;
+  P last = mkP(0, 0);
+  for (uint32_t i = 0; i < nv; ++i) {
+    switch (verbs[i]) {
+      case kMove: qv += 1; qp += 1; last = mkP(pts[2 * pi], pts[2 * pi + 1]); pi += 1; break;
+      case kLine: qv += 1; qp += 1; last = mkP(pts[2 * pi], pts[2 * pi + 1]); pi += 1; break;
+      case kQuad: qv += 1; qp += 2; last = mkP(pts[2 * pi + 2], pts[2 * pi + 3]); pi += 2; break;
+      case kConic: qv += 2; qp += 4; last = mkP(pts[2 * pi + 2], pts[2 * pi + 3]); pi += 2; break;
+      case kCubic: {
+        P c[4] = {last, mkP(pts[2 * pi], pts[2 * pi + 1]), mkP(pts[2 * pi + 2], pts[2 * pi + 3]),
+                  mkP(pts[2 * pi + 4], pts[2 * pi + 5])};
+        double n = CubicQuadCountD(c);
+        int64_t k = (int64_t)n + 1;
+        qv += k;
+        qp += 2 * k;
+        last = c[3];
+        pi += 3;
+      } break;
+      case kClose: qv += 2; qp += 1; break;
+      default: break;
+    }
+  }
+  for (int k = 0; k < 13; ++k) cap[k] = 0;
+  cap[0] = (int32_t)qv;
+  cap[1] = (int32_t)qp;
+  cap[2] = 0;
+  if (stroke) {
+    int64_t ov = 6 * qv + 16, op = 6 * qp + 16 * qv + 32, ow = 4 * qv + 8;
+    cap[3] = (int32_t)ov;
+    cap[4] = (int32_t)op;
+    cap[5] = (int32_t)ow;
+    cap[6] = (int32_t)ov;
+    cap[7] = (int32_t)op;
+    cap[8] = (int32_t)ow;
+  }
+}
+// Bounds that follow exactly from earlier stages' sizes.
+inline void DerivedCaps(int32_t cap[13], bool stroke) {
+  if (stroke) {
+    cap[9] = 2 * cap[3] + 2;
+    cap[10] = 2 * cap[4] + cap[3] + 2;
+    cap[11] = 0;
+    cap[12] = cap[9] + cap[10] + 2;
+  } else {
+    cap[12] = cap[0] + cap[1] + 2;
+  }
+}
+
+// Appends the passes of one DrawPath (fill/stroke in paint order) to `out`.
+inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
+                          uint32_t canvas, float tx, float ty, std::vector<PassDesc>& out) {
+  const PaintRec& pr = s.paints[d];
+  const uint8_t* verbs = s.verbs + s.vo[d];
+  uint32_t nv = s.vo[d + 1] - s.vo[d];
+  const float* pts = s.pts + 2 * (size_t)s.po[d];
+  auto make_brush = [&](bool stroke) {
+    Brush br;
+    std::memset(&br, 0, sizeof br);
+    br.blend = pr.blend;
+    br.global_alpha = 255;
+    const GradRec* g = pr.gradient >= 0 ? &s.grads[pr.gradient] : nullptr;
+    // Shader::MakeLinear / MakeRadial return null for < 2 stops or a
+    // negative radius (src/effect/shader.cc:21-45)
+    if (g && (g->stop_count < 2 || (g->type == 2 && g->radius[0] < 0.f) ||
+              (g->type != 1 && g->type != 2))) {
+      g = nullptr;
+    }
+    if (g) {
+      br.kind = g->type;
+      Mat4 dev_to_local = MatMul(MatTranslate(0, 0), InvertTranslate(tx, ty));
+      Mat4 m = MatMul(PointsToUnitMat(*g), dev_to_local);
+      br.m[0] = m.e[0][0];
+      br.m[1] = m.e[1][0];
+      br.m[2] = m.e[3][0];
+      br.m[3] = m.e[0][1];
+      br.m[4] = m.e[1][1];
+      br.m[5] = m.e[3][1];
+      br.tile = g->tile_mode;
+      br.stop_count = g->stop_count;
+      br.has_offsets = g->has_offsets;
+      br.stop0 = (uint32_t)hb.stop_colors.size();
+      for (uint32_t i = 0; i < g->stop_count; ++i) {
+        const float* c = s.stop_colors + 4 * (size_t)(g->stop_start + i);
+        hb.stop_colors.push_back(make_float4(c[0], c[1], c[2], c[3]));
+        hb.stop_offsets.push_back(g->has_offsets ? s.stop_offsets[g->stop_start + i] : 0.f);
+      }
+      // EnsureColorOffsetsNonDescending (gradient_shader.cc:14-21)
+      if (g->has_offsets) {
+        for (uint32_t i = 0; i + 1 < g->stop_count; ++i) {
+          float& a = hb.stop_offsets[br.stop0 + i];
+          float& b = hb.stop_offsets[br.stop0 + i + 1];
+          if (a > b) b = a;
+        }
+      }
+    } else {
+      br.kind = 0;
+      br.solid = SolidPM(stroke ? pr.stroke_color : pr.fill_color);
+    }
+    hb.brushes.push_back(br);
+    return (uint32_t)hb.brushes.size() - 1;
+  };
+  auto add = [&](bool stroke) {
+    PassDesc pd;
+    std::memset(&pd, 0, sizeof pd);
+    pd.draw = draw_index;
+    pd.canvas = canvas;
+    pd.flags = (stroke ? kPassStroke : 0) | ((!stroke && pr.fill_type == 1) ? kPassEvenOdd : 0) |
+               (pr.blend == 3 ? kPassSrcOver : 0);
+    pd.cap_join = (pr.cap & 0xFF) | ((pr.join & 0xFF) << 8);
+    pd.tx = tx;
+    pd.ty = ty;
+    pd.stroke_width = pr.stroke_width;
+    pd.miter = pr.miter;
+    pd.brush = make_brush(stroke);
+    pd.ga = hb.brushes[pd.brush].global_alpha;
+    InitialCaps(verbs, nv, pts, stroke, pd.cap);
+    DerivedCaps(pd.cap, stroke);
+    out.push_back(pd);
+  };
+  bool need_fill = pr.style != 1, need_stroke = pr.style != 0;
+  if (pr.style == 3) {
+    if (need_stroke) add(true);
+    if (need_fill) add(false);
+  } else {
+    if (need_fill) add(false);
+    if (need_stroke) add(true);
+  }
+}
+
+// One canvas of a stream into the batch; returns false on invalid input.
+inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
+  uint32_t cidx = (uint32_t)hb.canvases.size();
+  CanvasDesc cd;
+  std::memset(&cd, 0, sizeof cd);
+  cd.w = s.width;
+  cd.h = s.height;
+  cd.px_off = hb.AllocPixels((uint64_t)s.width * s.height * 4);
+  cd.has_clear = s.has_clear;
+  cd.clear_pm = s.has_clear ? SolidPM(s.clear) : 0;
+  hb.canvases.push_back(cd);
+  hb.main_canvases.push_back(cidx);
+  std::vector<PassDesc> main_passes;
+  std::vector<std::pair<uint32_t, std::vector<PassDesc>>> temps;
+  for (uint32_t d = 0; d < s.nd; ++d) {
+    const PaintRec& pr = s.paints[d];
+    if (pr.blend != 3 && pr.blend > 2) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    uint32_t draw = hb.AddDraw(s.verbs + s.vo[d], s.vo[d + 1] - s.vo[d], s.pts + 2 * (size_t)s.po[d],
+                               s.po[d + 1] - s.po[d], s.wts + s.wo[d], s.wo[d + 1] - s.wo[d]);
+    hb.draw_count++;
+    bool blur = pr.blur_style != 0 && pr.blur_radius > 0;  // MakeBlur(r <= 0) is null
+    if (!blur) {
+      AddDrawPasses(hb, s, d, draw, cidx, 0.f, 0.f, main_passes);
+      continue;
+    }
+    if (pr.blur_style != 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
+    const float* p = s.pts + 2 * (size_t)s.po[d];
+    uint32_t np = s.po[d + 1] - s.po[d];
+    uint32_t nv = s.vo[d + 1] - s.vo[d];
+    if (nv > 1 && s.verbs[s.vo[d] + nv - 1] == kMove) np--;
+    float l = 0, t = 0, r = 0, b = 0;
+    if (np > 0) {
+      l = r = p[0];
+      t = b = p[1];
+      for (uint32_t i = 1; i < np; ++i) {
+        l = std::min(l, p[2 * i]);
+        r = std::max(r, p[2 * i]);
+        t = std::min(t, p[2 * i + 1]);
+        b = std::max(b, p[2 * i + 1]);
+      }
+    }
+    if (pr.style != 0) {  // ComputeBoundsIfStroke (sw_canvas.cc:135-144)
+      float sw = pr.stroke_width;
+      l = std::floor(l - sw);
+      t = std::floor(t - sw);
+      r = std::floor(r + sw);
+      b = std::floor(b + sw);
+    }
+    float rad = pr.blur_radius;
+    float fl = std::floor(l - rad), ft = std::floor(t - rad);  // image_filter.cc:33-41
+    float fr = std::ceil(r + rad), fb = std::ceil(b + rad);
+    uint32_t fw = (uint32_t)(fr - fl), fh = (uint32_t)(fb - ft);
+    if (fw == 0 || fh == 0 || fw > 65535 || fh > 65535) continue;
+    // temp canvas (zeroed premul bitmap), the draw translated by -(fl, ft)
+    uint32_t tidx = (uint32_t)hb.canvases.size();
+    CanvasDesc tc;
+    std::memset(&tc, 0, sizeof tc);
+    tc.w = fw;
+    tc.h = fh;
+    tc.px_off = hb.AllocPixels((uint64_t)fw * fh * 4);
+    tc.blur_off = hb.AllocPixels((uint64_t)fw * fh * 4);
+    tc.has_clear = 1;
+    tc.clear_pm = 0;
+    tc.blur_radius = (int32_t)std::round(std::max(rad, rad));
+    hb.canvases.push_back(tc);
+    hb.temp_canvases.push_back(tidx);
+    hb.max_temp_w = std::max(hb.max_temp_w, fw);
+    hb.max_temp_h = std::max(hb.max_temp_h, fh);
+    std::vector<PassDesc> tp;
+    AddDrawPasses(hb, s, d, draw, tidx, -fl, -ft, tp);
+    temps.emplace_back(tidx, std::move(tp));
+    // DrawImage(blurred, filter_bounds, &paint) (sw_canvas.cc:641-677):
+    // a rect path with a decal/nearest pixmap brush, alpha = paint alpha
+    const uint8_t rv[5] = {kMove, kLine, kLine, kLine, kClose};
+    const float rp[8] = {fl, ft, fr, ft, fr, fb, fl, fb};
+    uint32_t rect = hb.AddDraw(rv, 5, rp, 4, nullptr, 0);
+    Brush br;
+    std::memset(&br, 0, sizeof br);
+    br.kind = 3;
+    br.blend = pr.blend;
+    br.global_alpha = (uint8_t)(255 * pr.fill_color[3]);
+    Mat4 local = MatMul(MatMul(MatTranslate(fl, ft),
+                               MatScale((fr - fl) / (float)fw, (fb - ft) / (float)fh)),
+                        MatTranslate(-0.f, -0.f));
+    Mat4 inv;
+    inv.identity();
+    if (!local.is_identity()) {
+      inv.e[3][0] = -local.e[3][0];
+      inv.e[3][1] = -local.e[3][1];
+    }
+    Mat4 m = MatMul(MatScale(1.f / fw, 1.f / fh), inv);
+    br.m[0] = m.e[0][0];
+    br.m[1] = m.e[1][0];
+    br.m[2] = m.e[3][0];
+    br.m[3] = m.e[0][1];
+    br.m[4] = m.e[1][1];
+    br.m[5] = m.e[3][1];
+    br.img_w = fw;
+    br.img_h = fh;
+    br.img_off = tc.px_off;
+    hb.brushes.push_back(br);
+    PassDesc pd;
+    std::memset(&pd, 0, sizeof pd);
+    pd.draw = rect;
+    pd.canvas = cidx;
+    pd.flags = pr.blend == 3 ? kPassSrcOver : 0;
+    pd.brush = (uint32_t)hb.brushes.size() - 1;
+    pd.ga = br.global_alpha;
+    pd.stroke_width = 1.f;
+    pd.miter = 4.f;
+    InitialCaps(rv, 5, rp, false, pd.cap);
+    DerivedCaps(pd.cap, false);
+    main_passes.push_back(pd);
+  }
+  hb.canvases[cidx].pass0 = (uint32_t)hb.passes.size();
+  hb.passes.insert(hb.passes.end(), main_passes.begin(), main_passes.end());
+  hb.canvases[cidx].pass1 = (uint32_t)hb.passes.size();
+  for (auto& tpp : temps) {
+    hb.canvases[tpp.first].pass0 = (uint32_t)hb.passes.size();
+    hb.passes.insert(hb.passes.end(), tpp.second.begin(), tpp.second.end());
+    hb.canvases[tpp.first].pass1 = (uint32_t)hb.passes.size();
+  }
+  return SKITY_CUDA_SUCCESS;
+}
+
+inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv, uint32_t chunk,
+                          std::vector<RowTask>& out) {
+  out.clear();
+  for (uint32_t c : canv) {
+    const CanvasDesc& cd = hb.canvases[c];
+    for (uint32_t y = 0; y < cd.h; ++y)
+      for (uint32_t x0 = 0; x0 < cd.w; x0 += chunk)
+        out.push_back(RowTask{c, y, x0, std::min(cd.w, x0 + chunk)});
+  }
+}
+
+
+// Per-pass sweep buffers and row tables from the geometry results.
+struct SweepPlan {
+  uint64_t work_edges = 0, acc_bytes = 0, rows = 0, edges = 0;
+};
+inline SweepPlan PlanSweep(const std::vector<PassGeom>& geom, std::vector<PassSweep>& sw) {
+  SweepPlan pl;
+  sw.assign(geom.size(), PassSweep{});
+  for (size_t p = 0; p < geom.size(); ++p) {
+    const PassGeom& g = geom[p];
+    sw[p].work_off = pl.work_edges;
+    sw[p].acc_off = pl.acc_bytes;
+    sw[p].rbase = (uint32_t)pl.rows;
+    if (g.n_edges > 0) {
+      pl.work_edges += (uint64_t)g.n_edges + 2;
+      pl.acc_bytes += (uint64_t)std::max(g.acc_width, 0);
+      pl.acc_bytes = (pl.acc_bytes + 15) & ~uint64_t(15);
+      pl.edges += (uint64_t)g.n_edges;
+    }
+    int nr = g.row1 - g.row0;
+    if (nr > 0) pl.rows += (uint64_t)nr + 1;
+  }
+  return pl;
+}
+// Compositor inputs from the span counts; returns the total span count.
+inline uint64_t PlanComp(const HostBatch& hb, const std::vector<PassGeom>& geom,
+                         const std::vector<PassSweep>& sw, const std::vector<uint32_t>& pass_spans,
+                         std::vector<PassComp>& comp) {
+  comp.assign(geom.size(), PassComp{});
+  uint64_t spans = 0;
+  for (size_t p = 0; p < geom.size(); ++p) {
+    const PassGeom& g = geom[p];
+    comp[p].row0 = g.row1 > g.row0 ? g.row0 : 0;
+    comp[p].row1 = g.row1 > g.row0 ? g.row1 : 0;
+    comp[p].rbase = sw[p].rbase;
+    comp[p].brush = hb.passes[p].brush;
+    comp[p].span_base = spans;
+    spans += pass_spans[p];
+  }
+  return spans;
+}
+// Grow the capacities of a pass whose geometry overflowed.
+inline void GrowCaps(PassDesc& pd, const PassGeom& g) {
+  bool stroke = (pd.flags & kPassStroke) != 0;
+  for (int k = 0; k < 13; ++k) pd.cap[k] = std::max(pd.cap[k], g.need[k] + 2);
+  DerivedCaps(pd.cap, stroke);
+  for (int k = 9; k < 13; ++k) pd.cap[k] = std::max(pd.cap[k], g.need[k] + 2);
+}
+
+}  // namespace skc

@@ -1,0 +1,168 @@
+// Shading and blending of one fragment: the brushes of
+// src/render/sw/sw_span_brush.cc (solid :140-152, linear/radial gradients
+// :164-383, pixmap nearest :555-579 with src/graphic/bitmap_sampler.cc) and
+// SWRenderTarget::BlendPixel with FastBlend (sw_render_target.cc:12-141),
+// premultiplied ARGB arithmetic of src/graphic/color_priv.hpp:20-72.
+#pragma once
+#include "geom.cuh"
+
+namespace skc {
+
+// Per-pass brush, prepared on the host the way SWCanvas::GenerateBrush
+// (sw_canvas.cc:727-795) prepares the reference's SWSpanBrush.
+struct Brush {
+  uint32_t kind;          // 0 solid, 1 linear, 2 radial, 3 image (blur mask)
+  uint32_t blend;         // BlendMode
+  uint32_t solid;         // premultiplied ARGB (kind 0)
+  uint32_t global_alpha;  // SWSpanBrush::global_alpha_ (255 except image)
+  float m[6];             // sx, kx, tx, ky, sy, ty of the device->unit matrix
+  uint32_t tile, stop_count, has_offsets, stop0;  // gradient stops
+  uint32_t img_w, img_h;  // image brush source
+  uint64_t img_off;       // byte offset of the source pixels (RGBA8 rows)
+};
+
+SKC_HD uint32_t GetA(uint32_t c) { return (c >> 24) & 0xFF; }
+SKC_HD uint32_t ARGB(uint32_t a, uint32_t r, uint32_t g, uint32_t b) {
+  return (a << 24) | (r << 16) | (g << 8) | b;
+}
+// RGBA8 bytes in memory (little-endian u32 R | G<<8 | B<<16 | A<<24) <-> ARGB
+SKC_HD uint32_t RGBAtoARGB(uint32_t m) {
+  return (m & 0xFF00FF00u) | ((m & 0xFFu) << 16) | ((m >> 16) & 0xFFu);
+}
+SKC_HD uint32_t ARGBtoRGBA(uint32_t c) { return RGBAtoARGB(c); }  // same swap
+
+SKC_HD uint8_t ChannelToByte(float v) {  // Color4fToColor (color.cc:53-59)
+  float s = v * 255;
+  s = min_(max_(s, 0.f), 255.f);
+  return (uint8_t)s;
+}
+SKC_HD uint32_t Color4fToColor(float r, float g, float b, float a) {
+  return ARGB(ChannelToByte(a), ChannelToByte(r), ChannelToByte(g), ChannelToByte(b));
+}
+SKC_HD uint32_t MulDiv255Round(uint32_t a, uint32_t b) {  // color_priv.hpp:31-47
+  uint32_t prod = a * b + 128;
+  return (prod + (prod >> 8)) >> 8;
+}
+SKC_HD uint32_t ColorToPMColor(uint32_t c) {  // color_priv.cc:105-108
+  uint32_t a = GetA(c), r = (c >> 16) & 0xFF, g = (c >> 8) & 0xFF, b = c & 0xFF;
+  if (a != 255) {
+    r = MulDiv255Round(r, a);
+    g = MulDiv255Round(g, a);
+    b = MulDiv255Round(b, a);
+  }
+  return (a << 24) | (r << 16) | (g << 8) | b;
+}
+SKC_HD uint32_t AlphaMulQ(uint32_t c, uint32_t scale) {  // color_priv.hpp:62-68
+  const uint32_t mask = 0xFF00FF;
+  uint32_t rb = ((c & mask) * scale) >> 8;
+  uint32_t ag = ((c >> 8) & mask) * scale;
+  return (rb & mask) | (ag & ~mask);
+}
+SKC_HD uint32_t PMSrcOver(uint32_t src, uint32_t dst) {  // color_priv.hpp:70-72
+  return src + AlphaMulQ(dst, 256 - GetA(src));
+}
+
+// BlendPixel (sw_render_target.cc:12-35) for the modes with a FastBlend rule
+// plus src-over; returns the new destination.
+SKC_HD uint32_t BlendPixel(uint32_t dst, uint32_t src, uint32_t mode) {
+  switch (mode) {
+    case 0: return 0;        // kClear
+    case 1: return src;      // kSrc
+    case 2: return dst;      // kDst
+    default: {               // kSrcOver
+      uint32_t a = GetA(src);
+      if (a == 0) return dst;
+      if (a == 255) return src;
+      return PMSrcOver(src, dst);
+    }
+  }
+}
+
+SKC_HD float RemapFloatTile(float t, uint32_t tile) {  // sw_span_brush.cc:21-32
+  if (tile == 0) {
+    t = min_(max_(t, 0.0f), 1.0f);
+  } else if (tile == 1) {
+    t = t - floor_(t);
+  } else if (tile == 2) {
+    // float - 2 * std::floor(float * 0.5) - 1 evaluates in double
+    float t1 = t - 1;
+    float t2 = (float)((double)t1 - 2.0 * floor((double)t1 * 0.5) - 1.0);
+    t = fabs_(t2);
+  }
+  return t;
+}
+
+// GradientColorBrush::LerpColor (sw_span_brush.cc:232-296) -> premul ARGB
+SKC_HD uint32_t GradientColor(const Brush& b, float current, const float4* colors,
+                              const float* offsets) {
+  const float kNZ = 1.0f / (1 << 12);
+  if (fabs_(current) <= kNZ) {
+    current = 0.0f;
+  } else if (fabs_(current - 1.0f) <= kNZ) {
+    current = 1.0f;
+  }
+  if (b.tile == 3 && (current < 0.0f || current >= 1.0f)) return 0;
+  current = RemapFloatTile(current, b.tile);
+  int color_count = (int)b.stop_count;
+  int stop_count = b.has_offsets ? color_count : 0;
+  const float4* c = colors + b.stop0;
+  const float* o = offsets + b.stop0;
+  float4 out;
+  if (stop_count > 0 && current <= o[0]) {
+    out = c[0];
+  } else {
+    float step = 1.f / (color_count - 1);
+    int i = 0, si = 0, ei = 1;
+    float start = 0.f, end = 0.f;
+    for (i = 0; i < color_count - 1; i++) {
+      if (stop_count > 0) {
+        start = o[i];
+        end = o[i + 1];
+      } else {
+        start = step * i;
+        end = step * (i + 1);
+      }
+      if (current >= start && current <= end) {
+        si = i;
+        ei = i + 1;
+        break;
+      }
+    }
+    if (i == color_count - 1 && color_count > 0) {
+      out = c[color_count - 1];
+    } else {
+      float total = end - start;
+      float value = current - start;
+      float mix = 0.5f;
+      if (total > 0) mix = value / total;
+      float om = 1 - mix;
+      out.x = c[si].x * om + c[ei].x * mix;
+      out.y = c[si].y * om + c[ei].y * mix;
+      out.z = c[si].z * om + c[ei].z * mix;
+      out.w = c[si].w * om + c[ei].w * mix;
+    }
+  }
+  return ColorToPMColor(Color4fToColor(out.x, out.y, out.z, out.w));
+}
+
+// CalculateColor of the pass's brush at pixel (x, y), premultiplied ARGB.
+// roundtrip[v] = Color4fToColor(Color4fFromColor(v)) per channel, the
+// PixmapBrush sampler's colour round trip (bitmap_sampler.cc:21-29,93-107).
+SKC_HD uint32_t BrushColor(const Brush& b, int x, int y, const float4* colors, const float* offsets,
+                           const uint8_t* images, const uint8_t* roundtrip) {
+  if (b.kind == 0) return b.solid;
+  float sx = x + 0.5f, sy = y + 0.5f;
+  float mx = sx * b.m[0] + sy * b.m[1] + b.m[2];
+  float my = sx * b.m[3] + sy * b.m[4] + b.m[5];
+  if (b.kind == 1) return GradientColor(b, mx, colors, offsets);
+  if (b.kind == 2) return GradientColor(b, sqrt_(mx * mx + my * my), colors, offsets);
+  // image brush, decal tiling, nearest sampling
+  if (mx < 0.0f || mx >= 1.0f || my < 0.0f || my >= 1.0f) return 0;
+  uint32_t ix = (uint32_t)(mx * (float)b.img_w), iy = (uint32_t)(my * (float)b.img_h);
+  ix = min_(ix, b.img_w - 1);
+  iy = min_(iy, b.img_h - 1);
+  const uint8_t* px = images + b.img_off + ((size_t)iy * b.img_w + ix) * 4;
+  return ARGB(roundtrip[px[3]], roundtrip[px[0]], roundtrip[px[1]], roundtrip[px[2]]);
+}
+
+}  // namespace skc

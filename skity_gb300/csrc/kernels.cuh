@@ -1,0 +1,134 @@
+// Device-side data layout shared by the kernels (kernels.cu) and the host
+// pipeline (pipeline.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "composite.cuh"
+#include "raster.cuh"
+
+namespace skc {
+
+// One rasterisation pass (the fill or the stroke of one DrawPath call),
+// in draw order within its canvas.
+struct PassDesc {
+  uint32_t draw;        // index into DrawDesc
+  uint32_t canvas;      // index into CanvasDesc
+  uint32_t flags;       // kPassStroke | kPassEvenOdd | kPassSrcOver
+  uint32_t cap_join;    // Paint::Cap | Paint::Join << 8
+  float tx, ty;         // translate applied to the path (blur temp canvases)
+  float stroke_width, miter;
+  uint32_t ga;          // brush global alpha (spans with cover & ga == 0 are dropped)
+  uint32_t brush;       // index into Brush
+  uint64_t slice_off;   // byte offset of this pass's geometry scratch
+  int32_t cap[13];      // scratch capacities, see SliceLayout
+  int32_t pad;
+};
+enum : uint32_t { kPassStroke = 1, kPassEvenOdd = 2, kPassSrcOver = 4 };
+
+struct DrawDesc {  // a Path inside the batch's verb/point/weight arrays
+  uint32_t v0, nv, p0, np, w0, nw;
+};
+
+struct CanvasDesc {
+  uint32_t w, h;
+  uint64_t px_off;     // byte offset of RGBA8 rows in the canvas buffer
+  uint64_t blur_off;   // temp canvases: byte offset of the blurred copy
+  uint32_t has_clear;
+  uint32_t clear_pm;   // premultiplied ARGB of the clear colour
+  uint32_t pass0, pass1;
+  int32_t blur_radius; // temp canvases: StackBlur radius (0 = not a temp)
+  uint32_t pad;
+};
+
+// Geometry scratch layout of one pass: capacities in elements.
+//   cap[0..2]  quad path (verbs, points, weights)
+//   cap[3..5]  stroke outline
+//   cap[6..8]  stroker inner path
+//   cap[9..11] quad path of the outline
+//   cap[12]    edges
+struct SliceLayout {
+  uint64_t off[16];
+  uint64_t bytes;
+  SKC_HD static uint64_t al(uint64_t v) { return (v + 15) & ~uint64_t(15); }
+  SKC_HD void compute(const int32_t* cap, uint32_t edge_bytes) {
+    uint64_t o = 0;
+    for (int k = 0; k < 4; ++k) {
+      off[3 * k + 0] = o; o = al(o + (uint64_t)cap[3 * k + 0]);
+      off[3 * k + 1] = o; o = al(o + 8 * (uint64_t)cap[3 * k + 1]);
+      off[3 * k + 2] = o; o = al(o + 4 * (uint64_t)cap[3 * k + 2]);
+    }
+    off[12] = o; o = al(o + (uint64_t)edge_bytes * cap[12]);        // built edges
+    off[13] = o; o = al(o + (uint64_t)edge_bytes * (cap[12] + 2));  // sorted + sentinels
+    off[14] = o; o = al(o + 4 * (uint64_t)cap[12]);                 // sort indices
+    bytes = o;
+  }
+};
+
+struct PassGeom {
+  int32_t status;       // 0 ok, 1 scratch overflow (retry with bigger caps)
+  int32_t n_edges;
+  int32_t start_y, stop_y;
+  int32_t left_bound, right_bound;
+  int32_t acc_left, acc_width;
+  float scan_top;
+  int32_t row0, row1;   // canvas rows that can receive spans
+  int32_t need[13];     // sizes seen (exact up to the failing stage)
+};
+
+struct PassSweep {      // per-pass sweep buffers, set after geometry
+  uint64_t work_off;    // edge working copy (element offset, n_edges + 2)
+  uint64_t acc_off;     // accumulator row (byte offset)
+  uint32_t rbase;       // row table base (rows + 1 entries)
+  uint32_t pad;
+};
+
+struct PassComp {       // per-pass data the compositor reads
+  int32_t row0, row1;
+  uint32_t rbase;
+  uint32_t brush;
+  uint64_t span_base;
+};
+
+struct RowTask {
+  uint32_t canvas, y, x0, x1;
+};
+
+// Batch device pointers handed to every kernel.
+struct DevBatch {
+  const uint8_t* verbs;
+  const P* pts;
+  const float* weights;
+  const DrawDesc* draws;
+  const PassDesc* passes;
+  uint32_t n_passes;
+  const CanvasDesc* canvases;
+  uint8_t* scratch;
+  PassGeom* geom;
+  const PassSweep* sweep;
+  Edge* work;
+  uint8_t* acc;
+  uint32_t* rowtab;
+  uint32_t* pass_spans;
+  const PassComp* comp;
+  uint2* spans;
+  const Brush* brushes;
+  const float4* stop_colors;
+  const float* stop_offsets;
+  uint8_t* pixels;
+  const uint8_t* roundtrip;
+  const uint32_t* pass_list;  // passes to (re)run in the geometry kernel
+  uint32_t n_list;
+};
+
+// kernel launchers (kernels.cu); all launch on `stream` and return the
+// number of launches made
+int LaunchGeometry(const DevBatch& b, cudaStream_t stream);
+int LaunchSweep(const DevBatch& b, bool emit, cudaStream_t stream);
+int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,
+                    cudaStream_t stream);
+int LaunchBlur(const DevBatch& b, const uint32_t* temp_canvases, uint32_t n_temp,
+               uint32_t max_h, uint32_t max_w, cudaStream_t stream);
+int LaunchClearCanvases(const DevBatch& b, const uint32_t* canvases, uint32_t n, cudaStream_t stream);
+
+}  // namespace skc

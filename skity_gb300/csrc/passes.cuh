@@ -1,0 +1,392 @@
+// Per-thread bodies of the raster kernels, host+device so the pipeline can
+// also be executed on the CPU by tests (the GPU runs them through the
+// __global__ wrappers in kernels.cu).
+#pragma once
+#include "kernels.cuh"
+#include "stroke.cuh"
+
+namespace skc {
+
+// ---------------------------------------------------------------------------
+// geometry: Path -> QuadPath (-> stroke -> QuadPath) -> edges -> introsort
+// ---------------------------------------------------------------------------
+SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
+  const PassDesc pd = b.passes[p];
+  const DrawDesc dd = b.draws[pd.draw];
+  PassGeom g;
+  g.status = 0;
+  g.n_edges = 0;
+  g.start_y = g.stop_y = 0;
+  g.left_bound = g.right_bound = 0;
+  g.acc_left = g.acc_width = 0;
+  g.scan_top = 0;
+  g.row0 = g.row1 = 0;
+  for (int k = 0; k < 13; ++k) g.need[k] = 0;
+
+  SliceLayout L;
+  L.compute(pd.cap, sizeof(Edge));
+  uint8_t* base = b.scratch + pd.slice_off;
+  PathView src;
+  src.verbs = b.verbs + dd.v0;
+  src.pts = b.pts + dd.p0;
+  src.w = b.weights + dd.w0;
+  src.nv = (int)dd.nv;
+  src.np = (int)dd.np;
+  src.nw = (int)dd.nw;
+
+  DPath q1;
+  q1.init(base + L.off[0], pd.cap[0], (P*)(base + L.off[1]), pd.cap[1], (float*)(base + L.off[2]),
+          pd.cap[2]);
+  QuadPath(src, &q1);
+  g.need[0] = q1.nv;
+  g.need[1] = q1.np;
+  g.need[2] = q1.nw;
+  if (q1.overflow()) {
+    g.status = 1;
+    b.geom[p] = g;
+    return;
+  }
+  PathView quad = q1.view();
+  DPath q2;
+  if (pd.flags & kPassStroke) {
+    DPath outer, inner;
+    outer.init(base + L.off[3], pd.cap[3], (P*)(base + L.off[4]), pd.cap[4],
+               (float*)(base + L.off[5]), pd.cap[5]);
+    inner.init(base + L.off[6], pd.cap[6], (P*)(base + L.off[7]), pd.cap[7],
+               (float*)(base + L.off[8]), pd.cap[8]);
+    int imax[3];
+    StrokePath(q1.view(), pd.stroke_width, pd.miter, (int)(pd.cap_join & 0xFF),
+               (int)(pd.cap_join >> 8), &outer, &inner, imax);
+    g.need[3] = outer.nv;
+    g.need[4] = outer.np;
+    g.need[5] = outer.nw;
+    g.need[6] = imax[0];
+    g.need[7] = imax[1];
+    g.need[8] = imax[2];
+    if (outer.overflow() || imax[0] > pd.cap[6] || imax[1] > pd.cap[7] || imax[2] > pd.cap[8]) {
+      g.status = 1;
+      b.geom[p] = g;
+      return;
+    }
+    q2.init(base + L.off[9], pd.cap[9], (P*)(base + L.off[10]), pd.cap[10],
+            (float*)(base + L.off[11]), pd.cap[11]);
+    QuadPath(outer.view(), &q2);
+    g.need[9] = q2.nv;
+    g.need[10] = q2.np;
+    g.need[11] = q2.nw;
+    if (q2.overflow()) {
+      g.status = 1;
+      b.geom[p] = g;
+      return;
+    }
+    quad = q2.view();
+  }
+  RasterBounds rb = ComputeBounds(quad, pd.tx, pd.ty);
+  if (rb.empty) {
+    b.geom[p] = g;
+    return;
+  }
+  Edge* edges = (Edge*)(base + L.off[12]);
+  int n = BuildEdges(quad, pd.tx, pd.ty, rb.st, rb.sb, edges, pd.cap[12]);
+  g.need[12] = n;
+  if (n > pd.cap[12]) {
+    g.status = 1;
+    b.geom[p] = g;
+    return;
+  }
+  if (n == 0) {
+    b.geom[p] = g;
+    return;
+  }
+  int32_t* idx = (int32_t*)(base + L.off[14]);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  EdgeLess less;
+  less.e = edges;
+  introsort(idx, n, less);
+  Edge* S = (Edge*)(base + L.off[13]);
+  for (int i = 0; i < n; ++i) {
+    S[i] = edges[idx[i]];
+    S[i].prev = i == 0 ? n : i - 1;
+    S[i].next = i + 1 == n ? n + 1 : i + 1;
+  }
+  // ProcessEdges sentinels (sw_raster.cc:706-729)
+  Edge h;
+  h.prev = -1;
+  h.next = 0;
+  h.upper_y = h.lower_y = kMinS32;
+  h.x = kMinS32;
+  h.dx = 0;
+  h.dy = kMaxS32;
+  h.upper_x = kMinS32;
+  h.y = 0;
+  h.curve_count = 0;
+  h.curve_shift = 0;
+  h.winding = 0;
+  Edge tl = h;
+  tl.prev = n - 1;
+  tl.next = -1;
+  tl.upper_y = tl.lower_y = kMaxS32;
+  tl.x = kMaxS32;
+  tl.upper_x = kMaxS32;
+  S[n] = h;
+  S[n + 1] = tl;
+
+  const CanvasDesc cd = b.canvases[pd.canvas];
+  g.n_edges = n;
+  g.start_y = (int)rb.t;
+  g.stop_y = (int)rb.sb;
+  // static_cast<uint32_t>(float) << 16 with x86-64 conversion semantics
+  g.left_bound = (Fixed)((uint32_t)(int64_t)rb.sl << 16);
+  g.right_bound = (Fixed)((uint32_t)(int64_t)rb.sr << 16);
+  g.acc_left = (int)rb.l;
+  g.acc_width = (int)(rb.r - rb.l);
+  g.scan_top = rb.st;
+  int r0 = max_(g.start_y, 0), r1 = min_(g.stop_y, (int)cd.h);
+  if (r0 < r1) {
+    g.row0 = r0;
+    g.row1 = r1;
+  }
+  b.geom[p] = g;
+}
+
+
+// ---------------------------------------------------------------------------
+// sweep: span sinks and the count / emit passes
+// ---------------------------------------------------------------------------
+// SWSpanBrush::Brush clipping (sw_span_brush.cc:78-99); false = dropped
+SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
+  if (y < 0 || y >= H) return false;
+  if (x >= W || x + len < 0) return false;
+  if (x < 0) {
+    len += x;
+    x = 0;
+  }
+  if (x + len >= W) len = W - x;
+  return len > 0;
+}
+
+struct CountSink {
+  uint32_t* rows;
+  int row0, row1, W, H;
+  uint32_t ga;
+  bool srcover;
+  SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
+    if (y < row0 || y >= row1) return false;
+    if (!ClipSpan(x, y, len, W, H)) return false;
+    return !(srcover && (a & ga) == 0);
+  }
+  SKC_HD void real(int x, int y, int len, uint8_t a) {
+    if (keep(x, y, len, a)) rows[y - row0]++;
+  }
+  SKC_HD void acc_row(int y, const uint8_t* acc, int left, int lo, int hi) {
+    if (y < row0 || y >= row1) return;
+    uint32_t n = 0;
+    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+      int x = left + s, len = w;
+      if (keep(x, y, len, a)) n++;
+    });
+    rows[y - row0] += n;
+  }
+};
+
+struct EmitSink {
+  uint2* spans;           // this pass's span range
+  const uint32_t* rows;   // exclusive offsets per row, rows+1 entries
+  int row0, row1, W, H;
+  uint32_t ga;
+  bool srcover;
+  int cur_row;
+  uint32_t cur;
+  SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
+    if (y < row0 || y >= row1) return false;
+    if (!ClipSpan(x, y, len, W, H)) return false;
+    return !(srcover && (a & ga) == 0);
+  }
+  SKC_HD void real(int x, int y, int len, uint8_t a) {
+    if (!keep(x, y, len, a)) return;
+    if (y != cur_row) {
+      cur_row = y;
+      cur = rows[y - row0];
+    }
+    spans[cur++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+  }
+  // The accumulated spans of a row follow its direct spans (the reference
+  // flushes a row's accumulator only after leaving the row), so they fill
+  // the tail of the row's slot.
+  SKC_HD void acc_row(int y, const uint8_t* acc, int left, int lo, int hi) {
+    if (y < row0 || y >= row1) return;
+    uint32_t n = 0;
+    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+      int x = left + s, len = w;
+      if (keep(x, y, len, a)) n++;
+    });
+    uint32_t o = rows[y - row0 + 1] - n;
+    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+      int x = left + s, len = w;
+      if (keep(x, y, len, a)) spans[o++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+    });
+  }
+};
+
+template <typename Sink>
+SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink) {
+  const PassDesc pd = b.passes[p];
+  const PassSweep sw = b.sweep[p];
+  SliceLayout L;
+  L.compute(pd.cap, sizeof(Edge));
+  const Edge* S = (const Edge*)(b.scratch + pd.slice_off + L.off[13]);
+  Edge* W = b.work + sw.work_off;
+  int n = g.n_edges;
+  for (int i = 0; i < n + 2; ++i) W[i] = S[i];
+  Sweep<Sink> s;
+  s.E = W;
+  s.head = n;
+  s.tail = n + 1;
+  s.sink = sink;
+  s.acc = b.acc + sw.acc_off;
+  s.acc_left = g.acc_left;
+  s.acc_width = g.acc_width;
+  s.acc_y = kNaN32;
+  s.touch_lo = 0x7fffffff;
+  s.touch_hi = -1;
+  s.scan_top = g.scan_top;
+  s.walk((pd.flags & kPassEvenOdd) != 0, g.start_y, g.stop_y, g.left_bound, g.right_bound);
+  s.flush_acc();
+}
+
+SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p) {
+  const PassGeom g = b.geom[p];
+  const PassSweep sw = b.sweep[p];
+  uint32_t* rows = b.rowtab + sw.rbase;
+  int nrows = g.row1 - g.row0;
+  if (g.n_edges > 0 && nrows > 0) {
+    const PassDesc pd = b.passes[p];
+    const CanvasDesc cd = b.canvases[pd.canvas];
+    CountSink sink;
+    sink.rows = rows;
+    sink.row0 = g.row0;
+    sink.row1 = g.row1;
+    sink.W = (int)cd.w;
+    sink.H = (int)cd.h;
+    sink.ga = pd.ga;
+    sink.srcover = (pd.flags & kPassSrcOver) != 0;
+    RunSweep(b, p, g, &sink);
+  }
+  uint32_t run = 0;
+  for (int r = 0; r < nrows; ++r) {
+    uint32_t c = rows[r];
+    rows[r] = run;
+    run += c;
+  }
+  if (nrows > 0) rows[nrows] = run;
+  b.pass_spans[p] = run;
+}
+
+SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p) {
+  const PassGeom g = b.geom[p];
+  int nrows = g.row1 - g.row0;
+  if (g.n_edges == 0 || nrows <= 0) return;
+  const PassDesc pd = b.passes[p];
+  const PassSweep sw = b.sweep[p];
+  const CanvasDesc cd = b.canvases[pd.canvas];
+  EmitSink sink;
+  sink.spans = b.spans + b.comp[p].span_base;
+  sink.rows = b.rowtab + sw.rbase;
+  sink.row0 = g.row0;
+  sink.row1 = g.row1;
+  sink.W = (int)cd.w;
+  sink.H = (int)cd.h;
+  sink.ga = pd.ga;
+  sink.srcover = (pd.flags & kPassSrcOver) != 0;
+  sink.cur_row = -1;
+  sink.cur = 0;
+  RunSweep(b, p, g, &sink);
+}
+
+
+// ---------------------------------------------------------------------------
+// StackBlur lines
+// ---------------------------------------------------------------------------
+SKC_HD int32_t StackBlurShr(int32_t r) {
+  uint32_t d = (uint32_t)(r + 1) * (uint32_t)(r + 1);
+  return (31 - clz_(d)) + 9;
+}
+SKC_HD uint64_t StackBlurMul(int32_t r) {
+  uint64_t d = (uint64_t)(r + 1) * (uint64_t)(r + 1);
+  return ((1ull << StackBlurShr(r)) + d - 1) / d;
+}
+
+// Blur one line of n pixels (stride in pixels) from src into dst. v_bug
+// reproduces the vertical pass's out_sum initialisation (slots 0 and 3 from
+// slot 1, sw_stack_blur.cc:175-179).
+SKC_HDN void BlurLine(const uint8_t* src, uint8_t* dst, int n, size_t stride, int r, bool v_bug) {
+  const int rp1 = r + 1;
+  const int nm1 = n - 1;
+  const uint64_t sum_factor = (uint64_t)(rp1 * (rp1 + 1) / 2);
+  const uint64_t mul = StackBlurMul(r);
+  const int shr = StackBlurShr(r);
+  auto px = [&](int i, int c) -> uint64_t { return src[(size_t)i * stride * 4 + c]; };
+  uint64_t sum[4], in_sum[4], out_sum[4];
+  for (int c = 0; c < 4; ++c) {
+    uint64_t p0 = px(0, c);
+    sum[c] = p0 * sum_factor;
+    out_sum[c] = p0 * rp1;
+    in_sum[c] = 0;
+  }
+  if (v_bug) {
+    out_sum[0] = px(0, 1) * rp1;
+    out_sum[3] = px(0, 1) * rp1;
+  }
+  for (int i = 1; i <= r; ++i) {
+    int k = min_(i, nm1);
+    for (int c = 0; c < 4; ++c) {
+      uint64_t v = px(k, c);
+      sum[c] += v * (uint64_t)(rp1 - i);
+      in_sum[c] += v;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    uint8_t* o = dst + (size_t)i * stride * 4;
+    int kout = max_(i - r, 0), kin = min_(i + rp1, nm1), kmid = min_(i + 1, nm1);
+    for (int c = 0; c < 4; ++c) {
+      o[c] = (uint8_t)((sum[c] * mul) >> shr);
+      sum[c] -= out_sum[c];
+      out_sum[c] -= px(kout, c);
+      in_sum[c] += px(kin, c);
+      sum[c] += in_sum[c];
+      uint64_t vm = px(kmid, c);
+      out_sum[c] += vm;
+      in_sum[c] -= vm;
+    }
+  }
+}
+
+
+// Scalar composite of one row task (CPU execution of the pipeline; the GPU
+// runs the warp-parallel form in kernels.cu with identical per-pixel order).
+SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* row) {
+  const CanvasDesc cd = b.canvases[rt.canvas];
+  const int y = (int)rt.y, x0 = (int)rt.x0, x1 = (int)rt.x1;
+  uint32_t* gpx = (uint32_t*)(b.pixels + cd.px_off) + (size_t)y * cd.w + x0;
+  for (int i = 0; i < x1 - x0; ++i) row[i] = cd.has_clear ? cd.clear_pm : RGBAtoARGB(gpx[i]);
+  for (uint32_t p = cd.pass0; p < cd.pass1; ++p) {
+    const PassComp pc = b.comp[p];
+    if (y < pc.row0 || y >= pc.row1) continue;
+    const uint32_t* rr = b.rowtab + pc.rbase + (y - pc.row0);
+    const Brush br = b.brushes[pc.brush];
+    for (uint32_t s = rr[0]; s < rr[1]; ++s) {
+      uint2 sp = b.spans[pc.span_base + s];
+      int sx = (int)(sp.x & 0xFFFF), slen = (int)(sp.x >> 16);
+      int xs = max_(sx, x0), xe = min_(sx + slen, x1);
+      uint32_t alpha = sp.y & br.global_alpha;
+      for (int x = xs; x < xe; ++x) {
+        uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+        if (alpha != 255) c = AlphaMulQ(c, alpha);
+        row[x - x0] = BlendPixel(row[x - x0], c, br.blend);
+      }
+    }
+  }
+  for (int i = 0; i < x1 - x0; ++i) gpx[i] = ARGBtoRGBA(row[i]);
+}
+
+}  // namespace skc

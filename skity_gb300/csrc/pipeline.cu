@@ -1,0 +1,641 @@
+// Host side of the GB300 raster backend: batch building, the launch
+// pipeline and the C ABI declared in include/skity_cuda.h.
+//
+// A batch is a set of canvases, each with its draws in order.  Every
+// DrawPath becomes one or two rasterisation passes (fill / stroke, in
+// Paint::Style order, src/render/paint_order.hpp:12-31).  A draw with a
+// kNormal blur mask filter becomes a temp canvas holding the draw
+// (SWCanvas::HandleFilter, src/render/sw/sw_canvas.cc:797-826) plus an image
+// pass on the main canvas that samples the blurred temp
+// (ImageFilterBase::BlurBitmapToCanvas, src/effect/image_filter.cc:184-194).
+//
+// Pipeline per render:
+//   geometry (retry passes whose scratch overflowed) -> host sizes rows ->
+//   sweep count -> host sizes spans -> sweep emit -> composite temp canvases
+//   -> StackBlur -> composite main canvases
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/skity_cuda.h"
+#include "batch.h"
+
+namespace skc {
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    release();
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+struct Context;
+
+// A batch resident on the device: inputs uploaded once, re-rendered on
+// demand.
+struct DeviceBatch {
+  Context* ctx = nullptr;
+  HostBatch hb;
+  DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
+  DevBuf scratch, geom, sweep, work, acc, rowtab, pass_spans, comp, spans, pixels;
+  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip;
+  std::vector<RowTask> h_tasks_main, h_tasks_temp;
+  uint32_t chunk = 1024;
+  bool uploaded = false;
+  std::vector<PassGeom> h_geom;
+  skity_cuda_stats stats{};
+};
+
+}  // namespace skc
+
+struct skity_cuda_context_s {
+  int device = 0;
+  uint64_t budget = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  skity_cuda_stats last{};
+  std::mutex mu;
+};
+
+namespace skc {
+
+static int32_t CudaErr(cudaError_t e) {
+  if (e == cudaSuccess) return SKITY_CUDA_SUCCESS;
+  if (e == cudaErrorMemoryAllocation) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+  return SKITY_CUDA_ERROR_DEVICE;
+}
+#define SKC_TRY(expr)                              \
+  do {                                             \
+    cudaError_t _e = (expr);                       \
+    if (_e != cudaSuccess) return CudaErr(_e);     \
+  } while (0)
+
+template <typename T>
+static cudaError_t Upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
+  cudaError_t e = d.ensure(std::max<size_t>(v.size() * sizeof(T), 16));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+static int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
+  cudaStream_t s = ctx->stream;
+  HostBatch& hb = db.hb;
+  if (hb.verbs.empty()) hb.verbs.push_back(0);
+  if (hb.pts.empty()) hb.pts.push_back(mkP(0, 0));
+  if (hb.weights.empty()) hb.weights.push_back(0);
+  if (hb.stop_colors.empty()) {
+    hb.stop_colors.push_back(make_float4(0, 0, 0, 0));
+    hb.stop_offsets.push_back(0);
+  }
+  SKC_TRY(Upload(db.verbs, hb.verbs, s));
+  SKC_TRY(Upload(db.pts, hb.pts, s));
+  SKC_TRY(Upload(db.weights, hb.weights, s));
+  SKC_TRY(Upload(db.draws, hb.draws, s));
+  SKC_TRY(Upload(db.canvases, hb.canvases, s));
+  SKC_TRY(Upload(db.brushes, hb.brushes, s));
+  SKC_TRY(Upload(db.stop_colors, hb.stop_colors, s));
+  SKC_TRY(Upload(db.stop_offsets, hb.stop_offsets, s));
+  SKC_TRY(Upload(db.temps, hb.temp_canvases, s));
+  uint32_t maxw = 1;
+  for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
+  db.chunk = std::min<uint32_t>(maxw, 2048);
+  BuildRowTasks(hb, hb.main_canvases, db.chunk, db.h_tasks_main);
+  BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
+  SKC_TRY(Upload(db.tasks_main, db.h_tasks_main, s));
+  SKC_TRY(Upload(db.tasks_temp, db.h_tasks_temp, s));
+  // PixmapBrush colour round trip per channel value (Color4fFromColor then
+  // Color4fToColor, bitmap_sampler.cc:21-29, color.cc:44-59)
+  std::vector<uint8_t> rtab(256);
+  for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
+  SKC_TRY(Upload(db.roundtrip, rtab, s));
+  SKC_TRY(db.pixels.ensure(std::max<uint64_t>(hb.pixel_bytes, 16)));
+  db.uploaded = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+// Full render of a resident batch; pixels stay on the device.
+static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
+  cudaStream_t s = ctx->stream;
+  HostBatch& hb = db.hb;
+  const uint32_t np = (uint32_t)hb.passes.size();
+  skity_cuda_stats st{};
+  st.draws = hb.draw_count;
+  st.passes = np;
+  if (timed) SKC_TRY(cudaEventRecord(ctx->ev0, s));
+
+  // ---- geometry with scratch-capacity retries
+  std::vector<uint32_t> todo(np);
+  for (uint32_t i = 0; i < np; ++i) todo[i] = i;
+  db.h_geom.assign(np, PassGeom{});
+  SKC_TRY(db.geom.ensure(std::max<size_t>(np, 1) * sizeof(PassGeom)));
+  for (int attempt = 0; attempt < 8 && !todo.empty(); ++attempt) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < np; ++i) {
+      SliceLayout L;
+      L.compute(hb.passes[i].cap, sizeof(Edge));
+      hb.passes[i].slice_off = total;
+      total += L.bytes;
+    }
+    if (ctx->budget && total > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+    SKC_TRY(db.scratch.ensure(std::max<uint64_t>(total, 16)));
+    SKC_TRY(Upload(db.passes, hb.passes, s));
+    SKC_TRY(Upload(db.pass_list, todo, s));
+    DevBatch b{};
+    b.verbs = db.verbs.as<uint8_t>();
+    b.pts = db.pts.as<P>();
+    b.weights = db.weights.as<float>();
+    b.draws = db.draws.as<DrawDesc>();
+    b.passes = db.passes.as<PassDesc>();
+    b.n_passes = np;
+    b.canvases = db.canvases.as<CanvasDesc>();
+    b.scratch = db.scratch.as<uint8_t>();
+    b.geom = db.geom.as<PassGeom>();
+    b.pass_list = db.pass_list.as<uint32_t>();
+    b.n_list = (uint32_t)todo.size();
+    st.kernel_launches += LaunchGeometry(b, s);
+    SKC_TRY(cudaGetLastError());
+    SKC_TRY(cudaMemcpyAsync(db.h_geom.data(), db.geom.p, np * sizeof(PassGeom),
+                            cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaStreamSynchronize(s));
+    // Passes whose scratch overflowed get bigger capacities; since every
+    // slice offset then moves, the whole geometry stage is run again.
+    uint32_t grown = 0;
+    for (uint32_t p : todo) {
+      const PassGeom& g = db.h_geom[p];
+      if (g.status == 0) continue;
+      GrowCaps(hb.passes[p], g);
+      grown++;
+    }
+    st.retries += grown;
+    if (grown == 0) todo.clear();
+  }
+  if (!todo.empty()) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+
+  // ---- per-pass sweep buffers and row tables
+  std::vector<PassSweep> sw;
+  SweepPlan pl = PlanSweep(db.h_geom, sw);
+  uint64_t work = pl.work_edges, acc = pl.acc_bytes, rows = pl.rows;
+  st.edges = pl.edges;
+  if (rows >= 0xFFFFFFFFull) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+  SKC_TRY(Upload(db.sweep, sw, s));
+  SKC_TRY(db.work.ensure(std::max<uint64_t>(work, 1) * sizeof(Edge)));
+  SKC_TRY(db.acc.ensure(std::max<uint64_t>(acc, 16)));
+  SKC_TRY(cudaMemsetAsync(db.acc.p, 0, std::max<uint64_t>(acc, 16), s));
+  SKC_TRY(db.rowtab.ensure(std::max<uint64_t>(rows, 1) * 4));
+  SKC_TRY(cudaMemsetAsync(db.rowtab.p, 0, std::max<uint64_t>(rows, 1) * 4, s));
+  SKC_TRY(db.pass_spans.ensure(std::max<size_t>(np, 1) * 4));
+
+  DevBatch b{};
+  b.verbs = db.verbs.as<uint8_t>();
+  b.pts = db.pts.as<P>();
+  b.weights = db.weights.as<float>();
+  b.draws = db.draws.as<DrawDesc>();
+  b.passes = db.passes.as<PassDesc>();
+  b.n_passes = np;
+  b.canvases = db.canvases.as<CanvasDesc>();
+  b.scratch = db.scratch.as<uint8_t>();
+  b.geom = db.geom.as<PassGeom>();
+  b.sweep = db.sweep.as<PassSweep>();
+  b.work = db.work.as<Edge>();
+  b.acc = db.acc.as<uint8_t>();
+  b.rowtab = db.rowtab.as<uint32_t>();
+  b.pass_spans = db.pass_spans.as<uint32_t>();
+  st.kernel_launches += LaunchSweep(b, false, s);
+  SKC_TRY(cudaGetLastError());
+  std::vector<uint32_t> pspans(np);
+  if (np) {
+    SKC_TRY(cudaMemcpyAsync(pspans.data(), db.pass_spans.p, np * 4, cudaMemcpyDeviceToHost, s));
+  }
+  SKC_TRY(cudaStreamSynchronize(s));
+  std::vector<PassComp> comp;
+  uint64_t spans = PlanComp(hb, db.h_geom, sw, pspans, comp);
+  st.spans = spans;
+  SKC_TRY(Upload(db.comp, comp, s));
+  SKC_TRY(db.spans.ensure(std::max<uint64_t>(spans, 1) * sizeof(uint2)));
+  b.comp = db.comp.as<PassComp>();
+  b.spans = db.spans.as<uint2>();
+  st.kernel_launches += LaunchSweep(b, true, s);
+  SKC_TRY(cudaGetLastError());
+
+  // ---- composite temp canvases, blur, composite main canvases
+  b.brushes = db.brushes.as<Brush>();
+  b.stop_colors = db.stop_colors.as<float4>();
+  b.stop_offsets = db.stop_offsets.as<float>();
+  b.pixels = db.pixels.as<uint8_t>();
+  b.roundtrip = db.roundtrip.as<uint8_t>();
+  if (!db.h_tasks_temp.empty()) {
+    st.kernel_launches += LaunchComposite(b, db.tasks_temp.as<RowTask>(),
+                                          (uint32_t)db.h_tasks_temp.size(), db.chunk, s);
+    st.kernel_launches += LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
+                                     hb.max_temp_h, hb.max_temp_w, s);
+  }
+  st.kernel_launches += LaunchComposite(b, db.tasks_main.as<RowTask>(),
+                                        (uint32_t)db.h_tasks_main.size(), db.chunk, s);
+  SKC_TRY(cudaGetLastError());
+  if (timed) SKC_TRY(cudaEventRecord(ctx->ev1, s));
+  SKC_TRY(cudaStreamSynchronize(s));
+  if (timed) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    st.device_ms = ms;
+  }
+  for (uint32_t c : hb.main_canvases) st.pixels += (uint64_t)hb.canvases[c].w * hb.canvases[c].h;
+  db.stats = st;
+  return SKITY_CUDA_SUCCESS;
+}
+
+static int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* const* streams,
+                                const size_t* bytes) {
+  for (uint32_t i = 0; i < count; ++i) {
+    StreamView sv;
+    if (!ParseStream(streams[i], bytes[i], &sv)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    int32_t rc = AddStreamCanvas(db.hb, sv);
+    if (rc != SKITY_CUDA_SUCCESS) return rc;
+  }
+  return SKITY_CUDA_SUCCESS;
+}
+
+static int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
+                          size_t row_bytes) {
+  if (index >= db.hb.main_canvases.size()) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  const CanvasDesc& cd = db.hb.canvases[db.hb.main_canvases[index]];
+  size_t w4 = (size_t)cd.w * 4;
+  if (row_bytes == 0) row_bytes = w4;
+  SKC_TRY(cudaMemcpy2DAsync(out, row_bytes, db.pixels.as<uint8_t>() + cd.px_off, w4, w4, cd.h,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  SKC_TRY(cudaStreamSynchronize(ctx->stream));
+  return SKITY_CUDA_SUCCESS;
+}
+
+}  // namespace skc
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct skity_cuda_batch_s {
+  skity_cuda_context ctx;
+  skc::DeviceBatch db;
+};
+
+struct skity_cuda_canvas_s {
+  skity_cuda_context ctx;
+  uint32_t width, height;
+  uint8_t* pixels;
+  size_t row_bytes;
+  // recorded scene (same records as the stream layout)
+  bool has_clear = false;
+  float clear[4] = {0, 0, 0, 0};
+  bool dirty = false;   // draws recorded since the last flush
+  std::vector<uint8_t> verbs;
+  std::vector<float> pts, wts;
+  std::vector<uint32_t> vo{0}, po{0}, wo{0};
+  std::vector<skc::PaintRec> paints;
+  std::vector<skc::GradRec> grads;
+  std::vector<float> stop_colors, stop_offsets;
+  skc::DeviceBatch db;
+};
+
+extern "C" {
+
+SKITY_CUDA_API const char* skity_cuda_version(void) { return "skity-gb300 0.1.0 (sm_103a)"; }
+
+SKITY_CUDA_API int32_t skity_cuda_context_create(const skity_cuda_context_create_info* info,
+                                                 skity_cuda_context* out) {
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int device = 0;
+  uint64_t budget = 16ull << 30;
+  if (info) {
+    if (info->struct_size < sizeof(skity_cuda_context_create_info))
+      return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    device = info->device;
+    if (info->device_memory_budget) budget = info->device_memory_budget;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || device < 0 || device >= n)
+    return SKITY_CUDA_ERROR_INITIALIZATION_FAILED;
+  auto* c = new (std::nothrow) skity_cuda_context_s();
+  if (!c) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  c->device = device;
+  c->budget = budget;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return SKITY_CUDA_ERROR_INITIALIZATION_FAILED;
+  }
+  *out = c;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaEventDestroy(ctx->ev0);
+  cudaEventDestroy(ctx->ev1);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_context_get_stats(skity_cuda_context ctx, skity_cuda_stats* out) {
+  if (!ctx) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  *out = ctx->last;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_render_streams(skity_cuda_context ctx, uint32_t count,
+                                                 const uint8_t* const* streams,
+                                                 const size_t* stream_bytes,
+                                                 uint8_t* const* out_pixels) {
+  if (!ctx) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!streams || !stream_bytes || !out_pixels) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  skc::DeviceBatch db;
+  int32_t rc = skc::BuildFromStreams(db, count, streams, stream_bytes);
+  if (rc) return rc;
+  rc = skc::UploadBatch(ctx, db);
+  if (rc) return rc;
+  rc = skc::RenderBatch(ctx, db, true);
+  if (rc) return rc;
+  for (uint32_t i = 0; i < count; ++i) {
+    rc = skc::ReadCanvas(ctx, db, i, out_pixels[i], 0);
+    if (rc) return rc;
+  }
+  db.stats.total_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  ctx->last = db.stats;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_create(skity_cuda_context ctx, uint32_t count,
+                                               const uint8_t* const* streams,
+                                               const size_t* stream_bytes, skity_cuda_batch* out) {
+  if (!ctx) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!streams || !stream_bytes || !out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  auto* b = new (std::nothrow) skity_cuda_batch_s();
+  if (!b) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  b->ctx = ctx;
+  int32_t rc = skc::BuildFromStreams(b->db, count, streams, stream_bytes);
+  if (!rc) rc = skc::UploadBatch(ctx, b->db);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch) {
+  if (!batch) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  std::lock_guard<std::mutex> lock(batch->ctx->mu);
+  cudaSetDevice(batch->ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  int32_t rc = skc::RenderBatch(batch->ctx, batch->db, true);
+  batch->db.stats.total_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  batch->ctx->last = batch->db.stats;
+  return rc;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
+                                             uint8_t* out_pixels) {
+  if (!batch) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!out_pixels) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(batch->ctx->mu);
+  cudaSetDevice(batch->ctx->device);
+  return skc::ReadCanvas(batch->ctx, batch->db, index, out_pixels, 0);
+}
+
+SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch) {
+  if (!batch) return;
+  {
+    std::lock_guard<std::mutex> lock(batch->ctx->mu);
+    cudaSetDevice(batch->ctx->device);
+    cudaStreamSynchronize(batch->ctx->stream);
+  }
+  delete batch;
+}
+
+// ---- canvas ----------------------------------------------------------------
+SKITY_CUDA_API int32_t skity_cuda_canvas_create(skity_cuda_context ctx, uint32_t width,
+                                                uint32_t height, void* pixels, size_t row_bytes,
+                                                skity_cuda_canvas* out) {
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!ctx) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  // MakeSoftwareCanvas: null bitmap or zero size -> no canvas
+  if (!pixels || width == 0 || height == 0) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (width > 65535 || height > 65535) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (row_bytes == 0) row_bytes = (size_t)width * 4;
+  if (row_bytes < (size_t)width * 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  auto* c = new (std::nothrow) skity_cuda_canvas_s();
+  if (!c) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  c->ctx = ctx;
+  c->width = width;
+  c->height = height;
+  c->pixels = (uint8_t*)pixels;
+  c->row_bytes = row_bytes;
+  *out = c;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API void skity_cuda_canvas_destroy(skity_cuda_canvas canvas) { delete canvas; }
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const float color[4]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!color) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  // a kSrc fill of the whole canvas overwrites everything drawn before
+  canvas->has_clear = true;
+  std::memcpy(canvas->clear, color, 16);
+  canvas->verbs.clear();
+  canvas->pts.clear();
+  canvas->wts.clear();
+  canvas->vo.assign(1, 0);
+  canvas->po.assign(1, 0);
+  canvas->wo.assign(1, 0);
+  canvas->paints.clear();
+  canvas->grads.clear();
+  canvas->stop_colors.clear();
+  canvas->stop_offsets.clear();
+  canvas->dirty = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
+                                                   const skity_cuda_path* path,
+                                                   const skity_cuda_paint* paint) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!path || !paint) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if ((path->verb_count && !path->verbs) || (path->point_count && !path->points) ||
+      (path->conic_weight_count && !path->conic_weights))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  // verb/point/weight counts must agree (Path storage invariant)
+  uint64_t need_p = 0, need_w = 0;
+  for (uint32_t i = 0; i < path->verb_count; ++i) {
+    switch (path->verbs[i]) {
+      case SKITY_CUDA_VERB_MOVE: case SKITY_CUDA_VERB_LINE: need_p += 1; break;
+      case SKITY_CUDA_VERB_QUAD: need_p += 2; break;
+      case SKITY_CUDA_VERB_CONIC: need_p += 2; need_w += 1; break;
+      case SKITY_CUDA_VERB_CUBIC: need_p += 3; break;
+      case SKITY_CUDA_VERB_CLOSE: break;
+      default: return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    }
+  }
+  if (need_p != path->point_count || need_w != path->conic_weight_count)
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (paint->blend_mode > 3) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (paint->blur_style > 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (!skc::ValidPaint(paint->style, paint->cap, paint->join, paint->stroke_width,
+                       paint->miter_limit, paint->blur_style ? paint->blur_radius : 0.f))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (!skc::ValidPath(path->verbs, path->verb_count, path->points, path->point_count,
+                      path->conic_weights, path->conic_weight_count))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (paint->shader && (paint->shader->stop_count > 4096 || paint->shader->tile_mode > 3))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  skc::PaintRec pr;
+  std::memset(&pr, 0, sizeof pr);
+  pr.style = paint->style;
+  pr.cap = paint->cap;
+  pr.join = paint->join;
+  pr.blend = paint->blend_mode;
+  pr.fill_type = path->fill_type ? 1 : 0;
+  pr.gradient = -1;
+  pr.blur_style = paint->blur_style;
+  pr.blur_radius = paint->blur_radius;
+  std::memcpy(pr.fill_color, paint->fill_color, 16);
+  std::memcpy(pr.stroke_color, paint->stroke_color, 16);
+  pr.stroke_width = paint->stroke_width;
+  pr.miter = paint->miter_limit;
+  if (paint->shader) {
+    const skity_cuda_gradient* g = paint->shader;
+    if (!g->colors || (g->has_offsets && !g->offsets)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    skc::GradRec gr;
+    std::memset(&gr, 0, sizeof gr);
+    gr.type = g->type;
+    gr.tile_mode = g->tile_mode;
+    gr.stop_count = g->stop_count;
+    gr.stop_start = (uint32_t)canvas->stop_offsets.size();
+    gr.has_offsets = g->has_offsets;
+    std::memcpy(gr.p0, g->p0, 8);
+    std::memcpy(gr.p1, g->p1, 8);
+    std::memcpy(gr.radius, g->radius, 8);
+    for (uint32_t i = 0; i < g->stop_count; ++i) {
+      canvas->stop_colors.insert(canvas->stop_colors.end(), g->colors + 4 * i, g->colors + 4 * i + 4);
+      canvas->stop_offsets.push_back(g->has_offsets ? g->offsets[i] : 0.f);
+    }
+    pr.gradient = (int32_t)canvas->grads.size();
+    canvas->grads.push_back(gr);
+  }
+  canvas->verbs.insert(canvas->verbs.end(), path->verbs, path->verbs + path->verb_count);
+  canvas->pts.insert(canvas->pts.end(), path->points, path->points + 2 * (size_t)path->point_count);
+  canvas->wts.insert(canvas->wts.end(), path->conic_weights,
+                     path->conic_weights + path->conic_weight_count);
+  canvas->vo.push_back((uint32_t)canvas->verbs.size());
+  canvas->po.push_back((uint32_t)(canvas->pts.size() / 2));
+  canvas->wo.push_back((uint32_t)canvas->wts.size());
+  canvas->paints.push_back(pr);
+  canvas->dirty = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!canvas->dirty) return SKITY_CUDA_SUCCESS;  // OnFlush with nothing recorded
+  skity_cuda_context ctx = canvas->ctx;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  // the recorded draws as one stream view
+  skc::StreamView sv;
+  std::memset(&sv, 0, sizeof sv);
+  sv.width = canvas->width;
+  sv.height = canvas->height;
+  sv.has_clear = canvas->has_clear ? 1 : 0;
+  std::memcpy(sv.clear, canvas->clear, 16);
+  sv.nd = (uint32_t)canvas->paints.size();
+  sv.vo = canvas->vo.data();
+  sv.po = canvas->po.data();
+  sv.wo = canvas->wo.data();
+  sv.verbs = canvas->verbs.data();
+  sv.pts = canvas->pts.data();
+  sv.wts = canvas->wts.data();
+  sv.paints = canvas->paints.data();
+  sv.grads = canvas->grads.data();
+  sv.stop_colors = canvas->stop_colors.data();
+  sv.stop_offsets = canvas->stop_offsets.data();
+  skc::DeviceBatch& db = canvas->db;
+  db.hb = skc::HostBatch();
+  int32_t rc = skc::AddStreamCanvas(db.hb, sv);
+  if (rc) return rc;
+  rc = skc::UploadBatch(ctx, db);
+  if (rc) return rc;
+  const skc::CanvasDesc& cd = db.hb.canvases[db.hb.main_canvases[0]];
+  if (!canvas->has_clear) {
+    // draws blend over the bitmap's current pixels
+    cudaError_t e = cudaMemcpy2DAsync(db.pixels.as<uint8_t>() + cd.px_off, (size_t)cd.w * 4,
+                                      canvas->pixels, canvas->row_bytes, (size_t)cd.w * 4, cd.h,
+                                      cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return skc::CudaErr(e);
+  }
+  rc = skc::RenderBatch(ctx, db, true);
+  if (rc) return rc;
+  rc = skc::ReadCanvas(ctx, db, 0, canvas->pixels, canvas->row_bytes);
+  if (rc) return rc;
+  db.stats.total_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  ctx->last = db.stats;
+  // the bitmap now holds the result; later draws blend over it
+  canvas->has_clear = false;
+  canvas->verbs.clear();
+  canvas->pts.clear();
+  canvas->wts.clear();
+  canvas->vo.assign(1, 0);
+  canvas->po.assign(1, 0);
+  canvas->wo.assign(1, 0);
+  canvas->paints.clear();
+  canvas->grads.clear();
+  canvas->stop_colors.clear();
+  canvas->stop_offsets.clear();
+  canvas->dirty = false;
+  return SKITY_CUDA_SUCCESS;
+}
+
+}  // extern "C"

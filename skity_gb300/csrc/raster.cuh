@@ -1,0 +1,984 @@
+// Fixed-point edges, the edge sort and the analytic-AA scanline sweep for
+// one draw on one GPU thread.  Restates src/render/sw/sw_edge.{hpp,cc} and
+// src/render/sw/sw_raster.cc of the reference; spans go to a sink instead of
+// a std::vector.
+#pragma once
+#include "geom.cuh"
+
+namespace skc {
+
+// SWEdge / SWQuadEdge (sw_edge.hpp:18-81), list links as indices
+struct Edge {
+  int32_t prev, next;
+  Fixed x, y, dx, dy, upper_x, upper_y, lower_y;
+  int8_t curve_count;
+  uint8_t curve_shift;
+  int8_t winding;
+  uint8_t pad;
+  Fixed qx, qy, qdx, qdy, qddx, qddy, q_first_y, q_last_x, q_last_y;
+  Fixed snapped_x, snapped_y;
+};
+
+SKC_HD Fixed SnapY(Fixed y) {  // sw_edge.hpp:36-41
+  return (Fixed)((((uint32_t)y + (uint32_t)(kFixed1 >> (kAccuracy + 1))) >> (16 - kAccuracy))
+                 << (16 - kAccuracy));
+}
+SKC_HD void GoYShift(Edge* e, Fixed dst_y, int y_shift) {  // :55-58
+  e->y = dst_y;
+  e->x = wadd(e->x, e->dx >> y_shift);
+}
+SKC_HD void GoY(Edge* e, Fixed dst_y) {  // :43-51
+  if (dst_y == wadd(e->y, kFixed1)) {
+    e->x = wadd(e->x, e->dx);
+    e->y = dst_y;
+  } else if (e->y != dst_y) {
+    e->x = wadd(e->upper_x, FixedMul(e->dx, wsub(e->y, e->upper_y)));
+    e->y = dst_y;
+  }
+}
+SKC_HD bool UpdateLine(Edge* e, Fixed x0, Fixed y0, Fixed x1, Fixed y1, Fixed slope) {  // sw_edge.cc:45-70
+  if (y0 > y1) {
+    swap_(x0, x1);
+    swap_(y0, y1);
+    e->winding = (int8_t)-e->winding;
+  }
+  FDot6 x0x1 = FixedToFDot6(wsub(x1, x0));
+  FDot6 y0y1 = FixedToFDot6(wsub(y1, y0));
+  if (y0y1 == 0) return false;
+  e->x = x0;
+  e->y = y0;
+  e->dx = slope;
+  e->dy = (x0x1 == 0 || slope == 0) ? kMaxS32 : iabs_(FixedDiv(y0y1, x0x1));
+  e->upper_x = x0;
+  e->upper_y = y0;
+  e->lower_y = y1;
+  return true;
+}
+SKC_HD bool SetLine(Edge* e, P p0, P p1) {  // sw_edge.cc:18-43
+  const int mul = 1 << kAccuracy;
+  Fixed x0 = FDot6ToFixed(ScalarToFDot6(p0.x * mul)) >> kAccuracy;
+  Fixed y0 = SnapY(FDot6ToFixed(ScalarToFDot6(p0.y * mul)) >> kAccuracy);
+  Fixed x1 = FDot6ToFixed(ScalarToFDot6(p1.x * mul)) >> kAccuracy;
+  Fixed y1 = SnapY(FDot6ToFixed(ScalarToFDot6(p1.y * mul)) >> kAccuracy);
+  e->winding = 1;
+  FDot6 y0y1 = FixedToFDot6(wsub(y1, y0));
+  if (y0y1 == 0) return false;
+  FDot6 x0x1 = FixedToFDot6(wsub(x1, x0));
+  Fixed slope = FixedDiv(x0x1, y0y1);
+  e->curve_count = 0;
+  e->curve_shift = 0;
+  return UpdateLine(e, x0, y0, x1, y1, slope);
+}
+SKC_HD bool CanBeIgnored(float top, float bottom, Fixed y0, Fixed y1) {  // :72-88
+  const int mul = 1 << kAccuracy;
+  Fixed start_y = SnapY(FDot6ToFixed(ScalarToFDot6(top * mul)) >> kAccuracy);
+  Fixed stop_y = SnapY(FDot6ToFixed(ScalarToFDot6(bottom * mul)) >> kAccuracy);
+  return y0 >= stop_y || y1 <= start_y;
+}
+SKC_HD int diff_to_shift(FDot6 dx, FDot6 dy, int shiftAA) {  // :97-119
+  dx = iabs_(dx);
+  dy = iabs_(dy);
+  FDot6 dist = max_(dx, dy) + (min_(dx, dy) >> 1);
+  dist = (dist + (1 << (2 + shiftAA))) >> (3 + shiftAA);
+  return (32 - clz_((uint32_t)dist)) >> 1;
+}
+SKC_HD bool UpdateQuad(Edge* e) {  // sw_edge.cc:233-292
+  int success = 0;
+  int count = e->curve_count;
+  Fixed oldx = e->qx, oldy = e->qy;
+  Fixed dx = e->qdx, dy = e->qdy;
+  Fixed newx = 0, newy = 0, nsx = 0, nsy = 0;
+  int shift = e->curve_shift;
+  do {
+    Fixed slope;
+    if (--count > 0) {
+      newx = wadd(oldx, dx >> shift);
+      newy = wadd(oldy, dy >> shift);
+      if (iabs_(dy >> shift) >= kFixed1 * 2) {
+        FDot6 diffY = FixedToFDot6(wsub(newy, e->snapped_y));
+        slope = diffY ? FixedDiv(FixedToFDot6(wsub(newx, e->snapped_x)), diffY) : kMaxS32;
+        nsy = min_<Fixed>(e->q_last_y, FixedRoundToFixed(newy));
+        nsx = wsub(newx, FixedMul(slope, wsub(newy, nsy)));
+      } else {
+        nsy = min_<Fixed>(e->q_last_y, SnapY(newy));
+        nsx = newx;
+        FDot6 diffY = FixedToFDot6(wsub(nsy, e->snapped_y));
+        slope = diffY ? FixedDiv(FixedToFDot6(wsub(newx, e->snapped_x)), diffY) : kMaxS32;
+      }
+      dx = wadd(dx, e->qddx);
+      dy = wadd(dy, e->qddy);
+    } else {
+      newx = e->q_last_x;
+      newy = e->q_last_y;
+      nsy = newy;
+      nsx = newx;
+      FDot6 diffY = wsub(newy, e->snapped_y) >> 10;
+      slope = diffY ? FixedDiv(wsub(newx, e->snapped_x) >> 10, diffY) : kMaxS32;
+    }
+    if (slope < kMaxS32) success = UpdateLine(e, e->snapped_x, e->snapped_y, nsx, nsy, slope);
+    oldx = newx;
+    oldy = newy;
+  } while (count > 0 && !success);
+  e->qx = newx;
+  e->qy = newy;
+  e->qdx = dx;
+  e->qdy = dy;
+  e->snapped_x = nsx;
+  e->snapped_y = nsy;
+  e->curve_count = (int8_t)count;
+  return success;
+}
+SKC_HD bool SetQuad(Edge* e, const P pts[3]) {  // sw_edge.cc:121-231
+  float scale = (float)(1 << (kAccuracy + 6));
+  FDot6 x0 = (int)(pts[0].x * scale), y0 = (int)(pts[0].y * scale);
+  FDot6 x1 = (int)(pts[1].x * scale), y1 = (int)(pts[1].y * scale);
+  FDot6 x2 = (int)(pts[2].x * scale), y2 = (int)(pts[2].y * scale);
+  int w = 1;
+  if (y0 > y2) {
+    swap_(x0, x2);
+    swap_(y0, y2);
+    w = -1;
+  }
+  if (FDot6Round(y0) == FDot6Round(y2)) return false;
+  FDot6 dx = (LShift(x1, 1) - x0 - x2) >> 2;
+  FDot6 dy = (LShift(y1, 1) - y0 - y2) >> 2;
+  int shift = diff_to_shift(dx, dy, kAccuracy);
+  if (shift == 0) {
+    shift = 1;
+  } else if (shift > 6) {
+    shift = 6;
+  }
+  e->winding = (int8_t)w;
+  e->curve_count = (int8_t)(1 << shift);
+  e->curve_shift = (uint8_t)(shift - 1);
+  Fixed A = FDot6ToFixedDiv2(x0 - x1 - x1 + x2);
+  Fixed B = FDot6ToFixed(x1 - x0);
+  e->qx = FDot6ToFixed(x0);
+  e->qdx = B + (A >> shift);
+  e->qddx = A >> (shift - 1);
+  A = FDot6ToFixedDiv2(y0 - y1 - y1 + y2);
+  B = FDot6ToFixed(y1 - y0);
+  e->qy = FDot6ToFixed(y0);
+  e->qdy = B + (A >> shift);
+  e->qddy = A >> (shift - 1);
+  e->q_last_x = FDot6ToFixed(x2);
+  e->q_last_y = FDot6ToFixed(y2);
+  e->qx >>= kAccuracy;
+  e->qy >>= kAccuracy;
+  e->qdx >>= kAccuracy;
+  e->qdy >>= kAccuracy;
+  e->qddx >>= kAccuracy;
+  e->qddy >>= kAccuracy;
+  e->q_last_x >>= kAccuracy;
+  e->q_last_y >>= kAccuracy;
+  e->qy = SnapY(e->qy);
+  e->q_last_y = SnapY(e->q_last_y);
+  e->q_first_y = e->qy;
+  e->snapped_x = e->qx;
+  e->snapped_y = e->qy;
+  UpdateQuad(e);
+  return true;
+}
+
+// ChopQuadAtYExtrema (src/geometry/geometry.cc:311-349)
+SKC_HD int ChopQuadAtYExtrema(const P src[3], P dst[5]) {
+  float a = src[0].y, b = src[1].y, c = src[2].y;
+  float ab = a - b, bc = b - c;
+  if (ab < 0) bc = -bc;
+  if (ab == 0 || bc < 0) {
+    float t;
+    if (valid_unit_divide(a - b, a - b - b + c, &t)) {
+      P p01 = mkP(src[0].x + (src[1].x - src[0].x) * t, src[0].y + (src[1].y - src[0].y) * t);
+      P p12 = mkP(src[1].x + (src[2].x - src[1].x) * t, src[1].y + (src[2].y - src[1].y) * t);
+      dst[0] = src[0];
+      dst[1] = p01;
+      dst[2] = mkP(p01.x + (p12.x - p01.x) * t, p01.y + (p12.y - p01.y) * t);
+      dst[3] = p12;
+      dst[4] = src[2];
+      dst[1].y = dst[3].y = dst[2].y;
+      return 1;
+    }
+    b = fabs_(a - b) < fabs_(b - c) ? a : c;
+  }
+  dst[0] = src[0];
+  dst[1] = src[1];
+  dst[2] = src[2];
+  dst[1].y = b;
+  return 0;
+}
+
+// Pixel-space bounds of a (translated) quad path and the scan bounds
+// derived from them (sw_raster.cc:731-754, path.cc:1341-1360).
+struct RasterBounds {
+  bool empty;
+  float l, t, r, b;      // floor/ceil of the path bounds (bounds_)
+  float sl, st, sr, sb;  // scan bounds
+};
+SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty) {
+  RasterBounds rb;
+  rb.empty = true;
+  rb.l = rb.t = rb.r = rb.b = rb.sl = rb.st = rb.sr = rb.sb = 0;
+  int n = q.np;
+  if (q.nv > 1 && q.verbs[q.nv - 1] == kMove) n--;
+  if (n <= 0) return rb;
+  float l = q.pts[0].x + tx, t = q.pts[0].y + ty, r = l, b = t;
+  for (int i = 1; i < n; ++i) {
+    float x = q.pts[i].x + tx, y = q.pts[i].y + ty;
+    l = min_(l, x);
+    r = max_(r, x);
+    t = min_(t, y);
+    b = max_(b, y);
+  }
+  rb.l = floor_(l);
+  rb.t = floor_(t);
+  rb.r = ceil_(r);
+  rb.b = ceil_(b);
+  float sl = max_(l, -1e9f), sr = min_(r, 1e9f), st = max_(t, -1e9f), sb = min_(b, 1e9f);
+  if (!(sl < sr && st < sb)) return rb;
+  sl = floor_(sl);
+  st = floor_(st);
+  sr = ceil_(sr);
+  sb = ceil_(sb);
+  if (!(sl < sr && st < sb)) return rb;
+  rb.empty = false;
+  rb.sl = sl;
+  rb.st = st;
+  rb.sr = sr;
+  rb.sb = sb;
+  return rb;
+}
+
+// SWEdgeBuilder::BuildEdges over PathEdgeIter (sw_edge.cc:299-336,
+// src/graphic/path_priv.hpp:75-170).  Points are translated by (tx, ty)
+// first: Path::CopyWithMatrix(Translate) computes (1*x + 0*y) + (0*0 + tx*1),
+// which is x + tx exactly.  Returns the number of edges (may exceed cap:
+// only cap are stored).
+SKC_HDN int BuildEdges(const PathView& q, float tx, float ty, float top, float bottom,
+                       Edge* out, int cap) {
+  int n = 0;
+  int vi = 0, pi = 0, move_to = 0;
+  bool needs_close = false;
+  auto T = [&](int i) { return mkP(q.pts[i].x + tx, q.pts[i].y + ty); };
+  auto add_line = [&](P a, P b) {
+    Edge e;
+    if (SetLine(&e, a, b) && !CanBeIgnored(top, bottom, e.upper_y, e.lower_y)) {
+      if (n < cap) out[n] = e;
+      n++;
+    }
+  };
+  auto add_quad = [&](const P* qq) {
+    Edge e;
+    if (SetQuad(&e, qq) && !CanBeIgnored(top, bottom, e.q_first_y, e.q_last_y)) {
+      if (n < cap) out[n] = e;
+      n++;
+    }
+  };
+  for (;;) {
+    if (vi == q.nv) {
+      if (needs_close) add_line(T(pi - 1), T(move_to));
+      return n;
+    }
+    uint8_t v = q.verbs[vi++];
+    if (v == kMove) {
+      if (needs_close) {
+        add_line(T(pi - 1), T(move_to));
+        needs_close = false;
+      }
+      move_to = pi++;
+    } else if (v == kClose) {
+      if (needs_close) {
+        add_line(T(pi - 1), T(move_to));
+        needs_close = false;
+      }
+    } else {
+      int k = (v + 2) / 2;
+      needs_close = true;
+      pi += k;
+      int s = pi - (k + 1);
+      if (v == kLine) {
+        add_line(T(s), T(s + 1));
+      } else if (v == kQuad) {
+        P seg[3] = {T(s), T(s + 1), T(s + 2)};
+        P mono[5];
+        int c = ChopQuadAtYExtrema(seg, mono);
+        for (int i = 0; i <= c; i++) add_quad(&mono[i * 2]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Edge sort: the reference sorts with std::sort (sw_raster.cc:679-704), whose
+// order among fully tied edges is that of introsort as the C++ runtime
+// implements it (Musser's introsort: median-of-three Hoare partitioning down
+// to blocks of 16, heapsort past a depth of 2*floor(log2 n), then insertion
+// sort).  Tied edges must keep that order for pixel parity, so the same
+// published algorithm is restated here over edge indices; tests compare its
+// permutation with std::sort.
+// ---------------------------------------------------------------------------
+struct EdgeLess {
+  const Edge* e;
+  SKC_HD bool operator()(int32_t ia, int32_t ib) const {
+    int va = e[ia].upper_y, vb = e[ib].upper_y;
+    if (va == vb) {
+      va = e[ia].x;
+      vb = e[ib].x;
+    }
+    if (va == vb) {
+      va = e[ia].dx;
+      vb = e[ib].dx;
+    }
+    return va < vb;
+  }
+};
+
+template <typename Less>
+SKC_HD void heap_sift(int32_t* a, int hole, int len, int32_t value, Less less) {
+  // move the hole down to a leaf along larger children, then sift value up
+  const int top = hole;
+  int child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (less(a[child], a[child - 1])) child--;
+    a[hole] = a[child];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    a[hole] = a[child - 1];
+    hole = child - 1;
+  }
+  int parent = (hole - 1) / 2;
+  while (hole > top && less(a[parent], value)) {
+    a[hole] = a[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  a[hole] = value;
+}
+template <typename Less>
+SKC_HD void heap_sort_range(int32_t* a, int len, Less less) {
+  if (len < 2) return;
+  for (int parent = (len - 2) / 2;; --parent) {
+    heap_sift(a, parent, len, a[parent], less);
+    if (parent == 0) break;
+  }
+  for (int last = len - 1; last > 0; --last) {
+    int32_t v = a[last];
+    a[last] = a[0];
+    heap_sift(a, 0, last, v, less);
+  }
+}
+template <typename Less>
+SKC_HD void median_to_first(int32_t* a, int r, int x, int y, int z, Less less) {
+  if (less(a[x], a[y])) {
+    if (less(a[y], a[z])) swap_(a[r], a[y]);
+    else if (less(a[x], a[z])) swap_(a[r], a[z]);
+    else swap_(a[r], a[x]);
+  } else if (less(a[x], a[z])) {
+    swap_(a[r], a[x]);
+  } else if (less(a[y], a[z])) {
+    swap_(a[r], a[z]);
+  } else {
+    swap_(a[r], a[y]);
+  }
+}
+template <typename Less>
+SKC_HD int partition_pivot(int32_t* a, int first, int last, Less less) {
+  int mid = first + (last - first) / 2;
+  median_to_first(a, first, first + 1, mid, last - 1, less);
+  int lo = first + 1, hi = last;
+  const int32_t pivot = a[first];
+  for (;;) {
+    while (less(a[lo], pivot)) ++lo;
+    --hi;
+    while (less(pivot, a[hi])) --hi;
+    if (!(lo < hi)) return lo;
+    swap_(a[lo], a[hi]);
+    ++lo;
+  }
+}
+template <typename Less>
+SKC_HD void insertion_sort(int32_t* a, int first, int last, Less less) {
+  if (first == last) return;
+  for (int i = first + 1; i < last; ++i) {
+    int32_t v = a[i];
+    if (less(v, a[first])) {
+      for (int k = i; k > first; --k) a[k] = a[k - 1];
+      a[first] = v;
+    } else {
+      int k = i;
+      while (less(v, a[k - 1])) {
+        a[k] = a[k - 1];
+        --k;
+      }
+      a[k] = v;
+    }
+  }
+}
+template <typename Less>
+SKC_HD void unguarded_insertion_sort(int32_t* a, int first, int last, Less less) {
+  for (int i = first; i < last; ++i) {
+    int32_t v = a[i];
+    int k = i;
+    while (less(v, a[k - 1])) {
+      a[k] = a[k - 1];
+      --k;
+    }
+    a[k] = v;
+  }
+}
+template <typename Less>
+SKC_HDN void introsort(int32_t* a, int n, Less less) {
+  if (n < 2) return;
+  // explicit stack of [first, last, depth] ranges (right part recursed
+  // first, left part looped), same visiting order as the recursive form
+  struct Range { int first, last, depth; };
+  Range stack[64];
+  int sp = 0;
+  int lg = 31 - clz_((uint32_t)n);
+  stack[sp++] = Range{0, n, 2 * lg};
+  while (sp > 0) {
+    Range r = stack[--sp];
+    int first = r.first, last = r.last, depth = r.depth;
+    while (last - first > 16) {
+      if (depth == 0) {
+        heap_sort_range(a + first, last - first, less);
+        break;
+      }
+      --depth;
+      int cut = partition_pivot(a, first, last, less);
+      // the recursive form sorts [cut, last) before continuing with
+      // [first, cut); both orders give the same result since the ranges are
+      // disjoint, but keep the reference's order for clarity
+      stack[sp++] = Range{first, cut, depth};
+      first = cut;
+      if (sp >= 63) break;  // cannot happen: depth <= 2*log2(n) < 62
+    }
+    if (last - first > 16 && depth != 0 && sp >= 63) {
+      heap_sort_range(a + first, last - first, less);
+    }
+  }
+  if (n > 16) {
+    insertion_sort(a, 0, 16, less);
+    unguarded_insertion_sort(a, 16, n, less);
+  } else {
+    insertion_sort(a, 0, n, less);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// AAA scanline sweep (sw_raster.cc:19-677) with a span sink
+// ---------------------------------------------------------------------------
+// Sink interface (Sink::real(x, y, len, alpha), Sink::acc_row(y, alphas,
+// left, lo, hi) is called at flush with the accumulated row).
+SKC_HD uint8_t partial_alpha_h(uint8_t alpha, Fixed h) {
+  return (uint8_t)FixedRoundToInt(wmul(alpha, h));
+}
+SKC_HD uint8_t partial_alpha_a(uint8_t alpha, uint8_t full) { return (uint8_t)((alpha * full) >> 8); }
+SKC_HD Fixed approximate_intersection(Fixed l1, Fixed r1, Fixed l2, Fixed r2) {
+  if (l1 > r1) swap_(l1, r1);
+  if (l2 > r2) swap_(l2, r2);
+  return wadd(max_(l1, l2), min_(r1, r2)) / 2;
+}
+SKC_HD uint8_t trapezoid_to_alpha(Fixed l1, Fixed l2) {
+  Fixed area = wadd(l1, l2) / 2;
+  return (uint8_t)(area >> 8);
+}
+SKC_HD uint8_t partial_triangle_to_alpha(Fixed a, Fixed b) {
+  Fixed area = wmul(wmul(a >> 11, a >> 11), b >> 11);
+  return (uint8_t)((area >> 8) & 0xFF);
+}
+
+template <typename Sink>
+struct Sweep {
+  Edge* E;
+  int head, tail;
+  Sink* sink;
+  // SpanBuilder accumulator (sw_raster.cc:62-136)
+  uint8_t* acc;
+  int acc_left, acc_width;
+  int acc_y;
+  int touch_lo, touch_hi;
+  float scan_top;
+  bool no_real_override;
+
+  SKC_HD void real(int x, int y, int len, uint8_t a) {
+    if (y < scan_top) return;
+    sink->real(x, y, len, a);
+  }
+  SKC_HD void real_spans(int x, int y, const uint8_t* aa, int len) {
+    if (y < scan_top) return;
+    for (int i = 0; i < len; i++) sink->real(x + i, y, 1, aa[i]);
+  }
+  SKC_HD void flush_acc() {
+    if (acc_y == kNaN32) return;
+    if (touch_lo <= touch_hi) {
+      sink->acc_row(acc_y, acc, acc_left, touch_lo, touch_hi + 1);
+      for (int i = touch_lo; i <= touch_hi; ++i) acc[i] = 0;
+    }
+    touch_lo = 0x7fffffff;
+    touch_hi = -1;
+  }
+  SKC_HD void flush_if_need(int y) {
+    if (acc_y == y) return;
+    if (acc_y == kNaN32) {
+      acc_y = y;
+      return;
+    }
+    flush_acc();
+    acc_y = y;
+  }
+  SKC_HD static uint8_t sat_add(uint8_t a, uint8_t d) {
+    return (uint16_t)a + (uint16_t)d > 255 ? 255 : (uint8_t)(a + d);
+  }
+  SKC_HD void acc_add(int x, int y, int width, uint8_t a) {
+    if (y < scan_top) return;
+    flush_if_need(y);
+    int off = x - acc_left;
+    for (int i = 0; i < width; i++) {
+      int o = off + i;
+      if ((unsigned)o < (unsigned)acc_width) {
+        acc[o] = sat_add(acc[o], a);
+        touch_lo = min_(touch_lo, o);
+        touch_hi = max_(touch_hi, o);
+      }
+    }
+  }
+  SKC_HD void acc_spans(int x, int y, const uint8_t* aa, int len) {
+    if (y < scan_top) return;
+    flush_if_need(y);
+    int off = x - acc_left;
+    for (int i = 0; i < len; i++) {
+      int o = off + i;
+      if ((unsigned)o < (unsigned)acc_width) {
+        acc[o] = sat_add(acc[o], aa[i]);
+        touch_lo = min_(touch_lo, o);
+        touch_hi = max_(touch_hi, o);
+      }
+    }
+  }
+
+  SKC_HD void blit_single(int y, int x, uint8_t alpha, uint8_t full, bool no_real) {
+    if (full == 0xFF && !no_real) real(x, y, 1, alpha);
+    else acc_add(x, y, 1, partial_alpha_a(alpha, full));
+  }
+  SKC_HD void blit_two(int y, int x, uint8_t a1, uint8_t a2, uint8_t full, bool no_real) {
+    if (full == 0xFF && !no_real) {
+      real(x, y, 1, a1);
+      real(x + 1, y, 1, a2);
+    } else {
+      acc_add(x, y, 1, a1);
+      acc_add(x + 1, y, 1, a2);
+    }
+  }
+  SKC_HD void blit_full(int y, int x, int len, uint8_t full, bool no_real) {
+    if (full == 0xFF && !no_real) real(x, y, len, full);
+    else acc_add(x, y, len, full);
+  }
+  SKC_HD static void alpha_above(uint8_t* alphas, Fixed l, Fixed r, Fixed dY, uint8_t full) {
+    int R = FixedCeilToInt(r);
+    if (R == 0) return;
+    if (R == 1) {
+      alphas[0] = partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
+      return;
+    }
+    Fixed first = kFixed1 - l;
+    Fixed last = r - ((R - 1) << 16);
+    Fixed firstH = FixedMul(first, dY);
+    alphas[0] = (uint8_t)(FixedMul(first, firstH) >> 9);
+    Fixed alpha16 = wadd(firstH, dY >> 1);
+    for (int i = 1; i < R - 1; ++i) {
+      alphas[i] = (uint8_t)(alpha16 >> 8);
+      alpha16 = wadd(alpha16, dY);
+    }
+    alphas[R - 1] = (uint8_t)(full - partial_triangle_to_alpha(last, dY));
+  }
+  SKC_HD static void alpha_below(uint8_t* alphas, Fixed l, Fixed r, Fixed dY, uint8_t full) {
+    int R = FixedCeilToInt(r);
+    if (R == 0) return;
+    if (R == 1) {
+      alphas[0] = partial_alpha_a(trapezoid_to_alpha(l, r), full);
+      return;
+    }
+    Fixed first = kFixed1 - l;
+    Fixed last = r - ((R - 1) << 16);
+    Fixed lastH = FixedMul(last, dY);
+    alphas[R - 1] = (uint8_t)(FixedMul(last, lastH) >> 9);
+    Fixed alpha16 = wadd(lastH, dY >> 1);
+    for (int i = R - 2; i > 0; i--) {
+      alphas[i] = (uint8_t)((alpha16 >> 8) & 0xFF);
+      alpha16 = wadd(alpha16, dY);
+    }
+    alphas[0] = (uint8_t)(full - partial_triangle_to_alpha(first, dY));
+  }
+
+  // blit_aaa_trapezoid_row (sw_raster.cc:372-455).  The per-pixel alpha
+  // arrays live in thread-local scratch: wider rows are processed in
+  // windows of kWin pixels (the alphas of one pixel depend only on that
+  // pixel's index), so any width fits.
+  static constexpr int kWin = 64;
+  SKC_HDN void aaa_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
+                       uint8_t full, bool no_real) {
+    int L = FixedFloorToInt(ul), R = FixedCeilToInt(lr);
+    int len = R - L;
+    if (len == 1) {
+      blit_single(y, L, trapezoid_to_alpha(ur - ul, lr - ll), full, no_real);
+      return;
+    }
+    int uL = FixedFloorToInt(ul), lL = FixedCeilToInt(ll);
+    int uR = FixedFloorToInt(ur), lR = FixedCeilToInt(lr);
+    bool two_left = uL + 2 == lL, two_right = uR + 2 == lR;
+    uint8_t la1 = 0, la2 = 0, ra1 = 0, ra2 = 0;
+    if (two_left) {
+      Fixed first = IntToFixed(uL) + kFixed1 - ul;
+      Fixed second = ll - ul - first;
+      la1 = (uint8_t)(full - partial_triangle_to_alpha(first, lDY));
+      la2 = partial_triangle_to_alpha(second, lDY);
+    }
+    if (two_right) {
+      Fixed first = IntToFixed(uR) + kFixed1 - ur;
+      Fixed second = lr - ur - first;
+      ra1 = partial_triangle_to_alpha(first, rDY);
+      ra2 = (uint8_t)(full - partial_triangle_to_alpha(second, rDY));
+    }
+    // full-width temp arrays computed on demand (left/right triangles can
+    // be wider than a window, so they are recomputed per window)
+    uint8_t alphas[kWin];
+    uint8_t templ[kWin + 1], tempr[kWin + 1];
+    for (int w0 = 0; w0 < len; w0 += kWin) {
+      int wn = min_(kWin, len - w0);
+      for (int i = 0; i < wn; ++i) alphas[i] = full;
+      // left edge (pixels uL .. lL-1)
+      if (two_left) {
+        if (w0 == 0) {
+          alphas[0] = alphas[0] > la1 ? (uint8_t)(alphas[0] - la1) : 0;
+          if (wn > 1) alphas[1] = alphas[1] > la2 ? (uint8_t)(alphas[1] - la2) : 0;
+        } else if (w0 == 1) {
+          alphas[0] = alphas[0] > la2 ? (uint8_t)(alphas[0] - la2) : 0;
+        }
+      } else if (lL > uL) {
+        int a0 = max_(uL, L + w0), a1 = min_(lL, L + w0 + wn);
+        if (a0 < a1) {
+          triangle_window(templ, true, ul - IntToFixed(uL), ll - IntToFixed(uL), lDY, full,
+                          a0 - uL, a1 - uL);
+          for (int i = a0; i < a1; ++i) {
+            uint8_t t = templ[i - a0];
+            uint8_t& d = alphas[i - L - w0];
+            d = d > t ? (uint8_t)(d - t) : 0;
+          }
+        }
+      }
+      // right edge (pixels uR .. lR-1)
+      if (two_right) {
+        int p0 = len - 2 - w0, p1 = len - 1 - w0;
+        if (p0 >= 0 && p0 < wn) alphas[p0] = alphas[p0] > ra1 ? (uint8_t)(alphas[p0] - ra1) : 0;
+        if (p1 >= 0 && p1 < wn) alphas[p1] = alphas[p1] > ra2 ? (uint8_t)(alphas[p1] - ra2) : 0;
+      } else if (lR > uR) {
+        int a0 = max_(uR, L + w0), a1 = min_(lR, L + w0 + wn);
+        if (a0 < a1) {
+          triangle_window(tempr, false, ur - IntToFixed(uR), lr - IntToFixed(uR), rDY, full,
+                          a0 - uR, a1 - uR);
+          for (int i = a0; i < a1; ++i) {
+            uint8_t t = tempr[i - a0];
+            uint8_t& d = alphas[i - L - w0];
+            d = d > t ? (uint8_t)(d - t) : 0;
+          }
+        }
+      }
+      if (full == 0xFF && !no_real) real_spans(L + w0, y, alphas, wn);
+      else acc_spans(L + w0, y, alphas, wn);
+    }
+  }
+  // Entries [i0, i1) of compute_alpha_below_line (below = true) or
+  // compute_alpha_above_line over R = ceil(r) pixels, into out[0 .. i1-i0).
+  // Entry i of the reference's array depends only on i (and the running sum
+  // alpha16, re-derived here), so windows reproduce it exactly.
+  SKC_HD static void triangle_window(uint8_t* out, bool below, Fixed l, Fixed r, Fixed dY,
+                                     uint8_t full, int i0, int i1) {
+    int R = FixedCeilToInt(r);
+    if (R <= 0) return;
+    if (R == 1) {
+      uint8_t v = below ? partial_alpha_a(trapezoid_to_alpha(l, r), full)
+                        : partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
+      if (i0 <= 0 && 0 < i1) out[0 - i0] = v;
+      return;
+    }
+    Fixed first = kFixed1 - l;
+    Fixed last = r - ((R - 1) << 16);
+    if (below) {
+      Fixed lastH = FixedMul(last, dY);
+      for (int i = i0; i < i1; ++i) {
+        uint8_t v;
+        if (i == R - 1) {
+          v = (uint8_t)(FixedMul(last, lastH) >> 9);
+        } else if (i == 0) {
+          v = (uint8_t)(full - partial_triangle_to_alpha(first, dY));
+        } else {
+          // alpha16 after (R - 2 - i) additions of dY to lastH + dY/2
+          Fixed a16 = wadd(wadd(lastH, dY >> 1), wmul(R - 2 - i, dY));
+          v = (uint8_t)((a16 >> 8) & 0xFF);
+        }
+        out[i - i0] = v;
+      }
+    } else {
+      Fixed firstH = FixedMul(first, dY);
+      for (int i = i0; i < i1; ++i) {
+        uint8_t v;
+        if (i == 0) {
+          v = (uint8_t)(FixedMul(first, firstH) >> 9);
+        } else if (i == R - 1) {
+          v = (uint8_t)(full - partial_triangle_to_alpha(last, dY));
+        } else {
+          Fixed a16 = wadd(wadd(firstH, dY >> 1), wmul(i - 1, dY));
+          v = (uint8_t)(a16 >> 8);
+        }
+        out[i - i0] = v;
+      }
+    }
+  }
+
+  SKC_HDN void trapezoid_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
+                             uint8_t full, bool no_real) {  // sw_raster.cc:457-544
+    if (ul > ur) return;
+    if (ll > lr) ll = lr = approximate_intersection(ul, ll, ur, lr);
+    if (ul == ur && ll == lr) return;
+    if (ul > ll) swap_(ul, ll);
+    if (ur > lr) swap_(ur, lr);
+    Fixed joinLeft = FixedCeilToFixed(ll);
+    Fixed joinRite = FixedFloorToFixed(ur);
+    if (joinLeft <= joinRite) {
+      if (ul < joinLeft) {
+        int len = FixedCeilToInt(joinLeft - ul);
+        if (len == 1) {
+          blit_single(y, ul >> 16, trapezoid_to_alpha(joinLeft - ul, joinLeft - ll), full, no_real);
+        } else if (len == 2) {
+          Fixed first = joinLeft - kFixed1 - ul;
+          Fixed second = ll - ul - first;
+          uint8_t a1 = partial_triangle_to_alpha(first, lDY);
+          uint8_t a2 = (uint8_t)(full - partial_triangle_to_alpha(second, lDY));
+          blit_two(y, ul >> 16, a1, a2, full, no_real);
+        } else {
+          aaa_row(y, ul, joinLeft, ll, joinLeft, lDY, kMaxS32, full, no_real);
+        }
+      }
+      if (joinLeft < joinRite) {
+        blit_full(y, FixedFloorToInt(joinLeft), FixedFloorToInt(joinRite - joinLeft), full, no_real);
+      }
+      if (lr > joinRite) {
+        int len = FixedCeilToInt(lr - joinRite);
+        if (len == 1) {
+          blit_single(y, joinRite >> 16, trapezoid_to_alpha(ur - joinRite, lr - joinRite), full, no_real);
+        } else if (len == 2) {
+          Fixed first = joinRite + kFixed1 - ur;
+          Fixed second = lr - ur - first;
+          uint8_t a1 = (uint8_t)(full - partial_triangle_to_alpha(first, rDY));
+          uint8_t a2 = partial_triangle_to_alpha(second, rDY);
+          blit_two(y, joinRite >> 16, a1, a2, full, no_real);
+        } else {
+          aaa_row(y, joinRite, ur, joinRite, lr, kMaxS32, rDY, full, no_real);
+        }
+      }
+    } else {
+      aaa_row(y, ul, ur, ll, lr, lDY, rDY, full, no_real);
+    }
+  }
+
+  // ---- active edge list (sw_raster.cc:138-247)
+  SKC_HD bool too_close_e(int prev, int next, Fixed lowerY) const {
+    if (next < 0 || prev < 0) return false;
+    return E[next].upper_y < lowerY &&
+           wadd(E[prev].x, kFixed1) >= wsub(E[next].x, iabs_(E[next].dx));
+  }
+  SKC_HD static bool too_close_r(int prevRite, Fixed ul, Fixed ll) {
+    return prevRite > FixedFloorToInt(ul) || prevRite > FixedFloorToInt(ll);
+  }
+  SKC_HD static void nny_update(Fixed y, Fixed next_y, Fixed* nny) {
+    *nny = y > next_y && y < *nny ? y : *nny;
+  }
+  SKC_HD void check_intersection(int edge, Fixed next_y, Fixed* nny) const {
+    const Edge& e = E[edge];
+    const Edge& p = E[e.prev];
+    if (p.prev >= 0 && wadd(p.x, p.dx) > wadd(e.x, e.dx)) *nny = next_y + (kFixed1 >> kAccuracy);
+  }
+  SKC_HD void remove_edge(int edge) {
+    E[E[edge].prev].next = E[edge].next;
+    E[E[edge].next].prev = E[edge].prev;
+  }
+  SKC_HD void insert_after(int edge, int after) {
+    E[edge].prev = after;
+    E[edge].next = E[after].next;
+    E[E[after].next].prev = edge;
+    E[after].next = edge;
+  }
+  SKC_HD void backward_insert(int edge) {
+    Fixed x = E[edge].x;
+    int prev = E[edge].prev;
+    while (E[prev].prev >= 0 && E[prev].x > x) prev = E[prev].prev;
+    if (E[prev].next != edge) {
+      remove_edge(edge);
+      insert_after(edge, prev);
+    }
+  }
+  SKC_HDN void insert_new_edges(int ne, Fixed y, Fixed* nny) {  // :207-247
+    if (E[ne].upper_y > y) {
+      nny_update(E[ne].upper_y, y, nny);
+      return;
+    }
+    int prev = E[ne].prev;
+    if (E[prev].x <= E[ne].x) {
+      while (E[ne].upper_y <= y) {
+        check_intersection(ne, y, nny);
+        nny_update(E[ne].lower_y, y, nny);
+        ne = E[ne].next;
+      }
+      nny_update(E[ne].upper_y, y, nny);
+      return;
+    }
+    int start = prev;
+    Fixed nx = E[ne].x;
+    while (E[start].prev >= 0 && E[start].x > nx) start = E[start].prev;
+    do {
+      int next = E[ne].next;
+      bool skip = false;
+      for (;;) {
+        if (E[start].next == ne) {
+          skip = true;
+          break;
+        }
+        int after = E[start].next;
+        if (E[after].x >= E[ne].x) break;
+        start = after;
+      }
+      if (!skip) {
+        remove_edge(ne);
+        insert_after(ne, start);
+      }
+      check_intersection(ne, y, nny);
+      nny_update(E[ne].lower_y, y, nny);
+      start = ne;
+      ne = next;
+    } while (E[ne].upper_y <= y);
+    nny_update(E[ne].upper_y, y, nny);
+  }
+
+  // WalkEdges (sw_raster.cc:546-677)
+  SKC_HDN void walk(bool even_odd, int start_y, int stop_y, Fixed left_clip, Fixed right_clip) {
+    E[head].x = E[head].upper_x = left_clip;
+    E[tail].x = E[tail].upper_x = right_clip;
+    Fixed y = max_(E[E[head].next].upper_y, IntToFixed(start_y));
+    Fixed nny = kMaxS32;
+    {
+      int edge;
+      for (edge = E[head].next; E[edge].upper_y <= y; edge = E[edge].next) {
+        GoY(&E[edge], y);
+        nny_update(E[edge].lower_y, y, &nny);
+      }
+      nny_update(E[edge].upper_y, y, &nny);
+    }
+    int winding_mask = even_odd ? 1 : -1;
+    for (;;) {
+      int w = 0;
+      bool in_interval = false;
+      Fixed prev_x = E[head].x;
+      Fixed next_y = min_(nny, FixedCeilToFixed(y + 1));
+      int curr = E[head].next;
+      int left_edge = head;
+      Fixed left = left_clip;
+      Fixed left_dy = 0;
+      int prev_right = FixedFloorToInt(left_clip);
+      nny = kMaxS32;
+      int y_shift = 0;
+      if ((next_y - y) & (kFixed1 >> 2)) {
+        y_shift = 2;
+        next_y = y + (kFixed1 >> 2);
+      } else if ((next_y - y) & (kFixed1 >> 1)) {
+        y_shift = 1;
+      }
+      uint8_t full = partial_alpha_h(0xFF, next_y - y);
+      while (E[curr].upper_y <= y) {
+        Edge& ce = E[curr];
+        w += ce.winding;
+        bool prev_in = in_interval;
+        in_interval = (w & winding_mask) != 0;
+        bool is_left = in_interval && !prev_in;
+        bool is_right = !in_interval && prev_in;
+        if (is_left) {
+          left = max_(ce.x, left_clip);
+          left_dy = ce.dy;
+          left_edge = curr;
+          GoYShift(&ce, next_y, y_shift);
+        } else if (is_right) {
+          Fixed right = min_(right_clip, ce.x);
+          GoYShift(&ce, next_y, y_shift);
+          Fixed next_left = max_(left_clip, E[left_edge].x);
+          Fixed next_right = min_(right_clip, ce.x);
+          bool no_real = full == 0xFF && (too_close_r(prev_right, left, E[left_edge].x) ||
+                                          too_close_e(curr, ce.next, next_y));
+          trapezoid_row(y >> 16, left, right, next_left, next_right, left_dy, ce.dy, full, no_real);
+          prev_right = FixedCeilToInt(max_(right, ce.x));
+        } else {
+          GoYShift(&ce, next_y, y_shift);
+        }
+        int next = ce.next;
+        while (E[curr].lower_y <= next_y) {
+          if (E[curr].curve_count > 0) {
+            E[curr].snapped_x = E[curr].x;  // KeepContinuous (sw_edge.cc:294-297)
+            E[curr].snapped_y = E[curr].y;
+            if (!UpdateQuad(&E[curr])) break;
+          } else {
+            break;
+          }
+        }
+        if (E[curr].lower_y <= next_y) {
+          remove_edge(curr);
+        } else {
+          nny_update(E[curr].lower_y, next_y, &nny);
+          Fixed new_x = E[curr].x;
+          if (new_x < prev_x) {
+            backward_insert(curr);
+          } else {
+            prev_x = new_x;
+          }
+          check_intersection(curr, next_y, &nny);
+        }
+        curr = next;
+      }
+      if (in_interval) {
+        bool no_real = full == 0xFF && too_close_e(E[left_edge].prev, left_edge, next_y);
+        trapezoid_row(y >> 16, left, right_clip, max_(left_clip, E[left_edge].x), right_clip,
+                      left_dy, 0, full, no_real);
+      }
+      y = next_y;
+      if (y >= IntToFixed(stop_y)) break;
+      insert_new_edges(curr, y, &nny);
+    }
+  }
+};
+
+// The flushed accumulator row as RLE spans (SpanBuilder::Flush,
+// sw_raster.cc:103-136): runs of equal nonzero alphas.
+template <typename F>
+SKC_HD void acc_runs(const uint8_t* acc, int lo, int hi, F&& emit) {
+  int curr = lo;
+  while (curr < hi) {
+    uint8_t a = acc[curr];
+    if (a > 0) {
+      int start = curr, width = 1;
+      for (;;) {
+        curr++;
+        if (curr >= hi) break;
+        if (acc[curr] == a) {
+          width++;
+        } else {
+          break;
+        }
+      }
+      emit(start, width, a);
+    } else {
+      curr++;
+    }
+  }
+}
+
+}  // namespace skc

@@ -1,0 +1,148 @@
+// Test-only: runs the CUDA kernels' per-thread bodies (skity_gb300/csrc/
+// passes.cuh) sequentially on the CPU, with the same host-side batch
+// building (batch.h) and the same buffer planning as the GPU pipeline.
+//
+// This is NOT a fallback of the library (the library has none): it lets the
+// CPU test suite check the device code paths -- geometry, introsort, sweep,
+// span layout, compositing, blur -- against the oracle before any GPU run.
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../skity_gb300/csrc/batch.h"
+#include "../skity_gb300/csrc/passes.cuh"
+
+using namespace skc;
+
+extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rgba,
+                              uint64_t stats[6]) {
+  StreamView sv;
+  if (!ParseStream(stream, len, &sv)) return -2;
+  HostBatch hb;
+  int rc = AddStreamCanvas(hb, sv);
+  if (rc) return rc;
+  const uint32_t np = (uint32_t)hb.passes.size();
+  if (hb.verbs.empty()) hb.verbs.push_back(0);
+  if (hb.pts.empty()) hb.pts.push_back(mkP(0, 0));
+  if (hb.weights.empty()) hb.weights.push_back(0);
+  if (hb.stop_colors.empty()) {
+    hb.stop_colors.push_back(make_float4(0, 0, 0, 0));
+    hb.stop_offsets.push_back(0);
+  }
+  std::vector<uint8_t> pixels(hb.pixel_bytes + 16, 0);
+  std::vector<uint8_t> rtab(256);
+  for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
+
+  DevBatch b{};
+  b.verbs = hb.verbs.data();
+  b.pts = hb.pts.data();
+  b.weights = hb.weights.data();
+  b.draws = hb.draws.data();
+  b.n_passes = np;
+  b.canvases = hb.canvases.data();
+  std::vector<PassGeom> geom(np);
+  std::vector<uint8_t> scratch;
+  uint64_t retries = 0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < np; ++i) {
+      SliceLayout L;
+      L.compute(hb.passes[i].cap, sizeof(Edge));
+      hb.passes[i].slice_off = total;
+      total += L.bytes;
+    }
+    scratch.assign(total + 16, 0);
+    b.passes = hb.passes.data();
+    b.scratch = scratch.data();
+    b.geom = geom.data();
+    for (uint32_t p = 0; p < np; ++p) GeometryPass(b, p);
+    uint32_t grown = 0;
+    for (uint32_t p = 0; p < np; ++p) {
+      if (geom[p].status) {
+        GrowCaps(hb.passes[p], geom[p]);
+        grown++;
+      }
+    }
+    retries += grown;
+    if (!grown) break;
+    if (attempt == 7) return -7;
+  }
+  std::vector<PassSweep> sw;
+  SweepPlan pl = PlanSweep(geom, sw);
+  std::vector<Edge> work(pl.work_edges + 1);
+  std::vector<uint8_t> acc(pl.acc_bytes + 16, 0);
+  std::vector<uint32_t> rowtab(pl.rows + 1, 0), pass_spans(np + 1, 0);
+  b.sweep = sw.data();
+  b.work = work.data();
+  b.acc = acc.data();
+  b.rowtab = rowtab.data();
+  b.pass_spans = pass_spans.data();
+  for (uint32_t p = 0; p < np; ++p) SweepCountPass(b, p);
+  std::vector<PassComp> comp;
+  uint64_t spans = PlanComp(hb, geom, sw, pass_spans, comp);
+  std::vector<uint2> span_buf(spans + 1);
+  b.comp = comp.data();
+  b.spans = span_buf.data();
+  for (uint32_t p = 0; p < np; ++p) SweepEmitPass(b, p);
+  b.brushes = hb.brushes.data();
+  b.stop_colors = hb.stop_colors.data();
+  b.stop_offsets = hb.stop_offsets.data();
+  b.pixels = pixels.data();
+  b.roundtrip = rtab.data();
+  std::vector<uint32_t> row(65536);
+  std::vector<RowTask> tasks;
+  BuildRowTasks(hb, hb.temp_canvases, 65535, tasks);
+  for (const RowTask& t : tasks) CompositeRowScalar(b, t, row.data());
+  for (uint32_t c : hb.temp_canvases) {
+    const CanvasDesc& cd = hb.canvases[c];
+    int r = std::min(cd.blur_radius, 254);
+    for (uint32_t y = 0; y < cd.h; ++y) {
+      const uint8_t* src = pixels.data() + cd.px_off + (size_t)y * cd.w * 4;
+      uint8_t* dst = pixels.data() + cd.blur_off + (size_t)y * cd.w * 4;
+      if (r <= 1) std::memcpy(dst, src, (size_t)cd.w * 4);
+      else BlurLine(src, dst, (int)cd.w, 1, r, false);
+    }
+    for (uint32_t x = 0; x < cd.w; ++x) {
+      const uint8_t* src = pixels.data() + cd.blur_off + (size_t)x * 4;
+      uint8_t* dst = pixels.data() + cd.px_off + (size_t)x * 4;
+      if (r <= 1) {
+        for (uint32_t y = 0; y < cd.h; ++y) std::memcpy(dst + (size_t)y * cd.w * 4, src + (size_t)y * cd.w * 4, 4);
+      } else {
+        BlurLine(src, dst, (int)cd.h, cd.w, r, true);
+      }
+    }
+  }
+  BuildRowTasks(hb, hb.main_canvases, 65535, tasks);
+  for (const RowTask& t : tasks) CompositeRowScalar(b, t, row.data());
+  const CanvasDesc& cd = hb.canvases[hb.main_canvases[0]];
+  std::memcpy(out_rgba, pixels.data() + cd.px_off, (size_t)cd.w * cd.h * 4);
+  if (stats) {
+    stats[0] = np;
+    stats[1] = pl.edges;
+    stats[2] = spans;
+    stats[3] = retries;
+    stats[4] = hb.temp_canvases.size();
+    stats[5] = hb.draw_count;
+  }
+  return 0;
+}
+
+// The device introsort on an arbitrary key array, for the permutation test
+// against std::sort.
+struct KeyLess {
+  const int32_t* k;
+  bool operator()(int32_t a, int32_t b) const { return k[a] < k[b]; }
+};
+extern "C" void skc_cpu_introsort(const int32_t* keys, int32_t* idx, int n) {
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  KeyLess less{keys};
+  introsort(idx, n, less);
+}
+
+// std::sort with the same "less" on the same initial order: the permutation
+// the reference's SortEdges produces (sw_raster.cc:679-704).
+#include <algorithm>
+extern "C" void skc_std_sort(const int32_t* keys, int32_t* idx, int n) {
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx, idx + n, [&](int32_t a, int32_t b) { return keys[a] < keys[b]; });
+}

@@ -1,0 +1,151 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle.
+Bar: <= 1 LSB per channel and >= 99.9% of pixels exact (bit-exact expected)."""
+import numpy as np
+import pytest
+
+from skity_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+TOL_LSB, MIN_EXACT = 1, 0.999
+
+
+def check(oracle_lib, got, sc, first=0, count=None):
+    ref, _ = oracle_lib.render(sc, first, count)
+    c = oracle_lib.compare(got, ref)
+    assert c["max_abs_diff"] <= TOL_LSB and c["exact_frac"] >= MIN_EXACT, c
+    return c
+
+
+def test_config1_full(gpu_ctx, oracle_lib):
+    sc = S.config1()
+    got = gpu_ctx.render_streams([sc])[0]
+    c = check(oracle_lib, got, sc)
+    assert c["bad_pixels"] == 0
+
+
+def test_config2_subset(gpu_ctx, oracle_lib):
+    sc = S.config2(n_paths=400)
+    got = gpu_ctx.render_streams([sc])[0]
+    check(oracle_lib, got, sc)
+
+
+def test_config4_blur_subset(gpu_ctx, oracle_lib):
+    sc = S.config4(n_outlines=3000, width=1024, height=1024, blur_frac=0.2)
+    got = gpu_ctx.render_streams([sc])[0]
+    check(oracle_lib, got, sc)
+
+
+def test_config3_batch(gpu_ctx, oracle_lib):
+    scenes = S.config3(n_canvases=12, scale=0.2)
+    outs = gpu_ctx.render_streams(scenes)
+    for sc, got in zip(scenes, outs):
+        check(oracle_lib, got, sc)
+
+
+def test_batch_rerender_is_deterministic(gpu_ctx, oracle_lib):
+    from skity_gb300.canvas import Batch
+    scenes = S.config3(n_canvases=4, scale=0.1)
+    b = Batch(gpu_ctx, scenes)
+    b.render()
+    first = [b.read(i) for i in range(len(scenes))]
+    b.render()
+    for i, sc in enumerate(scenes):
+        again = b.read(i)
+        assert np.array_equal(first[i], again)
+        check(oracle_lib, again, sc)
+    b.close()
+
+
+def test_canvas_api_like_reference_test(gpu_ctx):
+    """Restates the exact-pixel check of the reference's
+    test/ut/render/sw_canvas_test.cc (StrokeThenFill order) on the CUDA
+    canvas: a stroked-then-filled rect leaves white inside the fill and the
+    stroke colour on the border."""
+    from skity_gb300.canvas import Canvas, Paint, Path, Style, ColorSetARGB
+    bitmap = np.zeros((40, 40, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear(ColorSetARGB(0xFF, 0, 0, 0))
+    paint = Paint()
+    paint.SetStyle(Style.kStrokeThenFill_Style)
+    paint.SetStrokeWidth(10)
+    paint.SetFillColor(1, 1, 1, 1)
+    paint.SetStrokeColor(1, 0, 0, 1)
+    canvas.DrawPath(Path().AddRect(10, 10, 30, 30), paint)
+    canvas.Flush()
+    assert tuple(bitmap[20, 12]) == (255, 255, 255, 255)  # fill drawn over the stroke
+    assert tuple(bitmap[20, 7]) == (255, 0, 0, 255)       # stroke outside the rect
+
+
+def test_canvas_matches_stream_and_oracle(gpu_ctx, oracle_lib):
+    from skity_gb300.canvas import Canvas, Paint, Path, Shader, PathFillType, TileMode, MaskFilter, BlurStyle
+    sb = S.SceneBuilder(120, 90)
+    bitmap = np.zeros((90, 120, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    rng = np.random.default_rng(3)
+    for i in range(30):
+        path = Path().MoveTo(*rng.uniform(-10, 130, 2))
+        for _ in range(5):
+            path.CubicTo(*rng.uniform(-10, 130, 6))
+        path.Close().SetFillType(PathFillType.kEvenOdd if i % 3 == 0 else PathFillType.kWinding)
+        paint = Paint().SetColor(0xFF000000 | int(rng.integers(0, 1 << 24))).SetAlphaF(0.6)
+        if i % 4 == 1:
+            paint.SetStyle(1).SetStrokeWidth(3).SetStrokeCap(i % 3).SetStrokeJoin(i % 3)
+        if i % 5 == 2:
+            paint.SetShader(Shader.MakeLinear([(0, 0), (120, 90)], [[1, 0, 0, 1], [0, 0, 1, 0.5]], None, 2))
+        if i % 7 == 3:
+            paint.SetMaskFilter(MaskFilter.MakeBlur(BlurStyle.kNormal, 4.0))
+        canvas.DrawPath(path, paint)
+        g = -1
+        if paint.shader is not None:
+            s = paint.shader
+            g = sb.add_gradient(s.kind, s.p0, s.p1, s.radius, s.colors, None, TileMode.kClamp)
+        rec = paint.rec.copy(); rec["fill_type"] = path.fill_type; rec["gradient"] = g
+        if paint.mask_filter is not None:
+            rec["blur_style"] = paint.mask_filter.style
+            rec["blur_radius"] = paint.mask_filter.radius
+        sb.draw_path(path.verbs, path.points, rec)
+    canvas.Flush()
+    check(oracle_lib, bitmap, sb.build())
+
+
+def test_flush_then_draw_blends_over_previous_pixels(gpu_ctx, oracle_lib):
+    from skity_gb300.canvas import Canvas, Paint, Path
+    bitmap = np.zeros((32, 32, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((0.0, 0.5, 1.0, 1.0))
+    canvas.DrawPath(Path().MoveTo(2, 2).LineTo(30, 5).LineTo(8, 29).Close(),
+                    Paint().SetFillColor(1, 0, 0, 0.5))
+    canvas.Flush()
+    canvas.DrawPath(Path().MoveTo(30, 2).LineTo(1, 16).LineTo(30, 30).Close(),
+                    Paint().SetFillColor(0, 1, 0, 0.7))
+    canvas.Flush()
+    sb = S.SceneBuilder(32, 32, clear=(0.0, 0.5, 1.0, 1.0))
+    p = S.default_paint(); p["fill_color"] = (1, 0, 0, 0.5)
+    sb.draw_path([0, 1, 1, 5], [(2, 2), (30, 5), (8, 29)], p)
+    p2 = S.default_paint(); p2["fill_color"] = (0, 1, 0, 0.7)
+    sb.draw_path([0, 1, 1, 5], [(30, 2), (1, 16), (30, 30)], p2)
+    check(oracle_lib, bitmap, sb.build())
+
+
+def test_invalid_arguments_are_rejected(gpu_ctx):
+    import ctypes
+    from skity_gb300 import _lib
+    from skity_gb300.canvas import Canvas
+    assert Canvas.MakeCUDACanvas(gpu_ctx, None) is None
+    assert Canvas.MakeCUDACanvas(gpu_ctx, np.zeros((0, 0, 4), np.uint8)) is None
+    lib = gpu_ctx.lib
+    assert lib.skity_cuda_canvas_flush(None) == -1
+    bad = b"NOPE" + b"\0" * 100
+    ptrs = (ctypes.c_void_p * 1)(ctypes.cast(ctypes.c_char_p(bad), ctypes.c_void_p))
+    lens = (ctypes.c_size_t * 1)(len(bad))
+    out = np.zeros(16, np.uint8)
+    optr = (ctypes.c_void_p * 1)(out.ctypes.data)
+    assert lib.skity_cuda_render_streams(gpu_ctx.handle, 1, ptrs, lens, optr) == -2
+    bitmap = np.zeros((8, 8, 4), np.uint8)
+    c = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    verbs = (ctypes.c_uint8 * 2)(0, 9)   # unknown verb
+    pts = (ctypes.c_float * 2)(1, 1)
+    cp = _lib.Path_(ctypes.cast(verbs, ctypes.c_void_p), 2, ctypes.cast(pts, ctypes.c_void_p), 1, None, 0, 0)
+    paint = _lib.Paint_()
+    assert lib.skity_cuda_canvas_draw_path(c.handle, ctypes.byref(cp), ctypes.byref(paint)) == -2
