@@ -1,0 +1,287 @@
+"""Benchmark of the GB300 raster backend on the single-large-scene workload:
+a 2048x2048 premultiplied RGBA8 canvas cleared to white, 20,000 seeded
+synthetic paths of 3-64 verbs (50% lines / 25% quads / 25% cubics,
+coordinates uniform in [-64, 2112]^2), 30% even-odd, 50% solid / 25% linear
+/ 25% radial gradients, 20% stroked (width 1-8, all caps and joins), one
+DrawPath per path, one Flush (skity_gb300.scene.config2).
+
+One step = rendering the whole scene (every DrawPath + Flush).
+  value: paths/s with the scene resident in device memory (CUDA events
+         around each render on the library's stream), summed over ranks;
+  e2e:   the same through skity_cuda_render_streams with host buffers: the
+         scene stream uploaded and the pixels read back inside every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Multi-GPU: every rank renders its own replica (independent canvases, no
+collective on the data path); the timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = ("Mpix/s & paths/s, batched vs per-draw GPU vs CPU, ≤1 LSB; p50/p99 ms")
+WORKLOAD = ("config2: 2048x2048 RGBA8 canvas, 20,000 seeded paths (3-64 verbs line/quad/cubic, "
+            "coords U[-64,2112]^2, 30% even-odd, 25% linear + 25% radial gradients 2-8 stops, "
+            "20% stroked w U[1,8] all caps x joins), one DrawPath per path, one Flush")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"skity_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            os.unlink(self.path)
+        except Exception:
+            pass
+        loaded = [s for s in sm if s > 0.5 * (max(mx) if mx else 0)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_scene():
+    from skity_gb300 import scene as S
+    cache = os.path.join("/tmp", "skity_config2_v1.bin")
+    try:
+        with open(cache, "rb") as f:
+            return S.Scene.from_bytes(f.read())
+    except Exception:
+        sc = S.config2()
+        try:
+            with open(cache, "wb") as f:
+                f.write(sc.to_bytes())
+        except Exception:
+            pass
+        return sc
+
+
+def cpu_baseline(scene, threads: int, sample_paths: int, steps: int = 1):
+    """The oracle (CPU restatement of the reference path) on the first
+    `sample_paths` draws; paths/s over `steps` repetitions."""
+    from oracle import oracle
+    oracle.build()
+    secs = []
+    for _ in range(steps):
+        if threads == 1:
+            _, st = oracle.render(scene, 0, sample_paths)
+        else:
+            _, st = oracle.render_mt(scene, threads, 0, sample_paths)
+        secs.append(st.seconds)
+    return sample_paths / statistics.mean(secs), secs
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    scene = load_scene()
+    threads = os.cpu_count() or 1
+    sample = args.ref_sample_paths
+    # warm-up (untimed), then timed steps, each a bounded sample of the scene
+    for _ in range(args.warmup):
+        cpu_baseline(scene, threads, min(sample, 50))
+    value, secs = cpu_baseline(scene, threads, sample, steps=args.steps)
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs) * scene.n_draws / sample,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32/f32",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": WORKLOAD, "canvas": "2048x2048", "paths": scene.n_draws},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} of {scene.n_draws} paths per step, banded rows "
+                                   f"on {threads} threads (identical pixels)"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from skity_gb300.canvas import Batch, Context
+
+    scene = load_scene()
+    ctx = Context(local)
+    batch = Batch(ctx, [scene])
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    for _ in range(max(args.warmup, 1)):
+        batch.render()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms, stages = [], []
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush_buf.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        st = batch.render()
+        step_ms.append(st["device_ms"])
+        stages.append(st)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = torch.tensor([sum(step_ms)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(total_ms, op=dist.ReduceOp.MAX)
+    ms_per_step = total_ms.item() / args.steps
+    paths = scene.n_draws
+    value = world * paths / (ms_per_step / 1e3)
+    mpix = world * scene.width * scene.height / (ms_per_step / 1e3) / 1e6
+    last = stages[-1]
+
+    # end to end through the C ABI with host buffers (upload + render + readback)
+    e2e_ms = []
+    if not args.no_e2e:
+        ctx.render_streams([scene])  # warm
+        for _ in range(max(1, min(args.steps, 3))):
+            ctx.render_streams([scene])
+            e2e_ms.append(ctx.stats()["total_ms"])
+    e2e_ms_mean = statistics.mean(e2e_ms) if e2e_ms else None
+
+    # roofline of the dominant stage
+    stage_ms = {k: statistics.mean(s[k] for s in stages)
+                for k in ("geometry_ms", "sweep_count_ms", "sweep_emit_ms", "composite_ms", "blur_ms")}
+    dom = max(stage_ms, key=stage_ms.get)
+    peak, peak_kind = measured_peaks()
+    spans, frags, pixels, edges = last["spans"], last["fragments"], last["pixels"], last["edges"]
+    # algorithmic bytes per launch of each stage (measurement section)
+    alg = {
+        "composite_ms": spans * 8 + pixels * 4 * 2 + last["passes"] * 24,
+        "sweep_emit_ms": spans * 8 + edges * 84 * 2,
+        "sweep_count_ms": edges * 84 * 2,
+        "geometry_ms": edges * 84 * 2,
+        "blur_ms": 0,
+    }[dom]
+    achieved = alg / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32/f32",
+        "data": "synthetic (seeded, skity_gb300.scene.config2)",
+        "config": {"workload": WORKLOAD, "canvas": "2048x2048", "paths": paths,
+                   "l2": "flushed between steps (256 MiB device write)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "mpix_per_s": mpix,
+        "stage_ms": stage_ms,
+        "work": {"passes": last["passes"], "edges": edges, "spans": spans, "fragments": frags,
+                 "fragments_per_s": world * frags / (ms_per_step / 1e3)},
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stages)),
+        "clocks": clk,
+        "roofline": {"kernel": dom.replace("_ms", ""), "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else None,
+                     "peak_source": peak_kind, "traffic": None},
+        "e2e": {"value": (world * paths / (e2e_ms_mean / 1e3)) if e2e_ms_mean else None,
+                "unit": "paths/s", "h2d_bytes_per_step": len(scene.to_bytes()),
+                "d2h_bytes_per_step": scene.width * scene.height * 4,
+                "ms_per_step": e2e_ms_mean},
+        "wall_s": wall,
+    }
+    if rank == 0 and not args.no_cpu:
+        v, secs = cpu_baseline(scene, 1, args.cpu_sample_paths)
+        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": 1, "kind": "port",
+                                "sample": f"first {args.cpu_sample_paths} of {paths} paths, "
+                                          f"{secs[0]:.1f} s single-threaded"}
+    batch.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-sample-paths", type=int, default=400)
+    ap.add_argument("--ref-sample-paths", type=int, default=800)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    from skity_gb300 import build
+    build.build()
+    return run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

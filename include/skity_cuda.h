@@ -122,6 +122,14 @@ typedef struct skity_cuda_stats {
   uint64_t pixels;        /* canvas pixels written back */
   uint64_t kernel_launches;
   uint64_t retries;       /* scratch-capacity retries */
+  /* per-stage device time of the last render (CUDA events around each
+   * stage's launches on the context stream) */
+  double geometry_ms;     /* path -> quads -> stroke -> edges -> sort */
+  double sweep_count_ms;  /* AAA sweep, span counting */
+  double sweep_emit_ms;   /* AAA sweep, span writing */
+  double composite_ms;    /* span replay, shading, blending */
+  double blur_ms;         /* StackBlur of blur mask filter temp canvases */
+  uint64_t fragments;     /* sum of span lengths inside the canvases */
 } skity_cuda_stats;
 
 /* ---- context ------------------------------------------------------------ */

@@ -53,6 +53,10 @@ def lib() -> ctypes.CDLL:
         _lib.sko_render.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(Stats)]
         _lib.sko_render.restype = ctypes.c_int
+        _lib.sko_render_mt.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                       ctypes.POINTER(Stats)]
+        _lib.sko_render_mt.restype = ctypes.c_int
         _lib.sko_cubic_quad_count.argtypes = [ctypes.POINTER(ctypes.c_float)]
         _lib.sko_quad_edge.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]
         _lib.sko_path_spans.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
@@ -67,6 +71,18 @@ def render(scene, first: int = 0, count: int | None = None):
     out = np.zeros((scene.height, scene.width, 4), np.uint8)
     st = Stats()
     rc = lib().sko_render(b, len(b), first, count, out.ctypes.data, ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"oracle render failed ({rc})")
+    return out, st
+
+
+def render_mt(scene, threads: int, first: int = 0, count: int | None = None):
+    """render() on `threads` host threads (banded rows, identical pixels)."""
+    b = scene.to_bytes()
+    count = scene.n_draws if count is None else count
+    out = np.zeros((scene.height, scene.width, 4), np.uint8)
+    st = Stats()
+    rc = lib().sko_render_mt(b, len(b), first, count, out.ctypes.data, threads, ctypes.byref(st))
     if rc != 0:
         raise RuntimeError(f"oracle render failed ({rc})")
     return out, st

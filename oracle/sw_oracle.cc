@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "sw_oracle.h"
@@ -1453,6 +1454,7 @@ struct Brush {
 struct Target {
   uint8_t* px;
   int w, h;
+  int band0 = 0, band1 = 1 << 30;  // rows this target blends (banded replay)
   uint32_t Get(int x, int y) const {  // bitmap.cc:25-33 (RGBA)
     const uint8_t* c = px + ((size_t)y * w + x) * 4;
     return ColorSetARGB(c[3], c[0], c[1], c[2]);
@@ -1494,6 +1496,7 @@ static uint64_t BrushSpans(const std::vector<Span>& spans, const Brush& br, int 
   for (const Span& s : spans) {
     int x = s.x, y = s.y, len = s.len;
     if (y < 0 || y >= t->h) continue;
+    if (y < t->band0 || y >= t->band1) continue;
     if (x >= t->w || x + len < 0) continue;
     if (x < 0) {
       len += x;
@@ -1711,6 +1714,53 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
     stats->spans = st.spans;
     stats->edges = st.edges;
     stats->tie_groups = st.tie_groups;
+    stats->seconds = std::chrono::duration<double>(t1 - t0).count();
+    stats->draws = last > first ? last - first : 0;
+  }
+  return 0;
+}
+
+// Banded replay on `threads` host threads: every thread rasterises every
+// draw (the sweep is sequential per path) but blends only the spans of its
+// own band of rows.  Blending is per pixel and in draw order, so the result
+// equals the single-threaded replay; the brush work splits across threads.
+int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
+                  uint8_t* out_rgba, uint32_t threads, sko_stats* stats) {
+  using namespace sko;
+  SceneView s;
+  if (!ParseScene(scene, len, &s)) return -2;
+  if (threads == 0) threads = 1;
+  auto t0 = std::chrono::steady_clock::now();
+  uint32_t last = std::min<uint32_t>(s.nd, first + count);
+  std::vector<Stats> st(threads);
+  std::vector<std::thread> pool;
+  int h = (int)s.height;
+  for (uint32_t k = 0; k < threads; ++k) {
+    pool.emplace_back([&, k]() {
+      Target t{out_rgba, (int)s.width, (int)s.height};
+      t.band0 = (int)((int64_t)h * k / threads);
+      t.band1 = (int)((int64_t)h * (k + 1) / threads);
+      uint32_t c = s.has_clear ? ColorToPMColor(Color4fToColor(s.clear)) : 0;
+      for (int y = t.band0; y < t.band1; ++y)
+        for (int x = 0; x < t.w; ++x) t.Set(x, y, c);
+      std::vector<Span> spans;
+      for (uint32_t d = first; d < last; ++d) {
+        if (s.paints[d].blur_style != 0) {
+          HandleBlurFilter(s, d, &t, &st[k]);
+        } else {
+          DrawPath(s, d, &t, &st[k], &spans);
+        }
+      }
+    });
+  }
+  for (auto& th : pool) th.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    for (auto& x : st) stats->fragments += x.fragments;
+    stats->spans = st[0].spans;
+    stats->edges = st[0].edges;
+    stats->tie_groups = st[0].tie_groups;
     stats->seconds = std::chrono::duration<double>(t1 - t0).count();
     stats->draws = last > first ? last - first : 0;
   }

@@ -23,6 +23,10 @@ typedef struct sko_stats {
  * out_rgba (width*height*4 bytes). Returns 0, or -2 for a malformed stream. */
 int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
                uint8_t* out_rgba, sko_stats* stats);
+/* Same replay on `threads` host threads, each blending its own band of rows
+ * (identical output). */
+int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
+                  uint8_t* out_rgba, uint32_t threads, sko_stats* stats);
 /* Cubic::ToQuads quad count for one cubic (x0,y0,...,x3,y3). */
 int sko_cubic_quad_count(const float pts[8]);
 /* SWQuadEdge::SetQuad on a monotone quad: out = {1<<shift? no: shift,

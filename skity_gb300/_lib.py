@@ -57,7 +57,10 @@ class Stats_(ctypes.Structure):
                 ("draws", ctypes.c_uint64), ("passes", ctypes.c_uint64),
                 ("edges", ctypes.c_uint64), ("spans", ctypes.c_uint64),
                 ("pixels", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
-                ("retries", ctypes.c_uint64)]
+                ("retries", ctypes.c_uint64), ("geometry_ms", ctypes.c_double),
+                ("sweep_count_ms", ctypes.c_double), ("sweep_emit_ms", ctypes.c_double),
+                ("composite_ms", ctypes.c_double), ("blur_ms", ctypes.c_double),
+                ("fragments", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -32,22 +32,31 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
   return 1;
 }
 
-__global__ void __launch_bounds__(64) k_sweep_count(DevBatch b) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < b.n_passes) SweepCountPass(b, p);
+// one warp per pass: the sweep logic runs warp-uniformly, per-pixel work is
+// split across the lanes
+constexpr int kSweepWarps = 4;
+
+__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_count(DevBatch b) {
+  uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
+  Lanes L;
+  L.lane = threadIdx.x & 31;
+  if (p < b.n_passes) SweepCountPass(b, p, L);
 }
 
-__global__ void __launch_bounds__(64) k_sweep_emit(DevBatch b) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < b.n_passes) SweepEmitPass(b, p);
+__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_emit(DevBatch b) {
+  uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
+  Lanes L;
+  L.lane = threadIdx.x & 31;
+  if (p < b.n_passes) SweepEmitPass(b, p, L);
 }
 
 int LaunchSweep(const DevBatch& b, bool emit, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
+  unsigned grid = (b.n_passes + kSweepWarps - 1) / kSweepWarps;
   if (emit) {
-    k_sweep_emit<<<(b.n_passes + 63) / 64, 64, 0, stream>>>(b);
+    k_sweep_emit<<<grid, 32 * kSweepWarps, 0, stream>>>(b);
   } else {
-    k_sweep_count<<<(b.n_passes + 63) / 64, 64, 0, stream>>>(b);
+    k_sweep_count<<<grid, 32 * kSweepWarps, 0, stream>>>(b);
   }
   return 1;
 }

@@ -110,6 +110,7 @@ struct DevBatch {
   uint8_t* acc;
   uint32_t* rowtab;
   uint32_t* pass_spans;
+  unsigned long long* pass_frags;  // fragments (clipped span pixels) per pass
   const PassComp* comp;
   uint2* spans;
   const Brush* brushes;

@@ -165,27 +165,45 @@ SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
   return len > 0;
 }
 
+// Sinks are called warp-uniformly; global writes are made by the leader
+// lane, per-pixel spans are compacted with a ballot.
 struct CountSink {
   uint32_t* rows;
   int row0, row1, W, H;
   uint32_t ga;
   bool srcover;
+  unsigned long long frags;
   SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
     if (y < row0 || y >= row1) return false;
     if (!ClipSpan(x, y, len, W, H)) return false;
     return !(srcover && (a & ga) == 0);
   }
-  SKC_HD void real(int x, int y, int len, uint8_t a) {
-    if (keep(x, y, len, a)) rows[y - row0]++;
+  SKC_HD void real(const Lanes& L, int x, int y, int len, uint8_t a) {
+    if (keep(x, y, len, a)) {
+      if (L.leader()) rows[y - row0]++;
+      frags += (unsigned)len;
+    }
   }
-  SKC_HD void acc_row(int y, const uint8_t* acc, int left, int lo, int hi) {
+  SKC_HD void pixels(const Lanes& L, int x0, int y, uint8_t a, bool valid) {
+    int x = x0 + L.lane, len = 1;
+    unsigned m = L.ballot(valid && keep(x, y, len, a));
+    int n = Lanes::popc(m);
+    if (n) {
+      if (L.leader()) rows[y - row0] += (uint32_t)n;
+      frags += (unsigned)n;
+    }
+  }
+  SKC_HD void acc_row(const Lanes& L, int y, const uint8_t* acc, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return;
     uint32_t n = 0;
-    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
-      if (keep(x, y, len, a)) n++;
+      if (keep(x, y, len, a)) {
+        n++;
+        frags += (unsigned)len;
+      }
     });
-    rows[y - row0] += n;
+    if (n && L.leader()) rows[y - row0] += n;
   }
 };
 
@@ -202,34 +220,51 @@ struct EmitSink {
     if (!ClipSpan(x, y, len, W, H)) return false;
     return !(srcover && (a & ga) == 0);
   }
-  SKC_HD void real(int x, int y, int len, uint8_t a) {
-    if (!keep(x, y, len, a)) return;
+  SKC_HD void seek(int y) {
     if (y != cur_row) {
       cur_row = y;
       cur = rows[y - row0];
     }
-    spans[cur++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+  }
+  SKC_HD void real(const Lanes& L, int x, int y, int len, uint8_t a) {
+    if (!keep(x, y, len, a)) return;
+    seek(y);
+    if (L.leader()) spans[cur] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+    cur++;
+  }
+  SKC_HD void pixels(const Lanes& L, int x0, int y, uint8_t a, bool valid) {
+    int x = x0 + L.lane, len = 1;
+    bool k = valid && keep(x, y, len, a);
+    unsigned m = L.ballot(k);
+    if (!m) return;
+    seek(y);
+    if (k) spans[cur + Lanes::popc(m & L.lt_mask())] = make_uint2((uint32_t)x | (1u << 16), a);
+    cur += (uint32_t)Lanes::popc(m);
   }
   // The accumulated spans of a row follow its direct spans (the reference
   // flushes a row's accumulator only after leaving the row), so they fill
   // the tail of the row's slot.
-  SKC_HD void acc_row(int y, const uint8_t* acc, int left, int lo, int hi) {
+  SKC_HD void acc_row(const Lanes& L, int y, const uint8_t* acc, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return;
     uint32_t n = 0;
-    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) n++;
     });
     uint32_t o = rows[y - row0 + 1] - n;
-    acc_runs(acc, lo, hi, [&](int s, int w, uint8_t a) {
+    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
-      if (keep(x, y, len, a)) spans[o++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+      if (keep(x, y, len, a)) {
+        if (L.leader()) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        o++;
+      }
     });
   }
 };
 
 template <typename Sink>
-SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink) {
+SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink,
+                      const Lanes& lanes) {
   const PassDesc pd = b.passes[p];
   const PassSweep sw = b.sweep[p];
   SliceLayout L;
@@ -237,8 +272,10 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   const Edge* S = (const Edge*)(b.scratch + pd.slice_off + L.off[13]);
   Edge* W = b.work + sw.work_off;
   int n = g.n_edges;
-  for (int i = 0; i < n + 2; ++i) W[i] = S[i];
+  for (int i = lanes.lane; i < n + 2; i += Lanes::n) W[i] = S[i];
+  lanes.sync();
   Sweep<Sink> s;
+  s.L = lanes;
   s.E = W;
   s.head = n;
   s.tail = n + 1;
@@ -254,11 +291,12 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   s.flush_acc();
 }
 
-SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p) {
+SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   const PassGeom g = b.geom[p];
   const PassSweep sw = b.sweep[p];
   uint32_t* rows = b.rowtab + sw.rbase;
   int nrows = g.row1 - g.row0;
+  unsigned long long frags = 0;
   if (g.n_edges > 0 && nrows > 0) {
     const PassDesc pd = b.passes[p];
     const CanvasDesc cd = b.canvases[pd.canvas];
@@ -270,8 +308,13 @@ SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p) {
     sink.H = (int)cd.h;
     sink.ga = pd.ga;
     sink.srcover = (pd.flags & kPassSrcOver) != 0;
-    RunSweep(b, p, g, &sink);
+    sink.frags = 0;
+    RunSweep(b, p, g, &sink, lanes);
+    frags = sink.frags;
   }
+  lanes.sync();
+  if (!lanes.leader()) return;
+  if (b.pass_frags) b.pass_frags[p] = frags;
   uint32_t run = 0;
   for (int r = 0; r < nrows; ++r) {
     uint32_t c = rows[r];
@@ -282,7 +325,7 @@ SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p) {
   b.pass_spans[p] = run;
 }
 
-SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p) {
+SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   const PassGeom g = b.geom[p];
   int nrows = g.row1 - g.row0;
   if (g.n_edges == 0 || nrows <= 0) return;
@@ -300,7 +343,7 @@ SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p) {
   sink.srcover = (pd.flags & kPassSrcOver) != 0;
   sink.cur_row = -1;
   sink.cur = 0;
-  RunSweep(b, p, g, &sink);
+  RunSweep(b, p, g, &sink, lanes);
 }
 
 

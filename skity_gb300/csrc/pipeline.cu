@@ -68,7 +68,7 @@ struct DeviceBatch {
   HostBatch hb;
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
   DevBuf scratch, geom, sweep, work, acc, rowtab, pass_spans, comp, spans, pixels;
-  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip;
+  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
   uint32_t chunk = 1024;
   bool uploaded = false;
@@ -83,6 +83,7 @@ struct skity_cuda_context_s {
   uint64_t budget = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t stage[10] = {};
   skity_cuda_stats last{};
   std::mutex mu;
 };
@@ -182,7 +183,9 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
     b.geom = db.geom.as<PassGeom>();
     b.pass_list = db.pass_list.as<uint32_t>();
     b.n_list = (uint32_t)todo.size();
+    SKC_TRY(cudaEventRecord(ctx->stage[0], s));
     st.kernel_launches += LaunchGeometry(b, s);
+    SKC_TRY(cudaEventRecord(ctx->stage[1], s));
     SKC_TRY(cudaGetLastError());
     SKC_TRY(cudaMemcpyAsync(db.h_geom.data(), db.geom.p, np * sizeof(PassGeom),
                             cudaMemcpyDeviceToHost, s));
@@ -214,6 +217,7 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   SKC_TRY(db.rowtab.ensure(std::max<uint64_t>(rows, 1) * 4));
   SKC_TRY(cudaMemsetAsync(db.rowtab.p, 0, std::max<uint64_t>(rows, 1) * 4, s));
   SKC_TRY(db.pass_spans.ensure(std::max<size_t>(np, 1) * 4));
+  SKC_TRY(db.pass_frags.ensure(std::max<size_t>(np, 1) * 8));
 
   DevBatch b{};
   b.verbs = db.verbs.as<uint8_t>();
@@ -230,21 +234,29 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.acc = db.acc.as<uint8_t>();
   b.rowtab = db.rowtab.as<uint32_t>();
   b.pass_spans = db.pass_spans.as<uint32_t>();
+  b.pass_frags = db.pass_frags.as<unsigned long long>();
+  SKC_TRY(cudaEventRecord(ctx->stage[2], s));
   st.kernel_launches += LaunchSweep(b, false, s);
+  SKC_TRY(cudaEventRecord(ctx->stage[3], s));
   SKC_TRY(cudaGetLastError());
   std::vector<uint32_t> pspans(np);
+  std::vector<unsigned long long> pfrags(np);
   if (np) {
     SKC_TRY(cudaMemcpyAsync(pspans.data(), db.pass_spans.p, np * 4, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaMemcpyAsync(pfrags.data(), db.pass_frags.p, np * 8, cudaMemcpyDeviceToHost, s));
   }
   SKC_TRY(cudaStreamSynchronize(s));
   std::vector<PassComp> comp;
   uint64_t spans = PlanComp(hb, db.h_geom, sw, pspans, comp);
   st.spans = spans;
+  for (uint32_t p = 0; p < np; ++p) st.fragments += pfrags[p];
   SKC_TRY(Upload(db.comp, comp, s));
   SKC_TRY(db.spans.ensure(std::max<uint64_t>(spans, 1) * sizeof(uint2)));
   b.comp = db.comp.as<PassComp>();
   b.spans = db.spans.as<uint2>();
+  SKC_TRY(cudaEventRecord(ctx->stage[4], s));
   st.kernel_launches += LaunchSweep(b, true, s);
+  SKC_TRY(cudaEventRecord(ctx->stage[5], s));
   SKC_TRY(cudaGetLastError());
 
   // ---- composite temp canvases, blur, composite main canvases
@@ -253,14 +265,20 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.stop_offsets = db.stop_offsets.as<float>();
   b.pixels = db.pixels.as<uint8_t>();
   b.roundtrip = db.roundtrip.as<uint8_t>();
+  SKC_TRY(cudaEventRecord(ctx->stage[6], s));
   if (!db.h_tasks_temp.empty()) {
     st.kernel_launches += LaunchComposite(b, db.tasks_temp.as<RowTask>(),
                                           (uint32_t)db.h_tasks_temp.size(), db.chunk, s);
+  }
+  SKC_TRY(cudaEventRecord(ctx->stage[7], s));
+  if (!db.h_tasks_temp.empty()) {
     st.kernel_launches += LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
                                      hb.max_temp_h, hb.max_temp_w, s);
   }
+  SKC_TRY(cudaEventRecord(ctx->stage[8], s));
   st.kernel_launches += LaunchComposite(b, db.tasks_main.as<RowTask>(),
                                         (uint32_t)db.h_tasks_main.size(), db.chunk, s);
+  SKC_TRY(cudaEventRecord(ctx->stage[9], s));
   SKC_TRY(cudaGetLastError());
   if (timed) SKC_TRY(cudaEventRecord(ctx->ev1, s));
   SKC_TRY(cudaStreamSynchronize(s));
@@ -268,6 +286,18 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     st.device_ms = ms;
+  }
+  {
+    auto el = [&](int a, int b2) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ctx->stage[a], ctx->stage[b2]);
+      return (double)ms;
+    };
+    st.geometry_ms = el(0, 1);
+    st.sweep_count_ms = el(2, 3);
+    st.sweep_emit_ms = el(4, 5);
+    st.composite_ms = el(6, 7) + el(8, 9);
+    st.blur_ms = el(7, 8);
   }
   for (uint32_t c : hb.main_canvases) st.pixels += (uint64_t)hb.canvases[c].w * hb.canvases[c].h;
   db.stats = st;
@@ -354,6 +384,12 @@ SKITY_CUDA_API int32_t skity_cuda_context_create(const skity_cuda_context_create
     delete c;
     return SKITY_CUDA_ERROR_INITIALIZATION_FAILED;
   }
+  for (auto& e : c->stage) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      delete c;
+      return SKITY_CUDA_ERROR_INITIALIZATION_FAILED;
+    }
+  }
   *out = c;
   return SKITY_CUDA_SUCCESS;
 }
@@ -364,6 +400,7 @@ SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  for (auto& e : ctx->stage) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -468,6 +468,64 @@ SKC_HDN void introsort(int32_t* a, int n, Less less) {
 }
 
 // ---------------------------------------------------------------------------
+// Execution width of a sweep: a whole warp on the GPU (the sequential sweep
+// logic runs warp-uniformly -- every lane computes the same values -- and the
+// per-pixel loops are split across lanes), one thread on the CPU.
+// ---------------------------------------------------------------------------
+struct Lanes {
+#ifdef __CUDA_ARCH__
+  static constexpr int n = 32;
+  int lane;
+  __device__ unsigned ballot(bool p) const { return __ballot_sync(0xffffffffu, p); }
+  __device__ void sync() const { __syncwarp(); }
+  __device__ uint32_t shfl(uint32_t v, int src) const { return __shfl_sync(0xffffffffu, v, src); }
+  __device__ unsigned lt_mask() const { return (1u << lane) - 1u; }
+  __device__ static int popc(unsigned m) { return __popc(m); }
+  __device__ static int ffs(unsigned m) { return __ffs((int)m); }
+#else
+  static constexpr int n = 1;
+  int lane = 0;
+  unsigned ballot(bool p) const { return p ? 1u : 0u; }
+  void sync() const {}
+  uint32_t shfl(uint32_t v, int) const { return v; }
+  unsigned lt_mask() const { return 0u; }
+  static int popc(unsigned m) { return __builtin_popcount(m); }
+  static int ffs(unsigned m) { return __builtin_ffs((int)m); }
+#endif
+  SKC_HD bool leader() const { return lane == 0; }
+};
+
+// Runs of equal nonzero alphas in acc[lo, hi), in increasing x
+// (SpanBuilder::Flush, sw_raster.cc:103-136); emit(start, width, alpha) is
+// called warp-uniformly, one call per run.
+template <typename F>
+SKC_HD void acc_runs_lanes(const Lanes& L, const uint8_t* acc, int lo, int hi, F&& emit) {
+  int open_start = -1;
+  uint8_t open_v = 0;
+  for (int base = lo; base < hi; base += Lanes::n) {
+    int i = base + L.lane;
+    uint8_t v = i < hi ? acc[i] : 0;
+    uint8_t pv = (i > lo && i < hi) ? acc[i - 1] : 0;
+    unsigned mask = L.ballot(i < hi && v != pv);
+    while (mask) {
+      int bit = Lanes::ffs(mask) - 1;
+      mask &= mask - 1;
+      int pos = base + bit;
+      uint8_t bv = (uint8_t)L.shfl(v, bit);
+      if (open_start >= 0) {
+        emit(open_start, pos - open_start, open_v);
+        open_start = -1;
+      }
+      if (bv != 0) {
+        open_start = pos;
+        open_v = bv;
+      }
+    }
+  }
+  if (open_start >= 0) emit(open_start, hi - open_start, open_v);
+}
+
+// ---------------------------------------------------------------------------
 // AAA scanline sweep (sw_raster.cc:19-677) with a span sink
 // ---------------------------------------------------------------------------
 // Sink interface (Sink::real(x, y, len, alpha), Sink::acc_row(y, alphas,
@@ -492,6 +550,7 @@ SKC_HD uint8_t partial_triangle_to_alpha(Fixed a, Fixed b) {
 
 template <typename Sink>
 struct Sweep {
+  Lanes L;
   Edge* E;
   int head, tail;
   Sink* sink;
@@ -505,17 +564,15 @@ struct Sweep {
 
   SKC_HD void real(int x, int y, int len, uint8_t a) {
     if (y < scan_top) return;
-    sink->real(x, y, len, a);
-  }
-  SKC_HD void real_spans(int x, int y, const uint8_t* aa, int len) {
-    if (y < scan_top) return;
-    for (int i = 0; i < len; i++) sink->real(x + i, y, 1, aa[i]);
+    sink->real(L, x, y, len, a);
   }
   SKC_HD void flush_acc() {
     if (acc_y == kNaN32) return;
     if (touch_lo <= touch_hi) {
-      sink->acc_row(acc_y, acc, acc_left, touch_lo, touch_hi + 1);
-      for (int i = touch_lo; i <= touch_hi; ++i) acc[i] = 0;
+      sink->acc_row(L, acc_y, acc, acc_left, touch_lo, touch_hi + 1);
+      L.sync();
+      for (int i = touch_lo + L.lane; i <= touch_hi; i += Lanes::n) acc[i] = 0;
+      L.sync();
     }
     touch_lo = 0x7fffffff;
     touch_hi = -1;
@@ -532,31 +589,39 @@ struct Sweep {
   SKC_HD static uint8_t sat_add(uint8_t a, uint8_t d) {
     return (uint16_t)a + (uint16_t)d > 255 ? 255 : (uint8_t)(a + d);
   }
+  SKC_HD void touch(int o0, int o1) {  // [o0, o1) clipped to the row buffer
+    o0 = max_(o0, 0);
+    o1 = min_(o1, acc_width);
+    if (o0 < o1) {
+      touch_lo = min_(touch_lo, o0);
+      touch_hi = max_(touch_hi, o1 - 1);
+    }
+  }
   SKC_HD void acc_add(int x, int y, int width, uint8_t a) {
     if (y < scan_top) return;
     flush_if_need(y);
     int off = x - acc_left;
-    for (int i = 0; i < width; i++) {
+    for (int i = L.lane; i < width; i += Lanes::n) {
       int o = off + i;
-      if ((unsigned)o < (unsigned)acc_width) {
-        acc[o] = sat_add(acc[o], a);
-        touch_lo = min_(touch_lo, o);
-        touch_hi = max_(touch_hi, o);
-      }
+      if ((unsigned)o < (unsigned)acc_width) acc[o] = sat_add(acc[o], a);
     }
+    L.sync();
+    touch(off, off + width);
   }
-  SKC_HD void acc_spans(int x, int y, const uint8_t* aa, int len) {
+  // One alpha per lane for pixels x0 + lane (lanes with valid == false
+  // carry nothing): per-pixel spans (RealSpanBuilder::BuildSpans) or
+  // accumulation (SpanBuilder::BuildSpans).
+  SKC_HD void pixels(bool real_spans, int x0, int y, uint8_t a, bool valid, int count) {
     if (y < scan_top) return;
-    flush_if_need(y);
-    int off = x - acc_left;
-    for (int i = 0; i < len; i++) {
-      int o = off + i;
-      if ((unsigned)o < (unsigned)acc_width) {
-        acc[o] = sat_add(acc[o], aa[i]);
-        touch_lo = min_(touch_lo, o);
-        touch_hi = max_(touch_hi, o);
-      }
+    if (real_spans) {
+      sink->pixels(L, x0, y, a, valid);
+      return;
     }
+    flush_if_need(y);
+    int o = x0 - acc_left + L.lane;
+    if (valid && (unsigned)o < (unsigned)acc_width) acc[o] = sat_add(acc[o], a);
+    L.sync();
+    touch(x0 - acc_left, x0 - acc_left + count);
   }
 
   SKC_HD void blit_single(int y, int x, uint8_t alpha, uint8_t full, bool no_real) {
@@ -576,54 +641,15 @@ struct Sweep {
     if (full == 0xFF && !no_real) real(x, y, len, full);
     else acc_add(x, y, len, full);
   }
-  SKC_HD static void alpha_above(uint8_t* alphas, Fixed l, Fixed r, Fixed dY, uint8_t full) {
-    int R = FixedCeilToInt(r);
-    if (R == 0) return;
-    if (R == 1) {
-      alphas[0] = partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
-      return;
-    }
-    Fixed first = kFixed1 - l;
-    Fixed last = r - ((R - 1) << 16);
-    Fixed firstH = FixedMul(first, dY);
-    alphas[0] = (uint8_t)(FixedMul(first, firstH) >> 9);
-    Fixed alpha16 = wadd(firstH, dY >> 1);
-    for (int i = 1; i < R - 1; ++i) {
-      alphas[i] = (uint8_t)(alpha16 >> 8);
-      alpha16 = wadd(alpha16, dY);
-    }
-    alphas[R - 1] = (uint8_t)(full - partial_triangle_to_alpha(last, dY));
-  }
-  SKC_HD static void alpha_below(uint8_t* alphas, Fixed l, Fixed r, Fixed dY, uint8_t full) {
-    int R = FixedCeilToInt(r);
-    if (R == 0) return;
-    if (R == 1) {
-      alphas[0] = partial_alpha_a(trapezoid_to_alpha(l, r), full);
-      return;
-    }
-    Fixed first = kFixed1 - l;
-    Fixed last = r - ((R - 1) << 16);
-    Fixed lastH = FixedMul(last, dY);
-    alphas[R - 1] = (uint8_t)(FixedMul(last, lastH) >> 9);
-    Fixed alpha16 = wadd(lastH, dY >> 1);
-    for (int i = R - 2; i > 0; i--) {
-      alphas[i] = (uint8_t)((alpha16 >> 8) & 0xFF);
-      alpha16 = wadd(alpha16, dY);
-    }
-    alphas[0] = (uint8_t)(full - partial_triangle_to_alpha(first, dY));
-  }
-
-  // blit_aaa_trapezoid_row (sw_raster.cc:372-455).  The per-pixel alpha
-  // arrays live in thread-local scratch: wider rows are processed in
-  // windows of kWin pixels (the alphas of one pixel depend only on that
-  // pixel's index), so any width fits.
-  static constexpr int kWin = 64;
+  // blit_aaa_trapezoid_row (sw_raster.cc:372-455).  Lane l computes pixel
+  // L + w0 + l of each window of Lanes::n pixels; every pixel's alpha depends
+  // only on its index (the running sums are re-derived per pixel).
   SKC_HDN void aaa_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
                        uint8_t full, bool no_real) {
-    int L = FixedFloorToInt(ul), R = FixedCeilToInt(lr);
-    int len = R - L;
+    int L0 = FixedFloorToInt(ul), R = FixedCeilToInt(lr);
+    int len = R - L0;
     if (len == 1) {
-      blit_single(y, L, trapezoid_to_alpha(ur - ul, lr - ll), full, no_real);
+      blit_single(y, L0, trapezoid_to_alpha(ur - ul, lr - ll), full, no_real);
       return;
     }
     int uL = FixedFloorToInt(ul), lL = FixedCeilToInt(ll);
@@ -642,100 +668,55 @@ struct Sweep {
       ra1 = partial_triangle_to_alpha(first, rDY);
       ra2 = (uint8_t)(full - partial_triangle_to_alpha(second, rDY));
     }
-    // full-width temp arrays computed on demand (left/right triangles can
-    // be wider than a window, so they are recomputed per window)
-    uint8_t alphas[kWin];
-    uint8_t templ[kWin + 1], tempr[kWin + 1];
-    for (int w0 = 0; w0 < len; w0 += kWin) {
-      int wn = min_(kWin, len - w0);
-      for (int i = 0; i < wn; ++i) alphas[i] = full;
-      // left edge (pixels uL .. lL-1)
-      if (two_left) {
-        if (w0 == 0) {
-          alphas[0] = alphas[0] > la1 ? (uint8_t)(alphas[0] - la1) : 0;
-          if (wn > 1) alphas[1] = alphas[1] > la2 ? (uint8_t)(alphas[1] - la2) : 0;
-        } else if (w0 == 1) {
-          alphas[0] = alphas[0] > la2 ? (uint8_t)(alphas[0] - la2) : 0;
+    const bool real_spans = full == 0xFF && !no_real;
+    for (int w0 = 0; w0 < len; w0 += Lanes::n) {
+      int i = w0 + L.lane;  // pixel L0 + i
+      bool valid = i < len;
+      uint8_t a = full;
+      if (valid) {
+        int px = L0 + i;
+        if (two_left) {
+          if (i == 0) a = a > la1 ? (uint8_t)(a - la1) : 0;
+          if (i == 1) a = a > la2 ? (uint8_t)(a - la2) : 0;
+        } else if (px >= uL && px < lL) {
+          uint8_t t = triangle_entry(true, ul - IntToFixed(uL), ll - IntToFixed(uL), lDY, full,
+                                     px - uL);
+          a = a > t ? (uint8_t)(a - t) : 0;
         }
-      } else if (lL > uL) {
-        int a0 = max_(uL, L + w0), a1 = min_(lL, L + w0 + wn);
-        if (a0 < a1) {
-          triangle_window(templ, true, ul - IntToFixed(uL), ll - IntToFixed(uL), lDY, full,
-                          a0 - uL, a1 - uL);
-          for (int i = a0; i < a1; ++i) {
-            uint8_t t = templ[i - a0];
-            uint8_t& d = alphas[i - L - w0];
-            d = d > t ? (uint8_t)(d - t) : 0;
-          }
+        if (two_right) {
+          if (i == len - 2) a = a > ra1 ? (uint8_t)(a - ra1) : 0;
+          if (i == len - 1) a = a > ra2 ? (uint8_t)(a - ra2) : 0;
+        } else if (px >= uR && px < lR) {
+          uint8_t t = triangle_entry(false, ur - IntToFixed(uR), lr - IntToFixed(uR), rDY, full,
+                                     px - uR);
+          a = a > t ? (uint8_t)(a - t) : 0;
         }
       }
-      // right edge (pixels uR .. lR-1)
-      if (two_right) {
-        int p0 = len - 2 - w0, p1 = len - 1 - w0;
-        if (p0 >= 0 && p0 < wn) alphas[p0] = alphas[p0] > ra1 ? (uint8_t)(alphas[p0] - ra1) : 0;
-        if (p1 >= 0 && p1 < wn) alphas[p1] = alphas[p1] > ra2 ? (uint8_t)(alphas[p1] - ra2) : 0;
-      } else if (lR > uR) {
-        int a0 = max_(uR, L + w0), a1 = min_(lR, L + w0 + wn);
-        if (a0 < a1) {
-          triangle_window(tempr, false, ur - IntToFixed(uR), lr - IntToFixed(uR), rDY, full,
-                          a0 - uR, a1 - uR);
-          for (int i = a0; i < a1; ++i) {
-            uint8_t t = tempr[i - a0];
-            uint8_t& d = alphas[i - L - w0];
-            d = d > t ? (uint8_t)(d - t) : 0;
-          }
-        }
-      }
-      if (full == 0xFF && !no_real) real_spans(L + w0, y, alphas, wn);
-      else acc_spans(L + w0, y, alphas, wn);
+      pixels(real_spans, L0 + w0, y, a, valid, min_(Lanes::n, len - w0));
     }
   }
-  // Entries [i0, i1) of compute_alpha_below_line (below = true) or
-  // compute_alpha_above_line over R = ceil(r) pixels, into out[0 .. i1-i0).
-  // Entry i of the reference's array depends only on i (and the running sum
-  // alpha16, re-derived here), so windows reproduce it exactly.
-  SKC_HD static void triangle_window(uint8_t* out, bool below, Fixed l, Fixed r, Fixed dY,
-                                     uint8_t full, int i0, int i1) {
+  // Entry i of compute_alpha_below_line (below = true) or
+  // compute_alpha_above_line (sw_raster.cc:314-370) over R = ceil(r) pixels.
+  SKC_HD static uint8_t triangle_entry(bool below, Fixed l, Fixed r, Fixed dY, uint8_t full, int i) {
     int R = FixedCeilToInt(r);
-    if (R <= 0) return;
     if (R == 1) {
-      uint8_t v = below ? partial_alpha_a(trapezoid_to_alpha(l, r), full)
-                        : partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
-      if (i0 <= 0 && 0 < i1) out[0 - i0] = v;
-      return;
+      return below ? partial_alpha_a(trapezoid_to_alpha(l, r), full)
+                   : partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
     }
     Fixed first = kFixed1 - l;
     Fixed last = r - ((R - 1) << 16);
     if (below) {
       Fixed lastH = FixedMul(last, dY);
-      for (int i = i0; i < i1; ++i) {
-        uint8_t v;
-        if (i == R - 1) {
-          v = (uint8_t)(FixedMul(last, lastH) >> 9);
-        } else if (i == 0) {
-          v = (uint8_t)(full - partial_triangle_to_alpha(first, dY));
-        } else {
-          // alpha16 after (R - 2 - i) additions of dY to lastH + dY/2
-          Fixed a16 = wadd(wadd(lastH, dY >> 1), wmul(R - 2 - i, dY));
-          v = (uint8_t)((a16 >> 8) & 0xFF);
-        }
-        out[i - i0] = v;
-      }
-    } else {
-      Fixed firstH = FixedMul(first, dY);
-      for (int i = i0; i < i1; ++i) {
-        uint8_t v;
-        if (i == 0) {
-          v = (uint8_t)(FixedMul(first, firstH) >> 9);
-        } else if (i == R - 1) {
-          v = (uint8_t)(full - partial_triangle_to_alpha(last, dY));
-        } else {
-          Fixed a16 = wadd(wadd(firstH, dY >> 1), wmul(i - 1, dY));
-          v = (uint8_t)(a16 >> 8);
-        }
-        out[i - i0] = v;
-      }
+      if (i == R - 1) return (uint8_t)(FixedMul(last, lastH) >> 9);
+      if (i == 0) return (uint8_t)(full - partial_triangle_to_alpha(first, dY));
+      Fixed a16 = wadd(wadd(lastH, dY >> 1), wmul(R - 2 - i, dY));
+      return (uint8_t)((a16 >> 8) & 0xFF);
     }
+    Fixed firstH = FixedMul(first, dY);
+    if (i == 0) return (uint8_t)(FixedMul(first, firstH) >> 9);
+    if (i == R - 1) return (uint8_t)(full - partial_triangle_to_alpha(last, dY));
+    Fixed a16 = wadd(wadd(firstH, dY >> 1), wmul(i - 1, dY));
+    return (uint8_t)(a16 >> 8);
   }
 
   SKC_HDN void trapezoid_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
@@ -955,30 +936,5 @@ struct Sweep {
     }
   }
 };
-
-// The flushed accumulator row as RLE spans (SpanBuilder::Flush,
-// sw_raster.cc:103-136): runs of equal nonzero alphas.
-template <typename F>
-SKC_HD void acc_runs(const uint8_t* acc, int lo, int hi, F&& emit) {
-  int curr = lo;
-  while (curr < hi) {
-    uint8_t a = acc[curr];
-    if (a > 0) {
-      int start = curr, width = 1;
-      for (;;) {
-        curr++;
-        if (curr >= hi) break;
-        if (acc[curr] == a) {
-          width++;
-        } else {
-          break;
-        }
-      }
-      emit(start, width, a);
-    } else {
-      curr++;
-    }
-  }
-}
 
 }  // namespace skc

@@ -77,13 +77,14 @@ extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rg
   b.acc = acc.data();
   b.rowtab = rowtab.data();
   b.pass_spans = pass_spans.data();
-  for (uint32_t p = 0; p < np; ++p) SweepCountPass(b, p);
+  Lanes lanes;
+  for (uint32_t p = 0; p < np; ++p) SweepCountPass(b, p, lanes);
   std::vector<PassComp> comp;
   uint64_t spans = PlanComp(hb, geom, sw, pass_spans, comp);
   std::vector<uint2> span_buf(spans + 1);
   b.comp = comp.data();
   b.spans = span_buf.data();
-  for (uint32_t p = 0; p < np; ++p) SweepEmitPass(b, p);
+  for (uint32_t p = 0; p < np; ++p) SweepEmitPass(b, p, lanes);
   b.brushes = hb.brushes.data();
   b.stop_colors = hb.stop_colors.data();
   b.stop_offsets = hb.stop_offsets.data();
