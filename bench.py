@@ -170,6 +170,8 @@ def run_gpu(args, rank, world, local):
     from skity_gb300.canvas import Batch, Context
 
     scene = load_scene()
+    if args.paths:
+        scene = scene.subset(0, args.paths)
     ctx = Context(local)
     batch = Batch(ctx, [scene])
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -272,6 +274,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-sample-paths", type=int, default=400)
     ap.add_argument("--ref-sample-paths", type=int, default=800)
+    ap.add_argument("--paths", type=int, default=0,
+                    help="render only the first N paths of the scene (small profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

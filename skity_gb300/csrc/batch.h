@@ -18,6 +18,7 @@
 #include "../../include/skity_cuda.h"
 #include "kernels.cuh"
 #include "stroke.cuh"
+#include "sweep.cuh"
 
 namespace skc {
 
@@ -506,22 +507,22 @@ inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv
 
 // Per-pass sweep buffers and row tables from the geometry results.
 struct SweepPlan {
-  uint64_t work_edges = 0, acc_bytes = 0, rows = 0, edges = 0;
+  uint64_t sweep_bytes = 0, rows = 0, edges = 0;
 };
 inline SweepPlan PlanSweep(const std::vector<PassGeom>& geom, std::vector<PassSweep>& sw) {
   SweepPlan pl;
   sw.assign(geom.size(), PassSweep{});
   for (size_t p = 0; p < geom.size(); ++p) {
     const PassGeom& g = geom[p];
-    sw[p].work_off = pl.work_edges;
-    sw[p].acc_off = pl.acc_bytes;
+    sw[p].work_off = pl.sweep_bytes;
     sw[p].rbase = (uint32_t)pl.rows;
-    if (g.n_edges > 0) {
-      pl.work_edges += (uint64_t)g.n_edges + 2;
-      pl.acc_bytes += (uint64_t)std::max(g.acc_width, 0);
-      pl.acc_bytes = (pl.acc_bytes + 15) & ~uint64_t(15);
-      pl.edges += (uint64_t)g.n_edges;
+    if (g.n_edges > 0 && g.row1 > g.row0) {
+      uint64_t b = SweepMemBytes(g.n_edges, std::max(g.acc_width, 0));
+      b = (b + 255) & ~uint64_t(255);
+      sw[p].bytes = b;
+      pl.sweep_bytes += b;
     }
+    if (g.n_edges > 0) pl.edges += (uint64_t)g.n_edges;
     int nr = g.row1 - g.row0;
     if (nr > 0) pl.rows += (uint64_t)nr + 1;
   }

@@ -77,8 +77,8 @@ struct PassGeom {
 };
 
 struct PassSweep {      // per-pass sweep buffers, set after geometry
-  uint64_t work_off;    // edge working copy (element offset, n_edges + 2)
-  uint64_t acc_off;     // accumulator row (byte offset)
+  uint64_t work_off;    // byte offset of the pass's sweep memory
+  uint64_t bytes;       // its size
   uint32_t rbase;       // row table base (rows + 1 entries)
   uint32_t pad;
 };
@@ -106,10 +106,10 @@ struct DevBatch {
   uint8_t* scratch;
   PassGeom* geom;
   const PassSweep* sweep;
-  Edge* work;
-  uint8_t* acc;
+  uint8_t* sweepmem;   // per-pass sweep memory (SweepMemAt)
   uint32_t* rowtab;
   uint32_t* pass_spans;
+  uint32_t* err;       // nonzero: a device self-check tripped (see pipeline)
   unsigned long long* pass_frags;  // fragments (clipped span pixels) per pass
   const PassComp* comp;
   uint2* spans;

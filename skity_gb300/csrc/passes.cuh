@@ -4,6 +4,7 @@
 #pragma once
 #include "kernels.cuh"
 #include "stroke.cuh"
+#include "sweep.cuh"
 
 namespace skc {
 
@@ -165,38 +166,35 @@ SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
   return len > 0;
 }
 
-// Sinks are called warp-uniformly; global writes are made by the leader
-// lane, per-pixel spans are compacted with a ballot.
-struct CountSink {
-  uint32_t* rows;
+// Span sinks of the lane-parallel sweep.  keep() applies the clipping of
+// SWSpanBrush::Brush and drops spans whose alpha & global alpha is 0 under
+// src-over (they blend to nothing); counts and offsets are per canvas row.
+struct SinkBase {
   int row0, row1, W, H;
   uint32_t ga;
   bool srcover;
-  unsigned long long frags;
   SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
     if (y < row0 || y >= row1) return false;
     if (!ClipSpan(x, y, len, W, H)) return false;
     return !(srcover && (a & ga) == 0);
   }
-  SKC_HD void real(const Lanes& L, int x, int y, int len, uint8_t a) {
-    if (keep(x, y, len, a)) {
-      if (L.leader()) rows[y - row0]++;
-      frags += (unsigned)len;
-    }
+};
+
+struct CountSink : SinkBase {
+  static constexpr bool kEmit = false;
+  uint32_t* rows;
+  unsigned long long frags;
+  SKC_HD uint32_t row_cursor(int) { return 0; }
+  SKC_HD uint2* span_ptr(uint32_t) { return nullptr; }
+  SKC_HD bool in_range(uint32_t, uint32_t) { return true; }
+  SKC_HD void step_done(const Lanes& L, int y, uint32_t n, unsigned long long f) {
+    if (n && y >= row0 && y < row1 && L.leader()) rows[y - row0] += n;
+    frags += f;
   }
-  SKC_HD void pixels(const Lanes& L, int x0, int y, uint8_t a, bool valid) {
-    int x = x0 + L.lane, len = 1;
-    unsigned m = L.ballot(valid && keep(x, y, len, a));
-    int n = Lanes::popc(m);
-    if (n) {
-      if (L.leader()) rows[y - row0] += (uint32_t)n;
-      frags += (unsigned)n;
-    }
-  }
-  SKC_HD void acc_row(const Lanes& L, int y, const uint8_t* acc, int left, int lo, int hi) {
+  SKC_HD void acc_row(const Lanes& L, int y, const int32_t* diff, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return;
     uint32_t n = 0;
-    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
+    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) {
         n++;
@@ -207,55 +205,48 @@ struct CountSink {
   }
 };
 
-struct EmitSink {
+struct EmitSink : SinkBase {
+  static constexpr bool kEmit = true;
   uint2* spans;           // this pass's span range
   const uint32_t* rows;   // exclusive offsets per row, rows+1 entries
-  int row0, row1, W, H;
-  uint32_t ga;
-  bool srcover;
+  uint32_t total;         // spans of this pass (rows[nrows]); writes past it
+  uint32_t* err;          //   are skipped and flagged (self-check)
+  uint2 sink_slot;        // harmless target for skipped writes
   int cur_row;
   uint32_t cur;
-  SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
-    if (y < row0 || y >= row1) return false;
-    if (!ClipSpan(x, y, len, W, H)) return false;
-    return !(srcover && (a & ga) == 0);
-  }
-  SKC_HD void seek(int y) {
+  SKC_HD uint32_t row_cursor(int y) {
+    if (y < row0 || y >= row1) return 0;
     if (y != cur_row) {
       cur_row = y;
       cur = rows[y - row0];
     }
+    return cur;
   }
-  SKC_HD void real(const Lanes& L, int x, int y, int len, uint8_t a) {
-    if (!keep(x, y, len, a)) return;
-    seek(y);
-    if (L.leader()) spans[cur] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
-    cur++;
+  SKC_HD uint2* span_ptr(uint32_t i) { return spans + i; }
+  SKC_HD bool in_range(uint32_t i, uint32_t n) {
+    if ((uint64_t)i + n <= total) return true;
+    FlagError(err, 2);
+    return false;
   }
-  SKC_HD void pixels(const Lanes& L, int x0, int y, uint8_t a, bool valid) {
-    int x = x0 + L.lane, len = 1;
-    bool k = valid && keep(x, y, len, a);
-    unsigned m = L.ballot(k);
-    if (!m) return;
-    seek(y);
-    if (k) spans[cur + Lanes::popc(m & L.lt_mask())] = make_uint2((uint32_t)x | (1u << 16), a);
-    cur += (uint32_t)Lanes::popc(m);
+  SKC_HD void step_done(const Lanes&, int y, uint32_t n, unsigned long long) {
+    if (n && y == cur_row) cur += n;
   }
   // The accumulated spans of a row follow its direct spans (the reference
   // flushes a row's accumulator only after leaving the row), so they fill
   // the tail of the row's slot.
-  SKC_HD void acc_row(const Lanes& L, int y, const uint8_t* acc, int left, int lo, int hi) {
+  SKC_HD void acc_row(const Lanes& L, int y, const int32_t* diff, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return;
     uint32_t n = 0;
-    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
+    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) n++;
     });
     uint32_t o = rows[y - row0 + 1] - n;
-    acc_runs_lanes(L, acc, lo, hi, [&](int s, int w, uint8_t a) {
+    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) {
-        if (L.leader()) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        if (L.leader() && o < total) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        if (o >= total) FlagError(err, 2);
         o++;
       }
     });
@@ -270,17 +261,17 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   SliceLayout L;
   L.compute(pd.cap, sizeof(Edge));
   const Edge* S = (const Edge*)(b.scratch + pd.slice_off + L.off[13]);
-  Edge* W = b.work + sw.work_off;
   int n = g.n_edges;
-  for (int i = lanes.lane; i < n + 2; i += Lanes::n) W[i] = S[i];
+  SweepMem M = SweepMemAt(b.sweepmem + sw.work_off, n, g.acc_width);
+  for (int i = lanes.lane; i < n; i += Lanes::n) M.W[i] = S[i];
+  for (int i = lanes.lane; i <= g.acc_width; i += Lanes::n) M.diff[i] = 0;
   lanes.sync();
-  Sweep<Sink> s;
+  LaneSweep<Sink> s;
   s.L = lanes;
-  s.E = W;
-  s.head = n;
-  s.tail = n + 1;
+  s.M = M;
+  s.n = n;
+  s.err = b.err;
   s.sink = sink;
-  s.acc = b.acc + sw.acc_off;
   s.acc_left = g.acc_left;
   s.acc_width = g.acc_width;
   s.acc_y = kNaN32;
@@ -343,6 +334,8 @@ SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   sink.srcover = (pd.flags & kPassSrcOver) != 0;
   sink.cur_row = -1;
   sink.cur = 0;
+  sink.total = sink.rows[nrows];
+  sink.err = b.err;
   RunSweep(b, p, g, &sink, lanes);
 }
 

@@ -67,8 +67,8 @@ struct DeviceBatch {
   Context* ctx = nullptr;
   HostBatch hb;
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
-  DevBuf scratch, geom, sweep, work, acc, rowtab, pass_spans, comp, spans, pixels;
-  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags;
+  DevBuf scratch, geom, sweep, sweepmem, rowtab, pass_spans, comp, spans, pixels;
+  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
   uint32_t chunk = 1024;
   bool uploaded = false;
@@ -207,17 +207,17 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   // ---- per-pass sweep buffers and row tables
   std::vector<PassSweep> sw;
   SweepPlan pl = PlanSweep(db.h_geom, sw);
-  uint64_t work = pl.work_edges, acc = pl.acc_bytes, rows = pl.rows;
+  uint64_t rows = pl.rows;
   st.edges = pl.edges;
   if (rows >= 0xFFFFFFFFull) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
   SKC_TRY(Upload(db.sweep, sw, s));
-  SKC_TRY(db.work.ensure(std::max<uint64_t>(work, 1) * sizeof(Edge)));
-  SKC_TRY(db.acc.ensure(std::max<uint64_t>(acc, 16)));
-  SKC_TRY(cudaMemsetAsync(db.acc.p, 0, std::max<uint64_t>(acc, 16), s));
+  SKC_TRY(db.sweepmem.ensure(std::max<uint64_t>(pl.sweep_bytes, 16)));
   SKC_TRY(db.rowtab.ensure(std::max<uint64_t>(rows, 1) * 4));
   SKC_TRY(cudaMemsetAsync(db.rowtab.p, 0, std::max<uint64_t>(rows, 1) * 4, s));
   SKC_TRY(db.pass_spans.ensure(std::max<size_t>(np, 1) * 4));
   SKC_TRY(db.pass_frags.ensure(std::max<size_t>(np, 1) * 8));
+  SKC_TRY(db.err.ensure(16));
+  SKC_TRY(cudaMemsetAsync(db.err.p, 0, 16, s));
 
   DevBatch b{};
   b.verbs = db.verbs.as<uint8_t>();
@@ -230,11 +230,11 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.scratch = db.scratch.as<uint8_t>();
   b.geom = db.geom.as<PassGeom>();
   b.sweep = db.sweep.as<PassSweep>();
-  b.work = db.work.as<Edge>();
-  b.acc = db.acc.as<uint8_t>();
+  b.sweepmem = db.sweepmem.as<uint8_t>();
   b.rowtab = db.rowtab.as<uint32_t>();
   b.pass_spans = db.pass_spans.as<uint32_t>();
   b.pass_frags = db.pass_frags.as<unsigned long long>();
+  b.err = db.err.as<uint32_t>();
   SKC_TRY(cudaEventRecord(ctx->stage[2], s));
   st.kernel_launches += LaunchSweep(b, false, s);
   SKC_TRY(cudaEventRecord(ctx->stage[3], s));
@@ -281,7 +281,13 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   SKC_TRY(cudaEventRecord(ctx->stage[9], s));
   SKC_TRY(cudaGetLastError());
   if (timed) SKC_TRY(cudaEventRecord(ctx->ev1, s));
+  uint32_t err = 0;
+  SKC_TRY(cudaMemcpyAsync(&err, db.err.p, 4, cudaMemcpyDeviceToHost, s));
   SKC_TRY(cudaStreamSynchronize(s));
+  if (err) {
+    std::fprintf(stderr, "skity_cuda: device self-check failed (code %u)\n", err);
+    return SKITY_CUDA_ERROR_DEVICE;
+  }
   if (timed) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);

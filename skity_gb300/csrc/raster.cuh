@@ -548,393 +548,30 @@ SKC_HD uint8_t partial_triangle_to_alpha(Fixed a, Fixed b) {
   return (uint8_t)((area >> 8) & 0xFF);
 }
 
-template <typename Sink>
-struct Sweep {
-  Lanes L;
-  Edge* E;
-  int head, tail;
-  Sink* sink;
-  // SpanBuilder accumulator (sw_raster.cc:62-136)
-  uint8_t* acc;
-  int acc_left, acc_width;
-  int acc_y;
-  int touch_lo, touch_hi;
-  float scan_top;
-  bool no_real_override;
-
-  SKC_HD void real(int x, int y, int len, uint8_t a) {
-    if (y < scan_top) return;
-    sink->real(L, x, y, len, a);
+// Entry i of compute_alpha_below_line (below = true) or
+// compute_alpha_above_line (sw_raster.cc:314-370) over R = ceil(r) pixels;
+// the reference fills the entries with a running sum, re-derived here per
+// entry so any subset can be computed.
+SKC_HD uint8_t triangle_entry(bool below, Fixed l, Fixed r, Fixed dY, uint8_t full, int i) {
+  int R = FixedCeilToInt(r);
+  if (R == 1) {
+    return below ? partial_alpha_a(trapezoid_to_alpha(l, r), full)
+                 : partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
   }
-  SKC_HD void flush_acc() {
-    if (acc_y == kNaN32) return;
-    if (touch_lo <= touch_hi) {
-      sink->acc_row(L, acc_y, acc, acc_left, touch_lo, touch_hi + 1);
-      L.sync();
-      for (int i = touch_lo + L.lane; i <= touch_hi; i += Lanes::n) acc[i] = 0;
-      L.sync();
-    }
-    touch_lo = 0x7fffffff;
-    touch_hi = -1;
+  Fixed first = kFixed1 - l;
+  Fixed last = r - ((R - 1) << 16);
+  if (below) {
+    Fixed lastH = FixedMul(last, dY);
+    if (i == R - 1) return (uint8_t)(FixedMul(last, lastH) >> 9);
+    if (i == 0) return (uint8_t)(full - partial_triangle_to_alpha(first, dY));
+    Fixed a16 = wadd(wadd(lastH, dY >> 1), wmul(R - 2 - i, dY));
+    return (uint8_t)((a16 >> 8) & 0xFF);
   }
-  SKC_HD void flush_if_need(int y) {
-    if (acc_y == y) return;
-    if (acc_y == kNaN32) {
-      acc_y = y;
-      return;
-    }
-    flush_acc();
-    acc_y = y;
-  }
-  SKC_HD static uint8_t sat_add(uint8_t a, uint8_t d) {
-    return (uint16_t)a + (uint16_t)d > 255 ? 255 : (uint8_t)(a + d);
-  }
-  SKC_HD void touch(int o0, int o1) {  // [o0, o1) clipped to the row buffer
-    o0 = max_(o0, 0);
-    o1 = min_(o1, acc_width);
-    if (o0 < o1) {
-      touch_lo = min_(touch_lo, o0);
-      touch_hi = max_(touch_hi, o1 - 1);
-    }
-  }
-  SKC_HD void acc_add(int x, int y, int width, uint8_t a) {
-    if (y < scan_top) return;
-    flush_if_need(y);
-    int off = x - acc_left;
-    for (int i = L.lane; i < width; i += Lanes::n) {
-      int o = off + i;
-      if ((unsigned)o < (unsigned)acc_width) acc[o] = sat_add(acc[o], a);
-    }
-    L.sync();
-    touch(off, off + width);
-  }
-  // One alpha per lane for pixels x0 + lane (lanes with valid == false
-  // carry nothing): per-pixel spans (RealSpanBuilder::BuildSpans) or
-  // accumulation (SpanBuilder::BuildSpans).
-  SKC_HD void pixels(bool real_spans, int x0, int y, uint8_t a, bool valid, int count) {
-    if (y < scan_top) return;
-    if (real_spans) {
-      sink->pixels(L, x0, y, a, valid);
-      return;
-    }
-    flush_if_need(y);
-    int o = x0 - acc_left + L.lane;
-    if (valid && (unsigned)o < (unsigned)acc_width) acc[o] = sat_add(acc[o], a);
-    L.sync();
-    touch(x0 - acc_left, x0 - acc_left + count);
-  }
-
-  SKC_HD void blit_single(int y, int x, uint8_t alpha, uint8_t full, bool no_real) {
-    if (full == 0xFF && !no_real) real(x, y, 1, alpha);
-    else acc_add(x, y, 1, partial_alpha_a(alpha, full));
-  }
-  SKC_HD void blit_two(int y, int x, uint8_t a1, uint8_t a2, uint8_t full, bool no_real) {
-    if (full == 0xFF && !no_real) {
-      real(x, y, 1, a1);
-      real(x + 1, y, 1, a2);
-    } else {
-      acc_add(x, y, 1, a1);
-      acc_add(x + 1, y, 1, a2);
-    }
-  }
-  SKC_HD void blit_full(int y, int x, int len, uint8_t full, bool no_real) {
-    if (full == 0xFF && !no_real) real(x, y, len, full);
-    else acc_add(x, y, len, full);
-  }
-  // blit_aaa_trapezoid_row (sw_raster.cc:372-455).  Lane l computes pixel
-  // L + w0 + l of each window of Lanes::n pixels; every pixel's alpha depends
-  // only on its index (the running sums are re-derived per pixel).
-  SKC_HDN void aaa_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
-                       uint8_t full, bool no_real) {
-    int L0 = FixedFloorToInt(ul), R = FixedCeilToInt(lr);
-    int len = R - L0;
-    if (len == 1) {
-      blit_single(y, L0, trapezoid_to_alpha(ur - ul, lr - ll), full, no_real);
-      return;
-    }
-    int uL = FixedFloorToInt(ul), lL = FixedCeilToInt(ll);
-    int uR = FixedFloorToInt(ur), lR = FixedCeilToInt(lr);
-    bool two_left = uL + 2 == lL, two_right = uR + 2 == lR;
-    uint8_t la1 = 0, la2 = 0, ra1 = 0, ra2 = 0;
-    if (two_left) {
-      Fixed first = IntToFixed(uL) + kFixed1 - ul;
-      Fixed second = ll - ul - first;
-      la1 = (uint8_t)(full - partial_triangle_to_alpha(first, lDY));
-      la2 = partial_triangle_to_alpha(second, lDY);
-    }
-    if (two_right) {
-      Fixed first = IntToFixed(uR) + kFixed1 - ur;
-      Fixed second = lr - ur - first;
-      ra1 = partial_triangle_to_alpha(first, rDY);
-      ra2 = (uint8_t)(full - partial_triangle_to_alpha(second, rDY));
-    }
-    const bool real_spans = full == 0xFF && !no_real;
-    for (int w0 = 0; w0 < len; w0 += Lanes::n) {
-      int i = w0 + L.lane;  // pixel L0 + i
-      bool valid = i < len;
-      uint8_t a = full;
-      if (valid) {
-        int px = L0 + i;
-        if (two_left) {
-          if (i == 0) a = a > la1 ? (uint8_t)(a - la1) : 0;
-          if (i == 1) a = a > la2 ? (uint8_t)(a - la2) : 0;
-        } else if (px >= uL && px < lL) {
-          uint8_t t = triangle_entry(true, ul - IntToFixed(uL), ll - IntToFixed(uL), lDY, full,
-                                     px - uL);
-          a = a > t ? (uint8_t)(a - t) : 0;
-        }
-        if (two_right) {
-          if (i == len - 2) a = a > ra1 ? (uint8_t)(a - ra1) : 0;
-          if (i == len - 1) a = a > ra2 ? (uint8_t)(a - ra2) : 0;
-        } else if (px >= uR && px < lR) {
-          uint8_t t = triangle_entry(false, ur - IntToFixed(uR), lr - IntToFixed(uR), rDY, full,
-                                     px - uR);
-          a = a > t ? (uint8_t)(a - t) : 0;
-        }
-      }
-      pixels(real_spans, L0 + w0, y, a, valid, min_(Lanes::n, len - w0));
-    }
-  }
-  // Entry i of compute_alpha_below_line (below = true) or
-  // compute_alpha_above_line (sw_raster.cc:314-370) over R = ceil(r) pixels.
-  SKC_HD static uint8_t triangle_entry(bool below, Fixed l, Fixed r, Fixed dY, uint8_t full, int i) {
-    int R = FixedCeilToInt(r);
-    if (R == 1) {
-      return below ? partial_alpha_a(trapezoid_to_alpha(l, r), full)
-                   : partial_alpha_a((uint8_t)(wsub(wsub(R << 17, l), r) >> 9), full);
-    }
-    Fixed first = kFixed1 - l;
-    Fixed last = r - ((R - 1) << 16);
-    if (below) {
-      Fixed lastH = FixedMul(last, dY);
-      if (i == R - 1) return (uint8_t)(FixedMul(last, lastH) >> 9);
-      if (i == 0) return (uint8_t)(full - partial_triangle_to_alpha(first, dY));
-      Fixed a16 = wadd(wadd(lastH, dY >> 1), wmul(R - 2 - i, dY));
-      return (uint8_t)((a16 >> 8) & 0xFF);
-    }
-    Fixed firstH = FixedMul(first, dY);
-    if (i == 0) return (uint8_t)(FixedMul(first, firstH) >> 9);
-    if (i == R - 1) return (uint8_t)(full - partial_triangle_to_alpha(last, dY));
-    Fixed a16 = wadd(wadd(firstH, dY >> 1), wmul(i - 1, dY));
-    return (uint8_t)(a16 >> 8);
-  }
-
-  SKC_HDN void trapezoid_row(int y, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
-                             uint8_t full, bool no_real) {  // sw_raster.cc:457-544
-    if (ul > ur) return;
-    if (ll > lr) ll = lr = approximate_intersection(ul, ll, ur, lr);
-    if (ul == ur && ll == lr) return;
-    if (ul > ll) swap_(ul, ll);
-    if (ur > lr) swap_(ur, lr);
-    Fixed joinLeft = FixedCeilToFixed(ll);
-    Fixed joinRite = FixedFloorToFixed(ur);
-    if (joinLeft <= joinRite) {
-      if (ul < joinLeft) {
-        int len = FixedCeilToInt(joinLeft - ul);
-        if (len == 1) {
-          blit_single(y, ul >> 16, trapezoid_to_alpha(joinLeft - ul, joinLeft - ll), full, no_real);
-        } else if (len == 2) {
-          Fixed first = joinLeft - kFixed1 - ul;
-          Fixed second = ll - ul - first;
-          uint8_t a1 = partial_triangle_to_alpha(first, lDY);
-          uint8_t a2 = (uint8_t)(full - partial_triangle_to_alpha(second, lDY));
-          blit_two(y, ul >> 16, a1, a2, full, no_real);
-        } else {
-          aaa_row(y, ul, joinLeft, ll, joinLeft, lDY, kMaxS32, full, no_real);
-        }
-      }
-      if (joinLeft < joinRite) {
-        blit_full(y, FixedFloorToInt(joinLeft), FixedFloorToInt(joinRite - joinLeft), full, no_real);
-      }
-      if (lr > joinRite) {
-        int len = FixedCeilToInt(lr - joinRite);
-        if (len == 1) {
-          blit_single(y, joinRite >> 16, trapezoid_to_alpha(ur - joinRite, lr - joinRite), full, no_real);
-        } else if (len == 2) {
-          Fixed first = joinRite + kFixed1 - ur;
-          Fixed second = lr - ur - first;
-          uint8_t a1 = (uint8_t)(full - partial_triangle_to_alpha(first, rDY));
-          uint8_t a2 = partial_triangle_to_alpha(second, rDY);
-          blit_two(y, joinRite >> 16, a1, a2, full, no_real);
-        } else {
-          aaa_row(y, joinRite, ur, joinRite, lr, kMaxS32, rDY, full, no_real);
-        }
-      }
-    } else {
-      aaa_row(y, ul, ur, ll, lr, lDY, rDY, full, no_real);
-    }
-  }
-
-  // ---- active edge list (sw_raster.cc:138-247)
-  SKC_HD bool too_close_e(int prev, int next, Fixed lowerY) const {
-    if (next < 0 || prev < 0) return false;
-    return E[next].upper_y < lowerY &&
-           wadd(E[prev].x, kFixed1) >= wsub(E[next].x, iabs_(E[next].dx));
-  }
-  SKC_HD static bool too_close_r(int prevRite, Fixed ul, Fixed ll) {
-    return prevRite > FixedFloorToInt(ul) || prevRite > FixedFloorToInt(ll);
-  }
-  SKC_HD static void nny_update(Fixed y, Fixed next_y, Fixed* nny) {
-    *nny = y > next_y && y < *nny ? y : *nny;
-  }
-  SKC_HD void check_intersection(int edge, Fixed next_y, Fixed* nny) const {
-    const Edge& e = E[edge];
-    const Edge& p = E[e.prev];
-    if (p.prev >= 0 && wadd(p.x, p.dx) > wadd(e.x, e.dx)) *nny = next_y + (kFixed1 >> kAccuracy);
-  }
-  SKC_HD void remove_edge(int edge) {
-    E[E[edge].prev].next = E[edge].next;
-    E[E[edge].next].prev = E[edge].prev;
-  }
-  SKC_HD void insert_after(int edge, int after) {
-    E[edge].prev = after;
-    E[edge].next = E[after].next;
-    E[E[after].next].prev = edge;
-    E[after].next = edge;
-  }
-  SKC_HD void backward_insert(int edge) {
-    Fixed x = E[edge].x;
-    int prev = E[edge].prev;
-    while (E[prev].prev >= 0 && E[prev].x > x) prev = E[prev].prev;
-    if (E[prev].next != edge) {
-      remove_edge(edge);
-      insert_after(edge, prev);
-    }
-  }
-  SKC_HDN void insert_new_edges(int ne, Fixed y, Fixed* nny) {  // :207-247
-    if (E[ne].upper_y > y) {
-      nny_update(E[ne].upper_y, y, nny);
-      return;
-    }
-    int prev = E[ne].prev;
-    if (E[prev].x <= E[ne].x) {
-      while (E[ne].upper_y <= y) {
-        check_intersection(ne, y, nny);
-        nny_update(E[ne].lower_y, y, nny);
-        ne = E[ne].next;
-      }
-      nny_update(E[ne].upper_y, y, nny);
-      return;
-    }
-    int start = prev;
-    Fixed nx = E[ne].x;
-    while (E[start].prev >= 0 && E[start].x > nx) start = E[start].prev;
-    do {
-      int next = E[ne].next;
-      bool skip = false;
-      for (;;) {
-        if (E[start].next == ne) {
-          skip = true;
-          break;
-        }
-        int after = E[start].next;
-        if (E[after].x >= E[ne].x) break;
-        start = after;
-      }
-      if (!skip) {
-        remove_edge(ne);
-        insert_after(ne, start);
-      }
-      check_intersection(ne, y, nny);
-      nny_update(E[ne].lower_y, y, nny);
-      start = ne;
-      ne = next;
-    } while (E[ne].upper_y <= y);
-    nny_update(E[ne].upper_y, y, nny);
-  }
-
-  // WalkEdges (sw_raster.cc:546-677)
-  SKC_HDN void walk(bool even_odd, int start_y, int stop_y, Fixed left_clip, Fixed right_clip) {
-    E[head].x = E[head].upper_x = left_clip;
-    E[tail].x = E[tail].upper_x = right_clip;
-    Fixed y = max_(E[E[head].next].upper_y, IntToFixed(start_y));
-    Fixed nny = kMaxS32;
-    {
-      int edge;
-      for (edge = E[head].next; E[edge].upper_y <= y; edge = E[edge].next) {
-        GoY(&E[edge], y);
-        nny_update(E[edge].lower_y, y, &nny);
-      }
-      nny_update(E[edge].upper_y, y, &nny);
-    }
-    int winding_mask = even_odd ? 1 : -1;
-    for (;;) {
-      int w = 0;
-      bool in_interval = false;
-      Fixed prev_x = E[head].x;
-      Fixed next_y = min_(nny, FixedCeilToFixed(y + 1));
-      int curr = E[head].next;
-      int left_edge = head;
-      Fixed left = left_clip;
-      Fixed left_dy = 0;
-      int prev_right = FixedFloorToInt(left_clip);
-      nny = kMaxS32;
-      int y_shift = 0;
-      if ((next_y - y) & (kFixed1 >> 2)) {
-        y_shift = 2;
-        next_y = y + (kFixed1 >> 2);
-      } else if ((next_y - y) & (kFixed1 >> 1)) {
-        y_shift = 1;
-      }
-      uint8_t full = partial_alpha_h(0xFF, next_y - y);
-      while (E[curr].upper_y <= y) {
-        Edge& ce = E[curr];
-        w += ce.winding;
-        bool prev_in = in_interval;
-        in_interval = (w & winding_mask) != 0;
-        bool is_left = in_interval && !prev_in;
-        bool is_right = !in_interval && prev_in;
-        if (is_left) {
-          left = max_(ce.x, left_clip);
-          left_dy = ce.dy;
-          left_edge = curr;
-          GoYShift(&ce, next_y, y_shift);
-        } else if (is_right) {
-          Fixed right = min_(right_clip, ce.x);
-          GoYShift(&ce, next_y, y_shift);
-          Fixed next_left = max_(left_clip, E[left_edge].x);
-          Fixed next_right = min_(right_clip, ce.x);
-          bool no_real = full == 0xFF && (too_close_r(prev_right, left, E[left_edge].x) ||
-                                          too_close_e(curr, ce.next, next_y));
-          trapezoid_row(y >> 16, left, right, next_left, next_right, left_dy, ce.dy, full, no_real);
-          prev_right = FixedCeilToInt(max_(right, ce.x));
-        } else {
-          GoYShift(&ce, next_y, y_shift);
-        }
-        int next = ce.next;
-        while (E[curr].lower_y <= next_y) {
-          if (E[curr].curve_count > 0) {
-            E[curr].snapped_x = E[curr].x;  // KeepContinuous (sw_edge.cc:294-297)
-            E[curr].snapped_y = E[curr].y;
-            if (!UpdateQuad(&E[curr])) break;
-          } else {
-            break;
-          }
-        }
-        if (E[curr].lower_y <= next_y) {
-          remove_edge(curr);
-        } else {
-          nny_update(E[curr].lower_y, next_y, &nny);
-          Fixed new_x = E[curr].x;
-          if (new_x < prev_x) {
-            backward_insert(curr);
-          } else {
-            prev_x = new_x;
-          }
-          check_intersection(curr, next_y, &nny);
-        }
-        curr = next;
-      }
-      if (in_interval) {
-        bool no_real = full == 0xFF && too_close_e(E[left_edge].prev, left_edge, next_y);
-        trapezoid_row(y >> 16, left, right_clip, max_(left_clip, E[left_edge].x), right_clip,
-                      left_dy, 0, full, no_real);
-      }
-      y = next_y;
-      if (y >= IntToFixed(stop_y)) break;
-      insert_new_edges(curr, y, &nny);
-    }
-  }
-};
+  Fixed firstH = FixedMul(first, dY);
+  if (i == 0) return (uint8_t)(FixedMul(first, firstH) >> 9);
+  if (i == R - 1) return (uint8_t)(full - partial_triangle_to_alpha(last, dY));
+  Fixed a16 = wadd(wadd(firstH, dY >> 1), wmul(i - 1, dY));
+  return (uint8_t)(a16 >> 8);
+}
 
 }  // namespace skc

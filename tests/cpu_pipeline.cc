@@ -69,12 +69,14 @@ extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rg
   }
   std::vector<PassSweep> sw;
   SweepPlan pl = PlanSweep(geom, sw);
-  std::vector<Edge> work(pl.work_edges + 1);
-  std::vector<uint8_t> acc(pl.acc_bytes + 16, 0);
+  // exact size: an overrun of the planned layout is caught by the sanitizer
+  // build of this harness and shows up as a mismatch otherwise
+  std::vector<uint8_t> sweepmem(pl.sweep_bytes, 0);
   std::vector<uint32_t> rowtab(pl.rows + 1, 0), pass_spans(np + 1, 0);
   b.sweep = sw.data();
-  b.work = work.data();
-  b.acc = acc.data();
+  b.sweepmem = sweepmem.data();
+  uint32_t err = 0;
+  b.err = &err;
   b.rowtab = rowtab.data();
   b.pass_spans = pass_spans.data();
   Lanes lanes;
@@ -115,6 +117,7 @@ extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rg
   }
   BuildRowTasks(hb, hb.main_canvases, 65535, tasks);
   for (const RowTask& t : tasks) CompositeRowScalar(b, t, row.data());
+  if (err) return -6;
   const CanvasDesc& cd = hb.canvases[hb.main_canvases[0]];
   std::memcpy(out_rgba, pixels.data() + cd.px_off, (size_t)cd.w * cd.h * 4);
   if (stats) {
