@@ -47,6 +47,8 @@ typedef enum skity_cuda_result {
   SKITY_CUDA_ERROR_DEVICE = -6,                 /* a CUDA call failed */
   SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY = -7,   /* device budget exceeded */
   SKITY_CUDA_ERROR_DEVICE_TIMEOUT = -8,         /* a bounded device wait expired */
+  SKITY_CUDA_ERROR_SCRATCH_LIMIT = -9,          /* input too large for the fixed
+                                                   scratch of skity_cuda_draw_path_static */
 } skity_cuda_result;
 
 typedef struct skity_cuda_context_s* skity_cuda_context;
@@ -189,6 +191,40 @@ SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch);
 SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
                                              uint8_t* out_pixels);
 SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch);
+
+/* ---- drawing without allocation --------------------------------------------
+ * No counterpart in the reference: its software canvas allocates as it draws.
+ *
+ * skity_cuda_draw_path_static draws ONE path with a solid-colour paint
+ * (Canvas::DrawPath semantics: fill, stroke, stroke-and-fill or
+ * stroke-then-fill; blend modes clear/src/dst/src-over; no shader, no mask
+ * filter) onto a premultiplied RGBA8 canvas that already lives in device
+ * memory (`device_pixels`, `row_bytes` apart, a multiple of 4).  It allocates
+ * nothing: no device memory (no cudaMalloc / cudaFree), no host heap.  Every
+ * intermediate buffer comes from one fixed static device array of
+ * SKITY_CUDA_STATIC_SCRATCH_BYTES per device, so it suits callers that must
+ * not allocate while drawing -- a render loop held to a fixed footprint, or a
+ * host that cannot afford the device-wide synchronisation that freeing
+ * device memory implies.
+ *
+ * Limits: inputs whose path copy, geometry, sweep memory, row table and spans
+ * together need more than the static scratch are rejected with
+ * SKITY_CUDA_ERROR_SCRATCH_LIMIT before the canvas is touched.
+ *
+ * The scratch is one per device, not one per call: calls that overlap on the
+ * same device race on it, so callers on several host threads must serialise
+ * them.  The call runs on `stream` (NULL: the default stream) and returns
+ * once the draw is complete.  The first call on a device does a one-time
+ * set-up (it looks up the scratch's device address with that device
+ * current); make that first call -- an empty path is enough -- before any
+ * stream capture begins. */
+#define SKITY_CUDA_STATIC_SCRATCH_BYTES (16u << 20)
+SKITY_CUDA_API int32_t skity_cuda_draw_path_static(int32_t device, uint8_t* device_pixels,
+                                                   uint32_t width, uint32_t height,
+                                                   size_t row_bytes,
+                                                   const skity_cuda_path* path,
+                                                   const skity_cuda_paint* paint,
+                                                   void* stream);
 
 /* Library version string. */
 SKITY_CUDA_API const char* skity_cuda_version(void);

@@ -15,6 +15,7 @@ ERRORS = {
     -1: "invalid handle", -2: "invalid argument", -3: "initialization failed",
     -4: "out of host memory", -5: "not supported", -6: "device error",
     -7: "out of device memory", -8: "device timeout",
+    -9: "input exceeds the fixed scratch of skity_cuda_draw_path_static",
 }
 
 
@@ -86,6 +87,10 @@ SIGNATURES = {
     "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
     "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
     "skity_cuda_batch_destroy": (None, [_vp]),
+    "skity_cuda_draw_path_static": (ctypes.c_int32, [ctypes.c_int32, _vp, ctypes.c_uint32,
+                                                     ctypes.c_uint32, ctypes.c_size_t,
+                                                     ctypes.POINTER(Path_), ctypes.POINTER(Paint_),
+                                                     _vp]),
 }
 
 _LIB = None
