@@ -508,7 +508,13 @@ inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv
 // Per-pass sweep buffers and row tables from the geometry results.
 struct SweepPlan {
   uint64_t sweep_bytes = 0, rows = 0, edges = 0;
+  int32_t max_acc = 0;  // largest accumulator (acc_width + 1) of a swept pass
 };
+// Accumulator entries each register-sweep warp keeps in shared memory.
+inline int32_t RegDiffCap(const SweepPlan& pl) {
+  int32_t c = (pl.max_acc + 3) & ~3;
+  return std::max<int32_t>(4, std::min<int32_t>(c, kRegDiffMax));
+}
 inline SweepPlan PlanSweep(const std::vector<PassGeom>& geom, std::vector<PassSweep>& sw) {
   SweepPlan pl;
   sw.assign(geom.size(), PassSweep{});
@@ -521,6 +527,7 @@ inline SweepPlan PlanSweep(const std::vector<PassGeom>& geom, std::vector<PassSw
       b = (b + 255) & ~uint64_t(255);
       sw[p].bytes = b;
       pl.sweep_bytes += b;
+      pl.max_acc = std::max(pl.max_acc, std::max(g.acc_width, 0) + 1);
     }
     if (g.n_edges > 0) pl.edges += (uint64_t)g.n_edges;
     int nr = g.row1 - g.row0;

@@ -2,8 +2,10 @@
 //
 //   k_geometry   1 thread / pass : Path -> QuadPath (-> stroke -> QuadPath)
 //                                  -> fixed-point edges -> introsort
-//   k_sweep      1 thread / pass : analytic-AA sweep; count pass fills the
-//                                  per-row span counts, emit pass writes spans
+//   k_sweep_*    1 warp / pass   : analytic-AA sweep (register form, generic
+//                                  form for very long active lists); count
+//                                  pass fills the per-row span counts, emit
+//                                  pass writes spans
 //   k_composite  1 warp / row     : replays every pass's spans of the row in
 //                                  draw order into a shared-memory row, then
 //                                  writes the row back (16-byte stores)
@@ -32,33 +34,65 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
   return 1;
 }
 
-// one warp per pass: the sweep logic runs warp-uniformly, per-pixel work is
-// split across the lanes
+// Sweeps: one warp per pass.  The register sweep takes every pass whose
+// active list fits kRegMaxM edges (2 warps per block, each with its
+// RegShared block and accumulator in shared memory); the generic sweep
+// (4 warps per block, state in global memory) takes the passes the count
+// kernel marked, after the register kernels.
 constexpr int kSweepWarps = 4;
+constexpr int kRegWarps = 2;
+
+__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_count_reg(DevBatch b) {
+  extern __shared__ __align__(16) uint8_t reg_smem[];
+  const int w = threadIdx.x >> 5;
+  const uint32_t p = blockIdx.x * kRegWarps + w;
+  if (p >= b.n_passes) return;
+  Lanes L;
+  L.lane = threadIdx.x & 31;
+  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes(b.reg_diff_cap);
+  SweepCountPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)),
+                    b.reg_diff_cap);
+}
+
+__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_emit_reg(DevBatch b) {
+  extern __shared__ __align__(16) uint8_t reg_smem[];
+  const int w = threadIdx.x >> 5;
+  const uint32_t p = blockIdx.x * kRegWarps + w;
+  if (p >= b.n_passes || b.pass_class[p] != 0) return;
+  Lanes L;
+  L.lane = threadIdx.x & 31;
+  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes(b.reg_diff_cap);
+  SweepEmitPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)),
+                   b.reg_diff_cap);
+}
 
 __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_count(DevBatch b) {
   uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
   Lanes L;
   L.lane = threadIdx.x & 31;
-  if (p < b.n_passes) SweepCountPass(b, p, L);
+  if (p < b.n_passes && b.pass_class[p] == 1) SweepCountPass(b, p, L, true);
 }
 
 __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_emit(DevBatch b) {
   uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
   Lanes L;
   L.lane = threadIdx.x & 31;
-  if (p < b.n_passes) SweepEmitPass(b, p, L);
+  if (p < b.n_passes && b.pass_class[p] == 1) SweepEmitPass(b, p, L);
 }
 
 int LaunchSweep(const DevBatch& b, bool emit, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
-  unsigned grid = (b.n_passes + kSweepWarps - 1) / kSweepWarps;
+  const size_t smem = kRegWarps * RegSmemBytes(b.reg_diff_cap);
+  const unsigned rgrid = (b.n_passes + kRegWarps - 1) / kRegWarps;
+  const unsigned ggrid = (b.n_passes + kSweepWarps - 1) / kSweepWarps;
   if (emit) {
-    k_sweep_emit<<<grid, 32 * kSweepWarps, 0, stream>>>(b);
+    k_sweep_emit_reg<<<rgrid, 32 * kRegWarps, smem, stream>>>(b);
+    k_sweep_emit<<<ggrid, 32 * kSweepWarps, 0, stream>>>(b);
   } else {
-    k_sweep_count<<<grid, 32 * kSweepWarps, 0, stream>>>(b);
+    k_sweep_count_reg<<<rgrid, 32 * kRegWarps, smem, stream>>>(b);
+    k_sweep_count<<<ggrid, 32 * kSweepWarps, 0, stream>>>(b);
   }
-  return 1;
+  return 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -68,7 +102,8 @@ constexpr int kCompWarps = 4;
 
 __global__ void __launch_bounds__(32 * kCompWarps)
     k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk) {
-  extern __shared__ uint32_t smem[];
+  extern __shared__ __align__(16) uint8_t reg_smem[];
+  uint32_t* smem = (uint32_t*)reg_smem;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   uint32_t task = blockIdx.x * kCompWarps + wib;

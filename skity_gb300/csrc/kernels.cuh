@@ -120,7 +120,14 @@ struct DevBatch {
   const uint8_t* roundtrip;
   const uint32_t* pass_list;  // passes to (re)run in the geometry kernel
   uint32_t n_list;
+  uint8_t* pass_class;  // sweep form per pass: 0 register sweep, 1 generic
+  int32_t reg_diff_cap; // accumulator entries per warp in shared memory
 };
+
+// Shared memory of one register-sweep warp: its RegShared block, then an
+// accumulator of reg_diff_cap entries (passes with wider accumulators keep
+// theirs in the pass's sweep memory).
+constexpr int32_t kRegDiffMax = 3072;
 
 // kernel launchers (kernels.cu); all launch on `stream` and return the
 // number of launches made

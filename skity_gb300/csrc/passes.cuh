@@ -4,7 +4,7 @@
 #pragma once
 #include "kernels.cuh"
 #include "stroke.cuh"
-#include "sweep.cuh"
+#include "regsweep.cuh"
 
 namespace skc {
 
@@ -191,8 +191,9 @@ struct CountSink : SinkBase {
     if (n && y >= row0 && y < row1 && L.leader()) rows[y - row0] += n;
     frags += f;
   }
-  SKC_HD void acc_row(const Lanes& L, int y, const int32_t* diff, int left, int lo, int hi) {
-    if (y < row0 || y >= row1) return;
+  // Returns false when the row lies outside the canvas (diff not read).
+  SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
+    if (y < row0 || y >= row1) return false;
     uint32_t n = 0;
     DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
@@ -202,6 +203,7 @@ struct CountSink : SinkBase {
       }
     });
     if (n && L.leader()) rows[y - row0] += n;
+    return true;
   }
 };
 
@@ -232,24 +234,25 @@ struct EmitSink : SinkBase {
     if (n && y == cur_row) cur += n;
   }
   // The accumulated spans of a row follow its direct spans (the reference
-  // flushes a row's accumulator only after leaving the row), so they fill
-  // the tail of the row's slot.
-  SKC_HD void acc_row(const Lanes& L, int y, const int32_t* diff, int left, int lo, int hi) {
-    if (y < row0 || y >= row1) return;
-    uint32_t n = 0;
-    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
-      int x = left + s, len = w;
-      if (keep(x, y, len, a)) n++;
-    });
-    uint32_t o = rows[y - row0 + 1] - n;
+  // flushes a row's accumulator only after leaving the row): they continue
+  // at the row's cursor.  Returns false when the row lies outside the canvas.
+  SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
+    if (y < row0 || y >= row1) return false;
+    uint32_t o = y == cur_row ? cur : rows[y - row0];
+    const uint32_t end = rows[y - row0 + 1];
     DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) {
-        if (L.leader() && o < total) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
-        if (o >= total) FlagError(err, 2);
+        if (o < end && o < total) {
+          if (L.leader()) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        } else {
+          FlagError(err, 2);
+        }
         o++;
       }
     });
+    if (o != end) FlagError(err, 2);
+    return true;
   }
 };
 
@@ -282,12 +285,105 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   s.flush_acc();
 }
 
-SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
+SKC_HD uint64_t RegSmemBytes(int32_t diff_cap) {
+  return sizeof(RegShared) + 4ull * (uint64_t)diff_cap;
+}
+
+// The register sweep of pass p (RegWalk); returns 0 when its active list
+// outgrows the registers.  The accumulator sits in shared memory when it fits.
+template <typename Sink>
+SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink,
+                       const Lanes& lanes, RegShared* sh, int32_t* sdiff, int32_t sdiff_cap) {
+  const PassDesc pd = b.passes[p];
+  const PassSweep sw = b.sweep[p];
+  SliceLayout L;
+  L.compute(pd.cap, sizeof(Edge));
+  const Edge* S = (const Edge*)(b.scratch + pd.slice_off + L.off[13]);
+  const int n = g.n_edges;
+  SweepMem M = SweepMemAt(b.sweepmem + sw.work_off, n, g.acc_width);
+  for (int i = lanes.lane; i < n; i += Lanes::n) M.W[i] = S[i];
+  int32_t* diff = g.acc_width + 1 <= sdiff_cap ? sdiff : M.diff;
+  for (int i = lanes.lane; i <= g.acc_width; i += Lanes::n) diff[i] = 0;
+  lanes.sync();
+  AccState as;
+  as.diff = diff;
+  as.left = g.acc_left;
+  as.width = g.acc_width;
+  as.y = kNaN32;
+  as.lo = 0x7fffffff;
+  as.hi = -1;
+  if (!RegWalk(lanes, *sh, M.W, n, sink, as, g.scan_top, (pd.flags & kPassEvenOdd) != 0,
+               g.start_y, g.stop_y, g.left_bound, g.right_bound))
+    return 0;
+  AccFlush(lanes, as, sink);
+  return 1;
+}
+
+// Per-row counts -> exclusive offsets (rows + 1 entries), totals of the pass.
+SKC_HD void FinishCount(const DevBatch& b, uint32_t p, uint32_t* rows, int nrows,
+                        unsigned long long frags, const Lanes& lanes) {
+  lanes.sync();
+  if (!lanes.leader()) return;
+  if (b.pass_frags) b.pass_frags[p] = frags;
+  uint32_t run = 0;
+  for (int r = 0; r < nrows; ++r) {
+    uint32_t c = rows[r];
+    rows[r] = run;
+    run += c;
+  }
+  if (nrows > 0) rows[nrows] = run;
+  b.pass_spans[p] = run;
+}
+
+SKC_HD void InitCountSink(const DevBatch& b, uint32_t p, const PassGeom& g, uint32_t* rows,
+                          CountSink* sink) {
+  const PassDesc pd = b.passes[p];
+  const CanvasDesc cd = b.canvases[pd.canvas];
+  sink->rows = rows;
+  sink->row0 = g.row0;
+  sink->row1 = g.row1;
+  sink->W = (int)cd.w;
+  sink->H = (int)cd.h;
+  sink->ga = pd.ga;
+  sink->srcover = (pd.flags & kPassSrcOver) != 0;
+  sink->frags = 0;
+}
+
+// Count pass through the register sweep; a pass it cannot take is marked
+// for the generic sweep (pass_class 1) with its rows left for that pass.
+SKC_HD void SweepCountPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
+                              int32_t* sdiff, int32_t sdiff_cap) {
+  const PassGeom g = b.geom[p];
+  const PassSweep sw = b.sweep[p];
+  uint32_t* rows = b.rowtab + sw.rbase;
+  const int nrows = g.row1 - g.row0;
+  unsigned long long frags = 0;
+  if (g.n_edges > 0 && nrows > 0) {
+    CountSink sink;
+    InitCountSink(b, p, g, rows, &sink);
+    if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
+      lanes.sync();
+      if (lanes.leader()) b.pass_class[p] = 1;
+      return;
+    }
+    frags = sink.frags;
+  }
+  FinishCount(b, p, rows, nrows, frags, lanes);
+}
+
+// Generic count pass; `zero_rows` clears the row counts first (a pass the
+// register sweep gave up on may have added to them).
+SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p, const Lanes& lanes,
+                            bool zero_rows = false) {
   const PassGeom g = b.geom[p];
   const PassSweep sw = b.sweep[p];
   uint32_t* rows = b.rowtab + sw.rbase;
   int nrows = g.row1 - g.row0;
   unsigned long long frags = 0;
+  if (zero_rows) {
+    for (int r = lanes.lane; r <= nrows; r += Lanes::n) rows[r] = 0;
+    lanes.sync();
+  }
   if (g.n_edges > 0 && nrows > 0) {
     const PassDesc pd = b.passes[p];
     const CanvasDesc cd = b.canvases[pd.canvas];
@@ -314,6 +410,36 @@ SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   }
   if (nrows > 0) rows[nrows] = run;
   b.pass_spans[p] = run;
+}
+
+SKC_HD void InitEmitSink(const DevBatch& b, uint32_t p, const PassGeom& g, EmitSink* sink) {
+  const PassDesc pd = b.passes[p];
+  const PassSweep sw = b.sweep[p];
+  const CanvasDesc cd = b.canvases[pd.canvas];
+  const int nrows = g.row1 - g.row0;
+  sink->spans = b.spans + b.comp[p].span_base;
+  sink->rows = b.rowtab + sw.rbase;
+  sink->row0 = g.row0;
+  sink->row1 = g.row1;
+  sink->W = (int)cd.w;
+  sink->H = (int)cd.h;
+  sink->ga = pd.ga;
+  sink->srcover = (pd.flags & kPassSrcOver) != 0;
+  sink->cur_row = -1;
+  sink->cur = 0;
+  sink->total = sink->rows[nrows];
+  sink->err = b.err;
+}
+
+SKC_HD void SweepEmitPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
+                             int32_t* sdiff, int32_t sdiff_cap) {
+  const PassGeom g = b.geom[p];
+  const int nrows = g.row1 - g.row0;
+  if (g.n_edges == 0 || nrows <= 0) return;
+  EmitSink sink;
+  InitEmitSink(b, p, g, &sink);
+  // the count pass took this pass through the register sweep, so it fits
+  if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) FlagError(b.err, 4);
 }
 
 SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {

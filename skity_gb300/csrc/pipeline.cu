@@ -68,7 +68,7 @@ struct DeviceBatch {
   HostBatch hb;
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
   DevBuf scratch, geom, sweep, sweepmem, rowtab, pass_spans, comp, spans, pixels;
-  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err;
+  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
   uint32_t chunk = 1024;
   bool uploaded = false;
@@ -218,6 +218,8 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   SKC_TRY(db.pass_frags.ensure(std::max<size_t>(np, 1) * 8));
   SKC_TRY(db.err.ensure(16));
   SKC_TRY(cudaMemsetAsync(db.err.p, 0, 16, s));
+  SKC_TRY(db.pass_class.ensure(std::max<size_t>(np, 1)));
+  SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
 
   DevBatch b{};
   b.verbs = db.verbs.as<uint8_t>();
@@ -235,6 +237,8 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.pass_spans = db.pass_spans.as<uint32_t>();
   b.pass_frags = db.pass_frags.as<unsigned long long>();
   b.err = db.err.as<uint32_t>();
+  b.pass_class = db.pass_class.as<uint8_t>();
+  b.reg_diff_cap = RegDiffCap(pl);
   SKC_TRY(cudaEventRecord(ctx->stage[2], s));
   st.kernel_launches += LaunchSweep(b, false, s);
   SKC_TRY(cudaEventRecord(ctx->stage[3], s));

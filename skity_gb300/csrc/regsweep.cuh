@@ -1,0 +1,582 @@
+// The sweep of sweep.cuh with the active edges held in registers.
+//
+// Same per-step restatement of WalkEdges (src/render/sw/sw_raster.cc:546-677)
+// as LaneSweep, but the state that the generic form keeps in per-pass global
+// arrays lives on chip:
+//   * list position p of the active list is slot p / 32 of lane p % 32; a
+//     slot holds the edge's index, x, dx, dy, lower_y, winding and curve
+//     count in registers (the quad-piece state stays in the pass's edge
+//     copy in global memory and is touched only when a piece ends);
+//   * the per-position values an interval reads (x before the step, after
+//     GoY and after the update, dx, dy) and the interval endpoints are
+//     exchanged through a per-warp shared-memory block;
+//   * the reorder of the survivors is a compaction when their new x are
+//     already non-decreasing in list order (no crossing in the step), and
+//     the rank computation of LaneSweep otherwise;
+//   * each step's intervals, the one left open by a culled right edge
+//     included, are blitted in one pass after the reorder has been decided.
+// A path whose active list would exceed kRegMaxM edges is not swept here
+// (RegWalk returns 0 before touching its sink's output for the first time
+// at that size) and goes to LaneSweep.
+#pragma once
+#include "sweep.cuh"
+
+namespace skc {
+
+constexpr int kRegMaxM = 128;  // active edges held in registers
+
+// Per-warp shared block of the register sweep.
+struct RegShared {
+  int32_t xo[kRegMaxM];   // x before the step, by list position
+  int32_t xg[kRegMaxM];   //   after GoY
+  int32_t xf[kRegMaxM];   //   after the quad-piece update
+  int32_t dxo[kRegMaxM];  // dx before the step
+  int32_t dyo[kRegMaxM];  // dy before the step
+  int32_t dxf[kRegMaxM];  // dx after the update
+  int32_t ia[kRegMaxM];   // interval k: left position
+  int32_t ib[kRegMaxM];   //   right position
+  int32_t ax[kRegMaxM];   // active x at insertion time
+  // edge state by new list position (reorder and insertion)
+  int32_t p_idx[kRegMaxM], p_x[kRegMaxM], p_dx[kRegMaxM], p_dy[kRegMaxM];
+  int32_t p_low[kRegMaxM], p_wc[kRegMaxM];
+  uint8_t surv[kRegMaxM];  // 1: survives the step
+};
+
+SKC_HD int32_t MakeWc(int winding, int count) { return (winding & 0xFF) | ((count & 0xFF) << 8); }
+SKC_HD int WcWinding(int32_t wc) { return (int8_t)(wc & 0xFF); }
+SKC_HD int WcCount(int32_t wc) { return (int8_t)((wc >> 8) & 0xFF); }
+
+SKC_HD long long LaneMax64(const Lanes& L, long long v) {
+#ifdef __CUDA_ARCH__
+  for (int o = 16; o > 0; o >>= 1) {
+    long long t = __shfl_xor_sync(0xffffffffu, v, o);
+    v = t > v ? t : v;
+  }
+#endif
+  return v;
+}
+
+// Row accumulator of the sweep (the difference array and its touched range).
+struct AccState {
+  int32_t* diff;
+  int left, width;
+  int y;       // row being accumulated (kNaN32: none yet)
+  int lo, hi;  // touched entries [lo, hi]
+};
+
+template <typename Sink>
+SKC_HD void AccFlush(const Lanes& L, AccState& a, Sink* sink) {
+  if (a.y == kNaN32) return;
+  if (a.lo <= a.hi) {
+    const bool read = sink->acc_row(L, a.y, a.diff, a.left, a.lo, a.hi);
+    L.sync();
+    if (read) {
+      if (L.leader()) a.diff[a.hi] = 0;
+    } else {
+      for (int i = a.lo + L.lane; i <= a.hi; i += Lanes::n) a.diff[i] = 0;
+    }
+    L.sync();
+  }
+  a.lo = 0x7fffffff;
+  a.hi = -1;
+}
+
+template <typename Sink>
+SKC_HD void AccFlushIfNeed(const Lanes& L, AccState& a, Sink* sink, int row) {
+  if (a.y == row) return;
+  if (a.y != kNaN32) AccFlush(L, a, sink);
+  a.y = row;
+}
+
+// Lane-local output of one interval's trapezoid row.
+template <typename Sink>
+struct RegOut {
+  Sink* sink;
+  AccState* as;
+  int y;
+  bool do_acc;
+  uint32_t kept;
+  unsigned long long frags;
+  uint2* write;
+  int lo, hi;
+  SKC_HD void real(int x, int len, uint8_t a) {
+    if (!sink->keep(x, y, len, a)) return;
+    kept++;
+    frags += (unsigned)len;
+    if (write) *write++ = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+  }
+  SKC_HD void acc(int x, int len, uint8_t a) {
+    if (!do_acc) return;
+    int o0 = x - as->left, o1 = o0 + len;
+    o0 = max_(o0, 0);
+    o1 = min_(o1, as->width);
+    if (o0 >= o1) return;
+    lo = min_(lo, o0);
+    hi = max_(hi, o1);
+    if (a == 0) return;
+    AtomicAddI32(&as->diff[o0], (int32_t)a);
+    AtomicAddI32(&as->diff[o1], -(int32_t)a);
+  }
+};
+
+// The intervals [0, K) of a step, then (trailing_a >= 0) the interval left
+// open by the last left edge: blit_trapezoid_row for each, one interval per
+// lane, direct spans written in interval order.
+template <typename Sink>
+SKC_HD void RegBlit(const Lanes& L, const RegShared& sh, Sink* sink, AccState& as, const Edge* W,
+                    int n, int y, Fixed next_y, int K, int m, int k, uint8_t full,
+                    Fixed left_clip, Fixed right_clip, int trailing_a, bool trailing_nr) {
+  const int total = K + (trailing_a >= 0 ? 1 : 0);
+  AccFlushIfNeed(L, as, sink, y);
+  const bool emit = Sink::kEmit;
+  const uint32_t base = emit ? sink->row_cursor(y) : 0;
+  uint32_t run = 0;
+  unsigned long long frags = 0;
+  int lo = 0x7fffffff, hi = -1;
+  for (int kb = 0; kb < total; kb += Lanes::n) {
+    const int ki = kb + L.lane;
+    const bool valid = ki < total;
+    Fixed ul = 0, ur = 0, ll = 0, lr = 0, lDY = 0, rDY = 0;
+    bool nr = false;
+    if (valid) {
+      if (ki < K) {
+        const int a = sh.ia[ki], b = sh.ib[ki];
+        ul = max_(sh.xo[a], left_clip);
+        lDY = sh.dyo[a];
+        ur = min_(right_clip, sh.xo[b]);
+        ll = max_(left_clip, sh.xf[a]);
+        lr = min_(right_clip, sh.xg[b]);
+        rDY = sh.dyo[b];
+        int prev_right;
+        if (ki == 0) {
+          prev_right = FixedFloorToInt(left_clip);
+        } else {
+          const int pb = sh.ib[ki - 1];
+          prev_right = FixedCeilToInt(max_(min_(right_clip, sh.xo[pb]), sh.xg[pb]));
+        }
+        bool tc = prev_right > FixedFloorToInt(ul) || prev_right > FixedFloorToInt(sh.xf[a]);
+        if (!tc) {
+          // edges_too_close(right edge, its successor before the step)
+          int32_t nxo, ndx;
+          Fixed nup;
+          if (b + 1 < m) {
+            nxo = sh.xo[b + 1];
+            ndx = sh.dxo[b + 1];
+            nup = kMinS32;  // active: upper_y <= y < next_y
+          } else if (k < n) {
+            nxo = W[k].x;
+            ndx = W[k].dx;
+            nup = W[k].upper_y;
+          } else {
+            nxo = kMaxS32;
+            ndx = 0;
+            nup = kMaxS32;
+          }
+          tc = nup < next_y && wadd(sh.xg[b], kFixed1) >= wsub(nxo, iabs_(ndx));
+        }
+        nr = tc;
+      } else {
+        const int a = trailing_a;
+        ul = max_(sh.xo[a], left_clip);
+        lDY = sh.dyo[a];
+        ur = right_clip;
+        ll = max_(left_clip, sh.xf[a]);
+        lr = right_clip;
+        rDY = 0;
+        nr = trailing_nr;
+      }
+    }
+    RegOut<Sink> o;
+    o.sink = sink;
+    o.as = &as;
+    o.y = y;
+    o.do_acc = true;
+    o.kept = 0;
+    o.frags = 0;
+    o.write = nullptr;
+    o.lo = 0x7fffffff;
+    o.hi = -1;
+    if (valid) TrapezoidRow(o, ul, ur, ll, lr, lDY, rDY, full, nr);
+    lo = min_(lo, o.lo);
+    hi = max_(hi, o.hi);
+    if (emit) {
+      const int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
+      const uint32_t mine = base + run + (uint32_t)(incl - (int32_t)o.kept);
+      const int32_t chunk_total = LaneBcast(L, incl, Lanes::n - 1);
+      if (valid && o.kept && sink->in_range(mine, o.kept)) {
+        RegOut<Sink> w = o;
+        w.do_acc = false;
+        w.kept = 0;
+        w.frags = 0;
+        w.write = sink->span_ptr(mine);
+        TrapezoidRow(w, ul, ur, ll, lr, lDY, rDY, full, nr);
+      }
+      run += (uint32_t)chunk_total;
+    } else {
+      run += (uint32_t)LaneSum64(L, o.kept);
+    }
+    frags += o.frags;
+  }
+  frags = LaneSum64(L, frags);
+  lo = LaneMin(L, lo);
+  hi = LaneMax(L, hi);
+  if (lo <= hi) {
+    as.lo = min_(as.lo, lo);
+    as.hi = max_(as.hi, hi);
+  }
+  sink->step_done(L, y, run, frags);
+  L.sync();
+}
+
+// WalkEdges over the pass's sorted edges W[0, n) (modified in place: quad
+// pieces).  Returns 0 if the active list would exceed kRegMaxM edges.
+template <typename Sink>
+SKC_HD int RegWalk(const Lanes& L, RegShared& sh, Edge* W, int n, Sink* sink, AccState& as,
+                   float scan_top, bool even_odd, int start_y, int stop_y, Fixed left_clip,
+                   Fixed right_clip) {
+  constexpr int NL = Lanes::n;
+  constexpr int S = kRegMaxM / NL;
+  constexpr unsigned kFull = NL == 32 ? 0xffffffffu : 1u;
+  const int winding_mask = even_odd ? 1 : -1;
+  int32_t r_idx[S], r_x[S], r_dx[S], r_dy[S], r_low[S], r_wc[S];
+
+  Fixed y = max_(W[0].upper_y, IntToFixed(start_y));
+  // initial activation: the edges with upper_y <= y, in their sorted order
+  int k = 0;
+  for (int base = 0; base < n; base += NL) {
+    const int i = base + L.lane;
+    const unsigned mask = L.ballot(i < n && W[i].upper_y <= y);
+    k += Lanes::popc(mask);
+    if (mask != kFull) break;
+  }
+  if (k > kRegMaxM) return 0;
+  int m = k;
+  Fixed nny = kMaxS32;
+  {
+    int32_t lmin = kMaxS32;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int p = s * NL + L.lane;
+      r_idx[s] = r_x[s] = r_dx[s] = r_dy[s] = r_low[s] = r_wc[s] = 0;
+      if (p < m) {
+        Edge e = W[p];
+        GoY(&e, y);
+        r_idx[s] = p;
+        r_x[s] = e.x;
+        r_dx[s] = e.dx;
+        r_dy[s] = e.dy;
+        r_low[s] = e.lower_y;
+        r_wc[s] = MakeWc(e.winding, e.curve_count);
+        if (e.lower_y > y) lmin = min_(lmin, e.lower_y);
+      }
+    }
+    lmin = LaneMin(L, lmin);
+    nny = min_(nny, lmin);
+    if (k < n && W[k].upper_y > y) nny = min_(nny, W[k].upper_y);
+  }
+
+  for (;;) {
+    Fixed next_y = min_(nny, FixedCeilToFixed(y + 1));
+    int y_shift = 0;
+    if ((next_y - y) & (kFixed1 >> 2)) {
+      y_shift = 2;
+      next_y = y + (kFixed1 >> 2);
+    } else if ((next_y - y) & (kFixed1 >> 1)) {
+      y_shift = 1;
+    }
+    const uint8_t full = partial_alpha_h(0xFF, next_y - y);
+    nny = kMaxS32;
+    const int ns = (m + NL - 1) / NL;
+
+    // ---- A: advance every active edge
+    int32_t wcarry = 0;
+    int nl = 0, nr = 0;
+    unsigned smask[S];
+    int32_t lmin = kMaxS32;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      smask[s] = 0;
+      if (s < ns) {
+        const int p = s * NL + L.lane;
+        const bool valid = p < m;
+        const int32_t wv = valid ? (int32_t)WcWinding(r_wc[s]) : 0;
+        const int32_t incl = LaneScanIncl(L, wv) + wcarry;
+        const int32_t excl = incl - wv;
+        const bool in = (incl & winding_mask) != 0;
+        const bool pin = (excl & winding_mask) != 0;
+        const bool is_left = valid && in && !pin;
+        const bool is_right = valid && !in && pin;
+        const unsigned lm = L.ballot(is_left), rm = L.ballot(is_right);
+        bool surv = false;
+        if (valid) {
+          const int32_t xo = r_x[s], dxo = r_dx[s], dyo = r_dy[s];
+          int32_t x = wadd(xo, dxo >> y_shift);  // GoYShift
+          const int32_t xg = x;
+          if (r_low[s] <= next_y && WcCount(r_wc[s]) > 0) {
+            Edge e = W[r_idx[s]];
+            e.x = x;
+            e.y = next_y;
+            e.dx = dxo;
+            e.dy = dyo;
+            e.lower_y = r_low[s];
+            e.winding = (int8_t)WcWinding(r_wc[s]);
+            e.curve_count = (int8_t)WcCount(r_wc[s]);
+            while (e.lower_y <= next_y && e.curve_count > 0) {
+              e.snapped_x = e.x;  // KeepContinuous (sw_edge.cc:294-297)
+              e.snapped_y = e.y;
+              if (!UpdateQuad(&e)) break;
+            }
+            W[r_idx[s]] = e;
+            x = e.x;
+            r_dx[s] = e.dx;
+            r_dy[s] = e.dy;
+            r_low[s] = e.lower_y;
+            r_wc[s] = MakeWc(e.winding, e.curve_count);
+          }
+          r_x[s] = x;
+          surv = r_low[s] > next_y;
+          if (surv) lmin = min_(lmin, r_low[s]);
+          sh.xo[p] = xo;
+          sh.xg[p] = xg;
+          sh.xf[p] = x;
+          sh.dxo[p] = dxo;
+          sh.dyo[p] = dyo;
+          sh.dxf[p] = r_dx[s];
+          sh.surv[p] = surv ? 1 : 0;
+          if (is_left) sh.ia[nl + Lanes::popc(lm & L.lt_mask())] = p;
+          if (is_right) sh.ib[nr + Lanes::popc(rm & L.lt_mask())] = p;
+        }
+        smask[s] = L.ballot(surv);
+        nl += Lanes::popc(lm);
+        nr += Lanes::popc(rm);
+        wcarry = LaneBcast(L, incl, min_(NL, m - s * NL) - 1);
+      }
+    }
+    const bool final_in = (wcarry & winding_mask) != 0;
+    L.sync();
+
+    // ---- C: survivors in stable order of their new x; intersections
+    int m2 = 0;
+    int r_rank[S];
+    bool cross = false, inv = false;
+    {
+      int last = -1, before = 0;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        r_rank[s] = 0;
+        if (s < ns) {
+          const unsigned below = smask[s] & L.lt_mask();
+          const bool surv = (smask[s] >> (NL == 32 ? L.lane : 0)) & 1u;
+          const int q = below ? s * NL + (31 - clz_(below)) : last;
+          r_rank[s] = before + Lanes::popc(below);
+          if (surv && q >= 0) {
+            const int32_t xq = sh.xf[q];
+            if (xq > r_x[s]) inv = true;
+            if (wadd(xq, sh.dxf[q]) > wadd(r_x[s], r_dx[s])) cross = true;
+          }
+          before += Lanes::popc(smask[s]);
+          if (smask[s]) last = s * NL + (31 - clz_(smask[s]));
+        }
+      }
+      m2 = before;
+    }
+    if (L.ballot(inv)) {
+      // some survivor moves: rank = stable position by new x; the intersection
+      // check compares with the last earlier survivor whose x is not greater
+      int32_t bestx[S];
+      int best[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        r_rank[s] = 0;
+        best[s] = -1;
+        bestx[s] = 0;
+      }
+      for (int i = 0; i < m; ++i) {
+        if (!sh.surv[i]) continue;
+        const int32_t xi = sh.xf[i];
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const int p = s * NL + L.lane;
+          const int32_t xj = r_x[s];
+          if (xi < xj || (xi == xj && i < p)) r_rank[s]++;
+          if (i < p && xi <= xj && (best[s] < 0 || xi >= bestx[s])) {
+            best[s] = i;
+            bestx[s] = xi;
+          }
+        }
+      }
+      cross = false;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (s < ns && p < m && sh.surv[p] && best[s] >= 0 &&
+            wadd(bestx[s], sh.dxf[best[s]]) > wadd(r_x[s], r_dx[s]))
+          cross = true;
+      }
+    }
+    lmin = LaneMin(L, lmin);
+    nny = min_(nny, lmin);
+    if (L.ballot(cross)) nny = min_(nny, next_y + (kFixed1 >> kAccuracy));
+
+    // ---- the interval left open by the last left edge (its right edge was
+    // culled): too-close test against the left edge's predecessor after the
+    // reorder (its new predecessor if it survives, else the last processed
+    // survivor before it)
+    int trailing_a = -1;
+    bool trailing_nr = false;
+    if (final_in) {
+      const int a = sh.ia[nr];
+      const bool a_surv = sh.surv[a] != 0;
+      const int32_t xa = sh.xf[a];
+      long long key = 0;
+      bool found = false;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (s < ns && p < m && sh.surv[p]) {
+          const int32_t xi = r_x[s];
+          const bool cand = a_surv ? (p != a && (xi < xa || (xi == xa && p < a))) : p < a;
+          if (cand) {
+            const long long kk = ((long long)xi << 32) | (unsigned)p;
+            if (!found || kk > key) key = kk;
+            found = true;
+          }
+        }
+      }
+      const bool any = L.ballot(found) != 0;
+      if (!found) key = (long long)kMinS32 << 32;
+      key = LaneMax64(L, key);
+      const int32_t pred_x = any ? (int32_t)(key >> 32) : left_clip;
+      const bool tc = wadd(pred_x, kFixed1) >= wsub(xa, iabs_(sh.dxf[a]));
+      trailing_a = a;
+      trailing_nr = full == 0xFF && tc;
+    }
+
+    // ---- B: coverage of the step's intervals, in list order
+    const int row = y >> 16;
+    if (nr + (final_in ? 1 : 0) > 0 && !(row < scan_top)) {
+      RegBlit(L, sh, sink, as, W, n, row, next_y, nr, m, k, full, left_clip, right_clip,
+              trailing_a, trailing_nr);
+    }
+
+    // ---- reorder the survivors into the new list
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int p = s * NL + L.lane;
+      if (s < ns && ((smask[s] >> (NL == 32 ? L.lane : 0)) & 1u)) {
+        const int r = r_rank[s];
+        sh.p_idx[r] = r_idx[s];
+        sh.p_x[r] = r_x[s];
+        sh.p_dx[r] = r_dx[s];
+        sh.p_dy[r] = r_dy[s];
+        sh.p_low[r] = r_low[s];
+        sh.p_wc[r] = r_wc[s];
+      }
+      (void)p;
+    }
+    L.sync();
+    m = m2;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int p = s * NL + L.lane;
+      if (p < m) {
+        r_idx[s] = sh.p_idx[p];
+        r_x[s] = sh.p_x[p];
+        r_dx[s] = sh.p_dx[p];
+        r_dy[s] = sh.p_dy[p];
+        r_low[s] = sh.p_low[p];
+        r_wc[s] = sh.p_wc[p];
+      }
+    }
+    L.sync();
+    y = next_y;
+    if (y >= IntToFixed(stop_y)) break;
+
+    // ---- D: insert_new_edges (sw_raster.cc:207-247) as a merge
+    if (k < n && W[k].upper_y <= y) {
+      int c = 0;
+      for (int base = k; base < n; base += NL) {
+        const int i = base + L.lane;
+        const unsigned mask = L.ballot(i < n && W[i].upper_y <= y);
+        c += Lanes::popc(mask);
+        if (mask != kFull) break;
+      }
+      if (m + c > kRegMaxM) return 0;
+      const int32_t x0 = W[k].x;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (p < m) sh.ax[p] = r_x[s];
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (p < m) {
+          const int32_t xa = r_x[s];
+          int before = 0;
+          if (xa > x0) {
+            before = 1;
+            for (int t = 1; t < c; ++t) before += W[k + t].x <= xa ? 1 : 0;
+          }
+          const int np = p + before;
+          sh.p_idx[np] = r_idx[s];
+          sh.p_x[np] = r_x[s];
+          sh.p_dx[np] = r_dx[s];
+          sh.p_dy[np] = r_dy[s];
+          sh.p_low[np] = r_low[s];
+          sh.p_wc[np] = r_wc[s];
+        }
+      }
+      L.sync();
+      int32_t lmin2 = kMaxS32;
+      for (int tb = 0; tb < c; tb += NL) {
+        const int t = tb + L.lane;
+        if (t < c) {
+          const Edge e = W[k + t];
+          const int32_t xt = e.x;
+          int cnt = 0;
+          for (int i = 0; i < m; ++i) {
+            const int32_t xa = sh.ax[i];
+            cnt += (xa <= x0 || (t >= 1 && xa < xt)) ? 1 : 0;
+          }
+          const int np = t + cnt;
+          sh.p_idx[np] = k + t;
+          sh.p_x[np] = e.x;
+          sh.p_dx[np] = e.dx;
+          sh.p_dy[np] = e.dy;
+          sh.p_low[np] = e.lower_y;
+          sh.p_wc[np] = MakeWc(e.winding, e.curve_count);
+          if (e.lower_y > y) lmin2 = min_(lmin2, e.lower_y);
+        }
+      }
+      L.sync();
+      const int mm = m + c;
+      bool cross2 = false;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (p < mm) {
+          r_idx[s] = sh.p_idx[p];
+          r_x[s] = sh.p_x[p];
+          r_dx[s] = sh.p_dx[p];
+          r_dy[s] = sh.p_dy[p];
+          r_low[s] = sh.p_low[p];
+          r_wc[s] = sh.p_wc[p];
+          if (r_idx[s] >= k && p > 0 &&
+              wadd(sh.p_x[p - 1], sh.p_dx[p - 1]) > wadd(r_x[s], r_dx[s]))
+            cross2 = true;
+        }
+      }
+      L.sync();
+      lmin2 = LaneMin(L, lmin2);
+      nny = min_(nny, lmin2);
+      if (L.ballot(cross2)) nny = min_(nny, y + (kFixed1 >> kAccuracy));
+      m = mm;
+      k += c;
+    }
+    if (k < n && W[k].upper_y > y) nny = min_(nny, W[k].upper_y);
+  }
+  return 1;
+}
+
+}  // namespace skc

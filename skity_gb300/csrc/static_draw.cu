@@ -53,6 +53,7 @@ struct StaticDesc {  // the descriptor block at the start of the scratch
   PassComp comp;
   uint32_t err;
   uint32_t pass_spans[2];
+  uint32_t pass_class;
 };
 static_assert(sizeof(StaticDesc) <= kDescBytes, "descriptor block");
 static_assert(sizeof(P) == 8, "points are copied as float pairs");
@@ -140,6 +141,7 @@ int32_t StaticPass(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   b.err = &dev->err;
   b.comp = &dev->comp;
   b.brushes = &dev->brush;
+  b.pass_class = (uint8_t*)&dev->pass_class;
   b.pixels = pixels;
   b.n_list = 1;
   {
@@ -185,6 +187,8 @@ int32_t StaticPass(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   const uint64_t spans_off = Align256(rows_off + 4ull * ((uint64_t)nrows + 1));
   if (spans_off > kStaticScratchBytes) return SKITY_CUDA_ERROR_SCRATCH_LIMIT;
   b.sweepmem = base + sweep_off;
+  b.reg_diff_cap = std::max<int32_t>(
+      4, std::min<int32_t>(((g.acc_width > 0 ? g.acc_width : 0) + 1 + 3) & ~3, kRegDiffMax));
   b.rowtab = (uint32_t*)(base + rows_off);
   b.spans = (uint2*)(base + spans_off);
   const uint64_t span_cap = (kStaticScratchBytes - spans_off) / sizeof(uint2);
@@ -198,6 +202,7 @@ int32_t StaticPass(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   // the count pass adds into the row table; the self-check flag starts clear
   if (e == cudaSuccess) e = cudaMemsetAsync(b.rowtab, 0, 4ull * ((uint64_t)nrows + 1), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(&dev->err, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->pass_class, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return Err(e);
   LaunchSweep(b, false, st);
   uint32_t spans = 0;

@@ -81,37 +81,67 @@ SKC_HD void AtomicAddI32(int32_t* p, int32_t v) {
 // Runs of equal nonzero saturated sums of diff[lo, hi) (prefix sums,
 // min 255), in increasing x; emit(start, width, alpha) is called
 // warp-uniformly, one call per run (SpanBuilder::Flush, sw_raster.cc:103-136).
+// Each lane takes V consecutive entries per chunk; every entry read is reset
+// to zero, so the accumulator is clean for the next row except diff[hi].
 template <typename F>
-SKC_HD void DiffRuns(const Lanes& L, const int32_t* diff, int lo, int hi, F&& emit) {
+SKC_HD void DiffRuns(const Lanes& L, int32_t* diff, int lo, int hi, F&& emit) {
+  constexpr int V = Lanes::n == 32 ? 4 : 1;
   int open_start = -1;
   int32_t open_v = 0;
   int32_t carry = 0;      // prefix sum before this chunk
-  int32_t prev_sat = 0;   // saturated value of the pixel before this chunk
-  for (int base = lo; base < hi; base += Lanes::n) {
-    int i = base + L.lane;
-    int32_t d = i < hi ? diff[i] : 0;
-    int32_t v = LaneScanIncl(L, d) + carry;
-    int32_t sat = v > 255 ? 255 : v;
-    int32_t before = LaneBcast(L, sat, L.lane > 0 ? L.lane - 1 : 0);
-    if (L.lane == 0) before = prev_sat;
-    unsigned mask = L.ballot(i < hi && sat != before);
-    int cnt = min_(Lanes::n, hi - base);
-    while (mask) {
-      int bit = Lanes::ffs(mask) - 1;
-      mask &= mask - 1;
-      int pos = base + bit;
-      int32_t bv = LaneBcast(L, sat, bit);
-      if (open_start >= 0) {
-        emit(open_start, pos - open_start, (uint8_t)open_v);
-        open_start = -1;
+  int32_t prev_sat = 0;   // saturated value of the entry before this chunk
+  for (int base = lo; base < hi; base += Lanes::n * V) {
+    const int i0 = base + L.lane * V;
+    int32_t sat[V];
+    int32_t run = 0;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      int32_t d = 0;
+      if (i0 + j < hi) {
+        d = diff[i0 + j];
+        diff[i0 + j] = 0;
       }
-      if (bv != 0) {
-        open_start = pos;
-        open_v = bv;
+      run += d;
+      sat[j] = run;
+    }
+    const int32_t incl = LaneScanIncl(L, run);
+    const int32_t pre = incl - run + carry;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      const int32_t v = sat[j] + pre;
+      sat[j] = v > 255 ? 255 : v;
+    }
+    int32_t before = LaneBcast(L, sat[V - 1], L.lane > 0 ? L.lane - 1 : 0);
+    if (L.lane == 0) before = prev_sat;
+    unsigned bits = 0;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      const int32_t b = j == 0 ? before : sat[j - 1];
+      if (i0 + j < hi && sat[j] != b) bits |= 1u << j;
+    }
+    unsigned mask = L.ballot(bits != 0);
+    while (mask) {
+      const int src = Lanes::ffs(mask) - 1;
+      mask &= mask - 1;
+      const unsigned sb = (unsigned)LaneBcast(L, (int32_t)bits, src);
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        const int32_t bv = LaneBcast(L, sat[j], src);
+        if (sb & (1u << j)) {
+          const int pos = base + src * V + j;
+          if (open_start >= 0) {
+            emit(open_start, pos - open_start, (uint8_t)open_v);
+            open_start = -1;
+          }
+          if (bv != 0) {
+            open_start = pos;
+            open_v = bv;
+          }
+        }
       }
     }
-    carry = LaneBcast(L, v, cnt - 1);
-    prev_sat = LaneBcast(L, sat, cnt - 1);
+    carry += LaneBcast(L, incl, Lanes::n - 1);
+    prev_sat = LaneBcast(L, sat[V - 1], Lanes::n - 1);
   }
   if (open_start >= 0) emit(open_start, hi - open_start, (uint8_t)open_v);
 }

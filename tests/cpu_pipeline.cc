@@ -14,8 +14,10 @@
 
 using namespace skc;
 
-extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rgba,
-                              uint64_t stats[6]) {
+// mode 0: register sweep with the generic sweep for passes it gives up on
+// (the GPU pipeline's choice); mode 1: generic sweep for every pass.
+extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* out_rgba,
+                                   uint64_t stats[6], int mode) {
   StreamView sv;
   if (!ParseStream(stream, len, &sv)) return -2;
   HostBatch hb;
@@ -80,13 +82,29 @@ extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rg
   b.rowtab = rowtab.data();
   b.pass_spans = pass_spans.data();
   Lanes lanes;
-  for (uint32_t p = 0; p < np; ++p) SweepCountPass(b, p, lanes);
+  std::vector<uint8_t> pclass(np + 1, mode == 1 ? 1 : 0);
+  b.pass_class = pclass.data();
+  b.reg_diff_cap = RegDiffCap(pl);
+  std::vector<int32_t> regmem((RegSmemBytes(b.reg_diff_cap) + 3) / 4);
+  RegShared* sh = (RegShared*)regmem.data();
+  int32_t* sdiff = (int32_t*)((uint8_t*)regmem.data() + sizeof(RegShared));
+  uint64_t generic = 0;
+  for (uint32_t p = 0; p < np; ++p) {
+    if (pclass[p] == 0) SweepCountPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+    if (pclass[p] == 1) {
+      SweepCountPass(b, p, lanes, true);
+      generic++;
+    }
+  }
   std::vector<PassComp> comp;
   uint64_t spans = PlanComp(hb, geom, sw, pass_spans, comp);
   std::vector<uint2> span_buf(spans + 1);
   b.comp = comp.data();
   b.spans = span_buf.data();
-  for (uint32_t p = 0; p < np; ++p) SweepEmitPass(b, p, lanes);
+  for (uint32_t p = 0; p < np; ++p) {
+    if (pclass[p] == 0) SweepEmitPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+    else SweepEmitPass(b, p, lanes);
+  }
   b.brushes = hb.brushes.data();
   b.stop_colors = hb.stop_colors.data();
   b.stop_offsets = hb.stop_offsets.data();
@@ -126,9 +144,14 @@ extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rg
     stats[2] = spans;
     stats[3] = retries;
     stats[4] = hb.temp_canvases.size();
-    stats[5] = hb.draw_count;
+    stats[5] = generic;
   }
   return 0;
+}
+
+extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rgba,
+                              uint64_t stats[6]) {
+  return skc_cpu_render_mode(stream, len, out_rgba, stats, 0);
 }
 
 // The device introsort on an arbitrary key array, for the permutation test

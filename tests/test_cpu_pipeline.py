@@ -9,11 +9,13 @@ import pytest
 from skity_gb300 import scene as S
 
 
-def cpu_render(lib, sc):
+def cpu_render(lib, sc, mode=0):
+    """mode 0: register sweep (generic sweep for passes it gives up on), as
+    the GPU pipeline runs it; mode 1: generic sweep for every pass."""
     b = sc.to_bytes()
     out = np.zeros((sc.height, sc.width, 4), np.uint8)
     st = (ctypes.c_uint64 * 6)()
-    rc = lib.skc_cpu_render(b, len(b), out.ctypes.data, st)
+    rc = lib.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, mode)
     assert rc == 0, rc
     return out, list(st)
 
@@ -86,3 +88,41 @@ def test_edge_cases_bit_exact(cpu_pipeline, oracle_lib):
     got, _ = cpu_render(cpu_pipeline, sc)
     ref, _ = oracle_lib.render(sc)
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+def _stripes(b, paint, n, x0, y0s, w, h):
+    verbs, pts = [], []
+    for i in range(n):
+        x, y = x0 + 2.5 * i, y0s[i]
+        verbs += [S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE]
+        pts += [(x, y), (x + w, y + 0.3), (x + w, y + h), (x, y + h - 0.4)]
+    b.draw_path(verbs, pts, paint)
+
+
+def test_long_active_lists_fall_back_to_generic_sweep(cpu_pipeline, oracle_lib):
+    """More active edges than the register sweep holds (128): at the first
+    step and at an insertion; a path just under the limit stays in it.
+    Both sweep forms must give the oracle's pixels."""
+    b = S.SceneBuilder(420, 140)
+    p = S.default_paint()
+    p["fill_color"] = (0.1, 0.5, 0.9, 0.7)
+    _stripes(b, p, 90, 3.0, [5.0] * 90, 1.7, 60.0)                        # 180 at once
+    _stripes(b, p, 90, 5.0, [70.0 + 0.25 * i for i in range(90)], 1.3, 50.0)  # grows past 128
+    q = p.copy()
+    q["fill_type"] = S.EVEN_ODD
+    _stripes(b, q, 62, 40.0, [30.0 + 0.5 * i for i in range(62)], 2.1, 70.0)  # 124 at most
+    sc = b.build()
+    ref, _ = oracle_lib.render(sc)
+    got, st = cpu_render(cpu_pipeline, sc)
+    assert st[5] == 2, st
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+    generic, st1 = cpu_render(cpu_pipeline, sc, mode=1)
+    assert st1[5] == 3
+    assert np.array_equal(got, generic)
+
+
+def test_register_and_generic_sweeps_agree(cpu_pipeline):
+    sc = S.config2(n_paths=60, width=384, height=384)
+    a, _ = cpu_render(cpu_pipeline, sc, 0)
+    g, _ = cpu_render(cpu_pipeline, sc, 1)
+    assert np.array_equal(a, g)
