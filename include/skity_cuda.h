@@ -123,12 +123,13 @@ typedef struct skity_cuda_stats {
   uint64_t spans;         /* coverage spans emitted inside the canvases */
   uint64_t pixels;        /* canvas pixels written back */
   uint64_t kernel_launches;
-  uint64_t retries;       /* scratch-capacity retries */
+  uint64_t retries;       /* scratch-capacity and span-pool retries */
   /* per-stage device time of the last render (CUDA events around each
    * stage's launches on the context stream) */
   double geometry_ms;     /* path -> quads -> stroke -> edges -> sort */
-  double sweep_count_ms;  /* AAA sweep, span counting */
-  double sweep_emit_ms;   /* AAA sweep, span writing */
+  double sweep_count_ms;  /* AAA sweeps discarded because the context's span
+                             pool had to grow (0 once it has grown) */
+  double sweep_emit_ms;   /* AAA sweep writing the spans */
   double composite_ms;    /* span replay, shading, blending */
   double blur_ms;         /* StackBlur of blur mask filter temp canvases */
   uint64_t fragments;     /* sum of span lengths inside the canvases */

@@ -505,9 +505,10 @@ inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv
 }
 
 
-// Per-pass sweep buffers and row tables from the geometry results.
+// Per-pass sweep buffers and row-span tables from the geometry results.
 struct SweepPlan {
   uint64_t sweep_bytes = 0, rows = 0, edges = 0;
+  uint64_t span_estimate = 0;  // first guess of the span pool size
   int32_t max_acc = 0;  // largest accumulator (acc_width + 1) of a swept pass
 };
 // Accumulator entries each register-sweep warp keeps in shared memory.
@@ -515,42 +516,51 @@ inline int32_t RegDiffCap(const SweepPlan& pl) {
   int32_t c = (pl.max_acc + 3) & ~3;
   return std::max<int32_t>(4, std::min<int32_t>(c, kRegDiffMax));
 }
-inline SweepPlan PlanSweep(const std::vector<PassGeom>& geom, std::vector<PassSweep>& sw) {
+// Spans per pool chunk for a pass: a power of two holding any one row of it.
+// A row has at most one direct span per pixel plus one per interval end and
+// one accumulated run per pixel: 2 * width + 2 * edges + 64 bounds it.
+inline uint32_t SpanChunk(uint32_t width, int32_t edges) {
+  uint64_t need = 2ull * width + 2ull * (uint64_t)std::max(edges, 0) + 64;
+  uint64_t c = 4096;
+  while (c < need) c <<= 1;
+  return (uint32_t)std::min<uint64_t>(c, 1ull << 31);
+}
+inline SweepPlan PlanSweep(const HostBatch& hb, const std::vector<PassGeom>& geom,
+                           std::vector<PassSweep>& sw) {
   SweepPlan pl;
   sw.assign(geom.size(), PassSweep{});
   for (size_t p = 0; p < geom.size(); ++p) {
     const PassGeom& g = geom[p];
+    const CanvasDesc& cd = hb.canvases[hb.passes[p].canvas];
     sw[p].work_off = pl.sweep_bytes;
     sw[p].rbase = (uint32_t)pl.rows;
-    if (g.n_edges > 0 && g.row1 > g.row0) {
+    sw[p].chunk = SpanChunk(cd.w, g.n_edges);
+    const int nr = g.row1 - g.row0;
+    if (g.n_edges > 0 && nr > 0) {
       uint64_t b = SweepMemBytes(g.n_edges, std::max(g.acc_width, 0));
       b = (b + 255) & ~uint64_t(255);
       sw[p].bytes = b;
       pl.sweep_bytes += b;
       pl.max_acc = std::max(pl.max_acc, std::max(g.acc_width, 0) + 1);
+      pl.span_estimate += (uint64_t)nr * 32 + sw[p].chunk;
     }
     if (g.n_edges > 0) pl.edges += (uint64_t)g.n_edges;
-    int nr = g.row1 - g.row0;
-    if (nr > 0) pl.rows += (uint64_t)nr + 1;
+    if (nr > 0) pl.rows += (uint64_t)nr;
   }
   return pl;
 }
-// Compositor inputs from the span counts; returns the total span count.
-inline uint64_t PlanComp(const HostBatch& hb, const std::vector<PassGeom>& geom,
-                         const std::vector<PassSweep>& sw, const std::vector<uint32_t>& pass_spans,
-                         std::vector<PassComp>& comp) {
+// Compositor inputs per pass.
+inline void PlanComp(const HostBatch& hb, const std::vector<PassGeom>& geom,
+                     const std::vector<PassSweep>& sw, std::vector<PassComp>& comp) {
   comp.assign(geom.size(), PassComp{});
-  uint64_t spans = 0;
   for (size_t p = 0; p < geom.size(); ++p) {
     const PassGeom& g = geom[p];
-    comp[p].row0 = g.row1 > g.row0 ? g.row0 : 0;
-    comp[p].row1 = g.row1 > g.row0 ? g.row1 : 0;
+    const bool has = g.n_edges > 0 && g.row1 > g.row0;
+    comp[p].row0 = has ? g.row0 : 0;
+    comp[p].row1 = has ? g.row1 : 0;
     comp[p].rbase = sw[p].rbase;
     comp[p].brush = hb.passes[p].brush;
-    comp[p].span_base = spans;
-    spans += pass_spans[p];
   }
-  return spans;
 }
 // Grow the capacities of a pass whose geometry overflowed.
 inline void GrowCaps(PassDesc& pd, const PassGeom& g) {

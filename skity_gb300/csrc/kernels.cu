@@ -3,9 +3,9 @@
 //   k_geometry   1 thread / pass : Path -> QuadPath (-> stroke -> QuadPath)
 //                                  -> fixed-point edges -> introsort
 //   k_sweep_*    1 warp / pass   : analytic-AA sweep (register form, generic
-//                                  form for very long active lists); count
-//                                  pass fills the per-row span counts, emit
-//                                  pass writes spans
+//                                  form for very long active lists) writing
+//                                  each row's spans contiguously into the
+//                                  span pool
 //   k_composite  1 warp / row     : replays every pass's spans of the row in
 //                                  draw order into a shared-memory row, then
 //                                  writes the row back (16-byte stores)
@@ -42,56 +42,39 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
 constexpr int kSweepWarps = 4;
 constexpr int kRegWarps = 2;
 
-__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_count_reg(DevBatch b) {
+__device__ __forceinline__ uint32_t DynamicSmemBytes() {
+  uint32_t v;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(v));
+  return v;
+}
+
+__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   const int w = threadIdx.x >> 5;
   const uint32_t p = blockIdx.x * kRegWarps + w;
   if (p >= b.n_passes) return;
+  if (DynamicSmemBytes() < kRegWarps * RegSmemBytes(b.reg_diff_cap)) {  // self-check
+    FlagError(b.err, 16);
+    return;
+  }
   Lanes L;
   L.lane = threadIdx.x & 31;
   uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes(b.reg_diff_cap);
-  SweepCountPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)),
-                    b.reg_diff_cap);
+  SweepPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)), b.reg_diff_cap);
 }
 
-__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_emit_reg(DevBatch b) {
-  extern __shared__ __align__(16) uint8_t reg_smem[];
-  const int w = threadIdx.x >> 5;
-  const uint32_t p = blockIdx.x * kRegWarps + w;
-  if (p >= b.n_passes || b.pass_class[p] != 0) return;
-  Lanes L;
-  L.lane = threadIdx.x & 31;
-  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes(b.reg_diff_cap);
-  SweepEmitPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)),
-                   b.reg_diff_cap);
-}
-
-__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_count(DevBatch b) {
+__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
   uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
   Lanes L;
   L.lane = threadIdx.x & 31;
-  if (p < b.n_passes && b.pass_class[p] == 1) SweepCountPass(b, p, L, true);
+  if (p < b.n_passes && b.pass_class[p] == 1) SweepPass(b, p, L);
 }
 
-__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_emit(DevBatch b) {
-  uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
-  Lanes L;
-  L.lane = threadIdx.x & 31;
-  if (p < b.n_passes && b.pass_class[p] == 1) SweepEmitPass(b, p, L);
-}
-
-int LaunchSweep(const DevBatch& b, bool emit, cudaStream_t stream) {
+int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
   const size_t smem = kRegWarps * RegSmemBytes(b.reg_diff_cap);
-  const unsigned rgrid = (b.n_passes + kRegWarps - 1) / kRegWarps;
-  const unsigned ggrid = (b.n_passes + kSweepWarps - 1) / kSweepWarps;
-  if (emit) {
-    k_sweep_emit_reg<<<rgrid, 32 * kRegWarps, smem, stream>>>(b);
-    k_sweep_emit<<<ggrid, 32 * kSweepWarps, 0, stream>>>(b);
-  } else {
-    k_sweep_count_reg<<<rgrid, 32 * kRegWarps, smem, stream>>>(b);
-    k_sweep_count<<<ggrid, 32 * kSweepWarps, 0, stream>>>(b);
-  }
+  k_sweep_reg<<<(b.n_passes + kRegWarps - 1) / kRegWarps, 32 * kRegWarps, smem, stream>>>(b);
+  k_sweep<<<(b.n_passes + kSweepWarps - 1) / kSweepWarps, 32 * kSweepWarps, 0, stream>>>(b);
   return 2;
 }
 
@@ -125,7 +108,6 @@ __global__ void __launch_bounds__(32 * kCompWarps)
     PassComp pc;
     pc.row0 = pc.row1 = 0;
     pc.rbase = pc.brush = 0;
-    pc.span_base = 0;
     if (p < cd.pass1) {
       pc = b.comp[p];
       hit = y >= pc.row0 && y < pc.row1;
@@ -137,13 +119,11 @@ __global__ void __launch_bounds__(32 * kCompWarps)
       const int32_t qrow0 = __shfl_sync(0xffffffffu, pc.row0, bit);
       const uint32_t qrbase = __shfl_sync(0xffffffffu, pc.rbase, bit);
       const uint32_t qbrush = __shfl_sync(0xffffffffu, pc.brush, bit);
-      const unsigned long long qbase =
-          __shfl_sync(0xffffffffu, (unsigned long long)pc.span_base, bit);
-      const uint32_t* rt_row = b.rowtab + qrbase + (y - qrow0);
-      const uint32_t s0 = rt_row[0], s1 = rt_row[1];
+      const uint2 rs = b.rowspan[qrbase + (y - qrow0)];
+      const uint32_t s0 = rs.x, s1 = rs.x + rs.y;
       if (s0 == s1) continue;
       const Brush br = b.brushes[qbrush];
-      const uint2* sp = b.spans + qbase;
+      const uint2* sp = b.spans;
       for (uint32_t sb = s0; sb < s1; sb += 32) {
         uint2 mine = make_uint2(0, 0);
         if (sb + lane < s1) mine = sp[sb + lane];

@@ -79,15 +79,14 @@ struct PassGeom {
 struct PassSweep {      // per-pass sweep buffers, set after geometry
   uint64_t work_off;    // byte offset of the pass's sweep memory
   uint64_t bytes;       // its size
-  uint32_t rbase;       // row table base (rows + 1 entries)
-  uint32_t pad;
+  uint32_t rbase;       // first entry of the pass's rows in the row-span table
+  uint32_t chunk;       // spans per span-pool chunk (any row of the pass fits)
 };
 
 struct PassComp {       // per-pass data the compositor reads
-  int32_t row0, row1;
+  int32_t row0, row1;   // canvas rows with row-span entries
   uint32_t rbase;
   uint32_t brush;
-  uint64_t span_base;
 };
 
 struct RowTask {
@@ -107,12 +106,14 @@ struct DevBatch {
   PassGeom* geom;
   const PassSweep* sweep;
   uint8_t* sweepmem;   // per-pass sweep memory (SweepMemAt)
-  uint32_t* rowtab;
+  uint2* rowspan;      // (first span, count) per pass row, zero when empty
   uint32_t* pass_spans;
   uint32_t* err;       // nonzero: a device self-check tripped (see pipeline)
   unsigned long long* pass_frags;  // fragments (clipped span pixels) per pass
   const PassComp* comp;
-  uint2* spans;
+  uint2* spans;        // span pool: x | len << 16, alpha
+  uint64_t span_cap;   // its capacity in spans
+  unsigned long long* span_next;  // pool chunk allocator
   const Brush* brushes;
   const float4* stop_colors;
   const float* stop_offsets;
@@ -132,7 +133,7 @@ constexpr int32_t kRegDiffMax = 3072;
 // kernel launchers (kernels.cu); all launch on `stream` and return the
 // number of launches made
 int LaunchGeometry(const DevBatch& b, cudaStream_t stream);
-int LaunchSweep(const DevBatch& b, bool emit, cudaStream_t stream);
+int LaunchSweep(const DevBatch& b, cudaStream_t stream);
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,
                     cudaStream_t stream);
 int LaunchBlur(const DevBatch& b, const uint32_t* temp_canvases, uint32_t n_temp,

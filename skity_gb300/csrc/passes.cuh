@@ -152,7 +152,7 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
 
 
 // ---------------------------------------------------------------------------
-// sweep: span sinks and the count / emit passes
+// sweep: the span sink and the sweep passes
 // ---------------------------------------------------------------------------
 // SWSpanBrush::Brush clipping (sw_span_brush.cc:78-99); false = dropped
 SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
@@ -166,9 +166,8 @@ SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
   return len > 0;
 }
 
-// Span sinks of the lane-parallel sweep.  keep() applies the clipping of
-// SWSpanBrush::Brush and drops spans whose alpha & global alpha is 0 under
-// src-over (they blend to nothing); counts and offsets are per canvas row.
+// keep() applies the clipping of SWSpanBrush::Brush and drops spans whose
+// alpha & global alpha is 0 under src-over (they blend to nothing).
 struct SinkBase {
   int row0, row1, W, H;
   uint32_t ga;
@@ -180,82 +179,139 @@ struct SinkBase {
   }
 };
 
-struct CountSink : SinkBase {
-  static constexpr bool kEmit = false;
-  uint32_t* rows;
-  unsigned long long frags;
-  SKC_HD uint32_t row_cursor(int) { return 0; }
-  SKC_HD uint2* span_ptr(uint32_t) { return nullptr; }
-  SKC_HD bool in_range(uint32_t, uint32_t) { return true; }
-  SKC_HD void step_done(const Lanes& L, int y, uint32_t n, unsigned long long f) {
-    if (n && y >= row0 && y < row1 && L.leader()) rows[y - row0] += n;
-    frags += f;
-  }
-  // Returns false when the row lies outside the canvas (diff not read).
-  SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
-    if (y < row0 || y >= row1) return false;
-    uint32_t n = 0;
-    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
-      int x = left + s, len = w;
-      if (keep(x, y, len, a)) {
-        n++;
-        frags += (unsigned)len;
-      }
-    });
-    if (n && L.leader()) rows[y - row0] += n;
-    return true;
-  }
-};
+SKC_HD unsigned long long LaneBcast64(const Lanes& L, unsigned long long v, int src) {
+#ifdef __CUDA_ARCH__
+  return __shfl_sync(0xffffffffu, v, src);
+#else
+  return v;
+#endif
+}
 
-struct EmitSink : SinkBase {
-  static constexpr bool kEmit = true;
-  uint2* spans;           // this pass's span range
-  const uint32_t* rows;   // exclusive offsets per row, rows+1 entries
-  uint32_t total;         // spans of this pass (rows[nrows]); writes past it
-  uint32_t* err;          //   are skipped and flagged (self-check)
-  uint2 sink_slot;        // harmless target for skipped writes
+// Spans go to one device-wide pool handed out in chunks of `chunk` spans.
+// A pass writes its rows one after another, each row contiguous -- a row
+// that would run past the end of its chunk is moved to a fresh chunk -- and
+// records (first span, count) per canvas row.  When the pool is exhausted
+// the pass keeps taking chunks but writes nothing, so the allocator ends at
+// the exact size the pass needs; the caller then sweeps again with a pool
+// that large.  All members are warp-uniform; methods are called by the
+// whole warp.
+struct PoolSink : SinkBase {
+  uint2* pool;
+  uint64_t cap;                // pool capacity in spans
+  unsigned long long* next;    // spans handed out so far
+  uint32_t chunk;              // spans per chunk (holds any row of the pass)
+  uint2* rows;                 // (first span, count) per row of [row0, row1)
+  uint32_t* err;
   int cur_row;
-  uint32_t cur;
-  SKC_HD uint32_t row_cursor(int y) {
-    if (y < row0 || y >= row1) return 0;
-    if (y != cur_row) {
-      cur_row = y;
-      cur = rows[y - row0];
+  uint64_t row_start, cur, chunk_end;
+  bool dead;
+  uint64_t kept;
+  unsigned long long frags;
+
+  SKC_HD void finish_row(const Lanes& L) {
+    if (!dead && cur > row_start && cur_row >= row0 && cur_row < row1 && L.leader())
+      rows[cur_row - row0] = make_uint2((uint32_t)row_start, (uint32_t)(cur - row_start));
+  }
+  SKC_HD void row_begin(const Lanes& L, int y) {
+    if (y == cur_row) return;
+    finish_row(L);
+    cur_row = y;
+    row_start = cur;
+  }
+  // Room for `add` more spans after the `written` spans this step already
+  // put at cur; returns cur (the row may have moved to a new chunk).
+  SKC_HD uint64_t reserve(const Lanes& L, uint32_t written, uint32_t add) {
+    if (cur + written + add <= chunk_end) return cur;
+    const uint64_t have = cur + written - row_start;
+    if (have + add > chunk) {  // a row larger than a chunk (not expected)
+      FlagError(err, 8);
+      dead = true;
     }
+    unsigned long long c = 0;
+    if (L.leader()) {
+#ifdef __CUDA_ARCH__
+      c = atomicAdd(next, (unsigned long long)chunk);
+#else
+      c = *next;
+      *next += chunk;
+#endif
+    }
+    c = LaneBcast64(L, c, 0);
+    if (c + chunk > cap) dead = true;
+    if (!dead) {
+      L.sync();
+      for (uint64_t i = L.lane; i < have; i += Lanes::n) pool[c + i] = pool[row_start + i];
+      L.sync();
+    }
+    cur = c + (cur - row_start);
+    row_start = c;
+    chunk_end = c + chunk;
     return cur;
   }
-  SKC_HD uint2* span_ptr(uint32_t i) { return spans + i; }
-  SKC_HD bool in_range(uint32_t i, uint32_t n) {
-    if ((uint64_t)i + n <= total) return true;
-    FlagError(err, 2);
-    return false;
-  }
-  SKC_HD void step_done(const Lanes&, int y, uint32_t n, unsigned long long) {
-    if (n && y == cur_row) cur += n;
+  SKC_HD uint2* span_ptr(uint64_t i) { return dead ? nullptr : pool + i; }
+  SKC_HD void commit(const Lanes&, uint32_t n, unsigned long long f) {
+    cur += n;
+    kept += n;
+    frags += f;
   }
   // The accumulated spans of a row follow its direct spans (the reference
-  // flushes a row's accumulator only after leaving the row): they continue
-  // at the row's cursor.  Returns false when the row lies outside the canvas.
+  // flushes a row's accumulator only after leaving the row).  Returns false
+  // when the row lies outside the canvas (diff not read).
   SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return false;
-    uint32_t o = y == cur_row ? cur : rows[y - row0];
-    const uint32_t end = rows[y - row0 + 1];
+    row_begin(L, y);
     DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
       int x = left + s, len = w;
       if (keep(x, y, len, a)) {
-        if (o < end && o < total) {
-          if (L.leader()) spans[o] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
-        } else {
-          FlagError(err, 2);
-        }
-        o++;
+        const uint64_t at = reserve(L, 0, 1);
+        if (!dead && L.leader()) pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        commit(L, 1, (unsigned)len);
       }
     });
-    if (o != end) FlagError(err, 2);
     return true;
   }
 };
 
+SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, PoolSink* s) {
+  const PassDesc pd = b.passes[p];
+  const PassSweep sw = b.sweep[p];
+  const CanvasDesc cd = b.canvases[pd.canvas];
+  s->row0 = g.row0;
+  s->row1 = g.row1;
+  s->W = (int)cd.w;
+  s->H = (int)cd.h;
+  s->ga = pd.ga;
+  s->srcover = (pd.flags & kPassSrcOver) != 0;
+  s->pool = b.spans;
+  s->cap = b.span_cap;
+  s->next = b.span_next;
+  s->chunk = sw.chunk;
+  s->rows = b.rowspan + sw.rbase;
+  s->err = b.err;
+  s->cur_row = kNaN32;
+  s->row_start = s->cur = s->chunk_end = 0;
+  s->dead = false;
+  s->kept = 0;
+  s->frags = 0;
+}
+
+SKC_HD void FinishPass(const DevBatch& b, uint32_t p, PoolSink* s, const Lanes& L) {
+  s->finish_row(L);
+  L.sync();
+  if (L.leader()) {
+    b.pass_spans[p] = (uint32_t)s->kept;
+    if (b.pass_frags) b.pass_frags[p] = s->frags;
+  }
+}
+
+SKC_HD void EmptyPass(const DevBatch& b, uint32_t p, const Lanes& L) {
+  if (L.leader()) {
+    b.pass_spans[p] = 0;
+    if (b.pass_frags) b.pass_frags[p] = 0;
+  }
+}
+
+// The generic sweep of pass p (LaneSweep, state in the pass's sweep memory).
 template <typename Sink>
 SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink,
                       const Lanes& lanes) {
@@ -319,150 +375,41 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
   return 1;
 }
 
-// Per-row counts -> exclusive offsets (rows + 1 entries), totals of the pass.
-SKC_HD void FinishCount(const DevBatch& b, uint32_t p, uint32_t* rows, int nrows,
-                        unsigned long long frags, const Lanes& lanes) {
-  lanes.sync();
-  if (!lanes.leader()) return;
-  if (b.pass_frags) b.pass_frags[p] = frags;
-  uint32_t run = 0;
-  for (int r = 0; r < nrows; ++r) {
-    uint32_t c = rows[r];
-    rows[r] = run;
-    run += c;
-  }
-  if (nrows > 0) rows[nrows] = run;
-  b.pass_spans[p] = run;
-}
-
-SKC_HD void InitCountSink(const DevBatch& b, uint32_t p, const PassGeom& g, uint32_t* rows,
-                          CountSink* sink) {
-  const PassDesc pd = b.passes[p];
-  const CanvasDesc cd = b.canvases[pd.canvas];
-  sink->rows = rows;
-  sink->row0 = g.row0;
-  sink->row1 = g.row1;
-  sink->W = (int)cd.w;
-  sink->H = (int)cd.h;
-  sink->ga = pd.ga;
-  sink->srcover = (pd.flags & kPassSrcOver) != 0;
-  sink->frags = 0;
-}
-
-// Count pass through the register sweep; a pass it cannot take is marked
-// for the generic sweep (pass_class 1) with its rows left for that pass.
-SKC_HD void SweepCountPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
-                              int32_t* sdiff, int32_t sdiff_cap) {
+// Sweep of pass p through the register sweep; a pass whose active list
+// outgrows it is marked for the generic sweep (pass_class 1).
+SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
+                         int32_t* sdiff, int32_t sdiff_cap) {
   const PassGeom g = b.geom[p];
-  const PassSweep sw = b.sweep[p];
-  uint32_t* rows = b.rowtab + sw.rbase;
-  const int nrows = g.row1 - g.row0;
-  unsigned long long frags = 0;
-  if (g.n_edges > 0 && nrows > 0) {
-    CountSink sink;
-    InitCountSink(b, p, g, rows, &sink);
-    if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
-      lanes.sync();
-      if (lanes.leader()) b.pass_class[p] = 1;
-      return;
-    }
-    frags = sink.frags;
+  if (g.n_edges <= 0 || g.row1 <= g.row0) {
+    EmptyPass(b, p, lanes);
+    return;
   }
-  FinishCount(b, p, rows, nrows, frags, lanes);
-}
-
-// Generic count pass; `zero_rows` clears the row counts first (a pass the
-// register sweep gave up on may have added to them).
-SKC_HDN void SweepCountPass(const DevBatch& b, uint32_t p, const Lanes& lanes,
-                            bool zero_rows = false) {
-  const PassGeom g = b.geom[p];
-  const PassSweep sw = b.sweep[p];
-  uint32_t* rows = b.rowtab + sw.rbase;
-  int nrows = g.row1 - g.row0;
-  unsigned long long frags = 0;
-  if (zero_rows) {
-    for (int r = lanes.lane; r <= nrows; r += Lanes::n) rows[r] = 0;
+  PoolSink sink;
+  InitPoolSink(b, p, g, &sink);
+  if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();
+    if (lanes.leader()) b.pass_class[p] = 1;
+    return;
   }
-  if (g.n_edges > 0 && nrows > 0) {
-    const PassDesc pd = b.passes[p];
-    const CanvasDesc cd = b.canvases[pd.canvas];
-    CountSink sink;
-    sink.rows = rows;
-    sink.row0 = g.row0;
-    sink.row1 = g.row1;
-    sink.W = (int)cd.w;
-    sink.H = (int)cd.h;
-    sink.ga = pd.ga;
-    sink.srcover = (pd.flags & kPassSrcOver) != 0;
-    sink.frags = 0;
-    RunSweep(b, p, g, &sink, lanes);
-    frags = sink.frags;
+  FinishPass(b, p, &sink, lanes);
+}
+
+// Sweep of pass p through the generic sweep.  Row entries a register attempt
+// may have written are cleared first.
+SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
+  const PassGeom g = b.geom[p];
+  const int nrows = g.row1 - g.row0;
+  if (g.n_edges <= 0 || nrows <= 0) {
+    EmptyPass(b, p, lanes);
+    return;
   }
+  uint2* rows = b.rowspan + b.sweep[p].rbase;
+  for (int r = lanes.lane; r < nrows; r += Lanes::n) rows[r] = make_uint2(0, 0);
   lanes.sync();
-  if (!lanes.leader()) return;
-  if (b.pass_frags) b.pass_frags[p] = frags;
-  uint32_t run = 0;
-  for (int r = 0; r < nrows; ++r) {
-    uint32_t c = rows[r];
-    rows[r] = run;
-    run += c;
-  }
-  if (nrows > 0) rows[nrows] = run;
-  b.pass_spans[p] = run;
-}
-
-SKC_HD void InitEmitSink(const DevBatch& b, uint32_t p, const PassGeom& g, EmitSink* sink) {
-  const PassDesc pd = b.passes[p];
-  const PassSweep sw = b.sweep[p];
-  const CanvasDesc cd = b.canvases[pd.canvas];
-  const int nrows = g.row1 - g.row0;
-  sink->spans = b.spans + b.comp[p].span_base;
-  sink->rows = b.rowtab + sw.rbase;
-  sink->row0 = g.row0;
-  sink->row1 = g.row1;
-  sink->W = (int)cd.w;
-  sink->H = (int)cd.h;
-  sink->ga = pd.ga;
-  sink->srcover = (pd.flags & kPassSrcOver) != 0;
-  sink->cur_row = -1;
-  sink->cur = 0;
-  sink->total = sink->rows[nrows];
-  sink->err = b.err;
-}
-
-SKC_HD void SweepEmitPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
-                             int32_t* sdiff, int32_t sdiff_cap) {
-  const PassGeom g = b.geom[p];
-  const int nrows = g.row1 - g.row0;
-  if (g.n_edges == 0 || nrows <= 0) return;
-  EmitSink sink;
-  InitEmitSink(b, p, g, &sink);
-  // the count pass took this pass through the register sweep, so it fits
-  if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) FlagError(b.err, 4);
-}
-
-SKC_HDN void SweepEmitPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
-  const PassGeom g = b.geom[p];
-  int nrows = g.row1 - g.row0;
-  if (g.n_edges == 0 || nrows <= 0) return;
-  const PassDesc pd = b.passes[p];
-  const PassSweep sw = b.sweep[p];
-  const CanvasDesc cd = b.canvases[pd.canvas];
-  EmitSink sink;
-  sink.spans = b.spans + b.comp[p].span_base;
-  sink.rows = b.rowtab + sw.rbase;
-  sink.row0 = g.row0;
-  sink.row1 = g.row1;
-  sink.W = (int)cd.w;
-  sink.H = (int)cd.h;
-  sink.ga = pd.ga;
-  sink.srcover = (pd.flags & kPassSrcOver) != 0;
-  sink.cur_row = -1;
-  sink.cur = 0;
-  sink.total = sink.rows[nrows];
-  sink.err = b.err;
+  PoolSink sink;
+  InitPoolSink(b, p, g, &sink);
   RunSweep(b, p, g, &sink, lanes);
+  FinishPass(b, p, &sink, lanes);
 }
 
 
@@ -534,10 +481,10 @@ SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* 
   for (uint32_t p = cd.pass0; p < cd.pass1; ++p) {
     const PassComp pc = b.comp[p];
     if (y < pc.row0 || y >= pc.row1) continue;
-    const uint32_t* rr = b.rowtab + pc.rbase + (y - pc.row0);
+    const uint2 rs = b.rowspan[pc.rbase + (y - pc.row0)];
     const Brush br = b.brushes[pc.brush];
-    for (uint32_t s = rr[0]; s < rr[1]; ++s) {
-      uint2 sp = b.spans[pc.span_base + s];
+    for (uint32_t s = rs.x; s < rs.x + rs.y; ++s) {
+      uint2 sp = b.spans[s];
       int sx = (int)(sp.x & 0xFFFF), slen = (int)(sp.x >> 16);
       int xs = max_(sx, x0), xe = min_(sx + slen, x1);
       uint32_t alpha = sp.y & br.global_alpha;

@@ -67,7 +67,7 @@ struct DeviceBatch {
   Context* ctx = nullptr;
   HostBatch hb;
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
-  DevBuf scratch, geom, sweep, sweepmem, rowtab, pass_spans, comp, spans, pixels;
+  DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
   DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
   uint32_t chunk = 1024;
@@ -81,6 +81,9 @@ struct DeviceBatch {
 struct skity_cuda_context_s {
   int device = 0;
   uint64_t budget = 0;
+  // span pool shared by the context's renders (they are serialised), grown
+  // to what the largest render so far needed
+  skc::DevBuf span_pool, span_next;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t stage[10] = {};
@@ -204,22 +207,30 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   }
   if (!todo.empty()) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
 
-  // ---- per-pass sweep buffers and row tables
+  // ---- per-pass sweep buffers and row-span tables
   std::vector<PassSweep> sw;
-  SweepPlan pl = PlanSweep(db.h_geom, sw);
-  uint64_t rows = pl.rows;
+  SweepPlan pl = PlanSweep(hb, db.h_geom, sw);
+  const uint64_t rows = pl.rows;
   st.edges = pl.edges;
   if (rows >= 0xFFFFFFFFull) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
   SKC_TRY(Upload(db.sweep, sw, s));
   SKC_TRY(db.sweepmem.ensure(std::max<uint64_t>(pl.sweep_bytes, 16)));
-  SKC_TRY(db.rowtab.ensure(std::max<uint64_t>(rows, 1) * 4));
-  SKC_TRY(cudaMemsetAsync(db.rowtab.p, 0, std::max<uint64_t>(rows, 1) * 4, s));
+  SKC_TRY(db.rowspan.ensure(std::max<uint64_t>(rows, 1) * sizeof(uint2)));
   SKC_TRY(db.pass_spans.ensure(std::max<size_t>(np, 1) * 4));
   SKC_TRY(db.pass_frags.ensure(std::max<size_t>(np, 1) * 8));
   SKC_TRY(db.err.ensure(16));
-  SKC_TRY(cudaMemsetAsync(db.err.p, 0, 16, s));
   SKC_TRY(db.pass_class.ensure(std::max<size_t>(np, 1)));
-  SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
+  SKC_TRY(ctx->span_next.ensure(8));
+  std::vector<PassComp> comp;
+  PlanComp(hb, db.h_geom, sw, comp);
+  SKC_TRY(Upload(db.comp, comp, s));
+  // span indices are 32-bit
+  const uint64_t kMaxPool = 0xFFFFFFFFull;
+  uint64_t want = std::min<uint64_t>(std::max<uint64_t>(pl.span_estimate, 1 << 16), kMaxPool);
+  if (ctx->span_pool.cap / sizeof(uint2) < want) {
+    if (ctx->budget && want * sizeof(uint2) > ctx->budget) want = ctx->budget / sizeof(uint2);
+    SKC_TRY(ctx->span_pool.ensure(want * sizeof(uint2)));
+  }
 
   DevBatch b{};
   b.verbs = db.verbs.as<uint8_t>();
@@ -233,35 +244,43 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.geom = db.geom.as<PassGeom>();
   b.sweep = db.sweep.as<PassSweep>();
   b.sweepmem = db.sweepmem.as<uint8_t>();
-  b.rowtab = db.rowtab.as<uint32_t>();
+  b.rowspan = db.rowspan.as<uint2>();
   b.pass_spans = db.pass_spans.as<uint32_t>();
   b.pass_frags = db.pass_frags.as<unsigned long long>();
   b.err = db.err.as<uint32_t>();
   b.pass_class = db.pass_class.as<uint8_t>();
   b.reg_diff_cap = RegDiffCap(pl);
-  SKC_TRY(cudaEventRecord(ctx->stage[2], s));
-  st.kernel_launches += LaunchSweep(b, false, s);
-  SKC_TRY(cudaEventRecord(ctx->stage[3], s));
-  SKC_TRY(cudaGetLastError());
-  std::vector<uint32_t> pspans(np);
-  std::vector<unsigned long long> pfrags(np);
-  if (np) {
-    SKC_TRY(cudaMemcpyAsync(pspans.data(), db.pass_spans.p, np * 4, cudaMemcpyDeviceToHost, s));
-    SKC_TRY(cudaMemcpyAsync(pfrags.data(), db.pass_frags.p, np * 8, cudaMemcpyDeviceToHost, s));
-  }
-  SKC_TRY(cudaStreamSynchronize(s));
-  std::vector<PassComp> comp;
-  uint64_t spans = PlanComp(hb, db.h_geom, sw, pspans, comp);
-  st.spans = spans;
-  for (uint32_t p = 0; p < np; ++p) st.fragments += pfrags[p];
-  SKC_TRY(Upload(db.comp, comp, s));
-  SKC_TRY(db.spans.ensure(std::max<uint64_t>(spans, 1) * sizeof(uint2)));
   b.comp = db.comp.as<PassComp>();
-  b.spans = db.spans.as<uint2>();
-  SKC_TRY(cudaEventRecord(ctx->stage[4], s));
-  st.kernel_launches += LaunchSweep(b, true, s);
-  SKC_TRY(cudaEventRecord(ctx->stage[5], s));
-  SKC_TRY(cudaGetLastError());
+  b.span_next = ctx->span_next.as<unsigned long long>();
+  // The sweep; if the span pool ran out it is grown to the size the sweep
+  // reported and the sweep runs again (first renders of a context only).
+  double discarded_ms = 0;
+  for (int attempt = 0;; ++attempt) {
+    b.spans = ctx->span_pool.as<uint2>();
+    b.span_cap = ctx->span_pool.cap / sizeof(uint2);
+    SKC_TRY(cudaMemsetAsync(db.rowspan.p, 0, std::max<uint64_t>(rows, 1) * sizeof(uint2), s));
+    SKC_TRY(cudaMemsetAsync(db.err.p, 0, 16, s));
+    SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
+    SKC_TRY(cudaMemsetAsync(ctx->span_next.p, 0, 8, s));
+    SKC_TRY(cudaEventRecord(ctx->stage[4], s));
+    st.kernel_launches += LaunchSweep(b, s);
+    SKC_TRY(cudaEventRecord(ctx->stage[5], s));
+    SKC_TRY(cudaGetLastError());
+    unsigned long long used = 0;
+    SKC_TRY(cudaMemcpyAsync(&used, ctx->span_next.p, 8, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaStreamSynchronize(s));
+    if (used <= b.span_cap) break;
+    if (attempt == 2 || used > kMaxPool) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->stage[4], ctx->stage[5]);
+    discarded_ms += ms;
+    const uint64_t grow = std::min<uint64_t>(used + used / 16, kMaxPool);
+    if (ctx->budget && grow * sizeof(uint2) > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+    ctx->span_pool.release();
+    SKC_TRY(ctx->span_pool.ensure(grow * sizeof(uint2)));
+    st.retries++;
+  }
+  st.sweep_count_ms = discarded_ms;
 
   // ---- composite temp canvases, blur, composite main canvases
   b.brushes = db.brushes.as<Brush>();
@@ -304,12 +323,21 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
       return (double)ms;
     };
     st.geometry_ms = el(0, 1);
-    st.sweep_count_ms = el(2, 3);
     st.sweep_emit_ms = el(4, 5);
     st.composite_ms = el(6, 7) + el(8, 9);
     st.blur_ms = el(7, 8);
   }
   for (uint32_t c : hb.main_canvases) st.pixels += (uint64_t)hb.canvases[c].w * hb.canvases[c].h;
+  if (np) {
+    std::vector<uint32_t> pspans(np);
+    std::vector<unsigned long long> pfrags(np);
+    SKC_TRY(cudaMemcpy(pspans.data(), db.pass_spans.p, np * 4, cudaMemcpyDeviceToHost));
+    SKC_TRY(cudaMemcpy(pfrags.data(), db.pass_frags.p, np * 8, cudaMemcpyDeviceToHost));
+    for (uint32_t p = 0; p < np; ++p) {
+      st.spans += pspans[p];
+      st.fragments += pfrags[p];
+    }
+  }
   db.stats = st;
   return SKITY_CUDA_SUCCESS;
 }

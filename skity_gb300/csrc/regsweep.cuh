@@ -24,6 +24,7 @@
 namespace skc {
 
 constexpr int kRegMaxM = 128;  // active edges held in registers
+constexpr int kStageSpans = 8;  // direct spans a lane stages per interval
 
 // Per-warp shared block of the register sweep.
 struct RegShared {
@@ -39,8 +40,11 @@ struct RegShared {
   // edge state by new list position (reorder and insertion)
   int32_t p_idx[kRegMaxM], p_x[kRegMaxM], p_dx[kRegMaxM], p_dy[kRegMaxM];
   int32_t p_low[kRegMaxM], p_wc[kRegMaxM];
+  uint2 stage[32 * kStageSpans];  // each lane's direct spans of a step
   uint8_t surv[kRegMaxM];  // 1: survives the step
 };
+// Host and device must agree on this size (the host sizes the launch).
+static_assert(sizeof(RegShared) % 16 == 0, "RegShared keeps 16-byte alignment");
 
 SKC_HD int32_t MakeWc(int winding, int count) { return (winding & 0xFF) | ((count & 0xFF) << 8); }
 SKC_HD int WcWinding(int32_t wc) { return (int8_t)(wc & 0xFF); }
@@ -88,7 +92,8 @@ SKC_HD void AccFlushIfNeed(const Lanes& L, AccState& a, Sink* sink, int row) {
   a.y = row;
 }
 
-// Lane-local output of one interval's trapezoid row.
+// Lane-local output of one interval's trapezoid row: direct spans go to
+// `write` when set, else the first kStageSpans of them to `stage`.
 template <typename Sink>
 struct RegOut {
   Sink* sink;
@@ -98,12 +103,15 @@ struct RegOut {
   uint32_t kept;
   unsigned long long frags;
   uint2* write;
+  uint2* stage;
   int lo, hi;
   SKC_HD void real(int x, int len, uint8_t a) {
     if (!sink->keep(x, y, len, a)) return;
     kept++;
     frags += (unsigned)len;
-    if (write) *write++ = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+    const uint2 v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+    if (write) *write++ = v;
+    else if (kept <= (uint32_t)kStageSpans) stage[kept - 1] = v;
   }
   SKC_HD void acc(int x, int len, uint8_t a) {
     if (!do_acc) return;
@@ -123,13 +131,13 @@ struct RegOut {
 // open by the last left edge: blit_trapezoid_row for each, one interval per
 // lane, direct spans written in interval order.
 template <typename Sink>
-SKC_HD void RegBlit(const Lanes& L, const RegShared& sh, Sink* sink, AccState& as, const Edge* W,
+SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, const Edge* W,
                     int n, int y, Fixed next_y, int K, int m, int k, uint8_t full,
                     Fixed left_clip, Fixed right_clip, int trailing_a, bool trailing_nr) {
   const int total = K + (trailing_a >= 0 ? 1 : 0);
   AccFlushIfNeed(L, as, sink, y);
-  const bool emit = Sink::kEmit;
-  const uint32_t base = emit ? sink->row_cursor(y) : 0;
+  sink->row_begin(L, y);
+  uint2* stage = sh.stage + L.lane * kStageSpans;
   uint32_t run = 0;
   unsigned long long frags = 0;
   int lo = 0x7fffffff, hi = -1;
@@ -194,27 +202,31 @@ SKC_HD void RegBlit(const Lanes& L, const RegShared& sh, Sink* sink, AccState& a
     o.kept = 0;
     o.frags = 0;
     o.write = nullptr;
+    o.stage = stage;
     o.lo = 0x7fffffff;
     o.hi = -1;
     if (valid) TrapezoidRow(o, ul, ur, ll, lr, lDY, rDY, full, nr);
     lo = min_(lo, o.lo);
     hi = max_(hi, o.hi);
-    if (emit) {
-      const int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
-      const uint32_t mine = base + run + (uint32_t)(incl - (int32_t)o.kept);
-      const int32_t chunk_total = LaneBcast(L, incl, Lanes::n - 1);
-      if (valid && o.kept && sink->in_range(mine, o.kept)) {
-        RegOut<Sink> w = o;
-        w.do_acc = false;
-        w.kept = 0;
-        w.frags = 0;
-        w.write = sink->span_ptr(mine);
-        TrapezoidRow(w, ul, ur, ll, lr, lDY, rDY, full, nr);
+    const int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
+    const uint32_t chunk_total = (uint32_t)LaneBcast(L, incl, Lanes::n - 1);
+    if (chunk_total) {
+      const uint64_t at = sink->reserve(L, run, chunk_total);
+      uint2* dst = sink->span_ptr(at + run + (uint32_t)(incl - (int32_t)o.kept));
+      if (valid && o.kept && dst) {
+        if (o.kept <= (uint32_t)kStageSpans) {
+          for (uint32_t i = 0; i < o.kept; ++i) dst[i] = stage[i];
+        } else {  // more than the stage holds: run the row again, writing
+          RegOut<Sink> w = o;
+          w.do_acc = false;
+          w.kept = 0;
+          w.frags = 0;
+          w.write = dst;
+          TrapezoidRow(w, ul, ur, ll, lr, lDY, rDY, full, nr);
+        }
       }
-      run += (uint32_t)chunk_total;
-    } else {
-      run += (uint32_t)LaneSum64(L, o.kept);
     }
+    run += chunk_total;
     frags += o.frags;
   }
   frags = LaneSum64(L, frags);
@@ -224,7 +236,7 @@ SKC_HD void RegBlit(const Lanes& L, const RegShared& sh, Sink* sink, AccState& a
     as.lo = min_(as.lo, lo);
     as.hi = max_(as.hi, hi);
   }
-  sink->step_done(L, y, run, frags);
+  sink->commit(L, run, frags);
   L.sync();
 }
 

@@ -10,17 +10,18 @@
 // rejected with SKITY_CUDA_ERROR_SCRATCH_LIMIT.
 //
 // The work per rasterisation pass is the batch pipeline's, on one pass:
-// k_geometry (path -> quads -> stroke -> edges -> introsort), k_sweep_count,
-// k_sweep_emit, then k_static_composite below, which blends the pass's spans
+// k_geometry (path -> quads -> stroke -> edges -> introsort), the sweep
+// kernels, then k_static_composite below, which blends the pass's spans
 // straight into the caller's canvas rows.  Layout of the static scratch:
 //
 //   [0, 4 KiB)     descriptors: PassDesc, DrawDesc, CanvasDesc, Brush,
-//                  PassGeom, PassSweep, PassComp, self-check flag, span count
+//                  PassGeom, PassSweep, PassComp, self-check flag, span
+//                  count, span-pool allocator
 //   path copy      verbs, points, conic weights of the caller's path
 //   geometry       SliceLayout of the pass (capacities grown on overflow)
 //   sweep memory   SweepMemLayout(edges, accumulator width)
-//   row table      rows + 1 span offsets
-//   spans          whatever is left
+//   row table      (first span, count) per row
+//   span pool      whatever is left
 //
 // One scratch per device, not per call: calls that overlap on one device
 // race on it and must be serialised by the caller.
@@ -54,6 +55,8 @@ struct StaticDesc {  // the descriptor block at the start of the scratch
   uint32_t err;
   uint32_t pass_spans[2];
   uint32_t pass_class;
+  uint32_t pad;
+  unsigned long long span_next;
 };
 static_assert(sizeof(StaticDesc) <= kDescBytes, "descriptor block");
 static_assert(sizeof(P) == 8, "points are copied as float pairs");
@@ -93,7 +96,8 @@ __global__ void __launch_bounds__(32 * kStaticCompWarps)
   const PassComp pc = b.comp[0];
   const int y = pc.row0 + (int)(blockIdx.x * kStaticCompWarps + (threadIdx.x >> 5));
   if (y >= pc.row1) return;
-  const uint32_t s0 = b.rowtab[y - pc.row0], s1 = b.rowtab[y - pc.row0 + 1];
+  const uint2 rs = b.rowspan[y - pc.row0];
+  const uint32_t s0 = rs.x, s1 = rs.x + rs.y;
   if (s0 >= s1) return;
   const Brush br = b.brushes[0];
   uint32_t* row = (uint32_t*)(pixels + (size_t)y * row_bytes);
@@ -178,50 +182,54 @@ int32_t StaticPass(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   const int nrows = g.row1 - g.row0;
   if (g.n_edges <= 0 || nrows <= 0) return SKITY_CUDA_SUCCESS;
 
-  // sweep memory and row table after the slice
+  // sweep memory, row table and span pool after the slice
   SliceLayout L;
   L.compute(pd.cap, sizeof(Edge));
   const uint64_t sweep_off = Align256(slice_off0 + L.bytes);
   const uint64_t sweep_bytes = SweepMemBytes(g.n_edges, g.acc_width > 0 ? g.acc_width : 0);
   const uint64_t rows_off = Align256(sweep_off + sweep_bytes);
-  const uint64_t spans_off = Align256(rows_off + 4ull * ((uint64_t)nrows + 1));
+  const uint64_t spans_off = Align256(rows_off + sizeof(uint2) * (uint64_t)nrows);
   if (spans_off > kStaticScratchBytes) return SKITY_CUDA_ERROR_SCRATCH_LIMIT;
+  const uint64_t span_cap = (kStaticScratchBytes - spans_off) / sizeof(uint2);
+  const uint32_t chunk = SpanChunk(cd.w, g.n_edges);
+  if (chunk > span_cap) return SKITY_CUDA_ERROR_SCRATCH_LIMIT;
   b.sweepmem = base + sweep_off;
   b.reg_diff_cap = std::max<int32_t>(
       4, std::min<int32_t>(((g.acc_width > 0 ? g.acc_width : 0) + 1 + 3) & ~3, kRegDiffMax));
-  b.rowtab = (uint32_t*)(base + rows_off);
+  b.rowspan = (uint2*)(base + rows_off);
   b.spans = (uint2*)(base + spans_off);
-  const uint64_t span_cap = (kStaticScratchBytes - spans_off) / sizeof(uint2);
+  b.span_cap = span_cap;
+  b.span_next = &dev->span_next;
 
   PassSweep sw;
   std::memset(&sw, 0, sizeof sw);
   sw.work_off = 0;
   sw.bytes = sweep_bytes;
   sw.rbase = 0;
-  cudaError_t e = cudaMemcpyAsync(&dev->sweep, &sw, sizeof sw, cudaMemcpyHostToDevice, st);
-  // the count pass adds into the row table; the self-check flag starts clear
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.rowtab, 0, 4ull * ((uint64_t)nrows + 1), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->err, 0, sizeof(uint32_t), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->pass_class, 0, sizeof(uint32_t), st);
-  if (e != cudaSuccess) return Err(e);
-  LaunchSweep(b, false, st);
-  uint32_t spans = 0;
-  e = cudaMemcpyAsync(&spans, &dev->pass_spans[0], sizeof spans, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return Err(e);
-  if (spans > span_cap) return SKITY_CUDA_ERROR_SCRATCH_LIMIT;
-  if (spans == 0) return SKITY_CUDA_SUCCESS;
-
+  sw.chunk = chunk;
   PassComp pc;
   std::memset(&pc, 0, sizeof pc);
   pc.row0 = g.row0;
   pc.row1 = g.row1;
   pc.rbase = 0;
   pc.brush = 0;
-  pc.span_base = 0;
-  e = cudaMemcpyAsync(&dev->comp, &pc, sizeof pc, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(&dev->sweep, &sw, sizeof sw, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&dev->comp, &pc, sizeof pc, cudaMemcpyHostToDevice, st);
+  // empty rows read as (0, 0); the flag, the sweep form and the pool
+  // allocator start clear
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.rowspan, 0, sizeof(uint2) * (uint64_t)nrows, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->err, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->pass_class, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&dev->span_next, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return Err(e);
-  LaunchSweep(b, true, st);
+  LaunchSweep(b, st);
+  unsigned long long used = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&used, &dev->span_next, sizeof used, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return Err(e);
+  if (used > span_cap) return SKITY_CUDA_ERROR_SCRATCH_LIMIT;
   unsigned grid = (unsigned)((nrows + kStaticCompWarps - 1) / kStaticCompWarps);
   k_static_composite<<<grid, 32 * kStaticCompWarps, 0, st>>>(b, pixels, row_bytes);
   uint32_t err = 0;

@@ -392,8 +392,7 @@ struct LaneSweep {
     if (total == 0) return;
     if (y < scan_top) return;
     flush_if_need(y);
-    const bool emit = Sink::kEmit;
-    uint32_t base = emit ? sink->row_cursor(y) : 0;
+    sink->row_begin(L, y);
     uint32_t run = 0;  // kept direct spans so far in this step
     unsigned long long frags = 0;
     int lo = 0x7fffffff, hi = -1;
@@ -463,22 +462,22 @@ struct LaneSweep {
       if (valid) TrapezoidRow(o, ul, ur, ll, lr, lDY, rDY, full, nr);
       lo = min_(lo, o.lo);
       hi = max_(hi, o.hi);
-      if (emit) {
-        int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
-        uint32_t mine = base + run + (uint32_t)(incl - (int32_t)o.kept);
-        int32_t chunk_total = LaneBcast(L, incl, Lanes::n - 1);
-        if (valid && o.kept && sink->in_range(mine, o.kept)) {
+      const int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
+      const uint32_t chunk_total = (uint32_t)LaneBcast(L, incl, Lanes::n - 1);
+      if (chunk_total) {
+        const uint64_t at = sink->reserve(L, run, chunk_total);
+        uint2* dst = sink->span_ptr(at + run + (uint32_t)(incl - (int32_t)o.kept));
+        if (valid && o.kept && dst) {
           Out w = o;
           w.do_acc = false;
           w.kept = 0;
           w.frags = 0;
-          w.write = sink->span_ptr(mine);
+          w.write = dst;
           TrapezoidRow(w, ul, ur, ll, lr, lDY, rDY, full, nr);
         }
-        run += (uint32_t)chunk_total;
-      } else {
-        run += (uint32_t)LaneSum64(L, o.kept);
+        L.sync();
       }
+      run += chunk_total;
       frags += o.frags;
     }
     frags = LaneSum64(L, frags);
@@ -488,7 +487,7 @@ struct LaneSweep {
       touch_lo = min_(touch_lo, lo);
       touch_hi = max_(touch_hi, hi);
     }
-    sink->step_done(L, y, run, frags);
+    sink->commit(L, run, frags);
     L.sync();
   }
 

@@ -42,7 +42,8 @@ def cpu_pipeline():
     lib.skc_cpu_render.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p,
                                    ctypes.POINTER(ctypes.c_uint64)]
     lib.skc_cpu_render_mode.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p,
-                                        ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
+                                        ctypes.POINTER(ctypes.c_uint64), ctypes.c_int,
+                                        ctypes.c_uint64]
     lib.skc_cpu_introsort.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     lib.skc_std_sort.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     return lib

@@ -17,7 +17,7 @@ using namespace skc;
 // mode 0: register sweep with the generic sweep for passes it gives up on
 // (the GPU pipeline's choice); mode 1: generic sweep for every pass.
 extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* out_rgba,
-                                   uint64_t stats[6], int mode) {
+                                   uint64_t stats[6], int mode, uint64_t pool_hint) {
   StreamView sv;
   if (!ParseStream(stream, len, &sv)) return -2;
   HostBatch hb;
@@ -70,41 +70,52 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     if (attempt == 7) return -7;
   }
   std::vector<PassSweep> sw;
-  SweepPlan pl = PlanSweep(geom, sw);
+  SweepPlan pl = PlanSweep(hb, geom, sw);
   // exact size: an overrun of the planned layout is caught by the sanitizer
   // build of this harness and shows up as a mismatch otherwise
   std::vector<uint8_t> sweepmem(pl.sweep_bytes, 0);
-  std::vector<uint32_t> rowtab(pl.rows + 1, 0), pass_spans(np + 1, 0);
+  std::vector<uint2> rowspan(pl.rows + 1);
+  std::vector<uint32_t> pass_spans(np + 1, 0);
+  std::vector<PassComp> comp;
+  PlanComp(hb, geom, sw, comp);
   b.sweep = sw.data();
   b.sweepmem = sweepmem.data();
   uint32_t err = 0;
   b.err = &err;
-  b.rowtab = rowtab.data();
+  b.rowspan = rowspan.data();
   b.pass_spans = pass_spans.data();
+  b.comp = comp.data();
   Lanes lanes;
-  std::vector<uint8_t> pclass(np + 1, mode == 1 ? 1 : 0);
+  std::vector<uint8_t> pclass(np + 1);
   b.pass_class = pclass.data();
   b.reg_diff_cap = RegDiffCap(pl);
   std::vector<int32_t> regmem((RegSmemBytes(b.reg_diff_cap) + 3) / 4);
   RegShared* sh = (RegShared*)regmem.data();
   int32_t* sdiff = (int32_t*)((uint8_t*)regmem.data() + sizeof(RegShared));
-  uint64_t generic = 0;
-  for (uint32_t p = 0; p < np; ++p) {
-    if (pclass[p] == 0) SweepCountPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
-    if (pclass[p] == 1) {
-      SweepCountPass(b, p, lanes, true);
-      generic++;
+  // span pool: start small so that the regrowth path runs too
+  std::vector<uint2> pool(pool_hint ? pool_hint : 1024);
+  unsigned long long next = 0;
+  uint64_t generic = 0, spans = 0;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    std::fill(rowspan.begin(), rowspan.end(), make_uint2(0, 0));
+    std::fill(pclass.begin(), pclass.end(), (uint8_t)(mode == 1 ? 1 : 0));
+    next = 0;
+    b.spans = pool.data();
+    b.span_cap = pool.size();
+    b.span_next = &next;
+    generic = 0;
+    for (uint32_t p = 0; p < np; ++p) {
+      if (pclass[p] == 0) SweepPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+      if (pclass[p] == 1) {
+        SweepPass(b, p, lanes);
+        generic++;
+      }
     }
+    if (next <= pool.size()) break;
+    if (attempt == 2) return -7;
+    pool.assign(next, make_uint2(0, 0));
   }
-  std::vector<PassComp> comp;
-  uint64_t spans = PlanComp(hb, geom, sw, pass_spans, comp);
-  std::vector<uint2> span_buf(spans + 1);
-  b.comp = comp.data();
-  b.spans = span_buf.data();
-  for (uint32_t p = 0; p < np; ++p) {
-    if (pclass[p] == 0) SweepEmitPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
-    else SweepEmitPass(b, p, lanes);
-  }
+  for (uint32_t p = 0; p < np; ++p) spans += pass_spans[p];
   b.brushes = hb.brushes.data();
   b.stop_colors = hb.stop_colors.data();
   b.stop_offsets = hb.stop_offsets.data();
@@ -151,7 +162,7 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
 
 extern "C" int skc_cpu_render(const uint8_t* stream, size_t len, uint8_t* out_rgba,
                               uint64_t stats[6]) {
-  return skc_cpu_render_mode(stream, len, out_rgba, stats, 0);
+  return skc_cpu_render_mode(stream, len, out_rgba, stats, 0, 0);
 }
 
 // The device introsort on an arbitrary key array, for the permutation test

@@ -15,7 +15,7 @@ def cpu_render(lib, sc, mode=0):
     b = sc.to_bytes()
     out = np.zeros((sc.height, sc.width, 4), np.uint8)
     st = (ctypes.c_uint64 * 6)()
-    rc = lib.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, mode)
+    rc = lib.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, mode, 0)
     assert rc == 0, rc
     return out, list(st)
 
