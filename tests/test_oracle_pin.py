@@ -1,0 +1,87 @@
+"""Pins the oracle (oracle/sw_oracle.cc) to the reference software backend
+compiled from the reference's own sources (oracle/ref/Makefile ->
+oracle/_ref/ref_render): identical pixels on seeded scenes that cover every
+behaviour of the path.  Runs where the reference build exists (it needs the
+reference checkout to compile); CPU only."""
+import numpy as np
+import pytest
+
+from skity_gb300 import scene as S
+
+
+@pytest.fixture(scope="module")
+def ref(oracle_lib):
+    try:
+        ok = oracle_lib.build_reference()
+    except RuntimeError as e:
+        pytest.skip(f"reference build failed: {e}")
+    if not ok and not oracle_lib.reference_available():
+        pytest.skip("reference checkout not present")
+    return oracle_lib
+
+
+def _pin(oracle_lib, sc):
+    want = oracle_lib.render_reference(sc)
+    got, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, want)
+    assert c["bad_pixels"] == 0, c
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_fills(ref, seed):
+    sc = S.random_paths_scene(S.SEED_BASE + 300 + seed, 96 + 16 * seed, 80 + 8 * seed, 40,
+                              1, 24, coord_lo=(-20.0, -20.0),
+                              coord_hi=(116.0 + 16 * seed, 100.0 + 8 * seed),
+                              evenodd_frac=0.5)
+    _pin(ref, sc)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_strokes_and_gradients(ref, seed):
+    sc = S.random_paths_scene(S.SEED_BASE + 320 + seed, 200, 150, 50, 2, 40,
+                              coord_lo=(-30.0, -30.0), coord_hi=(230.0, 180.0),
+                              evenodd_frac=0.3, gradient_frac=0.6, stroke_frac=0.5)
+    _pin(ref, sc)
+
+
+def test_config2_subset(ref):
+    _pin(ref, S.config2(n_paths=200, width=2048, height=2048))
+
+
+def test_blur_outlines(ref):
+    _pin(ref, S.config4(seed=S.SEED_BASE + 340, n_outlines=400, width=384, height=384,
+                        blur_frac=0.5))
+
+
+def test_batch_canvases(ref):
+    for sc in S.config3(n_canvases=6, scale=0.1):
+        _pin(ref, sc)
+
+
+def test_styles_blend_modes_and_tile_modes(ref):
+    """Every Paint::Style, the four supported blend modes, all gradient tile
+    modes and evenly spaced stops (no offsets), no clear colour."""
+    b = S.SceneBuilder(120, 100, clear=None)
+    rng = np.random.default_rng(11)
+    for i in range(48):
+        n = 3 + i % 5
+        verbs = [S.MOVE] + [[S.LINE, S.QUAD, S.CUBIC][j % 3] for j in range(n)] + [S.CLOSE]
+        npts = 1 + sum({S.LINE: 1, S.QUAD: 2, S.CUBIC: 3}[v] for v in verbs[1:-1])
+        pts = rng.uniform(-10, 130, (npts, 2)).astype(np.float32)
+        p = S.default_paint()
+        p["style"] = i % 4
+        p["stroke_width"] = float(1 + i % 6)
+        p["cap"], p["join"] = i % 3, (i // 3) % 3
+        p["blend"] = [S.BLEND_SRC_OVER, S.BLEND_SRC, S.BLEND_CLEAR, S.BLEND_DST][i % 4] \
+            if i % 5 == 0 else S.BLEND_SRC_OVER
+        p["fill_color"] = tuple(rng.uniform(0, 1, 4).astype(np.float32))
+        p["stroke_color"] = tuple(rng.uniform(0, 1, 4).astype(np.float32))
+        if i % 3 == 1:
+            cols = rng.uniform(0, 1, (2 + i % 4, 4)).astype(np.float32)
+            offs = None if i % 2 else np.sort(rng.uniform(0, 1, len(cols))).astype(np.float32)
+            kind = S.GRAD_LINEAR if i % 6 == 1 else S.GRAD_RADIAL
+            p["gradient"] = b.add_gradient(kind, (float(pts[0, 0]), float(pts[0, 1])),
+                                           (float(pts[1, 0]), float(pts[1, 1])),
+                                           (float(5 + i), 0.0), cols, offs, tile_mode=i % 4)
+        b.draw_path(verbs, pts, p)
+    _pin(ref, b.build())
