@@ -121,6 +121,101 @@ def load_scene():
         return sc
 
 
+def load_config3():
+    from skity_gb300 import scene as S
+    cache = os.path.join("/tmp", "skity_config3_v1.bin")
+    try:
+        with open(cache, "rb") as f:
+            buf = f.read()
+        scenes, o = [], 0
+        while o < len(buf):
+            n = int.from_bytes(buf[o:o + 8], "little")
+            scenes.append(S.Scene.from_bytes(buf[o + 8:o + 8 + n]))
+            o += 8 + n
+        if len(scenes) == 256:
+            return scenes
+    except Exception:
+        pass
+    scenes = S.config3()
+    try:
+        with open(cache, "wb") as f:
+            for sc in scenes:
+                b = sc.to_bytes()
+                f.write(len(b).to_bytes(8, "little") + b)
+    except Exception:
+        pass
+    return scenes
+
+
+def batch_forms(ctx, steps: int, warmup: int, sample: int):
+    """The 256-canvas batching workload (log-uniform sides in [64,1024],
+    log-uniform 50-2,000 paths each, drawn as in the 512x512 scene) in three
+    forms: the batched form (one planned batch, re-rendered by CUDA graph
+    replay), the plain per-draw form (one launch sequence per DrawPath onto a
+    device canvas, skity_cuda_draw_path_static) on the first `sample`
+    canvases, and the CPU oracle over the same sample on all host cores.
+    The per-draw result is compared with the batched one on the sample."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle
+    from skity_gb300.canvas import Batch, DeviceCanvas
+
+    scenes = load_config3()
+    pix = sum(sc.width * sc.height for sc in scenes)
+    paths = sum(sc.n_draws for sc in scenes)
+    batch = Batch(ctx, scenes)
+    for _ in range(max(warmup, 1)):
+        batch.render()
+    ms = []
+    for _ in range(steps):
+        st = batch.render()
+        ms.append(st["device_ms"])
+    bms = statistics.mean(ms)
+    out = {"workload": "256 canvases, sides log-uniform [64,1024], 50-2,000 paths each "
+                       "(3-32 verbs line/quad/cubic, nonzero, solid colours)",
+           "canvases": len(scenes), "paths": paths, "mpix": pix / 1e6,
+           "batched": {"ms": bms, "mpix_per_s": pix / 1e3 / bms, "paths_per_s": paths * 1e3 / bms,
+                       "graph_replays": int(st["graph_replays"]), "form": "one planned batch, "
+                       "CUDA-graph replay (geometry, sweeps, composites)"}}
+    # per-draw form on a sample of canvases
+    sub = scenes[:sample]
+    spix = sum(sc.width * sc.height for sc in sub)
+    spaths = sum(sc.n_draws for sc in sub)
+    stream = torch.cuda.current_stream()
+    canv = [torch.full((sc.height, sc.width, 4), 255, dtype=torch.uint8, device="cuda")
+            for sc in sub]
+    dcs = [DeviceCanvas(c.data_ptr(), sc.width, sc.height, device=torch.cuda.current_device(),
+                        stream=stream.cuda_stream) for c, sc in zip(canv, sub)]
+    dcs[0].draw_scene(sub[0].subset(0, 8))  # first call: one-time set-up
+    for c in canv:
+        c.fill_(255)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for dc, sc in zip(dcs, sub):
+        dc.draw_scene(sc)
+    torch.cuda.synchronize()
+    pd_s = time.perf_counter() - t0
+    exact = all(np.array_equal(c.cpu().numpy(), batch.read(i)) for i, c in enumerate(canv))
+    out["per_draw"] = {"ms_per_canvas": 1e3 * pd_s / len(sub), "mpix_per_s": spix / 1e6 / pd_s,
+                       "paths_per_s": spaths / pd_s, "sample": f"first {len(sub)} canvases, "
+                       f"{spaths} paths", "matches_batched": exact,
+                       "form": "skity_cuda_draw_path_static per DrawPath on a device canvas"}
+    # CPU oracle on the same sample, one canvas per host thread
+    threads = os.cpu_count() or 1
+    oracle.build()
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda sc: oracle.render(sc), sub))
+    cpu_s = time.perf_counter() - t0
+    out["cpu"] = {"mpix_per_s": spix / 1e6 / cpu_s, "paths_per_s": spaths / cpu_s, "cores": threads,
+                  "kind": "port", "sample": f"first {len(sub)} canvases, one per thread"}
+    out["batched_over_per_draw"] = out["batched"]["paths_per_s"] / out["per_draw"]["paths_per_s"]
+    out["batched_over_cpu"] = out["batched"]["paths_per_s"] / out["cpu"]["paths_per_s"]
+    batch.close()
+    return out
+
+
 def cpu_baseline(scene, threads: int, sample_paths: int, steps: int = 1):
     """The oracle (CPU restatement of the reference path) on the first
     `sample_paths` draws; paths/s over `steps` repetitions."""
@@ -252,6 +347,8 @@ def run_gpu(args, rank, world, local):
                 "ms_per_step": e2e_ms_mean},
         "wall_s": wall,
     }
+    if rank == 0 and not args.no_forms:
+        line["batching"] = batch_forms(ctx, max(1, min(args.steps, 5)), 3, args.per_draw_sample)
     if rank == 0 and not args.no_cpu:
         v, secs = cpu_baseline(scene, 1, args.cpu_sample_paths)
         line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": 1, "kind": "port",
@@ -277,6 +374,9 @@ def main():
     ap.add_argument("--paths", type=int, default=0,
                     help="render only the first N paths of the scene (small profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the 256-canvas batched / per-draw / CPU comparison")
+    ap.add_argument("--per-draw-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()

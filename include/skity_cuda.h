@@ -133,6 +133,7 @@ typedef struct skity_cuda_stats {
   double composite_ms;    /* span replay, shading, blending */
   double blur_ms;         /* StackBlur of blur mask filter temp canvases */
   uint64_t fragments;     /* sum of span lengths inside the canvases */
+  uint64_t graph_replays; /* 1: the render replayed the batch's CUDA graph */
 } skity_cuda_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -183,7 +184,10 @@ SKITY_CUDA_API int32_t skity_cuda_render_streams(skity_cuda_context ctx,
 /* Device-resident batches: the streams are parsed and uploaded once
  * (skity_cuda_batch_create); each skity_cuda_batch_render re-renders every
  * canvas from its clear colour with inputs already in device memory;
- * skity_cuda_batch_read copies canvas i's pixels to host memory. */
+ * skity_cuda_batch_read copies canvas i's pixels to host memory.  The first
+ * render plans the batch (geometry sizes, sweep buffers, row tables, pass
+ * bins) and records its launches as a CUDA graph; later renders replay that
+ * graph with one launch. */
 SKITY_CUDA_API int32_t skity_cuda_batch_create(skity_cuda_context ctx, uint32_t count,
                                                const uint8_t* const* streams,
                                                const size_t* stream_bytes,

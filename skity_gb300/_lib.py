@@ -61,7 +61,7 @@ class Stats_(ctypes.Structure):
                 ("retries", ctypes.c_uint64), ("geometry_ms", ctypes.c_double),
                 ("sweep_count_ms", ctypes.c_double), ("sweep_emit_ms", ctypes.c_double),
                 ("composite_ms", ctypes.c_double), ("blur_ms", ctypes.c_double),
-                ("fragments", ctypes.c_uint64)]
+                ("fragments", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

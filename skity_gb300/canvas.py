@@ -325,3 +325,56 @@ class Canvas:
             self.close()
         except Exception:
             pass
+
+
+class DeviceCanvas:
+    """The plain per-draw form: a premultiplied RGBA8 canvas held in device
+    memory (any CUDA allocation, e.g. a torch uint8 tensor of shape
+    (h, w, 4)) drawn one DrawPath at a time through
+    skity_cuda_draw_path_static -- geometry, sweeps and composite launched
+    for every draw, as the software canvas rasterises every draw on its own.
+    Solid-colour paints only (no shader, no mask filter)."""
+
+    def __init__(self, device_ptr: int, width: int, height: int, row_bytes: int | None = None,
+                 device: int = 0, stream: int = 0):
+        self.lib = _lib.load()
+        self.ptr, self.width, self.height = int(device_ptr), int(width), int(height)
+        self.row_bytes = int(row_bytes) if row_bytes else 4 * self.width
+        self.device, self.stream = device, stream
+
+    def draw_record(self, verbs, points, weights, rec) -> None:
+        """DrawPath of one scene draw (path arrays + paint record)."""
+        verbs = np.ascontiguousarray(verbs, np.uint8)
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+        wts = np.ascontiguousarray(weights, np.float32)
+        cp = _lib.Path_(verbs.ctypes.data if len(verbs) else None, len(verbs),
+                        pts.ctypes.data if len(pts) else None, len(pts),
+                        wts.ctypes.data if len(wts) else None, len(wts), int(rec["fill_type"]))
+        p = _lib.Paint_()
+        p.style, p.cap, p.join, p.blend_mode = (int(rec["style"]), int(rec["cap"]),
+                                                int(rec["join"]), int(rec["blend"]))
+        p.fill_color[:] = [float(v) for v in rec["fill_color"]]
+        p.stroke_color[:] = [float(v) for v in rec["stroke_color"]]
+        p.stroke_width = float(rec["stroke_width"])
+        p.miter_limit = float(rec["miter"])
+        _lib.check(self.lib.skity_cuda_draw_path_static(self.device, self.ptr, self.width,
+                                                        self.height, self.row_bytes,
+                                                        ctypes.byref(cp), ctypes.byref(p),
+                                                        self.stream or None),
+                   "skity_cuda_draw_path_static")
+
+    def DrawPath(self, path: Path, paint: Paint) -> None:
+        if paint.shader is not None or paint.mask_filter is not None:
+            raise _lib.SkityCudaError(-5, "DeviceCanvas.DrawPath (solid colours only)")
+        rec = paint.rec.copy()
+        rec["fill_type"] = path.fill_type
+        self.draw_record(path.verbs, path.points, path.weights, rec)
+
+    def draw_scene(self, sc) -> int:
+        """Every draw of a scene (solid colours) in order; returns the count."""
+        for d in range(sc.n_draws):
+            v0, v1 = int(sc.verb_off[d]), int(sc.verb_off[d + 1])
+            p0, p1 = int(sc.point_off[d]), int(sc.point_off[d + 1])
+            w0, w1 = int(sc.weight_off[d]), int(sc.weight_off[d + 1])
+            self.draw_record(sc.verbs[v0:v1], sc.points[p0:p1], sc.weights[w0:w1], sc.paints[d])
+        return sc.n_draws

@@ -493,6 +493,39 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   return SKITY_CUDA_SUCCESS;
 }
 
+// Gives every canvas its range of row bands; returns the number of bands.
+inline uint32_t AssignBands(HostBatch& hb) {
+  uint32_t n = 0;
+  for (CanvasDesc& cd : hb.canvases) {
+    cd.band0 = n;
+    n += (cd.h + (1u << kBandShift) - 1) >> kBandShift;
+  }
+  return n;
+}
+// The compositor's pass bins: for every row band, the passes (in pass
+// order, which is draw order within a canvas) that have rows in it.
+inline void BuildBins(const HostBatch& hb, const std::vector<PassComp>& comp, uint32_t n_bands,
+                      std::vector<uint32_t>& band_off, std::vector<uint32_t>& bins) {
+  band_off.assign((size_t)n_bands + 1, 0);
+  for (size_t p = 0; p < comp.size(); ++p) {
+    const PassComp& c = comp[p];
+    if (c.row1 <= c.row0) continue;
+    const uint32_t b0 = hb.canvases[hb.passes[p].canvas].band0;
+    for (int32_t k = c.row0 >> kBandShift; k <= (c.row1 - 1) >> kBandShift; ++k)
+      band_off[b0 + (uint32_t)k + 1]++;
+  }
+  for (uint32_t i = 0; i < n_bands; ++i) band_off[i + 1] += band_off[i];
+  bins.assign(std::max<size_t>(band_off[n_bands], 1), 0);
+  std::vector<uint32_t> fill(band_off.begin(), band_off.end() - 1);
+  for (size_t p = 0; p < comp.size(); ++p) {
+    const PassComp& c = comp[p];
+    if (c.row1 <= c.row0) continue;
+    const uint32_t b0 = hb.canvases[hb.passes[p].canvas].band0;
+    for (int32_t k = c.row0 >> kBandShift; k <= (c.row1 - 1) >> kBandShift; ++k)
+      bins[fill[b0 + (uint32_t)k]++] = (uint32_t)p;
+  }
+}
+
 inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv, uint32_t chunk,
                           std::vector<RowTask>& out) {
   out.clear();

@@ -6,9 +6,9 @@
 //                                  form for very long active lists) writing
 //                                  each row's spans contiguously into the
 //                                  span pool
-//   k_composite  1 warp / row     : replays every pass's spans of the row in
-//                                  draw order into a shared-memory row, then
-//                                  writes the row back (16-byte stores)
+//   k_composite  1 warp / row tile: replays the spans of the row band's
+//                                  passes in draw order into a shared-memory
+//                                  tile, then writes the tile back
 //   k_blur_h/_v  1 thread / row / column of each blur temp canvas: StackBlur
 //
 // Geometry and sweeps are inherently sequential per path (the reference's
@@ -79,11 +79,17 @@ int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
 }
 
 // ---------------------------------------------------------------------------
-// composite: one warp per row task, the row held in shared memory
+// composite: one warp per row tile (x0, x1) of a canvas row, the tile held in
+// shared memory.  The passes come from the row band's bin (draw order); each
+// pass row's spans are loaded 32 at a time, the ones meeting the tile are
+// applied in emission order, in batches of disjoint spans (every pixel's
+// blends stay in the reference's order).
 // ---------------------------------------------------------------------------
 constexpr int kCompWarps = 4;
+// spans up to this many tile pixels are shaded by one lane
+constexpr int kShortSpan = 4;
 
-__global__ void __launch_bounds__(32 * kCompWarps)
+__global__ void __launch_bounds__(32 * kCompWarps, 4)
     k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   uint32_t* smem = (uint32_t*)reg_smem;
@@ -102,14 +108,16 @@ __global__ void __launch_bounds__(32 * kCompWarps)
     row[i] = cd.has_clear ? cd.clear_pm : RGBAtoARGB(gpx[i]);
   }
   __syncwarp();
-  for (uint32_t pb = cd.pass0; pb < cd.pass1; pb += 32) {
-    uint32_t p = pb + lane;
+  const uint32_t band = cd.band0 + ((uint32_t)y >> kBandShift);
+  const uint32_t e0 = b.band_off[band], e1 = b.band_off[band + 1];
+  for (uint32_t eb = e0; eb < e1; eb += 32) {
+    const uint32_t e = eb + lane;
     bool hit = false;
     PassComp pc;
     pc.row0 = pc.row1 = 0;
     pc.rbase = pc.brush = 0;
-    if (p < cd.pass1) {
-      pc = b.comp[p];
+    if (e < e1) {
+      pc = b.comp[b.bins[e]];
       hit = y >= pc.row0 && y < pc.row1;
     }
     uint32_t mask = __ballot_sync(0xffffffffu, hit);
@@ -125,24 +133,57 @@ __global__ void __launch_bounds__(32 * kCompWarps)
       const Brush br = b.brushes[qbrush];
       const uint2* sp = b.spans;
       for (uint32_t sb = s0; sb < s1; sb += 32) {
-        uint2 mine = make_uint2(0, 0);
-        if (sb + lane < s1) mine = sp[sb + lane];
-        const int cnt = (int)min(32u, s1 - sb);
-        for (int j = 0; j < cnt; ++j) {
-          const uint32_t xs_len = __shfl_sync(0xffffffffu, mine.x, j);
-          const uint32_t cover = __shfl_sync(0xffffffffu, mine.y, j);
-          const int sx = (int)(xs_len & 0xFFFF);
-          const int slen = (int)(xs_len >> 16);
-          const int xs = max(sx, x0), xe = min(sx + slen, x1);
-          if (xs >= xe) continue;
-          const uint32_t alpha = cover & br.global_alpha;
-          // each lane owns the pixels whose column is lane mod 32
-          for (int x = xs + ((lane - xs) & 31); x < xe; x += 32) {
-            uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
-            if (alpha != 255) c = AlphaMulQ(c, alpha);
-            uint32_t& d = row[x - x0];
-            d = BlendPixel(d, c, br.blend);
+        int xs = 0, xe = 0;
+        uint32_t alpha = 0;
+        bool pending = false;
+        if (sb + lane < s1) {
+          const uint2 mine = sp[sb + lane];
+          const int sx = (int)(mine.x & 0xFFFF), slen = (int)(mine.x >> 16);
+          xs = max(sx, x0);
+          xe = min(sx + slen, x1);
+          alpha = mine.y & br.global_alpha;
+          pending = xs < xe;
+        }
+        // Spans are applied in batches: the longest run of pending spans
+        // (in emission order) in which each starts at or after the end of
+        // the one before.  Those are disjoint, so inside a batch the order
+        // does not matter: short spans are shaded by their own lane, long
+        // ones by the whole warp (pixel column mod 32 per lane).
+        uint32_t pmask = __ballot_sync(0xffffffffu, pending);
+        while (pmask) {
+          const uint32_t below = pmask & ((1u << lane) - 1u);
+          const int prev = below ? 31 - __clz(below) : lane;
+          const int prev_xe = __shfl_sync(0xffffffffu, xe, prev);
+          const bool clash = pending && below && prev_xe > xs;
+          const uint32_t cmask = __ballot_sync(0xffffffffu, clash);
+          const uint32_t batch = cmask ? pmask & ((1u << (__ffs(cmask) - 1)) - 1u) : pmask;
+          const bool mine_now = (batch >> lane) & 1u;
+          const bool is_short = xe - xs <= kShortSpan;
+          if (mine_now && is_short) {
+            for (int x = xs; x < xe; ++x) {
+              uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+              if (alpha != 255) c = AlphaMulQ(c, alpha);
+              uint32_t& d = row[x - x0];
+              d = BlendPixel(d, c, br.blend);
+            }
           }
+          uint32_t lmask = __ballot_sync(0xffffffffu, mine_now && !is_short);
+          while (lmask) {
+            const int j = __ffs(lmask) - 1;
+            lmask &= lmask - 1;
+            const int qs = __shfl_sync(0xffffffffu, xs, j);
+            const int qe = __shfl_sync(0xffffffffu, xe, j);
+            const uint32_t qa = __shfl_sync(0xffffffffu, alpha, j);
+            for (int x = qs + ((lane - qs) & 31); x < qe; x += 32) {
+              uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+              if (qa != 255) c = AlphaMulQ(c, qa);
+              uint32_t& d = row[x - x0];
+              d = BlendPixel(d, c, br.blend);
+            }
+          }
+          __syncwarp();
+          if (mine_now) pending = false;
+          pmask &= ~batch;
         }
       }
     }

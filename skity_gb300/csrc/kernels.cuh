@@ -38,8 +38,13 @@ struct CanvasDesc {
   uint32_t clear_pm;   // premultiplied ARGB of the clear colour
   uint32_t pass0, pass1;
   int32_t blur_radius; // temp canvases: StackBlur radius (0 = not a temp)
-  uint32_t pad;
+  uint32_t band0;      // first entry of the canvas's row bands in band_off
 };
+
+// Rows of a canvas are grouped in bands of 1 << kBandShift rows; each band
+// lists, in draw order, the passes whose rows meet it (the compositor's
+// pass bins).
+constexpr int kBandShift = 4;
 
 // Geometry scratch layout of one pass: capacities in elements.
 //   cap[0..2]  quad path (verbs, points, weights)
@@ -123,6 +128,8 @@ struct DevBatch {
   uint32_t n_list;
   uint8_t* pass_class;  // sweep form per pass: 0 register sweep, 1 generic
   int32_t reg_diff_cap; // accumulator entries per warp in shared memory
+  const uint32_t* band_off;  // per band: first entry in bins (one past the end follows)
+  const uint32_t* bins;      // pass indices, per band in draw order
 };
 
 // Shared memory of one register-sweep warp: its RegShared block, then an

@@ -255,19 +255,131 @@ struct PoolSink : SinkBase {
     frags += f;
   }
   // The accumulated spans of a row follow its direct spans (the reference
-  // flushes a row's accumulator only after leaving the row).  Returns false
+  // flushes a row's accumulator only after leaving the row,
+  // SpanBuilder::Flush, sw_raster.cc:103-136): the runs of equal nonzero
+  // saturated prefix sums of diff[lo, hi), in increasing x.  Returns false
   // when the row lies outside the canvas (diff not read).
+  //
+  // Each lane takes V consecutive entries per chunk of Lanes::n * V; a run
+  // starts at every entry whose saturated sum differs from its left
+  // neighbour's and ends at the next such entry.  A lane closes the runs
+  // that start at its entries (the last one ends at the next lane's first
+  // start), the lane with the chunk's first start also closes the run left
+  // open by earlier chunks, and the chunk's spans are written after one
+  // prefix sum.  Every entry read is reset to zero.
   SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
     if (y < row0 || y >= row1) return false;
     row_begin(L, y);
-    DiffRuns(L, diff, lo, hi, [&](int s, int w, uint8_t a) {
-      int x = left + s, len = w;
-      if (keep(x, y, len, a)) {
+    constexpr int V = Lanes::n == 32 ? 4 : 1;
+    constexpr int kNone = 0x7fffffff;
+    int open_start = -1;   // warp-uniform: the run still open after a chunk
+    int32_t open_v = 0;
+    int32_t carry = 0;     // prefix sum before this chunk
+    int32_t prev_sat = 0;  // saturated value of the entry before this chunk
+    // Entries outside [lo, hi] are zero, so the chunks can start at a
+    // multiple of V (16-byte loads); a chunk of zeros changes no sum and
+    // starts no run, and is skipped after one load.
+    const bool vec = V == 4 && ((uintptr_t)diff & 15) == 0;
+    for (int base = vec ? (lo & ~(V - 1)) : lo; base < hi; base += Lanes::n * V) {
+      const int i0 = base + L.lane * V;
+      int32_t sat[V];
+      if (vec && i0 + V <= hi) {
+        const int4 q = *(const int4*)(diff + i0);
+        sat[0] = q.x;
+        sat[1 % V] = q.y;
+        sat[2 % V] = q.z;
+        sat[3 % V] = q.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) sat[j] = i0 + j < hi ? diff[i0 + j] : 0;
+      }
+      bool nz = false;
+#pragma unroll
+      for (int j = 0; j < V; ++j) nz |= sat[j] != 0;
+      if (!L.ballot(nz)) continue;
+      if (nz) {
+#pragma unroll
+        for (int j = 0; j < V; ++j)
+          if (i0 + j < hi) diff[i0 + j] = 0;
+      }
+      int32_t run = 0;
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        run += sat[j];
+        sat[j] = run;
+      }
+      const int32_t incl = LaneScanIncl(L, run);
+      const int32_t pre = incl - run + carry;
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        const int32_t v = sat[j] + pre;
+        sat[j] = v > 255 ? 255 : v;
+      }
+      int32_t before = LaneBcast(L, sat[V - 1], L.lane > 0 ? L.lane - 1 : 0);
+      if (L.lane == 0) before = prev_sat;
+      unsigned bits = 0;
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        const int32_t b = j == 0 ? before : sat[j - 1];
+        if (i0 + j < hi && sat[j] != b) bits |= 1u << j;
+      }
+      const unsigned has = L.ballot(bits != 0);
+      const int first_pos = bits ? i0 + Lanes::ffs(bits) - 1 : kNone;
+      const unsigned later = has & ~((2u << L.lane) - 1u);
+      int next_first = (int)L.shfl((uint32_t)first_pos, later ? Lanes::ffs(later) - 1 : L.lane);
+      if (!later) next_first = kNone;
+      // this lane's spans, in x order
+      uint2 out[V + 1];
+      int cnt = 0;
+      unsigned long long fr = 0;
+      auto put = [&](int s0, int w, int32_t a) {
+        int x = left + s0, len = w;
+        if (keep(x, y, len, (uint8_t)a)) {
+          out[cnt++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)a);
+          fr += (unsigned)len;
+        }
+      };
+      if (has && open_start >= 0 && L.lane == Lanes::ffs(has) - 1)
+        put(open_start, first_pos - open_start, open_v);
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        if (!(bits & (1u << j))) continue;
+        const unsigned rest = bits & ~((2u << j) - 1u);
+        const int end = rest ? i0 + Lanes::ffs(rest) - 1 : next_first;
+        if (end != kNone && sat[j] != 0) put(i0 + j, end - (i0 + j), sat[j]);
+      }
+      // the run left open: the chunk's last start, if any
+      if (has) {
+        const int src = 31 - clz_(has);
+        const int lb = 31 - clz_(bits ? bits : 1u);
+        const int32_t lv = sat[lb];
+        const int lpos = i0 + lb;
+        const int32_t v = LaneBcast(L, lv, Lanes::n == 32 ? src : 0);
+        const int pos = LaneBcast(L, lpos, Lanes::n == 32 ? src : 0);
+        open_start = v != 0 ? pos : -1;
+        open_v = v;
+      }
+      const int32_t ci = LaneScanIncl(L, cnt);
+      const uint32_t total = (uint32_t)LaneBcast(L, ci, Lanes::n - 1);
+      if (total) {
+        const uint64_t at = reserve(L, 0, total);
+        uint2* dst = span_ptr(at + (uint32_t)(ci - cnt));
+        if (dst) {
+          for (int i = 0; i < cnt; ++i) dst[i] = out[i];
+        }
+        commit(L, total, LaneSum64(L, fr));
+      }
+      carry += LaneBcast(L, incl, Lanes::n - 1);
+      prev_sat = LaneBcast(L, sat[V - 1], Lanes::n - 1);
+    }
+    if (open_start >= 0) {
+      int x = left + open_start, len = hi - open_start;
+      if (keep(x, y, len, (uint8_t)open_v)) {
         const uint64_t at = reserve(L, 0, 1);
-        if (!dead && L.leader()) pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+        if (!dead && L.leader()) pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
         commit(L, 1, (unsigned)len);
       }
-    });
+    }
     return true;
   }
 };
@@ -478,8 +590,9 @@ SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* 
   const int y = (int)rt.y, x0 = (int)rt.x0, x1 = (int)rt.x1;
   uint32_t* gpx = (uint32_t*)(b.pixels + cd.px_off) + (size_t)y * cd.w + x0;
   for (int i = 0; i < x1 - x0; ++i) row[i] = cd.has_clear ? cd.clear_pm : RGBAtoARGB(gpx[i]);
-  for (uint32_t p = cd.pass0; p < cd.pass1; ++p) {
-    const PassComp pc = b.comp[p];
+  const uint32_t band = cd.band0 + ((uint32_t)y >> kBandShift);
+  for (uint32_t e = b.band_off[band]; e < b.band_off[band + 1]; ++e) {
+    const PassComp pc = b.comp[b.bins[e]];
     if (y < pc.row0 || y >= pc.row1) continue;
     const uint2 rs = b.rowspan[pc.rbase + (y - pc.row0)];
     const Brush br = b.brushes[pc.brush];

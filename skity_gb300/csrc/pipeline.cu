@@ -69,9 +69,31 @@ struct DeviceBatch {
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
   DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
   DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
+  DevBuf band_off, bins;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
+  std::vector<uint32_t> h_band_off, h_bins;
   uint32_t chunk = 1024;
+  uint32_t n_bands = 0;
+  // true when the caller has loaded the canvases' current pixels (a canvas
+  // flush without a clear); otherwise a canvas without a clear colour starts
+  // from transparent black, as a fresh Bitmap does
+  bool keep_pixels = false;
   bool uploaded = false;
+  // Replay of the planned render as one CUDA graph (device-resident
+  // batches): the plan -- scratch capacities, sweep buffers, row tables,
+  // bins -- depends only on the batch's inputs, so a re-render can run the
+  // same launches on the same buffers without host round trips.
+  bool want_graph = false;
+  bool graph_ok = false;
+  cudaGraphExec_t graphs[5] = {};
+  DevBatch planned{};
+  uint64_t planned_rows = 0;
+  const void* planned_pool = nullptr;  // the context span pool the plan used
+  skity_cuda_stats planned_stats{};
+  ~DeviceBatch() {
+    for (auto g : graphs)
+      if (g) cudaGraphExecDestroy(g);
+  }
   std::vector<PassGeom> h_geom;
   skity_cuda_stats stats{};
 };
@@ -87,6 +109,7 @@ struct skity_cuda_context_s {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t stage[10] = {};
+  uint32_t tile_w = 256;  // composite row-tile width in pixels
   skity_cuda_stats last{};
   std::mutex mu;
 };
@@ -125,6 +148,7 @@ static int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.pts, hb.pts, s));
   SKC_TRY(Upload(db.weights, hb.weights, s));
   SKC_TRY(Upload(db.draws, hb.draws, s));
+  db.n_bands = AssignBands(hb);
   SKC_TRY(Upload(db.canvases, hb.canvases, s));
   SKC_TRY(Upload(db.brushes, hb.brushes, s));
   SKC_TRY(Upload(db.stop_colors, hb.stop_colors, s));
@@ -132,7 +156,7 @@ static int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.temps, hb.temp_canvases, s));
   uint32_t maxw = 1;
   for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
-  db.chunk = std::min<uint32_t>(maxw, 2048);
+  db.chunk = std::min<uint32_t>(maxw, std::max<uint32_t>(32, std::min<uint32_t>(ctx->tile_w, 2048)));
   BuildRowTasks(hb, hb.main_canvases, db.chunk, db.h_tasks_main);
   BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
   SKC_TRY(Upload(db.tasks_main, db.h_tasks_main, s));
@@ -147,8 +171,148 @@ static int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   return SKITY_CUDA_SUCCESS;
 }
 
-// Full render of a resident batch; pixels stay on the device.
+// The launches of a planned render, in five parts (so that the stages can
+// be timed between graph launches): 0 canvases without a clear colour
+// zeroed and the geometry of every pass; 1 sweep-state resets and the
+// sweeps; 2 composite of the blur temp canvases; 3 StackBlur; 4 composite
+// of the main canvases.  Returns the number of kernel launches.
+static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream_t s, int part) {
+  HostBatch& hb = db.hb;
+  DevBatch b = db.planned;
+  const uint32_t np = b.n_passes;
+  b.pass_list = nullptr;
+  b.n_list = np;
+  switch (part) {
+    case 0:
+      if (!db.keep_pixels) {
+        for (uint32_t c : hb.main_canvases) {
+          const CanvasDesc& cd = hb.canvases[c];
+          if (!cd.has_clear)
+            cudaMemsetAsync(db.pixels.as<uint8_t>() + cd.px_off, 0, (size_t)cd.w * cd.h * 4, s);
+        }
+      }
+      return LaunchGeometry(b, s);
+    case 1:
+      cudaMemsetAsync(db.rowspan.p, 0, std::max<uint64_t>(db.planned_rows, 1) * sizeof(uint2), s);
+      cudaMemsetAsync(db.err.p, 0, 16, s);
+      cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s);
+      cudaMemsetAsync(ctx->span_next.p, 0, 8, s);
+      return LaunchSweep(b, s);
+    case 2:
+      if (db.h_tasks_temp.empty()) return 0;
+      return LaunchComposite(b, db.tasks_temp.as<RowTask>(), (uint32_t)db.h_tasks_temp.size(),
+                             db.chunk, s);
+    case 3:
+      if (db.h_tasks_temp.empty()) return 0;
+      return LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
+                        hb.max_temp_h, hb.max_temp_w, s);
+    default:
+      return LaunchComposite(b, db.tasks_main.as<RowTask>(), (uint32_t)db.h_tasks_main.size(),
+                             db.chunk, s);
+  }
+}
+
+// Milliseconds between two recorded events (0 if the runtime cannot say;
+// the error is cleared so it does not surface at a later call).
+static double ElapsedMs(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.0;
+  }
+  return (double)ms;
+}
+static double StageMs(skity_cuda_context_s* ctx, int a, int b) {
+  return ElapsedMs(ctx->stage[a], ctx->stage[b]);
+}
+
+static void DropReplay(DeviceBatch& db) {
+  for (auto& g : db.graphs) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  db.graph_ok = false;
+}
+
+// Records the replay graphs of a batch whose plan is current.
+static void CaptureReplay(skity_cuda_context_s* ctx, DeviceBatch& db) {
+  DropReplay(db);
+  cudaStream_t s = ctx->stream;
+  bool ok = true;
+  for (int part = 0; part < 5 && ok; ++part) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      ok = false;
+      break;
+    }
+    const int n = EnqueuePlanned(ctx, db, s, part);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || !g) {
+      ok = false;
+    } else if (n > 0 || part == 0 || part == 1) {
+      if (cudaGraphInstantiate(&db.graphs[part], g, 0) != cudaSuccess) {
+        db.graphs[part] = nullptr;
+        ok = false;
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+  }
+  cudaGetLastError();
+  if (!ok) {
+    DropReplay(db);
+    return;
+  }
+  db.graph_ok = true;
+}
+
+static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed);
+
+// Render of a resident batch; pixels stay on the device.  A batch whose
+// replay graph is current re-renders with one graph launch; the graph's
+// device self-checks (error word, span pool use) are read back, and any
+// surprise falls back to a full planned render.
 static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
+  if (db.graph_ok && db.planned_pool == ctx->span_pool.p) {
+    cudaStream_t s = ctx->stream;
+    static const int kStageEv[5][2] = {{0, 1}, {4, 5}, {6, 7}, {7, 8}, {8, 9}};
+    SKC_TRY(cudaEventRecord(ctx->ev0, s));
+    for (int part = 0; part < 5; ++part) {
+      if (part != 3) SKC_TRY(cudaEventRecord(ctx->stage[kStageEv[part][0]], s));
+      if (db.graphs[part]) SKC_TRY(cudaGraphLaunch(db.graphs[part], s));
+      SKC_TRY(cudaEventRecord(ctx->stage[kStageEv[part][1]], s));
+    }
+    SKC_TRY(cudaEventRecord(ctx->ev1, s));
+    uint32_t err = 0;
+    unsigned long long used = 0;
+    SKC_TRY(cudaMemcpyAsync(&err, db.err.p, 4, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaMemcpyAsync(&used, ctx->span_next.p, 8, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaStreamSynchronize(s));
+    if (err == 0 && used <= db.planned.span_cap) {
+      skity_cuda_stats st = db.planned_stats;
+      st.device_ms = ElapsedMs(ctx->ev0, ctx->ev1);
+      st.geometry_ms = StageMs(ctx, 0, 1);
+      st.sweep_count_ms = 0;
+      st.sweep_emit_ms = StageMs(ctx, 4, 5);
+      st.composite_ms = StageMs(ctx, 6, 7) + StageMs(ctx, 8, 9);
+      st.blur_ms = StageMs(ctx, 7, 8);
+      st.retries = 0;
+      st.graph_replays = 1;
+      db.stats = st;
+      return SKITY_CUDA_SUCCESS;
+    }
+    DropReplay(db);
+  }
+  int32_t rc = PlanAndRender(ctx, db, timed);
+  if (rc == SKITY_CUDA_SUCCESS && db.want_graph) {
+    db.planned_pool = ctx->span_pool.p;
+    CaptureReplay(ctx, db);
+  }
+  return rc;
+}
+
+// Full render of a resident batch with planning (geometry sizes read back,
+// sweep buffers and bins built on the host); pixels stay on the device.
+static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
   cudaStream_t s = ctx->stream;
   HostBatch& hb = db.hb;
   const uint32_t np = (uint32_t)hb.passes.size();
@@ -156,6 +320,13 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   st.draws = hb.draw_count;
   st.passes = np;
   if (timed) SKC_TRY(cudaEventRecord(ctx->ev0, s));
+  if (!db.keep_pixels) {
+    for (uint32_t c : hb.main_canvases) {
+      const CanvasDesc& cd = hb.canvases[c];
+      if (!cd.has_clear)
+        SKC_TRY(cudaMemsetAsync(db.pixels.as<uint8_t>() + cd.px_off, 0, (size_t)cd.w * cd.h * 4, s));
+    }
+  }
 
   // ---- geometry with scratch-capacity retries
   std::vector<uint32_t> todo(np);
@@ -224,6 +395,9 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   std::vector<PassComp> comp;
   PlanComp(hb, db.h_geom, sw, comp);
   SKC_TRY(Upload(db.comp, comp, s));
+  BuildBins(hb, comp, db.n_bands, db.h_band_off, db.h_bins);
+  SKC_TRY(Upload(db.band_off, db.h_band_off, s));
+  SKC_TRY(Upload(db.bins, db.h_bins, s));
   // span indices are 32-bit
   const uint64_t kMaxPool = 0xFFFFFFFFull;
   uint64_t want = std::min<uint64_t>(std::max<uint64_t>(pl.span_estimate, 1 << 16), kMaxPool);
@@ -251,6 +425,8 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
   b.pass_class = db.pass_class.as<uint8_t>();
   b.reg_diff_cap = RegDiffCap(pl);
   b.comp = db.comp.as<PassComp>();
+  b.band_off = db.band_off.as<uint32_t>();
+  b.bins = db.bins.as<uint32_t>();
   b.span_next = ctx->span_next.as<unsigned long long>();
   // The sweep; if the span pool ran out it is grown to the size the sweep
   // reported and the sweep runs again (first renders of a context only).
@@ -271,9 +447,7 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
     SKC_TRY(cudaStreamSynchronize(s));
     if (used <= b.span_cap) break;
     if (attempt == 2 || used > kMaxPool) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->stage[4], ctx->stage[5]);
-    discarded_ms += ms;
+    discarded_ms += StageMs(ctx, 4, 5);
     const uint64_t grow = std::min<uint64_t>(used + used / 16, kMaxPool);
     if (ctx->budget && grow * sizeof(uint2) > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
     ctx->span_pool.release();
@@ -311,22 +485,13 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
     std::fprintf(stderr, "skity_cuda: device self-check failed (code %u)\n", err);
     return SKITY_CUDA_ERROR_DEVICE;
   }
-  if (timed) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    st.device_ms = ms;
-  }
-  {
-    auto el = [&](int a, int b2) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ctx->stage[a], ctx->stage[b2]);
-      return (double)ms;
-    };
-    st.geometry_ms = el(0, 1);
-    st.sweep_emit_ms = el(4, 5);
-    st.composite_ms = el(6, 7) + el(8, 9);
-    st.blur_ms = el(7, 8);
-  }
+  if (timed) st.device_ms = ElapsedMs(ctx->ev0, ctx->ev1);
+  st.geometry_ms = StageMs(ctx, 0, 1);
+  st.sweep_emit_ms = StageMs(ctx, 4, 5);
+  st.composite_ms = StageMs(ctx, 6, 7) + StageMs(ctx, 8, 9);
+  st.blur_ms = StageMs(ctx, 7, 8);
+  db.planned = b;
+  db.planned_rows = rows;
   for (uint32_t c : hb.main_canvases) st.pixels += (uint64_t)hb.canvases[c].w * hb.canvases[c].h;
   if (np) {
     std::vector<uint32_t> pspans(np);
@@ -339,6 +504,7 @@ static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool time
     }
   }
   db.stats = st;
+  db.planned_stats = st;
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -489,6 +655,7 @@ SKITY_CUDA_API int32_t skity_cuda_batch_create(skity_cuda_context ctx, uint32_t 
   b->ctx = ctx;
   int32_t rc = skc::BuildFromStreams(b->db, count, streams, stream_bytes);
   if (!rc) rc = skc::UploadBatch(ctx, b->db);
+  b->db.want_graph = true;
   if (rc) {
     delete b;
     return rc;
@@ -683,6 +850,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   rc = skc::UploadBatch(ctx, db);
   if (rc) return rc;
   const skc::CanvasDesc& cd = db.hb.canvases[db.hb.main_canvases[0]];
+  db.keep_pixels = !canvas->has_clear;
   if (!canvas->has_clear) {
     // draws blend over the bitmap's current pixels
     cudaError_t e = cudaMemcpy2DAsync(db.pixels.as<uint8_t>() + cd.px_off, (size_t)cd.w * 4,

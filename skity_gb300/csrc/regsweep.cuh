@@ -24,7 +24,37 @@
 namespace skc {
 
 constexpr int kRegMaxM = 128;  // active edges held in registers
-constexpr int kStageSpans = 8;  // direct spans a lane stages per interval
+// intervals of one step: at most one per pair of active edges, plus the one
+// left open by a culled right edge
+constexpr int kMaxIntervals = kRegMaxM / 2 + 4;
+
+// TrapRow set-ups of a step's intervals, one array per field.
+template <int N>
+struct TrapRowSoA {
+  int32_t ul[N], ur[N], ll[N], lr[N], ldy[N], rdy[N];
+  uint32_t meta[N];  // full | real << 8
+  SKC_HD void put(int i, const TrapRow& t) {
+    ul[i] = t.ul;
+    ur[i] = t.ur;
+    ll[i] = t.ll;
+    lr[i] = t.lr;
+    ldy[i] = t.lDY;
+    rdy[i] = t.rDY;
+    meta[i] = (uint32_t)t.full | (t.real ? 0x100u : 0u);
+  }
+  SKC_HD TrapRow get(int i) const {
+    TrapRow t;
+    t.ul = ul[i];
+    t.ur = ur[i];
+    t.ll = ll[i];
+    t.lr = lr[i];
+    t.lDY = ldy[i];
+    t.rDY = rdy[i];
+    t.full = (uint8_t)(meta[i] & 0xFF);
+    t.real = (meta[i] & 0x100u) != 0;
+    return t;
+  }
+};
 
 // Per-warp shared block of the register sweep.
 struct RegShared {
@@ -36,11 +66,13 @@ struct RegShared {
   int32_t dxf[kRegMaxM];  // dx after the update
   int32_t ia[kRegMaxM];   // interval k: left position
   int32_t ib[kRegMaxM];   //   right position
-  int32_t ax[kRegMaxM];   // active x at insertion time
+  int32_t ax[kRegMaxM];   // active x at insertion; new rank by list position in the reorder
   // edge state by new list position (reorder and insertion)
   int32_t p_idx[kRegMaxM], p_x[kRegMaxM], p_dx[kRegMaxM], p_dy[kRegMaxM];
   int32_t p_low[kRegMaxM], p_wc[kRegMaxM];
-  uint2 stage[32 * kStageSpans];  // each lane's direct spans of a step
+  // the step's intervals (blit_trapezoid_row set-ups) and their first span
+  TrapRowSoA<kMaxIntervals> iv;
+  int32_t iv_start[kMaxIntervals + 4];
   uint8_t surv[kRegMaxM];  // 1: survives the step
 };
 // Host and device must agree on this size (the host sizes the launch).
@@ -92,61 +124,28 @@ SKC_HD void AccFlushIfNeed(const Lanes& L, AccState& a, Sink* sink, int row) {
   a.y = row;
 }
 
-// Lane-local output of one interval's trapezoid row: direct spans go to
-// `write` when set, else the first kStageSpans of them to `stage`.
-template <typename Sink>
-struct RegOut {
-  Sink* sink;
-  AccState* as;
-  int y;
-  bool do_acc;
-  uint32_t kept;
-  unsigned long long frags;
-  uint2* write;
-  uint2* stage;
-  int lo, hi;
-  SKC_HD void real(int x, int len, uint8_t a) {
-    if (!sink->keep(x, y, len, a)) return;
-    kept++;
-    frags += (unsigned)len;
-    const uint2 v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
-    if (write) *write++ = v;
-    else if (kept <= (uint32_t)kStageSpans) stage[kept - 1] = v;
-  }
-  SKC_HD void acc(int x, int len, uint8_t a) {
-    if (!do_acc) return;
-    int o0 = x - as->left, o1 = o0 + len;
-    o0 = max_(o0, 0);
-    o1 = min_(o1, as->width);
-    if (o0 >= o1) return;
-    lo = min_(lo, o0);
-    hi = max_(hi, o1);
-    if (a == 0) return;
-    AtomicAddI32(&as->diff[o0], (int32_t)a);
-    AtomicAddI32(&as->diff[o1], -(int32_t)a);
-  }
-};
-
 // The intervals [0, K) of a step, then (trailing_a >= 0) the interval left
-// open by the last left edge: blit_trapezoid_row for each, one interval per
-// lane, direct spans written in interval order.
+// open by the last left edge: blit_trapezoid_row for each, in two passes.
+// First one lane per interval does the row's set-up and counts its spans;
+// then the step's spans, numbered in interval order, are spread over the
+// lanes (span g on lane g mod 32), so a long partial row does not hold one
+// lane while the others wait.  Direct spans are written in that order, the
+// others go to the row accumulator.
 template <typename Sink>
 SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, const Edge* W,
                     int n, int y, Fixed next_y, int K, int m, int k, uint8_t full,
                     Fixed left_clip, Fixed right_clip, int trailing_a, bool trailing_nr) {
+  constexpr int NL = Lanes::n;
   const int total = K + (trailing_a >= 0 ? 1 : 0);
   AccFlushIfNeed(L, as, sink, y);
   sink->row_begin(L, y);
-  uint2* stage = sh.stage + L.lane * kStageSpans;
-  uint32_t run = 0;
-  unsigned long long frags = 0;
-  int lo = 0x7fffffff, hi = -1;
-  for (int kb = 0; kb < total; kb += Lanes::n) {
+  int carry = 0;
+  for (int kb = 0; kb < total; kb += NL) {
     const int ki = kb + L.lane;
-    const bool valid = ki < total;
-    Fixed ul = 0, ur = 0, ll = 0, lr = 0, lDY = 0, rDY = 0;
-    bool nr = false;
-    if (valid) {
+    int cnt = 0;
+    if (ki < total) {
+      Fixed ul, ur, ll, lr, lDY, rDY;
+      bool nr;
       if (ki < K) {
         const int a = sh.ia[ki], b = sh.ib[ki];
         ul = max_(sh.xo[a], left_clip);
@@ -193,41 +192,61 @@ SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, con
         rDY = 0;
         nr = trailing_nr;
       }
+      TrapRow t;
+      if (TrapPrepare(t, ul, ur, ll, lr, lDY, rDY, full, nr)) {
+        cnt = TrapCount(t);
+        sh.iv.put(ki, t);
+      }
     }
-    RegOut<Sink> o;
-    o.sink = sink;
-    o.as = &as;
-    o.y = y;
-    o.do_acc = true;
-    o.kept = 0;
-    o.frags = 0;
-    o.write = nullptr;
-    o.stage = stage;
-    o.lo = 0x7fffffff;
-    o.hi = -1;
-    if (valid) TrapezoidRow(o, ul, ur, ll, lr, lDY, rDY, full, nr);
-    lo = min_(lo, o.lo);
-    hi = max_(hi, o.hi);
-    const int32_t incl = LaneScanIncl(L, (int32_t)o.kept);
-    const uint32_t chunk_total = (uint32_t)LaneBcast(L, incl, Lanes::n - 1);
-    if (chunk_total) {
-      const uint64_t at = sink->reserve(L, run, chunk_total);
-      uint2* dst = sink->span_ptr(at + run + (uint32_t)(incl - (int32_t)o.kept));
-      if (valid && o.kept && dst) {
-        if (o.kept <= (uint32_t)kStageSpans) {
-          for (uint32_t i = 0; i < o.kept; ++i) dst[i] = stage[i];
-        } else {  // more than the stage holds: run the row again, writing
-          RegOut<Sink> w = o;
-          w.do_acc = false;
-          w.kept = 0;
-          w.frags = 0;
-          w.write = dst;
-          TrapezoidRow(w, ul, ur, ll, lr, lDY, rDY, full, nr);
+    const int32_t incl = LaneScanIncl(L, cnt);
+    if (ki < total) sh.iv_start[ki] = carry + incl - cnt;
+    carry += LaneBcast(L, incl, NL - 1);
+  }
+  if (L.leader()) sh.iv_start[total] = carry;
+  L.sync();
+  const int T = carry;
+  uint32_t run = 0;
+  unsigned long long frags = 0;
+  int lo = 0x7fffffff, hi = -1;
+  int iv = 0;
+  for (int gb = 0; gb < T; gb += NL) {
+    const int g = gb + L.lane;
+    bool kept = false;
+    uint2 v = make_uint2(0, 0);
+    if (g < T) {
+      while (sh.iv_start[iv + 1] <= g) ++iv;
+      const TrapRow t = sh.iv.get(iv);
+      int x = 0, len = 0;
+      uint8_t a = 0;
+      TrapSpan(t, g - sh.iv_start[iv], x, len, a);
+      if (t.real) {
+        if (sink->keep(x, y, len, a)) {
+          kept = true;
+          v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+          frags += (unsigned)len;
+        }
+      } else {
+        int o0 = x - as.left, o1 = o0 + len;
+        o0 = max_(o0, 0);
+        o1 = min_(o1, as.width);
+        if (o0 < o1) {
+          lo = min_(lo, o0);
+          hi = max_(hi, o1);
+          if (a != 0) {
+            AtomicAddI32(&as.diff[o0], (int32_t)a);
+            AtomicAddI32(&as.diff[o1], -(int32_t)a);
+          }
         }
       }
     }
-    run += chunk_total;
-    frags += o.frags;
+    const unsigned km = L.ballot(kept);
+    const uint32_t cnt = (uint32_t)Lanes::popc(km);
+    if (cnt) {
+      const uint64_t at = sink->reserve(L, run, cnt);
+      uint2* dst = sink->span_ptr(at + run + (uint32_t)Lanes::popc(km & L.lt_mask()));
+      if (kept && dst) *dst = v;
+      run += cnt;
+    }
   }
   frags = LaneSum64(L, frags);
   lo = LaneMin(L, lo);
@@ -393,38 +412,59 @@ SKC_HD int RegWalk(const Lanes& L, RegShared& sh, Edge* W, int n, Sink* sink, Ac
       m2 = before;
     }
     if (L.ballot(inv)) {
-      // some survivor moves: rank = stable position by new x; the intersection
-      // check compares with the last earlier survivor whose x is not greater
-      int32_t bestx[S];
-      int best[S];
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        r_rank[s] = 0;
-        best[s] = -1;
-        bestx[s] = 0;
-      }
-      for (int i = 0; i < m; ++i) {
-        if (!sh.surv[i]) continue;
-        const int32_t xi = sh.xf[i];
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const int p = s * NL + L.lane;
-          const int32_t xj = r_x[s];
-          if (xi < xj || (xi == xj && i < p)) r_rank[s]++;
-          if (i < p && xi <= xj && (best[s] < 0 || xi >= bestx[s])) {
-            best[s] = i;
-            bestx[s] = xi;
-          }
-        }
-      }
-      cross = false;
+      // Some survivor moved left of an earlier one.  The reference ripples
+      // each such edge backwards (backward_insert_edge_based_on_x), which
+      // leaves the survivors stably sorted by new x; its crossing check then
+      // compares an edge with its predecessor at that moment: the latest
+      // (in sorted order) earlier-listed survivor whose x is not greater.
+      // Sort the survivors' (x, list position) keys in place by odd-even
+      // transposition (the list is nearly sorted, so few phases run), then
+      // find each one's predecessor by a short backward scan.
+      int32_t* kx = sh.p_x;
+      int32_t* kp = sh.p_idx;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         const int p = s * NL + L.lane;
-        if (s < ns && p < m && sh.surv[p] && best[s] >= 0 &&
-            wadd(bestx[s], sh.dxf[best[s]]) > wadd(r_x[s], r_dx[s]))
-          cross = true;
+        if (s < ns && p < m && sh.surv[p]) {
+          kx[r_rank[s]] = r_x[s];
+          kp[r_rank[s]] = p;
+        }
       }
+      L.sync();
+      bool dirty_prev = true;
+      for (int phase = 0; phase < m2 + 2; ++phase) {
+        bool swapped = false;
+        for (int i = 2 * L.lane + (phase & 1); i + 1 < m2; i += 2 * NL) {
+          const int32_t xa = kx[i], xb = kx[i + 1];
+          const int32_t pa = kp[i], pb = kp[i + 1];
+          if (xb < xa || (xb == xa && pb < pa)) {
+            kx[i] = xb;
+            kx[i + 1] = xa;
+            kp[i] = pb;
+            kp[i + 1] = pa;
+            swapped = true;
+          }
+        }
+        L.sync();
+        const bool dirty = L.ballot(swapped) != 0;
+        if (!dirty && !dirty_prev) break;
+        dirty_prev = dirty;
+      }
+      cross = false;
+      for (int r = L.lane; r < m2; r += NL) {
+        const int pr = kp[r];
+        sh.ax[pr] = r;
+        int q = r - 1;
+        while (q >= 0 && kp[q] > pr) --q;
+        if (q >= 0 && wadd(kx[q], sh.dxf[kp[q]]) > wadd(kx[r], sh.dxf[pr])) cross = true;
+      }
+      L.sync();
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (s < ns && p < m && sh.surv[p]) r_rank[s] = sh.ax[p];
+      }
+      L.sync();
     }
     lmin = LaneMin(L, lmin);
     nny = min_(nny, lmin);

@@ -266,6 +266,163 @@ SKC_HD void TrapezoidRow(Out& out, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed
   }
 }
 
+// The same row in indexed form, for span-parallel blits: TrapPrepare does
+// blit_trapezoid_row's set-up (false: the row emits nothing), TrapCount the
+// number of out.real / out.acc calls it makes, TrapSpan the k-th of them
+// (x, len, alpha; direct when `real`, an accumulator add otherwise), in the
+// order TrapezoidRow makes them.
+struct TrapRow {
+  Fixed ul, ur, ll, lr, lDY, rDY;
+  uint8_t full;
+  bool real;
+};
+
+SKC_HD bool TrapPrepare(TrapRow& t, Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY,
+                        uint8_t full, bool no_real) {
+  if (ul > ur) return false;
+  if (ll > lr) ll = lr = approximate_intersection(ul, ll, ur, lr);
+  if (ul == ur && ll == lr) return false;
+  if (ul > ll) swap_(ul, ll);
+  if (ur > lr) swap_(ur, lr);
+  t.ul = ul;
+  t.ur = ur;
+  t.ll = ll;
+  t.lr = lr;
+  t.lDY = lDY;
+  t.rDY = rDY;
+  t.full = full;
+  t.real = full == 0xFF && !no_real;
+  return true;
+}
+
+SKC_HD int AaaCount(Fixed ul, Fixed lr) {
+  const int len = FixedCeilToInt(lr) - FixedFloorToInt(ul);
+  return len > 0 ? len : 0;
+}
+
+SKC_HD int TrapCount(const TrapRow& t) {
+  const Fixed joinLeft = FixedCeilToFixed(t.ll);
+  const Fixed joinRite = FixedFloorToFixed(t.ur);
+  if (joinLeft > joinRite) return AaaCount(t.ul, t.lr);
+  int c = 0;
+  if (t.ul < joinLeft) {
+    const int len = FixedCeilToInt(joinLeft - t.ul);
+    c += len <= 2 ? len : AaaCount(t.ul, joinLeft);
+  }
+  if (joinLeft < joinRite) c += 1;
+  if (t.lr > joinRite) {
+    const int len = FixedCeilToInt(t.lr - joinRite);
+    c += len <= 2 ? len : AaaCount(joinRite, t.lr);
+  }
+  return c;
+}
+
+// Pixel i of blit_aaa_trapezoid_row (AaaRow above).
+SKC_HD void AaaSpan(Fixed ul, Fixed ur, Fixed ll, Fixed lr, Fixed lDY, Fixed rDY, uint8_t full,
+                    bool real, int i, int& x, int& len, uint8_t& a) {
+  const int L0 = FixedFloorToInt(ul), R = FixedCeilToInt(lr);
+  len = 1;
+  if (R - L0 == 1) {
+    const uint8_t t = trapezoid_to_alpha(ur - ul, lr - ll);
+    x = L0;
+    a = real ? t : partial_alpha_a(t, full);
+    return;
+  }
+  const int uL = FixedFloorToInt(ul), lL = FixedCeilToInt(ll);
+  const int uR = FixedFloorToInt(ur), lR = FixedCeilToInt(lr);
+  const bool two_left = uL + 2 == lL, two_right = uR + 2 == lR;
+  const int px = L0 + i;
+  const int n = R - L0;
+  uint8_t v = full;
+  if (two_left) {
+    if (i <= 1) {
+      const Fixed first = IntToFixed(uL) + kFixed1 - ul;
+      const uint8_t la = i == 0 ? (uint8_t)(full - partial_triangle_to_alpha(first, lDY))
+                                : partial_triangle_to_alpha(ll - ul - first, lDY);
+      v = v > la ? (uint8_t)(v - la) : 0;
+    }
+  } else if (px >= uL && px < lL) {
+    const uint8_t t = triangle_entry(true, ul - IntToFixed(uL), ll - IntToFixed(uL), lDY, full, px - uL);
+    v = v > t ? (uint8_t)(v - t) : 0;
+  }
+  if (two_right) {
+    if (i >= n - 2) {
+      const Fixed first = IntToFixed(uR) + kFixed1 - ur;
+      const uint8_t ra = i == n - 2 ? partial_triangle_to_alpha(first, rDY)
+                                    : (uint8_t)(full - partial_triangle_to_alpha(lr - ur - first, rDY));
+      v = v > ra ? (uint8_t)(v - ra) : 0;
+    }
+  } else if (px >= uR && px < lR) {
+    const uint8_t t = triangle_entry(false, ur - IntToFixed(uR), lr - IntToFixed(uR), rDY, full, px - uR);
+    v = v > t ? (uint8_t)(v - t) : 0;
+  }
+  x = px;
+  a = v;
+}
+
+SKC_HD void TrapSpan(const TrapRow& t, int k, int& x, int& len, uint8_t& a) {
+  const Fixed joinLeft = FixedCeilToFixed(t.ll);
+  const Fixed joinRite = FixedFloorToFixed(t.ur);
+  if (joinLeft > joinRite) {
+    AaaSpan(t.ul, t.ur, t.ll, t.lr, t.lDY, t.rDY, t.full, t.real, k, x, len, a);
+    return;
+  }
+  if (t.ul < joinLeft) {
+    const int n = FixedCeilToInt(joinLeft - t.ul);
+    if (n == 1) {
+      if (k == 0) {
+        const uint8_t v = trapezoid_to_alpha(joinLeft - t.ul, joinLeft - t.ll);
+        x = t.ul >> 16;
+        len = 1;
+        a = t.real ? v : partial_alpha_a(v, t.full);
+        return;
+      }
+      k -= 1;
+    } else if (n == 2) {
+      if (k < 2) {
+        const Fixed first = joinLeft - kFixed1 - t.ul;
+        x = (t.ul >> 16) + k;
+        len = 1;
+        a = k == 0 ? partial_triangle_to_alpha(first, t.lDY)
+                   : (uint8_t)(t.full - partial_triangle_to_alpha(t.ll - t.ul - first, t.lDY));
+        return;
+      }
+      k -= 2;
+    } else {
+      const int c = AaaCount(t.ul, joinLeft);
+      if (k < c) {
+        AaaSpan(t.ul, joinLeft, t.ll, joinLeft, t.lDY, kMaxS32, t.full, t.real, k, x, len, a);
+        return;
+      }
+      k -= c;
+    }
+  }
+  if (joinLeft < joinRite) {
+    if (k == 0) {
+      x = FixedFloorToInt(joinLeft);
+      len = FixedFloorToInt(joinRite - joinLeft);
+      a = t.full;
+      return;
+    }
+    k -= 1;
+  }
+  const int n = FixedCeilToInt(t.lr - joinRite);
+  if (n == 1) {
+    const uint8_t v = trapezoid_to_alpha(t.ur - joinRite, t.lr - joinRite);
+    x = joinRite >> 16;
+    len = 1;
+    a = t.real ? v : partial_alpha_a(v, t.full);
+  } else if (n == 2) {
+    const Fixed first = joinRite + kFixed1 - t.ur;
+    x = (joinRite >> 16) + k;
+    len = 1;
+    a = k == 0 ? (uint8_t)(t.full - partial_triangle_to_alpha(first, t.rDY))
+               : partial_triangle_to_alpha(t.lr - t.ur - first, t.rDY);
+  } else {
+    AaaSpan(joinRite, t.ur, joinRite, t.lr, kMaxS32, t.rDY, t.full, t.real, k, x, len, a);
+  }
+}
+
 // Per-pass sweep memory (capacity n edges; diff holds acc_width + 1).
 struct SweepMem {
   Edge* W;            // edges in sorted order; pending edges are W[k..n)

@@ -78,6 +78,8 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   std::vector<uint32_t> pass_spans(np + 1, 0);
   std::vector<PassComp> comp;
   PlanComp(hb, geom, sw, comp);
+  std::vector<uint32_t> band_off, bins;
+  BuildBins(hb, comp, AssignBands(hb), band_off, bins);
   b.sweep = sw.data();
   b.sweepmem = sweepmem.data();
   uint32_t err = 0;
@@ -85,6 +87,8 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   b.rowspan = rowspan.data();
   b.pass_spans = pass_spans.data();
   b.comp = comp.data();
+  b.band_off = band_off.data();
+  b.bins = bins.data();
   Lanes lanes;
   std::vector<uint8_t> pclass(np + 1);
   b.pass_class = pclass.data();
