@@ -38,6 +38,7 @@ extern "C" {
 /* Result codes: 0 and -1..-5 mean what skity_result means
  * (module/capi/include/skity_c/skity_base.h:48-56). */
 typedef enum skity_cuda_result {
+  SKITY_CUDA_NOT_READY = 1,                     /* skity_cuda_server_wait: not done yet */
   SKITY_CUDA_SUCCESS = 0,
   SKITY_CUDA_ERROR_INVALID_HANDLE = -1,
   SKITY_CUDA_ERROR_INVALID_ARGUMENT = -2,
@@ -49,6 +50,7 @@ typedef enum skity_cuda_result {
   SKITY_CUDA_ERROR_DEVICE_TIMEOUT = -8,         /* a bounded device wait expired */
   SKITY_CUDA_ERROR_SCRATCH_LIMIT = -9,          /* input too large for the fixed
                                                    scratch of skity_cuda_draw_path_static */
+  SKITY_CUDA_ERROR_CANCELLED = -10,             /* request dropped by skity_cuda_server_destroy */
 } skity_cuda_result;
 
 typedef struct skity_cuda_context_s* skity_cuda_context;
@@ -196,6 +198,49 @@ SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch);
 SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
                                              uint8_t* out_pixels);
 SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch);
+
+/* ---- serving ------------------------------------------------------------
+ * No single reference call: a request loop that renders canvases as they
+ * arrive.  Each request is one canvas given as a scene stream (the layout of
+ * skity_cuda_render_streams); it is copied at submit.  Requests are admitted
+ * in arrival order against a device-memory budget (an estimate of each
+ * request's footprint: canvas, span rows, geometry scratch) and rendered in
+ * batches by `workers` worker threads, each with its own stream, so batches
+ * overlap on the device: whatever is queued when a worker frees up goes into
+ * its next batch (up to max_batch requests).  A request whose footprint alone
+ * exceeds the budget is refused at submit (SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY).
+ * A request's pixels do not depend on the batch it lands in. */
+typedef struct skity_cuda_server_s* skity_cuda_server;
+
+typedef struct skity_cuda_server_create_info {
+  uint32_t struct_size;   /* sizeof(skity_cuda_server_create_info) */
+  int32_t device;         /* CUDA device ordinal */
+  uint64_t memory_budget; /* admission budget in bytes; 0 = 40 GiB */
+  uint32_t workers;       /* concurrent batches; 0 = 2 */
+  uint32_t max_batch;     /* requests per batch; 0 = 64 */
+} skity_cuda_server_create_info;
+
+typedef struct skity_cuda_request_info {
+  double queue_ms;        /* submit -> its batch started */
+  double latency_ms;      /* submit -> pixels ready */
+  uint32_t batch_size;    /* requests in its batch */
+  uint32_t width, height;
+} skity_cuda_request_info;
+
+SKITY_CUDA_API int32_t skity_cuda_server_create(const skity_cuda_server_create_info* info,
+                                                skity_cuda_server* out);
+/* Queues one request; *ticket names it in skity_cuda_server_wait. */
+SKITY_CUDA_API int32_t skity_cuda_server_submit(skity_cuda_server server, const uint8_t* stream,
+                                                size_t stream_bytes, uint64_t* ticket);
+/* Waits up to timeout_ms for a request: SKITY_CUDA_NOT_READY if it is not
+ * done yet (0 polls); otherwise its result code, with width*height*4 bytes of
+ * premultiplied RGBA8 written to out_pixels on success.  A finished request's
+ * ticket is released by this call. */
+SKITY_CUDA_API int32_t skity_cuda_server_wait(skity_cuda_server server, uint64_t ticket,
+                                              uint32_t timeout_ms, uint8_t* out_pixels,
+                                              skity_cuda_request_info* info);
+/* Cancels queued requests, waits for the batches in flight, frees the server. */
+SKITY_CUDA_API void skity_cuda_server_destroy(skity_cuda_server server);
 
 /* ---- drawing without allocation --------------------------------------------
  * No counterpart in the reference: its software canvas allocates as it draws.

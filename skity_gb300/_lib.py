@@ -11,7 +11,9 @@ import os
 from . import build as _build
 
 SUCCESS = 0
+NOT_READY = 1
 ERRORS = {
+    1: "not ready", -10: "cancelled",
     -1: "invalid handle", -2: "invalid argument", -3: "initialization failed",
     -4: "out of host memory", -5: "not supported", -6: "device error",
     -7: "out of device memory", -8: "device timeout",
@@ -67,6 +69,18 @@ class Stats_(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerInfo_(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("device", ctypes.c_int32),
+                ("memory_budget", ctypes.c_uint64), ("workers", ctypes.c_uint32),
+                ("max_batch", ctypes.c_uint32)]
+
+
+class RequestInfo_(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("batch_size", ctypes.c_uint32), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32)]
+
+
 # every entry point declared in include/skity_cuda.h: name -> (restype, argtypes)
 _vp = ctypes.c_void_p
 SIGNATURES = {
@@ -87,6 +101,12 @@ SIGNATURES = {
     "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
     "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
     "skity_cuda_batch_destroy": (None, [_vp]),
+    "skity_cuda_server_create": (ctypes.c_int32, [ctypes.POINTER(ServerInfo_), ctypes.POINTER(_vp)]),
+    "skity_cuda_server_submit": (ctypes.c_int32, [_vp, _vp, ctypes.c_size_t,
+                                                  ctypes.POINTER(ctypes.c_uint64)]),
+    "skity_cuda_server_wait": (ctypes.c_int32, [_vp, ctypes.c_uint64, ctypes.c_uint32, _vp,
+                                                ctypes.POINTER(RequestInfo_)]),
+    "skity_cuda_server_destroy": (None, [_vp]),
     "skity_cuda_draw_path_static": (ctypes.c_int32, [ctypes.c_int32, _vp, ctypes.c_uint32,
                                                      ctypes.c_uint32, ctypes.c_size_t,
                                                      ctypes.POINTER(Path_), ctypes.POINTER(Paint_),

@@ -1,6 +1,6 @@
 """Build step of the GB300 raster backend: compiles the CUDA library
-(skity_gb300/_build/libskity_cuda.so) for sm_103a with nvcc, three
-translation units in parallel.
+(skity_gb300/_build/libskity_cuda.so) for sm_103a with nvcc, one job per
+translation unit, in parallel.
 
 Numerics flags: -fmad=false (no FMA contraction on the device), IEEE
 division and square root (nvcc defaults, kept explicit), and
@@ -22,7 +22,7 @@ LIB = os.path.join(BUILD, "libskity_cuda.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden"]
-SOURCES = ["kernels.cu", "pipeline.cu", "static_draw.cu"]
+SOURCES = ["kernels.cu", "pipeline.cu", "static_draw.cu", "server.cu"]
 
 
 def nvcc() -> str:

@@ -378,3 +378,58 @@ class DeviceCanvas:
             w0, w1 = int(sc.weight_off[d]), int(sc.weight_off[d + 1])
             self.draw_record(sc.verbs[v0:v1], sc.points[p0:p1], sc.weights[w0:w1], sc.paints[d])
         return sc.n_draws
+
+
+class Server:
+    """The serving loop (skity_cuda_server): requests are scene streams of
+    one canvas each, admitted against a device-memory budget and rendered in
+    continuously formed batches by `workers` concurrent workers."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, workers: int = 0,
+                 max_batch: int = 0):
+        self.lib = _lib.load()
+        info = _lib.ServerInfo_(ctypes.sizeof(_lib.ServerInfo_), device, budget_bytes, workers,
+                                max_batch)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.skity_cuda_server_create(ctypes.byref(info), ctypes.byref(h)),
+                   "skity_cuda_server_create")
+        self.handle = h
+        self.sizes = {}
+
+    def submit(self, scene=None, stream: bytes | None = None) -> int:
+        b = stream if stream is not None else scene.to_bytes()
+        sc = scene if scene is not None else S.Scene.from_bytes(b)
+        t = ctypes.c_uint64()
+        _lib.check(self.lib.skity_cuda_server_submit(self.handle, b, len(b), ctypes.byref(t)),
+                   "skity_cuda_server_submit")
+        self.sizes[t.value] = (sc.height, sc.width)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000, want_pixels: bool = True):
+        """(pixels or None, info dict); raises on error; returns (None, None)
+        when the request is not done within the timeout."""
+        if ticket not in self.sizes:  # unknown or released: the C ABI reports it
+            want_pixels = False
+        h, w = self.sizes.get(ticket, (0, 0))
+        out = np.zeros((h, w, 4), np.uint8) if want_pixels else None
+        info = _lib.RequestInfo_()
+        rc = self.lib.skity_cuda_server_wait(self.handle, ticket, timeout_ms,
+                                             out.ctypes.data if want_pixels else None,
+                                             ctypes.byref(info))
+        if rc == _lib.NOT_READY:
+            return None, None
+        self.sizes.pop(ticket, None)
+        _lib.check(rc, "skity_cuda_server_wait")
+        return out, {"queue_ms": info.queue_ms, "latency_ms": info.latency_ms,
+                     "batch_size": info.batch_size}
+
+    def close(self):
+        if self.handle:
+            self.lib.skity_cuda_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

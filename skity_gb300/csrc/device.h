@@ -1,0 +1,114 @@
+// Device-side state of the raster pipeline shared by the batch / canvas C
+// ABI (pipeline.cu) and the serving loop (server.cu): device buffers, a
+// batch resident on the device, the context, and the pipeline entry points.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "../../include/skity_cuda.h"
+#include "batch.h"
+
+namespace skc {
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    release();
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+struct Context;
+
+// A batch resident on the device: inputs uploaded once, re-rendered on
+// demand.
+struct DeviceBatch {
+  Context* ctx = nullptr;
+  HostBatch hb;
+  DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
+  DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
+  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
+  DevBuf band_off, bins;
+  std::vector<RowTask> h_tasks_main, h_tasks_temp;
+  std::vector<uint32_t> h_band_off, h_bins;
+  uint32_t chunk = 1024;
+  uint32_t n_bands = 0;
+  // true when the caller has loaded the canvases' current pixels (a canvas
+  // flush without a clear); otherwise a canvas without a clear colour starts
+  // from transparent black, as a fresh Bitmap does
+  bool keep_pixels = false;
+  bool uploaded = false;
+  // Replay of the planned render as one CUDA graph (device-resident
+  // batches): the plan -- scratch capacities, sweep buffers, row tables,
+  // bins -- depends only on the batch's inputs, so a re-render can run the
+  // same launches on the same buffers without host round trips.
+  bool want_graph = false;
+  bool graph_ok = false;
+  cudaGraphExec_t graphs[5] = {};
+  DevBatch planned{};
+  uint64_t planned_rows = 0;
+  const void* planned_pool = nullptr;  // the context span pool the plan used
+  skity_cuda_stats planned_stats{};
+  ~DeviceBatch() {
+    for (auto g : graphs)
+      if (g) cudaGraphExecDestroy(g);
+  }
+  std::vector<PassGeom> h_geom;
+  skity_cuda_stats stats{};
+};
+
+}  // namespace skc
+
+struct skity_cuda_context_s {
+  int device = 0;
+  uint64_t budget = 0;
+  // span pool shared by the context's renders (they are serialised), grown
+  // to what the largest render so far needed
+  skc::DevBuf span_pool, span_next;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t stage[10] = {};
+  uint32_t tile_w = 256;  // composite row-tile width in pixels
+  skity_cuda_stats last{};
+  std::mutex mu;
+};
+
+namespace skc {
+
+int32_t CudaErr(cudaError_t e);
+// Parses scene streams into the batch's host description.
+int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* const* streams,
+                         const size_t* bytes);
+// Uploads the batch's inputs (once per batch).
+int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db);
+// Renders the batch on the context's stream (planned render, or the replay
+// graphs when the batch has them); pixels stay on the device.
+int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed);
+// Copies canvas `index` of the batch to host memory (row_bytes 0: packed).
+int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
+                   size_t row_bytes);
+
+}  // namespace skc

@@ -26,97 +26,11 @@
 #include <string>
 #include <vector>
 
-#include "../../include/skity_cuda.h"
-#include "batch.h"
+#include "device.h"
 
 namespace skc {
 
-// ---------------------------------------------------------------------------
-// device buffers
-// ---------------------------------------------------------------------------
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap && p) return cudaSuccess;
-    release();
-    size_t want = std::max<size_t>(bytes, 256);
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      return e;
-    }
-    cap = want;
-    return cudaSuccess;
-  }
-  template <typename T>
-  T* as() const { return (T*)p; }
-};
-
-struct Context;
-
-// A batch resident on the device: inputs uploaded once, re-rendered on
-// demand.
-struct DeviceBatch {
-  Context* ctx = nullptr;
-  HostBatch hb;
-  DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
-  DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
-  DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
-  DevBuf band_off, bins;
-  std::vector<RowTask> h_tasks_main, h_tasks_temp;
-  std::vector<uint32_t> h_band_off, h_bins;
-  uint32_t chunk = 1024;
-  uint32_t n_bands = 0;
-  // true when the caller has loaded the canvases' current pixels (a canvas
-  // flush without a clear); otherwise a canvas without a clear colour starts
-  // from transparent black, as a fresh Bitmap does
-  bool keep_pixels = false;
-  bool uploaded = false;
-  // Replay of the planned render as one CUDA graph (device-resident
-  // batches): the plan -- scratch capacities, sweep buffers, row tables,
-  // bins -- depends only on the batch's inputs, so a re-render can run the
-  // same launches on the same buffers without host round trips.
-  bool want_graph = false;
-  bool graph_ok = false;
-  cudaGraphExec_t graphs[5] = {};
-  DevBatch planned{};
-  uint64_t planned_rows = 0;
-  const void* planned_pool = nullptr;  // the context span pool the plan used
-  skity_cuda_stats planned_stats{};
-  ~DeviceBatch() {
-    for (auto g : graphs)
-      if (g) cudaGraphExecDestroy(g);
-  }
-  std::vector<PassGeom> h_geom;
-  skity_cuda_stats stats{};
-};
-
-}  // namespace skc
-
-struct skity_cuda_context_s {
-  int device = 0;
-  uint64_t budget = 0;
-  // span pool shared by the context's renders (they are serialised), grown
-  // to what the largest render so far needed
-  skc::DevBuf span_pool, span_next;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t stage[10] = {};
-  uint32_t tile_w = 256;  // composite row-tile width in pixels
-  skity_cuda_stats last{};
-  std::mutex mu;
-};
-
-namespace skc {
-
-static int32_t CudaErr(cudaError_t e) {
+int32_t CudaErr(cudaError_t e) {
   if (e == cudaSuccess) return SKITY_CUDA_SUCCESS;
   if (e == cudaErrorMemoryAllocation) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
   return SKITY_CUDA_ERROR_DEVICE;
@@ -134,7 +48,7 @@ static cudaError_t Upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
   return cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
 }
 
-static int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
+int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   cudaStream_t s = ctx->stream;
   HostBatch& hb = db.hb;
   if (hb.verbs.empty()) hb.verbs.push_back(0);
@@ -271,7 +185,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
 // replay graph is current re-renders with one graph launch; the graph's
 // device self-checks (error word, span pool use) are read back, and any
 // surprise falls back to a full planned render.
-static int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
+int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
   if (db.graph_ok && db.planned_pool == ctx->span_pool.p) {
     cudaStream_t s = ctx->stream;
     static const int kStageEv[5][2] = {{0, 1}, {4, 5}, {6, 7}, {7, 8}, {8, 9}};
@@ -508,7 +422,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   return SKITY_CUDA_SUCCESS;
 }
 
-static int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* const* streams,
+int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* const* streams,
                                 const size_t* bytes) {
   for (uint32_t i = 0; i < count; ++i) {
     StreamView sv;
@@ -519,7 +433,7 @@ static int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* 
   return SKITY_CUDA_SUCCESS;
 }
 
-static int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
+int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
                           size_t row_bytes) {
   if (index >= db.hb.main_canvases.size()) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   const CanvasDesc& cd = db.hb.canvases[db.hb.main_canvases[index]];
