@@ -61,6 +61,12 @@ def lib() -> ctypes.CDLL:
         _lib.sko_quad_edge.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]
         _lib.sko_path_spans.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
                                         ctypes.c_void_p, ctypes.c_uint32]
+        _lib.sko_fill_quads.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
+                                        ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                        ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+        _lib.ska_exact_coverage.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                            ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
     return _lib
 
 
@@ -86,6 +92,71 @@ def render_mt(scene, threads: int, first: int = 0, count: int | None = None):
     if rc != 0:
         raise RuntimeError(f"oracle render failed ({rc})")
     return out, st
+
+
+def fill_quads(scene, draw: int):
+    """The QuadPath one draw's fill rasterises: (verbs u8, points (n, 2) f32)."""
+    b = scene.to_bytes()
+    L = lib()
+    counts = (ctypes.c_uint32 * 2)()
+    L.sko_fill_quads(b, len(b), draw, None, 0, None, 0, counts)
+    verbs = np.zeros(max(counts[0], 1), np.uint8)
+    pts = np.zeros((max(counts[1], 1), 2), np.float32)
+    L.sko_fill_quads(b, len(b), draw, verbs.ctypes.data, counts[0], pts.ctypes.data, counts[1],
+                     counts)
+    return verbs[:counts[0]], pts[:counts[1]]
+
+
+def exact_coverage(scene, draw: int, tol: float = 1e-4) -> np.ndarray:
+    """FP64 exact-area coverage (height, width) in [0, 1] of one draw's fill
+    (oracle/exact_area.cc)."""
+    verbs, pts = fill_quads(scene, draw)
+    cov = np.zeros((scene.height, scene.width), np.float64)
+    pts = np.ascontiguousarray(pts, np.float32)
+    rc = lib().ska_exact_coverage(verbs.ctypes.data, len(verbs), pts.ctypes.data, len(pts),
+                                  int(scene.paints[draw]["fill_type"]) & 1, scene.width,
+                                  scene.height, tol, cov.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"exact coverage failed ({rc})")
+    return cov
+
+
+def coverage_scenes(scene):
+    """One single-draw scene per fill draw of `scene`: the draw's path and
+    fill rule, an opaque white solid paint, on a transparent canvas -- the
+    rendered alpha is the coverage the rasteriser gives the path."""
+    from skity_gb300 import scene as S
+    out = []
+    for d in range(scene.n_draws):
+        sub = scene.subset(d, 1)
+        p = sub.paints[0]
+        if p["style"] != S.FILL or p["blur_style"] != 0:
+            continue
+        p["fill_color"] = (1.0, 1.0, 1.0, 1.0)
+        p["gradient"] = -1
+        p["blend"] = S.BLEND_SRC_OVER
+        sub.clear = (0.0, 0.0, 0.0, 0.0)
+        out.append((d, sub))
+    return out
+
+
+def coverage_error(scene, alphas: list, tol: float = 1e-4) -> dict:
+    """Max and mean |rendered coverage - exact area| in 1/255 units over the
+    pixels either one touches, for the fill draws of `scene`; `alphas[i]` is
+    the alpha channel (h, w) rendered for coverage_scenes(scene)[i]."""
+    err_max, err_sum, n, edge = 0.0, 0.0, 0, 0
+    for (d, _), a in zip(coverage_scenes(scene), alphas):
+        ex = exact_coverage(scene, d, tol)
+        got = np.asarray(a, np.float64) / 255.0
+        m = (ex > 0) | (got > 0)
+        e = np.abs(got - ex)[m] * 255.0
+        if e.size:
+            err_max = max(err_max, float(e.max()))
+            err_sum += float(e.sum())
+            n += int(e.size)
+        edge += int(((ex > 0) & (ex < 1)).sum())
+    return {"max_err_255": err_max, "mean_err_255": err_sum / max(n, 1), "pixels": n,
+            "edge_pixels": edge, "tol_px": tol}
 
 
 def reference_available() -> bool:

@@ -1784,6 +1784,24 @@ int sko_quad_edge(const float pts[6], int32_t out[4]) {
   return 1;
 }
 
+int sko_fill_quads(const uint8_t* scene, size_t len, uint32_t draw, uint8_t* verbs,
+                   uint32_t vcap, float* pts, uint32_t pcap, uint32_t counts[2]) {
+  using namespace sko;
+  SceneView s;
+  if (!ParseScene(scene, len, &s) || draw >= s.nd) return -2;
+  Path path = BuildPath(s, draw);
+  Path quad;
+  QuadPath(path, &quad);
+  counts[0] = (uint32_t)quad.verbs.size();
+  counts[1] = (uint32_t)quad.pts.size();
+  for (uint32_t i = 0; i < counts[0] && i < vcap; ++i) verbs[i] = (uint8_t)quad.verbs[i];
+  for (uint32_t i = 0; i < counts[1] && i < pcap; ++i) {
+    pts[2 * i] = quad.pts[i].x;
+    pts[2 * i + 1] = quad.pts[i].y;
+  }
+  return 0;
+}
+
 int sko_path_spans(const uint8_t* scene, size_t len, uint32_t draw, int32_t* out,
                    uint32_t cap) {
   using namespace sko;

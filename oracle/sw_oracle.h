@@ -32,6 +32,14 @@ int sko_cubic_quad_count(const float pts[8]);
 /* SWQuadEdge::SetQuad on a monotone quad: out = {1<<shift? no: shift,
  * winding, first_y, last_y}; returns 0 if the quad makes no edge. */
 int sko_quad_edge(const float pts[6], int32_t out[4]);
+/* The path one draw's fill rasterises (QuadPath of the draw's path):
+ * counts = {verbs, points}; at most vcap verbs and pcap points are written. */
+int sko_fill_quads(const uint8_t* scene, size_t len, uint32_t draw, uint8_t* verbs,
+                   uint32_t vcap, float* pts, uint32_t pcap, uint32_t counts[2]);
+/* FP64 exact-area coverage (oracle/exact_area.cc) of a QuadPath: width*height
+ * coverages in [0, 1]; quads flattened within tol pixels. */
+int ska_exact_coverage(const uint8_t* verbs, uint32_t nv, const float* pts, uint32_t np,
+                       int even_odd, int width, int height, double tol, double* cov);
 /* Spans (x, y, len, cover) of one draw's fill, in emission order; returns
  * the span count (may exceed cap; only cap are written). */
 int sko_path_spans(const uint8_t* scene, size_t len, uint32_t draw, int32_t* out,
