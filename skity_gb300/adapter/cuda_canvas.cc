@@ -1,0 +1,142 @@
+// skity::Canvas over the GB300 raster backend's C ABI; see cuda_canvas.hpp.
+#include "cuda_canvas.hpp"
+
+#include <cstring>
+#include <skity/effect/mask_filter.hpp>
+#include <skity/effect/shader.hpp>
+#include <skity/graphic/paint.hpp>
+#include <skity/graphic/path.hpp>
+#include <vector>
+
+namespace skity {
+namespace cuda {
+
+CUDACanvas::CUDACanvas(skity_cuda_canvas canvas, Bitmap* bitmap)
+    : Canvas(), canvas_(canvas), bitmap_(bitmap) {}
+
+CUDACanvas::~CUDACanvas() { skity_cuda_canvas_destroy(canvas_); }
+
+void CUDACanvas::OnClipPath(Path const&, ClipOp) { status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED; }
+
+void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
+  if (!GetTotalMatrix().IsIdentity()) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  // Path storage as the reference keeps it (path.hpp:590-596)
+  std::vector<uint8_t> verbs;
+  std::vector<float> pts;
+  std::vector<float> weights;
+  verbs.reserve(path.CountVerbs());
+  uint32_t conics = 0;
+  for (const Path::Verb* v = path.VerbsBegin(); v != path.VerbsEnd(); ++v) {
+    verbs.push_back(static_cast<uint8_t>(*v));
+    if (*v == Path::Verb::kConic) conics++;
+  }
+  pts.reserve(2 * path.CountPoints());
+  for (size_t i = 0; i < path.CountPoints(); ++i) {
+    pts.push_back(path.Points()[i].x);
+    pts.push_back(path.Points()[i].y);
+  }
+  weights.assign(path.ConicWeights(), path.ConicWeights() + conics);
+  skity_cuda_path p{};
+  p.verbs = verbs.data();
+  p.verb_count = static_cast<uint32_t>(verbs.size());
+  p.points = pts.data();
+  p.point_count = static_cast<uint32_t>(path.CountPoints());
+  p.conic_weights = weights.data();
+  p.conic_weight_count = conics;
+  p.fill_type = path.GetFillType() == Path::PathFillType::kEvenOdd ? 1u : 0u;
+
+  skity_cuda_paint q{};
+  q.style = static_cast<uint32_t>(paint.GetStyle());
+  q.cap = static_cast<uint32_t>(paint.GetStrokeCap());
+  q.join = static_cast<uint32_t>(paint.GetStrokeJoin());
+  q.blend_mode = static_cast<uint32_t>(paint.GetBlendMode());
+  const Vector fc = paint.GetFillColor(), sc = paint.GetStrokeColor();
+  const float fill[4] = {fc.x, fc.y, fc.z, fc.w}, stroke[4] = {sc.x, sc.y, sc.z, sc.w};
+  std::memcpy(q.fill_color, fill, sizeof fill);
+  std::memcpy(q.stroke_color, stroke, sizeof stroke);
+  q.stroke_width = paint.GetStrokeWidth();
+  q.miter_limit = paint.GetStrokeMiter();
+
+  skity_cuda_gradient g{};
+  std::vector<float> colors;
+  std::vector<float> offsets;
+  if (const Shader* s = paint.GetShader().get()) {
+    Shader::GradientInfo info;
+    const Shader::GradientType t = s->AsGradient(&info);
+    if ((t != Shader::kLinear && t != Shader::kRadial) || !info.local_matrix.IsIdentity()) {
+      status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+      return;
+    }
+    g.type = t == Shader::kLinear ? 1u : 2u;
+    g.tile_mode = static_cast<uint32_t>(info.tile_mode);
+    g.stop_count = static_cast<uint32_t>(info.colors.size());
+    g.has_offsets = info.color_offsets.empty() ? 0u : 1u;
+    g.p0[0] = info.point[0].x;
+    g.p0[1] = info.point[0].y;
+    g.p1[0] = info.point[1].x;
+    g.p1[1] = info.point[1].y;
+    g.radius[0] = info.radius[0];
+    g.radius[1] = info.radius[1];
+    for (const Vec4& c : info.colors) colors.insert(colors.end(), {c.x, c.y, c.z, c.w});
+    offsets = info.color_offsets;
+    g.colors = colors.data();
+    g.offsets = offsets.empty() ? nullptr : offsets.data();
+    q.shader = &g;
+  }
+  if (const MaskFilter* mf = paint.GetMaskFilter().get()) {
+    q.blur_style = static_cast<uint32_t>(mf->GetBlurStyle());
+    q.blur_radius = mf->GetBlurRadius();
+  }
+  status_ = skity_cuda_canvas_draw_path(canvas_, &p, &q);
+}
+
+void CUDACanvas::OnSaveLayer(const Rect&, const Paint&) {
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
+void CUDACanvas::OnDrawBlob(const TextBlob*, float, float, Paint const&) {
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
+void CUDACanvas::OnDrawImageRect(std::shared_ptr<Image>, const Rect&, const Rect&,
+                                 const SamplingOptions&, Paint const*) {
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
+void CUDACanvas::OnDrawGlyphs(uint32_t, const GlyphID[], const float[], const float[],
+                              const Font&, const Paint&) {
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
+// Canvas::Clear(color) is DrawColor(color, kSrc) -> DrawPaint (canvas.cc:241-253):
+// a kSrc fill of the whole canvas with no shader is the clear entry point.
+void CUDACanvas::OnDrawPaint(Paint const& paint) {
+  if (paint.GetBlendMode() != BlendMode::kSrc || paint.GetShader() || paint.GetMaskFilter()) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  const Vector c = paint.GetFillColor();
+  const float rgba[4] = {c.x, c.y, c.z, c.w};
+  status_ = skity_cuda_canvas_clear(canvas_, rgba);
+}
+
+void CUDACanvas::OnFlush() { status_ = skity_cuda_canvas_flush(canvas_); }
+
+uint32_t CUDACanvas::OnGetWidth() const { return bitmap_->Width(); }
+
+uint32_t CUDACanvas::OnGetHeight() const { return bitmap_->Height(); }
+
+std::unique_ptr<CUDACanvas> MakeCUDACanvas(skity_cuda_context ctx, Bitmap* bitmap) {
+  if (!bitmap || bitmap->Width() == 0 || bitmap->Height() == 0) return nullptr;
+  skity_cuda_canvas c = nullptr;
+  if (skity_cuda_canvas_create(ctx, bitmap->Width(), bitmap->Height(), bitmap->GetPixelAddr(),
+                               bitmap->RowBytes(), &c) != SKITY_CUDA_SUCCESS)
+    return nullptr;
+  return std::make_unique<CUDACanvas>(c, bitmap);
+}
+
+}  // namespace cuda
+}  // namespace skity

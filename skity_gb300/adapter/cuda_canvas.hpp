@@ -1,0 +1,66 @@
+// skity::Canvas over the GB300 raster backend's C ABI (include/skity_cuda.h).
+//
+// The drop-in for Canvas::MakeSoftwareCanvas(Bitmap*)
+// (include/skity/render/canvas.hpp:359, src/render/sw/sw_canvas.cc:146-156):
+// MakeCUDACanvas(ctx, bitmap) returns a Canvas whose DrawPath / Clear /
+// DrawPaint(kSrc) / Flush run on the GPU.  It compiles inside a Skity tree
+// (it needs Skity's public headers) and links against libskity_cuda.so.
+//
+// What differs from the software canvas: pixels are written to the bitmap at
+// Flush(), not during each draw.  Operations outside the GPU raster path --
+// clips, layers, text, images, non-identity canvas matrices, shader local
+// matrices, sweep/conical gradients, blur styles other than kNormal, blend
+// modes other than clear/src/dst/src-over -- draw nothing and leave
+// SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus().
+#ifndef SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP
+#define SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP
+
+#include <memory>
+#include <skity/graphic/bitmap.hpp>
+#include <skity/render/canvas.hpp>
+
+#include "../../include/skity_cuda.h"
+
+namespace skity {
+namespace cuda {
+
+class CUDACanvas : public Canvas {
+ public:
+  CUDACanvas(skity_cuda_canvas canvas, Bitmap* bitmap);
+  ~CUDACanvas() override;
+
+  // Result of the last operation (SKITY_CUDA_SUCCESS or an error code).
+  int32_t LastStatus() const { return status_; }
+
+ protected:
+  void OnClipPath(Path const& path, ClipOp op) override;
+  void OnDrawPath(Path const& path, Paint const& paint) override;
+  void OnSaveLayer(const Rect& bounds, const Paint& paint) override;
+  void OnDrawBlob(const TextBlob* blob, float x, float y, Paint const& paint) override;
+  void OnDrawImageRect(std::shared_ptr<Image> image, const Rect& src, const Rect& dst,
+                       const SamplingOptions& sampling, Paint const* paint) override;
+  void OnDrawGlyphs(uint32_t count, const GlyphID glyphs[], const float position_x[],
+                    const float position_y[], const Font& font, const Paint& paint) override;
+  void OnDrawPaint(Paint const& paint) override;
+  void OnSave() override {}
+  void OnRestore() override {}
+  void OnRestoreToCount(int) override {}
+  void OnFlush() override;
+  uint32_t OnGetWidth() const override;
+  uint32_t OnGetHeight() const override;
+
+ private:
+  skity_cuda_canvas canvas_;
+  Bitmap* bitmap_;
+  int32_t status_ = SKITY_CUDA_SUCCESS;
+};
+
+// Same null / empty semantics as MakeSoftwareCanvas: nullptr for a null
+// bitmap or a zero width or height.  The bitmap must be kPremul_AlphaType,
+// kRGBA, and outlive the canvas.
+std::unique_ptr<CUDACanvas> MakeCUDACanvas(skity_cuda_context ctx, Bitmap* bitmap);
+
+}  // namespace cuda
+}  // namespace skity
+
+#endif  // SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP

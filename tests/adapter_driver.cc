@@ -1,0 +1,108 @@
+// Drives skity::cuda::CUDACanvas (skity_gb300/adapter) through Skity's own
+// Canvas / Path / Paint / Shader / MaskFilter API, with the C ABI replaced
+// by a recorder, and prints what reached the C ABI.  Built and run by
+// tests/test_adapter.py against the reference's headers and the reference
+// software library built by oracle/ref (CPU only).
+#include <cstdio>
+#include <skity/effect/mask_filter.hpp>
+#include <skity/effect/shader.hpp>
+#include <skity/graphic/bitmap.hpp>
+#include <skity/graphic/color.hpp>
+#include <skity/graphic/paint.hpp>
+#include <skity/graphic/path.hpp>
+
+#include "../skity_gb300/adapter/cuda_canvas.hpp"
+
+extern "C" {
+int32_t skity_cuda_canvas_create(skity_cuda_context ctx, uint32_t w, uint32_t h, void* pixels,
+                                 size_t row_bytes, skity_cuda_canvas* out) {
+  std::printf("create ctx=%p w=%u h=%u pixels=%d row_bytes=%zu\n", (void*)ctx, w, h,
+              pixels != nullptr, row_bytes);
+  *out = reinterpret_cast<skity_cuda_canvas>(0x10);
+  return SKITY_CUDA_SUCCESS;
+}
+void skity_cuda_canvas_destroy(skity_cuda_canvas c) { std::printf("destroy %p\n", (void*)c); }
+int32_t skity_cuda_canvas_clear(skity_cuda_canvas, const float c[4]) {
+  std::printf("clear %g %g %g %g\n", c[0], c[1], c[2], c[3]);
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas, const skity_cuda_path* p,
+                                    const skity_cuda_paint* q) {
+  std::printf("draw verbs=");
+  for (uint32_t i = 0; i < p->verb_count; ++i) std::printf("%u,", p->verbs[i]);
+  std::printf(" points=");
+  for (uint32_t i = 0; i < 2 * p->point_count; ++i) std::printf("%g,", p->points[i]);
+  std::printf(" weights=");
+  for (uint32_t i = 0; i < p->conic_weight_count; ++i) std::printf("%g,", p->conic_weights[i]);
+  std::printf(" fill_type=%u style=%u cap=%u join=%u blend=%u width=%g miter=%g", p->fill_type,
+              q->style, q->cap, q->join, q->blend_mode, q->stroke_width, q->miter_limit);
+  std::printf(" fill=%g,%g,%g,%g stroke=%g,%g,%g,%g", q->fill_color[0], q->fill_color[1],
+              q->fill_color[2], q->fill_color[3], q->stroke_color[0], q->stroke_color[1],
+              q->stroke_color[2], q->stroke_color[3]);
+  if (q->shader) {
+    const skity_cuda_gradient* g = q->shader;
+    std::printf(" shader=%u tile=%u stops=%u offsets=%u p0=%g,%g p1=%g,%g r=%g colors=", g->type,
+                g->tile_mode, g->stop_count, g->has_offsets, g->p0[0], g->p0[1], g->p1[0],
+                g->p1[1], g->radius[0]);
+    for (uint32_t i = 0; i < 4 * g->stop_count; ++i) std::printf("%g,", g->colors[i]);
+    if (g->has_offsets) {
+      std::printf(" pos=");
+      for (uint32_t i = 0; i < g->stop_count; ++i) std::printf("%g,", g->offsets[i]);
+    }
+  }
+  std::printf(" blur=%u,%g\n", q->blur_style, q->blur_radius);
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_flush(skity_cuda_canvas) {
+  std::printf("flush\n");
+  return SKITY_CUDA_SUCCESS;
+}
+}
+
+int main() {
+  using namespace skity;
+  auto ctx = reinterpret_cast<skity_cuda_context>(0x20);
+  std::printf("null=%d\n", cuda::MakeCUDACanvas(ctx, nullptr) == nullptr);
+  Bitmap empty;
+  std::printf("empty=%d\n", cuda::MakeCUDACanvas(ctx, &empty) == nullptr);
+  Bitmap bm(40, 30, AlphaType::kPremul_AlphaType);
+  auto canvas = cuda::MakeCUDACanvas(ctx, &bm);
+  canvas->Clear(Color4fFromColor(ColorSetARGB(255, 255, 128, 0)));
+  Path path;
+  path.MoveTo(1, 2);
+  path.LineTo(3, 4);
+  path.QuadTo(5, 6, 7, 8);
+  path.ConicTo(9, 10, 11, 12, 0.5f);
+  path.CubicTo(13, 14, 15, 16, 17, 18);
+  path.Close();
+  path.SetFillType(Path::PathFillType::kEvenOdd);
+  Paint paint;
+  paint.SetStyle(Paint::kStrokeAndFill_Style);
+  paint.SetStrokeWidth(3.f);
+  paint.SetStrokeCap(Paint::kRound_Cap);
+  paint.SetStrokeJoin(Paint::kBevel_Join);
+  paint.SetStrokeMiter(5.f);
+  paint.SetColor(ColorSetARGB(255, 0, 255, 0));
+  paint.SetAlphaF(0.5f);
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  Vec4 colors[3] = {{1, 0, 0, 1}, {0, 1, 0, 0.5f}, {0, 0, 1, 1}};
+  float pos[3] = {0.f, 0.25f, 1.f};
+  Point pts[2] = {{0, 0, 0, 1}, {40, 30, 0, 1}};
+  paint.SetShader(Shader::MakeLinear(pts, colors, pos, 3, TileMode::kMirror));
+  paint.SetMaskFilter(MaskFilter::MakeBlur(BlurStyle::kNormal, 4.5f));
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  paint.SetShader(Shader::MakeRadial(Point{20, 15, 0, 1}, 12.f, colors, nullptr, 3, TileMode::kClamp));
+  paint.SetMaskFilter(nullptr);
+  canvas->DrawPath(path, paint);
+  canvas->Save();
+  canvas->Translate(5, 0);
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Restore();
+  canvas->Flush();
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas.reset();
+  return 0;
+}

@@ -1,0 +1,62 @@
+"""The C++ drop-in (skity_gb300/adapter: skity::cuda::CUDACanvas, a
+skity::Canvas over the C ABI) compiled against the reference's own headers
+and software library, with the C ABI replaced by a recorder
+(tests/adapter_driver.cc): Skity's Canvas / Path / Paint / Shader /
+MaskFilter calls must reach skity_cuda_* with the reference's storage and
+values.  CPU only; runs where the reference checkout and its build exist."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference"
+
+
+@pytest.fixture(scope="module")
+def driver_output(oracle_lib, tmp_path_factory):
+    if not os.path.isdir(REF):
+        pytest.skip("reference checkout not present")
+    oracle_lib.build_reference()
+    lib = os.path.join(ROOT, "oracle", "_ref", "libskity_ref_sw.a")
+    exe = str(tmp_path_factory.mktemp("adapter") / "adapter_driver")
+    cmd = ["g++", "-std=c++17", "-O1", "-DSKITY_CPU", "-DSKITY_RELEASE", "-w",
+           "-I" + os.path.join(ROOT, "oracle", "ref", "glm_shim"), "-I" + REF + "/include",
+           "-I" + REF, "-I" + REF + "/src", os.path.join(ROOT, "tests", "adapter_driver.cc"),
+           os.path.join(ROOT, "skity_gb300", "adapter", "cuda_canvas.cc"), lib, "-lpthread",
+           "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    return r.stdout.splitlines()
+
+
+def test_factory_semantics_match_make_software_canvas(driver_output):
+    assert driver_output[0] == "null=1" and driver_output[1] == "empty=1"
+    assert driver_output[2] == "create ctx=0x20 w=40 h=30 pixels=1 row_bytes=160"
+
+
+def test_clear_and_path_storage(driver_output):
+    # Canvas::Clear -> DrawPaint(kSrc) -> skity_cuda_canvas_clear, Color4f of ARGB(255,255,128,0)
+    assert driver_output[3] == "clear 1 0.501961 0 1"
+    d = driver_output[4]
+    assert "verbs=0,1,2,3,4,5," in d and "weights=0.5," in d
+    assert "points=" + ",".join(str(v) for v in range(1, 19)) + "," in d
+    assert "fill_type=1 style=2 cap=1 join=2 blend=3 width=3 miter=5" in d
+    assert "fill=0,1,0,0.5 stroke=0,1,0,0.5" in d and d.endswith("blur=0,0")
+
+
+def test_shaders_and_mask_filter(driver_output):
+    lin = driver_output[6]
+    assert "shader=1 tile=2 stops=3 offsets=1 p0=0,0 p1=40,30" in lin
+    assert "colors=1,0,0,1,0,1,0,0.5,0,0,1,1," in lin and "pos=0,0.25,1," in lin
+    assert lin.endswith("blur=1,4.5")
+    rad = driver_output[8]
+    assert "shader=2 tile=0 stops=3 offsets=0 p0=20,15" in rad and "r=12" in rad
+
+
+def test_unsupported_ops_report_status(driver_output):
+    # a translated canvas matrix is outside the GPU path: nothing drawn, -5
+    assert driver_output[9] == "status=-5"
+    assert driver_output[10:] == ["flush", "status=0", "destroy 0x10"]
