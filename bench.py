@@ -172,11 +172,14 @@ def batch_forms(ctx, steps: int, warmup: int, sample: int):
         st = batch.render()
         ms.append(st["device_ms"])
     bms = statistics.mean(ms)
+    stage = {k: st[k] for k in ("geometry_ms", "sweep_emit_ms", "composite_ms", "blur_ms")}
     out = {"workload": "256 canvases, sides log-uniform [64,1024], 50-2,000 paths each "
                        "(3-32 verbs line/quad/cubic, nonzero, solid colours)",
            "canvases": len(scenes), "paths": paths, "mpix": pix / 1e6,
            "batched": {"ms": bms, "mpix_per_s": pix / 1e3 / bms, "paths_per_s": paths * 1e3 / bms,
-                       "graph_replays": int(st["graph_replays"]), "form": "one planned batch, "
+                       "graph_replays": int(st["graph_replays"]), "stage_ms": stage,
+                       "spans": st["spans"], "fragments": st["fragments"],
+                       "form": "one planned batch, "
                        "CUDA-graph replay (geometry, sweeps, composites)"}}
     # per-draw form on a sample of canvases
     sub = scenes[:sample]
@@ -214,6 +217,134 @@ def batch_forms(ctx, steps: int, warmup: int, sample: int):
     out["batched_over_cpu"] = out["batched"]["paths_per_s"] / out["cpu"]["paths_per_s"]
     batch.close()
     return out
+
+
+def serving_pool(n: int = 64):
+    """Request scenes of the serving workload: one canvas each, sides
+    log-uniform in [128, 2048], log-uniform 10-5,000 paths drawn as in the
+    512x512 scene; arrivals cycle through this seeded pool."""
+    from skity_gb300 import scene as S
+    cache = os.path.join("/tmp", f"skity_serving_pool_v1_{n}.bin")
+    try:
+        with open(cache, "rb") as f:
+            buf = f.read()
+        out, o = [], 0
+        while o < len(buf):
+            k = int.from_bytes(buf[o:o + 8], "little")
+            out.append(buf[o + 8:o + 8 + k])
+            o += 8 + k
+        if len(out) == n:
+            return out
+    except Exception:
+        pass
+    R = S.random_streams(S.SEED_BASE + 5, n, 4)
+    out = []
+    for i in range(n):
+        w = int(round(float(S.loguniform(R[i, 0], 128, 2048))))
+        h = int(round(float(S.loguniform(R[i, 1], 128, 2048))))
+        k = max(1, int(round(float(S.loguniform(R[i, 2], 10, 5000)))))
+        out.append(S.random_paths_scene(int(R[i, 3]), w, h, k, 3, 32).to_bytes())
+    try:
+        with open(cache, "wb") as f:
+            for b in out:
+                f.write(len(b).to_bytes(8, "little") + b)
+    except Exception:
+        pass
+    return out
+
+
+def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512):
+    """Poisson request streams against the serving loop: for each rate,
+    arrivals for `seconds` seconds (seeded exponential gaps), requests
+    drawn in turn from the pool; latency = submit -> pixels on the host.
+    Clients give up on an arrival while `max_outstanding` requests are
+    already waiting (counted as shed), which bounds the drain of a rate
+    beyond capacity.  Beside them, the offline batched form on the pool."""
+    import random
+    import threading
+    from skity_gb300 import scene as S
+    from skity_gb300.canvas import Batch, Server
+
+    pool = serving_pool()
+    scenes = [S.Scene.from_bytes(b) for b in pool]
+    paths = [sc.n_draws for sc in scenes]
+    off = Batch(ctx, scenes)
+    off.render()
+    st = off.render()
+    off.close()
+    offline = {"paths_per_s": sum(paths) * 1e3 / st["device_ms"],
+               "requests_per_s": len(pool) * 1e3 / st["device_ms"], "ms": st["device_ms"]}
+    results = []
+    for rate in rates:
+        srv = Server(device, workers=2, max_batch=64)
+        rng = random.Random(0x5EED0005 + int(rate))
+        tickets = []
+        lock = threading.Lock()
+        done = threading.Event()
+        shed = [0]
+        waited = [0]
+
+        def submitter():
+            t0 = time.perf_counter()
+            t_next, i = 0.0, 0
+            while t_next < seconds:
+                now = time.perf_counter() - t0
+                if now < t_next:
+                    time.sleep(min(t_next - now, 0.002))
+                    continue
+                k = i % len(pool)
+                with lock:
+                    outstanding = len(tickets) - waited[0]
+                if outstanding >= max_outstanding:
+                    shed[0] += 1
+                else:
+                    tk = srv.submit(stream=pool[k])
+                    with lock:
+                        tickets.append((tk, k))
+                i += 1
+                t_next += rng.expovariate(rate)
+            done.set()
+
+        lat, queue_ms, sizes, npaths = [], [], [], 0
+        t_start = time.perf_counter()
+        th = threading.Thread(target=submitter)
+        th.start()
+        j = 0
+        while True:
+            with lock:
+                have = len(tickets)
+            if j >= have:
+                if done.is_set():
+                    with lock:
+                        if j >= len(tickets):
+                            break
+                time.sleep(0.0005)
+                continue
+            tk, k = tickets[j]
+            _, info = srv.wait(tk, 600000, want_pixels=False)
+            lat.append(info["latency_ms"])
+            queue_ms.append(info["queue_ms"])
+            sizes.append(info["batch_size"])
+            npaths += paths[k]
+            j += 1
+            with lock:
+                waited[0] = j
+        wall = time.perf_counter() - t_start
+        th.join()
+        srv.close()
+        lat.sort()
+        q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
+        results.append({"rate_rps": rate, "seconds": seconds, "requests": len(lat),
+                        "shed": shed[0], "max_outstanding": max_outstanding,
+                        "achieved_rps": len(lat) / wall, "paths_per_s": npaths / wall,
+                        "p50_ms": q(0.50), "p99_ms": q(0.99), "max_ms": lat[-1],
+                        "mean_queue_ms": statistics.mean(queue_ms),
+                        "mean_batch": statistics.mean(sizes),
+                        "vs_offline_paths": (npaths / wall) / offline["paths_per_s"]})
+    return {"workload": "Poisson arrivals; requests cycle through 64 seeded canvases (sides "
+                        "log-uniform [128,2048], 10-5,000 paths, solid fills); admission budget "
+                        "40 GiB; 2 workers, up to 64 requests per batch",
+            "offline_batched": offline, "rates": results}
 
 
 def cpu_baseline(scene, threads: int, sample_paths: int, steps: int = 1):
@@ -347,6 +478,9 @@ def run_gpu(args, rank, world, local):
                 "ms_per_step": e2e_ms_mean},
         "wall_s": wall,
     }
+    if rank == 0 and args.serve_seconds > 0:
+        line["serving"] = serving(ctx, [float(r) for r in args.serve_rates.split(",")],
+                                  args.serve_seconds, local)
     if rank == 0 and not args.no_forms:
         line["batching"] = batch_forms(ctx, max(1, min(args.steps, 5)), 3, args.per_draw_sample)
     if rank == 0 and not args.no_cpu:
@@ -377,6 +511,10 @@ def main():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the 256-canvas batched / per-draw / CPU comparison")
     ap.add_argument("--per-draw-sample", type=int, default=16)
+    ap.add_argument("--serve-rates", default="200,1000,5000",
+                    help="Poisson request rates (requests/s) of the serving runs")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="arrival window per rate (the serving workload specifies 60 s); 0 skips")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
