@@ -595,6 +595,21 @@ inline void PlanComp(const HostBatch& hb, const std::vector<PassGeom>& geom,
     comp[p].brush = hb.passes[p].brush;
   }
 }
+// The order in which the sweeps take the passes: longest expected sweep
+// first (rows times the bound of the active list), so that the long sweeps
+// start early instead of forming the tail of the launch.
+inline void SweepOrder(const std::vector<PassGeom>& geom, std::vector<uint32_t>& order) {
+  order.resize(geom.size());
+  std::vector<uint64_t> cost(geom.size());
+  for (size_t p = 0; p < geom.size(); ++p) {
+    order[p] = (uint32_t)p;
+    const PassGeom& g = geom[p];
+    const int64_t rows = g.n_edges > 0 ? std::max<int64_t>(g.row1 - g.row0, 0) : 0;
+    cost[p] = (uint64_t)rows * (uint64_t)(1 + std::max(g.max_active, 0));
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+}
 // Grow the capacities of a pass whose geometry overflowed.
 inline void GrowCaps(PassDesc& pd, const PassGeom& g) {
   bool stroke = (pd.flags & kPassStroke) != 0;

@@ -51,7 +51,7 @@ struct DeviceBatch {
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
   DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
   DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
-  DevBuf band_off, bins;
+  DevBuf band_off, bins, sweep_order;
   std::vector<RowTask> h_tasks_main, h_tasks_temp;
   std::vector<uint32_t> h_band_off, h_bins;
   uint32_t chunk = 1024;

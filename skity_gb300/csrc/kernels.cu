@@ -34,11 +34,13 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
   return 1;
 }
 
-// Sweeps: one warp per pass.  The register sweep takes every pass whose
-// active list fits kRegMaxM edges (2 warps per block, each with its
-// RegShared block and accumulator in shared memory); the generic sweep
-// (4 warps per block, state in global memory) takes the passes the count
-// kernel marked, after the register kernels.
+// Sweeps: one warp per pass, passes taken in the batch's sweep order
+// (longest expected sweeps first, so the long ones do not form the tail).
+// Three forms, each launched over every pass and taking the ones
+// SweepForm gives it: the register form for up to 64 active edges, the
+// register form for up to 128 (2 warps per block, each with its RegSharedT
+// block and accumulator in shared memory), then the generic sweep (4 warps
+// per block, state in global memory) for longer lists.
 constexpr int kSweepWarps = 4;
 constexpr int kRegWarps = 2;
 
@@ -48,34 +50,54 @@ __device__ __forceinline__ uint32_t DynamicSmemBytes() {
   return v;
 }
 
+__device__ __forceinline__ uint32_t SweepPassAt(const DevBatch& b, uint32_t i) {
+  return b.sweep_order ? b.sweep_order[i] : i;
+}
+
+template <int M, int kForm>
 __global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   const int w = threadIdx.x >> 5;
-  const uint32_t p = blockIdx.x * kRegWarps + w;
-  if (p >= b.n_passes) return;
-  if (DynamicSmemBytes() < kRegWarps * RegSmemBytes(b.reg_diff_cap)) {  // self-check
+  const uint32_t i = blockIdx.x * kRegWarps + w;
+  if (i >= b.n_passes) return;
+  const uint32_t p = SweepPassAt(b, i);
+  if (SweepForm(b.geom[p].max_active, b.pass_class[p]) != kForm) return;
+  if (DynamicSmemBytes() < kRegWarps * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
     FlagError(b.err, 16);
     return;
   }
   Lanes L;
   L.lane = threadIdx.x & 31;
-  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes(b.reg_diff_cap);
-  SweepPassReg(b, p, L, (RegShared*)mine, (int32_t*)(mine + sizeof(RegShared)), b.reg_diff_cap);
+  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes<M>(b.reg_diff_cap);
+  SweepPassReg<M>(b, p, L, (RegSharedT<M>*)mine, (int32_t*)(mine + sizeof(RegSharedT<M>)),
+                  b.reg_diff_cap);
 }
 
 __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
-  uint32_t p = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
+  const uint32_t i = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
+  if (i >= b.n_passes) return;
+  const uint32_t p = SweepPassAt(b, i);
   Lanes L;
   L.lane = threadIdx.x & 31;
-  if (p < b.n_passes && b.pass_class[p] == 1) SweepPass(b, p, L);
+  if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
+}
+
+template <int M, int kForm>
+static void LaunchRegForm(const DevBatch& b, cudaStream_t stream) {
+  const size_t smem = kRegWarps * RegSmemBytes<M>(b.reg_diff_cap);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_sweep_reg<M, kForm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+  k_sweep_reg<M, kForm>
+      <<<(b.n_passes + kRegWarps - 1) / kRegWarps, 32 * kRegWarps, smem, stream>>>(b);
 }
 
 int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
-  const size_t smem = kRegWarps * RegSmemBytes(b.reg_diff_cap);
-  k_sweep_reg<<<(b.n_passes + kRegWarps - 1) / kRegWarps, 32 * kRegWarps, smem, stream>>>(b);
+  LaunchRegForm<64, kSweepReg64>(b, stream);
+  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
   k_sweep<<<(b.n_passes + kSweepWarps - 1) / kSweepWarps, 32 * kSweepWarps, 0, stream>>>(b);
-  return 2;
+  return 3;
 }
 
 // ---------------------------------------------------------------------------

@@ -79,6 +79,7 @@ struct PassGeom {
   float scan_top;
   int32_t row0, row1;   // canvas rows that can receive spans
   int32_t need[13];     // sizes seen (exact up to the failing stage)
+  int32_t max_active;   // bound of the sweep's active-list length
 };
 
 struct PassSweep {      // per-pass sweep buffers, set after geometry
@@ -130,9 +131,10 @@ struct DevBatch {
   int32_t reg_diff_cap; // accumulator entries per warp in shared memory
   const uint32_t* band_off;  // per band: first entry in bins (one past the end follows)
   const uint32_t* bins;      // pass indices, per band in draw order
+  const uint32_t* sweep_order;  // passes in the order the sweeps take them (null: index order)
 };
 
-// Shared memory of one register-sweep warp: its RegShared block, then an
+// Shared memory of one register-sweep warp: its RegSharedT block, then an
 // accumulator of reg_diff_cap entries (passes with wider accumulators keep
 // theirs in the pass's sweep memory).
 constexpr int32_t kRegDiffMax = 3072;

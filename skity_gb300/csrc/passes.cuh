@@ -23,6 +23,7 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
   g.scan_top = 0;
   g.row0 = g.row1 = 0;
   for (int k = 0; k < 13; ++k) g.need[k] = 0;
+  g.max_active = 0;
 
   SliceLayout L;
   L.compute(pd.cap, sizeof(Edge));
@@ -131,6 +132,27 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
   tl.upper_x = kMaxS32;
   S[n] = h;
   S[n + 1] = tl;
+  // Bound of the sweep's active list: an edge joins it at upper_y and
+  // leaves after its last piece, so the list never holds more edges than
+  // the largest overlap of the [upper_y, last y) ranges.
+  {
+    int32_t* low = idx;  // free after the copy above
+    for (int i = 0; i < n; ++i)
+      low[i] = S[i].curve_count != 0 ? max_(S[i].lower_y, S[i].q_last_y) : S[i].lower_y;
+    IntLess il;
+    introsort(low, n, il);
+    int cur = 0, best = 0;
+    for (int i = 0, j = 0; i < n;) {
+      if (j < n && low[j] <= S[i].upper_y) {
+        --cur;
+        ++j;
+      } else {
+        best = max_(best, ++cur);
+        ++i;
+      }
+    }
+    g.max_active = best;
+  }
 
   const CanvasDesc cd = b.canvases[pd.canvas];
   g.n_edges = n;
@@ -254,6 +276,113 @@ struct PoolSink : SinkBase {
     kept += n;
     frags += f;
   }
+  // Sparse form of acc_row; returns false (nothing read, nothing written)
+  // when the row has more than ev_cap nonzero entries.
+  SKC_HD bool acc_row_sparse(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi,
+                             int32_t* ev, int ev_cap) {
+    constexpr int V = 4;
+    constexpr int kNone = 0x7fffffff;
+    const bool vec = ((uintptr_t)diff & 15) == 0;
+    int ne = 0;
+    for (int base = vec ? (lo & ~(V - 1)) : lo; base < hi; base += Lanes::n * V) {
+      const int i0 = base + L.lane * V;
+      int32_t d[V];
+      if (vec && i0 + V <= hi) {
+        const int4 q = *(const int4*)(diff + i0);
+        d[0] = q.x;
+        d[1] = q.y;
+        d[2] = q.z;
+        d[3] = q.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) d[j] = i0 + j < hi ? diff[i0 + j] : 0;
+      }
+      int cnt = 0;
+#pragma unroll
+      for (int j = 0; j < V; ++j) cnt += d[j] != 0 ? 1 : 0;
+      if (!L.ballot(cnt != 0)) continue;
+      const int32_t incl = LaneScanIncl(L, cnt);
+      const int total = LaneBcast(L, incl, Lanes::n - 1);
+      if (ne + total > ev_cap) return false;
+      int at = ne + incl - cnt;
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        if (d[j] != 0) {
+          ev[2 * at] = i0 + j;
+          ev[2 * at + 1] = d[j];
+          at++;
+        }
+      }
+      ne += total;
+    }
+    L.sync();
+    int open_start = -1;  // warp-uniform: the run still open after a step
+    int32_t open_v = 0;
+    int32_t carry = 0, prev_sat = 0;
+    for (int eb = 0; eb < ne; eb += Lanes::n) {
+      const int e = eb + L.lane;
+      const bool valid = e < ne;
+      int pos = kNone;
+      int32_t v = 0;
+      if (valid) {
+        pos = ev[2 * e];
+        v = ev[2 * e + 1];
+        diff[pos] = 0;
+      }
+      const int32_t incl = LaneScanIncl(L, v) + carry;
+      const int32_t sat = incl > 255 ? 255 : incl;
+      int32_t before = LaneBcast(L, sat, L.lane > 0 ? L.lane - 1 : 0);
+      if (L.lane == 0) before = prev_sat;
+      const bool start = valid && sat != before;
+      const unsigned starts = L.ballot(start);
+      const unsigned later = starts & ~((2u << L.lane) - 1u);
+      int next = (int)L.shfl((uint32_t)pos, later ? Lanes::ffs(later) - 1 : L.lane);
+      if (!later) next = kNone;
+      uint2 out[2];
+      int cnt = 0;
+      unsigned long long fr = 0;
+      auto put = [&](int s0, int w, int32_t a) {
+        int x = left + s0, len = w;
+        if (keep(x, y, len, (uint8_t)a)) {
+          out[cnt++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)a);
+          fr += (unsigned)len;
+        }
+      };
+      if (starts && open_start >= 0 && L.lane == Lanes::ffs(starts) - 1)
+        put(open_start, pos - open_start, open_v);
+      if (start && next != kNone && sat != 0) put(pos, next - pos, sat);
+      if (starts) {
+        const int src = 31 - clz_(starts);
+        const int32_t lv = LaneBcast(L, sat, src);
+        const int lp = LaneBcast(L, pos, src);
+        open_start = lv != 0 ? lp : -1;
+        open_v = lv;
+      }
+      const int32_t ci = LaneScanIncl(L, cnt);
+      const uint32_t total = (uint32_t)LaneBcast(L, ci, Lanes::n - 1);
+      if (total) {
+        const uint64_t at = reserve(L, 0, total);
+        uint2* dst = span_ptr(at + (uint32_t)(ci - cnt));
+        if (dst) {
+          for (int i = 0; i < cnt; ++i) dst[i] = out[i];
+        }
+        commit(L, total, LaneSum64(L, fr));
+      }
+      carry = LaneBcast(L, incl, Lanes::n - 1);
+      prev_sat = LaneBcast(L, sat, Lanes::n - 1);
+    }
+    if (open_start >= 0) {
+      int x = left + open_start, len = hi - open_start;
+      if (keep(x, y, len, (uint8_t)open_v)) {
+        const uint64_t at = reserve(L, 0, 1);
+        if (!dead && L.leader())
+          pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
+        commit(L, 1, (unsigned)len);
+      }
+    }
+    return true;
+  }
+
   // The accumulated spans of a row follow its direct spans (the reference
   // flushes a row's accumulator only after leaving the row,
   // SpanBuilder::Flush, sw_raster.cc:103-136): the runs of equal nonzero
@@ -267,9 +396,17 @@ struct PoolSink : SinkBase {
   // start), the lane with the chunk's first start also closes the run left
   // open by earlier chunks, and the chunk's spans are written after one
   // prefix sum.  Every entry read is reset to zero.
-  SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi) {
+  //
+  // With an event scratch (ev, room for ev_cap (position, value) pairs) the
+  // nonzero entries are first gathered in x order -- a difference array has
+  // two per accumulated span, usually far fewer than the row is wide -- and
+  // the runs are found over that list, 32 entries per step, with the same
+  // rules; a row with more nonzero entries than ev_cap takes the dense path.
+  SKC_HD bool acc_row(const Lanes& L, int y, int32_t* diff, int left, int lo, int hi,
+                      int32_t* ev = nullptr, int ev_cap = 0) {
     if (y < row0 || y >= row1) return false;
     row_begin(L, y);
+    if (ev && Lanes::n == 32 && acc_row_sparse(L, y, diff, left, lo, hi, ev, ev_cap)) return true;
     constexpr int V = Lanes::n == 32 ? 4 : 1;
     constexpr int kNone = 0x7fffffff;
     int open_start = -1;   // warp-uniform: the run still open after a chunk
@@ -453,24 +590,25 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   s.flush_acc();
 }
 
+template <int M>
 SKC_HD uint64_t RegSmemBytes(int32_t diff_cap) {
-  return sizeof(RegShared) + 4ull * (uint64_t)diff_cap;
+  return sizeof(RegSharedT<M>) + 4ull * (uint64_t)diff_cap;
 }
 
 // The register sweep of pass p (RegWalk); returns 0 when its active list
 // outgrows the registers.  The accumulator sits in shared memory when it fits.
-template <typename Sink>
+template <int M, typename Sink>
 SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* sink,
-                       const Lanes& lanes, RegShared* sh, int32_t* sdiff, int32_t sdiff_cap) {
+                       const Lanes& lanes, RegSharedT<M>* sh, int32_t* sdiff, int32_t sdiff_cap) {
   const PassDesc pd = b.passes[p];
   const PassSweep sw = b.sweep[p];
   SliceLayout L;
   L.compute(pd.cap, sizeof(Edge));
   const Edge* S = (const Edge*)(b.scratch + pd.slice_off + L.off[13]);
   const int n = g.n_edges;
-  SweepMem M = SweepMemAt(b.sweepmem + sw.work_off, n, g.acc_width);
-  for (int i = lanes.lane; i < n; i += Lanes::n) M.W[i] = S[i];
-  int32_t* diff = g.acc_width + 1 <= sdiff_cap ? sdiff : M.diff;
+  SweepMem Mm = SweepMemAt(b.sweepmem + sw.work_off, n, g.acc_width);
+  for (int i = lanes.lane; i < n; i += Lanes::n) Mm.W[i] = S[i];
+  int32_t* diff = g.acc_width + 1 <= sdiff_cap ? sdiff : Mm.diff;
   for (int i = lanes.lane; i <= g.acc_width; i += Lanes::n) diff[i] = 0;
   lanes.sync();
   AccState as;
@@ -480,27 +618,46 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
   as.y = kNaN32;
   as.lo = 0x7fffffff;
   as.hi = -1;
-  if (!RegWalk(lanes, *sh, M.W, n, sink, as, g.scan_top, (pd.flags & kPassEvenOdd) != 0,
+  as.ev = sh->u.ev;
+  as.ev_cap = RegSharedT<M>::kFlushEvents;
+  if (!RegWalk(lanes, *sh, Mm.W, n, sink, as, g.scan_top, (pd.flags & kPassEvenOdd) != 0,
                g.start_y, g.stop_y, g.left_bound, g.right_bound))
     return 0;
   AccFlush(lanes, as, sink);
   return 1;
 }
 
-// Sweep of pass p through the register sweep; a pass whose active list
-// outgrows it is marked for the generic sweep (pass_class 1).
-SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegShared* sh,
+// Which sweep form takes pass p: the register form for up to 64 active
+// edges (kSweepReg64), for up to 128 (kSweepReg128), or the generic form.
+// The geometry bounds the active list (PassGeom::max_active); a register
+// form whose list outgrows it after all hands the pass on (pass_class).
+enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1 };
+SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
+  if (pass_class != 0) return pass_class;
+  return max_active <= 64 ? kSweepReg64 : max_active <= kRegMaxM ? kSweepReg128 : kSweepGeneric;
+}
+
+// Sweep of pass p through the register form of size M; a pass whose active
+// list outgrows it is marked for the next form (pass_class).
+template <int M>
+SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegSharedT<M>* sh,
                          int32_t* sdiff, int32_t sdiff_cap) {
   const PassGeom g = b.geom[p];
   if (g.n_edges <= 0 || g.row1 <= g.row0) {
     EmptyPass(b, p, lanes);
     return;
   }
+  if (M > 64 && g.max_active <= 64) {
+    // handed on by the 64-edge form: drop the row entries it wrote
+    uint2* rows = b.rowspan + b.sweep[p].rbase;
+    for (int r = lanes.lane; r < g.row1 - g.row0; r += Lanes::n) rows[r] = make_uint2(0, 0);
+    lanes.sync();
+  }
   PoolSink sink;
   InitPoolSink(b, p, g, &sink);
-  if (!RunRegSweep(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
+  if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();
-    if (lanes.leader()) b.pass_class[p] = 1;
+    if (lanes.leader()) b.pass_class[p] = M <= 64 ? kSweepReg128 : kSweepGeneric;
     return;
   }
   FinishPass(b, p, &sink, lanes);

@@ -312,6 +312,9 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   BuildBins(hb, comp, db.n_bands, db.h_band_off, db.h_bins);
   SKC_TRY(Upload(db.band_off, db.h_band_off, s));
   SKC_TRY(Upload(db.bins, db.h_bins, s));
+  std::vector<uint32_t> order;
+  SweepOrder(db.h_geom, order);
+  SKC_TRY(Upload(db.sweep_order, order, s));
   // span indices are 32-bit
   const uint64_t kMaxPool = 0xFFFFFFFFull;
   uint64_t want = std::min<uint64_t>(std::max<uint64_t>(pl.span_estimate, 1 << 16), kMaxPool);
@@ -341,6 +344,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.comp = db.comp.as<PassComp>();
   b.band_off = db.band_off.as<uint32_t>();
   b.bins = db.bins.as<uint32_t>();
+  b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.span_next = ctx->span_next.as<unsigned long long>();
   // The sweep; if the span pool ran out it is grown to the size the sweep
   // reported and the sweep runs again (first renders of a context only).

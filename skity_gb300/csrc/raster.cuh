@@ -428,6 +428,10 @@ SKC_HD void unguarded_insertion_sort(int32_t* a, int first, int last, Less less)
     a[k] = v;
   }
 }
+struct IntLess {
+  SKC_HD bool operator()(int32_t a, int32_t b) const { return a < b; }
+};
+
 template <typename Less>
 SKC_HDN void introsort(int32_t* a, int n, Less less) {
   if (n < 2) return;

@@ -15,7 +15,7 @@
 //     the rank computation of LaneSweep otherwise;
 //   * each step's intervals, the one left open by a culled right edge
 //     included, are blitted in one pass after the reorder has been decided.
-// A path whose active list would exceed kRegMaxM edges is not swept here
+// A path whose active list would exceed M edges (the form's size) is not swept here
 // (RegWalk returns 0 before touching its sink's output for the first time
 // at that size) and goes to LaneSweep.
 #pragma once
@@ -23,10 +23,10 @@
 
 namespace skc {
 
-constexpr int kRegMaxM = 128;  // active edges held in registers
-// intervals of one step: at most one per pair of active edges, plus the one
-// left open by a culled right edge
-constexpr int kMaxIntervals = kRegMaxM / 2 + 4;
+constexpr int kRegMaxM = 128;  // the largest active list held in registers
+// intervals of one step with at most M active edges: one per pair of them,
+// plus the one left open by a culled right edge
+SKC_HD constexpr int RegIntervals(int M) { return M / 2 + 4; }
 
 // TrapRow set-ups of a step's intervals, one array per field.
 template <int N>
@@ -56,27 +56,38 @@ struct TrapRowSoA {
   }
 };
 
-// Per-warp shared block of the register sweep.
-struct RegShared {
-  int32_t xo[kRegMaxM];   // x before the step, by list position
-  int32_t xg[kRegMaxM];   //   after GoY
-  int32_t xf[kRegMaxM];   //   after the quad-piece update
-  int32_t dxo[kRegMaxM];  // dx before the step
-  int32_t dyo[kRegMaxM];  // dy before the step
-  int32_t dxf[kRegMaxM];  // dx after the update
-  int32_t ia[kRegMaxM];   // interval k: left position
-  int32_t ib[kRegMaxM];   //   right position
-  int32_t ax[kRegMaxM];   // active x at insertion; new rank by list position in the reorder
+// Per-warp shared block of the register sweep for active lists of up to
+// M edges.
+template <int M>
+struct RegSharedT {
+  static constexpr int kIntervals = RegIntervals(M);
+  static constexpr int kFlushEvents = 2 * M;  // nonzero accumulator entries a flush gathers
+  int32_t xo[M];   // x before the step, by list position
+  int32_t xg[M];   //   after GoY
+  int32_t xf[M];   //   after the quad-piece update
+  int32_t dxo[M];  // dx before the step
+  int32_t dyo[M];  // dy before the step
+  int32_t dxf[M];  // dx after the update
+  int32_t ia[M];   // interval k: left position
+  int32_t ib[M];   //   right position
+  int32_t ax[M];   // active x at insertion; new rank by list position in the reorder
   // edge state by new list position (reorder and insertion)
-  int32_t p_idx[kRegMaxM], p_x[kRegMaxM], p_dx[kRegMaxM], p_dy[kRegMaxM];
-  int32_t p_low[kRegMaxM], p_wc[kRegMaxM];
-  // the step's intervals (blit_trapezoid_row set-ups) and their first span
-  TrapRowSoA<kMaxIntervals> iv;
-  int32_t iv_start[kMaxIntervals + 4];
-  uint8_t surv[kRegMaxM];  // 1: survives the step
+  int32_t p_idx[M], p_x[M], p_dx[M], p_dy[M];
+  int32_t p_low[M], p_wc[M];
+  union {
+    struct {
+      // the step's intervals (blit_trapezoid_row set-ups) and their first span
+      TrapRowSoA<kIntervals> iv;
+      int32_t iv_start[kIntervals + 4];
+    } b;
+    // accumulator flush scratch (used between steps, never during a blit)
+    int32_t ev[2 * kFlushEvents];
+  } u;
+  uint8_t surv[M];  // 1: survives the step
 };
-// Host and device must agree on this size (the host sizes the launch).
-static_assert(sizeof(RegShared) % 16 == 0, "RegShared keeps 16-byte alignment");
+// Host and device must agree on these sizes (the host sizes the launch).
+static_assert(sizeof(RegSharedT<64>) % 16 == 0, "RegSharedT keeps 16-byte alignment");
+static_assert(sizeof(RegSharedT<128>) % 16 == 0, "RegSharedT keeps 16-byte alignment");
 
 SKC_HD int32_t MakeWc(int winding, int count) { return (winding & 0xFF) | ((count & 0xFF) << 8); }
 SKC_HD int WcWinding(int32_t wc) { return (int8_t)(wc & 0xFF); }
@@ -98,13 +109,15 @@ struct AccState {
   int left, width;
   int y;       // row being accumulated (kNaN32: none yet)
   int lo, hi;  // touched entries [lo, hi]
+  int32_t* ev; // flush scratch: (position, value) of nonzero entries
+  int ev_cap;
 };
 
 template <typename Sink>
 SKC_HD void AccFlush(const Lanes& L, AccState& a, Sink* sink) {
   if (a.y == kNaN32) return;
   if (a.lo <= a.hi) {
-    const bool read = sink->acc_row(L, a.y, a.diff, a.left, a.lo, a.hi);
+    const bool read = sink->acc_row(L, a.y, a.diff, a.left, a.lo, a.hi, a.ev, a.ev_cap);
     L.sync();
     if (read) {
       if (L.leader()) a.diff[a.hi] = 0;
@@ -131,8 +144,8 @@ SKC_HD void AccFlushIfNeed(const Lanes& L, AccState& a, Sink* sink, int row) {
 // lanes (span g on lane g mod 32), so a long partial row does not hold one
 // lane while the others wait.  Direct spans are written in that order, the
 // others go to the row accumulator.
-template <typename Sink>
-SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, const Edge* W,
+template <int M, typename Sink>
+SKC_HD void RegBlit(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as, const Edge* W,
                     int n, int y, Fixed next_y, int K, int m, int k, uint8_t full,
                     Fixed left_clip, Fixed right_clip, int trailing_a, bool trailing_nr) {
   constexpr int NL = Lanes::n;
@@ -195,14 +208,14 @@ SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, con
       TrapRow t;
       if (TrapPrepare(t, ul, ur, ll, lr, lDY, rDY, full, nr)) {
         cnt = TrapCount(t);
-        sh.iv.put(ki, t);
+        sh.u.b.iv.put(ki, t);
       }
     }
     const int32_t incl = LaneScanIncl(L, cnt);
-    if (ki < total) sh.iv_start[ki] = carry + incl - cnt;
+    if (ki < total) sh.u.b.iv_start[ki] = carry + incl - cnt;
     carry += LaneBcast(L, incl, NL - 1);
   }
-  if (L.leader()) sh.iv_start[total] = carry;
+  if (L.leader()) sh.u.b.iv_start[total] = carry;
   L.sync();
   const int T = carry;
   uint32_t run = 0;
@@ -214,11 +227,11 @@ SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, con
     bool kept = false;
     uint2 v = make_uint2(0, 0);
     if (g < T) {
-      while (sh.iv_start[iv + 1] <= g) ++iv;
-      const TrapRow t = sh.iv.get(iv);
+      while (sh.u.b.iv_start[iv + 1] <= g) ++iv;
+      const TrapRow t = sh.u.b.iv.get(iv);
       int x = 0, len = 0;
       uint8_t a = 0;
-      TrapSpan(t, g - sh.iv_start[iv], x, len, a);
+      TrapSpan(t, g - sh.u.b.iv_start[iv], x, len, a);
       if (t.real) {
         if (sink->keep(x, y, len, a)) {
           kept = true;
@@ -260,13 +273,13 @@ SKC_HD void RegBlit(const Lanes& L, RegShared& sh, Sink* sink, AccState& as, con
 }
 
 // WalkEdges over the pass's sorted edges W[0, n) (modified in place: quad
-// pieces).  Returns 0 if the active list would exceed kRegMaxM edges.
-template <typename Sink>
-SKC_HD int RegWalk(const Lanes& L, RegShared& sh, Edge* W, int n, Sink* sink, AccState& as,
+// pieces).  Returns 0 if the active list would exceed M edges.
+template <int M, typename Sink>
+SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink, AccState& as,
                    float scan_top, bool even_odd, int start_y, int stop_y, Fixed left_clip,
                    Fixed right_clip) {
   constexpr int NL = Lanes::n;
-  constexpr int S = kRegMaxM / NL;
+  constexpr int S = M / NL;
   constexpr unsigned kFull = NL == 32 ? 0xffffffffu : 1u;
   const int winding_mask = even_odd ? 1 : -1;
   int32_t r_idx[S], r_x[S], r_dx[S], r_dy[S], r_low[S], r_wc[S];
@@ -280,7 +293,7 @@ SKC_HD int RegWalk(const Lanes& L, RegShared& sh, Edge* W, int n, Sink* sink, Ac
     k += Lanes::popc(mask);
     if (mask != kFull) break;
   }
-  if (k > kRegMaxM) return 0;
+  if (k > M) return 0;
   int m = k;
   Fixed nny = kMaxS32;
   {
@@ -553,7 +566,7 @@ SKC_HD int RegWalk(const Lanes& L, RegShared& sh, Edge* W, int n, Sink* sink, Ac
         c += Lanes::popc(mask);
         if (mask != kFull) break;
       }
-      if (m + c > kRegMaxM) return 0;
+      if (m + c > M) return 0;
       const int32_t x0 = W[k].x;
 #pragma unroll
       for (int s = 0; s < S; ++s) {

@@ -93,9 +93,15 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   std::vector<uint8_t> pclass(np + 1);
   b.pass_class = pclass.data();
   b.reg_diff_cap = RegDiffCap(pl);
-  std::vector<int32_t> regmem((RegSmemBytes(b.reg_diff_cap) + 3) / 4);
-  RegShared* sh = (RegShared*)regmem.data();
-  int32_t* sdiff = (int32_t*)((uint8_t*)regmem.data() + sizeof(RegShared));
+  std::vector<int32_t> regmem64((RegSmemBytes<64>(b.reg_diff_cap) + 3) / 4);
+  auto* sh64 = (RegSharedT<64>*)regmem64.data();
+  int32_t* sdiff64 = (int32_t*)((uint8_t*)regmem64.data() + sizeof(RegSharedT<64>));
+  std::vector<int32_t> regmem((RegSmemBytes<kRegMaxM>(b.reg_diff_cap) + 3) / 4);
+  auto* sh = (RegSharedT<kRegMaxM>*)regmem.data();
+  int32_t* sdiff = (int32_t*)((uint8_t*)regmem.data() + sizeof(RegSharedT<kRegMaxM>));
+  std::vector<uint32_t> order;
+  SweepOrder(geom, order);
+  b.sweep_order = order.data();
   // span pool: start small so that the regrowth path runs too
   std::vector<uint2> pool(pool_hint ? pool_hint : 1024);
   unsigned long long next = 0;
@@ -108,9 +114,20 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     b.span_cap = pool.size();
     b.span_next = &next;
     generic = 0;
-    for (uint32_t p = 0; p < np; ++p) {
-      if (pclass[p] == 0) SweepPassReg(b, p, lanes, sh, sdiff, b.reg_diff_cap);
-      if (pclass[p] == 1) {
+    // the three sweep launches of the device pipeline, in the sweep order
+    for (uint32_t i = 0; i < np; ++i) {
+      const uint32_t p = order[i];
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg64)
+        SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap);
+    }
+    for (uint32_t i = 0; i < np; ++i) {
+      const uint32_t p = order[i];
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
+        SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+    }
+    for (uint32_t i = 0; i < np; ++i) {
+      const uint32_t p = order[i];
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepGeneric) {
         SweepPass(b, p, lanes);
         generic++;
       }
