@@ -136,12 +136,28 @@ typedef struct skity_cuda_stats {
   double blur_ms;         /* StackBlur of blur mask filter temp canvases */
   uint64_t fragments;     /* sum of span lengths inside the canvases */
   uint64_t graph_replays; /* 1: the render replayed the batch's CUDA graph */
+  uint64_t fragments_by_brush[4]; /* fragments shaded by solid, linear, radial
+                                     and image (blur composite) brushes */
 } skity_cuda_stats;
+
+/* Launch shape of the compositor and the granularity of its pass bins; no
+ * effect on the pixels.  The autotuner (skity_gb300/autotune.py) picks one
+ * per workload by timing batch renders. */
+typedef struct skity_cuda_raster_config {
+  uint32_t struct_size;   /* sizeof(skity_cuda_raster_config) */
+  uint32_t tile_width;    /* compositor row tile in pixels: 32..2048 (default 256) */
+  uint32_t ctas_per_sm;   /* persistent compositor CTAs per SM, 0: one warp per
+                             tile, no work queue (default 4) */
+  uint32_t band_rows;     /* rows per pass-bin band: 8, 16, 32 or 64 (default 16) */
+} skity_cuda_raster_config;
 
 /* ---- context ------------------------------------------------------------ */
 SKITY_CUDA_API int32_t skity_cuda_context_create(
     const skity_cuda_context_create_info* info, skity_cuda_context* out);
 SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx);
+/* Configuration of the context's batches and canvases created from now on. */
+SKITY_CUDA_API int32_t skity_cuda_context_set_config(skity_cuda_context ctx,
+                                                     const skity_cuda_raster_config* cfg);
 /* Stats of the context's last flush or batch render. */
 SKITY_CUDA_API int32_t skity_cuda_context_get_stats(skity_cuda_context ctx,
                                                     skity_cuda_stats* out);
@@ -198,6 +214,11 @@ SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch);
 SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
                                              uint8_t* out_pixels);
 SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch);
+/* Reconfigures a batch; its next render plans again (new replay graph). */
+SKITY_CUDA_API int32_t skity_cuda_batch_set_config(skity_cuda_batch batch,
+                                                   const skity_cuda_raster_config* cfg);
+SKITY_CUDA_API int32_t skity_cuda_batch_get_config(skity_cuda_batch batch,
+                                                   skity_cuda_raster_config* out);
 
 /* ---- serving ------------------------------------------------------------
  * No single reference call: a request loop that renders canvases as they

@@ -63,10 +63,13 @@ class Stats_(ctypes.Structure):
                 ("retries", ctypes.c_uint64), ("geometry_ms", ctypes.c_double),
                 ("sweep_count_ms", ctypes.c_double), ("sweep_emit_ms", ctypes.c_double),
                 ("composite_ms", ctypes.c_double), ("blur_ms", ctypes.c_double),
-                ("fragments", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64)]
+                ("fragments", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
+                ("fragments_by_brush", ctypes.c_uint64 * 4)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["fragments_by_brush"] = list(self.fragments_by_brush)
+        return d
 
 
 class ServerInfo_(ctypes.Structure):
@@ -79,6 +82,11 @@ class RequestInfo_(ctypes.Structure):
     _fields_ = [("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
                 ("batch_size", ctypes.c_uint32), ("width", ctypes.c_uint32),
                 ("height", ctypes.c_uint32)]
+
+
+class RasterConfig_(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("tile_width", ctypes.c_uint32),
+                ("ctas_per_sm", ctypes.c_uint32), ("band_rows", ctypes.c_uint32)]
 
 
 # every entry point declared in include/skity_cuda.h: name -> (restype, argtypes)
@@ -101,6 +109,9 @@ SIGNATURES = {
     "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
     "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
     "skity_cuda_batch_destroy": (None, [_vp]),
+    "skity_cuda_context_set_config": (ctypes.c_int32, [_vp, ctypes.POINTER(RasterConfig_)]),
+    "skity_cuda_batch_set_config": (ctypes.c_int32, [_vp, ctypes.POINTER(RasterConfig_)]),
+    "skity_cuda_batch_get_config": (ctypes.c_int32, [_vp, ctypes.POINTER(RasterConfig_)]),
     "skity_cuda_server_create": (ctypes.c_int32, [ctypes.POINTER(ServerInfo_), ctypes.POINTER(_vp)]),
     "skity_cuda_server_submit": (ctypes.c_int32, [_vp, _vp, ctypes.c_size_t,
                                                   ctypes.POINTER(ctypes.c_uint64)]),

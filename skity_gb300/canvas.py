@@ -227,6 +227,20 @@ class Batch:
         _lib.check(self.lib.skity_cuda_batch_render(self.handle), "skity_cuda_batch_render")
         return self.ctx.stats()
 
+    def set_config(self, tile_width: int = 256, ctas_per_sm: int = 4, band_rows: int = 16):
+        """skity_cuda_batch_set_config: the compositor's launch shape and bin
+        granularity (the pixels do not change); the next render replans."""
+        c = _lib.RasterConfig_(ctypes.sizeof(_lib.RasterConfig_), tile_width, ctas_per_sm,
+                               band_rows)
+        _lib.check(self.lib.skity_cuda_batch_set_config(self.handle, ctypes.byref(c)),
+                   "skity_cuda_batch_set_config")
+
+    def config(self) -> dict:
+        c = _lib.RasterConfig_()
+        _lib.check(self.lib.skity_cuda_batch_get_config(self.handle, ctypes.byref(c)),
+                   "skity_cuda_batch_get_config")
+        return {"tile_width": c.tile_width, "ctas_per_sm": c.ctas_per_sm, "band_rows": c.band_rows}
+
     def read(self, i: int, out: np.ndarray | None = None) -> np.ndarray:
         h, w = self.sizes[i]
         if out is None:

@@ -493,25 +493,26 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   return SKITY_CUDA_SUCCESS;
 }
 
-// Gives every canvas its range of row bands; returns the number of bands.
-inline uint32_t AssignBands(HostBatch& hb) {
+// Gives every canvas its range of row bands (1 << shift rows each);
+// returns the number of bands.
+inline uint32_t AssignBands(HostBatch& hb, int shift) {
   uint32_t n = 0;
   for (CanvasDesc& cd : hb.canvases) {
     cd.band0 = n;
-    n += (cd.h + (1u << kBandShift) - 1) >> kBandShift;
+    n += (cd.h + (1u << shift) - 1) >> shift;
   }
   return n;
 }
 // The compositor's pass bins: for every row band, the passes (in pass
 // order, which is draw order within a canvas) that have rows in it.
 inline void BuildBins(const HostBatch& hb, const std::vector<PassComp>& comp, uint32_t n_bands,
-                      std::vector<uint32_t>& band_off, std::vector<uint32_t>& bins) {
+                      int shift, std::vector<uint32_t>& band_off, std::vector<uint32_t>& bins) {
   band_off.assign((size_t)n_bands + 1, 0);
   for (size_t p = 0; p < comp.size(); ++p) {
     const PassComp& c = comp[p];
     if (c.row1 <= c.row0) continue;
     const uint32_t b0 = hb.canvases[hb.passes[p].canvas].band0;
-    for (int32_t k = c.row0 >> kBandShift; k <= (c.row1 - 1) >> kBandShift; ++k)
+    for (int32_t k = c.row0 >> shift; k <= (c.row1 - 1) >> shift; ++k)
       band_off[b0 + (uint32_t)k + 1]++;
   }
   for (uint32_t i = 0; i < n_bands; ++i) band_off[i + 1] += band_off[i];
@@ -521,9 +522,28 @@ inline void BuildBins(const HostBatch& hb, const std::vector<PassComp>& comp, ui
     const PassComp& c = comp[p];
     if (c.row1 <= c.row0) continue;
     const uint32_t b0 = hb.canvases[hb.passes[p].canvas].band0;
-    for (int32_t k = c.row0 >> kBandShift; k <= (c.row1 - 1) >> kBandShift; ++k)
+    for (int32_t k = c.row0 >> shift; k <= (c.row1 - 1) >> shift; ++k)
       bins[fill[b0 + (uint32_t)k]++] = (uint32_t)p;
   }
+}
+
+// Row tiles in the order the compositor should take them: most work first
+// (passes in the tile's band times its width), so that the heavy tiles do
+// not form the tail of the launch.
+inline void OrderRowTasks(const HostBatch& hb, const std::vector<uint32_t>& band_off, int shift,
+                          std::vector<RowTask>& tasks) {
+  std::vector<uint64_t> cost(tasks.size());
+  for (size_t i = 0; i < tasks.size(); ++i) {
+    const RowTask& t = tasks[i];
+    const uint32_t band = hb.canvases[t.canvas].band0 + (t.y >> shift);
+    cost[i] = (uint64_t)(band_off[band + 1] - band_off[band] + 1) * (t.x1 - t.x0);
+  }
+  std::vector<uint32_t> idx(tasks.size());
+  for (size_t i = 0; i < idx.size(); ++i) idx[i] = (uint32_t)i;
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  std::vector<RowTask> out(tasks.size());
+  for (size_t i = 0; i < idx.size(); ++i) out[i] = tasks[idx[i]];
+  tasks.swap(out);
 }
 
 inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv, uint32_t chunk,

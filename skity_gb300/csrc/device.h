@@ -43,6 +43,14 @@ struct DevBuf {
 
 struct Context;
 
+// Launch shape of the compositor and the granularity of its pass bins
+// (skity_cuda_raster_config; chosen per batch, e.g. by the autotuner).
+struct RasterConfig {
+  uint32_t tile_w = 256;     // row-tile width in pixels
+  uint32_t ctas_per_sm = 4;  // persistent compositor CTAs per SM (0: one warp per tile)
+  int32_t band_shift = 4;    // pass-bin bands of 1 << band_shift rows
+};
+
 // A batch resident on the device: inputs uploaded once, re-rendered on
 // demand.
 struct DeviceBatch {
@@ -56,6 +64,8 @@ struct DeviceBatch {
   std::vector<uint32_t> h_band_off, h_bins;
   uint32_t chunk = 1024;
   uint32_t n_bands = 0;
+  RasterConfig cfg;
+  DevBuf task_next;  // persistent compositor's counters
   // true when the caller has loaded the canvases' current pixels (a canvas
   // flush without a clear); otherwise a canvas without a clear colour starts
   // from transparent black, as a fresh Bitmap does
@@ -91,7 +101,8 @@ struct skity_cuda_context_s {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t stage[10] = {};
-  uint32_t tile_w = 256;  // composite row-tile width in pixels
+  skc::RasterConfig cfg;  // default launch shape of new batches and canvases
+  uint32_t num_sms = 0;
   skity_cuda_stats last{};
   std::mutex mu;
 };
@@ -107,6 +118,9 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db);
 // Renders the batch on the context's stream (planned render, or the replay
 // graphs when the batch has them); pixels stay on the device.
 int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed);
+// Rebuilds the row tiles and bands of an uploaded batch for `cfg`; the next
+// render plans again.
+int32_t ApplyConfig(skity_cuda_context_s* ctx, DeviceBatch& db, const RasterConfig& cfg);
 // Copies canvas `index` of the batch to host memory (row_bytes 0: packed).
 int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
                    size_t row_bytes);

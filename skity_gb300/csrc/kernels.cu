@@ -17,6 +17,8 @@
 // across pixels with a fixed lane per pixel column (no cross-lane hazards).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 
 #include "passes.cuh"
 
@@ -111,17 +113,34 @@ constexpr int kCompWarps = 4;
 // spans up to this many tile pixels are shaded by one lane
 constexpr int kShortSpan = 4;
 
+__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row, int lane);
+
+// counter == null: warp w of block k takes tile 4k + w; otherwise every warp
+// takes tiles from the counter until none is left (persistent grid).
 __global__ void __launch_bounds__(32 * kCompWarps, 4)
-    k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk) {
+    k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk,
+                unsigned int* counter) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
-  uint32_t* smem = (uint32_t*)reg_smem;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  uint32_t task = blockIdx.x * kCompWarps + wib;
-  if (task >= n_tasks) return;
-  const RowTask rt = tasks[task];
+  uint32_t* row = (uint32_t*)reg_smem + wib * chunk;
+  if (!counter) {
+    const uint32_t task = blockIdx.x * kCompWarps + wib;
+    if (task < n_tasks) CompositeTile(b, tasks[task], row, lane);
+    return;
+  }
+  for (;;) {
+    uint32_t task = 0;
+    if (lane == 0) task = atomicAdd(counter, 1u);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= n_tasks) return;
+    CompositeTile(b, tasks[task], row, lane);
+    __syncwarp();
+  }
+}
+
+__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row, int lane) {
   const CanvasDesc cd = b.canvases[rt.canvas];
-  uint32_t* row = smem + wib * chunk;
   const int y = (int)rt.y;
   const int x0 = (int)rt.x0, x1 = (int)rt.x1;
   const int n = x1 - x0;
@@ -130,7 +149,7 @@ __global__ void __launch_bounds__(32 * kCompWarps, 4)
     row[i] = cd.has_clear ? cd.clear_pm : RGBAtoARGB(gpx[i]);
   }
   __syncwarp();
-  const uint32_t band = cd.band0 + ((uint32_t)y >> kBandShift);
+  const uint32_t band = cd.band0 + ((uint32_t)y >> b.band_shift);
   const uint32_t e0 = b.band_off[band], e1 = b.band_off[band + 1];
   for (uint32_t eb = e0; eb < e1; eb += 32) {
     const uint32_t e = eb + lane;
@@ -215,14 +234,20 @@ __global__ void __launch_bounds__(32 * kCompWarps, 4)
 }
 
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,
+                    uint32_t ctas_per_sm, uint32_t num_sms, unsigned int* counter,
                     cudaStream_t stream) {
   if (n_tasks == 0) return 0;
   size_t smem = (size_t)kCompWarps * chunk * sizeof(uint32_t);
   if (smem > 48 * 1024) {
     cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
-  k_composite<<<(n_tasks + kCompWarps - 1) / kCompWarps, 32 * kCompWarps, smem, stream>>>(
-      b, tasks, n_tasks, chunk);
+  uint32_t grid = (n_tasks + kCompWarps - 1) / kCompWarps;
+  if (ctas_per_sm > 0 && counter) {
+    grid = std::min<uint32_t>(grid, ctas_per_sm * std::max<uint32_t>(num_sms, 1));
+  } else {
+    counter = nullptr;
+  }
+  k_composite<<<grid, 32 * kCompWarps, smem, stream>>>(b, tasks, n_tasks, chunk, counter);
   return 1;
 }
 

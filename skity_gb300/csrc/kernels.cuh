@@ -41,10 +41,9 @@ struct CanvasDesc {
   uint32_t band0;      // first entry of the canvas's row bands in band_off
 };
 
-// Rows of a canvas are grouped in bands of 1 << kBandShift rows; each band
-// lists, in draw order, the passes whose rows meet it (the compositor's
-// pass bins).
-constexpr int kBandShift = 4;
+// Rows of a canvas are grouped in bands of 1 << DevBatch::band_shift rows;
+// each band lists, in draw order, the passes whose rows meet it (the
+// compositor's pass bins).
 
 // Geometry scratch layout of one pass: capacities in elements.
 //   cap[0..2]  quad path (verbs, points, weights)
@@ -132,6 +131,8 @@ struct DevBatch {
   const uint32_t* band_off;  // per band: first entry in bins (one past the end follows)
   const uint32_t* bins;      // pass indices, per band in draw order
   const uint32_t* sweep_order;  // passes in the order the sweeps take them (null: index order)
+  int32_t band_shift;        // rows per pass-bin band: 1 << band_shift
+  unsigned int* task_next;   // persistent compositor's work counters (temp, main)
 };
 
 // Shared memory of one register-sweep warp: its RegSharedT block, then an
@@ -143,7 +144,10 @@ constexpr int32_t kRegDiffMax = 3072;
 // number of launches made
 int LaunchGeometry(const DevBatch& b, cudaStream_t stream);
 int LaunchSweep(const DevBatch& b, cudaStream_t stream);
+// ctas_per_sm > 0: a persistent grid of ctas_per_sm CTAs per SM taking row
+// tiles from `counter` (zeroed before the launch); 0: one warp per tile.
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,
+                    uint32_t ctas_per_sm, uint32_t num_sms, unsigned int* counter,
                     cudaStream_t stream);
 int LaunchBlur(const DevBatch& b, const uint32_t* temp_canvases, uint32_t n_temp,
                uint32_t max_h, uint32_t max_w, cudaStream_t stream);

@@ -747,7 +747,7 @@ SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* 
   const int y = (int)rt.y, x0 = (int)rt.x0, x1 = (int)rt.x1;
   uint32_t* gpx = (uint32_t*)(b.pixels + cd.px_off) + (size_t)y * cd.w + x0;
   for (int i = 0; i < x1 - x0; ++i) row[i] = cd.has_clear ? cd.clear_pm : RGBAtoARGB(gpx[i]);
-  const uint32_t band = cd.band0 + ((uint32_t)y >> kBandShift);
+  const uint32_t band = cd.band0 + ((uint32_t)y >> b.band_shift);
   for (uint32_t e = b.band_off[band]; e < b.band_off[band + 1]; ++e) {
     const PassComp pc = b.comp[b.bins[e]];
     if (y < pc.row0 || y >= pc.row1) continue;

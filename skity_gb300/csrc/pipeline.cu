@@ -62,7 +62,8 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.pts, hb.pts, s));
   SKC_TRY(Upload(db.weights, hb.weights, s));
   SKC_TRY(Upload(db.draws, hb.draws, s));
-  db.n_bands = AssignBands(hb);
+  db.cfg = ctx->cfg;
+  db.n_bands = AssignBands(hb, db.cfg.band_shift);
   SKC_TRY(Upload(db.canvases, hb.canvases, s));
   SKC_TRY(Upload(db.brushes, hb.brushes, s));
   SKC_TRY(Upload(db.stop_colors, hb.stop_colors, s));
@@ -70,7 +71,7 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.temps, hb.temp_canvases, s));
   uint32_t maxw = 1;
   for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
-  db.chunk = std::min<uint32_t>(maxw, std::max<uint32_t>(32, std::min<uint32_t>(ctx->tile_w, 2048)));
+  db.chunk = std::min<uint32_t>(maxw, std::max<uint32_t>(32, std::min<uint32_t>(db.cfg.tile_w, 2048)));
   BuildRowTasks(hb, hb.main_canvases, db.chunk, db.h_tasks_main);
   BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
   SKC_TRY(Upload(db.tasks_main, db.h_tasks_main, s));
@@ -81,7 +82,28 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
   SKC_TRY(Upload(db.roundtrip, rtab, s));
   SKC_TRY(db.pixels.ensure(std::max<uint64_t>(hb.pixel_bytes, 16)));
+  SKC_TRY(db.task_next.ensure(16));
   db.uploaded = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+int32_t ApplyConfig(skity_cuda_context_s* ctx, DeviceBatch& db, const RasterConfig& cfg) {
+  cudaStream_t s = ctx->stream;
+  HostBatch& hb = db.hb;
+  db.cfg = cfg;
+  db.n_bands = AssignBands(hb, cfg.band_shift);
+  SKC_TRY(Upload(db.canvases, hb.canvases, s));
+  uint32_t maxw = 1;
+  for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
+  db.chunk = std::min<uint32_t>(maxw, std::max<uint32_t>(32, std::min<uint32_t>(cfg.tile_w, 2048)));
+  BuildRowTasks(hb, hb.main_canvases, db.chunk, db.h_tasks_main);
+  BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
+  for (auto& g : db.graphs) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  db.graph_ok = false;
+  SKC_TRY(cudaStreamSynchronize(s));
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -114,15 +136,17 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
       return LaunchSweep(b, s);
     case 2:
       if (db.h_tasks_temp.empty()) return 0;
+      cudaMemsetAsync(b.task_next, 0, 4, s);
       return LaunchComposite(b, db.tasks_temp.as<RowTask>(), (uint32_t)db.h_tasks_temp.size(),
-                             db.chunk, s);
+                             db.chunk, db.cfg.ctas_per_sm, ctx->num_sms, b.task_next, s);
     case 3:
       if (db.h_tasks_temp.empty()) return 0;
       return LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
                         hb.max_temp_h, hb.max_temp_w, s);
     default:
+      cudaMemsetAsync(b.task_next + 1, 0, 4, s);
       return LaunchComposite(b, db.tasks_main.as<RowTask>(), (uint32_t)db.h_tasks_main.size(),
-                             db.chunk, s);
+                             db.chunk, db.cfg.ctas_per_sm, ctx->num_sms, b.task_next + 1, s);
   }
 }
 
@@ -309,9 +333,13 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   std::vector<PassComp> comp;
   PlanComp(hb, db.h_geom, sw, comp);
   SKC_TRY(Upload(db.comp, comp, s));
-  BuildBins(hb, comp, db.n_bands, db.h_band_off, db.h_bins);
+  BuildBins(hb, comp, db.n_bands, db.cfg.band_shift, db.h_band_off, db.h_bins);
   SKC_TRY(Upload(db.band_off, db.h_band_off, s));
   SKC_TRY(Upload(db.bins, db.h_bins, s));
+  OrderRowTasks(hb, db.h_band_off, db.cfg.band_shift, db.h_tasks_main);
+  OrderRowTasks(hb, db.h_band_off, db.cfg.band_shift, db.h_tasks_temp);
+  SKC_TRY(Upload(db.tasks_main, db.h_tasks_main, s));
+  SKC_TRY(Upload(db.tasks_temp, db.h_tasks_temp, s));
   std::vector<uint32_t> order;
   SweepOrder(db.h_geom, order);
   SKC_TRY(Upload(db.sweep_order, order, s));
@@ -345,6 +373,8 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.band_off = db.band_off.as<uint32_t>();
   b.bins = db.bins.as<uint32_t>();
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
+  b.band_shift = db.cfg.band_shift;
+  b.task_next = db.task_next.as<unsigned int>();
   b.span_next = ctx->span_next.as<unsigned long long>();
   // The sweep; if the span pool ran out it is grown to the size the sweep
   // reported and the sweep runs again (first renders of a context only).
@@ -381,9 +411,11 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.pixels = db.pixels.as<uint8_t>();
   b.roundtrip = db.roundtrip.as<uint8_t>();
   SKC_TRY(cudaEventRecord(ctx->stage[6], s));
+  SKC_TRY(cudaMemsetAsync(db.task_next.p, 0, 8, s));
   if (!db.h_tasks_temp.empty()) {
     st.kernel_launches += LaunchComposite(b, db.tasks_temp.as<RowTask>(),
-                                          (uint32_t)db.h_tasks_temp.size(), db.chunk, s);
+                                          (uint32_t)db.h_tasks_temp.size(), db.chunk,
+                                          db.cfg.ctas_per_sm, ctx->num_sms, b.task_next, s);
   }
   SKC_TRY(cudaEventRecord(ctx->stage[7], s));
   if (!db.h_tasks_temp.empty()) {
@@ -392,7 +424,8 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   }
   SKC_TRY(cudaEventRecord(ctx->stage[8], s));
   st.kernel_launches += LaunchComposite(b, db.tasks_main.as<RowTask>(),
-                                        (uint32_t)db.h_tasks_main.size(), db.chunk, s);
+                                        (uint32_t)db.h_tasks_main.size(), db.chunk,
+                                        db.cfg.ctas_per_sm, ctx->num_sms, b.task_next + 1, s);
   SKC_TRY(cudaEventRecord(ctx->stage[9], s));
   SKC_TRY(cudaGetLastError());
   if (timed) SKC_TRY(cudaEventRecord(ctx->ev1, s));
@@ -419,6 +452,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     for (uint32_t p = 0; p < np; ++p) {
       st.spans += pspans[p];
       st.fragments += pfrags[p];
+      st.fragments_by_brush[hb.brushes[hb.passes[p].brush].kind & 3] += pfrags[p];
     }
   }
   db.stats = st;
@@ -500,6 +534,9 @@ SKITY_CUDA_API int32_t skity_cuda_context_create(const skity_cuda_context_create
   if (!c) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
   c->device = device;
   c->budget = budget;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess)
+    c->num_sms = (uint32_t)sms;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
@@ -525,6 +562,29 @@ SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx) {
   for (auto& e : ctx->stage) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+static bool ToConfig(const skity_cuda_raster_config* c, skc::RasterConfig* out) {
+  if (!c || c->struct_size < sizeof(skity_cuda_raster_config)) return false;
+  if (c->tile_width < 32 || c->tile_width > 2048 || c->ctas_per_sm > 64) return false;
+  int shift = -1;
+  for (int k = 3; k <= 6; ++k)
+    if (c->band_rows == (1u << k)) shift = k;
+  if (shift < 0) return false;
+  out->tile_w = c->tile_width;
+  out->ctas_per_sm = c->ctas_per_sm;
+  out->band_shift = shift;
+  return true;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_context_set_config(skity_cuda_context ctx,
+                                                     const skity_cuda_raster_config* cfg) {
+  if (!ctx) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  skc::RasterConfig rc;
+  if (!ToConfig(cfg, &rc)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->cfg = rc;
+  return SKITY_CUDA_SUCCESS;
 }
 
 SKITY_CUDA_API int32_t skity_cuda_context_get_stats(skity_cuda_context ctx, skity_cuda_stats* out) {
@@ -601,6 +661,27 @@ SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t in
   std::lock_guard<std::mutex> lock(batch->ctx->mu);
   cudaSetDevice(batch->ctx->device);
   return skc::ReadCanvas(batch->ctx, batch->db, index, out_pixels, 0);
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_set_config(skity_cuda_batch batch,
+                                                   const skity_cuda_raster_config* cfg) {
+  if (!batch) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  skc::RasterConfig rc;
+  if (!ToConfig(cfg, &rc)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(batch->ctx->mu);
+  cudaSetDevice(batch->ctx->device);
+  return skc::ApplyConfig(batch->ctx, batch->db, rc);
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_get_config(skity_cuda_batch batch,
+                                                   skity_cuda_raster_config* out) {
+  if (!batch) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  out->struct_size = sizeof(skity_cuda_raster_config);
+  out->tile_width = batch->db.cfg.tile_w;
+  out->ctas_per_sm = batch->db.cfg.ctas_per_sm;
+  out->band_rows = 1u << batch->db.cfg.band_shift;
+  return SKITY_CUDA_SUCCESS;
 }
 
 SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch) {

@@ -79,7 +79,8 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   std::vector<PassComp> comp;
   PlanComp(hb, geom, sw, comp);
   std::vector<uint32_t> band_off, bins;
-  BuildBins(hb, comp, AssignBands(hb), band_off, bins);
+  b.band_shift = 4;
+  BuildBins(hb, comp, AssignBands(hb, b.band_shift), b.band_shift, band_off, bins);
   b.sweep = sw.data();
   b.sweepmem = sweepmem.data();
   uint32_t err = 0;
