@@ -105,6 +105,29 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# Integer ops per fragment, counted from the reference's formulas: coverage
+# AlphaMulQ 9 + PMSrcOver 14 (color_priv.hpp:62-72) for every fragment; a
+# linear gradient adds the mapping 4, stop search and lerp ~26, Color4fToColor
+# 16 and premultiply 18 (sw_span_brush.cc:239-320, color.cc:53-59,
+# color_priv.hpp:47-58); radial adds the second coordinate and the length 8;
+# the blur composite's image brush adds the mapping and a nearest sample 12.
+OPS_PER_FRAGMENT = (23, 93, 101, 35)  # solid, linear, radial, image
+
+
+def issue_roofline(st, frame_ms, composite_ms, clk):
+    """Fragment work against the int32 issue peak (152 SMs x 128 lanes x the
+    SM clock sampled during the timed region): over the whole frame and over
+    the compositing stage, where the fragments are shaded and blended."""
+    frags = st.get("fragments_by_brush") or [st["fragments"], 0, 0, 0]
+    ops = sum(o * f for o, f in zip(OPS_PER_FRAGMENT, frags))
+    mhz = clk.get("sm_mhz") or 2070.0
+    peak = 152 * 128 * mhz * 1e6
+    return {"ops_per_frame": ops, "peak_ops_per_s": peak, "sm_mhz": mhz,
+            "frac_frame": ops / (frame_ms / 1e3) / peak if frame_ms else None,
+            "frac_composite": ops / (composite_ms / 1e3) / peak if composite_ms else None,
+            "fragments_by_brush": dict(zip(("solid", "linear", "radial", "image"), frags))}
+
+
 def load_scene():
     from skity_gb300 import scene as S
     cache = os.path.join("/tmp", "skity_config2_v1.bin")
@@ -347,6 +370,56 @@ def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512)
             "offline_batched": offline, "rates": results}
 
 
+def load_config4():
+    from skity_gb300 import scene as S
+    cache = os.path.join("/tmp", "skity_config4_v1.bin")
+    try:
+        with open(cache, "rb") as f:
+            return S.Scene.from_bytes(f.read())
+    except Exception:
+        sc = S.config4()
+        try:
+            with open(cache, "wb") as f:
+                f.write(sc.to_bytes())
+        except Exception:
+            pass
+        return sc
+
+
+def other_workloads(ctx, steps: int):
+    """The 512x512 scene (1,000 fills) and the glyph-dense scene (4096x4096,
+    100,000 small even-odd outlines, a tenth with a kNormal blur): resident
+    batch renders (CUDA-graph replays) against the CPU oracle on one core
+    over the whole scene (a single canvas has no parallelism in the
+    reference)."""
+    from oracle import oracle
+    from skity_gb300 import scene as S
+    from skity_gb300.canvas import Batch
+    out = {}
+    for name, sc, desc in [
+            ("config1", S.config1(), "512x512, 1,000 fills of 3-32 verbs, nonzero, solid"),
+            ("config4", load_config4(), "4096x4096, 100,000 outlines (1-3 contours, 8-48 px), "
+                                        "even-odd, 10% kNormal blur sigma 2-20")]:
+        b = Batch(ctx, [sc])
+        for _ in range(3):
+            b.render()
+        ms = [b.render()["device_ms"] for _ in range(steps)]
+        st = ctx.stats()
+        b.close()
+        gms = statistics.mean(ms)
+        _, cst = oracle.render(sc)
+        px = sc.width * sc.height
+        out[name] = {"workload": desc, "paths": sc.n_draws,
+                     "gpu": {"ms": gms, "paths_per_s": sc.n_draws * 1e3 / gms,
+                             "mpix_per_s": px / 1e3 / gms,
+                             "stage_ms": {k: st[k] for k in ("geometry_ms", "sweep_emit_ms",
+                                                             "composite_ms", "blur_ms")}},
+                     "cpu": {"s": cst.seconds, "paths_per_s": sc.n_draws / cst.seconds,
+                             "cores": 1, "kind": "port", "sample": "whole scene"},
+                     "gpu_over_cpu": (sc.n_draws * 1e3 / gms) / (sc.n_draws / cst.seconds)}
+    return out
+
+
 def cpu_baseline(scene, threads: int, sample_paths: int, steps: int = 1):
     """The oracle (CPU restatement of the reference path) on the first
     `sample_paths` draws; paths/s over `steps` repetitions."""
@@ -472,12 +545,15 @@ def run_gpu(args, rank, world, local):
         "roofline": {"kernel": dom.replace("_ms", ""), "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else None,
                      "peak_source": peak_kind, "traffic": None},
+        "issue_roofline": issue_roofline(last, ms_per_step, stage_ms["composite_ms"], clk),
         "e2e": {"value": (world * paths / (e2e_ms_mean / 1e3)) if e2e_ms_mean else None,
                 "unit": "paths/s", "h2d_bytes_per_step": len(scene.to_bytes()),
                 "d2h_bytes_per_step": scene.width * scene.height * 4,
                 "ms_per_step": e2e_ms_mean},
         "wall_s": wall,
     }
+    if rank == 0 and not args.no_others:
+        line["other_workloads"] = other_workloads(ctx, max(1, min(args.steps, 5)))
     if rank == 0 and args.serve_seconds > 0:
         line["serving"] = serving(ctx, [float(r) for r in args.serve_rates.split(",")],
                                   args.serve_seconds, local)
@@ -511,6 +587,8 @@ def main():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the 256-canvas batched / per-draw / CPU comparison")
     ap.add_argument("--per-draw-sample", type=int, default=16)
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the 512x512 and glyph-dense scenes")
     ap.add_argument("--serve-rates", default="200,1000,5000",
                     help="Poisson request rates (requests/s) of the serving runs")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
