@@ -188,6 +188,8 @@ def batch_forms(ctx, steps: int, warmup: int, sample: int):
     pix = sum(sc.width * sc.height for sc in scenes)
     paths = sum(sc.n_draws for sc in scenes)
     batch = Batch(ctx, scenes)
+    from skity_gb300 import autotune
+    tuned = autotune.tune(batch, autotune.signature(scenes, "GB300"), reps=2)
     for _ in range(max(warmup, 1)):
         batch.render()
     ms = []
@@ -201,6 +203,8 @@ def batch_forms(ctx, steps: int, warmup: int, sample: int):
            "canvases": len(scenes), "paths": paths, "mpix": pix / 1e6,
            "batched": {"ms": bms, "mpix_per_s": pix / 1e3 / bms, "paths_per_s": paths * 1e3 / bms,
                        "graph_replays": int(st["graph_replays"]), "stage_ms": stage,
+                       "raster_config": tuned["config"], "autotune_cached": tuned["cached"],
+                       "autotune_trials": len(tuned.get("trials", [])),
                        "spans": st["spans"], "fragments": st["fragments"],
                        "form": "one planned batch, "
                        "CUDA-graph replay (geometry, sweeps, composites)"}}

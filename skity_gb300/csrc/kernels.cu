@@ -113,7 +113,16 @@ constexpr int kCompWarps = 4;
 // spans up to this many tile pixels are shaded by one lane
 constexpr int kShortSpan = 4;
 
-__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row, int lane);
+// gradient stops a warp stages in shared memory (longer gradients are read
+// from global memory)
+constexpr int kStagedStops = 16;
+// shared memory of one compositor warp: its tile row, then the staged stops
+__host__ __device__ constexpr size_t CompWarpSmem(uint32_t chunk) {
+  return (size_t)chunk * 4 + kStagedStops * (16 + 4);
+}
+
+__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
+                              float4* stage_colors, float* stage_offsets, int lane);
 
 // counter == null: warp w of block k takes tile 4k + w; otherwise every warp
 // takes tiles from the counter until none is left (persistent grid).
@@ -123,10 +132,13 @@ __global__ void __launch_bounds__(32 * kCompWarps, 4)
   extern __shared__ __align__(16) uint8_t reg_smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  uint32_t* row = (uint32_t*)reg_smem + wib * chunk;
+  uint8_t* mine = reg_smem + (size_t)wib * CompWarpSmem(chunk);
+  uint32_t* row = (uint32_t*)mine;
+  float4* stage_colors = (float4*)(mine + (size_t)chunk * 4);
+  float* stage_offsets = (float*)(stage_colors + kStagedStops);
   if (!counter) {
     const uint32_t task = blockIdx.x * kCompWarps + wib;
-    if (task < n_tasks) CompositeTile(b, tasks[task], row, lane);
+    if (task < n_tasks) CompositeTile(b, tasks[task], row, stage_colors, stage_offsets, lane);
     return;
   }
   for (;;) {
@@ -134,12 +146,13 @@ __global__ void __launch_bounds__(32 * kCompWarps, 4)
     if (lane == 0) task = atomicAdd(counter, 1u);
     task = __shfl_sync(0xffffffffu, task, 0);
     if (task >= n_tasks) return;
-    CompositeTile(b, tasks[task], row, lane);
+    CompositeTile(b, tasks[task], row, stage_colors, stage_offsets, lane);
     __syncwarp();
   }
 }
 
-__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row, int lane) {
+__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
+                              float4* stage_colors, float* stage_offsets, int lane) {
   const CanvasDesc cd = b.canvases[rt.canvas];
   const int y = (int)rt.y;
   const int x0 = (int)rt.x0, x1 = (int)rt.x1;
@@ -151,27 +164,42 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
   __syncwarp();
   const uint32_t band = cd.band0 + ((uint32_t)y >> b.band_shift);
   const uint32_t e0 = b.band_off[band], e1 = b.band_off[band + 1];
+  // 32 bin entries at a time: each lane looks up its pass's row entry, so
+  // the row-table loads of 32 passes are in flight together and passes
+  // with no spans on this row cost no serial step
   for (uint32_t eb = e0; eb < e1; eb += 32) {
     const uint32_t e = eb + lane;
-    bool hit = false;
-    PassComp pc;
-    pc.row0 = pc.row1 = 0;
-    pc.rbase = pc.brush = 0;
+    uint2 rs = make_uint2(0, 0);
+    uint32_t brush = 0;
     if (e < e1) {
-      pc = b.comp[b.bins[e]];
-      hit = y >= pc.row0 && y < pc.row1;
+      const PassComp pc = b.comp[b.bins[e]];
+      if (y >= pc.row0 && y < pc.row1) {
+        rs = b.rowspan[pc.rbase + (y - pc.row0)];
+        brush = pc.brush;
+      }
     }
-    uint32_t mask = __ballot_sync(0xffffffffu, hit);
+    uint32_t mask = __ballot_sync(0xffffffffu, rs.y != 0);
     while (mask) {
-      int bit = __ffs(mask) - 1;
+      const int bit = __ffs(mask) - 1;
       mask &= mask - 1;
-      const int32_t qrow0 = __shfl_sync(0xffffffffu, pc.row0, bit);
-      const uint32_t qrbase = __shfl_sync(0xffffffffu, pc.rbase, bit);
-      const uint32_t qbrush = __shfl_sync(0xffffffffu, pc.brush, bit);
-      const uint2 rs = b.rowspan[qrbase + (y - qrow0)];
-      const uint32_t s0 = rs.x, s1 = rs.x + rs.y;
-      if (s0 == s1) continue;
-      const Brush br = b.brushes[qbrush];
+      const uint32_t s0 = __shfl_sync(0xffffffffu, rs.x, bit);
+      const uint32_t s1 = s0 + __shfl_sync(0xffffffffu, rs.y, bit);
+      const uint32_t qbrush = __shfl_sync(0xffffffffu, brush, bit);
+      Brush br = b.brushes[qbrush];
+      const float4* stop_colors = b.stop_colors;
+      const float* stop_offsets = b.stop_offsets;
+      if ((br.kind == 1 || br.kind == 2) && br.stop_count <= (uint32_t)kStagedStops) {
+        // the gradient's stops, read for every pixel, staged in shared memory
+        __syncwarp();
+        if (lane < (int)br.stop_count) {
+          stage_colors[lane] = b.stop_colors[br.stop0 + lane];
+          stage_offsets[lane] = b.stop_offsets[br.stop0 + lane];
+        }
+        __syncwarp();
+        stop_colors = stage_colors;
+        stop_offsets = stage_offsets;
+        br.stop0 = 0;
+      }
       const uint2* sp = b.spans;
       for (uint32_t sb = s0; sb < s1; sb += 32) {
         int xs = 0, xe = 0;
@@ -202,7 +230,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
           const bool is_short = xe - xs <= kShortSpan;
           if (mine_now && is_short) {
             for (int x = xs; x < xe; ++x) {
-              uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip);
               if (alpha != 255) c = AlphaMulQ(c, alpha);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);
@@ -216,7 +244,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
             const int qe = __shfl_sync(0xffffffffu, xe, j);
             const uint32_t qa = __shfl_sync(0xffffffffu, alpha, j);
             for (int x = qs + ((lane - qs) & 31); x < qe; x += 32) {
-              uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip);
               if (qa != 255) c = AlphaMulQ(c, qa);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);
@@ -237,7 +265,7 @@ int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, u
                     uint32_t ctas_per_sm, uint32_t num_sms, unsigned int* counter,
                     cudaStream_t stream) {
   if (n_tasks == 0) return 0;
-  size_t smem = (size_t)kCompWarps * chunk * sizeof(uint32_t);
+  size_t smem = (size_t)kCompWarps * CompWarpSmem(chunk);
   if (smem > 48 * 1024) {
     cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
