@@ -180,6 +180,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas,
 SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
                                                    const skity_cuda_path* path,
                                                    const skity_cuda_paint* paint);
+/* Canvas::Save / Restore / Translate (include/skity/render/canvas.hpp):
+ * the canvas matrix as a translation; later draws are recorded with it.
+ * Other matrices (scale, rotation, skew) are not taken by this canvas. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas);
+SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas);
+SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy);
 /* Canvas::Flush: renders the recorded draws on the GPU and writes the
  * bitmap's pixels. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas);

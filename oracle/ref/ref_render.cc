@@ -34,7 +34,7 @@ struct PaintRec {
   float fill_color[4];
   float stroke_color[4];
   float stroke_width, miter;
-  uint32_t reserved[2];
+  float translate[2];  // Canvas::Translate in effect for the draw
 };
 static_assert(sizeof(PaintRec) == 80, "paint record layout");
 
@@ -196,7 +196,16 @@ int main(int argc, char** argv) {
   if (s.has_clear) {
     canvas->Clear(skity::Color4f{s.clear[0], s.clear[1], s.clear[2], s.clear[3]});
   }
-  for (size_t i = 0; i < paths.size(); ++i) canvas->DrawPath(paths[i], paints[i]);
+  for (size_t i = 0; i < paths.size(); ++i) {
+    const PaintRec& pr = s.paints[first + i];
+    const bool moved = pr.translate[0] != 0.f || pr.translate[1] != 0.f;
+    if (moved) {
+      canvas->Save();
+      canvas->Translate(pr.translate[0], pr.translate[1]);
+    }
+    canvas->DrawPath(paths[i], paints[i]);
+    if (moved) canvas->Restore();
+  }
   canvas->Flush();
   auto t1 = std::chrono::steady_clock::now();
   if (timed) {

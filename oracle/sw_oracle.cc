@@ -1526,7 +1526,7 @@ struct PaintRec {
   float fill_color[4];
   float stroke_color[4];
   float stroke_width, miter;
-  uint32_t reserved[2];
+  float translate[2];  // canvas translation of the draw
 };
 static_assert(sizeof(PaintRec) == 80, "paint layout");
 struct GradRec {
@@ -1704,6 +1704,10 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
   for (uint32_t d = first; d < last; ++d) {
     if (s.paints[d].blur_style != 0) {
       HandleBlurFilter(s, d, &t, &st);
+    } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
+      // Canvas::Translate then DrawPath: the CTM reaches RastePath and the brush
+      DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
+                         s.paints[d].translate[1], &t, &st);
     } else {
       DrawPath(s, d, &t, &st, &spans);
     }
@@ -1747,6 +1751,9 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
       for (uint32_t d = first; d < last; ++d) {
         if (s.paints[d].blur_style != 0) {
           HandleBlurFilter(s, d, &t, &st[k]);
+        } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
+          DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
+                             s.paints[d].translate[1], &t, &st[k]);
         } else {
           DrawPath(s, d, &t, &st[k], &spans);
         }

@@ -102,6 +102,9 @@ SIGNATURES = {
     "skity_cuda_canvas_clear": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "skity_cuda_canvas_draw_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.POINTER(Paint_)]),
     "skity_cuda_canvas_flush": (ctypes.c_int32, [_vp]),
+    "skity_cuda_canvas_save": (ctypes.c_int32, [_vp]),
+    "skity_cuda_canvas_restore": (ctypes.c_int32, [_vp]),
+    "skity_cuda_canvas_translate": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
     "skity_cuda_render_streams": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
                                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),

@@ -18,8 +18,19 @@ CUDACanvas::~CUDACanvas() { skity_cuda_canvas_destroy(canvas_); }
 
 void CUDACanvas::OnClipPath(Path const&, ClipOp) { status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED; }
 
+// The canvas matrix as a translation, or false when it is anything else.
+static bool TranslationOf(const Matrix& m, float* tx, float* ty) {
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r)
+      if (!(c == 3 && r < 2) && m.Get(r, c) != (r == c ? 1.f : 0.f)) return false;
+  *tx = m.GetTranslateX();
+  *ty = m.GetTranslateY();
+  return true;
+}
+
 void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
-  if (!GetTotalMatrix().IsIdentity()) {
+  float tx = 0.f, ty = 0.f;
+  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     return;
   }
@@ -90,7 +101,13 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
     q.blur_style = static_cast<uint32_t>(mf->GetBlurStyle());
     q.blur_radius = mf->GetBlurRadius();
   }
+  const bool moved = tx != 0.f || ty != 0.f;
+  if (moved) {
+    skity_cuda_canvas_save(canvas_);
+    skity_cuda_canvas_translate(canvas_, tx, ty);
+  }
   status_ = skity_cuda_canvas_draw_path(canvas_, &p, &q);
+  if (moved) skity_cuda_canvas_restore(canvas_);
 }
 
 void CUDACanvas::OnSaveLayer(const Rect&, const Paint&) {

@@ -8,7 +8,7 @@
 //
 // What differs from the software canvas: pixels are written to the bitmap at
 // Flush(), not during each draw.  Operations outside the GPU raster path --
-// clips, layers, text, images, non-identity canvas matrices, shader local
+// clips, layers, text, images, canvas matrices other than translations, shader local
 // matrices, sweep/conical gradients, blur styles other than kNormal, blend
 // modes other than clear/src/dst/src-over -- draw nothing and leave
 // SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus().

@@ -326,6 +326,16 @@ class Canvas:
                                                         ctypes.byref(cpaint)),
                    "skity_cuda_canvas_draw_path")
 
+    def Save(self):
+        _lib.check(self.lib.skity_cuda_canvas_save(self.handle), "skity_cuda_canvas_save")
+
+    def Restore(self):
+        _lib.check(self.lib.skity_cuda_canvas_restore(self.handle), "skity_cuda_canvas_restore")
+
+    def Translate(self, dx, dy):
+        _lib.check(self.lib.skity_cuda_canvas_translate(self.handle, float(dx), float(dy)),
+                   "skity_cuda_canvas_translate")
+
     def Flush(self):
         _lib.check(self.lib.skity_cuda_canvas_flush(self.handle), "skity_cuda_canvas_flush")
 

@@ -33,7 +33,7 @@ struct PaintRec {
   float fill_color[4];
   float stroke_color[4];
   float stroke_width, miter;
-  uint32_t reserved[2];
+  float translate[2];  // canvas translation of the draw (CTM = Translate(tx, ty))
 };
 static_assert(sizeof(PaintRec) == 80, "paint layout");
 struct GradRec {
@@ -98,6 +98,18 @@ inline bool ValidPaint(uint32_t style, uint32_t cap, uint32_t join, float stroke
   return true;
 }
 
+// A canvas translation keeps the draw's points inside the coordinate range
+// ValidPath allows.
+inline bool ValidTranslate(const float t[2], const float* pts, uint32_t np) {
+  if (!(std::fabs(t[0]) <= kMaxCoord && std::fabs(t[1]) <= kMaxCoord)) return false;
+  if (t[0] == 0.f && t[1] == 0.f) return true;
+  for (uint32_t i = 0; i < np; ++i) {
+    if (!(std::fabs(pts[2 * i] + t[0]) <= kMaxCoord && std::fabs(pts[2 * i + 1] + t[1]) <= kMaxCoord))
+      return false;
+  }
+  return true;
+}
+
 inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   if (!buf || len < 72 || std::memcmp(buf, "SKSC", 4) != 0) return false;
   uint32_t hdr[7];
@@ -143,6 +155,8 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
     if (s->paints[d].gradient >= (int32_t)s->ng) return false;
     const PaintRec& pr = s->paints[d];
     if (!ValidPaint(pr.style, pr.cap, pr.join, pr.stroke_width, pr.miter, pr.blur_radius))
+      return false;
+    if (!ValidTranslate(pr.translate, s->pts + 2 * (size_t)s->po[d], s->po[d + 1] - s->po[d]))
       return false;
     if (!ValidPath(s->verbs + s->vo[d], s->vo[d + 1] - s->vo[d], s->pts + 2 * (size_t)s->po[d],
                    s->po[d + 1] - s->po[d], s->wts + s->wo[d], s->wo[d + 1] - s->wo[d]))
@@ -389,9 +403,12 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     hb.draw_count++;
     bool blur = pr.blur_style != 0 && pr.blur_radius > 0;  // MakeBlur(r <= 0) is null
     if (!blur) {
-      AddDrawPasses(hb, s, d, draw, cidx, 0.f, 0.f, main_passes);
+      // the canvas translation goes where the reference's CopyWithMatrix
+      // and device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
+      AddDrawPasses(hb, s, d, draw, cidx, pr.translate[0], pr.translate[1], main_passes);
       continue;
     }
+    if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (pr.blur_style != 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
     const float* p = s.pts + 2 * (size_t)s.po[d];

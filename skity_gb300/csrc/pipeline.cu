@@ -508,6 +508,9 @@ struct skity_cuda_canvas_s {
   std::vector<skc::PaintRec> paints;
   std::vector<skc::GradRec> grads;
   std::vector<float> stop_colors, stop_offsets;
+  // canvas matrix (a translation) and its save stack
+  float tx = 0.f, ty = 0.f;
+  std::vector<std::pair<float, float>> saved;
   skc::DeviceBatch db;
 };
 
@@ -785,6 +788,13 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   std::memcpy(pr.stroke_color, paint->stroke_color, 16);
   pr.stroke_width = paint->stroke_width;
   pr.miter = paint->miter_limit;
+  pr.translate[0] = canvas->tx;
+  pr.translate[1] = canvas->ty;
+  if (!skc::ValidTranslate(pr.translate, path->points, path->point_count))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if ((canvas->tx != 0.f || canvas->ty != 0.f) && paint->blur_style != 0 &&
+      paint->blur_radius > 0.f)
+    return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (paint->shader) {
     const skity_cuda_gradient* g = paint->shader;
     if (!g->colors || (g->has_offsets && !g->offsets)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
@@ -814,6 +824,33 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   canvas->wo.push_back((uint32_t)canvas->wts.size());
   canvas->paints.push_back(pr);
   canvas->dirty = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  canvas->saved.emplace_back(canvas->tx, canvas->ty);
+  return SKITY_CUDA_SUCCESS;
+}
+
+// Canvas::Restore with nothing saved leaves the matrix as it is.
+SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!canvas->saved.empty()) {
+    canvas->tx = canvas->saved.back().first;
+    canvas->ty = canvas->saved.back().second;
+    canvas->saved.pop_back();
+  }
+  return SKITY_CUDA_SUCCESS;
+}
+
+// The product of two translations: Translate(tx, ty) * Translate(dx, dy)
+// holds tx + dx in float (matrix.cc:452-460 with the zero terms exact).
+SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!std::isfinite(dx) || !std::isfinite(dy)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  canvas->tx = canvas->tx + dx;
+  canvas->ty = canvas->ty + dy;
   return SKITY_CUDA_SUCCESS;
 }
 

@@ -45,12 +45,14 @@ BLUR_NONE, BLUR_NORMAL = 0, 1
 MAGIC = b"SKSC"
 VERSION = 1
 
-# paint record: 20 x 4 bytes (matches skity_cuda_paint in include/skity_cuda.h)
+# paint record: 20 x 4 bytes: the Paint fields the raster path reads, the
+# path's fill type, and the canvas translation in effect for the draw
+# (Canvas::Translate; the rest of the canvas matrix is identity)
 PAINT_DTYPE = np.dtype([
     ("style", "<u4"), ("cap", "<u4"), ("join", "<u4"), ("blend", "<u4"),
     ("fill_type", "<u4"), ("gradient", "<i4"), ("blur_style", "<u4"),
     ("blur_radius", "<f4"), ("fill_color", "<f4", 4), ("stroke_color", "<f4", 4),
-    ("stroke_width", "<f4"), ("miter", "<f4"), ("reserved", "<u4", 2)])
+    ("stroke_width", "<f4"), ("miter", "<f4"), ("translate", "<f4", 2)])
 assert PAINT_DTYPE.itemsize == 80
 # gradient record: 12 x 4 bytes (matches skity_cuda_gradient)
 GRADIENT_DTYPE = np.dtype([

@@ -53,6 +53,18 @@ int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas, const skity_cuda_path* p,
   std::printf(" blur=%u,%g\n", q->blur_style, q->blur_radius);
   return SKITY_CUDA_SUCCESS;
 }
+int32_t skity_cuda_canvas_save(skity_cuda_canvas) {
+  std::printf("save\n");
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_restore(skity_cuda_canvas) {
+  std::printf("restore\n");
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_translate(skity_cuda_canvas, float dx, float dy) {
+  std::printf("translate %g %g\n", dx, dy);
+  return SKITY_CUDA_SUCCESS;
+}
 int32_t skity_cuda_canvas_flush(skity_cuda_canvas) {
   std::printf("flush\n");
   return SKITY_CUDA_SUCCESS;
@@ -98,6 +110,10 @@ int main() {
   canvas->DrawPath(path, paint);
   canvas->Save();
   canvas->Translate(5, 0);
+  canvas->Translate(0.5f, -2);
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Scale(2, 2);
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
   canvas->Restore();

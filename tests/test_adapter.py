@@ -56,7 +56,11 @@ def test_shaders_and_mask_filter(driver_output):
     assert "shader=2 tile=0 stops=3 offsets=0 p0=20,15" in rad and "r=12" in rad
 
 
-def test_unsupported_ops_report_status(driver_output):
-    # a translated canvas matrix is outside the GPU path: nothing drawn, -5
-    assert driver_output[9] == "status=-5"
-    assert driver_output[10:] == ["flush", "status=0", "destroy 0x10"]
+def test_translation_forwarded_other_matrices_refused(driver_output):
+    # Translate(5, 0) then Translate(0.5, -2): one translation of (5.5, -2)
+    # around the draw; a scaled matrix is outside the GPU path (-5)
+    assert driver_output[9:12] == ["save", "translate 5.5 -2", driver_output[11]]
+    assert driver_output[11].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[12:14] == ["restore", "status=0"]
+    assert driver_output[14] == "status=-5"
+    assert driver_output[15:] == ["flush", "status=0", "destroy 0x10"]

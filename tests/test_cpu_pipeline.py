@@ -126,3 +126,11 @@ def test_register_and_generic_sweeps_agree(cpu_pipeline):
     a, _ = cpu_render(cpu_pipeline, sc, 0)
     g, _ = cpu_render(cpu_pipeline, sc, 1)
     assert np.array_equal(a, g)
+
+
+def test_canvas_translate_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import translated_scene
+    sc = translated_scene()
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0

@@ -149,3 +149,36 @@ def test_invalid_arguments_are_rejected(gpu_ctx):
     cp = _lib.Path_(ctypes.cast(verbs, ctypes.c_void_p), 2, ctypes.cast(pts, ctypes.c_void_p), 1, None, 0, 0)
     paint = _lib.Paint_()
     assert lib.skity_cuda_canvas_draw_path(c.handle, ctypes.byref(cp), ctypes.byref(paint)) == -2
+
+
+def test_canvas_translate_matches_oracle(gpu_ctx, oracle_lib):
+    """Canvas::Save / Translate / Restore: the translated scene rendered
+    as a batch and through the canvas API against the oracle (pinned to the
+    reference's Canvas::Translate)."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import translated_scene
+    from skity_gb300.canvas import Canvas, Paint, Path
+    sc = translated_scene()
+    check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
+    bitmap = np.zeros((40, 48, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    tri = Path().MoveTo(2, 2).LineTo(20, 5).LineTo(6, 19).Close()
+    paint = Paint().SetFillColor(0.2, 0.3, 0.9, 0.8)
+    canvas.DrawPath(tri, paint)
+    canvas.Save()
+    canvas.Translate(10.5, 3)
+    canvas.Translate(4, 7.25)
+    canvas.DrawPath(tri, paint)
+    canvas.Restore()
+    canvas.DrawPath(tri, Paint().SetFillColor(0.9, 0.1, 0.1, 0.5))
+    canvas.Flush()
+    sb = S.SceneBuilder(48, 40)
+    for tr, col in [((0, 0), (0.2, 0.3, 0.9, 0.8)), ((14.5, 10.25), (0.2, 0.3, 0.9, 0.8)),
+                    ((0, 0), (0.9, 0.1, 0.1, 0.5))]:
+        p = S.default_paint()
+        p["fill_color"] = col
+        p["translate"] = tr
+        sb.draw_path(tri.verbs, tri.points, p)
+    check(oracle_lib, bitmap, sb.build())

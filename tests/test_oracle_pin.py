@@ -85,3 +85,20 @@ def test_styles_blend_modes_and_tile_modes(ref):
                                            (float(5 + i), 0.0), cols, offs, tile_mode=i % 4)
         b.draw_path(verbs, pts, p)
     _pin(ref, b.build())
+
+
+def translated_scene(seed=S.SEED_BASE + 360):
+    """Draws under Canvas::Translate: fills, strokes and gradients with
+    per-draw translations (some fractional, some moving paths off-canvas)."""
+    sc = S.random_paths_scene(seed, 180, 140, 40, 2, 24, coord_lo=(-20.0, -20.0),
+                              coord_hi=(160.0, 120.0), evenodd_frac=0.4, gradient_frac=0.5,
+                              stroke_frac=0.3)
+    rng = np.random.default_rng(seed & 0xFFFF)
+    for d in range(sc.n_draws):
+        if d % 4 != 3:
+            sc.paints[d]["translate"] = rng.uniform(-40, 40, 2).astype(np.float32)
+    return sc
+
+
+def test_canvas_translate(ref):
+    _pin(ref, translated_scene())
