@@ -95,9 +95,27 @@ static void LaunchRegForm(const DevBatch& b, cudaStream_t stream) {
 }
 
 int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
+  return LaunchSweep(b, stream, nullptr, nullptr, nullptr);
+}
+
+// With a side stream the two register forms run concurrently -- the
+// 128-edge form (few, long sweeps) on the side stream, the 64-edge form on
+// `stream` -- so the long sweeps overlap the many short ones instead of
+// forming a tail of their own; the generic form runs after both.
+int LaunchSweep(const DevBatch& b, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork,
+                cudaEvent_t join) {
   if (b.n_passes == 0) return 0;
-  LaunchRegForm<64, kSweepReg64>(b, stream);
-  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
+  if (side) {
+    cudaEventRecord(fork, stream);
+    cudaStreamWaitEvent(side, fork, 0);
+    LaunchRegForm<kRegMaxM, kSweepReg128>(b, side);
+    LaunchRegForm<64, kSweepReg64>(b, stream);
+    cudaEventRecord(join, side);
+    cudaStreamWaitEvent(stream, join, 0);
+  } else {
+    LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
+    LaunchRegForm<64, kSweepReg64>(b, stream);
+  }
   k_sweep<<<(b.n_passes + kSweepWarps - 1) / kSweepWarps, 32 * kSweepWarps, 0, stream>>>(b);
   return 3;
 }

@@ -630,7 +630,8 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
 // Which sweep form takes pass p: the register form for up to 64 active
 // edges (kSweepReg64), for up to 128 (kSweepReg128), or the generic form.
 // The geometry bounds the active list (PassGeom::max_active); a register
-// form whose list outgrows it after all hands the pass on (pass_class).
+// form whose list outgrows it after all hands the pass to the generic form
+// (pass_class).
 enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1 };
 SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
@@ -638,7 +639,8 @@ SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
 }
 
 // Sweep of pass p through the register form of size M; a pass whose active
-// list outgrows it is marked for the next form (pass_class).
+// list outgrows it after all is handed to the generic form (pass_class),
+// which runs after both register forms and clears the rows first.
 template <int M>
 SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegSharedT<M>* sh,
                          int32_t* sdiff, int32_t sdiff_cap) {
@@ -647,17 +649,11 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
     EmptyPass(b, p, lanes);
     return;
   }
-  if (M > 64 && g.max_active <= 64) {
-    // handed on by the 64-edge form: drop the row entries it wrote
-    uint2* rows = b.rowspan + b.sweep[p].rbase;
-    for (int r = lanes.lane; r < g.row1 - g.row0; r += Lanes::n) rows[r] = make_uint2(0, 0);
-    lanes.sync();
-  }
   PoolSink sink;
   InitPoolSink(b, p, g, &sink);
   if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();
-    if (lanes.leader()) b.pass_class[p] = M <= 64 ? kSweepReg128 : kSweepGeneric;
+    if (lanes.leader()) b.pass_class[p] = kSweepGeneric;
     return;
   }
   FinishPass(b, p, &sink, lanes);

@@ -118,13 +118,13 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     // the three sweep launches of the device pipeline, in the sweep order
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg64)
-        SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap);
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
+        SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
-        SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg64)
+        SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
