@@ -99,8 +99,6 @@ struct skity_cuda_context_s {
   // to what the largest render so far needed
   skc::DevBuf span_pool, span_next;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;  // second stream: sweep forms run concurrently
-  cudaEvent_t fork = nullptr, join = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t stage[10] = {};
   skc::RasterConfig cfg;  // default launch shape of new batches and canvases

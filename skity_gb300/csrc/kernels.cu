@@ -38,11 +38,11 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
 
 // Sweeps: one warp per pass, passes taken in the batch's sweep order
 // (longest expected sweeps first, so the long ones do not form the tail).
-// Three forms, each launched over every pass and taking the ones
-// SweepForm gives it: the register form for up to 64 active edges, the
-// register form for up to 128 (2 warps per block, each with its RegSharedT
-// block and accumulator in shared memory), then the generic sweep (4 warps
-// per block, state in global memory) for longer lists.
+// Four forms, each launched over every pass and taking the ones SweepForm
+// gives it: register forms for up to 32, 64 and 128 active edges (2 warps
+// per block, each with its RegSharedT block and accumulator in shared
+// memory), then the generic sweep (4 warps per block, state in global
+// memory) for longer lists.
 constexpr int kSweepWarps = 4;
 constexpr int kRegWarps = 2;
 
@@ -56,8 +56,12 @@ __device__ __forceinline__ uint32_t SweepPassAt(const DevBatch& b, uint32_t i) {
   return b.sweep_order ? b.sweep_order[i] : i;
 }
 
+// Minimum resident blocks per SM asked of the compiler for the form of size
+// M (a register budget: fewer registers per thread, more warps per SM).
+__host__ __device__ constexpr int RegMinBlocks(int M) { return M <= 32 ? 10 : 1; }
+
 template <int M, int kForm>
-__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
+__global__ void __launch_bounds__(32 * kRegWarps, RegMinBlocks(M)) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   const int w = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * kRegWarps + w;
@@ -95,29 +99,12 @@ static void LaunchRegForm(const DevBatch& b, cudaStream_t stream) {
 }
 
 int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
-  return LaunchSweep(b, stream, nullptr, nullptr, nullptr);
-}
-
-// With a side stream the two register forms run concurrently -- the
-// 128-edge form (few, long sweeps) on the side stream, the 64-edge form on
-// `stream` -- so the long sweeps overlap the many short ones instead of
-// forming a tail of their own; the generic form runs after both.
-int LaunchSweep(const DevBatch& b, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork,
-                cudaEvent_t join) {
   if (b.n_passes == 0) return 0;
-  if (side) {
-    cudaEventRecord(fork, stream);
-    cudaStreamWaitEvent(side, fork, 0);
-    LaunchRegForm<kRegMaxM, kSweepReg128>(b, side);
-    LaunchRegForm<64, kSweepReg64>(b, stream);
-    cudaEventRecord(join, side);
-    cudaStreamWaitEvent(stream, join, 0);
-  } else {
-    LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
-    LaunchRegForm<64, kSweepReg64>(b, stream);
-  }
+  LaunchRegForm<32, kSweepReg32>(b, stream);
+  LaunchRegForm<64, kSweepReg64>(b, stream);
+  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
   k_sweep<<<(b.n_passes + kSweepWarps - 1) / kSweepWarps, 32 * kSweepWarps, 0, stream>>>(b);
-  return 3;
+  return 4;
 }
 
 // ---------------------------------------------------------------------------

@@ -144,8 +144,6 @@ constexpr int32_t kRegDiffMax = 3072;
 // number of launches made
 int LaunchGeometry(const DevBatch& b, cudaStream_t stream);
 int LaunchSweep(const DevBatch& b, cudaStream_t stream);
-int LaunchSweep(const DevBatch& b, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork,
-                cudaEvent_t join);
 // ctas_per_sm > 0: a persistent grid of ctas_per_sm CTAs per SM taking row
 // tiles from `counter` (zeroed before the launch); 0: one warp per tile.
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,

@@ -627,15 +627,18 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
   return 1;
 }
 
-// Which sweep form takes pass p: the register form for up to 64 active
-// edges (kSweepReg64), for up to 128 (kSweepReg128), or the generic form.
+// Which sweep form takes pass p: the register form for up to 32, 64 or 128
+// active edges, or the generic form.
 // The geometry bounds the active list (PassGeom::max_active); a register
 // form whose list outgrows it after all hands the pass to the generic form
 // (pass_class).
-enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1 };
+enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1, kSweepReg32 = 3 };
 SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
-  return max_active <= 64 ? kSweepReg64 : max_active <= kRegMaxM ? kSweepReg128 : kSweepGeneric;
+  return max_active <= 32   ? kSweepReg32
+         : max_active <= 64 ? kSweepReg64
+         : max_active <= kRegMaxM ? kSweepReg128
+                                  : kSweepGeneric;
 }
 
 // Sweep of pass p through the register form of size M; a pass whose active

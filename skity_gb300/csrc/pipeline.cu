@@ -133,7 +133,7 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
       cudaMemsetAsync(db.err.p, 0, 16, s);
       cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s);
       cudaMemsetAsync(ctx->span_next.p, 0, 8, s);
-      return LaunchSweep(b, s, ctx->side, ctx->fork, ctx->join);
+      return LaunchSweep(b, s);
     case 2:
       if (db.h_tasks_temp.empty()) return 0;
       cudaMemsetAsync(b.task_next, 0, 4, s);
@@ -387,7 +387,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
     SKC_TRY(cudaMemsetAsync(ctx->span_next.p, 0, 8, s));
     SKC_TRY(cudaEventRecord(ctx->stage[4], s));
-    st.kernel_launches += LaunchSweep(b, s, ctx->side, ctx->fork, ctx->join);
+    st.kernel_launches += LaunchSweep(b, s);
     SKC_TRY(cudaEventRecord(ctx->stage[5], s));
     SKC_TRY(cudaGetLastError());
     unsigned long long used = 0;
@@ -542,10 +542,7 @@ SKITY_CUDA_API int32_t skity_cuda_context_create(const skity_cuda_context_create
     c->num_sms = (uint32_t)sms;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
     delete c;
     return SKITY_CUDA_ERROR_INITIALIZATION_FAILED;
   }
@@ -563,12 +560,8 @@ SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  cudaStreamSynchronize(ctx->side);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
-  cudaEventDestroy(ctx->fork);
-  cudaEventDestroy(ctx->join);
-  cudaStreamDestroy(ctx->side);
   for (auto& e : ctx->stage) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -86,6 +86,7 @@ struct RegSharedT {
   uint8_t surv[M];  // 1: survives the step
 };
 // Host and device must agree on these sizes (the host sizes the launch).
+static_assert(sizeof(RegSharedT<32>) % 16 == 0, "RegSharedT keeps 16-byte alignment");
 static_assert(sizeof(RegSharedT<64>) % 16 == 0, "RegSharedT keeps 16-byte alignment");
 static_assert(sizeof(RegSharedT<128>) % 16 == 0, "RegSharedT keeps 16-byte alignment");
 

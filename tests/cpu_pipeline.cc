@@ -94,6 +94,9 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   std::vector<uint8_t> pclass(np + 1);
   b.pass_class = pclass.data();
   b.reg_diff_cap = RegDiffCap(pl);
+  std::vector<int32_t> regmem32((RegSmemBytes<32>(b.reg_diff_cap) + 3) / 4);
+  auto* sh32 = (RegSharedT<32>*)regmem32.data();
+  int32_t* sdiff32 = (int32_t*)((uint8_t*)regmem32.data() + sizeof(RegSharedT<32>));
   std::vector<int32_t> regmem64((RegSmemBytes<64>(b.reg_diff_cap) + 3) / 4);
   auto* sh64 = (RegSharedT<64>*)regmem64.data();
   int32_t* sdiff64 = (int32_t*)((uint8_t*)regmem64.data() + sizeof(RegSharedT<64>));
@@ -120,6 +123,11 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
       const uint32_t p = order[i];
       if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
         SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+    }
+    for (uint32_t i = 0; i < np; ++i) {
+      const uint32_t p = order[i];
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg32)
+        SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
