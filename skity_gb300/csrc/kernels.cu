@@ -60,50 +60,80 @@ __device__ __forceinline__ uint32_t SweepPassAt(const DevBatch& b, uint32_t i) {
 // M (a register budget: fewer registers per thread, more warps per SM).
 __host__ __device__ constexpr int RegMinBlocks(int M) { return M <= 32 ? 10 : 1; }
 
+// Lets the next overlapped launch start once every CTA of this one runs.
+__device__ __forceinline__ void AllowNextLaunch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// End of a sweep kernel that may have overlapped the one before it: the
+// CTA that finishes last waits for that kernel to complete, so this kernel
+// completes only after every earlier sweep kernel has, and the work queued
+// after the sweeps sees all of them done.  (In a launch that overlapped
+// nothing the wait returns at once.)
+__device__ __forceinline__ void FinishOverlapped(unsigned int* done) {
+  if (!done) return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(done, 1u) == gridDim.x - 1) asm volatile("griddepcontrol.wait;" ::: "memory");
+  }
+}
+
 template <int M, int kForm>
 __global__ void __launch_bounds__(32 * kRegWarps, RegMinBlocks(M)) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
+  AllowNextLaunch();
   const int w = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * kRegWarps + w;
-  if (i >= b.n_passes) return;
-  const uint32_t p = SweepPassAt(b, i);
-  if (SweepForm(b.geom[p].max_active, b.pass_class[p]) != kForm) return;
-  if (DynamicSmemBytes() < kRegWarps * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
-    FlagError(b.err, 16);
-    return;
+  if (i < b.n_passes) {
+    const uint32_t p = SweepPassAt(b, i);
+    if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kForm) {
+      if (DynamicSmemBytes() < kRegWarps * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
+        FlagError(b.err, 16);
+      } else {
+        Lanes L;
+        L.lane = threadIdx.x & 31;
+        uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes<M>(b.reg_diff_cap);
+        SweepPassReg<M>(b, p, L, (RegSharedT<M>*)mine,
+                        (int32_t*)(mine + sizeof(RegSharedT<M>)), b.reg_diff_cap);
+      }
+    }
   }
-  Lanes L;
-  L.lane = threadIdx.x & 31;
-  uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes<M>(b.reg_diff_cap);
-  SweepPassReg<M>(b, p, L, (RegSharedT<M>*)mine, (int32_t*)(mine + sizeof(RegSharedT<M>)),
-                  b.reg_diff_cap);
+  FinishOverlapped(b.sweep_done ? b.sweep_done + (kForm & 3) : nullptr);
 }
 
 __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
+  AllowNextLaunch();
   const uint32_t i = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
-  if (i >= b.n_passes) return;
-  const uint32_t p = SweepPassAt(b, i);
-  Lanes L;
-  L.lane = threadIdx.x & 31;
-  if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
+  if (i < b.n_passes) {
+    const uint32_t p = SweepPassAt(b, i);
+    Lanes L;
+    L.lane = threadIdx.x & 31;
+    if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
+  }
+  FinishOverlapped(b.sweep_done ? b.sweep_done + kSweepGeneric : nullptr);
 }
 
 template <int M, int kForm>
-static void LaunchRegForm(const DevBatch& b, cudaStream_t stream) {
+static void LaunchRegForm(const DevBatch& b, cudaStream_t stream, bool overlap) {
   const size_t smem = kRegWarps * RegSmemBytes<M>(b.reg_diff_cap);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_sweep_reg<M, kForm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-  k_sweep_reg<M, kForm>
-      <<<(b.n_passes + kRegWarps - 1) / kRegWarps, 32 * kRegWarps, smem, stream>>>(b);
+  LaunchOverlapped(k_sweep_reg<M, kForm>, dim3((b.n_passes + kRegWarps - 1) / kRegWarps),
+                   dim3(32 * kRegWarps), smem, stream, overlap, b);
 }
 
+// With b.sweep_done (four zeroed counters) the later forms overlap the
+// earlier ones' tails; without, they run one after the other.
 int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
-  LaunchRegForm<32, kSweepReg32>(b, stream);
-  LaunchRegForm<64, kSweepReg64>(b, stream);
-  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream);
-  k_sweep<<<(b.n_passes + kSweepWarps - 1) / kSweepWarps, 32 * kSweepWarps, 0, stream>>>(b);
+  const bool overlap = b.sweep_done != nullptr;
+  LaunchRegForm<32, kSweepReg32>(b, stream, false);
+  LaunchRegForm<64, kSweepReg64>(b, stream, overlap);
+  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream, overlap);
+  LaunchOverlapped(k_sweep, dim3((b.n_passes + kSweepWarps - 1) / kSweepWarps),
+                   dim3(32 * kSweepWarps), 0, stream, overlap, b);
   return 4;
 }
 

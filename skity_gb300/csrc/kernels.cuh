@@ -133,6 +133,8 @@ struct DevBatch {
   const uint32_t* sweep_order;  // passes in the order the sweeps take them (null: index order)
   int32_t band_shift;        // rows per pass-bin band: 1 << band_shift
   unsigned int* task_next;   // persistent compositor's work counters (temp, main)
+  unsigned int* sweep_done;  // per sweep form, CTAs finished (zeroed before the sweeps);
+                             // null: the forms' launches do not overlap
 };
 
 // Shared memory of one register-sweep warp: its RegSharedT block, then an

@@ -628,10 +628,10 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
 }
 
 // Which sweep form takes pass p: the register form for up to 32, 64 or 128
-// active edges, or the generic form.
-// The geometry bounds the active list (PassGeom::max_active); a register
-// form whose list outgrows it after all hands the pass to the generic form
-// (pass_class).
+// active edges, or the generic form, by the geometry's bound of the active
+// list (PassGeom::max_active); pass_class != 0 forces the generic form.
+// The forms' kernels take disjoint passes and depend on nothing the others
+// write, so their launches may overlap.
 enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1, kSweepReg32 = 3 };
 SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
@@ -641,9 +641,11 @@ SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
                                   : kSweepGeneric;
 }
 
-// Sweep of pass p through the register form of size M; a pass whose active
-// list outgrows it after all is handed to the generic form (pass_class),
-// which runs after both register forms and clears the rows first.
+SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes);
+
+// Sweep of pass p through the register form of size M; should its active
+// list outgrow M after all, the same warp sweeps the pass again with the
+// generic form (which clears the rows the attempt wrote).
 template <int M>
 SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegSharedT<M>* sh,
                          int32_t* sdiff, int32_t sdiff_cap) {
@@ -656,7 +658,7 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
   InitPoolSink(b, p, g, &sink);
   if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();
-    if (lanes.leader()) b.pass_class[p] = kSweepGeneric;
+    SweepPass(b, p, lanes);
     return;
   }
   FinishPass(b, p, &sink, lanes);

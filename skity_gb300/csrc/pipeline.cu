@@ -82,7 +82,7 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
   SKC_TRY(Upload(db.roundtrip, rtab, s));
   SKC_TRY(db.pixels.ensure(std::max<uint64_t>(hb.pixel_bytes, 16)));
-  SKC_TRY(db.task_next.ensure(16));
+  SKC_TRY(db.task_next.ensure(32));
   db.uploaded = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -133,6 +133,7 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
       cudaMemsetAsync(db.err.p, 0, 16, s);
       cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s);
       cudaMemsetAsync(ctx->span_next.p, 0, 8, s);
+      cudaMemsetAsync(b.sweep_done, 0, 16, s);
       return LaunchSweep(b, s);
     case 2:
       if (db.h_tasks_temp.empty()) return 0;
@@ -375,6 +376,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.band_shift = db.cfg.band_shift;
   b.task_next = db.task_next.as<unsigned int>();
+  b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.span_next = ctx->span_next.as<unsigned long long>();
   // The sweep; if the span pool ran out it is grown to the size the sweep
   // reported and the sweep runs again (first renders of a context only).
@@ -386,6 +388,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     SKC_TRY(cudaMemsetAsync(db.err.p, 0, 16, s));
     SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
     SKC_TRY(cudaMemsetAsync(ctx->span_next.p, 0, 8, s));
+    SKC_TRY(cudaMemsetAsync(b.sweep_done, 0, 16, s));
     SKC_TRY(cudaEventRecord(ctx->stage[4], s));
     st.kernel_launches += LaunchSweep(b, s);
     SKC_TRY(cudaEventRecord(ctx->stage[5], s));
