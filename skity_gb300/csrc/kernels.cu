@@ -114,6 +114,26 @@ __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
   FinishOverlapped(b.sweep_done ? b.sweep_done + kSweepGeneric : nullptr);
 }
 
+// Launch with programmatic stream serialization: the kernel may start as
+// soon as every CTA of the kernel before it has started (and signalled, at
+// its beginning), so it fills the SMs that kernel's tail leaves idle.  The
+// sweep forms take disjoint passes and read nothing the others write.
+template <typename... Args>
+static void LaunchOverlapped(void (*kernel)(Args...), dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t stream, bool overlap, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = overlap ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int M, int kForm>
 static void LaunchRegForm(const DevBatch& b, cudaStream_t stream, bool overlap) {
   const size_t smem = kRegWarps * RegSmemBytes<M>(b.reg_diff_cap);
