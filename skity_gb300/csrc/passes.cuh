@@ -271,6 +271,8 @@ struct PoolSink : SinkBase {
     return cur;
   }
   SKC_HD uint2* span_ptr(uint64_t i) { return dead ? nullptr : pool + i; }
+  // n: spans appended (warp-uniform); f: this lane's share of their
+  // fragments (the shares are summed once, when the pass finishes)
   SKC_HD void commit(const Lanes&, uint32_t n, unsigned long long f) {
     cur += n;
     kept += n;
@@ -366,7 +368,7 @@ struct PoolSink : SinkBase {
         if (dst) {
           for (int i = 0; i < cnt; ++i) dst[i] = out[i];
         }
-        commit(L, total, LaneSum64(L, fr));
+        commit(L, total, fr);
       }
       carry = LaneBcast(L, incl, Lanes::n - 1);
       prev_sat = LaneBcast(L, sat, Lanes::n - 1);
@@ -377,7 +379,7 @@ struct PoolSink : SinkBase {
         const uint64_t at = reserve(L, 0, 1);
         if (!dead && L.leader())
           pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
-        commit(L, 1, (unsigned)len);
+        commit(L, 1, L.leader() ? (unsigned)len : 0u);
       }
     }
     return true;
@@ -504,7 +506,7 @@ struct PoolSink : SinkBase {
         if (dst) {
           for (int i = 0; i < cnt; ++i) dst[i] = out[i];
         }
-        commit(L, total, LaneSum64(L, fr));
+        commit(L, total, fr);
       }
       carry += LaneBcast(L, incl, Lanes::n - 1);
       prev_sat = LaneBcast(L, sat[V - 1], Lanes::n - 1);
@@ -514,7 +516,7 @@ struct PoolSink : SinkBase {
       if (keep(x, y, len, (uint8_t)open_v)) {
         const uint64_t at = reserve(L, 0, 1);
         if (!dead && L.leader()) pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
-        commit(L, 1, (unsigned)len);
+        commit(L, 1, L.leader() ? (unsigned)len : 0u);
       }
     }
     return true;
@@ -546,10 +548,11 @@ SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, PoolS
 
 SKC_HD void FinishPass(const DevBatch& b, uint32_t p, PoolSink* s, const Lanes& L) {
   s->finish_row(L);
+  const unsigned long long frags = LaneSum64(L, s->frags);
   L.sync();
   if (L.leader()) {
     b.pass_spans[p] = (uint32_t)s->kept;
-    if (b.pass_frags) b.pass_frags[p] = s->frags;
+    if (b.pass_frags) b.pass_frags[p] = frags;
   }
 }
 

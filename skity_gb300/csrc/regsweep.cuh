@@ -109,7 +109,7 @@ struct AccState {
   int32_t* diff;
   int left, width;
   int y;       // row being accumulated (kNaN32: none yet)
-  int lo, hi;  // touched entries [lo, hi]
+  int lo, hi;  // touched entries [lo, hi] (this lane's adds; reduced at the flush)
   int32_t* ev; // flush scratch: (position, value) of nonzero entries
   int ev_cap;
 };
@@ -117,6 +117,8 @@ struct AccState {
 template <typename Sink>
 SKC_HD void AccFlush(const Lanes& L, AccState& a, Sink* sink) {
   if (a.y == kNaN32) return;
+  a.lo = LaneMin(L, a.lo);
+  a.hi = LaneMax(L, a.hi);
   if (a.lo <= a.hi) {
     const bool read = sink->acc_row(L, a.y, a.diff, a.left, a.lo, a.hi, a.ev, a.ev_cap);
     L.sync();
@@ -262,13 +264,10 @@ SKC_HD void RegBlit(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as,
       run += cnt;
     }
   }
-  frags = LaneSum64(L, frags);
-  lo = LaneMin(L, lo);
-  hi = LaneMax(L, hi);
-  if (lo <= hi) {
-    as.lo = min_(as.lo, lo);
-    as.hi = max_(as.hi, hi);
-  }
+  // the fragment count and the accumulator's touched range stay per lane
+  // (summed at the pass's end, reduced at the row's flush)
+  as.lo = min_(as.lo, lo);
+  as.hi = max_(as.hi, hi);
   sink->commit(L, run, frags);
   L.sync();
 }

@@ -637,14 +637,13 @@ struct LaneSweep {
       run += chunk_total;
       frags += o.frags;
     }
-    frags = LaneSum64(L, frags);
     lo = LaneMin(L, lo);
     hi = LaneMax(L, hi);
     if (lo <= hi) {
       touch_lo = min_(touch_lo, lo);
       touch_hi = max_(touch_hi, hi);
     }
-    sink->commit(L, run, frags);
+    sink->commit(L, run, frags);  // this lane's share
     L.sync();
   }
 
