@@ -148,12 +148,14 @@ static void LaunchRegForm(const DevBatch& b, cudaStream_t stream, bool overlap) 
 // earlier ones' tails; without, they run one after the other.
 int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   if (b.n_passes == 0) return 0;
+  // heaviest form first: the longest sweeps start at once, and each later
+  // (lighter) form fills the SMs the earlier ones' tails leave idle
   const bool overlap = b.sweep_done != nullptr;
-  LaunchRegForm<32, kSweepReg32>(b, stream, false);
-  LaunchRegForm<64, kSweepReg64>(b, stream, overlap);
-  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream, overlap);
   LaunchOverlapped(k_sweep, dim3((b.n_passes + kSweepWarps - 1) / kSweepWarps),
-                   dim3(32 * kSweepWarps), 0, stream, overlap, b);
+                   dim3(32 * kSweepWarps), 0, stream, false, b);
+  LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream, overlap);
+  LaunchRegForm<64, kSweepReg64>(b, stream, overlap);
+  LaunchRegForm<32, kSweepReg32>(b, stream, overlap);
   return 4;
 }
 

@@ -118,16 +118,19 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     b.span_cap = pool.size();
     b.span_next = &next;
     generic = 0;
-    // the three sweep launches of the device pipeline, in the sweep order
+    // the sweep launches of the device pipeline (heaviest form first), each
+    // in the sweep order
+    for (uint32_t i = 0; i < np; ++i) {
+      const uint32_t p = order[i];
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepGeneric) {
+        SweepPass(b, p, lanes);
+        generic++;
+      }
+    }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
       if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
         SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
-    }
-    for (uint32_t i = 0; i < np; ++i) {
-      const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg32)
-        SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
@@ -136,10 +139,8 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepGeneric) {
-        SweepPass(b, p, lanes);
-        generic++;
-      }
+      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg32)
+        SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
     }
     if (next <= pool.size()) break;
     if (attempt == 2) return -7;
