@@ -593,6 +593,24 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
   s.flush_acc();
 }
 
+// Sweep of pass p through the generic sweep.  Row entries a register attempt
+// may have written are cleared first.
+SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
+  const PassGeom g = b.geom[p];
+  const int nrows = g.row1 - g.row0;
+  if (g.n_edges <= 0 || nrows <= 0) {
+    EmptyPass(b, p, lanes);
+    return;
+  }
+  uint2* rows = b.rowspan + b.sweep[p].rbase;
+  for (int r = lanes.lane; r < nrows; r += Lanes::n) rows[r] = make_uint2(0, 0);
+  lanes.sync();
+  PoolSink sink;
+  InitPoolSink(b, p, g, &sink);
+  RunSweep(b, p, g, &sink, lanes);
+  FinishPass(b, p, &sink, lanes);
+}
+
 template <int M>
 SKC_HD uint64_t RegSmemBytes(int32_t diff_cap) {
   return sizeof(RegSharedT<M>) + 4ull * (uint64_t)diff_cap;
@@ -644,8 +662,6 @@ SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
                                   : kSweepGeneric;
 }
 
-SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes);
-
 // Sweep of pass p through the register form of size M; should its active
 // list outgrow M after all, the same warp sweeps the pass again with the
 // generic form (which clears the rows the attempt wrote).
@@ -667,23 +683,6 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
   FinishPass(b, p, &sink, lanes);
 }
 
-// Sweep of pass p through the generic sweep.  Row entries a register attempt
-// may have written are cleared first.
-SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
-  const PassGeom g = b.geom[p];
-  const int nrows = g.row1 - g.row0;
-  if (g.n_edges <= 0 || nrows <= 0) {
-    EmptyPass(b, p, lanes);
-    return;
-  }
-  uint2* rows = b.rowspan + b.sweep[p].rbase;
-  for (int r = lanes.lane; r < nrows; r += Lanes::n) rows[r] = make_uint2(0, 0);
-  lanes.sync();
-  PoolSink sink;
-  InitPoolSink(b, p, g, &sink);
-  RunSweep(b, p, g, &sink, lanes);
-  FinishPass(b, p, &sink, lanes);
-}
 
 
 // ---------------------------------------------------------------------------
