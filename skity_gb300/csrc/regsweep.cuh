@@ -140,21 +140,96 @@ SKC_HD void AccFlushIfNeed(const Lanes& L, AccState& a, Sink* sink, int row) {
   a.y = row;
 }
 
-// The intervals [0, K) of a step, then (trailing_a >= 0) the interval left
-// open by the last left edge: blit_trapezoid_row for each, in two passes.
-// First one lane per interval does the row's set-up and counts its spans;
-// then the step's spans, numbered in interval order, are spread over the
-// lanes (span g on lane g mod 32), so a long partial row does not hold one
-// lane while the others wait.  Direct spans are written in that order, the
-// others go to the row accumulator.
+// Trapezoid rows of a row's steps waiting for their spans: the set-ups of
+// intervals [0, n) in the shared interval block, `total` spans, canvas row y.
+struct BlitPending {
+  int n, total, y;
+};
+
+// The spans of the pending intervals, numbered in interval order, spread
+// over the lanes (span g on lane g mod 32), so a long partial row does not
+// hold one lane while the others wait.  Direct spans are written in that
+// order, the others go to the row accumulator.
 template <int M, typename Sink>
-SKC_HD void RegBlit(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as, const Edge* W,
-                    int n, int y, Fixed next_y, int K, int m, int k, uint8_t full,
-                    Fixed left_clip, Fixed right_clip, int trailing_a, bool trailing_nr) {
+SKC_HD void RegBlitFlush(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as,
+                         BlitPending& pend) {
+  constexpr int NL = Lanes::n;
+  if (pend.n == 0) return;
+  sink->row_begin(L, pend.y);
+  if (L.leader()) sh.u.b.iv_start[pend.n] = pend.total;
+  L.sync();
+  const int T = pend.total;
+  const int y = pend.y;
+  uint32_t run = 0;
+  unsigned long long frags = 0;
+  int lo = 0x7fffffff, hi = -1;
+  int iv = 0;
+  for (int gb = 0; gb < T; gb += NL) {
+    const int g = gb + L.lane;
+    bool kept = false;
+    uint2 v = make_uint2(0, 0);
+    if (g < T) {
+      while (sh.u.b.iv_start[iv + 1] <= g) ++iv;
+      const TrapRow t = sh.u.b.iv.get(iv);
+      int x = 0, len = 0;
+      uint8_t a = 0;
+      TrapSpan(t, g - sh.u.b.iv_start[iv], x, len, a);
+      if (t.real) {
+        if (sink->keep(x, y, len, a)) {
+          kept = true;
+          v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+          frags += (unsigned)len;
+        }
+      } else {
+        int o0 = x - as.left, o1 = o0 + len;
+        o0 = max_(o0, 0);
+        o1 = min_(o1, as.width);
+        if (o0 < o1) {
+          lo = min_(lo, o0);
+          hi = max_(hi, o1);
+          if (a != 0) {
+            AtomicAddI32(&as.diff[o0], (int32_t)a);
+            AtomicAddI32(&as.diff[o1], -(int32_t)a);
+          }
+        }
+      }
+    }
+    const unsigned km = L.ballot(kept);
+    const uint32_t cnt = (uint32_t)Lanes::popc(km);
+    if (cnt) {
+      const uint64_t at = sink->reserve(L, run, cnt);
+      uint2* dst = sink->span_ptr(at + run + (uint32_t)Lanes::popc(km & L.lt_mask()));
+      if (kept && dst) *dst = v;
+      run += cnt;
+    }
+  }
+  // the fragment count and the accumulator's touched range stay per lane
+  // (summed at the pass's end, reduced at the row's flush)
+  as.lo = min_(as.lo, lo);
+  as.hi = max_(as.hi, hi);
+  sink->commit(L, run, frags);
+  pend.n = 0;
+  pend.total = 0;
+  L.sync();
+}
+
+// The intervals [0, K) of a step, then (trailing_a >= 0) the interval left
+// open by the last left edge: blit_trapezoid_row for each.  One lane per
+// interval does the row's set-up and counts its spans; the set-ups wait in
+// the interval block, with those of the row's earlier steps, until the row
+// ends or the block is full (a row's partial steps all go to the
+// accumulator, whose sums do not depend on order; a full step is the only
+// step of its row), and their spans are then made in one pass.
+template <int M, typename Sink>
+SKC_HD void RegBlit(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as,
+                    BlitPending& pend, const Edge* W, int n, int y, Fixed next_y, int K, int m,
+                    int k, uint8_t full, Fixed left_clip, Fixed right_clip, int trailing_a,
+                    bool trailing_nr) {
   constexpr int NL = Lanes::n;
   const int total = K + (trailing_a >= 0 ? 1 : 0);
+  if (pend.n > 0 && (pend.y != y || pend.n + total > RegSharedT<M>::kIntervals))
+    RegBlitFlush(L, sh, sink, as, pend);
   AccFlushIfNeed(L, as, sink, y);
-  sink->row_begin(L, y);
   int carry = 0;
   for (int kb = 0; kb < total; kb += NL) {
     const int ki = kb + L.lane;
@@ -211,64 +286,16 @@ SKC_HD void RegBlit(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState& as,
       TrapRow t;
       if (TrapPrepare(t, ul, ur, ll, lr, lDY, rDY, full, nr)) {
         cnt = TrapCount(t);
-        sh.u.b.iv.put(ki, t);
+        sh.u.b.iv.put(pend.n + ki, t);
       }
     }
     const int32_t incl = LaneScanIncl(L, cnt);
-    if (ki < total) sh.u.b.iv_start[ki] = carry + incl - cnt;
+    if (ki < total) sh.u.b.iv_start[pend.n + ki] = pend.total + carry + incl - cnt;
     carry += LaneBcast(L, incl, NL - 1);
   }
-  if (L.leader()) sh.u.b.iv_start[total] = carry;
-  L.sync();
-  const int T = carry;
-  uint32_t run = 0;
-  unsigned long long frags = 0;
-  int lo = 0x7fffffff, hi = -1;
-  int iv = 0;
-  for (int gb = 0; gb < T; gb += NL) {
-    const int g = gb + L.lane;
-    bool kept = false;
-    uint2 v = make_uint2(0, 0);
-    if (g < T) {
-      while (sh.u.b.iv_start[iv + 1] <= g) ++iv;
-      const TrapRow t = sh.u.b.iv.get(iv);
-      int x = 0, len = 0;
-      uint8_t a = 0;
-      TrapSpan(t, g - sh.u.b.iv_start[iv], x, len, a);
-      if (t.real) {
-        if (sink->keep(x, y, len, a)) {
-          kept = true;
-          v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
-          frags += (unsigned)len;
-        }
-      } else {
-        int o0 = x - as.left, o1 = o0 + len;
-        o0 = max_(o0, 0);
-        o1 = min_(o1, as.width);
-        if (o0 < o1) {
-          lo = min_(lo, o0);
-          hi = max_(hi, o1);
-          if (a != 0) {
-            AtomicAddI32(&as.diff[o0], (int32_t)a);
-            AtomicAddI32(&as.diff[o1], -(int32_t)a);
-          }
-        }
-      }
-    }
-    const unsigned km = L.ballot(kept);
-    const uint32_t cnt = (uint32_t)Lanes::popc(km);
-    if (cnt) {
-      const uint64_t at = sink->reserve(L, run, cnt);
-      uint2* dst = sink->span_ptr(at + run + (uint32_t)Lanes::popc(km & L.lt_mask()));
-      if (kept && dst) *dst = v;
-      run += cnt;
-    }
-  }
-  // the fragment count and the accumulator's touched range stay per lane
-  // (summed at the pass's end, reduced at the row's flush)
-  as.lo = min_(as.lo, lo);
-  as.hi = max_(as.hi, hi);
-  sink->commit(L, run, frags);
+  pend.y = y;
+  pend.n += total;
+  pend.total += carry;
   L.sync();
 }
 
@@ -284,6 +311,9 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
   const int winding_mask = even_odd ? 1 : -1;
   int32_t r_idx[S], r_x[S], r_dx[S], r_dy[S], r_low[S], r_wc[S];
 
+  BlitPending pend;
+  pend.n = pend.total = 0;
+  pend.y = kNaN32;
   Fixed y = max_(W[0].upper_y, IntToFixed(start_y));
   // initial activation: the edges with upper_y <= y, in their sorted order
   int k = 0;
@@ -520,7 +550,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
     // ---- B: coverage of the step's intervals, in list order
     const int row = y >> 16;
     if (nr + (final_in ? 1 : 0) > 0 && !(row < scan_top)) {
-      RegBlit(L, sh, sink, as, W, n, row, next_y, nr, m, k, full, left_clip, right_clip,
+      RegBlit(L, sh, sink, as, pend, W, n, row, next_y, nr, m, k, full, left_clip, right_clip,
               trailing_a, trailing_nr);
     }
 
@@ -641,6 +671,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
     }
     if (k < n && W[k].upper_y > y) nny = min_(nny, W[k].upper_y);
   }
+  RegBlitFlush(L, sh, sink, as, pend);
   return 1;
 }
 
