@@ -56,10 +56,6 @@ __device__ __forceinline__ uint32_t SweepPassAt(const DevBatch& b, uint32_t i) {
   return b.sweep_order ? b.sweep_order[i] : i;
 }
 
-// Minimum resident blocks per SM asked of the compiler for the form of size
-// M (a register budget: fewer registers per thread, more warps per SM).
-__host__ __device__ constexpr int RegMinBlocks(int M) { return M <= 32 ? 10 : 1; }
-
 // Lets the next overlapped launch start once every CTA of this one runs.
 __device__ __forceinline__ void AllowNextLaunch() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -80,14 +76,14 @@ __device__ __forceinline__ void FinishOverlapped(unsigned int* done) {
 }
 
 template <int M, int kForm>
-__global__ void __launch_bounds__(32 * kRegWarps, RegMinBlocks(M)) k_sweep_reg(DevBatch b) {
+__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   AllowNextLaunch();
   const int w = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * kRegWarps + w;
   if (i < b.n_passes) {
     const uint32_t p = SweepPassAt(b, i);
-    if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kForm) {
+    if (SweepForm(b.geom[p], b.pass_class[p]) == kForm) {
       if (DynamicSmemBytes() < kRegWarps * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
         FlagError(b.err, 16);
       } else {
@@ -109,7 +105,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
     const uint32_t p = SweepPassAt(b, i);
     Lanes L;
     L.lane = threadIdx.x & 31;
-    if (SweepForm(b.geom[p].max_active, b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
+    if (SweepForm(b.geom[p], b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
   }
   FinishOverlapped(b.sweep_done ? b.sweep_done + kSweepGeneric : nullptr);
 }

@@ -654,12 +654,16 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
 // The forms' kernels take disjoint passes and depend on nothing the others
 // write, so their launches may overlap.
 enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1, kSweepReg32 = 3 };
-SKC_HD int SweepForm(int max_active, uint8_t pass_class) {
+// The 32-edge form runs last (lightest form) and takes only short passes,
+// so that no long sweep starts at the end of the sweep launches.
+constexpr int kReg32MaxRows = 640;
+SKC_HD int SweepForm(const PassGeom& g, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
-  return max_active <= 32   ? kSweepReg32
-         : max_active <= 64 ? kSweepReg64
-         : max_active <= kRegMaxM ? kSweepReg128
-                                  : kSweepGeneric;
+  const int ma = g.max_active;
+  return (ma <= 32 && g.row1 - g.row0 <= kReg32MaxRows) ? kSweepReg32
+         : ma <= 64                                     ? kSweepReg64
+         : ma <= kRegMaxM                               ? kSweepReg128
+                                                        : kSweepGeneric;
 }
 
 // Sweep of pass p through the register form of size M; should its active

@@ -122,24 +122,24 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     // in the sweep order
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepGeneric) {
+      if (SweepForm(geom[p], pclass[p]) == kSweepGeneric) {
         SweepPass(b, p, lanes);
         generic++;
       }
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg128)
+      if (SweepForm(geom[p], pclass[p]) == kSweepReg128)
         SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg64)
+      if (SweepForm(geom[p], pclass[p]) == kSweepReg64)
         SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
-      if (SweepForm(geom[p].max_active, pclass[p]) == kSweepReg32)
+      if (SweepForm(geom[p], pclass[p]) == kSweepReg32)
         SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
     }
     if (next <= pool.size()) break;
