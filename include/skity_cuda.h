@@ -145,9 +145,9 @@ typedef struct skity_cuda_stats {
  * per workload by timing batch renders. */
 typedef struct skity_cuda_raster_config {
   uint32_t struct_size;   /* sizeof(skity_cuda_raster_config) */
-  uint32_t tile_width;    /* compositor row tile in pixels: 32..2048 (default 512) */
+  uint32_t tile_width;    /* compositor row tile in pixels: 32..2048 (default 1024) */
   uint32_t ctas_per_sm;   /* persistent compositor CTAs per SM, 0: one warp per
-                             tile, no work queue (default 4) */
+                             tile, no work queue (default 6) */
   uint32_t band_rows;     /* rows per pass-bin band: 8, 16, 32 or 64 (default 16) */
 } skity_cuda_raster_config;
 

@@ -46,8 +46,8 @@ struct Context;
 // Launch shape of the compositor and the granularity of its pass bins
 // (skity_cuda_raster_config; chosen per batch, e.g. by the autotuner).
 struct RasterConfig {
-  uint32_t tile_w = 512;     // row-tile width in pixels
-  uint32_t ctas_per_sm = 4;  // persistent compositor CTAs per SM (0: one warp per tile)
+  uint32_t tile_w = 1024;    // row-tile width in pixels
+  uint32_t ctas_per_sm = 6;  // persistent compositor CTAs per SM (0: one warp per tile)
   int32_t band_shift = 4;    // pass-bin bands of 1 << band_shift rows
 };
 

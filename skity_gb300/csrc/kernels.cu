@@ -163,6 +163,9 @@ int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
 // blends stay in the reference's order).
 // ---------------------------------------------------------------------------
 constexpr int kCompWarps = 4;
+// CTAs per SM the compositor's register budget leaves room for (its stalls
+// are mostly dependent integer chains: more resident warps hide them)
+constexpr int kCompMinBlocks = 6;
 // spans up to this many tile pixels are shaded by one lane
 constexpr int kShortSpan = 4;
 
@@ -179,7 +182,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
 
 // counter == null: warp w of block k takes tile 4k + w; otherwise every warp
 // takes tiles from the counter until none is left (persistent grid).
-__global__ void __launch_bounds__(32 * kCompWarps, 4)
+__global__ void __launch_bounds__(32 * kCompWarps, kCompMinBlocks)
     k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk,
                 unsigned int* counter) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
