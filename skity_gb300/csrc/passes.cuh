@@ -656,7 +656,7 @@ SKC_HD int RunRegSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s
 enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1, kSweepReg32 = 3 };
 // The 32-edge form runs last (lightest form) and takes only short passes,
 // so that no long sweep starts at the end of the sweep launches.
-constexpr int kReg32MaxRows = 640;
+constexpr int kReg32MaxRows = 1100;
 SKC_HD int SweepForm(const PassGeom& g, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
   const int ma = g.max_active;
