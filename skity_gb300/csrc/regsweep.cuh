@@ -454,7 +454,8 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
       }
       m2 = before;
     }
-    if (L.ballot(inv)) {
+    const bool any_inv = L.ballot(inv) != 0;
+    if (any_inv) {
       // Some survivor moved left of an earlier one.  The reference ripples
       // each such edge backwards (backward_insert_edge_based_on_x), which
       // leaves the survivors stably sorted by new x; its crossing check then
@@ -554,36 +555,37 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
               trailing_a, trailing_nr);
     }
 
-    // ---- reorder the survivors into the new list
+    // ---- reorder the survivors into the new list (nothing moves when every
+    // edge survives in order: the rank of position p is then p)
+    if (m2 != m || any_inv) {
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const int p = s * NL + L.lane;
-      if (s < ns && ((smask[s] >> (NL == 32 ? L.lane : 0)) & 1u)) {
-        const int r = r_rank[s];
-        sh.p_idx[r] = r_idx[s];
-        sh.p_x[r] = r_x[s];
-        sh.p_dx[r] = r_dx[s];
-        sh.p_dy[r] = r_dy[s];
-        sh.p_low[r] = r_low[s];
-        sh.p_wc[r] = r_wc[s];
+      for (int s = 0; s < S; ++s) {
+        if (s < ns && ((smask[s] >> (NL == 32 ? L.lane : 0)) & 1u)) {
+          const int r = r_rank[s];
+          sh.p_idx[r] = r_idx[s];
+          sh.p_x[r] = r_x[s];
+          sh.p_dx[r] = r_dx[s];
+          sh.p_dy[r] = r_dy[s];
+          sh.p_low[r] = r_low[s];
+          sh.p_wc[r] = r_wc[s];
+        }
       }
-      (void)p;
+      L.sync();
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = s * NL + L.lane;
+        if (p < m2) {
+          r_idx[s] = sh.p_idx[p];
+          r_x[s] = sh.p_x[p];
+          r_dx[s] = sh.p_dx[p];
+          r_dy[s] = sh.p_dy[p];
+          r_low[s] = sh.p_low[p];
+          r_wc[s] = sh.p_wc[p];
+        }
+      }
+      L.sync();
     }
-    L.sync();
     m = m2;
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const int p = s * NL + L.lane;
-      if (p < m) {
-        r_idx[s] = sh.p_idx[p];
-        r_x[s] = sh.p_x[p];
-        r_dx[s] = sh.p_dx[p];
-        r_dy[s] = sh.p_dy[p];
-        r_low[s] = sh.p_low[p];
-        r_wc[s] = sh.p_wc[p];
-      }
-    }
-    L.sync();
     y = next_y;
     if (y >= IntToFixed(stop_y)) break;
 
