@@ -11,6 +11,11 @@
 #include <stdint.h>
 #include <vector_types.h>  // float4 / uint2 on host builds too
 
+// branch hints: SKC_COLD(c) for conditions that are rarely true on the hot
+// path (keeps their blocks out of the straight-line code), SKC_LIKELY(c)
+#define SKC_COLD(c) __builtin_expect(!!(c), 0)
+#define SKC_LIKELY(c) __builtin_expect(!!(c), 1)
+
 #ifdef __CUDACC__
 #define SKC_HD __host__ __device__ __forceinline__
 #define SKC_HDN inline __host__ __device__ __noinline__

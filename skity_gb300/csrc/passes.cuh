@@ -243,7 +243,7 @@ struct PoolSink : SinkBase {
   // Room for `add` more spans after the `written` spans this step already
   // put at cur; returns cur (the row may have moved to a new chunk).
   SKC_HD uint64_t reserve(const Lanes& L, uint32_t written, uint32_t add) {
-    if (cur + written + add <= chunk_end) return cur;
+    if (SKC_LIKELY(cur + written + add <= chunk_end)) return cur;
     const uint64_t have = cur + written - row_start;
     if (have + add > chunk) {  // a row larger than a chunk (not expected)
       FlagError(err, 8);
@@ -305,7 +305,7 @@ struct PoolSink : SinkBase {
       if (!L.ballot(cnt != 0)) continue;
       const int32_t incl = LaneScanIncl(L, cnt);
       const int total = LaneBcast(L, incl, Lanes::n - 1);
-      if (ne + total > ev_cap) return false;
+      if (SKC_COLD(ne + total > ev_cap)) return false;
       int at = ne + incl - cnt;
 #pragma unroll
       for (int j = 0; j < V; ++j) {

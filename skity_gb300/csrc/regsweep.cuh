@@ -122,7 +122,7 @@ SKC_HD void AccFlush(const Lanes& L, AccState& a, Sink* sink) {
   if (a.lo <= a.hi) {
     const bool read = sink->acc_row(L, a.y, a.diff, a.left, a.lo, a.hi, a.ev, a.ev_cap);
     L.sync();
-    if (read) {
+    if (SKC_LIKELY(read)) {
       if (L.leader()) a.diff[a.hi] = 0;
     } else {
       for (int i = a.lo + L.lane; i <= a.hi; i += Lanes::n) a.diff[i] = 0;
@@ -386,7 +386,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           const int32_t xo = r_x[s], dxo = r_dx[s], dyo = r_dy[s];
           int32_t x = wadd(xo, dxo >> y_shift);  // GoYShift
           const int32_t xg = x;
-          if (r_low[s] <= next_y && WcCount(r_wc[s]) > 0) {
+          if (SKC_COLD(r_low[s] <= next_y && WcCount(r_wc[s]) > 0)) {
             Edge e = W[r_idx[s]];
             e.x = x;
             e.y = next_y;
@@ -455,7 +455,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
       m2 = before;
     }
     const bool any_inv = L.ballot(inv) != 0;
-    if (any_inv) {
+    if (SKC_COLD(any_inv)) {
       // Some survivor moved left of an earlier one.  The reference ripples
       // each such edge backwards (backward_insert_edge_based_on_x), which
       // leaves the survivors stably sorted by new x; its crossing check then
@@ -520,7 +520,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
     // survivor before it)
     int trailing_a = -1;
     bool trailing_nr = false;
-    if (final_in) {
+    if (SKC_COLD(final_in)) {
       const int a = sh.ia[nr];
       const bool a_surv = sh.surv[a] != 0;
       const int32_t xa = sh.xf[a];
@@ -557,7 +557,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
 
     // ---- reorder the survivors into the new list (nothing moves when every
     // edge survives in order: the rank of position p is then p)
-    if (m2 != m || any_inv) {
+    if (SKC_COLD(m2 != m || any_inv)) {
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         if (s < ns && ((smask[s] >> (NL == 32 ? L.lane : 0)) & 1u)) {
@@ -590,7 +590,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
     if (y >= IntToFixed(stop_y)) break;
 
     // ---- D: insert_new_edges (sw_raster.cc:207-247) as a merge
-    if (k < n && W[k].upper_y <= y) {
+    if (SKC_COLD(k < n && W[k].upper_y <= y)) {
       int c = 0;
       for (int base = k; base < n; base += NL) {
         const int i = base + L.lane;
@@ -598,7 +598,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
         c += Lanes::popc(mask);
         if (mask != kFull) break;
       }
-      if (m + c > M) return 0;
+      if (SKC_COLD(m + c > M)) return 0;
       const int32_t x0 = W[k].x;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
