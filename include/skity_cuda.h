@@ -186,6 +186,16 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
 SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas);
 SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas);
 SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy);
+/* Canvas::ClipRect(rect, ClipOp::kIntersect) (canvas.hpp; canvas.cc:130-135,
+ * 463-476): the rect, mapped by the current translation, narrows the
+ * canvas's global clip bounds (kept and restored by Save / Restore); later
+ * DrawPath calls rasterise only inside them, as SWCanvas does for a
+ * scale/translate matrix (sw_canvas.cc:279-295).  Clear is not clipped
+ * (SWCanvas::OnDrawPaint rasterises the whole canvas).  kDifference and
+ * ClipPath are not taken by this canvas; a blurred draw under a clip
+ * returns SKITY_CUDA_ERROR_NOT_SUPPORTED. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
+                                                   float right, float bottom);
 /* Canvas::Flush: renders the recorded draws on the GPU and writes the
  * bitmap's pixels. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas);

@@ -53,6 +53,7 @@ struct Scene {
   std::vector<PaintRec> paints;
   std::vector<GradRec> grads;
   std::vector<float> stop_colors, stop_offsets;
+  std::vector<float> clips;  // per draw device-space (l, t, r, b), when present
 };
 
 template <typename T>
@@ -75,6 +76,7 @@ bool Load(const char* path, Scene* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
+  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds follow the stops
   size_t o = 32;
   std::memcpy(s->clear, buf.data() + o, 16);
   o += 16;
@@ -93,6 +95,7 @@ bool Load(const char* path, Scene* s) {
   Take(buf, o, s->grads, cnt[4]);
   Take(buf, o, s->stop_colors, 4 * size_t(cnt[5]));
   Take(buf, o, s->stop_offsets, cnt[5]);
+  if (flags & 1) Take(buf, o, s->clips, 4 * size_t(nd));
   return o <= buf.size();
 }
 
@@ -199,12 +202,16 @@ int main(int argc, char** argv) {
   for (size_t i = 0; i < paths.size(); ++i) {
     const PaintRec& pr = s.paints[first + i];
     const bool moved = pr.translate[0] != 0.f || pr.translate[1] != 0.f;
-    if (moved) {
-      canvas->Save();
-      canvas->Translate(pr.translate[0], pr.translate[1]);
-    }
+    const float* c = s.clips.empty() ? nullptr : s.clips.data() + 4 * (first + i);
+    const bool clipped =
+        c && !(c[0] == -1e9f && c[1] == -1e9f && c[2] == 1e9f && c[3] == 1e9f);
+    if (moved || clipped) canvas->Save();
+    // the stored clip is already in device space: ClipRect before the
+    // translation leaves exactly these global clip bounds
+    if (clipped) canvas->ClipRect(skity::Rect::MakeLTRB(c[0], c[1], c[2], c[3]));
+    if (moved) canvas->Translate(pr.translate[0], pr.translate[1]);
     canvas->DrawPath(paths[i], paints[i]);
-    if (moved) canvas->Restore();
+    if (moved || clipped) canvas->Restore();
   }
   canvas->Flush();
   auto t1 = std::chrono::steady_clock::now();

@@ -1153,8 +1153,15 @@ struct RasterStats {
   uint64_t edges = 0, tie_groups = 0;
 };
 
+// The canvas's global clip bounds in device space (Canvas::
+// global_clip_bounds_stack_, canvas.cc:19-22,463-476): kMaxCullRect
+// (include/skity/render/canvas.hpp:26) unless a ClipRect narrowed them.
+struct Clip {
+  float l = -1e9f, t = -1e9f, r = 1e9f, b = 1e9f;
+};
+
 static void RastePathQuads(const Path& quad, bool even_odd, std::vector<Span>* spans,
-                           RasterStats* st) {
+                           RasterStats* st, Clip clip = Clip()) {
   spans->clear();
   // bounds of the (identity-)transformed quad path (path.cc:1341-1360)
   size_t npts = quad.pts.size();
@@ -1168,9 +1175,10 @@ static void RastePathQuads(const Path& quad, bool even_odd, std::vector<Span>* s
     b = std::max(b, quad.pts[i].y);
   }
   float bl = std::floor(l), bt = std::floor(t), br = std::ceil(r), bb = std::ceil(b);
-  // scan_bounds = bounds n kMaxCullRect (+-1e9); empty intersection -> empty
-  float sl = std::max(l, -1e9f), sr = std::min(r, 1e9f);
-  float stp = std::max(t, -1e9f), sbm = std::min(b, 1e9f);
+  // scan_bounds.Intersect(clip_bounds) (sw_raster.cc:746-748, rect.cc:160-172);
+  // an empty intersection leaves nothing to scan
+  float sl = std::max(l, clip.l), sr = std::min(r, clip.r);
+  float stp = std::max(t, clip.t), sbm = std::min(b, clip.b);
   if (!(sl < sr && stp < sbm)) return;
   sl = std::floor(sl);
   stp = std::floor(stp);
@@ -1545,7 +1553,19 @@ struct SceneView {
   const PaintRec* paints;
   const GradRec* grads;
   const float *stop_colors, *stop_offsets;
+  const float* clips;  // per draw (l, t, r, b) when the stream has the clip section
 };
+
+static Clip ClipOf(const SceneView& s, uint32_t d) {
+  Clip c;
+  if (s.clips) {
+    c.l = s.clips[4 * (size_t)d];
+    c.t = s.clips[4 * (size_t)d + 1];
+    c.r = s.clips[4 * (size_t)d + 2];
+    c.b = s.clips[4 * (size_t)d + 3];
+  }
+  return c;
+}
 
 static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   if (len < 72 || std::memcmp(buf, "SKSC", 4) != 0) return false;
@@ -1555,6 +1575,8 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
+  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds follow the stops
+  if (flags & ~1u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -1578,7 +1600,20 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->grads = (const GradRec*)at(sizeof(GradRec) * cnt[4]);
   s->stop_colors = (const float*)at(16 * (size_t)cnt[5]);
   s->stop_offsets = (const float*)at(4 * (size_t)cnt[5]);
+  s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
   return o <= len;
+}
+
+// A blurred draw under a narrowed clip: the blur's temp canvas and its
+// image draw under a clip are not restated here (the GPU path refuses the
+// same draws).
+static bool BlurUnderClip(const SceneView& s) {
+  for (uint32_t d = 0; d < s.nd && s.clips; ++d) {
+    const Clip c = ClipOf(s, d);
+    const bool narrowed = !(c.l == -1e9f && c.t == -1e9f && c.r == 1e9f && c.b == 1e9f);
+    if (narrowed && s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f) return true;
+  }
+  return false;
 }
 
 static Path BuildPath(const SceneView& s, uint32_t d) {
@@ -1638,10 +1673,11 @@ static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
   bool need_fill = paint.style != 1;
   bool need_stroke = paint.style != 0;
   RasterStats rs;
+  const Clip clip = ClipOf(s, d);
   auto draw_fill = [&]() {
     Path quad;
     QuadPath(path, &quad);
-    RastePathQuads(quad, even_odd, spans, &rs);
+    RastePathQuads(quad, even_odd, spans, &rs, clip);
     Brush br = MakeBrush(s, paint, false);
     st->fragments += BrushSpans(*spans, br, (int)paint.blend, t);
     st->spans += spans->size();
@@ -1654,7 +1690,7 @@ static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
     // RastePath reads the fill type of the path it is given: the stroke
     // outline is a fresh Path (kWinding), whatever the source's fill type
     // (sw_canvas.cc:388-407, sw_raster.cc:783-784)
-    RastePathQuads(quad2, false, spans, &rs);
+    RastePathQuads(quad2, false, spans, &rs, clip);
     Brush br = MakeBrush(s, paint, true);
     st->fragments += BrushSpans(*spans, br, (int)paint.blend, t);
     st->spans += spans->size();
@@ -1687,6 +1723,7 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
   using namespace sko;
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
+  if (BlurUnderClip(s)) return -3;
   Target t{out_rgba, (int)s.width, (int)s.height};
   auto t0 = std::chrono::steady_clock::now();
   if (s.has_clear) {
@@ -1707,7 +1744,7 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
     } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
       // Canvas::Translate then DrawPath: the CTM reaches RastePath and the brush
       DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
-                         s.paints[d].translate[1], &t, &st);
+                         s.paints[d].translate[1], ClipOf(s, d), &t, &st);
     } else {
       DrawPath(s, d, &t, &st, &spans);
     }
@@ -1733,6 +1770,7 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
   using namespace sko;
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
+  if (BlurUnderClip(s)) return -3;
   if (threads == 0) threads = 1;
   auto t0 = std::chrono::steady_clock::now();
   uint32_t last = std::min<uint32_t>(s.nd, first + count);
@@ -1753,7 +1791,7 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
           HandleBlurFilter(s, d, &t, &st[k]);
         } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
           DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
-                             s.paints[d].translate[1], &t, &st[k]);
+                             s.paints[d].translate[1], ClipOf(s, d), &t, &st[k]);
         } else {
           DrawPath(s, d, &t, &st[k], &spans);
         }
@@ -1818,7 +1856,7 @@ int sko_path_spans(const uint8_t* scene, size_t len, uint32_t draw, int32_t* out
   Path quad;
   QuadPath(path, &quad);
   std::vector<Span> spans;
-  RastePathQuads(quad, s.paints[draw].fill_type == 1, &spans, nullptr);
+  RastePathQuads(quad, s.paints[draw].fill_type == 1, &spans, nullptr, ClipOf(s, draw));
   uint32_t n = (uint32_t)spans.size();
   for (uint32_t i = 0; i < n && i < cap; ++i) {
     out[4 * i] = spans[i].x;

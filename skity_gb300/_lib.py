@@ -105,6 +105,8 @@ SIGNATURES = {
     "skity_cuda_canvas_save": (ctypes.c_int32, [_vp]),
     "skity_cuda_canvas_restore": (ctypes.c_int32, [_vp]),
     "skity_cuda_canvas_translate": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
+    "skity_cuda_canvas_clip_rect": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
+                                                     ctypes.c_float, ctypes.c_float]),
     "skity_cuda_render_streams": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
                                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),

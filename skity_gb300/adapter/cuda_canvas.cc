@@ -16,8 +16,6 @@ CUDACanvas::CUDACanvas(skity_cuda_canvas canvas, Bitmap* bitmap)
 
 CUDACanvas::~CUDACanvas() { skity_cuda_canvas_destroy(canvas_); }
 
-void CUDACanvas::OnClipPath(Path const&, ClipOp) { status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED; }
-
 // The canvas matrix as a translation, or false when it is anything else.
 static bool TranslationOf(const Matrix& m, float* tx, float* ty) {
   for (int c = 0; c < 4; ++c)
@@ -28,9 +26,32 @@ static bool TranslationOf(const Matrix& m, float* tx, float* ty) {
   return true;
 }
 
+// Canvas::ClipRect has already narrowed the global clip bounds
+// (canvas.cc:130-135,463-476); for kIntersect under a translation that is
+// all SWCanvas does too (sw_canvas.cc:279-295).  Other clips are refused.
+void CUDACanvas::OnClipRect(Rect const&, ClipOp op) {
+  float tx = 0.f, ty = 0.f;
+  if (op != ClipOp::kIntersect || !TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+    bad_clip_.back() = true;
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  status_ = SKITY_CUDA_SUCCESS;
+}
+
+void CUDACanvas::OnClipRRect(RRect const&, ClipOp) {
+  bad_clip_.back() = true;
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
+void CUDACanvas::OnClipPath(Path const&, ClipOp) {
+  bad_clip_.back() = true;
+  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+}
+
 void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
   float tx = 0.f, ty = 0.f;
-  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+  if (bad_clip_.back() || !TranslationOf(GetTotalMatrix(), &tx, &ty)) {
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     return;
   }
@@ -101,13 +122,19 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
     q.blur_style = static_cast<uint32_t>(mf->GetBlurStyle());
     q.blur_radius = mf->GetBlurRadius();
   }
+  // the C-ABI canvas holds no state between draws: each draw carries its
+  // device-space clip bounds (set before the translation, so they stay as
+  // they are) and its translation
+  const Rect& clip = GetGlobalClipBounds();
+  const bool clipped = !(clip.Left() == -1e9f && clip.Top() == -1e9f && clip.Right() == 1e9f &&
+                         clip.Bottom() == 1e9f);
   const bool moved = tx != 0.f || ty != 0.f;
-  if (moved) {
-    skity_cuda_canvas_save(canvas_);
-    skity_cuda_canvas_translate(canvas_, tx, ty);
-  }
+  if (moved || clipped) skity_cuda_canvas_save(canvas_);
+  if (clipped)
+    skity_cuda_canvas_clip_rect(canvas_, clip.Left(), clip.Top(), clip.Right(), clip.Bottom());
+  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
   status_ = skity_cuda_canvas_draw_path(canvas_, &p, &q);
-  if (moved) skity_cuda_canvas_restore(canvas_);
+  if (moved || clipped) skity_cuda_canvas_restore(canvas_);
 }
 
 void CUDACanvas::OnSaveLayer(const Rect&, const Paint&) {

@@ -7,16 +7,21 @@
 // (it needs Skity's public headers) and links against libskity_cuda.so.
 //
 // What differs from the software canvas: pixels are written to the bitmap at
-// Flush(), not during each draw.  Operations outside the GPU raster path --
-// clips, layers, text, images, canvas matrices other than translations, shader local
-// matrices, sweep/conical gradients, blur styles other than kNormal, blend
-// modes other than clear/src/dst/src-over -- draw nothing and leave
-// SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus().
+// Flush(), not during each draw.  ClipRect(kIntersect) under a translation is
+// taken (the global clip bounds the base class keeps bound each draw's scan,
+// as SWCanvas::OnClipRect relies on, sw_canvas.cc:279-295).  Operations
+// outside the GPU raster path -- ClipPath, kDifference clips, layers, text,
+// images, canvas matrices other than translations, shader local matrices,
+// sweep/conical gradients, blur styles other than kNormal, blend modes other
+// than clear/src/dst/src-over -- draw nothing and leave
+// SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus(); draws under a clip this
+// canvas did not take draw nothing either, until the Restore that drops it.
 #ifndef SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP
 #define SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP
 
 #include <memory>
 #include <skity/graphic/bitmap.hpp>
+#include <vector>
 #include <skity/render/canvas.hpp>
 
 #include "../../include/skity_cuda.h"
@@ -33,6 +38,8 @@ class CUDACanvas : public Canvas {
   int32_t LastStatus() const { return status_; }
 
  protected:
+  void OnClipRect(Rect const& rect, ClipOp op) override;
+  void OnClipRRect(RRect const& rrect, ClipOp op) override;
   void OnClipPath(Path const& path, ClipOp op) override;
   void OnDrawPath(Path const& path, Paint const& paint) override;
   void OnSaveLayer(const Rect& bounds, const Paint& paint) override;
@@ -42,8 +49,10 @@ class CUDACanvas : public Canvas {
   void OnDrawGlyphs(uint32_t count, const GlyphID glyphs[], const float position_x[],
                     const float position_y[], const Font& font, const Paint& paint) override;
   void OnDrawPaint(Paint const& paint) override;
-  void OnSave() override {}
-  void OnRestore() override {}
+  void OnSave() override { bad_clip_.push_back(bad_clip_.back()); }
+  void OnRestore() override {
+    if (bad_clip_.size() > 1) bad_clip_.pop_back();
+  }
   void OnRestoreToCount(int) override {}
   void OnFlush() override;
   uint32_t OnGetWidth() const override;
@@ -53,6 +62,8 @@ class CUDACanvas : public Canvas {
   skity_cuda_canvas canvas_;
   Bitmap* bitmap_;
   int32_t status_ = SKITY_CUDA_SUCCESS;
+  // per save level: a clip this canvas does not take is in effect
+  std::vector<bool> bad_clip_{false};
 };
 
 // Same null / empty semantics as MakeSoftwareCanvas: nullptr for a null

@@ -336,6 +336,13 @@ class Canvas:
         _lib.check(self.lib.skity_cuda_canvas_translate(self.handle, float(dx), float(dy)),
                    "skity_cuda_canvas_translate")
 
+    def ClipRect(self, left, top, right, bottom):
+        """Canvas::ClipRect(rect, ClipOp::kIntersect) under the current
+        translation; Save / Restore keep and restore the clip."""
+        _lib.check(self.lib.skity_cuda_canvas_clip_rect(self.handle, float(left), float(top),
+                                                        float(right), float(bottom)),
+                   "skity_cuda_canvas_clip_rect")
+
     def Flush(self):
         _lib.check(self.lib.skity_cuda_canvas_flush(self.handle), "skity_cuda_canvas_flush")
 

@@ -52,6 +52,7 @@ struct StreamView {
   const PaintRec* paints;
   const GradRec* grads;
   const float *stop_colors, *stop_offsets;
+  const float* clips;  // per draw device-space clip bounds (l, t, r, b), or null: none
 };
 
 // A draw the device code can take: the verb sequence of a skity::Path
@@ -110,6 +111,16 @@ inline bool ValidTranslate(const float t[2], const float* pts, uint32_t np) {
   return true;
 }
 
+// Clip bounds: finite floats (the empty rect (0, 0, 0, 0) included).
+inline bool ValidClip(const float c[4]) {
+  return std::isfinite(c[0]) && std::isfinite(c[1]) && std::isfinite(c[2]) && std::isfinite(c[3]);
+}
+// The global clip bounds of a canvas that no ClipRect narrowed
+// (kMaxCullRect, include/skity/render/canvas.hpp:26).
+inline bool IsNoClip(const float c[4]) {
+  return c[0] == -1e9f && c[1] == -1e9f && c[2] == 1e9f && c[3] == 1e9f;
+}
+
 inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   if (!buf || len < 72 || std::memcmp(buf, "SKSC", 4) != 0) return false;
   uint32_t hdr[7];
@@ -118,6 +129,8 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
+  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds follow the stops
+  if (flags & ~1u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -146,6 +159,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->grads = (const GradRec*)at(sizeof(GradRec) * s->ng);
   s->stop_colors = (const float*)at(16 * (size_t)s->ns);
   s->stop_offsets = (const float*)at(4 * (size_t)s->ns);
+  s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
   for (uint32_t d = 0; d < s->nd; ++d) {
@@ -158,6 +172,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
       return false;
     if (!ValidTranslate(pr.translate, s->pts + 2 * (size_t)s->po[d], s->po[d + 1] - s->po[d]))
       return false;
+    if (s->clips && !ValidClip(s->clips + 4 * (size_t)d)) return false;
     if (!ValidPath(s->verbs + s->vo[d], s->vo[d + 1] - s->vo[d], s->pts + 2 * (size_t)s->po[d],
                    s->po[d + 1] - s->po[d], s->wts + s->wo[d], s->wo[d + 1] - s->wo[d]))
       return false;
@@ -363,6 +378,10 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     pd.cap_join = (pr.cap & 0xFF) | ((pr.join & 0xFF) << 8);
     pd.tx = tx;
     pd.ty = ty;
+    if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
+      pd.clipped = 1;
+      std::memcpy(pd.clip, s.clips + 4 * (size_t)d, sizeof pd.clip);
+    }
     pd.stroke_width = pr.stroke_width;
     pd.miter = pr.miter;
     pd.brush = make_brush(stroke);
@@ -409,6 +428,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       continue;
     }
     if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (pr.blur_style != 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
     const float* p = s.pts + 2 * (size_t)s.po[d];

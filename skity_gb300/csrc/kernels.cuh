@@ -22,7 +22,8 @@ struct PassDesc {
   uint32_t brush;       // index into Brush
   uint64_t slice_off;   // byte offset of this pass's geometry scratch
   int32_t cap[13];      // scratch capacities, see SliceLayout
-  int32_t pad;
+  uint32_t clipped;     // 1: clip (device-space LTRB) bounds the scan; 0: kMaxCullRect
+  float clip[4];
 };
 enum : uint32_t { kPassStroke = 1, kPassEvenOdd = 2, kPassSrcOver = 4 };
 

@@ -83,7 +83,9 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
     }
     quad = q2.view();
   }
-  RasterBounds rb = ComputeBounds(quad, pd.tx, pd.ty);
+  RasterBounds rb = pd.clipped
+                        ? ComputeBounds(quad, pd.tx, pd.ty, pd.clip[0], pd.clip[1], pd.clip[2], pd.clip[3])
+                        : ComputeBounds(quad, pd.tx, pd.ty);
   if (rb.empty) {
     b.geom[p] = g;
     return;

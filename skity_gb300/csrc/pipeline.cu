@@ -511,9 +511,15 @@ struct skity_cuda_canvas_s {
   std::vector<skc::PaintRec> paints;
   std::vector<skc::GradRec> grads;
   std::vector<float> stop_colors, stop_offsets;
-  // canvas matrix (a translation) and its save stack
-  float tx = 0.f, ty = 0.f;
-  std::vector<std::pair<float, float>> saved;
+  // canvas matrix (a translation), global clip bounds and their save stack
+  struct State {
+    float tx = 0.f, ty = 0.f;
+    float clip[4] = {-1e9f, -1e9f, 1e9f, 1e9f};  // kMaxCullRect
+  };
+  State st;
+  std::vector<State> saved;
+  std::vector<float> clips;  // per recorded draw: its clip bounds
+  bool any_clip = false;
   skc::DeviceBatch db;
 };
 
@@ -741,6 +747,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
   canvas->grads.clear();
   canvas->stop_colors.clear();
   canvas->stop_offsets.clear();
+  canvas->clips.clear();
+  canvas->any_clip = false;
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -791,11 +799,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   std::memcpy(pr.stroke_color, paint->stroke_color, 16);
   pr.stroke_width = paint->stroke_width;
   pr.miter = paint->miter_limit;
-  pr.translate[0] = canvas->tx;
-  pr.translate[1] = canvas->ty;
+  pr.translate[0] = canvas->st.tx;
+  pr.translate[1] = canvas->st.ty;
   if (!skc::ValidTranslate(pr.translate, path->points, path->point_count))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
-  if ((canvas->tx != 0.f || canvas->ty != 0.f) && paint->blur_style != 0 &&
+  const bool clipped = !skc::IsNoClip(canvas->st.clip);
+  if ((canvas->st.tx != 0.f || canvas->st.ty != 0.f || clipped) && paint->blur_style != 0 &&
       paint->blur_radius > 0.f)
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (paint->shader) {
@@ -826,13 +835,15 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   canvas->po.push_back((uint32_t)(canvas->pts.size() / 2));
   canvas->wo.push_back((uint32_t)canvas->wts.size());
   canvas->paints.push_back(pr);
+  canvas->clips.insert(canvas->clips.end(), canvas->st.clip, canvas->st.clip + 4);
+  canvas->any_clip = canvas->any_clip || clipped;
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
 
 SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
-  canvas->saved.emplace_back(canvas->tx, canvas->ty);
+  canvas->saved.push_back(canvas->st);
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -840,8 +851,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas) {
 SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!canvas->saved.empty()) {
-    canvas->tx = canvas->saved.back().first;
-    canvas->ty = canvas->saved.back().second;
+    canvas->st = canvas->saved.back();
     canvas->saved.pop_back();
   }
   return SKITY_CUDA_SUCCESS;
@@ -852,8 +862,34 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas) {
 SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!std::isfinite(dx) || !std::isfinite(dy)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
-  canvas->tx = canvas->tx + dx;
-  canvas->ty = canvas->ty + dy;
+  canvas->st.tx = canvas->st.tx + dx;
+  canvas->st.ty = canvas->st.ty + dy;
+  return SKITY_CUDA_SUCCESS;
+}
+
+// Canvas::CalculateGlobalClipBounds (canvas.cc:463-476) for kIntersect
+// under a translation: Matrix::MapRect (matrix.cc:306-337) gives the
+// corners x + tx, y + ty, ordered by min/max; Rect::Intersect (rect.cc:
+// 160-172) keeps the overlap, or the bounds become the empty rect.
+SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
+                                                   float right, float bottom) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!std::isfinite(left) || !std::isfinite(top) || !std::isfinite(right) ||
+      !std::isfinite(bottom))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  float* c = canvas->st.clip;
+  const float x0 = left + canvas->st.tx, x1 = right + canvas->st.tx;
+  const float y0 = top + canvas->st.ty, y1 = bottom + canvas->st.ty;
+  const float l = std::max(c[0], std::min(x0, x1)), r = std::min(c[2], std::max(x0, x1));
+  const float t = std::max(c[1], std::min(y0, y1)), b = std::min(c[3], std::max(y0, y1));
+  if (!(l < r && t < b)) {
+    c[0] = c[1] = c[2] = c[3] = 0.f;
+  } else {
+    c[0] = l;
+    c[1] = t;
+    c[2] = r;
+    c[3] = b;
+  }
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -882,6 +918,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   sv.grads = canvas->grads.data();
   sv.stop_colors = canvas->stop_colors.data();
   sv.stop_offsets = canvas->stop_offsets.data();
+  sv.clips = canvas->any_clip ? canvas->clips.data() : nullptr;
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
   int32_t rc = skc::AddStreamCanvas(db.hb, sv);
@@ -916,6 +953,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->grads.clear();
   canvas->stop_colors.clear();
   canvas->stop_offsets.clear();
+  canvas->clips.clear();
+  canvas->any_clip = false;
   canvas->dirty = false;
   return SKITY_CUDA_SUCCESS;
 }

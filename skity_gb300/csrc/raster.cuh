@@ -214,7 +214,11 @@ struct RasterBounds {
   float l, t, r, b;      // floor/ceil of the path bounds (bounds_)
   float sl, st, sr, sb;  // scan bounds
 };
-SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty) {
+// The clip bounds (cl, ct, cr, cb) are the canvas's global clip bounds:
+// kMaxCullRect (+-1e9, include/skity/render/canvas.hpp:26) unless a
+// ClipRect narrowed them.
+SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty, float cl = -1e9f,
+                                  float ct = -1e9f, float cr = 1e9f, float cb = 1e9f) {
   RasterBounds rb;
   rb.empty = true;
   rb.l = rb.t = rb.r = rb.b = rb.sl = rb.st = rb.sr = rb.sb = 0;
@@ -233,7 +237,8 @@ SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty) {
   rb.t = floor_(t);
   rb.r = ceil_(r);
   rb.b = ceil_(b);
-  float sl = max_(l, -1e9f), sr = min_(r, 1e9f), st = max_(t, -1e9f), sb = min_(b, 1e9f);
+  // scan_bounds.Intersect(clip_bounds) (sw_raster.cc:746-748, rect.cc:160-172)
+  float sl = max_(l, cl), sr = min_(r, cr), st = max_(t, ct), sb = min_(b, cb);
   if (!(sl < sr && st < sb)) return rb;
   sl = floor_(sl);
   st = floor_(st);

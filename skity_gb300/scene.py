@@ -13,7 +13,14 @@ the C boundary, see ``include/skity_cuda.h``):
 * per draw: verb/point/weight offsets and one 80-byte paint record mirroring
   ``skity::Paint`` (include/skity/graphic/paint.hpp:46-285);
 * gradient records (``Shader::MakeLinear`` / ``MakeRadial``,
-  src/effect/gradient_shader.cc:96-158) and their colour stops.
+  src/effect/gradient_shader.cc:96-158) and their colour stops;
+* optionally (header flag 1), per draw the canvas clip bounds in device
+  space, float (left, top, right, bottom): ``Canvas::ClipRect`` with
+  ``kIntersect`` under a translation, which the software canvas applies as
+  the global clip bounds that bound the scan (src/render/canvas.cc:463-476,
+  src/render/sw/sw_canvas.cc:279-295); without the section every draw has
+  the canvas's initial bounds ``kMaxCullRect`` (+-1e9,
+  include/skity/render/canvas.hpp:26).
 
 The binary file layout (``Scene.to_bytes``) is read by the CPU oracle, by the
 reference-driver recipe and by the C-ABI batch entry point.
@@ -44,6 +51,8 @@ BLUR_NONE, BLUR_NORMAL = 0, 1
 
 MAGIC = b"SKSC"
 VERSION = 1
+FLAG_CLIPS = 1  # header flags: the per-draw clip section is present
+NO_CLIP = (-1e9, -1e9, 1e9, 1e9)  # kMaxCullRect
 
 # paint record: 20 x 4 bytes: the Paint fields the raster path reads, the
 # path's fill type, and the canvas translation in effect for the draw
@@ -90,6 +99,7 @@ class Scene:
     gradients: np.ndarray = field(default_factory=lambda: np.zeros(0, GRADIENT_DTYPE))
     stop_colors: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.float32))
     stop_offsets: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    clips: np.ndarray | None = None  # (n_draws, 4) float32 LTRB, or None: no clip
 
     @property
     def n_draws(self) -> int:
@@ -97,8 +107,9 @@ class Scene:
 
     def to_bytes(self) -> bytes:
         nd = self.n_draws
+        flags = FLAG_CLIPS if self.clips is not None else 0
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
-                                  1 if self.clear is not None else 0, 0, 0, 0)]
+                                  1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
                               np.float32).tobytes())
         out.append(struct.pack("<6I", nd, len(self.verbs), len(self.points),
@@ -114,13 +125,17 @@ class Scene:
         out.append(np.ascontiguousarray(self.gradients, GRADIENT_DTYPE).tobytes())
         out.append(np.ascontiguousarray(self.stop_colors, np.float32).tobytes())
         out.append(np.ascontiguousarray(self.stop_offsets, np.float32).tobytes())
+        if self.clips is not None:
+            c = np.ascontiguousarray(self.clips, np.float32).reshape(-1, 4)
+            assert len(c) == nd
+            out.append(c.tobytes())
         return b"".join(out)
 
     @staticmethod
     def from_bytes(buf: bytes) -> "Scene":
         if buf[:4] != MAGIC:
             raise ValueError("not a scene stream")
-        ver, w, h, has_clear, _, _, _ = struct.unpack_from("<7I", buf, 4)
+        ver, w, h, has_clear, flags, _, _ = struct.unpack_from("<7I", buf, 4)
         if ver != VERSION:
             raise ValueError(f"scene version {ver}")
         o = 32
@@ -140,8 +155,9 @@ class Scene:
         grads = take(GRADIENT_DTYPE, ng)
         sc = take(np.float32, 4 * ns, (ns, 4))
         so = take(np.float32, ns)
+        clips = take(np.float32, 4 * nd, (nd, 4)) if flags & FLAG_CLIPS else None
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so)
+                     paints, grads, sc, so, clips)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -169,7 +185,26 @@ class Scene:
                      (self.weight_off[first:last + 1] - w0).astype(np.uint32),
                      paints, grads,
                      np.concatenate(sc) if sc else np.zeros((0, 4), np.float32),
-                     np.concatenate(so) if so else np.zeros(0, np.float32))
+                     np.concatenate(so) if so else np.zeros(0, np.float32),
+                     None if self.clips is None else self.clips[first:last].copy())
+
+
+def map_clip(clip, rect, tx=0.0, ty=0.0):
+    """Canvas::ClipRect(rect, kIntersect) under Translate(tx, ty): the
+    global clip bounds after the call (Canvas::CalculateGlobalClipBounds,
+    src/render/canvas.cc:463-476): the rect mapped by the translation
+    (Matrix::MapRect, src/geometry/matrix.cc:306-337 -- corners x + tx,
+    then min/max) intersected with `clip` (Rect::Intersect,
+    src/geometry/rect.cc:160-172), or the empty rect (0, 0, 0, 0)."""
+    f = np.float32
+    xs = (f(rect[0]) + f(tx), f(rect[2]) + f(tx))
+    ys = (f(rect[1]) + f(ty), f(rect[3]) + f(ty))
+    ml, mr, mt, mb = min(xs), max(xs), min(ys), max(ys)
+    l, r = max(f(clip[0]), ml), min(f(clip[2]), mr)
+    t, b = max(f(clip[1]), mt), min(f(clip[3]), mb)
+    if not (l < r and t < b):
+        return (0.0, 0.0, 0.0, 0.0)
+    return (float(l), float(t), float(r), float(b))
 
 
 class SceneBuilder:
@@ -181,6 +216,7 @@ class SceneBuilder:
         self._verbs, self._pts, self._wts = [], [], []
         self._vo, self._po, self._wo = [0], [0], [0]
         self._paints, self._grads, self._sc, self._so = [], [], [], []
+        self._clips = []
         self._nv = self._np = self._nw = 0
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
@@ -198,7 +234,9 @@ class SceneBuilder:
                                    else np.zeros(len(colors)), np.float32))
         return len(self._grads) - 1
 
-    def draw_path(self, verbs, points, paint, weights=()):
+    def draw_path(self, verbs, points, paint, weights=(), clip=None):
+        """`clip`: device-space clip bounds (l, t, r, b) in effect for the
+        draw (see map_clip); None: the canvas's initial bounds."""
         verbs = np.asarray(verbs, np.uint8)
         points = np.asarray(points, np.float32).reshape(-1, 2)
         self._verbs.append(verbs); self._pts.append(points)
@@ -206,6 +244,7 @@ class SceneBuilder:
         self._nv += len(verbs); self._np += len(points); self._nw += len(weights)
         self._vo.append(self._nv); self._po.append(self._np); self._wo.append(self._nw)
         self._paints.append(paint)
+        self._clips.append(NO_CLIP if clip is None else tuple(clip))
 
     def build(self) -> Scene:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
@@ -216,7 +255,9 @@ class SceneBuilder:
                      np.asarray(self._wo, np.uint32),
                      np.array(self._paints, PAINT_DTYPE) if self._paints else np.zeros(0, PAINT_DTYPE),
                      np.array(self._grads, GRADIENT_DTYPE) if self._grads else np.zeros(0, GRADIENT_DTYPE),
-                     cat(self._sc, np.float32, (0, 4)), cat(self._so, np.float32, 0))
+                     cat(self._sc, np.float32, (0, 4)), cat(self._so, np.float32, 0),
+                     (np.array(self._clips, np.float32).reshape(-1, 4)
+                      if any(c != NO_CLIP for c in self._clips) else None))
 
 
 # ---------------------------------------------------------------------------

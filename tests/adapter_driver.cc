@@ -65,6 +65,10 @@ int32_t skity_cuda_canvas_translate(skity_cuda_canvas, float dx, float dy) {
   std::printf("translate %g %g\n", dx, dy);
   return SKITY_CUDA_SUCCESS;
 }
+int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas, float l, float t, float r, float b) {
+  std::printf("clip %g %g %g %g\n", l, t, r, b);
+  return SKITY_CUDA_SUCCESS;
+}
 int32_t skity_cuda_canvas_flush(skity_cuda_canvas) {
   std::printf("flush\n");
   return SKITY_CUDA_SUCCESS;
@@ -117,6 +121,21 @@ int main() {
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
   canvas->Restore();
+  // ClipRect(kIntersect) under a translation: device-space bounds per draw
+  canvas->Save();
+  canvas->Translate(2, 1);
+  canvas->ClipRect(Rect::MakeLTRB(1.5f, 0, 30, 20));
+  canvas->ClipRect(Rect::MakeLTRB(-5, 2, 25, 40));
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Save();
+  canvas->ClipRect(Rect::MakeLTRB(0, 0, 10, 10), Canvas::ClipOp::kDifference);
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Restore();
+  canvas->Restore();
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
   canvas->Flush();
   std::printf("status=%d\n", canvas->LastStatus());
   canvas.reset();

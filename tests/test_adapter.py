@@ -63,4 +63,17 @@ def test_translation_forwarded_other_matrices_refused(driver_output):
     assert driver_output[11].startswith("draw verbs=0,1,2,3,4,5,")
     assert driver_output[12:14] == ["restore", "status=0"]
     assert driver_output[14] == "status=-5"
-    assert driver_output[15:] == ["flush", "status=0", "destroy 0x10"]
+
+
+def test_clip_rect_forwarded_other_clips_refused(driver_output):
+    # Translate(2, 1); ClipRect(1.5, 0, 30, 20) -> device (3.5, 1, 32, 21);
+    # ClipRect(-5, 2, 25, 40) -> (-3, 3, 27, 41); the global clip bounds are
+    # their intersection (3.5, 3, 27, 21), set before the translation
+    assert driver_output[15:18] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[18].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[19:21] == ["restore", "status=0"]
+    # a kDifference clip is refused and the draws under it draw nothing
+    assert driver_output[21] == "status=-5"
+    # after the Restores the canvas is unclipped and untranslated again
+    assert driver_output[22].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[23:] == ["status=0", "flush", "status=0", "destroy 0x10"]

@@ -134,3 +134,26 @@ def test_canvas_translate_bit_exact(cpu_pipeline, oracle_lib):
     got, _ = cpu_render(cpu_pipeline, sc)
     ref, _ = oracle_lib.render(sc)
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_clip_rect_bit_exact(cpu_pipeline, oracle_lib, seed):
+    """Canvas::ClipRect bounds the scan of every later draw (fills, strokes,
+    gradients, under translations, empty clips included)."""
+    from test_oracle_pin import clipped_scene
+    sc = clipped_scene(S.SEED_BASE + 380 + seed)
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+def test_blur_under_clip_refused(cpu_pipeline, oracle_lib):
+    """A blurred draw under a narrowed clip is refused by the batch builder
+    (not supported) rather than drawn unclipped."""
+    sc = S.config4(seed=S.SEED_BASE + 390, n_outlines=20, width=96, height=96, blur_frac=1.0)
+    sc.clips = np.tile(np.array([[4, 4, 60, 60]], np.float32), (sc.n_draws, 1))
+    b = sc.to_bytes()
+    out = np.zeros((sc.height, sc.width, 4), np.uint8)
+    st = (ctypes.c_uint64 * 6)()
+    rc = cpu_pipeline.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, 0, 0)
+    assert rc == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED

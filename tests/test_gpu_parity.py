@@ -182,3 +182,53 @@ def test_canvas_translate_matches_oracle(gpu_ctx, oracle_lib):
         p["translate"] = tr
         sb.draw_path(tri.verbs, tri.points, p)
     check(oracle_lib, bitmap, sb.build())
+
+
+@pytest.mark.gpu
+def test_clip_rect_matches_oracle(gpu_ctx, oracle_lib):
+    """Canvas::ClipRect (kIntersect) under Save / Translate / Restore: the
+    clipped scenes rendered as a batch, and a draw sequence through the
+    canvas API, against the oracle (pinned to the reference's ClipRect)."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import clipped_scene
+    from skity_gb300.canvas import Canvas, Paint, Path
+    scenes = [clipped_scene(S.SEED_BASE + 380 + k) for k in range(3)]
+    for sc, got in zip(scenes, gpu_ctx.render_streams(scenes)):
+        check(oracle_lib, got, sc)
+    bitmap = np.zeros((40, 48, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    tri = Path().MoveTo(1, 1).LineTo(30, 4).LineTo(5, 33).Close()
+    blue = Paint().SetFillColor(0.2, 0.3, 0.9, 0.8)
+    red = Paint().SetFillColor(0.9, 0.1, 0.1, 0.5)
+    canvas.Save()
+    canvas.ClipRect(3.5, 2.25, 21, 18.75)
+    canvas.DrawPath(tri, blue)
+    canvas.Save()
+    canvas.Translate(10.5, 3)
+    canvas.ClipRect(-2, 0, 12, 40)  # device (8.5, 3, 22.5, 43): narrows the clip to x >= 8.5
+    canvas.DrawPath(tri, red)
+    canvas.Restore()
+    canvas.DrawPath(tri, red)  # the first clip again
+    canvas.Restore()
+    canvas.Save()
+    canvas.ClipRect(40, 0, 44, 5)
+    canvas.ClipRect(0, 30, 5, 40)  # disjoint: empty clip, nothing drawn
+    canvas.DrawPath(tri, blue)
+    canvas.Restore()
+    canvas.DrawPath(tri, Paint().SetFillColor(0.1, 0.8, 0.2, 0.4))  # unclipped
+    canvas.Flush()
+    c1 = S.map_clip(S.NO_CLIP, (3.5, 2.25, 21, 18.75))
+    c2 = S.map_clip(c1, (-2, 0, 12, 40), 10.5, 3)
+    c3 = S.map_clip(S.map_clip(S.NO_CLIP, (40, 0, 44, 5)), (0, 30, 5, 40))
+    assert c3 == (0.0, 0.0, 0.0, 0.0)
+    sb = S.SceneBuilder(48, 40)
+    for tr, col, clip in [((0, 0), (0.2, 0.3, 0.9, 0.8), c1), ((10.5, 3), (0.9, 0.1, 0.1, 0.5), c2),
+                          ((0, 0), (0.9, 0.1, 0.1, 0.5), c1), ((0, 0), (0.2, 0.3, 0.9, 0.8), c3),
+                          ((0, 0), (0.1, 0.8, 0.2, 0.4), None)]:
+        p = S.default_paint()
+        p["fill_color"] = col
+        p["translate"] = tr
+        sb.draw_path(tri.verbs, tri.points, p, clip=clip)
+    check(oracle_lib, bitmap, sb.build())

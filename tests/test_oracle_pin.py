@@ -102,3 +102,36 @@ def translated_scene(seed=S.SEED_BASE + 360):
 
 def test_canvas_translate(ref):
     _pin(ref, translated_scene())
+
+
+def clipped_scene(seed=S.SEED_BASE + 380, width=180, height=140):
+    """Draws under Canvas::ClipRect (kIntersect) and Translate, as a canvas
+    sees them between Save and Restore: one or two nested clip rects per
+    draw (fractional, unordered, partly off-canvas, disjoint = empty clip),
+    some under a translation, some draws with the canvas's initial bounds."""
+    sc = S.random_paths_scene(seed, width, height, 48, 2, 24, coord_lo=(-20.0, -20.0),
+                              coord_hi=(width - 20.0, height - 20.0), evenodd_frac=0.4,
+                              gradient_frac=0.5, stroke_frac=0.3)
+    rng = np.random.default_rng(seed & 0xFFFF)
+    clips = np.zeros((sc.n_draws, 4), np.float32)
+    for d in range(sc.n_draws):
+        tx, ty = (rng.uniform(-30, 30, 2).astype(np.float32) if d % 3 == 1 else (0.0, 0.0))
+        sc.paints[d]["translate"] = (tx, ty)
+        clip = S.NO_CLIP
+        if d % 6 != 5:
+            for _ in range(1 + (d % 4 == 0)):
+                x0, x1 = rng.uniform(-30, width + 30, 2)
+                y0, y1 = rng.uniform(-30, height + 30, 2)
+                if d % 5 == 2:  # whole-pixel rects
+                    x0, x1, y0, y1 = np.round([x0, x1, y0, y1])
+                clip = S.map_clip(clip, (x0, y0, x1, y1), tx, ty)
+        clips[d] = clip
+    sc.clips = clips
+    return sc
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_canvas_clip_rect(ref, seed):
+    sc = clipped_scene(S.SEED_BASE + 380 + seed)
+    assert np.any(sc.clips[:, 2] == 0)  # some draws under an empty clip
+    _pin(ref, sc)
