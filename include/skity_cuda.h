@@ -99,7 +99,7 @@ typedef struct skity_cuda_paint {
   uint32_t style;      /* Paint::Style: fill, stroke, stroke-and-fill, stroke-then-fill */
   uint32_t cap;        /* Paint::Cap: butt, round, square */
   uint32_t join;       /* Paint::Join: miter, round, bevel */
-  uint32_t blend_mode; /* BlendMode (kSrcOver = 3) */
+  uint32_t blend_mode; /* BlendMode, kClear = 0 .. kLuminosity = 28 (kSrcOver = 3) */
   float fill_color[4];
   float stroke_color[4];
   float stroke_width;
@@ -284,7 +284,7 @@ SKITY_CUDA_API void skity_cuda_server_destroy(skity_cuda_server server);
  *
  * skity_cuda_draw_path_static draws ONE path with a solid-colour paint
  * (Canvas::DrawPath semantics: fill, stroke, stroke-and-fill or
- * stroke-then-fill; blend modes clear/src/dst/src-over; no shader, no mask
+ * stroke-then-fill; any BlendMode kClear..kLuminosity; no shader, no mask
  * filter) onto a premultiplied RGBA8 canvas that already lives in device
  * memory (`device_pixels`, `row_bytes` apart, a multiple of 4).  It allocates
  * nothing: no device memory (no cudaMalloc / cudaFree), no host heap.  Every

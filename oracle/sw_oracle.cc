@@ -1297,6 +1297,71 @@ static inline uint32_t AlphaMulQ(uint32_t c, uint32_t scale) {  // :62-68
 static inline uint32_t PMSrcOver(uint32_t src, uint32_t dst) {  // :70-72
   return src + AlphaMulQ(dst, 255 - GetA(src) + 1);
 }
+static inline uint32_t Alpha255To256(uint32_t a) { return a + 1; }  // :20-25
+static inline uint32_t PMColorMul(uint32_t s, uint32_t d) {        // :74-79
+  return (MulDiv255Round(GetA(s), GetA(d)) << 24) | (MulDiv255Round(GetR(s), GetR(d)) << 16) |
+         (MulDiv255Round(GetG(s), GetG(d)) << 8) | MulDiv255Round(GetB(s), GetB(d));
+}
+
+// SoftLightComponent (blend_mode.cc:91-108); x = colour, y = alpha.
+static float SoftLightComponent(float sx, float sy, float dx, float dy) {
+  if (2.f * sx <= sy) return dx * dx * (sy - 2 * sx) / dy + (1 - dy) * sx + dx * (-sy + 2 * sx + 1);
+  if (4.f * dx <= dy) {
+    float dsq = dx * dx, dcub = dsq * dx, dasq = dy * dy, dacub = dasq * dy;
+    return (dasq * (sx - dx * (3 * sy - 6 * sx - 1)) + 12 * dy * dsq * (sy - 2 * sx) -
+            16 * dcub * (sy - 2 * sx) - dacub * sx) /
+           dasq;
+  }
+  return dx * (sy - 2 * sx + 1) + sx - std::sqrt(dy * dx) * (sy - 2 * sx) - dy * sx;
+}
+
+// PorterDuffBlend (blend_mode.cc:123-191).  Modes past kScreen other than
+// kSoftLight fall back to kDefault (kSrcOver).
+static uint32_t PorterDuffBlend(uint32_t src, uint32_t dst, int mode) {
+  if (mode > 14 && mode != 21) mode = 3;
+  switch (mode) {
+    case 0: return 0;
+    case 1: return src;
+    case 2: return dst;
+    case 3:
+      if (GetA(src) == 0) return dst;
+      return PMSrcOver(src, dst);
+    case 4:
+      if (GetA(dst) == 255) return dst;
+      return PMSrcOver(dst, src);
+    case 5: return GetA(dst) == 255 ? src : AlphaMulQ(src, Alpha255To256(GetA(dst)));
+    case 6:
+      if (GetA(src) == 255) return dst;
+      return AlphaMulQ(dst, Alpha255To256(GetA(src)));
+    case 7: return GetA(dst) == 0 ? src : AlphaMulQ(src, Alpha255To256(255 - GetA(dst)));
+    case 8:
+      if (GetA(src) == 0) return dst;
+      return AlphaMulQ(dst, Alpha255To256(255 - GetA(src)));
+    case 9:
+      return AlphaMulQ(src, Alpha255To256(GetA(dst))) +
+             AlphaMulQ(dst, Alpha255To256(255 - GetA(src)));
+    case 10:
+      return AlphaMulQ(dst, Alpha255To256(GetA(src))) +
+             AlphaMulQ(src, Alpha255To256(255 - GetA(dst)));
+    case 11:
+      return AlphaMulQ(src, Alpha255To256(255 - GetA(dst))) +
+             AlphaMulQ(dst, Alpha255To256(255 - GetA(src)));
+    case 12:
+      return ColorSetARGB(std::min(GetA(src) + GetA(dst), 255u), std::min(GetR(src) + GetR(dst), 255u),
+                          std::min(GetG(src) + GetG(dst), 255u), std::min(GetB(src) + GetB(dst), 255u));
+    case 13: return PMColorMul(src, dst);
+    case 14: return src + dst - PMColorMul(src, dst);
+    default: {  // kSoftLight (:110-121)
+      if (GetA(dst) == 0) return src;
+      float s[4] = {GetR(src) / 255.f, GetG(src) / 255.f, GetB(src) / 255.f, GetA(src) / 255.f};
+      float d[4] = {GetR(dst) / 255.f, GetG(dst) / 255.f, GetB(dst) / 255.f, GetA(dst) / 255.f};
+      float out[4] = {SoftLightComponent(s[0], s[3], d[0], d[3]),
+                      SoftLightComponent(s[1], s[3], d[1], d[3]),
+                      SoftLightComponent(s[2], s[3], d[2], d[3]), s[3] + (1 - s[3]) * d[3]};
+      return Color4fToColor(out);
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Brushes (src/render/sw/sw_span_brush.cc:66-383)
@@ -1486,14 +1551,29 @@ struct Target {
       return;
     }
     if (mode == 2) return;  // kDst
-    // kSrcOver (the only other mode this oracle covers)
     uint32_t a = GetA(src);
-    if (a == 0) return;
-    if (a == 255) {
-      Set(x, y, src);
-      return;
+    if (mode == 3) {  // kSrcOver
+      if (a == 0) return;
+      if (a == 255) {
+        Set(x, y, src);
+        return;
+      }
+    } else if (mode == 4) {  // kDstOver over an opaque pixel
+      if (GetA(Get(x, y)) == 255) return;
+    } else if (mode == 6) {  // kDstIn
+      if (a == 255) return;
+      if (a == 0) {
+        Set(x, y, 0);
+        return;
+      }
+    } else if (mode == 8) {  // kDstOut
+      if (a == 0) return;
+      if (a == 255) {
+        Set(x, y, 0);
+        return;
+      }
     }
-    Set(x, y, PMSrcOver(src, Get(x, y)));
+    Set(x, y, PorterDuffBlend(src, Get(x, y), mode));
   }
 };
 

@@ -416,7 +416,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   std::vector<std::pair<uint32_t, std::vector<PassDesc>>> temps;
   for (uint32_t d = 0; d < s.nd; ++d) {
     const PaintRec& pr = s.paints[d];
-    if (pr.blend != 3 && pr.blend > 2) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    if (pr.blend > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
     uint32_t draw = hb.AddDraw(s.verbs + s.vo[d], s.vo[d + 1] - s.vo[d], s.pts + 2 * (size_t)s.po[d],
                                s.po[d + 1] - s.po[d], s.wts + s.wo[d], s.wo[d + 1] - s.wo[d]);
     hb.draw_count++;

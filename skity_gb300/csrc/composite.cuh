@@ -62,20 +62,100 @@ SKC_HD uint32_t PMSrcOver(uint32_t src, uint32_t dst) {  // color_priv.hpp:70-72
   return src + AlphaMulQ(dst, 256 - GetA(src));
 }
 
-// BlendPixel (sw_render_target.cc:12-35) for the modes with a FastBlend rule
-// plus src-over; returns the new destination.
+SKC_HD uint32_t GetR(uint32_t c) { return (c >> 16) & 0xFF; }
+SKC_HD uint32_t GetG(uint32_t c) { return (c >> 8) & 0xFF; }
+SKC_HD uint32_t GetB(uint32_t c) { return c & 0xFF; }
+SKC_HD uint32_t PMColorMul(uint32_t s, uint32_t d) {  // color_priv.hpp:74-79
+  return (MulDiv255Round(GetA(s), GetA(d)) << 24) | (MulDiv255Round(GetR(s), GetR(d)) << 16) |
+         (MulDiv255Round(GetG(s), GetG(d)) << 8) | MulDiv255Round(GetB(s), GetB(d));
+}
+
+// SoftLight of one channel (blend_mode.cc:91-108): s = (colour, alpha) of
+// the source, d of the destination, as fractions of 255.
+SKC_HD float SoftLightChannel(float sc, float sa, float dc, float da) {
+  if (2.f * sc <= sa) {
+    return dc * dc * (sa - 2 * sc) / da + (1 - da) * sc + dc * (-sa + 2 * sc + 1);
+  }
+  if (4.f * dc <= da) {
+    const float d2 = dc * dc, d3 = d2 * dc, a2 = da * da, a3 = a2 * da;
+    return (a2 * (sc - dc * (3 * sa - 6 * sc - 1)) + 12 * da * d2 * (sa - 2 * sc) -
+            16 * d3 * (sa - 2 * sc) - a3 * sc) /
+           a2;
+  }
+  return dc * (sa - 2 * sc + 1) + sc - sqrt_(da * dc) * (sa - 2 * sc) - da * sc;
+}
+
+// PorterDuffBlend (blend_mode.cc:123-191): the coefficient modes up to
+// kScreen and kSoftLight; any other mode blends as kSrcOver (kDefault).
+SKC_HD uint32_t PorterDuff(uint32_t src, uint32_t dst, uint32_t mode) {
+  if (mode > 14 && mode != 21) mode = 3;
+  const uint32_t sa = GetA(src), da = GetA(dst);
+  switch (mode) {
+    case 0: return 0;
+    case 1: return src;
+    case 2: return dst;
+    case 3: return sa == 0 ? dst : PMSrcOver(src, dst);
+    case 4: return da == 255 ? dst : PMSrcOver(dst, src);                    // kDstOver
+    case 5: return da == 255 ? src : AlphaMulQ(src, da + 1);                // kSrcIn
+    case 6: return sa == 255 ? dst : AlphaMulQ(dst, sa + 1);                // kDstIn
+    case 7: return da == 0 ? src : AlphaMulQ(src, 256 - da);                // kSrcOut
+    case 8: return sa == 0 ? dst : AlphaMulQ(dst, 256 - sa);                // kDstOut
+    case 9: return AlphaMulQ(src, da + 1) + AlphaMulQ(dst, 256 - sa);       // kSrcATop
+    case 10: return AlphaMulQ(dst, sa + 1) + AlphaMulQ(src, 256 - da);      // kDstATop
+    case 11: return AlphaMulQ(src, 256 - da) + AlphaMulQ(dst, 256 - sa);    // kXor
+    case 12:                                                                 // kPlus
+      return ARGB(min_(sa + da, 255u), min_(GetR(src) + GetR(dst), 255u),
+                  min_(GetG(src) + GetG(dst), 255u), min_(GetB(src) + GetB(dst), 255u));
+    case 13: return PMColorMul(src, dst);                                    // kModulate
+    case 14: return src + dst - PMColorMul(src, dst);                        // kScreen
+    default: {                                                               // kSoftLight
+      if (da == 0) return src;
+      // Color4fFromColor (color.cc:44-51)
+      const float s_r = GetR(src) / 255.f, s_g = GetG(src) / 255.f, s_b = GetB(src) / 255.f;
+      const float s_a = sa / 255.f;
+      const float d_r = GetR(dst) / 255.f, d_g = GetG(dst) / 255.f, d_b = GetB(dst) / 255.f;
+      const float d_a = da / 255.f;
+      const float r = SoftLightChannel(s_r, s_a, d_r, d_a);
+      const float g = SoftLightChannel(s_g, s_a, d_g, d_a);
+      const float b = SoftLightChannel(s_b, s_a, d_b, d_a);
+      const float a = s_a + (1 - s_a) * d_a;
+      return Color4fToColor(r, g, b, a);
+    }
+  }
+}
+
+// SWRenderTarget::BlendPixel (sw_render_target.cc:12-35): the FastBlend
+// shortcuts (:89-141), else PorterDuffBlend; returns the new destination.
 SKC_HD uint32_t BlendPixel(uint32_t dst, uint32_t src, uint32_t mode) {
   switch (mode) {
     case 0: return 0;        // kClear
     case 1: return src;      // kSrc
     case 2: return dst;      // kDst
-    default: {               // kSrcOver
-      uint32_t a = GetA(src);
+    case 3: {                // kSrcOver
+      const uint32_t a = GetA(src);
       if (a == 0) return dst;
       if (a == 255) return src;
       return PMSrcOver(src, dst);
     }
+    case 4:                  // kDstOver
+      if (GetA(dst) == 255) return dst;
+      break;
+    case 6: {                // kDstIn
+      const uint32_t a = GetA(src);
+      if (a == 255) return dst;
+      if (a == 0) return 0;
+      break;
+    }
+    case 8: {                // kDstOut
+      const uint32_t a = GetA(src);
+      if (a == 0) return dst;
+      if (a == 255) return 0;
+      break;
+    }
+    default:
+      break;
   }
+  return PorterDuff(src, dst, mode);
 }
 
 SKC_HD float RemapFloatTile(float t, uint32_t tile) {  // sw_span_brush.cc:21-32

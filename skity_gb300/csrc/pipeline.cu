@@ -775,7 +775,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   }
   if (need_p != path->point_count || need_w != path->conic_weight_count)
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
-  if (paint->blend_mode > 3) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
   if (paint->blur_style > 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (!skc::ValidPaint(paint->style, paint->cap, paint->join, paint->stroke_width,
                        paint->miter_limit, paint->blur_style ? paint->blur_radius : 0.f))

@@ -157,3 +157,11 @@ def test_blur_under_clip_refused(cpu_pipeline, oracle_lib):
     st = (ctypes.c_uint64 * 6)()
     rc = cpu_pipeline.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, 0, 0)
     assert rc == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
+
+
+def test_every_blend_mode_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import blend_modes_scene
+    sc = blend_modes_scene()
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0

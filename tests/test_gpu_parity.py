@@ -232,3 +232,14 @@ def test_clip_rect_matches_oracle(gpu_ctx, oracle_lib):
         p["translate"] = tr
         sb.draw_path(tri.verbs, tri.points, p, clip=clip)
     check(oracle_lib, bitmap, sb.build())
+
+
+@pytest.mark.gpu
+def test_every_blend_mode_matches_oracle(gpu_ctx, oracle_lib):
+    """kClear .. kLuminosity (PorterDuffBlend with FastBlend, SoftLight in
+    float, the rest as kSrcOver) over translucent and transparent pixels."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import blend_modes_scene
+    sc = blend_modes_scene()
+    check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)

@@ -135,3 +135,38 @@ def test_canvas_clip_rect(ref, seed):
     sc = clipped_scene(S.SEED_BASE + 380 + seed)
     assert np.any(sc.clips[:, 2] == 0)  # some draws under an empty clip
     _pin(ref, sc)
+
+
+
+def blend_modes_scene(seed=S.SEED_BASE + 395, width=120, height=96):
+    """Every BlendMode (kClear .. kLuminosity; the modes past kScreen other
+    than kSoftLight blend as kSrcOver) with solid and gradient paints,
+    fills and strokes, over a canvas cleared to a translucent colour so the
+    destination alpha varies (opaque, translucent and transparent pixels)."""
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height, clear=(0.3, 0.6, 0.2, 0.5))
+    for i in range(3 * 29):
+        mode = i % 29
+        n = 3 + i % 6
+        verbs = [S.MOVE] + [[S.LINE, S.QUAD, S.CUBIC][j % 3] for j in range(n)] + [S.CLOSE]
+        npts = 1 + sum({S.LINE: 1, S.QUAD: 2, S.CUBIC: 3}[v] for v in verbs[1:-1])
+        pts = rng.uniform(-10, width + 10, (npts, 2)).astype(np.float32)
+        p = S.default_paint()
+        p["blend"] = mode
+        p["style"] = [S.FILL, S.STROKE, S.FILL][i // 29]
+        p["stroke_width"] = float(2 + i % 5)
+        alpha = [1.0, 0.0, rng.uniform(0.05, 0.95)][i % 3]
+        p["fill_color"] = tuple(np.append(rng.uniform(0, 1, 3), alpha).astype(np.float32))
+        p["stroke_color"] = p["fill_color"]
+        if i % 4 == 3:
+            cols = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+            p["gradient"] = b.add_gradient(S.GRAD_LINEAR if i % 8 == 3 else S.GRAD_RADIAL,
+                                           (float(pts[0, 0]), float(pts[0, 1])),
+                                           (float(pts[1, 0]), float(pts[1, 1])),
+                                           (float(10 + i), 0.0), cols)
+        b.draw_path(verbs, pts, p)
+    return b.build()
+
+
+def test_every_blend_mode(ref):
+    _pin(ref, blend_modes_scene())
