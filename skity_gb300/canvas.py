@@ -21,7 +21,11 @@ Style = type("Style", (), {"kFill_Style": 0, "kStroke_Style": 1, "kStrokeAndFill
 Cap = type("Cap", (), {"kButt_Cap": 0, "kRound_Cap": 1, "kSquare_Cap": 2})
 Join = type("Join", (), {"kMiter_Join": 0, "kRound_Join": 1, "kBevel_Join": 2})
 PathFillType = type("PathFillType", (), {"kWinding": 0, "kEvenOdd": 1})
-BlendMode = type("BlendMode", (), {"kClear": 0, "kSrc": 1, "kDst": 2, "kSrcOver": 3})
+# BlendMode (include/skity/graphic/blend_mode.hpp:45-80)
+BlendMode = type("BlendMode", (), {n: i for i, n in enumerate(
+    "kClear kSrc kDst kSrcOver kDstOver kSrcIn kDstIn kSrcOut kDstOut kSrcATop kDstATop kXor "
+    "kPlus kModulate kScreen kOverlay kDarken kLighten kColorDodge kColorBurn kHardLight "
+    "kSoftLight kDifference kExclusion kMultiply kHue kSaturation kColor kLuminosity".split())})
 TileMode = type("TileMode", (), {"kClamp": 0, "kRepeat": 1, "kMirror": 2, "kDecal": 3})
 BlurStyle = type("BlurStyle", (), {"kNormal": 1, "kSolid": 2, "kOuter": 3, "kInner": 4})
 
