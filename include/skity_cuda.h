@@ -80,9 +80,15 @@ typedef struct skity_cuda_path {
   uint32_t fill_type;
 } skity_cuda_path;
 
-/* Shader::MakeLinear / MakeRadial (include/skity/effect/shader.hpp:88-109). */
+/* A gradient shader as Shader::AsGradient describes it (GradientInfo,
+ * include/skity/effect/shader.hpp:48-70): Shader::MakeLinear, MakeRadial,
+ * MakeSweep (radius = bias, scale of the angle: -start/360 and
+ * 1 / ((end - start) / 360), shader.cc:88-104) and MakeTwoPointConical
+ * (the degenerate concentric cases are radial gradients, shader.cc:50-86). */
 typedef struct skity_cuda_gradient {
-  uint32_t type;      /* 1 linear (p0 -> p1), 2 radial (centre p0, radius[0]) */
+  uint32_t type;      /* 1 linear (p0 -> p1), 2 radial (centre p0, radius[0]),
+                         3 sweep (centre p0, radius = bias, scale),
+                         4 two-point conical (p0, radius[0] -> p1, radius[1]) */
   uint32_t tile_mode; /* TileMode: 0 clamp, 1 repeat, 2 mirror, 3 decal */
   uint32_t stop_count;
   uint32_t has_offsets; /* 0: stops evenly spaced (pos == nullptr) */
@@ -137,6 +143,7 @@ typedef struct skity_cuda_stats {
   uint64_t fragments;     /* sum of span lengths inside the canvases */
   uint64_t graph_replays; /* 1: the render replayed the batch's CUDA graph */
   uint64_t fragments_by_brush[4]; /* fragments shaded by solid, linear, radial
+                                     (sweep and two-point conical included)
                                      and image (blur composite) brushes */
 } skity_cuda_stats;
 

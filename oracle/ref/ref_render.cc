@@ -24,6 +24,8 @@
 #include <string>
 #include <vector>
 
+#include "src/effect/gradient_shader.hpp"  // the sweep / conical shader classes
+
 namespace {
 
 struct PaintRec {
@@ -152,6 +154,19 @@ skity::Paint BuildPaint(const Scene& s, uint32_t d) {
       paint.SetShader(skity::Shader::MakeRadial(
           skity::Point{g.p0[0], g.p0[1], 0, 1}, g.radius[0], colors.data(),
           pos, int(g.stop_count), tile));
+    } else if (g.type == 3 && g.stop_count >= 2) {
+      // the record holds the shader's GradientInfo (bias, scale), which is
+      // what Shader::MakeSweep builds from its angles (shader.cc:88-104)
+      paint.SetShader(std::make_shared<skity::SweepGradientShader>(
+          g.p0[0], g.p0[1], g.radius[0], g.radius[1], colors.data(), pos,
+          int(g.stop_count), tile, 0));
+    } else if (g.type == 4 && g.stop_count >= 2) {
+      // the two-point conical shader itself (MakeTwoPointConical's
+      // concentric special cases are radial records)
+      paint.SetShader(std::make_shared<skity::TwoPointConicalGradientShader>(
+          skity::Point{g.p0[0], g.p0[1], 0, 1}, g.radius[0],
+          skity::Point{g.p1[0], g.p1[1], 0, 1}, g.radius[1], colors.data(), pos,
+          int(g.stop_count), tile, 0));
     }
   }
   if (r.blur_style != 0) {

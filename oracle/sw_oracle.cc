@@ -1410,7 +1410,7 @@ static Mat MatTranslate(float tx, float ty) {
 }
 
 struct Gradient {
-  int type;  // 1 linear, 2 radial
+  int type;  // 1 linear, 2 radial, 3 sweep, 4 two-point conical
   int tile;
   int count;
   bool has_offsets;
@@ -1421,6 +1421,8 @@ struct Gradient {
 
 // PointsToUnit (sw_span_brush.cc:164-200)
 static Mat PointsToUnit(const Gradient& g) {
+  if (g.type == 3) return MatTranslate(-g.p0[0], -g.p0[1]);
+  if (g.type == 4) return Mat::Identity();  // the conical brush keeps its own
   if (g.type == 1) {
     float sx = g.p0[0], sy = g.p0[1];
     float ssx = g.p1[0] - sx, ssy = g.p1[1] - sy;
@@ -1504,21 +1506,150 @@ static void LerpColor(const Gradient& g, float current, float out[4]) {
   for (int k = 0; k < 4; ++k) out[k] = c0[k] * (1 - mix) + c1[k] * mix;
 }
 
+// MapPoint (sw_span_brush.cc:224-227)
+static inline void MapPoint(const Mat& m, float x, float y, float* ox, float* oy) {
+  *ox = x * m.e[0][0] + y * m.e[1][0] + m.e[3][0];
+  *oy = x * m.e[0][1] + y * m.e[1][1] + m.e[3][1];
+}
+
+// ConicalGradientColorBrush's state after OnPreBrush (sw_span_brush.cc:394-437)
+struct Conical {
+  float c0[4], c1[4];  // Points (z = 0, w = 1)
+  float r0 = 0, r1 = 0, r1_square = 0;
+  float delta_center = 0, delta_radius = 0;
+  bool radial = false, strip = false, swap_01 = false;
+  float scale = 0, scale_sign = 0, bias = 0, f = 0;
+  Mat c0c1, cfc1;
+};
+
+static float Length4(const float a[4]) {  // Vec4::Length (vector.hpp:233-281)
+  return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
+}
+
+static Mat LineToUnit(const float p0[4], const float p1[4]) {  // PointsToUnit(p0, p1)
+  Gradient g{};
+  g.type = 1;
+  g.p0[0] = p0[0];
+  g.p0[1] = p0[1];
+  g.p1[0] = p1[0];
+  g.p1[1] = p1[1];
+  return PointsToUnit(g);
+}
+
+static Conical ConicalPreBrush(const Gradient& g) {
+  const float kNZ = 1.0f / (1 << 12);
+  Conical c;
+  c.c0[0] = g.p0[0], c.c0[1] = g.p0[1], c.c0[2] = 0.f, c.c0[3] = 1.f;
+  c.c1[0] = g.p1[0], c.c1[1] = g.p1[1], c.c1[2] = 0.f, c.c1[3] = 1.f;
+  c.r0 = g.radius[0];
+  c.r1 = g.radius[1];
+  float d[4];
+  for (int i = 0; i < 4; ++i) d[i] = c.c1[i] - c.c0[i];
+  c.delta_center = Length4(d);
+  c.delta_radius = std::abs(c.r1 - c.r0);
+  if (c.r0 < 0 || c.r1 < 0) return c;
+  c.radial = c.delta_center < kNZ;
+  c.strip = c.delta_radius < kNZ;
+  if (c.radial) {
+    if (!c.strip) {
+      c.scale = 1.0 / c.delta_radius;
+      c.scale_sign = c.delta_radius < 0 ? -1.f : 1.f;
+      c.bias = c.r0 / c.delta_radius;
+    }
+  } else if (c.strip) {
+    c.c0c1 = LineToUnit(c.c0, c.c1);
+  } else {
+    c.swap_01 = c.r1 < kNZ;
+    if (c.swap_01) {
+      for (int i = 0; i < 4; ++i) std::swap(c.c0[i], c.c1[i]);
+      std::swap(c.r0, c.r1);
+    }
+    c.f = c.r0 / (c.r0 - c.r1);
+    float cf[4], e[4];
+    for (int i = 0; i < 4; ++i) cf[i] = c.c0[i] * (1.f - c.f) + c.c1[i] * c.f;
+    for (int i = 0; i < 4; ++i) e[i] = c.c1[i] - cf[i];
+    c.r1 = c.r1 / Length4(e);
+    c.r1_square = c.r1 * c.r1;
+    c.cfc1 = LineToUnit(cf, c.c1);
+  }
+  return c;
+}
+
+// CalculateConical (sw_span_brush.cc:441-507); false: transparent
+static bool ConicalParam(const Conical& c, const Mat& d2l, int x, int y, float* out) {
+  if (c.r0 < 0 || c.r1 < 0) return false;
+  float px, py;
+  MapPoint(d2l, x + 0.5f, y + 0.5f, &px, &py);
+  float t = 0;
+  if (c.radial) {
+    if (c.strip) return false;
+    float qx = (px - c.c0[0]) * c.scale, qy = (py - c.c0[1]) * c.scale;
+    t = std::sqrt(qx * qx + qy * qy) * c.scale_sign - c.bias;
+  } else if (c.strip) {
+    float r = c.r0 / c.delta_center;
+    float r_2 = r * r;
+    float qx, qy;
+    MapPoint(c.c0c1, px, py, &qx, &qy);
+    t = r_2 - qy * qy;
+    if (t < 0.0) return false;
+    t = qx + ::sqrt(t);  // unqualified sqrt of a float: the C library's double sqrt
+  } else {
+    float qx, qy;
+    MapPoint(c.cfc1, px, py, &qx, &qy);
+    float xt = -1.f;
+    if (std::abs(c.r1 - 1.f) < 1.0f / (1 << 12)) {
+      xt = (qx * qx + qy * qy) / 2;
+    } else if (c.r1 > 1.f) {
+      float m = c.r1_square - 1.f;
+      float delta = m * qy * qy + c.r1_square * qx * qx;
+      xt = (std::sqrt(delta) - qx) / m;
+    } else {
+      float m = c.r1_square - 1.f;
+      float delta = m * qy * qy + c.r1_square * qx * qx;
+      if (delta > 0) {
+        float xt1 = (std::sqrt(delta) - qx) / m;
+        float xt2 = (-std::sqrt(delta) - qx) / m;
+        xt = 1.f - c.f < 0 ? std::min(xt1, xt2) : std::max(xt1, xt2);
+      }
+    }
+    if (xt < 0) return false;
+    t = c.f + (1.f - c.f) * xt;
+    if (c.swap_01) t = 1.0 - t;
+  }
+  *out = t;
+  return true;
+}
+
 struct Brush {
-  int kind = 0;  // 0 solid, 1 linear, 2 radial
+  int kind = 0;  // 0 solid, 1 linear, 2 radial, 3 sweep, 4 two-point conical
   uint32_t solid = 0;
   Gradient g{};
   Mat m{};
+  Mat d2l = Mat::Identity();  // conical: device_to_local, mapped before its own transforms
+  Conical con{};
   uint8_t global_alpha = 255;
 
   uint32_t ColorAt(int x, int y) const {
     if (kind == 0) return solid;
-    float sx = x + 0.5f, sy = y + 0.5f;
-    // MapPoint (sw_span_brush.cc:224-227)
-    float mx = sx * m.e[0][0] + sy * m.e[1][0] + m.e[3][0];
-    float my = sx * m.e[0][1] + sy * m.e[1][1] + m.e[3][1];
-    float t = kind == 1 ? mx : std::sqrt(mx * mx + my * my);
     float c[4];
+    if (kind == 4) {
+      float t;
+      if (!ConicalParam(con, d2l, x, y, &t)) return 0;  // Colors::kTransparent
+      LerpColor(g, t, c);
+      return ColorToPMColor(Color4fToColor(c));
+    }
+    float mx, my;
+    MapPoint(m, x + 0.5f, y + 0.5f, &mx, &my);
+    float t;
+    if (kind == 1) {
+      t = mx;
+    } else if (kind == 2) {
+      t = std::sqrt(mx * mx + my * my);
+    } else {  // sweep (sw_span_brush.cc:336-349)
+      float angle = std::atan2(-my, -mx);
+      constexpr float k1Over2Pi = 0.1591549430918;
+      t = (angle * k1Over2Pi + 0.5 + g.radius[0]) * g.radius[1];
+    }
     LerpColor(g, t, c);
     return ColorToPMColor(Color4fToColor(c));
   }
@@ -1737,6 +1868,7 @@ static Brush MakeBrush(const SceneView& s, const PaintRec& p, bool stroke) {
     std::memcpy(br.g.p1, g.p1, 8);
     std::memcpy(br.g.radius, g.radius, 8);
     br.m = PointsToUnit(br.g);
+    if (br.kind == 4) br.con = ConicalPreBrush(br.g);
     return br;
   }
   br.kind = 0;

@@ -98,11 +98,13 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
   if (const Shader* s = paint.GetShader().get()) {
     Shader::GradientInfo info;
     const Shader::GradientType t = s->AsGradient(&info);
-    if ((t != Shader::kLinear && t != Shader::kRadial) || !info.local_matrix.IsIdentity()) {
+    if ((t != Shader::kLinear && t != Shader::kRadial && t != Shader::kSweep &&
+         t != Shader::kConical) ||
+        !info.local_matrix.IsIdentity()) {
       status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
       return;
     }
-    g.type = t == Shader::kLinear ? 1u : 2u;
+    g.type = t == Shader::kLinear ? 1u : t == Shader::kRadial ? 2u : t == Shader::kSweep ? 3u : 4u;
     g.tile_mode = static_cast<uint32_t>(info.tile_mode);
     g.stop_count = static_cast<uint32_t>(info.colors.size());
     g.has_offsets = info.color_offsets.empty() ? 0u : 1u;

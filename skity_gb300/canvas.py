@@ -131,6 +131,45 @@ class Shader:
             return None
         return Shader(S.GRAD_RADIAL, center, (0.0, 0.0), (radius, 0.0), colors[:count], pos, tile_mode)
 
+    @staticmethod
+    def MakeSweep(cx, cy, start_angle, end_angle, colors, pos, count, tile_mode=TileMode.kClamp):
+        """Shader::MakeSweep (src/effect/shader.cc:88-104): null for fewer
+        than two stops or start >= end; the shader keeps bias = -start/360
+        and scale = 1 / (end/360 - start/360), in float."""
+        if count < 2 or not (start_angle < end_angle):
+            return None
+        f = np.float32
+        t0, t1 = f(start_angle) / f(360), f(end_angle) / f(360)
+        bias, scale = -t0, f(1) / (t1 - t0)
+        return Shader(S.GRAD_SWEEP, (cx, cy), (0.0, 0.0), (float(bias), float(scale)),
+                      colors[:count], pos, tile_mode)
+
+    @staticmethod
+    def MakeTwoPointConical(start, start_radius, end, end_radius, colors, pos, count,
+                            tile_mode=TileMode.kClamp):
+        """Shader::MakeTwoPointConical (src/effect/shader.cc:50-86): null for
+        fewer than two stops or equal concentric circles; concentric with one
+        radius zero is a radial gradient (reversed stops when the end radius
+        is the zero one)."""
+        if count < 2:
+            return None
+        f = np.float32
+        near0 = lambda v: abs(f(v)) <= f(1.0 / (1 << 12))  # FloatNearlyZero
+        same_radius = near0(f(start_radius) - f(end_radius))
+        if near0(f(start[0]) - f(end[0])) and near0(f(start[1]) - f(end[1])):
+            if same_radius:
+                return None
+            if near0(start_radius) or near0(end_radius):
+                cols = np.asarray(colors, np.float32).reshape(-1, 4)[:count]
+                if near0(end_radius):
+                    rpos = None if pos is None else [float(f(1) - f(p)) for p in list(pos)[:count][::-1]]
+                    return Shader(S.GRAD_RADIAL, start, (0.0, 0.0), (start_radius, 0.0),
+                                  cols[::-1], rpos, tile_mode)
+                return Shader(S.GRAD_RADIAL, start, (0.0, 0.0), (end_radius, 0.0), cols, pos,
+                              tile_mode)
+        return Shader(S.GRAD_CONICAL, start, end, (start_radius, end_radius), colors[:count], pos,
+                      tile_mode)
+
 
 class MaskFilter:
     def __init__(self, style, radius):

@@ -208,6 +208,81 @@ inline Mat4 PointsToUnitMat(const GradRec& g) {
   float scale = radius > 0 ? 1.0f / radius : 0;
   return MatMul(MatScale(scale, scale), MatTranslate(-g.p0[0], -g.p0[1]));
 }
+// PointsToUnit(p0, p1) (sw_span_brush.cc:196-214): the line p0 -> p1 to
+// the unit x axis.
+inline Mat4 LineToUnit(float p0x, float p0y, float p1x, float p1y) {
+  GradRec g;
+  std::memset(&g, 0, sizeof g);
+  g.type = 1;
+  g.p0[0] = p0x;
+  g.p0[1] = p0y;
+  g.p1[0] = p1x;
+  g.p1[1] = p1y;
+  return PointsToUnitMat(g);
+}
+inline void MapPointForm(const Mat4& m, float out[6]) {  // MapPoint's six terms
+  out[0] = m.e[0][0];
+  out[1] = m.e[1][0];
+  out[2] = m.e[3][0];
+  out[3] = m.e[0][1];
+  out[4] = m.e[1][1];
+  out[5] = m.e[3][1];
+}
+
+// ConicalGradientColorBrush::OnPreBrush (sw_span_brush.cc:394-437) on the
+// gradient's points (Points: z = 0, w = 1) and radii; vector lengths are
+// glm lengths of the 4-component points.
+inline ConicalParams ConicalSetup(const GradRec& g, const Mat4& device_to_local) {
+  const float kNZ = 1.0f / (1 << 12);
+  ConicalParams c;
+  std::memset(&c, 0, sizeof c);
+  MapPointForm(device_to_local, c.d2l);
+  float c0[4] = {g.p0[0], g.p0[1], 0.f, 1.f}, c1[4] = {g.p1[0], g.p1[1], 0.f, 1.f};
+  float r0 = g.radius[0], r1 = g.radius[1];
+  auto len4 = [](const float a[4], const float b[4]) {
+    const float d[4] = {a[0] - b[0], a[1] - b[1], a[2] - b[2], a[3] - b[3]};
+    return std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3]);
+  };
+  const float delta_center = len4(c1, c0);
+  const float delta_radius = std::fabs(r1 - r0);
+  c.mode = 0;
+  if (!(r0 < 0 || r1 < 0)) {
+    const bool radial = delta_center < kNZ, strip = delta_radius < kNZ;
+    if (radial) {
+      c.mode = strip ? 2 : 1;
+      if (!strip) {
+        c.scale = (float)(1.0 / delta_radius);
+        c.scale_sign = delta_radius < 0 ? -1.f : 1.f;
+        c.bias = r0 / delta_radius;
+      }
+      c.c0x = c0[0];
+      c.c0y = c0[1];
+    } else if (strip) {
+      c.mode = 3;
+      MapPointForm(LineToUnit(c0[0], c0[1], c1[0], c1[1]), c.t);
+      const float r = r0 / delta_center;
+      c.r2 = r * r;
+    } else {
+      c.mode = 4;
+      c.swap01 = r1 < kNZ ? 1u : 0u;
+      if (c.swap01) {
+        for (int i = 0; i < 4; ++i) std::swap(c0[i], c1[i]);
+        std::swap(r0, r1);
+      }
+      const float f = r0 / (r0 - r1);
+      float cf[4];
+      for (int i = 0; i < 4; ++i) cf[i] = c0[i] * (1.f - f) + c1[i] * f;
+      r1 = r1 / len4(c1, cf);
+      c.f = f;
+      c.r1 = r1;
+      c.r1_square = r1 * r1;
+      MapPointForm(LineToUnit(cf[0], cf[1], c1[0], c1[1]), c.t);
+      if (r0 < 0 || r1 < 0) c.mode = 0;  // CalculateConical's check, on the final radii
+    }
+  }
+  return c;
+}
+
 // Matrix::Invert of a translate-only CTM (matrix.cc:134-142, 242-266)
 inline Mat4 InvertTranslate(float tx, float ty) {
   Mat4 m = MatTranslate(tx, ty);
@@ -232,6 +307,7 @@ struct HostBatch {
   std::vector<DrawDesc> draws;
   std::vector<PassDesc> passes;
   std::vector<Brush> brushes;
+  std::vector<ConicalParams> conicals;
   std::vector<CanvasDesc> canvases;
   std::vector<float4> stop_colors;
   std::vector<float> stop_offsets;
@@ -330,14 +406,28 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     const GradRec* g = pr.gradient >= 0 ? &s.grads[pr.gradient] : nullptr;
     // Shader::MakeLinear / MakeRadial return null for < 2 stops or a
     // negative radius (src/effect/shader.cc:21-45)
-    if (g && (g->stop_count < 2 || (g->type == 2 && g->radius[0] < 0.f) ||
-              (g->type != 1 && g->type != 2))) {
+    if (g && (g->stop_count < 2 || (g->type == 2 && g->radius[0] < 0.f) || g->type < 1 ||
+              g->type > 4)) {
       g = nullptr;
     }
     if (g) {
-      br.kind = g->type;
+      // brush kinds: 1 linear, 2 radial, 4 sweep, 5 conical (3 is the image brush)
+      br.kind = g->type <= 2 ? g->type : g->type + 1;
       Mat4 dev_to_local = MatMul(MatTranslate(0, 0), InvertTranslate(tx, ty));
-      Mat4 m = MatMul(PointsToUnitMat(*g), dev_to_local);
+      // PointsToUnit (sw_span_brush.cc:164-194): the sweep's is a translation
+      // to its centre; the conical brush maps device_to_local and its own
+      // transforms one after the other
+      Mat4 m = g->type == 3   ? MatMul(MatTranslate(-g->p0[0], -g->p0[1]), dev_to_local)
+               : g->type == 4 ? dev_to_local
+                              : MatMul(PointsToUnitMat(*g), dev_to_local);
+      if (g->type == 3) {
+        br.bias = g->radius[0];
+        br.scale = g->radius[1];
+      }
+      if (g->type == 4) {
+        br.conical = (uint32_t)hb.conicals.size();
+        hb.conicals.push_back(ConicalSetup(*g, dev_to_local));
+      }
       br.m[0] = m.e[0][0];
       br.m[1] = m.e[1][0];
       br.m[2] = m.e[3][0];

@@ -11,7 +11,7 @@ namespace skc {
 // Per-pass brush, prepared on the host the way SWCanvas::GenerateBrush
 // (sw_canvas.cc:727-795) prepares the reference's SWSpanBrush.
 struct Brush {
-  uint32_t kind;          // 0 solid, 1 linear, 2 radial, 3 image (blur mask)
+  uint32_t kind;          // 0 solid, 1 linear, 2 radial, 3 image (blur mask), 4 sweep, 5 conical
   uint32_t blend;         // BlendMode
   uint32_t solid;         // premultiplied ARGB (kind 0)
   uint32_t global_alpha;  // SWSpanBrush::global_alpha_ (255 except image)
@@ -19,6 +19,24 @@ struct Brush {
   uint32_t tile, stop_count, has_offsets, stop0;  // gradient stops
   uint32_t img_w, img_h;  // image brush source
   uint64_t img_off;       // byte offset of the source pixels (RGBA8 rows)
+  float bias, scale;      // sweep: GradientInfo::radius (bias, scale of the angle)
+  uint32_t conical;       // conical: index of its ConicalParams
+  uint32_t pad;
+};
+
+// ConicalGradientColorBrush after OnPreBrush (sw_span_brush.cc:394-437),
+// prepared on the host; MapPoint form of the matrices (sx, kx, tx, ky, sy, ty).
+struct ConicalParams {
+  float d2l[6];           // device_to_local, applied first
+  float t[6];             // then c0 -> c1 (strip) or cf -> c1 (general) to unit
+  float c0x, c0y;         // radial: start centre
+  float scale, scale_sign, bias;  // radial
+  float r2;               // strip: (r0 / |c1 - c0|)^2
+  float f, r1, r1_square; // general
+  uint32_t mode;          // 0 transparent (a negative radius), 1 radial, 2 radial with equal
+                          // radii (transparent), 3 strip, 4 general
+  uint32_t swap01;        // general: the ends were swapped (t -> 1 - t)
+  uint32_t pad;
 };
 
 SKC_HD uint32_t GetA(uint32_t c) { return (c >> 24) & 0xFF; }
@@ -225,17 +243,77 @@ SKC_HD uint32_t GradientColor(const Brush& b, float current, const float4* color
   return ColorToPMColor(Color4fToColor(out.x, out.y, out.z, out.w));
 }
 
+// SweepGradientColorBrush::CalculateColor's parameter (sw_span_brush.cc:
+// 336-349) at the mapped point: the angle of (-y, -x) as a float
+// (std::atan2 on floats), then (angle / 2pi + 0.5 + bias) * scale in double
+// (0.5 is a double literal there).  The float angle is the double atan2
+// rounded to float.
+SKC_HD float SweepT(const Brush& b, float mx, float my) {
+  const float angle = (float)atan2d_((double)-my, (double)-mx);
+  const float k1Over2Pi = 0.1591549430918f;
+  return (float)(((double)(angle * k1Over2Pi) + 0.5 + (double)b.bias) * (double)b.scale);
+}
+
+// ConicalGradientColorBrush::CalculateConical (sw_span_brush.cc:441-507):
+// false when the pixel is transparent, else the gradient parameter.
+SKC_HD bool ConicalT(const ConicalParams& c, int x, int y, float* t_out) {
+  if (c.mode == 0 || c.mode == 2) return false;
+  const float sx = x + 0.5f, sy = y + 0.5f;
+  const float px = sx * c.d2l[0] + sy * c.d2l[1] + c.d2l[2];
+  const float py = sx * c.d2l[3] + sy * c.d2l[4] + c.d2l[5];
+  float t;
+  if (c.mode == 1) {
+    const float qx = (px - c.c0x) * c.scale, qy = (py - c.c0y) * c.scale;
+    t = sqrt_(qx * qx + qy * qy) * c.scale_sign - c.bias;
+  } else {
+    const float qx = px * c.t[0] + py * c.t[1] + c.t[2];
+    const float qy = px * c.t[3] + py * c.t[4] + c.t[5];
+    if (c.mode == 3) {
+      t = c.r2 - qy * qy;
+      if (t < 0.0f) return false;
+      t = (float)((double)qx + sqrtd_((double)t));  // sqrt of a float here is ::sqrt(double)
+    } else {
+      float xt = -1.f;
+      if (fabs_(c.r1 - 1.f) < 1.0f / (1 << 12)) {
+        xt = (qx * qx + qy * qy) / 2;
+      } else {
+        const float m = c.r1_square - 1.f;
+        const float delta = m * qy * qy + c.r1_square * qx * qx;
+        if (c.r1 > 1.f) {
+          xt = (sqrt_(delta) - qx) / m;
+        } else if (delta > 0) {
+          const float xt1 = (sqrt_(delta) - qx) / m;
+          const float xt2 = (-sqrt_(delta) - qx) / m;
+          xt = 1.f - c.f < 0 ? (xt2 < xt1 ? xt2 : xt1) : (xt1 < xt2 ? xt2 : xt1);
+        }
+      }
+      if (xt < 0) return false;
+      t = c.f + (1.f - c.f) * xt;
+      if (c.swap01) t = (float)(1.0 - (double)t);
+    }
+  }
+  *t_out = t;
+  return true;
+}
+
 // CalculateColor of the pass's brush at pixel (x, y), premultiplied ARGB.
 // roundtrip[v] = Color4fToColor(Color4fFromColor(v)) per channel, the
 // PixmapBrush sampler's colour round trip (bitmap_sampler.cc:21-29,93-107).
 SKC_HD uint32_t BrushColor(const Brush& b, int x, int y, const float4* colors, const float* offsets,
-                           const uint8_t* images, const uint8_t* roundtrip) {
+                           const uint8_t* images, const uint8_t* roundtrip,
+                           const ConicalParams* conicals) {
   if (b.kind == 0) return b.solid;
+  if (b.kind == 5) {
+    float t;
+    if (!ConicalT(conicals[b.conical], x, y, &t)) return 0;
+    return GradientColor(b, t, colors, offsets);
+  }
   float sx = x + 0.5f, sy = y + 0.5f;
   float mx = sx * b.m[0] + sy * b.m[1] + b.m[2];
   float my = sx * b.m[3] + sy * b.m[4] + b.m[5];
   if (b.kind == 1) return GradientColor(b, mx, colors, offsets);
   if (b.kind == 2) return GradientColor(b, sqrt_(mx * mx + my * my), colors, offsets);
+  if (b.kind == 4) return GradientColor(b, SweepT(b, mx, my), colors, offsets);
   // image brush, decal tiling, nearest sampling
   if (mx < 0.0f || mx >= 1.0f || my < 0.0f || my >= 1.0f) return 0;
   uint32_t ix = (uint32_t)(mx * (float)b.img_w), iy = (uint32_t)(my * (float)b.img_h);

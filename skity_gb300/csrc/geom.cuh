@@ -34,6 +34,7 @@ namespace skc {
 SKC_HD float fabs_(float x) { return fabsf(x); }
 SKC_HD float sqrt_(float x) { return sqrtf(x); }
 SKC_HD double sqrtd_(double x) { return sqrt(x); }
+SKC_HD double atan2d_(double y, double x) { return atan2(y, x); }
 SKC_HD float floor_(float x) { return floorf(x); }
 SKC_HD float ceil_(float x) { return ceilf(x); }
 SKC_HD double ceild_(double x) { return ceil(x); }
@@ -46,6 +47,7 @@ SKC_HD float round_(float x) { return roundf(x); }
 SKC_HD float fabs_(float x) { return std::fabs(x); }
 SKC_HD float sqrt_(float x) { return std::sqrt(x); }
 SKC_HD double sqrtd_(double x) { return std::sqrt(x); }
+SKC_HD double atan2d_(double y, double x) { return std::atan2(y, x); }
 SKC_HD float floor_(float x) { return std::floor(x); }
 SKC_HD float ceil_(float x) { return std::ceil(x); }
 SKC_HD double ceild_(double x) { return std::ceil(x); }

@@ -286,7 +286,8 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
           const bool is_short = xe - xs <= kShortSpan;
           if (mine_now && is_short) {
             for (int x = xs; x < xe; ++x) {
-              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip);
+              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
+                                      b.conicals);
               if (alpha != 255) c = AlphaMulQ(c, alpha);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);
@@ -300,7 +301,8 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
             const int qe = __shfl_sync(0xffffffffu, xe, j);
             const uint32_t qa = __shfl_sync(0xffffffffu, alpha, j);
             for (int x = qs + ((lane - qs) & 31); x < qe; x += 32) {
-              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip);
+              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
+                                      b.conicals);
               if (qa != 255) c = AlphaMulQ(c, qa);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);

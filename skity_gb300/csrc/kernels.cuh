@@ -121,6 +121,7 @@ struct DevBatch {
   uint64_t span_cap;   // its capacity in spans
   unsigned long long* span_next;  // pool chunk allocator
   const Brush* brushes;
+  const ConicalParams* conicals;  // per conical-gradient brush (Brush::conical)
   const float4* stop_colors;
   const float* stop_offsets;
   uint8_t* pixels;

@@ -768,7 +768,8 @@ SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* 
       int xs = max_(sx, x0), xe = min_(sx + slen, x1);
       uint32_t alpha = sp.y & br.global_alpha;
       for (int x = xs; x < xe; ++x) {
-        uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip);
+        uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip,
+                                b.conicals);
         if (alpha != 255) c = AlphaMulQ(c, alpha);
         row[x - x0] = BlendPixel(row[x - x0], c, br.blend);
       }

@@ -68,6 +68,8 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.brushes, hb.brushes, s));
   SKC_TRY(Upload(db.stop_colors, hb.stop_colors, s));
   SKC_TRY(Upload(db.stop_offsets, hb.stop_offsets, s));
+  if (hb.conicals.empty()) hb.conicals.push_back(ConicalParams{});
+  SKC_TRY(Upload(db.conicals, hb.conicals, s));
   SKC_TRY(Upload(db.temps, hb.temp_canvases, s));
   uint32_t maxw = 1;
   for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
@@ -409,6 +411,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
 
   // ---- composite temp canvases, blur, composite main canvases
   b.brushes = db.brushes.as<Brush>();
+  b.conicals = db.conicals.as<ConicalParams>();
   b.stop_colors = db.stop_colors.as<float4>();
   b.stop_offsets = db.stop_offsets.as<float>();
   b.pixels = db.pixels.as<uint8_t>();
@@ -455,7 +458,9 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     for (uint32_t p = 0; p < np; ++p) {
       st.spans += pspans[p];
       st.fragments += pfrags[p];
-      st.fragments_by_brush[hb.brushes[hb.passes[p].brush].kind & 3] += pfrags[p];
+      // sweep and two-point conical gradients count with the radial ones
+      const uint32_t kind = hb.brushes[hb.passes[p].brush].kind;
+      st.fragments_by_brush[kind >= 4 ? 2 : kind] += pfrags[p];
     }
   }
   db.stats = st;

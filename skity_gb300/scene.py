@@ -46,7 +46,7 @@ MITER_JOIN, ROUND_JOIN, BEVEL_JOIN = 0, 1, 2
 BLEND_CLEAR, BLEND_SRC, BLEND_DST, BLEND_SRC_OVER = 0, 1, 2, 3
 WINDING, EVEN_ODD = 0, 1
 TILE_CLAMP, TILE_REPEAT, TILE_MIRROR, TILE_DECAL = 0, 1, 2, 3
-GRAD_LINEAR, GRAD_RADIAL = 1, 2
+GRAD_LINEAR, GRAD_RADIAL, GRAD_SWEEP, GRAD_CONICAL = 1, 2, 3, 4
 BLUR_NONE, BLUR_NORMAL = 0, 1
 
 MAGIC = b"SKSC"

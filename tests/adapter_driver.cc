@@ -136,6 +136,13 @@ int main() {
   canvas->Restore();
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
+  // sweep and two-point conical shaders reach the C ABI as GradientInfo
+  paint.SetShader(Shader::MakeSweep(20, 15, 90, 270, colors, pos, 3, TileMode::kRepeat));
+  canvas->DrawPath(path, paint);
+  paint.SetShader(Shader::MakeTwoPointConical(Point{5, 6, 0, 1}, 2.f, Point{30, 20, 0, 1}, 12.f,
+                                              colors, nullptr, 3, TileMode::kClamp));
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
   canvas->Flush();
   std::printf("status=%d\n", canvas->LastStatus());
   canvas.reset();

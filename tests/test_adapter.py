@@ -76,4 +76,13 @@ def test_clip_rect_forwarded_other_clips_refused(driver_output):
     assert driver_output[21] == "status=-5"
     # after the Restores the canvas is unclipped and untranslated again
     assert driver_output[22].startswith("draw verbs=0,1,2,3,4,5,")
-    assert driver_output[23:] == ["status=0", "flush", "status=0", "destroy 0x10"]
+    assert driver_output[23] == "status=0"
+
+
+def test_sweep_and_conical_shaders_forwarded(driver_output):
+    # MakeSweep(20, 15, 90, 270): GradientInfo radius = (bias, scale) =
+    # (-0.25, 2); MakeTwoPointConical keeps both circles
+    sweep, conical = driver_output[24], driver_output[25]
+    assert "shader=3 tile=1 stops=3 offsets=1 p0=20,15" in sweep and "r=-0.25" in sweep
+    assert "shader=4 tile=0 stops=3 offsets=0 p0=5,6 p1=30,20 r=2" in conical
+    assert driver_output[26:] == ["status=0", "flush", "status=0", "destroy 0x10"]

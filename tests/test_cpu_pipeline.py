@@ -165,3 +165,12 @@ def test_every_blend_mode_bit_exact(cpu_pipeline, oracle_lib):
     got, _ = cpu_render(cpu_pipeline, sc)
     ref, _ = oracle_lib.render(sc)
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+def test_sweep_and_conical_gradients_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import sweep_conical_scene
+    sc = sweep_conical_scene()
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, ref)
+    assert c["bad_pixels"] == 0, c

@@ -243,3 +243,36 @@ def test_every_blend_mode_matches_oracle(gpu_ctx, oracle_lib):
     from test_oracle_pin import blend_modes_scene
     sc = blend_modes_scene()
     check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
+
+
+@pytest.mark.gpu
+def test_sweep_and_conical_gradients_match_oracle(gpu_ctx, oracle_lib):
+    """Shader::MakeSweep and MakeTwoPointConical through the batch entry point
+    and through the canvas API.  Bar as above; the sweep angle is the double
+    atan2 rounded to float, the float atan2 of the reference in all but
+    near-tie cases, so the run also records how many pixels are exact."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import sweep_conical_scene
+    from skity_gb300.canvas import Canvas, Paint, Path, Shader
+    sc = sweep_conical_scene()
+    c = check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
+    print("sweep/conical parity", c)
+    bitmap = np.zeros((60, 80, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    rect = Path().MoveTo(2, 2).LineTo(78, 3).LineTo(76, 58).LineTo(4, 55).Close()
+    cols = np.array([[1, 0, 0, 1], [0, 1, 0, 0.6], [0, 0, 1, 1]], np.float32)
+    shaders = [Shader.MakeSweep(40, 30, -30, 250, cols, None, 3),
+               Shader.MakeTwoPointConical((20, 20), 5.0, (50, 35), 30.0, cols, [0, 0.3, 1], 3, 2)]
+    sb = S.SceneBuilder(80, 60)
+    for sh in shaders:
+        paint = Paint().SetFillColor(0, 0, 0, 1)
+        paint.shader = sh
+        canvas.DrawPath(rect, paint)
+        p = S.default_paint()
+        p["gradient"] = sb.add_gradient(sh.kind, sh.p0, sh.p1, sh.radius, sh.colors, sh.pos,
+                                        tile_mode=sh.tile)
+        sb.draw_path(rect.verbs, rect.points, p)
+    canvas.Flush()
+    check(oracle_lib, bitmap, sb.build())

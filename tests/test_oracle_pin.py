@@ -170,3 +170,62 @@ def blend_modes_scene(seed=S.SEED_BASE + 395, width=120, height=96):
 
 def test_every_blend_mode(ref):
     _pin(ref, blend_modes_scene())
+
+
+def sweep_conical_scene(seed=S.SEED_BASE + 396, width=140, height=110):
+    """Sweep gradients (angle ranges within and past a turn, every tile
+    mode) and two-point conical gradients in each of the brush's cases --
+    general with the focal circle inside and outside, swapped ends (zero end
+    radius), equal radii (strip), concentric (radial), a negative radius
+    (transparent) -- on fills and strokes, some under a translation."""
+    from skity_gb300.canvas import Shader
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height)
+    cases = ["sweep", "general", "general_big", "swap", "strip", "radial", "negative"]
+    for i in range(6 * len(cases)):
+        case = cases[i % len(cases)]
+        n = 3 + i % 5
+        verbs = [S.MOVE] + [[S.LINE, S.QUAD, S.CUBIC][j % 3] for j in range(n)] + [S.CLOSE]
+        npts = 1 + sum({S.LINE: 1, S.QUAD: 2, S.CUBIC: 3}[v] for v in verbs[1:-1])
+        pts = rng.uniform(-10, [width + 10, height + 10], (npts, 2)).astype(np.float32)
+        p = S.default_paint()
+        p["style"] = S.STROKE if i % 5 == 4 else S.FILL
+        p["stroke_width"] = 3.0
+        if i % 4 == 1:
+            p["translate"] = tuple(rng.uniform(-15, 15, 2).astype(np.float32))
+        k = 2 + i % 4
+        cols = rng.uniform(0, 1, (k, 4)).astype(np.float32)
+        offs = None if i % 3 == 0 else np.sort(rng.uniform(0, 1, k)).astype(np.float32)
+        tile = (i // len(cases)) % 4
+        c0 = tuple(rng.uniform(0, [width, height]).astype(np.float32))
+        c1 = tuple(rng.uniform(0, [width, height]).astype(np.float32))
+        if case == "sweep":
+            a0 = float(rng.uniform(-180, 180))
+            sh = Shader.MakeSweep(c0[0], c0[1], a0, a0 + float(rng.uniform(20, 500)), cols, offs, k,
+                                  tile)
+        elif case == "general":
+            sh = Shader.MakeTwoPointConical(c0, float(rng.uniform(5, 20)), c1,
+                                            float(rng.uniform(25, 60)), cols, offs, k, tile)
+        elif case == "general_big":  # the start circle not inside the end one
+            sh = Shader.MakeTwoPointConical(c0, float(rng.uniform(30, 60)), c1,
+                                            float(rng.uniform(2, 10)), cols, offs, k, tile)
+        elif case == "swap":
+            sh = Shader.MakeTwoPointConical(c0, float(rng.uniform(10, 40)), c1, 0.0, cols, offs,
+                                            k, tile)
+        elif case == "strip":
+            r = float(rng.uniform(5, 30))
+            sh = Shader.MakeTwoPointConical(c0, r, c1, r, cols, offs, k, tile)
+        elif case == "radial":
+            sh = Shader.MakeTwoPointConical(c0, float(rng.uniform(5, 15)), c0,
+                                            float(rng.uniform(20, 50)), cols, offs, k, tile)
+        else:
+            sh = Shader.MakeTwoPointConical(c0, -5.0, c1, 30.0, cols, offs, k, tile)
+        assert sh is not None and sh.kind in (S.GRAD_SWEEP, S.GRAD_CONICAL), case
+        p["gradient"] = b.add_gradient(sh.kind, sh.p0, sh.p1, sh.radius, sh.colors, sh.pos,
+                                       tile_mode=sh.tile)
+        b.draw_path(verbs, pts, p)
+    return b.build()
+
+
+def test_sweep_and_conical_gradients(ref):
+    _pin(ref, sweep_conical_scene())
