@@ -111,7 +111,7 @@ typedef struct skity_cuda_paint {
   float stroke_width;
   float miter_limit;
   const skity_cuda_gradient* shader; /* NULL: solid colour */
-  uint32_t blur_style;  /* 0: no mask filter; BlurStyle (kNormal = 1) */
+  uint32_t blur_style;  /* 0: no mask filter; BlurStyle: 1 kNormal, 2 kSolid, 3 kOuter, 4 kInner */
   float blur_radius;    /* MaskFilter::MakeBlur radius */
 } skity_cuda_paint;
 

@@ -11,8 +11,8 @@
 // taken (the global clip bounds the base class keeps bound each draw's scan,
 // as SWCanvas::OnClipRect relies on, sw_canvas.cc:279-295).  Operations
 // outside the GPU raster path -- ClipPath, kDifference clips, layers, text,
-// images, canvas matrices other than translations, shader local matrices,
-// blur styles other than kNormal -- draw nothing and leave
+// images, canvas matrices other than translations, shader local matrices --
+// draw nothing and leave
 // SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus(); draws under a clip this
 // canvas did not take draw nothing either, until the Restore that drops it.
 #ifndef SKITY_GB300_ADAPTER_CUDA_CANVAS_HPP

@@ -519,7 +519,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     }
     if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
-    if (pr.blur_style != 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    if (pr.blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
     // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
     const float* p = s.pts + 2 * (size_t)s.po[d];
     uint32_t np = s.po[d + 1] - s.po[d];
@@ -559,6 +559,10 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     tc.has_clear = 1;
     tc.clear_pm = 0;
     tc.blur_radius = (int32_t)std::round(std::max(rad, rad));
+    tc.blur_style = pr.blur_style;
+    // MaskFilterOnFilter (mask_filter.cc:51-103): kNormal draws the blurred
+    // bitmap; the other styles combine it with the unblurred one, kept
+    tc.out_off = pr.blur_style == 1 ? tc.px_off : hb.AllocPixels((uint64_t)fw * fh * 4);
     hb.canvases.push_back(tc);
     hb.temp_canvases.push_back(tidx);
     hb.max_temp_w = std::max(hb.max_temp_w, fw);
@@ -594,7 +598,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     br.m[5] = m.e[3][1];
     br.img_w = fw;
     br.img_h = fh;
-    br.img_off = tc.px_off;
+    br.img_off = tc.out_off;
     hb.brushes.push_back(br);
     PassDesc pd;
     std::memset(&pd, 0, sizeof pd);

@@ -176,6 +176,21 @@ SKC_HD uint32_t BlendPixel(uint32_t dst, uint32_t src, uint32_t mode) {
   return PorterDuff(src, dst, mode);
 }
 
+// One pixel of MaskFilterOnFilter's combine (mask_filter.cc:61-100) for
+// BlurStyle kSolid (2), kOuter (3), kInner (4): raw = the unblurred draw,
+// blur = its StackBlur (both ARGB); returns the filtered pixel.
+SKC_HD uint32_t BlurStylePixel(uint32_t style, uint32_t raw, uint32_t blur) {
+  const uint32_t raw_a = GetA(raw), blur_a = GetA(blur);
+  if (style == 2) return raw_a > 0 ? raw : blur;
+  if (style == 3) return (raw_a > 0 && raw_a >= blur_a) ? 0u : blur;
+  if (style == 4) {
+    if (raw_a == 0) return 0;
+    const float a_factor = 1.f / 255.f;
+    return AlphaMulQ(blur, (uint32_t)(a_factor * raw_a * blur_a));
+  }
+  return blur;
+}
+
 SKC_HD float RemapFloatTile(float t, uint32_t tile) {  // sw_span_brush.cc:21-32
   if (tile == 0) {
     t = min_(max_(t, 0.0f), 1.0f);

@@ -369,13 +369,30 @@ __global__ void k_blur_v(DevBatch b, const uint32_t* temps, uint32_t n_temp, uin
   if (x >= cd.w) return;
   int r = min(cd.blur_radius, 254);
   const uint8_t* src = b.pixels + cd.blur_off + (size_t)x * 4;
-  uint8_t* dst = b.pixels + cd.px_off + (size_t)x * 4;
+  uint8_t* dst = b.pixels + cd.out_off + (size_t)x * 4;
   if (r <= 1) {
     for (uint32_t yy = 0; yy < cd.h; ++yy)
       for (int c = 0; c < 4; ++c) dst[(size_t)yy * cd.w * 4 + c] = src[(size_t)yy * cd.w * 4 + c];
     return;
   }
   BlurLine(src, dst, (int)cd.h, cd.w, r, true);
+}
+
+// MaskFilterOnFilter's styles (mask_filter.cc:61-100) for the temp canvases
+// that are not kNormal: the blurred image (out_off) against the unblurred
+// one (px_off), per pixel, in place in out_off.  One thread per pixel; the
+// grid's y is the temp canvas.
+__global__ void k_blur_style(DevBatch b, const uint32_t* temps, uint32_t n_temp) {
+  const uint32_t t = blockIdx.y;
+  if (t >= n_temp) return;
+  const CanvasDesc cd = b.canvases[temps[t]];
+  if (cd.blur_style <= 1) return;
+  const uint64_t n = (uint64_t)cd.w * cd.h;
+  const uint32_t* raw = (const uint32_t*)(b.pixels + cd.px_off);
+  uint32_t* out = (uint32_t*)(b.pixels + cd.out_off);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = ARGBtoRGBA(BlurStylePixel(cd.blur_style, RGBAtoARGB(raw[i]), RGBAtoARGB(out[i])));
 }
 
 int LaunchBlur(const DevBatch& b, const uint32_t* temps, uint32_t n_temp, uint32_t max_h,
@@ -385,7 +402,10 @@ int LaunchBlur(const DevBatch& b, const uint32_t* temps, uint32_t n_temp, uint32
   k_blur_h<<<gh, 64, 0, stream>>>(b, temps, n_temp, max_h);
   dim3 gv((max_w + 63) / 64, n_temp);
   k_blur_v<<<gv, 64, 0, stream>>>(b, temps, n_temp, max_w);
-  return 2;
+  const uint64_t px = (uint64_t)max_w * max_h;
+  dim3 gs((unsigned)std::min<uint64_t>((px + 255) / 256, 1024), n_temp);
+  k_blur_style<<<gs, 256, 0, stream>>>(b, temps, n_temp);
+  return 3;
 }
 
 }  // namespace skc

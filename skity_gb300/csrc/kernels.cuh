@@ -40,6 +40,10 @@ struct CanvasDesc {
   uint32_t pass0, pass1;
   int32_t blur_radius; // temp canvases: StackBlur radius (0 = not a temp)
   uint32_t band0;      // first entry of the canvas's row bands in band_off
+  uint32_t blur_style; // temp canvases: BlurStyle (1 normal, 2 solid, 3 outer, 4 inner)
+  uint32_t pad;
+  uint64_t out_off;    // temp canvases: the filtered image the draw samples (px_off for
+                       // kNormal, which blurs back in place; a third buffer otherwise)
 };
 
 // Rows of a canvas are grouped in bands of 1 << DevBatch::band_shift rows;

@@ -781,7 +781,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   if (need_p != path->point_count || need_w != path->conic_weight_count)
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
-  if (paint->blur_style > 1) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (paint->blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
   if (!skc::ValidPaint(paint->style, paint->cap, paint->join, paint->stroke_width,
                        paint->miter_limit, paint->blur_style ? paint->blur_radius : 0.f))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;

@@ -168,12 +168,18 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     }
     for (uint32_t x = 0; x < cd.w; ++x) {
       const uint8_t* src = pixels.data() + cd.blur_off + (size_t)x * 4;
-      uint8_t* dst = pixels.data() + cd.px_off + (size_t)x * 4;
+      uint8_t* dst = pixels.data() + cd.out_off + (size_t)x * 4;
       if (r <= 1) {
         for (uint32_t y = 0; y < cd.h; ++y) std::memcpy(dst + (size_t)y * cd.w * 4, src + (size_t)y * cd.w * 4, 4);
       } else {
         BlurLine(src, dst, (int)cd.h, cd.w, r, true);
       }
+    }
+    if (cd.blur_style > 1) {  // k_blur_style
+      const uint32_t* raw = (const uint32_t*)(pixels.data() + cd.px_off);
+      uint32_t* outp = (uint32_t*)(pixels.data() + cd.out_off);
+      for (uint64_t i = 0; i < (uint64_t)cd.w * cd.h; ++i)
+        outp[i] = ARGBtoRGBA(BlurStylePixel(cd.blur_style, RGBAtoARGB(raw[i]), RGBAtoARGB(outp[i])));
     }
   }
   BuildRowTasks(hb, hb.main_canvases, 65535, tasks);

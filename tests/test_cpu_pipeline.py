@@ -174,3 +174,12 @@ def test_sweep_and_conical_gradients_bit_exact(cpu_pipeline, oracle_lib):
     ref, _ = oracle_lib.render(sc)
     c = oracle_lib.compare(got, ref)
     assert c["bad_pixels"] == 0, c
+
+
+def test_blur_styles_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import blur_styles_scene
+    sc = blur_styles_scene()
+    got, st = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert st[4] > 0  # temp canvases
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0

@@ -276,3 +276,14 @@ def test_sweep_and_conical_gradients_match_oracle(gpu_ctx, oracle_lib):
         sb.draw_path(rect.verbs, rect.points, p)
     canvas.Flush()
     check(oracle_lib, bitmap, sb.build())
+
+
+@pytest.mark.gpu
+def test_blur_styles_match_oracle(gpu_ctx, oracle_lib):
+    """MaskFilter::MakeBlur with kNormal, kSolid, kOuter and kInner."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import blur_styles_scene
+    sc = blur_styles_scene()
+    c = check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
+    assert c["bad_pixels"] == 0

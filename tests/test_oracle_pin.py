@@ -229,3 +229,18 @@ def sweep_conical_scene(seed=S.SEED_BASE + 396, width=140, height=110):
 
 def test_sweep_and_conical_gradients(ref):
     _pin(ref, sweep_conical_scene())
+
+
+def blur_styles_scene(seed=S.SEED_BASE + 397):
+    """Blurred outlines with every BlurStyle (kNormal, kSolid, kOuter,
+    kInner) and their fills, over a cleared canvas."""
+    sc = S.config4(seed=seed, n_outlines=240, width=256, height=256, blur_frac=0.6)
+    blurred = np.nonzero(sc.paints["blur_style"] != 0)[0]
+    sc.paints["blur_style"][blurred] = 1 + (np.arange(len(blurred)) % 4)
+    return sc
+
+
+def test_blur_styles(ref):
+    sc = blur_styles_scene()
+    assert set(np.unique(sc.paints["blur_style"])) >= {1, 2, 3, 4}
+    _pin(ref, sc)
