@@ -99,6 +99,17 @@ typedef struct skity_cuda_gradient {
   const float* offsets; /* stop_count floats when has_offsets */
 } skity_cuda_gradient;
 
+/* A colour filter (include/skity/effect/color_filter.hpp, ColorFilters::*):
+ * the fields of the filter ColorFilterBase describes (src/effect/
+ * color_filter_base.hpp). */
+typedef struct skity_cuda_color_filter {
+  uint32_t type;       /* 1 Blend, 2 Matrix, 3 LinearToSRGBGamma, 4 SRGBToLinearGamma,
+                          5 Compose (the identity on the software path) */
+  uint32_t blend_mode; /* Blend: BlendMode */
+  uint32_t color;      /* Blend: Color, ARGB */
+  float matrix[20];    /* Matrix: row-major 4 x 5 */
+} skity_cuda_color_filter;
+
 /* The skity::Paint state the raster path reads (paint.hpp:46-285).
  * Colours are Color4f (unpremultiplied RGBA floats). */
 typedef struct skity_cuda_paint {
@@ -113,6 +124,7 @@ typedef struct skity_cuda_paint {
   const skity_cuda_gradient* shader; /* NULL: solid colour */
   uint32_t blur_style;  /* 0: no mask filter; BlurStyle: 1 kNormal, 2 kSolid, 3 kOuter, 4 kInner */
   float blur_radius;    /* MaskFilter::MakeBlur radius */
+  const skity_cuda_color_filter* color_filter; /* NULL: none */
 } skity_cuda_paint;
 
 typedef struct skity_cuda_context_create_info {

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <skity/effect/color_filter.hpp>
 #include <skity/effect/mask_filter.hpp>
 #include <skity/effect/shader.hpp>
 #include <skity/graphic/bitmap.hpp>
@@ -56,6 +57,11 @@ struct Scene {
   std::vector<GradRec> grads;
   std::vector<float> stop_colors, stop_offsets;
   std::vector<float> clips;  // per draw device-space (l, t, r, b), when present
+  struct Filter {
+    uint32_t type, mode, color, pad;
+    float matrix[20];
+  };
+  std::vector<Filter> filters;  // per draw colour filter, when present
 };
 
 template <typename T>
@@ -98,6 +104,7 @@ bool Load(const char* path, Scene* s) {
   Take(buf, o, s->stop_colors, 4 * size_t(cnt[5]));
   Take(buf, o, s->stop_offsets, cnt[5]);
   if (flags & 1) Take(buf, o, s->clips, 4 * size_t(nd));
+  if (flags & 2) Take(buf, o, s->filters, nd);
   return o <= buf.size();
 }
 
@@ -167,6 +174,28 @@ skity::Paint BuildPaint(const Scene& s, uint32_t d) {
           skity::Point{g.p0[0], g.p0[1], 0, 1}, g.radius[0],
           skity::Point{g.p1[0], g.p1[1], 0, 1}, g.radius[1], colors.data(), pos,
           int(g.stop_count), tile, 0));
+    }
+  }
+  if (!s.filters.empty() && s.filters[d].type != 0) {
+    const Scene::Filter& f = s.filters[d];
+    using skity::ColorFilters;
+    switch (f.type) {
+      case 1:
+        paint.SetColorFilter(ColorFilters::Blend(f.color, static_cast<skity::BlendMode>(f.mode)));
+        break;
+      case 2:
+        paint.SetColorFilter(ColorFilters::Matrix(f.matrix));
+        break;
+      case 3:
+        paint.SetColorFilter(ColorFilters::LinearToSRGBGamma());
+        break;
+      case 4:
+        paint.SetColorFilter(ColorFilters::SRGBToLinearGamma());
+        break;
+      default:  // a composition (of two gamma filters)
+        paint.SetColorFilter(ColorFilters::Compose(ColorFilters::LinearToSRGBGamma(),
+                                                   ColorFilters::SRGBToLinearGamma()));
+        break;
     }
   }
   if (r.blur_style != 0) {

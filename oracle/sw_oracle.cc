@@ -1620,6 +1620,72 @@ static bool ConicalParam(const Conical& c, const Mat& d2l, int x, int y, float* 
   return true;
 }
 
+// A paint's colour filter (src/effect/color_filter.cc:56-186), as the
+// stream records it: type 0 none, 1 blend, 2 matrix, 3 linear->sRGB,
+// 4 sRGB->linear, 5 compose.
+struct FilterRec {
+  uint32_t type, mode, color, pad;
+  float matrix[20];
+};
+static_assert(sizeof(FilterRec) == 96, "colour filter layout");
+
+// UnPreMultiply::g_table_ (color_priv.cc:52-95): entry a is 255 * 2^24 / a,
+// rounded to nearest.
+static uint32_t UnpremulScale(uint32_t a) {
+  return a == 0 ? 0u : (uint32_t)((((uint64_t)255 << 24) + a / 2) / a);
+}
+static uint32_t PMColorToColor(uint32_t c) {  // color_priv.cc:97-103
+  uint32_t a = GetA(c), scale = UnpremulScale(a);
+  auto apply = [&](uint32_t v) -> uint32_t { return (scale * v + (1u << 23)) >> 24; };
+  return ColorSetARGB(a, apply(GetR(c)), apply(GetG(c)), apply(GetB(c)));
+}
+
+// The sRGB transfer tables of SRGBGammaColorFilter (color_filter.cc:121-166),
+// rebuilt from the transfer functions: floor(255 * f(i / 255)), the argument
+// and the product in float, f in double.
+struct SRGBTables {
+  uint8_t to_srgb[256], to_linear[256];
+  SRGBTables() {
+    for (int i = 0; i < 256; ++i) {
+      float x = i / 255.f;
+      double xd = x;
+      double e = xd <= 0.0031308 ? 12.92 * xd : 1.055 * std::pow(xd, 1 / 2.4) - 0.055;
+      double l = xd <= 0.04045 ? xd / 12.92 : std::pow((xd + 0.055) / 1.055, 2.4);
+      to_srgb[i] = (uint8_t)std::floor((float)e * 255.f);
+      to_linear[i] = (uint8_t)std::floor((float)l * 255.f);
+    }
+  }
+};
+
+static uint32_t ApplyColorFilter(const FilterRec* f, uint32_t c) {
+  if (!f) return c;
+  switch (f->type) {
+    case 1:  // BlendColorFilter::OnFilterColor
+      return PorterDuffBlend(ColorToPMColor(f->color), c, (int)f->mode);
+    case 2: {  // MatrixColorFilter::OnFilterColor
+      int16_t m[4][5];
+      for (int i = 0; i < 20; ++i) m[i / 5][i % 5] = (int16_t)(f->matrix[i] * 255);
+      uint32_t src = PMColorToColor(c);
+      int32_t v[4] = {(int32_t)GetR(src), (int32_t)GetG(src), (int32_t)GetB(src), (int32_t)GetA(src)};
+      uint8_t out[4];
+      for (int i = 0; i < 4; ++i) {
+        int32_t mul = v[0] * m[i][0] + v[1] * m[i][1] + v[2] * m[i][2] + v[3] * m[i][3];
+        out[i] = (uint8_t)std::clamp(mul / 255 + m[i][4], 0, 255);
+      }
+      return ColorToPMColor(ColorSetARGB(out[3], out[0], out[1], out[2]));
+    }
+    case 3:
+    case 4: {  // SRGBGammaColorFilter::OnFilterColor
+      static const SRGBTables tables;
+      const uint8_t* t = f->type == 3 ? tables.to_srgb : tables.to_linear;
+      uint32_t src = PMColorToColor(c);
+      return ColorToPMColor(ColorSetARGB(GetA(src), t[GetR(src)], t[GetG(src)], t[GetB(src)]));
+    }
+    default:  // none; ComposeColorFilter::OnFilterColor returns its input
+      return c;
+  }
+}
+
 struct Brush {
   int kind = 0;  // 0 solid, 1 linear, 2 radial, 3 sweep, 4 two-point conical
   uint32_t solid = 0;
@@ -1628,6 +1694,7 @@ struct Brush {
   Mat d2l = Mat::Identity();  // conical: device_to_local, mapped before its own transforms
   Conical con{};
   uint8_t global_alpha = 255;
+  const FilterRec* filter = nullptr;  // the paint's colour filter
 
   uint32_t ColorAt(int x, int y) const {
     if (kind == 0) return solid;
@@ -1728,6 +1795,7 @@ static uint64_t BrushSpans(const std::vector<Span>& spans, const Brush& br, int 
     for (int i = 0; i < len; ++i) {
       uint32_t c = br.ColorAt(x + i, y);
       if (alpha != 255) c = AlphaMulQ(c, alpha);
+      c = ApplyColorFilter(br.filter, c);
       t->Blend(x + i, y, c, mode);
     }
   }
@@ -1765,7 +1833,15 @@ struct SceneView {
   const GradRec* grads;
   const float *stop_colors, *stop_offsets;
   const float* clips;  // per draw (l, t, r, b) when the stream has the clip section
+  const FilterRec* filters;  // per draw colour filter when the stream has that section
 };
+
+// The colour filter of the draw whose paint record is `p` (a record of s).
+static const FilterRec* FilterOf(const SceneView& s, const PaintRec& p) {
+  if (!s.filters) return nullptr;
+  const size_t d = (size_t)(&p - s.paints);
+  return d < s.nd && s.filters[d].type != 0 ? &s.filters[d] : nullptr;
+}
 
 static Clip ClipOf(const SceneView& s, uint32_t d) {
   Clip c;
@@ -1786,8 +1862,8 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
-  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds follow the stops
-  if (flags & ~1u) return false;
+  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds, 2: per-draw colour filters
+  if (flags & ~3u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -1812,6 +1888,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->stop_colors = (const float*)at(16 * (size_t)cnt[5]);
   s->stop_offsets = (const float*)at(4 * (size_t)cnt[5]);
   s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
+  s->filters = (flags & 2) ? (const FilterRec*)at(sizeof(FilterRec) * s->nd) : nullptr;
   return o <= len;
 }
 
@@ -1869,10 +1946,12 @@ static Brush MakeBrush(const SceneView& s, const PaintRec& p, bool stroke) {
     std::memcpy(br.g.radius, g.radius, 8);
     br.m = PointsToUnit(br.g);
     if (br.kind == 4) br.con = ConicalPreBrush(br.g);
+    br.filter = FilterOf(s, p);
     return br;
   }
   br.kind = 0;
   br.solid = ColorToPMColor(Color4fToColor(stroke ? p.stroke_color : p.fill_color));
+  br.filter = FilterOf(s, p);
   return br;
 }
 

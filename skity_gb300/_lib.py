@@ -42,12 +42,18 @@ class Gradient_(ctypes.Structure):
                 ("offsets", ctypes.c_void_p)]
 
 
+class ColorFilter_(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("blend_mode", ctypes.c_uint32),
+                ("color", ctypes.c_uint32), ("matrix", ctypes.c_float * 20)]
+
+
 class Paint_(ctypes.Structure):
     _fields_ = [("style", ctypes.c_uint32), ("cap", ctypes.c_uint32), ("join", ctypes.c_uint32),
                 ("blend_mode", ctypes.c_uint32), ("fill_color", ctypes.c_float * 4),
                 ("stroke_color", ctypes.c_float * 4), ("stroke_width", ctypes.c_float),
                 ("miter_limit", ctypes.c_float), ("shader", ctypes.POINTER(Gradient_)),
-                ("blur_style", ctypes.c_uint32), ("blur_radius", ctypes.c_float)]
+                ("blur_style", ctypes.c_uint32), ("blur_radius", ctypes.c_float),
+                ("color_filter", ctypes.POINTER(ColorFilter_))]
 
 
 class ContextInfo_(ctypes.Structure):

@@ -2,11 +2,14 @@
 #include "cuda_canvas.hpp"
 
 #include <cstring>
+#include <skity/effect/color_filter.hpp>
 #include <skity/effect/mask_filter.hpp>
 #include <skity/effect/shader.hpp>
 #include <skity/graphic/paint.hpp>
 #include <skity/graphic/path.hpp>
 #include <vector>
+
+#include "src/effect/color_filter_base.hpp"  // the filter kinds and their parameters
 
 namespace skity {
 namespace cuda {
@@ -119,6 +122,45 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
     g.colors = colors.data();
     g.offsets = offsets.empty() ? nullptr : offsets.data();
     q.shader = &g;
+  }
+  skity_cuda_color_filter cf{};
+  if (const ColorFilter* f = paint.GetColorFilter().get()) {
+    const ColorFilterBase* base = As_CFB(f);
+    switch (base->GetType()) {
+      case ColorFilterType::kBlend: {
+        const auto* b = static_cast<const BlendColorFilter*>(base);
+        cf.type = 1;
+        cf.blend_mode = static_cast<uint32_t>(b->GetBlendMode());
+        cf.color = b->GetColor();
+        break;
+      }
+      case ColorFilterType::kMatrix: {
+        // GetMatrix: columns of the 4 x 4 part, then the bias column
+        auto mm = const_cast<MatrixColorFilter*>(static_cast<const MatrixColorFilter*>(base))
+                      ->GetMatrix();
+        const Matrix& mul = std::get<0>(mm);
+        const Vec4& add = std::get<1>(mm);
+        cf.type = 2;
+        for (int r = 0; r < 4; ++r) {
+          for (int c = 0; c < 4; ++c) cf.matrix[5 * r + c] = mul.Get(r, c);
+        }
+        cf.matrix[4] = add.x;
+        cf.matrix[9] = add.y;
+        cf.matrix[14] = add.z;
+        cf.matrix[19] = add.w;
+        break;
+      }
+      case ColorFilterType::kLinearToSRGBGamma:
+        cf.type = 3;
+        break;
+      case ColorFilterType::kSRGBToLinearGamma:
+        cf.type = 4;
+        break;
+      default:
+        cf.type = 5;  // compose: the identity on the software path
+        break;
+    }
+    q.color_filter = &cf;
   }
   if (const MaskFilter* mf = paint.GetMaskFilter().get()) {
     q.blur_style = static_cast<uint32_t>(mf->GetBlurStyle());

@@ -171,6 +171,58 @@ class Shader:
                       tile_mode)
 
 
+class ColorFilter:
+    """A colour filter as ColorFilterBase describes it (src/effect/
+    color_filter_base.hpp): kind scene.FILTER_*, blend mode and ARGB colour,
+    or the 20 row-major matrix terms."""
+
+    def __init__(self, kind, mode=0, color=0, matrix=None):
+        self.kind, self.mode, self.color = kind, mode, color
+        self.matrix = None if matrix is None else [float(v) for v in np.asarray(matrix, np.float32).reshape(20)]
+
+    def record(self):
+        return S.filter_record(self.kind, self.mode, self.color, self.matrix)
+
+
+class ColorFilters:
+    """ColorFilters (include/skity/effect/color_filter.hpp; factories in
+    src/effect/color_filter.cc:61-106)."""
+
+    @staticmethod
+    def Blend(color, mode):
+        a = (int(color) >> 24) & 0xFF
+        if mode == BlendMode.kDst or (mode == BlendMode.kDstIn and a == 255) or \
+                (mode == BlendMode.kDstOut and a == 0):
+            return None
+        return ColorFilter(S.FILTER_BLEND, mode, int(color) & 0xFFFFFFFF)
+
+    @staticmethod
+    def Matrix(row_major):
+        if row_major is None:
+            return None
+        m = np.asarray(row_major, np.float32).reshape(20)
+        if np.array_equal(m, np.array([1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0],
+                                      np.float32)):
+            return None
+        return ColorFilter(S.FILTER_MATRIX, matrix=m)
+
+    @staticmethod
+    def LinearToSRGBGamma():
+        return ColorFilter(S.FILTER_LINEAR_TO_SRGB)
+
+    @staticmethod
+    def SRGBToLinearGamma():
+        return ColorFilter(S.FILTER_SRGB_TO_LINEAR)
+
+    @staticmethod
+    def Compose(outer, inner):
+        if inner is None:
+            return outer
+        if outer is None:
+            return inner
+        return ColorFilter(S.FILTER_COMPOSE)
+
+
 class MaskFilter:
     def __init__(self, style, radius):
         self.style, self.radius = style, radius
@@ -185,6 +237,7 @@ class Paint:
         self.rec = S.default_paint()
         self.shader: Shader | None = None
         self.mask_filter: MaskFilter | None = None
+        self.color_filter: ColorFilter | None = None
 
     def SetStyle(self, s): self.rec["style"] = s; return self
     def SetStrokeWidth(self, w): self.rec["stroke_width"] = w; return self
@@ -192,6 +245,7 @@ class Paint:
     def SetStrokeCap(self, c): self.rec["cap"] = c; return self
     def SetStrokeJoin(self, j): self.rec["join"] = j; return self
     def SetBlendMode(self, m): self.rec["blend"] = m; return self
+    def SetColorFilter(self, f): self.color_filter = f; return self
     def SetShader(self, s): self.shader = s; return self
     def SetMaskFilter(self, m): self.mask_filter = m; return self
 
@@ -365,6 +419,14 @@ class Canvas:
         if paint.mask_filter is not None:
             cpaint.blur_style = paint.mask_filter.style
             cpaint.blur_radius = paint.mask_filter.radius
+        if paint.color_filter is not None:
+            cf = _lib.ColorFilter_()
+            cf.type, cf.blend_mode, cf.color = (paint.color_filter.kind, paint.color_filter.mode,
+                                                paint.color_filter.color)
+            if paint.color_filter.matrix is not None:
+                cf.matrix[:] = paint.color_filter.matrix
+            keep.append(cf)
+            cpaint.color_filter = ctypes.pointer(cf)
         _lib.check(self.lib.skity_cuda_canvas_draw_path(self.handle, ctypes.byref(cp),
                                                         ctypes.byref(cpaint)),
                    "skity_cuda_canvas_draw_path")

@@ -41,6 +41,14 @@ struct GradRec {
   float p0[2], p1[2], radius[2];
 };
 static_assert(sizeof(GradRec) == 48, "gradient layout");
+// A paint's colour filter (include/skity/effect/color_filter.hpp): type 0
+// none, else 1 + ColorFilterType (1 blend, 2 matrix, 3 linear->sRGB gamma,
+// 4 sRGB->linear gamma, 5 compose).
+struct ColorFilterRec {
+  uint32_t type, mode, color, pad;  // blend: BlendMode and ARGB colour
+  float matrix[20];                 // matrix: row-major 4 x 5
+};
+static_assert(sizeof(ColorFilterRec) == 96, "colour filter layout");
 
 struct StreamView {
   uint32_t width, height, has_clear;
@@ -53,6 +61,7 @@ struct StreamView {
   const GradRec* grads;
   const float *stop_colors, *stop_offsets;
   const float* clips;  // per draw device-space clip bounds (l, t, r, b), or null: none
+  const ColorFilterRec* filters;  // per draw colour filter, or null: none
 };
 
 // A draw the device code can take: the verb sequence of a skity::Path
@@ -121,6 +130,31 @@ inline bool IsNoClip(const float c[4]) {
   return c[0] == -1e9f && c[1] == -1e9f && c[2] == 1e9f && c[3] == 1e9f;
 }
 
+// A colour filter record: a known type, a blend mode up to kLuminosity, and
+// matrix terms whose int16 form (term * 255) is defined.
+inline bool ValidColorFilter(const ColorFilterRec& f) {
+  if (f.type > 5 || f.mode > 28) return false;
+  if (f.type == 2) {
+    for (float v : f.matrix)
+      if (!(std::fabs(v * 255) < 32767.f)) return false;
+  }
+  return true;
+}
+
+// SRGBGammaColorFilter's tables (color_filter.cc:121-166), from the sRGB
+// transfer functions: entry i = floor(255 * f(i / 255)), with i / 255 and the
+// product in float and f in double.
+inline void SRGBTables(uint8_t out[512]) {
+  for (int i = 0; i < 256; ++i) {
+    const float x = i / 255.f;
+    const double xd = x;
+    const double enc = xd <= 0.0031308 ? 12.92 * xd : 1.055 * std::pow(xd, 1 / 2.4) - 0.055;
+    const double dec = xd <= 0.04045 ? xd / 12.92 : std::pow((xd + 0.055) / 1.055, 2.4);
+    out[i] = (uint8_t)std::floor((float)enc * 255.f);
+    out[256 + i] = (uint8_t)std::floor((float)dec * 255.f);
+  }
+}
+
 inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   if (!buf || len < 72 || std::memcmp(buf, "SKSC", 4) != 0) return false;
   uint32_t hdr[7];
@@ -129,8 +163,9 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
-  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds follow the stops
-  if (flags & ~1u) return false;
+  // 1: per-draw clip bounds follow the stops; 2: then per-draw colour filters
+  const uint32_t flags = hdr[4];
+  if (flags & ~3u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -160,6 +195,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->stop_colors = (const float*)at(16 * (size_t)s->ns);
   s->stop_offsets = (const float*)at(4 * (size_t)s->ns);
   s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
+  s->filters = (flags & 2) ? (const ColorFilterRec*)at(sizeof(ColorFilterRec) * s->nd) : nullptr;
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
   for (uint32_t d = 0; d < s->nd; ++d) {
@@ -173,6 +209,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
     if (!ValidTranslate(pr.translate, s->pts + 2 * (size_t)s->po[d], s->po[d + 1] - s->po[d]))
       return false;
     if (s->clips && !ValidClip(s->clips + 4 * (size_t)d)) return false;
+    if (s->filters && !ValidColorFilter(s->filters[d])) return false;
     if (!ValidPath(s->verbs + s->vo[d], s->vo[d + 1] - s->vo[d], s->pts + 2 * (size_t)s->po[d],
                    s->po[d + 1] - s->po[d], s->wts + s->wo[d], s->wo[d + 1] - s->wo[d]))
       return false;
@@ -308,6 +345,7 @@ struct HostBatch {
   std::vector<PassDesc> passes;
   std::vector<Brush> brushes;
   std::vector<ConicalParams> conicals;
+  std::vector<int16_t> cf_matrices;  // colour-filter matrices, 20 terms each
   std::vector<CanvasDesc> canvases;
   std::vector<float4> stop_colors;
   std::vector<float> stop_offsets;
@@ -391,6 +429,32 @@ inline void DerivedCaps(int32_t cap[13], bool stroke) {
   }
 }
 
+// The paint's colour filter on a brush (SWSpanBrush applies it to each
+// covered colour before blending, sw_span_brush.cc:108-136).  Compose is
+// the identity on this path (ComposeColorFilter::OnFilterColor,
+// color_filter.cc:182-186).
+inline void SetColorFilter(HostBatch& hb, const StreamView& s, uint32_t d, Brush* br) {
+  br->cf_type = 0;
+  if (!s.filters) return;
+  const ColorFilterRec& f = s.filters[d];
+  if (f.type == 1) {  // BlendColorFilter (color_filter.cc:109-111)
+    br->cf_type = 1;
+    br->cf_mode = f.mode;
+    br->cf_pm = ColorToPMColor(f.color);
+  } else if (f.type == 2) {  // MatrixColorFilter: int16 terms = row_major * 255 (truncated)
+    br->cf_type = 2;
+    br->cf_index = (uint32_t)hb.cf_matrices.size();
+    for (int i = 0; i < 20; ++i) hb.cf_matrices.push_back((int16_t)(f.matrix[i] * 255));
+  } else if (f.type == 3 || f.type == 4) {
+    br->cf_type = f.type;
+  }
+}
+
+// The draw has a colour filter that is not the identity (Compose is, here).
+inline bool FiltersColor(const StreamView& s, uint32_t d) {
+  return s.filters && s.filters[d].type != 0 && s.filters[d].type != 5;
+}
+
 // Appends the passes of one DrawPath (fill/stroke in paint order) to `out`.
 inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
                           uint32_t canvas, float tx, float ty, std::vector<PassDesc>& out) {
@@ -455,6 +519,7 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
       br.kind = 0;
       br.solid = SolidPM(stroke ? pr.stroke_color : pr.fill_color);
     }
+    SetColorFilter(hb, s, d, &br);
     hb.brushes.push_back(br);
     return (uint32_t)hb.brushes.size() - 1;
   };
@@ -463,8 +528,10 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     std::memset(&pd, 0, sizeof pd);
     pd.draw = draw_index;
     pd.canvas = canvas;
+    // kPassSrcOver lets the sweep drop spans of zero coverage (a no-op under
+    // src-over) -- unless a colour filter can turn transparent into a colour
     pd.flags = (stroke ? kPassStroke : 0) | ((!stroke && pr.fill_type == 1) ? kPassEvenOdd : 0) |
-               (pr.blend == 3 ? kPassSrcOver : 0);
+               ((pr.blend == 3 && !FiltersColor(s, d)) ? kPassSrcOver : 0);
     pd.cap_join = (pr.cap & 0xFF) | ((pr.join & 0xFF) << 8);
     pd.tx = tx;
     pd.ty = ty;
@@ -599,12 +666,13 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     br.img_w = fw;
     br.img_h = fh;
     br.img_off = tc.out_off;
+    SetColorFilter(hb, s, d, &br);  // the image draw's paint keeps the filter
     hb.brushes.push_back(br);
     PassDesc pd;
     std::memset(&pd, 0, sizeof pd);
     pd.draw = rect;
     pd.canvas = cidx;
-    pd.flags = pr.blend == 3 ? kPassSrcOver : 0;
+    pd.flags = (pr.blend == 3 && !FiltersColor(s, d)) ? kPassSrcOver : 0;
     pd.brush = (uint32_t)hb.brushes.size() - 1;
     pd.ga = br.global_alpha;
     pd.stroke_width = 1.f;

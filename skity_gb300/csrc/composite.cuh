@@ -21,6 +21,11 @@ struct Brush {
   uint64_t img_off;       // byte offset of the source pixels (RGBA8 rows)
   float bias, scale;      // sweep: GradientInfo::radius (bias, scale of the angle)
   uint32_t conical;       // conical: index of its ConicalParams
+  uint32_t cf_type;       // colour filter: 0 none, 1 blend, 2 matrix, 3 linear->sRGB,
+                          // 4 sRGB->linear (compose is the identity on this path)
+  uint32_t cf_mode;       // blend filter: BlendMode
+  uint32_t cf_pm;         // blend filter: its colour, premultiplied
+  uint32_t cf_index;      // matrix filter: first of its 20 int16 terms in DevBatch::cf_matrices
   uint32_t pad;
 };
 
@@ -189,6 +194,48 @@ SKC_HD uint32_t BlurStylePixel(uint32_t style, uint32_t raw, uint32_t blur) {
     return AlphaMulQ(blur, (uint32_t)(a_factor * raw_a * blur_a));
   }
   return blur;
+}
+
+// PMColorToColor (color_priv.cc:20-104): channel * (255 << 24) / a, rounded,
+// as UnPreMultiply's scale table holds it (entry a = round(255 * 2^24 / a)).
+SKC_HD uint32_t UnpremulScale(uint32_t a) {
+  return a == 0 ? 0u : (uint32_t)(((255ull << 24) + a / 2) / a);
+}
+SKC_HD uint32_t PMColorToColor(uint32_t c) {
+  const uint32_t a = GetA(c), s = UnpremulScale(a);
+  auto ch = [&](uint32_t v) { return (s * v + (1u << 23)) >> 24; };  // uint32 arithmetic
+  return ARGB(a, ch(GetR(c)), ch(GetG(c)), ch(GetB(c)));
+}
+
+// ColorFilter::FilterColor (color_filter.cc:56-186) of a premultiplied
+// colour.  tables: [0, 256) linear->sRGB, [256, 512) sRGB->linear;
+// matrices: int16 terms (row_major * 255, truncated), 4 rows of 5.
+SKC_HD uint32_t FilterColor(const Brush& b, uint32_t c, const uint8_t* tables,
+                            const int16_t* matrices) {
+  switch (b.cf_type) {
+    case 1:  // BlendColorFilter: PorterDuffBlend(filter colour, c, mode)
+      return PorterDuff(b.cf_pm, c, b.cf_mode);
+    case 2: {  // MatrixColorFilter
+      const uint32_t u = PMColorToColor(c);
+      const int32_t v[4] = {(int32_t)GetR(u), (int32_t)GetG(u), (int32_t)GetB(u), (int32_t)GetA(u)};
+      const int16_t* m = matrices + b.cf_index;
+      uint32_t o[4];
+      for (int i = 0; i < 4; ++i) {
+        const int32_t mul = v[0] * m[5 * i] + v[1] * m[5 * i + 1] + v[2] * m[5 * i + 2] +
+                            v[3] * m[5 * i + 3];
+        o[i] = (uint32_t)min_(max_(mul / 255 + m[5 * i + 4], 0), 255);
+      }
+      return ColorToPMColor(ARGB(o[3], o[0], o[1], o[2]));
+    }
+    case 3:
+    case 4: {  // SRGBGammaColorFilter
+      const uint32_t u = PMColorToColor(c);
+      const uint8_t* t = tables + (b.cf_type == 3 ? 0 : 256);
+      return ColorToPMColor(ARGB(GetA(u), t[GetR(u)], t[GetG(u)], t[GetB(u)]));
+    }
+    default:
+      return c;
+  }
 }
 
 SKC_HD float RemapFloatTile(float t, uint32_t tile) {  // sw_span_brush.cc:21-32

@@ -57,7 +57,7 @@ struct DeviceBatch {
   Context* ctx = nullptr;
   HostBatch hb;
   DevBuf verbs, pts, weights, draws, passes, canvases, brushes, stop_colors, stop_offsets;
-  DevBuf conicals;
+  DevBuf conicals, cf_matrices, srgb_tables;
   DevBuf scratch, geom, sweep, sweepmem, rowspan, pass_spans, comp, pixels;
   DevBuf tasks_main, tasks_temp, temps, pass_list, roundtrip, pass_frags, err, pass_class;
   DevBuf band_off, bins, sweep_order;

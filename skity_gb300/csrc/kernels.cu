@@ -289,6 +289,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
               uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
                                       b.conicals);
               if (alpha != 255) c = AlphaMulQ(c, alpha);
+              if (br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);
             }
@@ -304,6 +305,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
               uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
                                       b.conicals);
               if (qa != 255) c = AlphaMulQ(c, qa);
+              if (br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
               uint32_t& d = row[x - x0];
               d = BlendPixel(d, c, br.blend);
             }

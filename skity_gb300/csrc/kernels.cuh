@@ -126,6 +126,8 @@ struct DevBatch {
   unsigned long long* span_next;  // pool chunk allocator
   const Brush* brushes;
   const ConicalParams* conicals;  // per conical-gradient brush (Brush::conical)
+  const uint8_t* srgb_tables;     // colour filters: linear->sRGB, sRGB->linear (256 each)
+  const int16_t* cf_matrices;     // colour filters: matrix terms (Brush::cf_index)
   const float4* stop_colors;
   const float* stop_offsets;
   uint8_t* pixels;

@@ -771,6 +771,7 @@ SKC_HDN void CompositeRowScalar(const DevBatch& b, const RowTask& rt, uint32_t* 
         uint32_t c = BrushColor(br, x, y, b.stop_colors, b.stop_offsets, b.pixels, b.roundtrip,
                                 b.conicals);
         if (alpha != 255) c = AlphaMulQ(c, alpha);
+        if (br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
         row[x - x0] = BlendPixel(row[x - x0], c, br.blend);
       }
     }

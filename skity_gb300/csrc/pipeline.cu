@@ -70,6 +70,13 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   SKC_TRY(Upload(db.stop_offsets, hb.stop_offsets, s));
   if (hb.conicals.empty()) hb.conicals.push_back(ConicalParams{});
   SKC_TRY(Upload(db.conicals, hb.conicals, s));
+  if (hb.cf_matrices.empty()) hb.cf_matrices.push_back(0);
+  SKC_TRY(Upload(db.cf_matrices, hb.cf_matrices, s));
+  {
+    std::vector<uint8_t> tables(512);
+    SRGBTables(tables.data());
+    SKC_TRY(Upload(db.srgb_tables, tables, s));
+  }
   SKC_TRY(Upload(db.temps, hb.temp_canvases, s));
   uint32_t maxw = 1;
   for (uint32_t c : hb.main_canvases) maxw = std::max(maxw, hb.canvases[c].w);
@@ -412,6 +419,8 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   // ---- composite temp canvases, blur, composite main canvases
   b.brushes = db.brushes.as<Brush>();
   b.conicals = db.conicals.as<ConicalParams>();
+  b.srgb_tables = db.srgb_tables.as<uint8_t>();
+  b.cf_matrices = db.cf_matrices.as<int16_t>();
   b.stop_colors = db.stop_colors.as<float4>();
   b.stop_offsets = db.stop_offsets.as<float>();
   b.pixels = db.pixels.as<uint8_t>();
@@ -525,6 +534,8 @@ struct skity_cuda_canvas_s {
   std::vector<State> saved;
   std::vector<float> clips;  // per recorded draw: its clip bounds
   bool any_clip = false;
+  std::vector<skc::ColorFilterRec> filters;  // per recorded draw: its colour filter
+  bool any_filter = false;
   skc::DeviceBatch db;
 };
 
@@ -754,6 +765,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
   canvas->stop_offsets.clear();
   canvas->clips.clear();
   canvas->any_clip = false;
+  canvas->filters.clear();
+  canvas->any_filter = false;
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -781,6 +794,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   if (need_p != path->point_count || need_w != path->conic_weight_count)
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
+  if (paint->color_filter) {
+    skc::ColorFilterRec fr;
+    std::memset(&fr, 0, sizeof fr);
+    fr.type = paint->color_filter->type;
+    fr.mode = paint->color_filter->blend_mode;
+    std::memcpy(fr.matrix, paint->color_filter->matrix, sizeof fr.matrix);
+    if (fr.type == 0 || !skc::ValidColorFilter(fr)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  }
   if (paint->blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
   if (!skc::ValidPaint(paint->style, paint->cap, paint->join, paint->stroke_width,
                        paint->miter_limit, paint->blur_style ? paint->blur_radius : 0.f))
@@ -842,6 +863,16 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   canvas->paints.push_back(pr);
   canvas->clips.insert(canvas->clips.end(), canvas->st.clip, canvas->st.clip + 4);
   canvas->any_clip = canvas->any_clip || clipped;
+  skc::ColorFilterRec fr;
+  std::memset(&fr, 0, sizeof fr);
+  if (paint->color_filter) {
+    fr.type = paint->color_filter->type;
+    fr.mode = paint->color_filter->blend_mode;
+    fr.color = paint->color_filter->color;
+    std::memcpy(fr.matrix, paint->color_filter->matrix, sizeof fr.matrix);
+    canvas->any_filter = true;
+  }
+  canvas->filters.push_back(fr);
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -924,6 +955,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   sv.stop_colors = canvas->stop_colors.data();
   sv.stop_offsets = canvas->stop_offsets.data();
   sv.clips = canvas->any_clip ? canvas->clips.data() : nullptr;
+  sv.filters = canvas->any_filter ? canvas->filters.data() : nullptr;
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
   int32_t rc = skc::AddStreamCanvas(db.hb, sv);
@@ -960,6 +992,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->stop_offsets.clear();
   canvas->clips.clear();
   canvas->any_clip = false;
+  canvas->filters.clear();
+  canvas->any_filter = false;
   canvas->dirty = false;
   return SKITY_CUDA_SUCCESS;
 }

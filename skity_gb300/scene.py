@@ -20,7 +20,10 @@ the C boundary, see ``include/skity_cuda.h``):
   the global clip bounds that bound the scan (src/render/canvas.cc:463-476,
   src/render/sw/sw_canvas.cc:279-295); without the section every draw has
   the canvas's initial bounds ``kMaxCullRect`` (+-1e9,
-  include/skity/render/canvas.hpp:26).
+  include/skity/render/canvas.hpp:26);
+* optionally (header flag 2), per draw the paint's colour filter
+  (``ColorFilters::Blend / Matrix / LinearToSRGBGamma / SRGBToLinearGamma /
+  Compose``, include/skity/effect/color_filter.hpp), 96 bytes each.
 
 The binary file layout (``Scene.to_bytes``) is read by the CPU oracle, by the
 reference-driver recipe and by the C-ABI batch entry point.
@@ -51,7 +54,8 @@ BLUR_NONE, BLUR_NORMAL = 0, 1
 
 MAGIC = b"SKSC"
 VERSION = 1
-FLAG_CLIPS = 1  # header flags: the per-draw clip section is present
+FLAG_CLIPS = 1    # header flags: the per-draw clip section is present
+FLAG_FILTERS = 2  # the per-draw colour-filter section is present
 NO_CLIP = (-1e9, -1e9, 1e9, 1e9)  # kMaxCullRect
 
 # paint record: 20 x 4 bytes: the Paint fields the raster path reads, the
@@ -64,6 +68,15 @@ PAINT_DTYPE = np.dtype([
     ("stroke_width", "<f4"), ("miter", "<f4"), ("translate", "<f4", 2)])
 assert PAINT_DTYPE.itemsize == 80
 # gradient record: 12 x 4 bytes (matches skity_cuda_gradient)
+# colour-filter record: type (0 none, 1 + ColorFilterType: 1 blend, 2 matrix,
+# 3 linear->sRGB gamma, 4 sRGB->linear gamma, 5 compose), blend mode, the
+# blend colour (ARGB u32), the 4x5 row-major matrix
+FILTER_NONE, FILTER_BLEND, FILTER_MATRIX, FILTER_LINEAR_TO_SRGB, FILTER_SRGB_TO_LINEAR, \
+    FILTER_COMPOSE = 0, 1, 2, 3, 4, 5
+FILTER_DTYPE = np.dtype([("type", "<u4"), ("mode", "<u4"), ("color", "<u4"), ("pad", "<u4"),
+                         ("matrix", "<f4", 20)])
+assert FILTER_DTYPE.itemsize == 96
+
 GRADIENT_DTYPE = np.dtype([
     ("type", "<u4"), ("tile_mode", "<u4"), ("stop_count", "<u4"),
     ("stop_start", "<u4"), ("has_offsets", "<u4"), ("reserved", "<u4"),
@@ -100,6 +113,7 @@ class Scene:
     stop_colors: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.float32))
     stop_offsets: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     clips: np.ndarray | None = None  # (n_draws, 4) float32 LTRB, or None: no clip
+    filters: np.ndarray | None = None  # (n_draws,) FILTER_DTYPE, or None: no colour filters
 
     @property
     def n_draws(self) -> int:
@@ -107,7 +121,8 @@ class Scene:
 
     def to_bytes(self) -> bytes:
         nd = self.n_draws
-        flags = FLAG_CLIPS if self.clips is not None else 0
+        flags = (FLAG_CLIPS if self.clips is not None else 0) | \
+            (FLAG_FILTERS if self.filters is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -129,6 +144,10 @@ class Scene:
             c = np.ascontiguousarray(self.clips, np.float32).reshape(-1, 4)
             assert len(c) == nd
             out.append(c.tobytes())
+        if self.filters is not None:
+            f = np.ascontiguousarray(self.filters, FILTER_DTYPE)
+            assert len(f) == nd
+            out.append(f.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -156,8 +175,9 @@ class Scene:
         sc = take(np.float32, 4 * ns, (ns, 4))
         so = take(np.float32, ns)
         clips = take(np.float32, 4 * nd, (nd, 4)) if flags & FLAG_CLIPS else None
+        filters = take(FILTER_DTYPE, nd) if flags & FLAG_FILTERS else None
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so, clips)
+                     paints, grads, sc, so, clips, filters)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -186,7 +206,8 @@ class Scene:
                      paints, grads,
                      np.concatenate(sc) if sc else np.zeros((0, 4), np.float32),
                      np.concatenate(so) if so else np.zeros(0, np.float32),
-                     None if self.clips is None else self.clips[first:last].copy())
+                     None if self.clips is None else self.clips[first:last].copy(),
+                     None if self.filters is None else self.filters[first:last].copy())
 
 
 def map_clip(clip, rect, tx=0.0, ty=0.0):
@@ -216,7 +237,7 @@ class SceneBuilder:
         self._verbs, self._pts, self._wts = [], [], []
         self._vo, self._po, self._wo = [0], [0], [0]
         self._paints, self._grads, self._sc, self._so = [], [], [], []
-        self._clips = []
+        self._clips, self._filters = [], []
         self._nv = self._np = self._nw = 0
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
@@ -234,9 +255,10 @@ class SceneBuilder:
                                    else np.zeros(len(colors)), np.float32))
         return len(self._grads) - 1
 
-    def draw_path(self, verbs, points, paint, weights=(), clip=None):
+    def draw_path(self, verbs, points, paint, weights=(), clip=None, color_filter=None):
         """`clip`: device-space clip bounds (l, t, r, b) in effect for the
-        draw (see map_clip); None: the canvas's initial bounds."""
+        draw (see map_clip); None: the canvas's initial bounds.
+        `color_filter`: a FILTER_DTYPE record, or None."""
         verbs = np.asarray(verbs, np.uint8)
         points = np.asarray(points, np.float32).reshape(-1, 2)
         self._verbs.append(verbs); self._pts.append(points)
@@ -245,6 +267,7 @@ class SceneBuilder:
         self._vo.append(self._nv); self._po.append(self._np); self._wo.append(self._nw)
         self._paints.append(paint)
         self._clips.append(NO_CLIP if clip is None else tuple(clip))
+        self._filters.append(np.zeros((), FILTER_DTYPE) if color_filter is None else color_filter)
 
     def build(self) -> Scene:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
@@ -257,7 +280,19 @@ class SceneBuilder:
                      np.array(self._grads, GRADIENT_DTYPE) if self._grads else np.zeros(0, GRADIENT_DTYPE),
                      cat(self._sc, np.float32, (0, 4)), cat(self._so, np.float32, 0),
                      (np.array(self._clips, np.float32).reshape(-1, 4)
-                      if any(c != NO_CLIP for c in self._clips) else None))
+                      if any(c != NO_CLIP for c in self._clips) else None),
+                     (np.array(self._filters, FILTER_DTYPE)
+                      if any(int(f["type"]) != FILTER_NONE for f in self._filters) else None))
+
+
+def filter_record(kind, mode=0, color=0, matrix=None):
+    """A FILTER_DTYPE record: kind FILTER_*, blend mode and ARGB colour for
+    FILTER_BLEND, 20 row-major floats for FILTER_MATRIX."""
+    r = np.zeros((), FILTER_DTYPE)
+    r["type"], r["mode"], r["color"] = kind, mode, color
+    if matrix is not None:
+        r["matrix"] = np.asarray(matrix, np.float32).reshape(20)
+    return r
 
 
 # ---------------------------------------------------------------------------

@@ -4,6 +4,7 @@
 // tests/test_adapter.py against the reference's headers and the reference
 // software library built by oracle/ref (CPU only).
 #include <cstdio>
+#include <skity/effect/color_filter.hpp>
 #include <skity/effect/mask_filter.hpp>
 #include <skity/effect/shader.hpp>
 #include <skity/graphic/bitmap.hpp>
@@ -49,6 +50,11 @@ int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas, const skity_cuda_path* p,
       std::printf(" pos=");
       for (uint32_t i = 0; i < g->stop_count; ++i) std::printf("%g,", g->offsets[i]);
     }
+  }
+  if (q->color_filter) {
+    const skity_cuda_color_filter* f = q->color_filter;
+    std::printf(" filter=%u mode=%u color=%08x m=", f->type, f->blend_mode, f->color);
+    for (float v : f->matrix) std::printf("%g,", v);
   }
   std::printf(" blur=%u,%g\n", q->blur_style, q->blur_radius);
   return SKITY_CUDA_SUCCESS;
@@ -141,6 +147,16 @@ int main() {
   canvas->DrawPath(path, paint);
   paint.SetShader(Shader::MakeTwoPointConical(Point{5, 6, 0, 1}, 2.f, Point{30, 20, 0, 1}, 12.f,
                                               colors, nullptr, 3, TileMode::kClamp));
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  // colour filters reach the C ABI with their parameters
+  paint.SetShader(nullptr);
+  paint.SetColorFilter(ColorFilters::Blend(0x80102030u, BlendMode::kScreen));
+  canvas->DrawPath(path, paint);
+  const float rm[20] = {0, 1, 0, 0, 0.25f, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0.5f, 0};
+  paint.SetColorFilter(ColorFilters::Matrix(rm));
+  canvas->DrawPath(path, paint);
+  paint.SetColorFilter(ColorFilters::SRGBToLinearGamma());
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
   canvas->Flush();

@@ -149,6 +149,11 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   for (uint32_t p = 0; p < np; ++p) spans += pass_spans[p];
   b.brushes = hb.brushes.data();
   b.conicals = hb.conicals.data();
+  std::vector<uint8_t> srgb(512);
+  SRGBTables(srgb.data());
+  b.srgb_tables = srgb.data();
+  if (hb.cf_matrices.empty()) hb.cf_matrices.push_back(0);
+  b.cf_matrices = hb.cf_matrices.data();
   b.stop_colors = hb.stop_colors.data();
   b.stop_offsets = hb.stop_offsets.data();
   b.pixels = pixels.data();

@@ -85,4 +85,12 @@ def test_sweep_and_conical_shaders_forwarded(driver_output):
     sweep, conical = driver_output[24], driver_output[25]
     assert "shader=3 tile=1 stops=3 offsets=1 p0=20,15" in sweep and "r=-0.25" in sweep
     assert "shader=4 tile=0 stops=3 offsets=0 p0=5,6 p1=30,20 r=2" in conical
-    assert driver_output[26:] == ["status=0", "flush", "status=0", "destroy 0x10"]
+    assert driver_output[26] == "status=0"
+
+
+def test_color_filters_forwarded(driver_output):
+    blend, matrix, gamma = driver_output[27:30]
+    assert " filter=1 mode=14 color=80102030 " in blend
+    assert " filter=2 mode=0 color=00000000 m=0,1,0,0,0.25,1,0,0,0,0,0,0,1,0,0,0,0,0,0.5,0," in matrix
+    assert " filter=4 " in gamma
+    assert driver_output[30:] == ["status=0", "flush", "status=0", "destroy 0x10"]

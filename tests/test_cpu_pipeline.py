@@ -183,3 +183,11 @@ def test_blur_styles_bit_exact(cpu_pipeline, oracle_lib):
     ref, _ = oracle_lib.render(sc)
     assert st[4] > 0  # temp canvases
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+def test_color_filters_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import color_filters_scene
+    sc = color_filters_scene()
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0

@@ -287,3 +287,30 @@ def test_blur_styles_match_oracle(gpu_ctx, oracle_lib):
     sc = blur_styles_scene()
     c = check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
     assert c["bad_pixels"] == 0
+
+
+@pytest.mark.gpu
+def test_color_filters_match_oracle(gpu_ctx, oracle_lib):
+    """ColorFilters::Blend / Matrix / LinearToSRGBGamma / SRGBToLinearGamma /
+    Compose through the batch entry point and the canvas API."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import color_filters_scene
+    from skity_gb300.canvas import BlendMode, Canvas, ColorFilters, Paint, Path
+    sc = color_filters_scene()
+    c = check(oracle_lib, gpu_ctx.render_streams([sc])[0], sc)
+    assert c["bad_pixels"] == 0
+    bitmap = np.zeros((40, 48, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    tri = Path().MoveTo(2, 2).LineTo(44, 5).LineTo(6, 37).Close()
+    filters = [ColorFilters.Blend(0x80FF2040, BlendMode.kScreen),
+               ColorFilters.Matrix([0, 1, 0, 0, 0.1, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0.5, 0]),
+               ColorFilters.SRGBToLinearGamma()]
+    sb = S.SceneBuilder(48, 40)
+    for k, f in enumerate(filters):
+        paint = Paint().SetFillColor(0.3 + 0.2 * k, 0.6, 0.2, 0.7).SetColorFilter(f)
+        canvas.DrawPath(tri, paint)
+        sb.draw_path(tri.verbs, tri.points, paint.rec.copy(), color_filter=f.record())
+    canvas.Flush()
+    check(oracle_lib, bitmap, sb.build())

@@ -244,3 +244,50 @@ def test_blur_styles(ref):
     sc = blur_styles_scene()
     assert set(np.unique(sc.paints["blur_style"])) >= {1, 2, 3, 4}
     _pin(ref, sc)
+
+
+def color_filters_scene(seed=S.SEED_BASE + 398, width=128, height=100):
+    """Every colour filter: Blend (all 29 modes, opaque, translucent and
+    transparent colours), Matrix (channel swaps, negative terms, biases,
+    saturating terms), LinearToSRGBGamma, SRGBToLinearGamma and Compose, on
+    solid and gradient fills, strokes and blurred draws."""
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height, clear=(0.8, 0.7, 0.3, 0.9))
+    for i in range(96):
+        n = 3 + i % 5
+        verbs = [S.MOVE] + [[S.LINE, S.QUAD, S.CUBIC][j % 3] for j in range(n)] + [S.CLOSE]
+        npts = 1 + sum({S.LINE: 1, S.QUAD: 2, S.CUBIC: 3}[v] for v in verbs[1:-1])
+        pts = rng.uniform(-10, [width + 10, height + 10], (npts, 2)).astype(np.float32)
+        p = S.default_paint()
+        p["style"] = S.STROKE if i % 7 == 3 else S.FILL
+        p["stroke_width"] = 3.0
+        p["fill_color"] = tuple(np.append(rng.uniform(0, 1, 3), rng.uniform(0.2, 1)).astype(np.float32))
+        p["stroke_color"] = p["fill_color"]
+        if i % 5 == 2:
+            cols = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+            p["gradient"] = b.add_gradient(S.GRAD_LINEAR, (float(pts[0, 0]), float(pts[0, 1])),
+                                           (float(pts[1, 0]), float(pts[1, 1])), (0.0, 0.0), cols)
+        if i % 11 == 6:
+            p["blur_style"], p["blur_radius"] = 1 + i % 4, float(rng.uniform(1, 6))
+        kind = [S.FILTER_BLEND, S.FILTER_MATRIX, S.FILTER_LINEAR_TO_SRGB, S.FILTER_SRGB_TO_LINEAR,
+                S.FILTER_COMPOSE, S.FILTER_BLEND][i % 6]
+        if kind == S.FILTER_BLEND:
+            a = [255, 0, int(rng.integers(1, 255))][i % 3]
+            argb = (a << 24) | int(rng.integers(0, 1 << 24))
+            f = S.filter_record(kind, mode=(i // 6 + 7 * (i % 2)) % 29, color=argb)
+        elif kind == S.FILTER_MATRIX:
+            m = rng.uniform(-1.2, 1.2, 20).astype(np.float32)
+            m[[4, 9, 14, 19]] = rng.uniform(-0.5, 0.5, 4)
+            if i % 4 == 1:  # a channel swap with the alpha kept
+                m = np.array([0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0], np.float32)
+            f = S.filter_record(kind, matrix=m)
+        else:
+            f = S.filter_record(kind)
+        b.draw_path(verbs, pts, p, color_filter=f)
+    return b.build()
+
+
+def test_color_filters(ref):
+    sc = color_filters_scene()
+    assert set(np.unique(sc.filters["type"])) == {1, 2, 3, 4, 5}
+    _pin(ref, sc)
