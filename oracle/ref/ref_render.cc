@@ -62,6 +62,14 @@ struct Scene {
     float matrix[20];
   };
   std::vector<Filter> filters;  // per draw colour filter, when present
+  struct ClipState {
+    uint32_t parent, op, fill_type, nv, np, nw;
+    float translate[2], bounds[4];
+  };
+  std::vector<ClipState> clip_states;  // path clips, when present
+  std::vector<uint8_t> clip_verbs;
+  std::vector<float> clip_pts, clip_wts;
+  std::vector<uint32_t> draw_clip_state;  // per draw, 1-based (0: none)
 };
 
 template <typename T>
@@ -105,7 +113,63 @@ bool Load(const char* path, Scene* s) {
   Take(buf, o, s->stop_offsets, cnt[5]);
   if (flags & 1) Take(buf, o, s->clips, 4 * size_t(nd));
   if (flags & 2) Take(buf, o, s->filters, nd);
+  if (flags & 4) {
+    uint32_t n_states = 0;
+    if (o + 4 > buf.size()) return false;
+    std::memcpy(&n_states, buf.data() + o, 4);
+    o += 4;
+    Take(buf, o, s->clip_states, n_states);
+    size_t tv = 0, tp = 0, tw = 0;
+    for (const auto& c : s->clip_states) {
+      tv += c.nv;
+      tp += c.np;
+      tw += c.nw;
+    }
+    Take(buf, o, s->clip_verbs, tv);
+    o += (4 - tv % 4) % 4;
+    Take(buf, o, s->clip_pts, 2 * tp);
+    Take(buf, o, s->clip_wts, tw);
+    Take(buf, o, s->draw_clip_state, nd);
+  }
   return o <= buf.size();
+}
+
+skity::Path BuildPathFrom(const uint8_t* verbs, uint32_t nv, const float* p,
+                          const float* w) {
+  skity::Path path;
+  for (uint32_t v = 0; v < nv; ++v) {
+    switch (verbs[v]) {
+      case 0: path.MoveTo(p[0], p[1]); p += 2; break;
+      case 1: path.LineTo(p[0], p[1]); p += 2; break;
+      case 2: path.QuadTo(p[0], p[1], p[2], p[3]); p += 4; break;
+      case 3: path.ConicTo(p[0], p[1], p[2], p[3], *w++); p += 4; break;
+      case 4: path.CubicTo(p[0], p[1], p[2], p[3], p[4], p[5]); p += 6; break;
+      case 5: path.Close(); break;
+      default: break;
+    }
+  }
+  return path;
+}
+
+// Replays the ClipPath calls of clip state k (1-based) and its ancestors,
+// each with the global clip bounds and translation it was made under.
+void ReplayClipState(const Scene& s, skity::Canvas* canvas, uint32_t k) {
+  if (k == 0 || k > s.clip_states.size()) return;
+  const Scene::ClipState& c = s.clip_states[k - 1];
+  ReplayClipState(s, canvas, c.parent);
+  size_t v0 = 0, p0 = 0, w0 = 0;
+  for (uint32_t i = 0; i + 1 < k; ++i) {
+    v0 += s.clip_states[i].nv;
+    p0 += s.clip_states[i].np;
+    w0 += s.clip_states[i].nw;
+  }
+  skity::Path path = BuildPathFrom(s.clip_verbs.data() + v0, c.nv, s.clip_pts.data() + 2 * p0,
+                                   s.clip_wts.data() + w0);
+  if (c.fill_type == 1) path.SetFillType(skity::Path::PathFillType::kEvenOdd);
+  canvas->ClipRect(skity::Rect::MakeLTRB(c.bounds[0], c.bounds[1], c.bounds[2], c.bounds[3]));
+  canvas->Translate(c.translate[0], c.translate[1]);
+  canvas->ClipPath(path, static_cast<skity::Canvas::ClipOp>(c.op));
+  canvas->Translate(-c.translate[0], -c.translate[1]);
 }
 
 skity::Path BuildPath(const Scene& s, uint32_t d) {
@@ -249,13 +313,15 @@ int main(int argc, char** argv) {
     const float* c = s.clips.empty() ? nullptr : s.clips.data() + 4 * (first + i);
     const bool clipped =
         c && !(c[0] == -1e9f && c[1] == -1e9f && c[2] == 1e9f && c[3] == 1e9f);
-    if (moved || clipped) canvas->Save();
+    const uint32_t cstate = s.draw_clip_state.empty() ? 0 : s.draw_clip_state[first + i];
+    if (moved || clipped || cstate) canvas->Save();
+    ReplayClipState(s, canvas.get(), cstate);
     // the stored clip is already in device space: ClipRect before the
     // translation leaves exactly these global clip bounds
     if (clipped) canvas->ClipRect(skity::Rect::MakeLTRB(c[0], c[1], c[2], c[3]));
     if (moved) canvas->Translate(pr.translate[0], pr.translate[1]);
     canvas->DrawPath(paths[i], paints[i]);
-    if (moved || clipped) canvas->Restore();
+    if (moved || clipped || cstate) canvas->Restore();
   }
   canvas->Flush();
   auto t1 = std::chrono::steady_clock::now();

@@ -1834,6 +1834,17 @@ struct SceneView {
   const float *stop_colors, *stop_offsets;
   const float* clips;  // per draw (l, t, r, b) when the stream has the clip section
   const FilterRec* filters;  // per draw colour filter when the stream has that section
+  // path clips (Canvas::ClipPath states), when the stream has that section
+  struct ClipStateRec {
+    uint32_t parent, op, fill_type, nv, np, nw;
+    float translate[2], bounds[4];
+  };
+  uint32_t n_clip_states = 0;
+  const ClipStateRec* clip_states = nullptr;
+  const uint8_t* clip_verbs = nullptr;
+  const float *clip_pts = nullptr, *clip_wts = nullptr;
+  const uint32_t* draw_clip_state = nullptr;  // per draw, 1-based (0: none)
+  const struct ClipStates* clip_cache = nullptr;  // the states' span lists (set per render)
 };
 
 // The colour filter of the draw whose paint record is `p` (a record of s).
@@ -1862,8 +1873,9 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
-  const uint32_t flags = hdr[4];  // 1: per-draw clip bounds, 2: per-draw colour filters
-  if (flags & ~3u) return false;
+  // 1: per-draw clip bounds, 2: per-draw colour filters, 4: path clips
+  const uint32_t flags = hdr[4];
+  if (flags & ~7u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -1889,6 +1901,25 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->stop_offsets = (const float*)at(4 * (size_t)cnt[5]);
   s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
   s->filters = (flags & 2) ? (const FilterRec*)at(sizeof(FilterRec) * s->nd) : nullptr;
+  if (flags & 4) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_clip_states, buf + o, 4);
+    o += 4;
+    s->clip_states = (const SceneView::ClipStateRec*)at(sizeof(SceneView::ClipStateRec) *
+                                                         (size_t)s->n_clip_states);
+    if (o > len) return false;
+    size_t tv = 0, tp = 0, tw = 0;
+    for (uint32_t i = 0; i < s->n_clip_states; ++i) {
+      tv += s->clip_states[i].nv;
+      tp += s->clip_states[i].np;
+      tw += s->clip_states[i].nw;
+    }
+    s->clip_verbs = at(tv);
+    o += (4 - tv % 4) % 4;
+    s->clip_pts = (const float*)at(8 * tp);
+    s->clip_wts = (const float*)at(4 * tw);
+    s->draw_clip_state = (const uint32_t*)at(4 * (size_t)s->nd);
+  }
   return o <= len;
 }
 
@@ -1900,6 +1931,10 @@ static bool BlurUnderClip(const SceneView& s) {
     const Clip c = ClipOf(s, d);
     const bool narrowed = !(c.l == -1e9f && c.t == -1e9f && c.r == 1e9f && c.b == 1e9f);
     if (narrowed && s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f) return true;
+  }
+  for (uint32_t d = 0; d < s.nd && s.draw_clip_state; ++d) {
+    if (s.draw_clip_state[d] != 0 && s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f)
+      return true;
   }
   return false;
 }
@@ -1955,6 +1990,173 @@ static Brush MakeBrush(const SceneView& s, const PaintRec& p, bool stroke) {
   return br;
 }
 
+// ---------------------------------------------------------------------------
+// Path clips: SWCanvas::State's span algebra (sw_canvas.cc:42-265) and
+// OnClipPath (:317-336)
+// ---------------------------------------------------------------------------
+// FindSpan (:218-262): the pieces of `s` under each clip span of its row,
+// in clip-list order, covers min'd.
+static void FindSubSpans(const Span& s, const std::vector<Span>& clip, std::vector<Span>* out) {
+  for (const Span& c : clip) {
+    if (c.y != s.y) continue;
+    const int32_t cover = std::min(c.cover, s.cover);
+    if (c.x < s.x) {
+      if (c.x + c.len < s.x) continue;
+      out->push_back(Span{s.x, s.y, std::min(c.x + c.len, s.x + s.len) - s.x, cover});
+    } else if (c.x == s.x) {
+      out->push_back(Span{s.x, s.y, std::min(s.len, c.len), cover});
+    } else {
+      if (s.x + s.len < c.x) continue;
+      // the reference's + 1: the piece reaches one pixel past the span
+      out->push_back(Span{c.x, s.y, std::min(s.x + s.len - c.x + 1, c.len), cover});
+    }
+  }
+}
+
+// spans_subtraction (:59-133): each span of `a` minus the spans of `b` on
+// its row (those sorted by x with std::sort), pieces in x order.
+static std::vector<Span> SubtractSpans(const std::vector<Span>& a, const std::vector<Span>& b) {
+  std::vector<Span> out;
+  for (const Span& sp : a) {
+    std::vector<Span> ms;
+    for (const Span& m : b)
+      if (m.y == sp.y) ms.push_back(m);
+    if (ms.empty()) {
+      out.push_back(sp);
+      continue;
+    }
+    std::sort(ms.begin(), ms.end(), [](const Span& p, const Span& q) { return p.x < q.x; });
+    int32_t x = sp.x, len = sp.len;
+    for (const Span& m : ms) {
+      if (m.x + m.len < x || m.x > x + len) continue;
+      if (m.x < x) {
+        if (m.x + m.len > x + len) {  // all of it is subtracted
+          len = 0;
+          break;
+        }
+        const int32_t end = x + len, piece = m.x + m.len - x;
+        if (piece == 0) continue;
+        out.push_back(Span{x, sp.y, piece, sp.cover});
+        x += piece;
+        len = end - x;
+      } else if (m.x + m.len < x + len) {
+        const int32_t end = x + len;
+        out.push_back(Span{x, sp.y, m.x - x, sp.cover});
+        x = m.x + m.len;
+        len = end - x;
+      } else {
+        out.push_back(Span{x, sp.y, m.x - x, sp.cover});
+        len = 0;
+      }
+      if (len <= 0) break;
+    }
+    if (len > 0) out.push_back(Span{x, sp.y, len, sp.cover});
+  }
+  return out;
+}
+
+struct ClipState {  // SWCanvas::State: the clip's spans and op
+  std::vector<Span> spans;
+  uint32_t op = 1;  // Canvas::ClipOp: 0 kDifference, 1 kIntersect
+  bool HasClip() const { return !spans.empty(); }
+};
+
+// State::PerformClip (:157-175)
+static std::vector<Span> PerformClipOf(const ClipState& st, const std::vector<Span>& spans) {
+  if (st.op == 0) return SubtractSpans(spans, st.spans);
+  std::vector<Span> out;
+  for (const Span& sp : spans) FindSubSpans(sp, st.spans, &out);
+  return out;
+}
+
+// State::RecursiveClip (:177-193) and PerformMerge (:195-216)
+static std::vector<Span> RecursiveClipOf(const ClipState& st, const std::vector<Span>& spans,
+                                         uint32_t op) {
+  if (st.op == op) {
+    if (op == 1) return PerformClipOf(st, spans);
+    std::vector<Span> all(spans);
+    all.insert(all.end(), st.spans.begin(), st.spans.end());
+    std::sort(all.begin(), all.end(), [](const Span& a, const Span& b) {
+      if (a.y != b.y) return a.y < b.y;
+      if (a.x != b.x) return a.x < b.x;
+      return a.cover > b.cover;
+    });
+    return all;
+  }
+  return st.op == 0 ? SubtractSpans(spans, st.spans) : SubtractSpans(st.spans, spans);
+}
+
+struct ClipStates {
+  std::vector<ClipState> states;  // index 0: no clip; k: after the k-th ClipPath
+};
+
+static Path BuildPathFrom(const uint8_t* verbs, uint32_t nv, const float* p, const float* w) {
+  Path path;
+  for (uint32_t v = 0; v < nv; ++v) {
+    switch (verbs[v]) {
+      case kMove: path.MoveTo(P{p[0], p[1]}); p += 2; break;
+      case kLine: path.LineTo(P{p[0], p[1]}); p += 2; break;
+      case kQuad: path.QuadTo(P{p[0], p[1]}, P{p[2], p[3]}); p += 4; break;
+      case kConic: path.ConicTo(P{p[0], p[1]}, P{p[2], p[3]}, *w++); p += 4; break;
+      case kCubic: path.CubicTo(P{p[0], p[1]}, P{p[2], p[3]}, P{p[4], p[5]}); p += 6; break;
+      case kClose: path.Close(); break;
+      default: break;
+    }
+  }
+  return path;
+}
+
+// OnClipPath for every state of the stream, in order (a parent comes first).
+static void ComputeClipStates(const SceneView& s, ClipStates* cs) {
+  cs->states.assign(1, ClipState{});
+  const uint8_t* v = s.clip_verbs;
+  const float* p = s.clip_pts;
+  const float* w = s.clip_wts;
+  for (uint32_t i = 0; i < s.n_clip_states; ++i) {
+    const SceneView::ClipStateRec& r = s.clip_states[i];
+    Path path = BuildPathFrom(v, r.nv, p, w);
+    v += r.nv;
+    p += 2 * (size_t)r.np;
+    w += r.nw;
+    // RastePath(path, CurrentTransform(), GetScanClipBounds())
+    Path quad;
+    QuadPath(path, &quad);
+    for (auto& q : quad.pts) {
+      const float x = q.x, y = q.y;
+      q.x = (1.f * x + 0.f * y) + (0.f * 0.f + r.translate[0] * 1.f);
+      q.y = (0.f * x + 1.f * y) + (0.f * 0.f + r.translate[1] * 1.f);
+    }
+    Clip bounds;
+    bounds.l = r.bounds[0];
+    bounds.t = r.bounds[1];
+    bounds.r = r.bounds[2];
+    bounds.b = r.bounds[3];
+    std::vector<Span> raster;
+    RastePathQuads(quad, r.fill_type == 1, &raster, nullptr, bounds);
+    ClipState st = r.parent <= i ? cs->states[r.parent] : ClipState{};
+    if (st.HasClip()) {
+      st.spans = RecursiveClipOf(st, raster, r.op);
+      if (st.op != r.op) st.op = 1;
+    } else {
+      st.spans = raster;
+      st.op = r.op;
+    }
+    cs->states.push_back(std::move(st));
+  }
+}
+
+// DoBrush's clip step (sw_canvas.cc:338-353): the spans a draw brushes;
+// false when the clip leaves none.
+static bool ClipDrawSpans(const SceneView& s, uint32_t d, std::vector<Span>* spans) {
+  if (!s.draw_clip_state || !s.clip_cache) return true;
+  const uint32_t k = s.draw_clip_state[d];
+  if (k == 0 || k >= s.clip_cache->states.size()) return true;
+  const ClipState& st = s.clip_cache->states[k];
+  if (!st.HasClip()) return true;
+  *spans = PerformClipOf(st, *spans);
+  return !spans->empty();
+}
+
 // SWCanvas::OnDrawPath (sw_canvas.cc:357-411) for draws without filters
 static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
                      std::vector<Span>* spans) {
@@ -1969,6 +2171,7 @@ static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
     Path quad;
     QuadPath(path, &quad);
     RastePathQuads(quad, even_odd, spans, &rs, clip);
+    if (!ClipDrawSpans(s, d, spans)) return;
     Brush br = MakeBrush(s, paint, false);
     st->fragments += BrushSpans(*spans, br, (int)paint.blend, t);
     st->spans += spans->size();
@@ -1982,6 +2185,7 @@ static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
     // outline is a fresh Path (kWinding), whatever the source's fill type
     // (sw_canvas.cc:388-407, sw_raster.cc:783-784)
     RastePathQuads(quad2, false, spans, &rs, clip);
+    if (!ClipDrawSpans(s, d, spans)) return;
     Brush br = MakeBrush(s, paint, true);
     st->fragments += BrushSpans(*spans, br, (int)paint.blend, t);
     st->spans += spans->size();
@@ -2015,6 +2219,9 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
   if (BlurUnderClip(s)) return -3;
+  ClipStates clip_states;
+  ComputeClipStates(s, &clip_states);
+  s.clip_cache = &clip_states;
   Target t{out_rgba, (int)s.width, (int)s.height};
   auto t0 = std::chrono::steady_clock::now();
   if (s.has_clear) {
@@ -2062,6 +2269,9 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
   if (BlurUnderClip(s)) return -3;
+  ClipStates clip_states;
+  ComputeClipStates(s, &clip_states);
+  s.clip_cache = &clip_states;
   if (threads == 0) threads = 1;
   auto t0 = std::chrono::steady_clock::now();
   uint32_t last = std::min<uint32_t>(s.nd, first + count);

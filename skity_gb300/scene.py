@@ -23,7 +23,13 @@ the C boundary, see ``include/skity_cuda.h``):
   include/skity/render/canvas.hpp:26);
 * optionally (header flag 2), per draw the paint's colour filter
   (``ColorFilters::Blend / Matrix / LinearToSRGBGamma / SRGBToLinearGamma /
-  Compose``, include/skity/effect/color_filter.hpp), 96 bytes each.
+  Compose``, include/skity/effect/color_filter.hpp), 96 bytes each;
+* optionally (header flag 4), the canvas's path clips (``Canvas::ClipPath``,
+  ``ClipRRect``, ``ClipRect`` with ``kDifference``; the software canvas keeps
+  them as span lists, src/render/sw/sw_canvas.cc:157-336): a table of clip
+  states -- each one ClipPath call on top of its parent state, with the
+  path, the op, the translation and the global clip bounds in effect -- and
+  per draw the clip state it is drawn under (0: none).
 
 The binary file layout (``Scene.to_bytes``) is read by the CPU oracle, by the
 reference-driver recipe and by the C-ABI batch entry point.
@@ -56,6 +62,15 @@ MAGIC = b"SKSC"
 VERSION = 1
 FLAG_CLIPS = 1    # header flags: the per-draw clip section is present
 FLAG_FILTERS = 2  # the per-draw colour-filter section is present
+FLAG_PATH_CLIPS = 4  # the clip-state table and per-draw clip states are present
+CLIP_DIFFERENCE, CLIP_INTERSECT = 0, 1  # Canvas::ClipOp
+# clip state record: parent state (1-based, 0: none), ClipOp, the path's
+# fill type, its verb / point / weight counts, the canvas translation and
+# the global clip bounds (l, t, r, b) in effect at the ClipPath call
+CLIP_STATE_DTYPE = np.dtype([("parent", "<u4"), ("op", "<u4"), ("fill_type", "<u4"),
+                             ("nv", "<u4"), ("np", "<u4"), ("nw", "<u4"),
+                             ("translate", "<f4", 2), ("bounds", "<f4", 4)])
+assert CLIP_STATE_DTYPE.itemsize == 48
 NO_CLIP = (-1e9, -1e9, 1e9, 1e9)  # kMaxCullRect
 
 # paint record: 20 x 4 bytes: the Paint fields the raster path reads, the
@@ -114,6 +129,9 @@ class Scene:
     stop_offsets: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     clips: np.ndarray | None = None  # (n_draws, 4) float32 LTRB, or None: no clip
     filters: np.ndarray | None = None  # (n_draws,) FILTER_DTYPE, or None: no colour filters
+    # path clips: (states CLIP_STATE_DTYPE, verbs u8, points (n, 2) f32, weights f32,
+    # per-draw state u32), or None
+    path_clips: tuple | None = None
 
     @property
     def n_draws(self) -> int:
@@ -122,7 +140,8 @@ class Scene:
     def to_bytes(self) -> bytes:
         nd = self.n_draws
         flags = (FLAG_CLIPS if self.clips is not None else 0) | \
-            (FLAG_FILTERS if self.filters is not None else 0)
+            (FLAG_FILTERS if self.filters is not None else 0) | \
+            (FLAG_PATH_CLIPS if self.path_clips is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -148,6 +167,18 @@ class Scene:
             f = np.ascontiguousarray(self.filters, FILTER_DTYPE)
             assert len(f) == nd
             out.append(f.tobytes())
+        if self.path_clips is not None:
+            states, cverbs, cpts, cwts, per_draw = self.path_clips
+            states = np.ascontiguousarray(states, CLIP_STATE_DTYPE)
+            out.append(struct.pack("<I", len(states)))
+            out.append(states.tobytes())
+            vb = np.ascontiguousarray(cverbs, np.uint8).tobytes()
+            out.append(vb + b"\0" * ((-len(vb)) % 4))
+            out.append(np.ascontiguousarray(cpts, np.float32).tobytes())
+            out.append(np.ascontiguousarray(cwts, np.float32).tobytes())
+            pd = np.ascontiguousarray(per_draw, np.uint32)
+            assert len(pd) == nd
+            out.append(pd.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -176,8 +207,19 @@ class Scene:
         so = take(np.float32, ns)
         clips = take(np.float32, 4 * nd, (nd, 4)) if flags & FLAG_CLIPS else None
         filters = take(FILTER_DTYPE, nd) if flags & FLAG_FILTERS else None
+        path_clips = None
+        if flags & FLAG_PATH_CLIPS:
+            (n_states,) = struct.unpack_from("<I", buf, o); o += 4
+            states = take(CLIP_STATE_DTYPE, n_states)
+            tv, tp, tw = (int(states["nv"].sum()), int(states["np"].sum()),
+                          int(states["nw"].sum()))
+            cverbs = take(np.uint8, tv); o += (-tv) % 4
+            cpts = take(np.float32, 2 * tp, (tp, 2))
+            cwts = take(np.float32, tw)
+            per_draw = take(np.uint32, nd)
+            path_clips = (states, cverbs, cpts, cwts, per_draw)
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so, clips, filters)
+                     paints, grads, sc, so, clips, filters, path_clips)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -207,7 +249,9 @@ class Scene:
                      np.concatenate(sc) if sc else np.zeros((0, 4), np.float32),
                      np.concatenate(so) if so else np.zeros(0, np.float32),
                      None if self.clips is None else self.clips[first:last].copy(),
-                     None if self.filters is None else self.filters[first:last].copy())
+                     None if self.filters is None else self.filters[first:last].copy(),
+                     None if self.path_clips is None else
+                     self.path_clips[:4] + (self.path_clips[4][first:last].copy(),))
 
 
 def map_clip(clip, rect, tx=0.0, ty=0.0):
@@ -239,6 +283,10 @@ class SceneBuilder:
         self._paints, self._grads, self._sc, self._so = [], [], [], []
         self._clips, self._filters = [], []
         self._nv = self._np = self._nw = 0
+        # path clips: state records and their paths; the current state and
+        # the save stack of it (Canvas::Save / Restore)
+        self._cstates, self._cverbs, self._cpts, self._cwts = [], [], [], []
+        self._cstate, self._csaved, self._draw_cstate = 0, [], []
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
                      tile_mode=TILE_CLAMP) -> int:
@@ -268,6 +316,33 @@ class SceneBuilder:
         self._paints.append(paint)
         self._clips.append(NO_CLIP if clip is None else tuple(clip))
         self._filters.append(np.zeros((), FILTER_DTYPE) if color_filter is None else color_filter)
+        self._draw_cstate.append(self._cstate)
+
+    def save(self):
+        """Canvas::Save for the path-clip state."""
+        self._csaved.append(self._cstate)
+
+    def restore(self):
+        if self._csaved:
+            self._cstate = self._csaved.pop()
+
+    def clip_path(self, verbs, points, op, fill_type=WINDING, weights=(), translate=(0.0, 0.0),
+                  bounds=NO_CLIP):
+        """Canvas::ClipPath(path, op) on the current state, with the canvas
+        translation and the global clip bounds in effect at the call."""
+        st = np.zeros((), CLIP_STATE_DTYPE)
+        verbs = np.asarray(verbs, np.uint8)
+        points = np.asarray(points, np.float32).reshape(-1, 2)
+        weights = np.asarray(weights, np.float32)
+        st["parent"], st["op"], st["fill_type"] = self._cstate, op, fill_type
+        st["nv"], st["np"], st["nw"] = len(verbs), len(points), len(weights)
+        st["translate"], st["bounds"] = translate, bounds
+        self._cstates.append(st)
+        self._cverbs.append(verbs)
+        self._cpts.append(points)
+        self._cwts.append(weights)
+        self._cstate = len(self._cstates)
+        return self._cstate
 
     def build(self) -> Scene:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
@@ -282,7 +357,11 @@ class SceneBuilder:
                      (np.array(self._clips, np.float32).reshape(-1, 4)
                       if any(c != NO_CLIP for c in self._clips) else None),
                      (np.array(self._filters, FILTER_DTYPE)
-                      if any(int(f["type"]) != FILTER_NONE for f in self._filters) else None))
+                      if any(int(f["type"]) != FILTER_NONE for f in self._filters) else None),
+                     ((np.array(self._cstates, CLIP_STATE_DTYPE), cat(self._cverbs, np.uint8, 0),
+                       cat(self._cpts, np.float32, (0, 2)), cat(self._cwts, np.float32, 0),
+                       np.asarray(self._draw_cstate, np.uint32))
+                      if self._cstates else None))
 
 
 def filter_record(kind, mode=0, color=0, matrix=None):

@@ -291,3 +291,116 @@ def test_color_filters(ref):
     sc = color_filters_scene()
     assert set(np.unique(sc.filters["type"])) == {1, 2, 3, 4, 5}
     _pin(ref, sc)
+
+
+def _random_closed_path(rng, lo, hi, n_verbs):
+    verbs = [S.MOVE] + [[S.LINE, S.QUAD, S.CUBIC][int(rng.integers(0, 3))] for _ in range(n_verbs)]
+    verbs.append(S.CLOSE)
+    npts = 1 + sum({S.LINE: 1, S.QUAD: 2, S.CUBIC: 3}[v] for v in verbs[1:-1])
+    return verbs, rng.uniform(lo, hi, (npts, 2)).astype(np.float32)
+
+
+def path_clips_scene(seed=S.SEED_BASE + 399, width=160, height=120, n_ops=90):
+    """Canvas::ClipPath with kIntersect and kDifference (curved and polygon
+    paths, both fill rules, rects), nested under Save / Restore, mixed with
+    ClipRect and Translate, over fills, strokes and gradients; the draws
+    replay the canvas's clip state as the software canvas keeps it."""
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height, clear=(1.0, 1.0, 1.0, 1.0))
+    glob, t = S.NO_CLIP, (0.0, 0.0)
+    stack = []
+    for i in range(n_ops):
+        r = rng.random()
+        if r < 0.08 and stack:
+            b.restore()
+            glob, t = stack.pop()
+        elif r < 0.16:
+            b.save()
+            stack.append((glob, t))
+        elif r < 0.30:
+            op = S.CLIP_INTERSECT if rng.random() < 0.6 else S.CLIP_DIFFERENCE
+            if rng.random() < 0.3:
+                x0, y0 = rng.uniform(-20, [width, height])
+                x1, y1 = x0 + rng.uniform(10, 90), y0 + rng.uniform(10, 70)
+                verbs = [S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE]
+                pts = np.array([[x0, y0], [x1, y0], [x1, y1], [x0, y1]], np.float32)
+            else:
+                verbs, pts = _random_closed_path(rng, [-20, -20], [width + 20, height + 20],
+                                                 int(rng.integers(3, 9)))
+            fill = S.EVEN_ODD if rng.random() < 0.3 else S.WINDING
+            b.clip_path(verbs, pts, op, fill, translate=t, bounds=glob)
+            if op == S.CLIP_INTERSECT:  # ClipPath narrows the global clip bounds too
+                pb = (pts[:, 0].min(), pts[:, 1].min(), pts[:, 0].max(), pts[:, 1].max())
+                glob = S.map_clip(glob, pb, t[0], t[1])
+        elif r < 0.34:
+            t = (float(np.float32(t[0]) + np.float32(rng.uniform(-12, 12))),
+                 float(np.float32(t[1]) + np.float32(rng.uniform(-12, 12))))
+        elif r < 0.38:
+            x0, y0 = rng.uniform(-10, [width, height])
+            glob = S.map_clip(glob, (x0, y0, x0 + rng.uniform(20, 120), y0 + rng.uniform(20, 90)),
+                              t[0], t[1])
+        else:
+            verbs, pts = _random_closed_path(rng, [-10, -10], [width + 10, height + 10],
+                                             int(rng.integers(2, 12)))
+            p = S.default_paint()
+            p["style"] = S.STROKE if rng.random() < 0.2 else S.FILL
+            p["stroke_width"] = float(rng.uniform(1, 6))
+            p["fill_type"] = S.EVEN_ODD if rng.random() < 0.3 else S.WINDING
+            p["fill_color"] = tuple(np.append(rng.uniform(0, 1, 3), rng.uniform(0.3, 1)).astype(np.float32))
+            p["stroke_color"] = p["fill_color"]
+            p["translate"] = t
+            if rng.random() < 0.15:
+                p["blend"] = S.BLEND_SRC
+            if rng.random() < 0.2:
+                cols = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+                p["gradient"] = b.add_gradient(S.GRAD_RADIAL, (float(pts[0, 0]), float(pts[0, 1])),
+                                               (0.0, 0.0), (float(rng.uniform(10, 60)), 0.0), cols)
+            b.draw_path(verbs, pts, p, clip=glob)
+    return b.build()
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_clip_path(ref, seed):
+    sc = path_clips_scene(S.SEED_BASE + 399 + seed)
+    assert sc.path_clips is not None and (sc.path_clips[4] != 0).any()
+    _pin(ref, sc)
+
+
+def clip_path_cases_scene():
+    """The path-clip combinations one by one (intersect, difference, and each
+    op nested in each, an even-odd star, a clip under a translation), each
+    between Save and Restore, over a rect and a stroked curve."""
+    b = S.SceneBuilder(96, 72)
+    tri = ([S.MOVE, S.LINE, S.LINE, S.CLOSE], [[5, 5], [90, 12], [30, 68]])
+    band = ([S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE], [[0, 28], [96, 28], [96, 44], [0, 44]])
+    star = ([S.MOVE, S.LINE, S.LINE, S.LINE, S.LINE, S.CLOSE],
+            [[48, 2], [70, 66], [10, 24], [86, 24], [26, 66]])
+    rect = ([S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE], [[3, 3], [93, 3], [93, 69], [3, 69]])
+    curve = ([S.MOVE, S.CUBIC], [[4, 60], [30, -20], [60, 100], [92, 8]])
+    cases = [((tri, S.CLIP_INTERSECT, S.WINDING), None), ((tri, S.CLIP_DIFFERENCE, S.WINDING), None),
+             ((tri, S.CLIP_INTERSECT, S.WINDING), (band, S.CLIP_INTERSECT)),
+             ((tri, S.CLIP_INTERSECT, S.WINDING), (band, S.CLIP_DIFFERENCE)),
+             ((tri, S.CLIP_DIFFERENCE, S.WINDING), (band, S.CLIP_DIFFERENCE)),
+             ((tri, S.CLIP_DIFFERENCE, S.WINDING), (band, S.CLIP_INTERSECT)),
+             ((star, S.CLIP_INTERSECT, S.EVEN_ODD), None)]
+    for k, (first, second) in enumerate(cases):
+        b.save()
+        t = (float(k % 3) * 0.5, float(k % 2) * 1.25)
+        (verbs, pts), op, fill = first
+        b.clip_path(verbs, pts, op, fill, translate=t)
+        if second is not None:
+            (v2, p2), op2 = second
+            b.clip_path(v2, p2, op2)
+        p = S.default_paint()
+        p["fill_color"] = (0.1 * k, 0.9 - 0.1 * k, 0.5, 0.6)
+        b.draw_path(*rect, p)
+        q = S.default_paint()
+        q["style"], q["stroke_width"] = S.STROKE, 3.0
+        q["stroke_color"] = (0.9, 0.1, 0.1 * k, 0.8)
+        b.draw_path(*curve, q)
+        b.restore()
+    return b.build()
+
+
+def test_clip_path_cases(ref):
+    _pin(ref, clip_path_cases_scene())
