@@ -215,6 +215,16 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, flo
  * returns SKITY_CUDA_ERROR_NOT_SUPPORTED. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
                                                    float right, float bottom);
+/* Canvas::ClipPath(path, op) (canvas.hpp; SWCanvas::OnClipPath,
+ * sw_canvas.cc:317-336), op 0 kDifference / 1 kIntersect: later draws (and
+ * Clear) are clipped by the path's spans the way the software canvas clips
+ * them, nested clips combined as it combines them; Save / Restore keep and
+ * restore the clip.  A kIntersect clip also narrows the global clip bounds
+ * by the path's bounds.  ClipRRect and ClipRect with kDifference are path
+ * clips of the rounded rect's / rect's path.  A blurred draw under a path
+ * clip returns SKITY_CUDA_ERROR_NOT_SUPPORTED at flush. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
+                                                   const skity_cuda_path* path, uint32_t op);
 /* Canvas::Flush: renders the recorded draws on the GPU and writes the
  * bitmap's pixels. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas);

@@ -113,6 +113,7 @@ SIGNATURES = {
     "skity_cuda_canvas_translate": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
     "skity_cuda_canvas_clip_rect": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
                                                      ctypes.c_float, ctypes.c_float]),
+    "skity_cuda_canvas_clip_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.c_uint32]),
     "skity_cuda_render_streams": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
                                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),

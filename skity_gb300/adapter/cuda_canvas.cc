@@ -29,27 +29,48 @@ static bool TranslationOf(const Matrix& m, float* tx, float* ty) {
   return true;
 }
 
+static void PathStorage(const Path& path, std::vector<uint8_t>* verbs, std::vector<float>* pts,
+                        std::vector<float>* weights, skity_cuda_path* p);
+
 // Canvas::ClipRect has already narrowed the global clip bounds
 // (canvas.cc:130-135,463-476); for kIntersect under a translation that is
-// all SWCanvas does too (sw_canvas.cc:279-295).  Other clips are refused.
-void CUDACanvas::OnClipRect(Rect const&, ClipOp op) {
+// all SWCanvas does too (sw_canvas.cc:279-295).  kDifference goes on as a
+// path clip of the rect (Canvas::OnClipRect, canvas.cc:144-150).
+void CUDACanvas::OnClipRect(Rect const& rect, ClipOp op) {
   float tx = 0.f, ty = 0.f;
-  if (op != ClipOp::kIntersect || !TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
     bad_clip_.back() = true;
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  if (op != ClipOp::kIntersect) {
+    Canvas::OnClipRect(rect, op);
     return;
   }
   status_ = SKITY_CUDA_SUCCESS;
 }
 
-void CUDACanvas::OnClipRRect(RRect const&, ClipOp) {
-  bad_clip_.back() = true;
-  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
-}
-
-void CUDACanvas::OnClipPath(Path const&, ClipOp) {
-  bad_clip_.back() = true;
-  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+// SWCanvas::OnClipPath (sw_canvas.cc:317-336): the C ABI canvas records the
+// clip on its state for this save level, with the translation and the
+// global clip bounds in effect (the base class has already narrowed them).
+void CUDACanvas::OnClipPath(Path const& path, ClipOp op) {
+  float tx = 0.f, ty = 0.f;
+  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+    bad_clip_.back() = true;
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  std::vector<uint8_t> verbs;
+  std::vector<float> pts, weights;
+  skity_cuda_path p{};
+  PathStorage(path, &verbs, &pts, &weights, &p);
+  const Rect& g = GetGlobalClipBounds();
+  if (!(g.Left() == -1e9f && g.Top() == -1e9f && g.Right() == 1e9f && g.Bottom() == 1e9f))
+    skity_cuda_canvas_clip_rect(canvas_, g.Left(), g.Top(), g.Right(), g.Bottom());
+  const bool moved = tx != 0.f || ty != 0.f;
+  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  status_ = skity_cuda_canvas_clip_path(canvas_, &p, op == ClipOp::kIntersect ? 1u : 0u);
+  if (moved) skity_cuda_canvas_translate(canvas_, -tx, -ty);
 }
 
 void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
@@ -58,30 +79,11 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     return;
   }
-  // Path storage as the reference keeps it (path.hpp:590-596)
   std::vector<uint8_t> verbs;
   std::vector<float> pts;
   std::vector<float> weights;
-  verbs.reserve(path.CountVerbs());
-  uint32_t conics = 0;
-  for (const Path::Verb* v = path.VerbsBegin(); v != path.VerbsEnd(); ++v) {
-    verbs.push_back(static_cast<uint8_t>(*v));
-    if (*v == Path::Verb::kConic) conics++;
-  }
-  pts.reserve(2 * path.CountPoints());
-  for (size_t i = 0; i < path.CountPoints(); ++i) {
-    pts.push_back(path.Points()[i].x);
-    pts.push_back(path.Points()[i].y);
-  }
-  weights.assign(path.ConicWeights(), path.ConicWeights() + conics);
   skity_cuda_path p{};
-  p.verbs = verbs.data();
-  p.verb_count = static_cast<uint32_t>(verbs.size());
-  p.points = pts.data();
-  p.point_count = static_cast<uint32_t>(path.CountPoints());
-  p.conic_weights = weights.data();
-  p.conic_weight_count = conics;
-  p.fill_type = path.GetFillType() == Path::PathFillType::kEvenOdd ? 1u : 0u;
+  PathStorage(path, &verbs, &pts, &weights, &p);
 
   skity_cuda_paint q{};
   q.style = static_cast<uint32_t>(paint.GetStyle());
@@ -179,6 +181,31 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
   if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
   status_ = skity_cuda_canvas_draw_path(canvas_, &p, &q);
   if (moved || clipped) skity_cuda_canvas_restore(canvas_);
+}
+
+// Path storage as the reference keeps it (path.hpp:590-596), in the C ABI's
+// path record (pointing into the vectors).
+static void PathStorage(const Path& path, std::vector<uint8_t>* verbs, std::vector<float>* pts,
+                        std::vector<float>* weights, skity_cuda_path* p) {
+  verbs->reserve(path.CountVerbs());
+  uint32_t conics = 0;
+  for (const Path::Verb* v = path.VerbsBegin(); v != path.VerbsEnd(); ++v) {
+    verbs->push_back(static_cast<uint8_t>(*v));
+    if (*v == Path::Verb::kConic) conics++;
+  }
+  pts->reserve(2 * path.CountPoints());
+  for (size_t i = 0; i < path.CountPoints(); ++i) {
+    pts->push_back(path.Points()[i].x);
+    pts->push_back(path.Points()[i].y);
+  }
+  weights->assign(path.ConicWeights(), path.ConicWeights() + conics);
+  p->verbs = verbs->data();
+  p->verb_count = static_cast<uint32_t>(verbs->size());
+  p->points = pts->data();
+  p->point_count = static_cast<uint32_t>(path.CountPoints());
+  p->conic_weights = weights->data();
+  p->conic_weight_count = conics;
+  p->fill_type = path.GetFillType() == Path::PathFillType::kEvenOdd ? 1u : 0u;
 }
 
 void CUDACanvas::OnSaveLayer(const Rect&, const Paint&) {

@@ -9,8 +9,10 @@
 // What differs from the software canvas: pixels are written to the bitmap at
 // Flush(), not during each draw.  ClipRect(kIntersect) under a translation is
 // taken (the global clip bounds the base class keeps bound each draw's scan,
-// as SWCanvas::OnClipRect relies on, sw_canvas.cc:279-295).  Operations
-// outside the GPU raster path -- ClipPath, kDifference clips, layers, text,
+// as SWCanvas::OnClipRect relies on, sw_canvas.cc:279-295), and so are
+// ClipPath, ClipRRect and ClipRect(kDifference) under a translation (path
+// clips the C ABI canvas keeps per save level, as SWCanvas does).  Operations
+// outside the GPU raster path -- clips under other matrices, layers, text,
 // images, canvas matrices other than translations, shader local matrices --
 // draw nothing and leave
 // SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus(); draws under a clip this
@@ -38,7 +40,6 @@ class CUDACanvas : public Canvas {
 
  protected:
   void OnClipRect(Rect const& rect, ClipOp op) override;
-  void OnClipRRect(RRect const& rrect, ClipOp op) override;
   void OnClipPath(Path const& path, ClipOp op) override;
   void OnDrawPath(Path const& path, Paint const& paint) override;
   void OnSaveLayer(const Rect& bounds, const Paint& paint) override;
@@ -48,9 +49,13 @@ class CUDACanvas : public Canvas {
   void OnDrawGlyphs(uint32_t count, const GlyphID glyphs[], const float position_x[],
                     const float position_y[], const Font& font, const Paint& paint) override;
   void OnDrawPaint(Paint const& paint) override;
-  void OnSave() override { bad_clip_.push_back(bad_clip_.back()); }
+  void OnSave() override {
+    bad_clip_.push_back(bad_clip_.back());
+    skity_cuda_canvas_save(canvas_);
+  }
   void OnRestore() override {
     if (bad_clip_.size() > 1) bad_clip_.pop_back();
+    skity_cuda_canvas_restore(canvas_);
   }
   void OnRestoreToCount(int) override {}
   void OnFlush() override;

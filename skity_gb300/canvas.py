@@ -441,6 +441,17 @@ class Canvas:
         _lib.check(self.lib.skity_cuda_canvas_translate(self.handle, float(dx), float(dy)),
                    "skity_cuda_canvas_translate")
 
+    def ClipPath(self, path: Path, op=1):
+        """Canvas::ClipPath(path, op): op 0 kDifference, 1 kIntersect."""
+        verbs = np.asarray(path.verbs, np.uint8)
+        pts = np.asarray(path.points, np.float32).reshape(-1, 2)
+        wts = np.asarray(path.weights, np.float32)
+        cp = _lib.Path_(verbs.ctypes.data if len(verbs) else None, len(verbs),
+                        pts.ctypes.data if len(pts) else None, len(pts),
+                        wts.ctypes.data if len(wts) else None, len(wts), path.fill_type)
+        _lib.check(self.lib.skity_cuda_canvas_clip_path(self.handle, ctypes.byref(cp), int(op)),
+                   "skity_cuda_canvas_clip_path")
+
     def ClipRect(self, left, top, right, bottom):
         """Canvas::ClipRect(rect, ClipOp::kIntersect) under the current
         translation; Save / Restore keep and restore the clip."""

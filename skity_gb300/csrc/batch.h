@@ -62,7 +62,22 @@ struct StreamView {
   const float *stop_colors, *stop_offsets;
   const float* clips;  // per draw device-space clip bounds (l, t, r, b), or null: none
   const ColorFilterRec* filters;  // per draw colour filter, or null: none
+  // path clips (Canvas::ClipPath states) when the stream has them
+  uint32_t n_clip_states;
+  const struct ClipStateRec* clip_states;
+  const uint8_t* clip_verbs;
+  const float *clip_pts, *clip_wts;
+  const uint32_t* draw_clip_state;  // per draw, 1-based (0: none)
 };
+
+// A ClipPath call of the stream: its parent state (1-based, 0: none), the
+// op, the path's fill type and counts, the canvas translation and the global
+// clip bounds at the call.
+struct ClipStateRec {
+  uint32_t parent, op, fill_type, nv, np, nw;
+  float translate[2], bounds[4];
+};
+static_assert(sizeof(ClipStateRec) == 48, "clip state layout");
 
 // A draw the device code can take: the verb sequence of a skity::Path
 // (first verb kMove, a kMove after every kClose -- Path::LineTo/QuadTo/...
@@ -163,9 +178,10 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->width = hdr[1];
   s->height = hdr[2];
   s->has_clear = hdr[3];
-  // 1: per-draw clip bounds follow the stops; 2: then per-draw colour filters
+  // 1: per-draw clip bounds follow the stops; 2: then per-draw colour
+  // filters; 4: then the path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~3u) return false;
+  if (flags & ~7u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -196,6 +212,50 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   s->stop_offsets = (const float*)at(4 * (size_t)s->ns);
   s->clips = (flags & 1) ? (const float*)at(16 * (size_t)s->nd) : nullptr;
   s->filters = (flags & 2) ? (const ColorFilterRec*)at(sizeof(ColorFilterRec) * s->nd) : nullptr;
+  s->n_clip_states = 0;
+  s->clip_states = nullptr;
+  s->clip_verbs = nullptr;
+  s->clip_pts = s->clip_wts = nullptr;
+  s->draw_clip_state = nullptr;
+  if (flags & 4) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_clip_states, buf + o, 4);
+    o += 4;
+    if (s->n_clip_states > (1u << 20)) return false;
+    s->clip_states = (const ClipStateRec*)at(sizeof(ClipStateRec) * (size_t)s->n_clip_states);
+    if (o > len) return false;
+    uint64_t tv = 0, tp = 0, tw = 0;
+    for (uint32_t i = 0; i < s->n_clip_states; ++i) {
+      const ClipStateRec& c = s->clip_states[i];
+      if (c.parent > i || c.op > 1 || c.fill_type > 1 || !ValidClip(c.bounds) ||
+          !(std::fabs(c.translate[0]) <= kMaxCoord && std::fabs(c.translate[1]) <= kMaxCoord))
+        return false;
+      tv += c.nv;
+      tp += c.np;
+      tw += c.nw;
+    }
+    if (tv + tp + tw > len) return false;
+    s->clip_verbs = at(tv);
+    o += (4 - tv % 4) % 4;
+    s->clip_pts = (const float*)at(8 * tp);
+    s->clip_wts = (const float*)at(4 * tw);
+    s->draw_clip_state = (const uint32_t*)at(4 * (size_t)s->nd);
+    if (o > len) return false;
+    const uint8_t* v = s->clip_verbs;
+    const float* p = s->clip_pts;
+    const float* w = s->clip_wts;
+    for (uint32_t i = 0; i < s->n_clip_states; ++i) {
+      const ClipStateRec& c = s->clip_states[i];
+      if (!ValidPath(v, c.nv, p, c.np, w, c.nw)) return false;
+      float t[2] = {c.translate[0], c.translate[1]};
+      if (!ValidTranslate(t, p, c.np)) return false;
+      v += c.nv;
+      p += 2 * (size_t)c.np;
+      w += c.nw;
+    }
+    for (uint32_t d = 0; d < s->nd; ++d)
+      if (s->draw_clip_state[d] > s->n_clip_states) return false;
+  }
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
   for (uint32_t d = 0; d < s->nd; ++d) {
@@ -346,6 +406,7 @@ struct HostBatch {
   std::vector<Brush> brushes;
   std::vector<ConicalParams> conicals;
   std::vector<int16_t> cf_matrices;  // colour-filter matrices, 20 terms each
+  std::vector<ClipStateDesc> clip_states;  // path-clip states of all canvases, in call order
   std::vector<CanvasDesc> canvases;
   std::vector<float4> stop_colors;
   std::vector<float> stop_offsets;
@@ -571,8 +632,50 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   hb.main_canvases.push_back(cidx);
   std::vector<PassDesc> main_passes;
   std::vector<std::pair<uint32_t, std::vector<PassDesc>>> temps;
+  // Path clips: one pass rasterising each ClipPath path (RastePath with the
+  // canvas translation and global clip bounds of the call, sw_canvas.cc:
+  // 317-324), its spans kept raw for the clip stages; states numbered
+  // across the batch.
+  const uint32_t state_base = (uint32_t)hb.clip_states.size();
+  std::vector<uint32_t> clip_pass_pos;
+  {
+    const uint8_t* v = s.clip_verbs;
+    const float* p = s.clip_pts;
+    const float* w = s.clip_wts;
+    for (uint32_t i = 0; i < s.n_clip_states; ++i) {
+      const ClipStateRec& c = s.clip_states[i];
+      const uint32_t draw = hb.AddDraw(v, c.nv, p, c.np, w, c.nw);
+      PassDesc pd;
+      std::memset(&pd, 0, sizeof pd);
+      pd.draw = draw;
+      pd.canvas = cidx;
+      pd.flags = kPassClipPath | kPassRawSpans | (c.fill_type == 1 ? kPassEvenOdd : 0);
+      pd.tx = c.translate[0];
+      pd.ty = c.translate[1];
+      if (!IsNoClip(c.bounds)) {
+        pd.clipped = 1;
+        std::memcpy(pd.clip, c.bounds, sizeof pd.clip);
+      }
+      pd.stroke_width = 1.f;
+      pd.miter = 4.f;
+      pd.ga = 255;
+      InitialCaps(v, c.nv, p, false, pd.cap);
+      DerivedCaps(pd.cap, false);
+      clip_pass_pos.push_back((uint32_t)main_passes.size());
+      main_passes.push_back(pd);
+      ClipStateDesc st;
+      std::memset(&st, 0, sizeof st);
+      st.parent = c.parent ? state_base + c.parent : 0;
+      st.op = c.op;
+      hb.clip_states.push_back(st);
+      v += c.nv;
+      p += 2 * (size_t)c.np;
+      w += c.nw;
+    }
+  }
   for (uint32_t d = 0; d < s.nd; ++d) {
     const PaintRec& pr = s.paints[d];
+    const uint32_t path_clip = s.draw_clip_state ? s.draw_clip_state[d] : 0u;
     if (pr.blend > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
     uint32_t draw = hb.AddDraw(s.verbs + s.vo[d], s.vo[d + 1] - s.vo[d], s.pts + 2 * (size_t)s.po[d],
                                s.po[d + 1] - s.po[d], s.wts + s.wo[d], s.wo[d + 1] - s.wo[d]);
@@ -581,9 +684,17 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     if (!blur) {
       // the canvas translation goes where the reference's CopyWithMatrix
       // and device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
+      const size_t first_pass = main_passes.size();
       AddDrawPasses(hb, s, d, draw, cidx, pr.translate[0], pr.translate[1], main_passes);
+      if (path_clip) {  // DoBrush clips the raster's spans by the state (sw_canvas.cc:338-353)
+        for (size_t q = first_pass; q < main_passes.size(); ++q) {
+          main_passes[q].path_clip = state_base + path_clip;
+          main_passes[q].flags |= kPassRawSpans;
+        }
+      }
       continue;
     }
+    if (path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a blur under a path clip
     if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (pr.blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
@@ -682,6 +793,8 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     main_passes.push_back(pd);
   }
   hb.canvases[cidx].pass0 = (uint32_t)hb.passes.size();
+  for (uint32_t i = 0; i < (uint32_t)clip_pass_pos.size(); ++i)
+    hb.clip_states[state_base + i].pass = hb.canvases[cidx].pass0 + clip_pass_pos[i];
   hb.passes.insert(hb.passes.end(), main_passes.begin(), main_passes.end());
   hb.canvases[cidx].pass1 = (uint32_t)hb.passes.size();
   for (auto& tpp : temps) {
@@ -807,13 +920,53 @@ inline void PlanComp(const HostBatch& hb, const std::vector<PassGeom>& geom,
   comp.assign(geom.size(), PassComp{});
   for (size_t p = 0; p < geom.size(); ++p) {
     const PassGeom& g = geom[p];
-    const bool has = g.n_edges > 0 && g.row1 > g.row0;
+    const bool has = g.n_edges > 0 && g.row1 > g.row0 && !(hb.passes[p].flags & kPassClipPath);
     comp[p].row0 = has ? g.row0 : 0;
     comp[p].row1 = has ? g.row1 : 0;
     comp[p].rbase = sw[p].rbase;
     comp[p].brush = hb.passes[p].brush;
   }
 }
+// Rows of the clip states (their clip path's rows and their parent's) and
+// the (pass, row) items of the draws under a path clip; returns the number
+// of state rows.
+inline uint64_t PlanPathClips(HostBatch& hb, const std::vector<PassGeom>& geom,
+                              std::vector<uint2>& items) {
+  uint64_t rbase = 0;
+  for (ClipStateDesc& st : hb.clip_states) {
+    const PassGeom& g = geom[st.pass];
+    int32_t y0 = 0, y1 = 0;
+    if (g.n_edges > 0 && g.row1 > g.row0) {
+      y0 = g.row0;
+      y1 = g.row1;
+    }
+    if (st.parent) {
+      const ClipStateDesc& ps = hb.clip_states[st.parent - 1];
+      if (ps.y1 > ps.y0) {
+        if (y1 > y0) {
+          y0 = std::min(y0, ps.y0);
+          y1 = std::max(y1, ps.y1);
+        } else {
+          y0 = ps.y0;
+          y1 = ps.y1;
+        }
+      }
+    }
+    st.y0 = y0;
+    st.y1 = y1;
+    st.rbase = (uint32_t)rbase;
+    rbase += (uint64_t)(y1 - y0);
+  }
+  items.clear();
+  for (uint32_t p = 0; p < (uint32_t)hb.passes.size(); ++p) {
+    if (!hb.passes[p].path_clip) continue;
+    const PassGeom& g = geom[p];
+    if (g.n_edges <= 0) continue;
+    for (int32_t y = g.row0; y < g.row1; ++y) items.push_back(make_uint2(p, (uint32_t)y));
+  }
+  return rbase;
+}
+
 // The order in which the sweeps take the passes: longest expected sweep
 // first (rows times the bound of the active list), so that the long sweeps
 // start early instead of forming the tail of the launch.

@@ -67,6 +67,7 @@ struct DeviceBatch {
   uint32_t n_bands = 0;
   RasterConfig cfg;
   DevBuf task_next;  // persistent compositor's counters
+  DevBuf clip_states, clip_flags, clip_rows, clip_items;  // path clips
   // true when the caller has loaded the canvases' current pixels (a canvas
   // flush without a clear); otherwise a canvas without a clear colour starts
   // from transparent black, as a fresh Bitmap does

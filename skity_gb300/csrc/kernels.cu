@@ -21,6 +21,7 @@
 
 
 #include "passes.cuh"
+#include "clip.cuh"
 
 namespace skc {
 
@@ -337,6 +338,43 @@ int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, u
   }
   k_composite<<<grid, 32 * kCompWarps, smem, stream>>>(b, tasks, n_tasks, chunk, counter);
   return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Path clips (clip.cuh): each clip state's span rows, one launch per state
+// in order (a state reads its parent's rows and whether the parent's list
+// is empty, known only once the parent's launch is complete), then the rows
+// of the draws under a clip, one thread per (pass, row).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_clip_state(DevBatch b, uint32_t k, int32_t y0, int32_t y1) {
+  const int32_t y = y0 + (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (y >= y1) return;
+  int32_t order[kClipRowCap];
+  ClipStateStage(b, k, y, order);
+}
+
+__global__ void __launch_bounds__(128) k_clip_apply(DevBatch b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.n_clip_items) return;
+  int32_t order[kClipRowCap];
+  ClipApplyStage(b, i, order);
+}
+
+int LaunchPathClips(const DevBatch& b, const ClipStateDesc* states, uint32_t n_states,
+                    cudaStream_t stream) {
+  int launches = 0;
+  for (uint32_t k = 1; k <= n_states; ++k) {
+    const ClipStateDesc& st = states[k - 1];
+    if (st.y1 <= st.y0) continue;
+    const uint32_t rows = (uint32_t)(st.y1 - st.y0);
+    k_clip_state<<<(rows + 127) / 128, 128, 0, stream>>>(b, k, st.y0, st.y1);
+    launches++;
+  }
+  if (b.n_clip_items) {
+    k_clip_apply<<<(b.n_clip_items + 127) / 128, 128, 0, stream>>>(b);
+    launches++;
+  }
+  return launches;
 }
 
 // ---------------------------------------------------------------------------

@@ -24,8 +24,30 @@ struct PassDesc {
   int32_t cap[13];      // scratch capacities, see SliceLayout
   uint32_t clipped;     // 1: clip (device-space LTRB) bounds the scan; 0: kMaxCullRect
   float clip[4];
+  uint32_t path_clip;   // the path-clip state the draw is under (1-based; 0: none)
+  uint32_t pad2;
 };
-enum : uint32_t { kPassStroke = 1, kPassEvenOdd = 2, kPassSrcOver = 4 };
+// kPassRawSpans: the sweep stores the raster's spans as they are (any x,
+// zero coverage kept; ClipSpanRaw format) for the path-clip stages;
+// kPassClipPath: the pass rasterises a ClipPath path (never composited, all
+// of its rows kept, on the canvas or not)
+enum : uint32_t {
+  kPassStroke = 1,
+  kPassEvenOdd = 2,
+  kPassSrcOver = 4,
+  kPassRawSpans = 8,
+  kPassClipPath = 16
+};
+
+// One Canvas::ClipPath call (SWCanvas::OnClipPath, sw_canvas.cc:317-336) on
+// top of its parent state; its span rows are computed on the device.
+struct ClipStateDesc {
+  uint32_t parent;      // 1-based index of the parent state in the batch (0: none)
+  uint32_t op;          // Canvas::ClipOp: 0 kDifference, 1 kIntersect
+  uint32_t pass;        // the pass rasterising the clip path
+  int32_t y0, y1;       // rows of this state's span list (its path's and its parent's)
+  uint32_t rbase;       // first entry of its rows in DevBatch::clip_rows
+};
 
 struct DrawDesc {  // a Path inside the batch's verb/point/weight arrays
   uint32_t v0, nv, p0, np, w0, nw;
@@ -143,6 +165,13 @@ struct DevBatch {
   unsigned int* task_next;   // persistent compositor's work counters (temp, main)
   unsigned int* sweep_done;  // per sweep form, CTAs finished (zeroed before the sweeps);
                              // null: the forms' launches do not overlap
+  // path clips
+  const ClipStateDesc* clip_states;  // [n_clip_states]
+  uint32_t n_clip_states;
+  uint32_t* clip_flags;       // per state: [0] its span list is not empty, [1] its op
+  uint2* clip_rows;           // per state row: (first span, count) in the span pool
+  const uint2* clip_items;    // (pass, canvas row) of the draws under a path clip
+  uint32_t n_clip_items;
 };
 
 // Shared memory of one register-sweep warp: its RegSharedT block, then an
@@ -154,6 +183,9 @@ constexpr int32_t kRegDiffMax = 3072;
 // number of launches made
 int LaunchGeometry(const DevBatch& b, cudaStream_t stream);
 int LaunchSweep(const DevBatch& b, cudaStream_t stream);
+// the path-clip stages after the sweeps; states: the host copy of b.clip_states
+int LaunchPathClips(const DevBatch& b, const ClipStateDesc* states, uint32_t n_states,
+                    cudaStream_t stream);
 // ctas_per_sm > 0: a persistent grid of ctas_per_sm CTAs per SM taking row
 // tiles from `counter` (zeroed before the launch); 0: one warp per tile.
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,

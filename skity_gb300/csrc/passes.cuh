@@ -166,7 +166,10 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
   g.acc_left = (int)rb.l;
   g.acc_width = (int)(rb.r - rb.l);
   g.scan_top = rb.st;
-  int r0 = max_(g.start_y, 0), r1 = min_(g.stop_y, (int)cd.h);
+  // canvas rows; a ClipPath pass keeps all of its rows (the clip's span list
+  // is empty or not over all rows, SWCanvas::State::HasClip)
+  const bool all_rows = (pd.flags & kPassClipPath) != 0;
+  int r0 = all_rows ? g.start_y : max_(g.start_y, 0), r1 = all_rows ? g.stop_y : min_(g.stop_y, (int)cd.h);
   if (r0 < r1) {
     g.row0 = r0;
     g.row1 = r1;
@@ -191,15 +194,25 @@ SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
 }
 
 // keep() applies the clipping of SWSpanBrush::Brush and drops spans whose
-// alpha & global alpha is 0 under src-over (they blend to nothing).
+// alpha & global alpha is 0 under src-over (they blend to nothing).  A raw
+// sink (the passes of the path-clip stages) keeps every span of its rows as
+// the raster made it, in the raw format of pack().
 struct SinkBase {
   int row0, row1, W, H;
   uint32_t ga;
   bool srcover;
+  bool raw;
   SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
     if (y < row0 || y >= row1) return false;
+    if (raw) return true;
     if (!ClipSpan(x, y, len, W, H)) return false;
     return !(srcover && (a & ga) == 0);
+  }
+  // A stored span: x | len << 16 and the alpha; raw: x (int32) and
+  // len | alpha << 24.
+  SKC_HD uint2 pack(int x, int len, uint32_t a) const {
+    return raw ? make_uint2((uint32_t)x, ((uint32_t)len & 0xFFFFFFu) | (a << 24))
+               : make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
   }
 };
 
@@ -348,7 +361,7 @@ struct PoolSink : SinkBase {
       auto put = [&](int s0, int w, int32_t a) {
         int x = left + s0, len = w;
         if (keep(x, y, len, (uint8_t)a)) {
-          out[cnt++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)a);
+          out[cnt++] = pack(x, len, (uint32_t)a);
           fr += (unsigned)len;
         }
       };
@@ -380,7 +393,7 @@ struct PoolSink : SinkBase {
       if (keep(x, y, len, (uint8_t)open_v)) {
         const uint64_t at = reserve(L, 0, 1);
         if (!dead && L.leader())
-          pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
+          pool[at] = pack(x, len, (uint32_t)open_v);
         commit(L, 1, L.leader() ? (unsigned)len : 0u);
       }
     }
@@ -476,7 +489,7 @@ struct PoolSink : SinkBase {
       auto put = [&](int s0, int w, int32_t a) {
         int x = left + s0, len = w;
         if (keep(x, y, len, (uint8_t)a)) {
-          out[cnt++] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)a);
+          out[cnt++] = pack(x, len, (uint32_t)a);
           fr += (unsigned)len;
         }
       };
@@ -517,7 +530,7 @@ struct PoolSink : SinkBase {
       int x = left + open_start, len = hi - open_start;
       if (keep(x, y, len, (uint8_t)open_v)) {
         const uint64_t at = reserve(L, 0, 1);
-        if (!dead && L.leader()) pool[at] = make_uint2((uint32_t)x | ((uint32_t)len << 16), (uint32_t)open_v);
+        if (!dead && L.leader()) pool[at] = pack(x, len, (uint32_t)open_v);
         commit(L, 1, L.leader() ? (unsigned)len : 0u);
       }
     }
@@ -535,6 +548,7 @@ SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, PoolS
   s->H = (int)cd.h;
   s->ga = pd.ga;
   s->srcover = (pd.flags & kPassSrcOver) != 0;
+  s->raw = (pd.flags & kPassRawSpans) != 0;
   s->pool = b.spans;
   s->cap = b.span_cap;
   s->next = b.span_next;

@@ -143,7 +143,14 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
       cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s);
       cudaMemsetAsync(ctx->span_next.p, 0, 8, s);
       cudaMemsetAsync(b.sweep_done, 0, 16, s);
-      return LaunchSweep(b, s);
+      {
+        int n = LaunchSweep(b, s);
+        if (b.n_clip_states || b.n_clip_items) {
+          cudaMemsetAsync(b.clip_flags, 0, 8 * (size_t)std::max<uint32_t>(b.n_clip_states, 1), s);
+          n += LaunchPathClips(b, hb.clip_states.data(), b.n_clip_states, s);
+        }
+        return n;
+      }
     case 2:
       if (db.h_tasks_temp.empty()) return 0;
       cudaMemsetAsync(b.task_next, 0, 4, s);
@@ -353,6 +360,15 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   std::vector<uint32_t> order;
   SweepOrder(db.h_geom, order);
   SKC_TRY(Upload(db.sweep_order, order, s));
+  // path clips: the states' rows and the clipped draws' (pass, row) items
+  std::vector<uint2> clip_items;
+  const uint64_t clip_state_rows = PlanPathClips(hb, db.h_geom, clip_items);
+  if (clip_state_rows >= 0xFFFFFFFFull || clip_items.size() >= 0xFFFFFFFFull)
+    return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+  if (!hb.clip_states.empty()) SKC_TRY(Upload(db.clip_states, hb.clip_states, s));
+  SKC_TRY(db.clip_flags.ensure(8 * std::max<size_t>(hb.clip_states.size(), 1)));
+  SKC_TRY(db.clip_rows.ensure(8 * std::max<uint64_t>(clip_state_rows, 1)));
+  if (!clip_items.empty()) SKC_TRY(Upload(db.clip_items, clip_items, s));
   // span indices are 32-bit
   const uint64_t kMaxPool = 0xFFFFFFFFull;
   uint64_t want = std::min<uint64_t>(std::max<uint64_t>(pl.span_estimate, 1 << 16), kMaxPool);
@@ -387,6 +403,12 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.task_next = db.task_next.as<unsigned int>();
   b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.span_next = ctx->span_next.as<unsigned long long>();
+  b.clip_states = db.clip_states.as<ClipStateDesc>();
+  b.n_clip_states = (uint32_t)hb.clip_states.size();
+  b.clip_flags = db.clip_flags.as<uint32_t>();
+  b.clip_rows = db.clip_rows.as<uint2>();
+  b.clip_items = db.clip_items.as<uint2>();
+  b.n_clip_items = (uint32_t)clip_items.size();
   // The sweep; if the span pool ran out it is grown to the size the sweep
   // reported and the sweep runs again (first renders of a context only).
   double discarded_ms = 0;
@@ -400,15 +422,24 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     SKC_TRY(cudaMemsetAsync(b.sweep_done, 0, 16, s));
     SKC_TRY(cudaEventRecord(ctx->stage[4], s));
     st.kernel_launches += LaunchSweep(b, s);
+    if (b.n_clip_states || b.n_clip_items) {  // the path-clip stages use the span pool too
+      SKC_TRY(cudaMemsetAsync(b.clip_flags, 0, 8 * (size_t)std::max<uint32_t>(b.n_clip_states, 1), s));
+      st.kernel_launches += LaunchPathClips(b, hb.clip_states.data(), b.n_clip_states, s);
+    }
     SKC_TRY(cudaEventRecord(ctx->stage[5], s));
     SKC_TRY(cudaGetLastError());
     unsigned long long used = 0;
     SKC_TRY(cudaMemcpyAsync(&used, ctx->span_next.p, 8, cudaMemcpyDeviceToHost, s));
     SKC_TRY(cudaStreamSynchronize(s));
     if (used <= b.span_cap) break;
-    if (attempt == 2 || used > kMaxPool) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+    // the path-clip stages read rows the sweep wrote: a row past the end of
+    // a short pool reads as empty, so a chain of clip states can show more
+    // need on each try; with clips the pool doubles
+    const int attempts = 3 + (int)hb.clip_states.size();
+    if (attempt == attempts - 1 || used > kMaxPool) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
     discarded_ms += StageMs(ctx, 4, 5);
-    const uint64_t grow = std::min<uint64_t>(used + used / 16, kMaxPool);
+    const uint64_t grow =
+        std::min<uint64_t>(hb.clip_states.empty() ? used + used / 16 : 2 * used, kMaxPool);
     if (ctx->budget && grow * sizeof(uint2) > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
     ctx->span_pool.release();
     SKC_TRY(ctx->span_pool.ensure(grow * sizeof(uint2)));
@@ -529,6 +560,7 @@ struct skity_cuda_canvas_s {
   struct State {
     float tx = 0.f, ty = 0.f;
     float clip[4] = {-1e9f, -1e9f, 1e9f, 1e9f};  // kMaxCullRect
+    uint32_t path_clip = 0;  // the path-clip state (1-based in clip_states; 0: none)
   };
   State st;
   std::vector<State> saved;
@@ -536,6 +568,11 @@ struct skity_cuda_canvas_s {
   bool any_clip = false;
   std::vector<skc::ColorFilterRec> filters;  // per recorded draw: its colour filter
   bool any_filter = false;
+  // path clips: the ClipPath calls (with their paths) and each draw's state
+  std::vector<skc::ClipStateRec> clip_states;
+  std::vector<uint8_t> clip_verbs;
+  std::vector<float> clip_pts, clip_wts;
+  std::vector<uint32_t> draw_clip_state;
   skc::DeviceBatch db;
 };
 
@@ -750,6 +787,33 @@ SKITY_CUDA_API void skity_cuda_canvas_destroy(skity_cuda_canvas canvas) { delete
 SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const float color[4]) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!color) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->st.path_clip) {
+    // SWCanvas::OnDrawPaint under a path clip (sw_canvas.cc:413-439): the
+    // canvas rect, rasterised with no matrix and no clip bounds, clipped by
+    // the state, brushed with kSrc
+    const float w = (float)canvas->width, h = (float)canvas->height;
+    const uint8_t verbs[5] = {SKITY_CUDA_VERB_MOVE, SKITY_CUDA_VERB_LINE, SKITY_CUDA_VERB_LINE,
+                              SKITY_CUDA_VERB_LINE, SKITY_CUDA_VERB_CLOSE};
+    const float pts[8] = {0.f, 0.f, w, 0.f, w, h, 0.f, h};
+    skity_cuda_path path{};
+    path.verbs = verbs;
+    path.verb_count = 5;
+    path.points = pts;
+    path.point_count = 4;
+    skity_cuda_paint paint{};
+    paint.blend_mode = 1;  // kSrc
+    std::memcpy(paint.fill_color, color, 16);
+    std::memcpy(paint.stroke_color, color, 16);
+    paint.stroke_width = 1.f;
+    paint.miter_limit = 4.f;
+    const skity_cuda_canvas_s::State keep = canvas->st;
+    canvas->st.tx = canvas->st.ty = 0.f;
+    canvas->st.clip[0] = canvas->st.clip[1] = -1e9f;
+    canvas->st.clip[2] = canvas->st.clip[3] = 1e9f;
+    const int32_t rc = skity_cuda_canvas_draw_path(canvas, &path, &paint);
+    canvas->st = keep;
+    return rc;
+  }
   // a kSrc fill of the whole canvas overwrites everything drawn before
   canvas->has_clear = true;
   std::memcpy(canvas->clear, color, 16);
@@ -767,6 +831,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
   canvas->any_clip = false;
   canvas->filters.clear();
   canvas->any_filter = false;
+  canvas->draw_clip_state.clear();
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -873,6 +938,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
     canvas->any_filter = true;
   }
   canvas->filters.push_back(fr);
+  canvas->draw_clip_state.push_back(canvas->st.path_clip);
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -900,6 +966,76 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, flo
   if (!std::isfinite(dx) || !std::isfinite(dy)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   canvas->st.tx = canvas->st.tx + dx;
   canvas->st.ty = canvas->st.ty + dy;
+  return SKITY_CUDA_SUCCESS;
+}
+
+// Canvas::ClipPath(path, op) (canvas.cc:157-162; SWCanvas::OnClipPath,
+// sw_canvas.cc:317-336): a new path-clip state on top of the current one,
+// recorded with the canvas translation and the global clip bounds, which a
+// kIntersect clip first narrows by the path's bounds (Path::GetBounds,
+// path.cc:1341-1360).
+SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
+                                                   const skity_cuda_path* path, uint32_t op) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!path || op > 1 || (path->verb_count && !path->verbs) ||
+      (path->point_count && !path->points) || (path->conic_weight_count && !path->conic_weights))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  uint32_t need_p = 0, need_w = 0;
+  for (uint32_t i = 0; i < path->verb_count; ++i) {
+    switch (path->verbs[i]) {
+      case SKITY_CUDA_VERB_MOVE: case SKITY_CUDA_VERB_LINE: need_p += 1; break;
+      case SKITY_CUDA_VERB_QUAD: need_p += 2; break;
+      case SKITY_CUDA_VERB_CONIC: need_p += 2; need_w += 1; break;
+      case SKITY_CUDA_VERB_CUBIC: need_p += 3; break;
+      case SKITY_CUDA_VERB_CLOSE: break;
+      default: return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    }
+  }
+  if (need_p != path->point_count || need_w != path->conic_weight_count)
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (!skc::ValidPath(path->verbs, path->verb_count, path->points, path->point_count,
+                      path->conic_weights, path->conic_weight_count))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  float t[2] = {canvas->st.tx, canvas->st.ty};
+  if (!skc::ValidTranslate(t, path->points, path->point_count)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (op == 1) {
+    // the path's bounds: its points but a trailing move
+    uint32_t n = path->point_count;
+    if (path->verb_count > 1 && path->verbs[path->verb_count - 1] == SKITY_CUDA_VERB_MOVE) n--;
+    float l = 0.f, tp = 0.f, r = 0.f, b = 0.f;
+    for (uint32_t i = 0; i < n; ++i) {
+      const float x = path->points[2 * i], y = path->points[2 * i + 1];
+      if (i == 0) {
+        l = r = x;
+        tp = b = y;
+      } else {
+        l = std::min(l, x);
+        r = std::max(r, x);
+        tp = std::min(tp, y);
+        b = std::max(b, y);
+      }
+    }
+    const int32_t rc = skity_cuda_canvas_clip_rect(canvas, l, tp, r, b);
+    if (rc) return rc;
+  }
+  skc::ClipStateRec c;
+  std::memset(&c, 0, sizeof c);
+  c.parent = canvas->st.path_clip;
+  c.op = op;
+  c.fill_type = path->fill_type ? 1u : 0u;
+  c.nv = path->verb_count;
+  c.np = path->point_count;
+  c.nw = path->conic_weight_count;
+  c.translate[0] = canvas->st.tx;
+  c.translate[1] = canvas->st.ty;
+  std::memcpy(c.bounds, canvas->st.clip, sizeof c.bounds);
+  canvas->clip_states.push_back(c);
+  canvas->clip_verbs.insert(canvas->clip_verbs.end(), path->verbs, path->verbs + path->verb_count);
+  canvas->clip_pts.insert(canvas->clip_pts.end(), path->points, path->points + 2 * (size_t)path->point_count);
+  canvas->clip_wts.insert(canvas->clip_wts.end(), path->conic_weights,
+                          path->conic_weights + path->conic_weight_count);
+  canvas->st.path_clip = (uint32_t)canvas->clip_states.size();
+  canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -956,6 +1092,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   sv.stop_offsets = canvas->stop_offsets.data();
   sv.clips = canvas->any_clip ? canvas->clips.data() : nullptr;
   sv.filters = canvas->any_filter ? canvas->filters.data() : nullptr;
+  if (!canvas->clip_states.empty()) {
+    sv.n_clip_states = (uint32_t)canvas->clip_states.size();
+    sv.clip_states = canvas->clip_states.data();
+    sv.clip_verbs = canvas->clip_verbs.data();
+    sv.clip_pts = canvas->clip_pts.data();
+    sv.clip_wts = canvas->clip_wts.data();
+    sv.draw_clip_state = canvas->draw_clip_state.data();
+  }
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
   int32_t rc = skc::AddStreamCanvas(db.hb, sv);
@@ -994,6 +1138,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->any_clip = false;
   canvas->filters.clear();
   canvas->any_filter = false;
+  canvas->draw_clip_state.clear();
   canvas->dirty = false;
   return SKITY_CUDA_SUCCESS;
 }

@@ -177,7 +177,7 @@ SKC_HD void RegBlitFlush(const Lanes& L, RegSharedT<M>& sh, Sink* sink, AccState
       if (t.real) {
         if (sink->keep(x, y, len, a)) {
           kept = true;
-          v = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+          v = sink->pack(x, len, a);
           frags += (unsigned)len;
         }
       } else {

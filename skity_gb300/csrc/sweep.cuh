@@ -520,7 +520,7 @@ struct LaneSweep {
       if (!s->sink->keep(x, y, len, a)) return;
       kept++;
       frags += (unsigned)len;
-      if (write) *write++ = make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+      if (write) *write++ = s->sink->pack(x, len, a);
     }
     SKC_HD void acc(int x, int len, uint8_t a) {
       if (!do_acc) return;

@@ -71,6 +71,14 @@ int32_t skity_cuda_canvas_translate(skity_cuda_canvas, float dx, float dy) {
   std::printf("translate %g %g\n", dx, dy);
   return SKITY_CUDA_SUCCESS;
 }
+int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas, const skity_cuda_path* p, uint32_t op) {
+  std::printf("clip_path op=%u fill=%u verbs=", op, p->fill_type);
+  for (uint32_t i = 0; i < p->verb_count; ++i) std::printf("%u,", p->verbs[i]);
+  std::printf(" points=");
+  for (uint32_t i = 0; i < 2 * p->point_count; ++i) std::printf("%g,", p->points[i]);
+  std::printf("\n");
+  return SKITY_CUDA_SUCCESS;
+}
 int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas, float l, float t, float r, float b) {
   std::printf("clip %g %g %g %g\n", l, t, r, b);
   return SKITY_CUDA_SUCCESS;

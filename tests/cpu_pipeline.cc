@@ -11,6 +11,7 @@
 
 #include "../skity_gb300/csrc/batch.h"
 #include "../skity_gb300/csrc/passes.cuh"
+#include "../skity_gb300/csrc/clip.cuh"
 
 using namespace skc;
 
@@ -106,11 +107,27 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   std::vector<uint32_t> order;
   SweepOrder(geom, order);
   b.sweep_order = order.data();
+  // path clips (the device's k_clip_state / k_clip_apply, in launch order)
+  std::vector<uint2> clip_items;
+  const uint64_t clip_state_rows = PlanPathClips(hb, geom, clip_items);
+  std::vector<uint32_t> clip_flags(2 * hb.clip_states.size() + 2, 0);
+  std::vector<uint2> clip_rows(clip_state_rows + 1);
+  b.clip_states = hb.clip_states.data();
+  b.n_clip_states = (uint32_t)hb.clip_states.size();
+  b.clip_flags = clip_flags.data();
+  b.clip_rows = clip_rows.data();
+  b.clip_items = clip_items.data();
+  b.n_clip_items = (uint32_t)clip_items.size();
+  std::vector<int32_t> clip_order(kClipRowCap);
   // span pool: start small so that the regrowth path runs too
   std::vector<uint2> pool(pool_hint ? pool_hint : 1024);
   unsigned long long next = 0;
   uint64_t generic = 0, spans = 0;
-  for (int attempt = 0; attempt < 3; ++attempt) {
+  // the path-clip stages read rows the sweep wrote: a row past the end of a
+  // short pool reads as empty, so a chain of clip states can show more need
+  // on each try (the pool doubles until it holds everything)
+  const int attempts = 3 + (int)hb.clip_states.size();
+  for (int attempt = 0; attempt < attempts; ++attempt) {
     std::fill(rowspan.begin(), rowspan.end(), make_uint2(0, 0));
     std::fill(pclass.begin(), pclass.end(), (uint8_t)(mode == 1 ? 1 : 0));
     next = 0;
@@ -142,9 +159,15 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
       if (SweepForm(geom[p], pclass[p]) == kSweepReg32)
         SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
     }
+    std::fill(clip_flags.begin(), clip_flags.end(), 0u);
+    for (uint32_t k = 1; k <= b.n_clip_states; ++k) {
+      const ClipStateDesc& st = hb.clip_states[k - 1];
+      for (int32_t y = st.y0; y < st.y1; ++y) ClipStateStage(b, k, y, clip_order.data());
+    }
+    for (uint32_t i = 0; i < b.n_clip_items; ++i) ClipApplyStage(b, i, clip_order.data());
     if (next <= pool.size()) break;
-    if (attempt == 2) return -7;
-    pool.assign(next, make_uint2(0, 0));
+    if (attempt == attempts - 1) return -7;
+    pool.assign(hb.clip_states.empty() ? next : 2 * next, make_uint2(0, 0));
   }
   for (uint32_t p = 0; p < np; ++p) spans += pass_spans[p];
   b.brushes = hb.brushes.data();

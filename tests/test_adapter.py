@@ -57,40 +57,52 @@ def test_shaders_and_mask_filter(driver_output):
 
 
 def test_translation_forwarded_other_matrices_refused(driver_output):
+    # Canvas::Save reaches the C ABI (its save level keeps the path clips);
     # Translate(5, 0) then Translate(0.5, -2): one translation of (5.5, -2)
     # around the draw; a scaled matrix is outside the GPU path (-5)
-    assert driver_output[9:12] == ["save", "translate 5.5 -2", driver_output[11]]
-    assert driver_output[11].startswith("draw verbs=0,1,2,3,4,5,")
-    assert driver_output[12:14] == ["restore", "status=0"]
-    assert driver_output[14] == "status=-5"
+    assert driver_output[9:12] == ["save", "save", "translate 5.5 -2"]
+    assert driver_output[12].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[13:16] == ["restore", "status=0", "status=-5"]
+    assert driver_output[16] == "restore"
 
 
-def test_clip_rect_forwarded_other_clips_refused(driver_output):
+def test_clip_rect_forwarded(driver_output):
     # Translate(2, 1); ClipRect(1.5, 0, 30, 20) -> device (3.5, 1, 32, 21);
     # ClipRect(-5, 2, 25, 40) -> (-3, 3, 27, 41); the global clip bounds are
     # their intersection (3.5, 3, 27, 21), set before the translation
-    assert driver_output[15:18] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
-    assert driver_output[18].startswith("draw verbs=0,1,2,3,4,5,")
-    assert driver_output[19:21] == ["restore", "status=0"]
-    # a kDifference clip is refused and the draws under it draw nothing
-    assert driver_output[21] == "status=-5"
+    assert driver_output[17:21] == ["save", "save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[21].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[22:24] == ["restore", "status=0"]
+
+
+def test_difference_clip_rect_is_a_path_clip(driver_output):
+    # ClipRect(0, 0, 10, 10, kDifference) under Translate(2, 1): the rect's
+    # path (Canvas::OnClipRect) clipped on the C ABI canvas at this save
+    # level, with the global clip bounds and the translation of the call
+    assert driver_output[24:27] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[27] == "clip_path op=0 fill=0 verbs=0,1,1,1,5, points=0,0,10,0,10,10,0,10,"
+    assert driver_output[28] == "translate -2 -1"
+    # the draw under it is taken (the path clip is recorded on the state)
+    assert driver_output[29:32] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[32].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[33:37] == ["restore", "status=0", "restore", "restore"]
     # after the Restores the canvas is unclipped and untranslated again
-    assert driver_output[22].startswith("draw verbs=0,1,2,3,4,5,")
-    assert driver_output[23] == "status=0"
+    assert driver_output[37].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[38] == "status=0"
 
 
 def test_sweep_and_conical_shaders_forwarded(driver_output):
     # MakeSweep(20, 15, 90, 270): GradientInfo radius = (bias, scale) =
     # (-0.25, 2); MakeTwoPointConical keeps both circles
-    sweep, conical = driver_output[24], driver_output[25]
+    sweep, conical = driver_output[39], driver_output[40]
     assert "shader=3 tile=1 stops=3 offsets=1 p0=20,15" in sweep and "r=-0.25" in sweep
     assert "shader=4 tile=0 stops=3 offsets=0 p0=5,6 p1=30,20 r=2" in conical
-    assert driver_output[26] == "status=0"
+    assert driver_output[41] == "status=0"
 
 
 def test_color_filters_forwarded(driver_output):
-    blend, matrix, gamma = driver_output[27:30]
+    blend, matrix, gamma = driver_output[42:45]
     assert " filter=1 mode=14 color=80102030 " in blend
     assert " filter=2 mode=0 color=00000000 m=0,1,0,0,0.25,1,0,0,0,0,0,0,1,0,0,0,0,0,0.5,0," in matrix
     assert " filter=4 " in gamma
-    assert driver_output[30:] == ["status=0", "flush", "status=0", "destroy 0x10"]
+    assert driver_output[45:] == ["status=0", "flush", "status=0", "destroy 0x10"]

@@ -191,3 +191,24 @@ def test_color_filters_bit_exact(cpu_pipeline, oracle_lib):
     got, _ = cpu_render(cpu_pipeline, sc)
     ref, _ = oracle_lib.render(sc)
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_clip_path_bit_exact(cpu_pipeline, oracle_lib, seed):
+    """Canvas::ClipPath states (intersect / difference, nested) computed row
+    by row and applied to the draws' rows, against the oracle."""
+    from test_oracle_pin import path_clips_scene
+    sc = path_clips_scene(S.SEED_BASE + 399 + seed)
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, ref)
+    assert c["bad_pixels"] == 0, c
+
+
+def test_clip_path_cases_bit_exact(cpu_pipeline, oracle_lib):
+    from test_oracle_pin import clip_path_cases_scene
+    sc = clip_path_cases_scene()
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, ref)
+    assert c["bad_pixels"] == 0, c

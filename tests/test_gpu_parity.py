@@ -314,3 +314,54 @@ def test_color_filters_match_oracle(gpu_ctx, oracle_lib):
         sb.draw_path(tri.verbs, tri.points, paint.rec.copy(), color_filter=f.record())
     canvas.Flush()
     check(oracle_lib, bitmap, sb.build())
+
+
+@pytest.mark.gpu
+def test_clip_path_matches_oracle(gpu_ctx, oracle_lib):
+    """Canvas::ClipPath (intersect and difference, nested under Save /
+    Restore, with ClipRect and Translate) through the batch entry point, and
+    through the canvas API with a Clear under a path clip."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_pin import clip_path_cases_scene, path_clips_scene
+    from skity_gb300.canvas import Canvas, Paint, Path
+    scenes = [path_clips_scene(S.SEED_BASE + 399 + k) for k in range(4)] + [clip_path_cases_scene()]
+    for sc, got in zip(scenes, gpu_ctx.render_streams(scenes)):
+        c = check(oracle_lib, got, sc)
+        assert c["bad_pixels"] == 0, c
+    bitmap = np.zeros((40, 48, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    tri = Path().MoveTo(2, 2).LineTo(46, 6).LineTo(8, 38).Close()
+    band = Path().MoveTo(0, 12).LineTo(48, 12).LineTo(48, 24).LineTo(0, 24).Close()
+    canvas.Save()
+    canvas.ClipPath(tri, 1)
+    canvas.Clear((0.2, 0.4, 0.9, 1.0))  # DrawPaint under the clip
+    canvas.Save()
+    canvas.Translate(1.5, 0.5)
+    canvas.ClipPath(band, 0)
+    canvas.DrawPath(Path().MoveTo(0, 0).LineTo(48, 0).LineTo(48, 40).LineTo(0, 40).Close(),
+                    Paint().SetFillColor(0.9, 0.2, 0.1, 0.7))
+    canvas.Restore()
+    canvas.Restore()
+    canvas.DrawPath(band, Paint().SetFillColor(0.1, 0.8, 0.2, 0.5))
+    canvas.Flush()
+    sb = S.SceneBuilder(48, 40)
+    sb.save()
+    sb.clip_path(tri.verbs, tri.points, S.CLIP_INTERSECT)
+    glob = S.map_clip(S.NO_CLIP, (2, 2, 46, 38))
+    p = S.default_paint()
+    p["blend"], p["fill_color"] = S.BLEND_SRC, (0.2, 0.4, 0.9, 1.0)
+    sb.draw_path([S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE], [[0, 0], [48, 0], [48, 40], [0, 40]], p)
+    sb.save()
+    sb.clip_path(band.verbs, band.points, S.CLIP_DIFFERENCE, translate=(1.5, 0.5), bounds=glob)
+    q = S.default_paint()
+    q["fill_color"], q["translate"] = (0.9, 0.2, 0.1, 0.7), (1.5, 0.5)
+    sb.draw_path([S.MOVE, S.LINE, S.LINE, S.LINE, S.CLOSE], [[0, 0], [48, 0], [48, 40], [0, 40]], q,
+                 clip=glob)
+    sb.restore()
+    sb.restore()
+    r = S.default_paint()
+    r["fill_color"] = (0.1, 0.8, 0.2, 0.5)
+    sb.draw_path(band.verbs, band.points, r)
+    check(oracle_lib, bitmap, sb.build())
