@@ -792,6 +792,17 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     DerivedCaps(pd.cap, false);
     main_passes.push_back(pd);
   }
+  // canvases with passes the compositor's common form does not take
+  auto general = [&](const std::vector<PassDesc>& ps) {
+    for (const PassDesc& pd : ps) {
+      if (pd.flags & kPassClipPath) continue;
+      const Brush& br = hb.brushes[pd.brush];
+      if (br.kind >= 4 || br.cf_type != 0 || br.blend > 3) return 1u;
+    }
+    return 0u;
+  };
+  hb.canvases[cidx].general = general(main_passes);
+  for (auto& tpp : temps) hb.canvases[tpp.first].general = general(tpp.second);
   hb.canvases[cidx].pass0 = (uint32_t)hb.passes.size();
   for (uint32_t i = 0; i < (uint32_t)clip_pass_pos.size(); ++i)
     hb.clip_states[state_base + i].pass = hb.canvases[cidx].pass0 + clip_pass_pos[i];

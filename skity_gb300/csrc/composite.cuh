@@ -147,6 +147,28 @@ SKC_HD uint32_t PorterDuff(uint32_t src, uint32_t dst, uint32_t mode) {
   }
 }
 
+// BlendPixel for the modes the compositor's common form takes: kClear,
+// kSrc, kDst, kSrcOver (their FastBlend rules and PMSrcOver).
+SKC_HD uint32_t BlendPixelCommon(uint32_t dst, uint32_t src, uint32_t mode) {
+  switch (mode) {
+    case 0: return 0;
+    case 1: return src;
+    case 2: return dst;
+    default: {
+      const uint32_t a = GetA(src);
+      if (a == 0) return dst;
+      if (a == 255) return src;
+      return PMSrcOver(src, dst);
+    }
+  }
+}
+
+// PorterDuff out of line: the compositor's loop keeps only the common modes'
+// code (its registers are budgeted for the residency it runs at).
+SKC_HDN uint32_t PorterDuffOutOfLine(uint32_t src, uint32_t dst, uint32_t mode) {
+  return PorterDuff(src, dst, mode);
+}
+
 // SWRenderTarget::BlendPixel (sw_render_target.cc:12-35): the FastBlend
 // shortcuts (:89-141), else PorterDuffBlend; returns the new destination.
 SKC_HD uint32_t BlendPixel(uint32_t dst, uint32_t src, uint32_t mode) {
@@ -178,7 +200,7 @@ SKC_HD uint32_t BlendPixel(uint32_t dst, uint32_t src, uint32_t mode) {
     default:
       break;
   }
-  return PorterDuff(src, dst, mode);
+  return PorterDuffOutOfLine(src, dst, mode);
 }
 
 // One pixel of MaskFilterOnFilter's combine (mask_filter.cc:61-100) for
@@ -210,8 +232,21 @@ SKC_HD uint32_t PMColorToColor(uint32_t c) {
 // ColorFilter::FilterColor (color_filter.cc:56-186) of a premultiplied
 // colour.  tables: [0, 256) linear->sRGB, [256, 512) sRGB->linear;
 // matrices: int16 terms (row_major * 255, truncated), 4 rows of 5.
+SKC_HDN uint32_t FilterColorOutOfLine(uint32_t cf_type, uint32_t cf_mode, uint32_t cf_pm,
+                                      uint32_t cf_index, uint32_t c, const uint8_t* tables,
+                                      const int16_t* matrices);
 SKC_HD uint32_t FilterColor(const Brush& b, uint32_t c, const uint8_t* tables,
                             const int16_t* matrices) {
+  return FilterColorOutOfLine(b.cf_type, b.cf_mode, b.cf_pm, b.cf_index, c, tables, matrices);
+}
+SKC_HDN uint32_t FilterColorOutOfLine(uint32_t cf_type, uint32_t cf_mode, uint32_t cf_pm,
+                                      uint32_t cf_index, uint32_t c, const uint8_t* tables,
+                                      const int16_t* matrices) {
+  Brush b;
+  b.cf_type = cf_type;
+  b.cf_mode = cf_mode;
+  b.cf_pm = cf_pm;
+  b.cf_index = cf_index;
   switch (b.cf_type) {
     case 1:  // BlendColorFilter: PorterDuffBlend(filter colour, c, mode)
       return PorterDuff(b.cf_pm, c, b.cf_mode);
@@ -361,21 +396,60 @@ SKC_HD bool ConicalT(const ConicalParams& c, int x, int y, float* t_out) {
 // CalculateColor of the pass's brush at pixel (x, y), premultiplied ARGB.
 // roundtrip[v] = Color4fToColor(Color4fFromColor(v)) per channel, the
 // PixmapBrush sampler's colour round trip (bitmap_sampler.cc:21-29,93-107).
-SKC_HD uint32_t BrushColor(const Brush& b, int x, int y, const float4* colors, const float* offsets,
-                           const uint8_t* images, const uint8_t* roundtrip,
-                           const ConicalParams* conicals) {
-  if (b.kind == 0) return b.solid;
-  if (b.kind == 5) {
-    float t;
-    if (!ConicalT(conicals[b.conical], x, y, &t)) return 0;
-    return GradientColor(b, t, colors, offsets);
+// The sweep and two-point conical brushes out of line (they are rare, and
+// their code would crowd the compositor's loop): the brush's gradient
+// fields by value.
+SKC_HDN uint32_t OtherGradientColor(uint32_t kind, uint32_t tile, uint32_t stop_count,
+                                    uint32_t has_offsets, uint32_t stop0, float bias, float scale,
+                                    uint32_t conical, float mx, float my, int x, int y,
+                                    const float4* colors, const float* offsets,
+                                    const ConicalParams* conicals) {
+  Brush g;
+  g.tile = tile;
+  g.stop_count = stop_count;
+  g.has_offsets = has_offsets;
+  g.stop0 = stop0;
+  g.bias = bias;
+  g.scale = scale;
+  float t;
+  if (kind == 5) {
+    if (!ConicalT(conicals[conical], x, y, &t)) return 0;
+  } else {
+    t = SweepT(g, mx, my);
   }
+  return GradientColor(g, t, colors, offsets);
+}
+
+// BrushColor for the solid, linear, radial and image brushes.
+SKC_HD uint32_t BrushColorCommon(const Brush& b, int x, int y, const float4* colors,
+                                 const float* offsets, const uint8_t* images,
+                                 const uint8_t* roundtrip) {
+  if (b.kind == 0) return b.solid;
   float sx = x + 0.5f, sy = y + 0.5f;
   float mx = sx * b.m[0] + sy * b.m[1] + b.m[2];
   float my = sx * b.m[3] + sy * b.m[4] + b.m[5];
   if (b.kind == 1) return GradientColor(b, mx, colors, offsets);
   if (b.kind == 2) return GradientColor(b, sqrt_(mx * mx + my * my), colors, offsets);
-  if (b.kind == 4) return GradientColor(b, SweepT(b, mx, my), colors, offsets);
+  if (mx < 0.0f || mx >= 1.0f || my < 0.0f || my >= 1.0f) return 0;
+  uint32_t ix = (uint32_t)(mx * (float)b.img_w), iy = (uint32_t)(my * (float)b.img_h);
+  ix = min_(ix, b.img_w - 1);
+  iy = min_(iy, b.img_h - 1);
+  const uint8_t* px = images + b.img_off + ((size_t)iy * b.img_w + ix) * 4;
+  return ARGB(roundtrip[px[3]], roundtrip[px[0]], roundtrip[px[1]], roundtrip[px[2]]);
+}
+
+SKC_HD uint32_t BrushColor(const Brush& b, int x, int y, const float4* colors, const float* offsets,
+                           const uint8_t* images, const uint8_t* roundtrip,
+                           const ConicalParams* conicals) {
+  if (b.kind == 0) return b.solid;
+  float sx = x + 0.5f, sy = y + 0.5f;
+  float mx = sx * b.m[0] + sy * b.m[1] + b.m[2];
+  float my = sx * b.m[3] + sy * b.m[4] + b.m[5];
+  if (b.kind == 1) return GradientColor(b, mx, colors, offsets);
+  if (b.kind == 2) return GradientColor(b, sqrt_(mx * mx + my * my), colors, offsets);
+  if (b.kind >= 4)
+    return OtherGradientColor(b.kind, b.tile, b.stop_count, b.has_offsets, b.stop0, b.bias, b.scale,
+                              b.conical, mx, my, x, y, colors, offsets, conicals);
   // image brush, decal tiling, nearest sampling
   if (mx < 0.0f || mx >= 1.0f || my < 0.0f || my >= 1.0f) return 0;
   uint32_t ix = (uint32_t)(mx * (float)b.img_w), iy = (uint32_t)(my * (float)b.img_h);

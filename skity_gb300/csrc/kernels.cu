@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
   FinishOverlapped(b.sweep_done ? b.sweep_done + (kForm & 3) : nullptr);
 }
 
+template <bool kRaw>
 __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
   AllowNextLaunch();
   const uint32_t i = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) k_sweep(DevBatch b) {
     const uint32_t p = SweepPassAt(b, i);
     Lanes L;
     L.lane = threadIdx.x & 31;
-    if (SweepForm(b.geom[p], b.pass_class[p]) == kSweepGeneric) SweepPass(b, p, L);
+    if (SweepForm(b.geom[p], b.pass_class[p]) == kSweepGeneric) SweepPass<kRaw>(b, p, L);
   }
   FinishOverlapped(b.sweep_done ? b.sweep_done + kSweepGeneric : nullptr);
 }
@@ -148,7 +149,9 @@ int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   // heaviest form first: the longest sweeps start at once, and each later
   // (lighter) form fills the SMs the earlier ones' tails leave idle
   const bool overlap = b.sweep_done != nullptr;
-  LaunchOverlapped(k_sweep, dim3((b.n_passes + kSweepWarps - 1) / kSweepWarps),
+  // path-clip passes (raw spans) come only with clip states
+  LaunchOverlapped(b.n_clip_states ? k_sweep<true> : k_sweep<false>,
+                   dim3((b.n_passes + kSweepWarps - 1) / kSweepWarps),
                    dim3(32 * kSweepWarps), 0, stream, false, b);
   LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream, overlap);
   LaunchRegForm<64, kSweepReg64>(b, stream, overlap);
@@ -178,11 +181,17 @@ __host__ __device__ constexpr size_t CompWarpSmem(uint32_t chunk) {
   return (size_t)chunk * 4 + kStagedStops * (16 + 4);
 }
 
-__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
-                              float4* stage_colors, float* stage_offsets, int lane);
+template <bool kAll>
+__device__ __forceinline__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
+                                              float4* stage_colors, float* stage_offsets,
+                                              int lane);
 
 // counter == null: warp w of block k takes tile 4k + w; otherwise every warp
 // takes tiles from the counter until none is left (persistent grid).
+// kAll: the general form (every brush kind, colour filter and blend mode),
+// launched for batches with a general canvas; the common form has no calls
+// and keeps its loops in registers.
+template <bool kAll>
 __global__ void __launch_bounds__(32 * kCompWarps, kCompMinBlocks)
     k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk,
                 unsigned int* counter) {
@@ -195,7 +204,7 @@ __global__ void __launch_bounds__(32 * kCompWarps, kCompMinBlocks)
   float* stage_offsets = (float*)(stage_colors + kStagedStops);
   if (!counter) {
     const uint32_t task = blockIdx.x * kCompWarps + wib;
-    if (task < n_tasks) CompositeTile(b, tasks[task], row, stage_colors, stage_offsets, lane);
+    if (task < n_tasks) CompositeTile<kAll>(b, tasks[task], row, stage_colors, stage_offsets, lane);
     return;
   }
   for (;;) {
@@ -203,13 +212,89 @@ __global__ void __launch_bounds__(32 * kCompWarps, kCompMinBlocks)
     if (lane == 0) task = atomicAdd(counter, 1u);
     task = __shfl_sync(0xffffffffu, task, 0);
     if (task >= n_tasks) return;
-    CompositeTile(b, tasks[task], row, stage_colors, stage_offsets, lane);
+    CompositeTile<kAll>(b, tasks[task], row, stage_colors, stage_offsets, lane);
     __syncwarp();
   }
 }
 
-__device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
-                              float4* stage_colors, float* stage_offsets, int lane) {
+// The spans [s0, s1) of one pass row applied to the row tile.  kAll: every
+// brush kind, colour filter and blend mode; otherwise the common ones only
+// (solid, linear, radial and image brushes; clear, src, dst, src-over).
+template <bool kAll>
+__device__ __forceinline__ void CompositeSpans(const DevBatch& b, const Brush& br,
+                                               const float4* stop_colors,
+                                               const float* stop_offsets, uint32_t s0,
+                                               uint32_t s1, int x0, int x1, int y, uint32_t* row,
+                                               int lane) {
+  const uint2* sp = b.spans;
+  for (uint32_t sb = s0; sb < s1; sb += 32) {
+    int xs = 0, xe = 0;
+    uint32_t alpha = 0;
+    bool pending = false;
+    if (sb + lane < s1) {
+      const uint2 mine = sp[sb + lane];
+      const int sx = (int)(mine.x & 0xFFFF), slen = (int)(mine.x >> 16);
+      xs = max(sx, x0);
+      xe = min(sx + slen, x1);
+      alpha = mine.y & br.global_alpha;
+      pending = xs < xe;
+    }
+    // Spans are applied in batches: the longest run of pending spans
+    // (in emission order) in which each starts at or after the end of
+    // the one before.  Those are disjoint, so inside a batch the order
+    // does not matter: short spans are shaded by their own lane, long
+    // ones by the whole warp (pixel column mod 32 per lane).
+    uint32_t pmask = __ballot_sync(0xffffffffu, pending);
+    while (pmask) {
+      const uint32_t below = pmask & ((1u << lane) - 1u);
+      const int prev = below ? 31 - __clz(below) : lane;
+      const int prev_xe = __shfl_sync(0xffffffffu, xe, prev);
+      const bool clash = pending && below && prev_xe > xs;
+      const uint32_t cmask = __ballot_sync(0xffffffffu, clash);
+      const uint32_t batch = cmask ? pmask & ((1u << (__ffs(cmask) - 1)) - 1u) : pmask;
+      const bool mine_now = (batch >> lane) & 1u;
+      const bool is_short = xe - xs <= kShortSpan;
+      if (mine_now && is_short) {
+        for (int x = xs; x < xe; ++x) {
+          uint32_t c = kAll ? BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels,
+                                         b.roundtrip, b.conicals)
+                            : BrushColorCommon(br, x, y, stop_colors, stop_offsets, b.pixels,
+                                               b.roundtrip);
+          if (alpha != 255) c = AlphaMulQ(c, alpha);
+          if (kAll && br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
+          uint32_t& d = row[x - x0];
+          d = kAll ? BlendPixel(d, c, br.blend) : BlendPixelCommon(d, c, br.blend);
+        }
+      }
+      uint32_t lmask = __ballot_sync(0xffffffffu, mine_now && !is_short);
+      while (lmask) {
+        const int j = __ffs(lmask) - 1;
+        lmask &= lmask - 1;
+        const int qs = __shfl_sync(0xffffffffu, xs, j);
+        const int qe = __shfl_sync(0xffffffffu, xe, j);
+        const uint32_t qa = __shfl_sync(0xffffffffu, alpha, j);
+        for (int x = qs + ((lane - qs) & 31); x < qe; x += 32) {
+          uint32_t c = kAll ? BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels,
+                                         b.roundtrip, b.conicals)
+                            : BrushColorCommon(br, x, y, stop_colors, stop_offsets, b.pixels,
+                                               b.roundtrip);
+          if (qa != 255) c = AlphaMulQ(c, qa);
+          if (kAll && br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
+          uint32_t& d = row[x - x0];
+          d = kAll ? BlendPixel(d, c, br.blend) : BlendPixelCommon(d, c, br.blend);
+        }
+      }
+      __syncwarp();
+      if (mine_now) pending = false;
+      pmask &= ~batch;
+    }
+  }
+}
+
+template <bool kAll>
+__device__ __forceinline__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* row,
+                                              float4* stage_colors, float* stage_offsets,
+                                              int lane) {
   const CanvasDesc cd = b.canvases[rt.canvas];
   const int y = (int)rt.y;
   const int x0 = (int)rt.x0, x1 = (int)rt.x1;
@@ -257,65 +342,7 @@ __device__ void CompositeTile(const DevBatch& b, const RowTask& rt, uint32_t* ro
         stop_offsets = stage_offsets;
         br.stop0 = 0;
       }
-      const uint2* sp = b.spans;
-      for (uint32_t sb = s0; sb < s1; sb += 32) {
-        int xs = 0, xe = 0;
-        uint32_t alpha = 0;
-        bool pending = false;
-        if (sb + lane < s1) {
-          const uint2 mine = sp[sb + lane];
-          const int sx = (int)(mine.x & 0xFFFF), slen = (int)(mine.x >> 16);
-          xs = max(sx, x0);
-          xe = min(sx + slen, x1);
-          alpha = mine.y & br.global_alpha;
-          pending = xs < xe;
-        }
-        // Spans are applied in batches: the longest run of pending spans
-        // (in emission order) in which each starts at or after the end of
-        // the one before.  Those are disjoint, so inside a batch the order
-        // does not matter: short spans are shaded by their own lane, long
-        // ones by the whole warp (pixel column mod 32 per lane).
-        uint32_t pmask = __ballot_sync(0xffffffffu, pending);
-        while (pmask) {
-          const uint32_t below = pmask & ((1u << lane) - 1u);
-          const int prev = below ? 31 - __clz(below) : lane;
-          const int prev_xe = __shfl_sync(0xffffffffu, xe, prev);
-          const bool clash = pending && below && prev_xe > xs;
-          const uint32_t cmask = __ballot_sync(0xffffffffu, clash);
-          const uint32_t batch = cmask ? pmask & ((1u << (__ffs(cmask) - 1)) - 1u) : pmask;
-          const bool mine_now = (batch >> lane) & 1u;
-          const bool is_short = xe - xs <= kShortSpan;
-          if (mine_now && is_short) {
-            for (int x = xs; x < xe; ++x) {
-              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
-                                      b.conicals);
-              if (alpha != 255) c = AlphaMulQ(c, alpha);
-              if (br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
-              uint32_t& d = row[x - x0];
-              d = BlendPixel(d, c, br.blend);
-            }
-          }
-          uint32_t lmask = __ballot_sync(0xffffffffu, mine_now && !is_short);
-          while (lmask) {
-            const int j = __ffs(lmask) - 1;
-            lmask &= lmask - 1;
-            const int qs = __shfl_sync(0xffffffffu, xs, j);
-            const int qe = __shfl_sync(0xffffffffu, xe, j);
-            const uint32_t qa = __shfl_sync(0xffffffffu, alpha, j);
-            for (int x = qs + ((lane - qs) & 31); x < qe; x += 32) {
-              uint32_t c = BrushColor(br, x, y, stop_colors, stop_offsets, b.pixels, b.roundtrip,
-                                      b.conicals);
-              if (qa != 255) c = AlphaMulQ(c, qa);
-              if (br.cf_type) c = FilterColor(br, c, b.srgb_tables, b.cf_matrices);
-              uint32_t& d = row[x - x0];
-              d = BlendPixel(d, c, br.blend);
-            }
-          }
-          __syncwarp();
-          if (mine_now) pending = false;
-          pmask &= ~batch;
-        }
-      }
+      CompositeSpans<kAll>(b, br, stop_colors, stop_offsets, s0, s1, x0, x1, y, row, lane);
     }
   }
   __syncwarp();
@@ -327,8 +354,9 @@ int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, u
                     cudaStream_t stream) {
   if (n_tasks == 0) return 0;
   size_t smem = (size_t)kCompWarps * CompWarpSmem(chunk);
+  auto kernel = b.any_general ? k_composite<true> : k_composite<false>;
   if (smem > 48 * 1024) {
-    cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   uint32_t grid = (n_tasks + kCompWarps - 1) / kCompWarps;
   if (ctas_per_sm > 0 && counter) {
@@ -336,7 +364,7 @@ int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, u
   } else {
     counter = nullptr;
   }
-  k_composite<<<grid, 32 * kCompWarps, smem, stream>>>(b, tasks, n_tasks, chunk, counter);
+  kernel<<<grid, 32 * kCompWarps, smem, stream>>>(b, tasks, n_tasks, chunk, counter);
   return 1;
 }
 

@@ -63,7 +63,8 @@ struct CanvasDesc {
   int32_t blur_radius; // temp canvases: StackBlur radius (0 = not a temp)
   uint32_t band0;      // first entry of the canvas's row bands in band_off
   uint32_t blur_style; // temp canvases: BlurStyle (1 normal, 2 solid, 3 outer, 4 inner)
-  uint32_t pad;
+  uint32_t general;    // 1: a pass has a sweep / conical brush, a colour filter or a blend
+                       // mode past the Porter-Duff src-over family
   uint64_t out_off;    // temp canvases: the filtered image the draw samples (px_off for
                        // kNormal, which blurs back in place; a third buffer otherwise)
 };
@@ -106,6 +107,7 @@ struct PassGeom {
   int32_t row0, row1;   // canvas rows that can receive spans
   int32_t need[13];     // sizes seen (exact up to the failing stage)
   int32_t max_active;   // bound of the sweep's active-list length
+  int32_t raw_spans;    // the pass keeps raw spans (kPassRawSpans): swept by the generic form
 };
 
 struct PassSweep {      // per-pass sweep buffers, set after geometry
@@ -172,6 +174,9 @@ struct DevBatch {
   uint2* clip_rows;           // per state row: (first span, count) in the span pool
   const uint2* clip_items;    // (pass, canvas row) of the draws under a path clip
   uint32_t n_clip_items;
+  // a canvas is general (CanvasDesc::general): the compositor's general
+  // form runs for the whole batch
+  uint32_t any_general;
 };
 
 // Shared memory of one register-sweep warp: its RegSharedT block, then an

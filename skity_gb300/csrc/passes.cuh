@@ -22,6 +22,7 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
   g.acc_left = g.acc_width = 0;
   g.scan_top = 0;
   g.row0 = g.row1 = 0;
+  g.raw_spans = (pd.flags & kPassRawSpans) != 0 ? 1 : 0;
   for (int k = 0; k < 13; ++k) g.need[k] = 0;
   g.max_active = 0;
 
@@ -196,7 +197,10 @@ SKC_HD bool ClipSpan(int& x, int y, int& len, int W, int H) {
 // keep() applies the clipping of SWSpanBrush::Brush and drops spans whose
 // alpha & global alpha is 0 under src-over (they blend to nothing).  A raw
 // sink (the passes of the path-clip stages) keeps every span of its rows as
-// the raster made it, in the raw format of pack().
+// the raster made it, in the raw format of pack(); only sinks built with
+// kRawCapable take that form (the generic sweep's), so the register sweeps
+// carry no test for it.
+template <bool kRawCapable>
 struct SinkBase {
   int row0, row1, W, H;
   uint32_t ga;
@@ -204,15 +208,15 @@ struct SinkBase {
   bool raw;
   SKC_HD bool keep(int& x, int y, int& len, uint8_t a) const {
     if (y < row0 || y >= row1) return false;
-    if (raw) return true;
+    if (kRawCapable && raw) return true;
     if (!ClipSpan(x, y, len, W, H)) return false;
     return !(srcover && (a & ga) == 0);
   }
   // A stored span: x | len << 16 and the alpha; raw: x (int32) and
   // len | alpha << 24.
   SKC_HD uint2 pack(int x, int len, uint32_t a) const {
-    return raw ? make_uint2((uint32_t)x, ((uint32_t)len & 0xFFFFFFu) | (a << 24))
-               : make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
+    return (kRawCapable && raw) ? make_uint2((uint32_t)x, ((uint32_t)len & 0xFFFFFFu) | (a << 24))
+                                : make_uint2((uint32_t)x | ((uint32_t)len << 16), a);
   }
 };
 
@@ -232,7 +236,12 @@ SKC_HD unsigned long long LaneBcast64(const Lanes& L, unsigned long long v, int 
 // the exact size the pass needs; the caller then sweeps again with a pool
 // that large.  All members are warp-uniform; methods are called by the
 // whole warp.
-struct PoolSink : SinkBase {
+template <bool kRawCapable>
+struct PoolSinkT : SinkBase<kRawCapable> {
+  using SinkBase<kRawCapable>::keep;
+  using SinkBase<kRawCapable>::pack;
+  using SinkBase<kRawCapable>::row0;
+  using SinkBase<kRawCapable>::row1;
   uint2* pool;
   uint64_t cap;                // pool capacity in spans
   unsigned long long* next;    // spans handed out so far
@@ -538,7 +547,11 @@ struct PoolSink : SinkBase {
   }
 };
 
-SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, PoolSink* s) {
+using PoolSink = PoolSinkT<true>;       // the generic sweep's: every pass form
+using PoolSinkReg = PoolSinkT<false>;   // the register sweeps': never raw
+
+template <typename Sink>
+SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* s) {
   const PassDesc pd = b.passes[p];
   const PassSweep sw = b.sweep[p];
   const CanvasDesc cd = b.canvases[pd.canvas];
@@ -562,7 +575,8 @@ SKC_HD void InitPoolSink(const DevBatch& b, uint32_t p, const PassGeom& g, PoolS
   s->frags = 0;
 }
 
-SKC_HD void FinishPass(const DevBatch& b, uint32_t p, PoolSink* s, const Lanes& L) {
+template <typename Sink>
+SKC_HD void FinishPass(const DevBatch& b, uint32_t p, Sink* s, const Lanes& L) {
   s->finish_row(L);
   const unsigned long long frags = LaneSum64(L, s->frags);
   L.sync();
@@ -610,7 +624,9 @@ SKC_HDN void RunSweep(const DevBatch& b, uint32_t p, const PassGeom& g, Sink* si
 }
 
 // Sweep of pass p through the generic sweep.  Row entries a register attempt
-// may have written are cleared first.
+// may have written are cleared first.  kRaw: the pass may be a path clip's
+// (raw spans); batches without path clips take the form without that test.
+template <bool kRaw = true>
 SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   const PassGeom g = b.geom[p];
   const int nrows = g.row1 - g.row0;
@@ -621,7 +637,7 @@ SKC_HDN void SweepPass(const DevBatch& b, uint32_t p, const Lanes& lanes) {
   uint2* rows = b.rowspan + b.sweep[p].rbase;
   for (int r = lanes.lane; r < nrows; r += Lanes::n) rows[r] = make_uint2(0, 0);
   lanes.sync();
-  PoolSink sink;
+  PoolSinkT<kRaw> sink;
   InitPoolSink(b, p, g, &sink);
   RunSweep(b, p, g, &sink, lanes);
   FinishPass(b, p, &sink, lanes);
@@ -675,6 +691,7 @@ enum : int { kSweepReg64 = 0, kSweepReg128 = 2, kSweepGeneric = 1, kSweepReg32 =
 constexpr int kReg32MaxRows = 1100;
 SKC_HD int SweepForm(const PassGeom& g, uint8_t pass_class) {
   if (pass_class != 0) return pass_class;
+  if (g.raw_spans) return kSweepGeneric;  // the path-clip stages' passes (rare)
   const int ma = g.max_active;
   return (ma <= 32 && g.row1 - g.row0 <= kReg32MaxRows) ? kSweepReg32
          : ma <= 64                                     ? kSweepReg64
@@ -693,7 +710,7 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
     EmptyPass(b, p, lanes);
     return;
   }
-  PoolSink sink;
+  PoolSinkReg sink;
   InitPoolSink(b, p, g, &sink);
   if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();

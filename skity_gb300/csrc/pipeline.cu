@@ -405,6 +405,8 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.span_next = ctx->span_next.as<unsigned long long>();
   b.clip_states = db.clip_states.as<ClipStateDesc>();
   b.n_clip_states = (uint32_t)hb.clip_states.size();
+  b.any_general = 0;
+  for (const CanvasDesc& cd : hb.canvases) b.any_general |= cd.general;
   b.clip_flags = db.clip_flags.as<uint32_t>();
   b.clip_rows = db.clip_rows.as<uint2>();
   b.clip_items = db.clip_items.as<uint2>();
