@@ -110,6 +110,25 @@ typedef struct skity_cuda_color_filter {
   float matrix[20];    /* Matrix: row-major 4 x 5 */
 } skity_cuda_color_filter;
 
+/* An image (include/skity/graphic/image.hpp Image::MakeImage over an RGBA
+ * Pixmap, include/skity/io/pixmap.hpp). */
+typedef struct skity_cuda_image {
+  uint32_t width, height;
+  uint32_t alpha_type;  /* AlphaType: 2 kPremul_AlphaType, 3 kUnpremul_AlphaType */
+  uint32_t reserved;
+  const void* pixels;   /* RGBA8 rows, width * 4 bytes each; copied when recorded */
+} skity_cuda_image;
+
+/* Shader::MakeShader(image, sampling, x_tile_mode, y_tile_mode,
+ * local_matrix) (include/skity/effect/shader.hpp:148-153). */
+typedef struct skity_cuda_image_shader {
+  const skity_cuda_image* image;
+  uint32_t filter;          /* FilterMode: 0 kNearest, 1 kLinear; 2: a cubic resampler
+                               (sampled bilinearly, as the software backend does) */
+  uint32_t tile_x, tile_y;  /* TileMode: 0 kClamp, 1 kRepeat, 2 kMirror, 3 kDecal */
+  float local_matrix[6];    /* sx, kx, tx, ky, sy, ty: scale and translate only (kx = ky = 0) */
+} skity_cuda_image_shader;
+
 /* The skity::Paint state the raster path reads (paint.hpp:46-285).
  * Colours are Color4f (unpremultiplied RGBA floats). */
 typedef struct skity_cuda_paint {
@@ -125,6 +144,7 @@ typedef struct skity_cuda_paint {
   uint32_t blur_style;  /* 0: no mask filter; BlurStyle: 1 kNormal, 2 kSolid, 3 kOuter, 4 kInner */
   float blur_radius;    /* MaskFilter::MakeBlur radius */
   const skity_cuda_color_filter* color_filter; /* NULL: none */
+  const skity_cuda_image_shader* image_shader; /* NULL: none; not together with shader */
 } skity_cuda_paint;
 
 typedef struct skity_cuda_context_create_info {
@@ -215,6 +235,16 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, flo
  * returns SKITY_CUDA_ERROR_NOT_SUPPORTED. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
                                                    float right, float bottom);
+/* Canvas::DrawImageRect(image, src, dst, sampling, paint) (canvas.hpp:342;
+ * SWCanvas::OnDrawImageRect, sw_canvas.cc:641-677): a fill of dst with the
+ * image's src rectangle mapped onto it (decal tiling, the paint's alpha and
+ * blend mode).  src / dst are (left, top, right, bottom); a NULL image or an
+ * empty src or dst draws nothing; paint NULL: Paint(). */
+SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canvas,
+                                                         const skity_cuda_image* image,
+                                                         const float src[4], const float dst[4],
+                                                         uint32_t filter,
+                                                         const skity_cuda_paint* paint);
 /* Canvas::ClipPath(path, op) (canvas.hpp; SWCanvas::OnClipPath,
  * sw_canvas.cc:317-336), op 0 kDifference / 1 kIntersect: later draws (and
  * Clear) are clipped by the path's spans the way the software canvas clips

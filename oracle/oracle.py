@@ -53,6 +53,8 @@ def lib() -> ctypes.CDLL:
         _lib.sko_render.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(Stats)]
         _lib.sko_render.restype = ctypes.c_int
+        _lib.sko_sample.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 6 + [ctypes.c_float] * 2
+        _lib.sko_sample.restype = ctypes.c_uint32
         _lib.sko_render_mt.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_uint32,
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
                                        ctypes.POINTER(Stats)]
@@ -68,6 +70,15 @@ def lib() -> ctypes.CDLL:
                                             ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
     return _lib
+
+
+def sample(rgba, alpha_type, filter, tile_x, tile_y, u, v) -> int:
+    """BitmapSampler::GetColor of an (h, w, 4) RGBA8 pixmap at unit
+    coordinates (u, v), premultiplied as the pixmap brush does for
+    unpremultiplied pixels: an ARGB colour."""
+    px = np.ascontiguousarray(rgba, np.uint8)
+    return int(lib().sko_sample(px.ctypes.data, px.shape[1], px.shape[0], alpha_type, filter,
+                                tile_x, tile_y, u, v))
 
 
 def render(scene, first: int = 0, count: int | None = None):

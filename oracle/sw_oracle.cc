@@ -1686,8 +1686,74 @@ static uint32_t ApplyColorFilter(const FilterRec* f, uint32_t c) {
   }
 }
 
+// BitmapSampler (bitmap_sampler.cc:12-108) over an RGBA8 pixmap, and
+// PixmapBrush::CalculateColor's premultiply of unpremultiplied pixels
+// (sw_span_brush.cc:568-579).
+struct Sampler {
+  const uint8_t* px = nullptr;
+  uint32_t w = 0, h = 0;
+  int filter = 0;            // 0 nearest, else bilinear (cubic samples bilinearly)
+  int tile_x = 0, tile_y = 0;  // TileMode: clamp, repeat, mirror, decal
+  bool unpremul = false;
+
+  static float Remap(float t, int mode) {  // RemapFloatTile
+    switch (mode) {
+      case 0: return std::clamp(t, 0.0f, 1.0f);
+      case 1: return t - std::floor(t);  // FloatFract
+      case 2: {
+        float t1 = t - 1;
+        float t2 = t1 - 2 * std::floor(t1 * 0.5) - 1;  // floor of a double
+        return std::abs(t2);
+      }
+      default: return t;
+    }
+  }
+  // glm::clamp<uint32_t>(v, 0, n - 1): the float argument converts to
+  // uint32_t the way x86-64 builds of the reference convert it (through a
+  // 64-bit signed integer: -1 becomes 0xFFFFFFFF, clamped to n - 1).
+  static uint32_t Index(float v, uint32_t n) {
+    uint32_t u = (uint32_t)(int64_t)v;
+    return std::min(u, n - 1);
+  }
+  void Texel(float x, float y, float out[4]) const {  // SampleXY, Color4fFromColor
+    const uint8_t* c = px + ((size_t)Index(y, h) * w + Index(x, w)) * 4;
+    for (int i = 0; i < 4; ++i) out[i] = c[i] / 255.f;  // r, g, b, a
+  }
+  uint32_t Color(float u, float v) const {  // GetColor, then the brush's premultiply
+    if ((tile_x == 3 && (u < 0.0 || u >= 1.0)) || (tile_y == 3 && (v < 0.0 || v >= 1.0)))
+      return 0;
+    u = Remap(u, tile_x);
+    v = Remap(v, tile_y);
+    float c[4];
+    if (filter != 0) {  // SampleUnitLinear
+      float fw = (float)w, fh = (float)h;
+      float x = u * fw, y = v * fh;
+      float i0 = std::floor(x - 0.5f), j0 = std::floor(y - 0.5f);
+      if (tile_x == 1) i0 = i0 - fw * std::floor(i0 / fw);  // glm::mod
+      if (tile_y == 1) j0 = j0 - fh * std::floor(j0 / fh);
+      float i1 = i0 + 1.0f, j1 = j0 + 1.0f;
+      if (tile_x == 1) i1 = i1 - fw * std::floor(i1 / fw);
+      if (tile_y == 1) j1 = j1 - fh * std::floor(j1 / fh);
+      float fx = x - 0.5f, fy = y - 0.5f;
+      float a = fx - std::floor(fx), b = fy - std::floor(fy);  // glm::fract
+      float t00[4], t10[4], t01[4], t11[4];
+      Texel(i0, j0, t00);
+      Texel(i1, j0, t10);
+      Texel(i0, j1, t01);
+      Texel(i1, j1, t11);
+      float k00 = (1 - a) * (1 - b), k10 = a * (1 - b), k01 = (1 - a) * b, k11 = a * b;
+      for (int i = 0; i < 4; ++i) c[i] = k00 * t00[i] + k10 * t10[i] + k01 * t01[i] + k11 * t11[i];
+    } else {  // SampleUnitNearest
+      Texel(u * (float)w, v * (float)h, c);
+    }
+    uint32_t col = Color4fToColor(c);
+    return unpremul ? ColorToPMColor(col) : col;
+  }
+};
+
 struct Brush {
-  int kind = 0;  // 0 solid, 1 linear, 2 radial, 3 sweep, 4 two-point conical
+  int kind = 0;  // 0 solid, 1 linear, 2 radial, 3 sweep, 4 two-point conical, 5 image shader
+  Sampler img{};
   uint32_t solid = 0;
   Gradient g{};
   Mat m{};
@@ -1707,6 +1773,7 @@ struct Brush {
     }
     float mx, my;
     MapPoint(m, x + 0.5f, y + 0.5f, &mx, &my);
+    if (kind == 5) return img.Color(mx, my);
     float t;
     if (kind == 1) {
       t = mx;
@@ -1845,6 +1912,21 @@ struct SceneView {
   const float *clip_pts = nullptr, *clip_wts = nullptr;
   const uint32_t* draw_clip_state = nullptr;  // per draw, 1-based (0: none)
   const struct ClipStates* clip_cache = nullptr;  // the states' span lists (set per render)
+  // images (header flag 8): records, pixel blob, per-draw image shaders
+  struct ImageRec {
+    uint32_t width, height, alpha_type, pad;
+    uint64_t offset;
+  };
+  struct ImageShaderRec {
+    uint32_t image, filter, tile_x, tile_y;
+    float local[6];
+    uint32_t rect, pad;
+    float src[4], dst[4];
+  };
+  uint32_t n_images = 0;
+  const ImageRec* images = nullptr;
+  const uint8_t* image_pixels = nullptr;
+  const ImageShaderRec* image_shaders = nullptr;
 };
 
 // The colour filter of the draw whose paint record is `p` (a record of s).
@@ -1875,7 +1957,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->has_clear = hdr[3];
   // 1: per-draw clip bounds, 2: per-draw colour filters, 4: path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~7u) return false;
+  if (flags & ~15u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -1919,6 +2001,21 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
     s->clip_pts = (const float*)at(8 * tp);
     s->clip_wts = (const float*)at(4 * tw);
     s->draw_clip_state = (const uint32_t*)at(4 * (size_t)s->nd);
+  }
+  if (flags & 8) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_images, buf + o, 4);
+    o += 4;
+    s->images = (const SceneView::ImageRec*)at(sizeof(SceneView::ImageRec) * (size_t)s->n_images);
+    uint64_t nb = 0;
+    if (o + 8 > len) return false;
+    std::memcpy(&nb, buf + o, 8);
+    o += 8;
+    if (nb > len) return false;
+    s->image_pixels = at(nb);
+    o += (4 - nb % 4) % 4;
+    s->image_shaders =
+        (const SceneView::ImageShaderRec*)at(sizeof(SceneView::ImageShaderRec) * (size_t)s->nd);
   }
   return o <= len;
 }
@@ -1967,6 +2064,37 @@ struct Stats {
 // GenerateBrush (sw_canvas.cc:727-795) for the main canvas (identity CTM)
 static Brush MakeBrush(const SceneView& s, const PaintRec& p, bool stroke) {
   Brush br;
+  const size_t d = (size_t)(&p - s.paints);
+  if (s.image_shaders && d < s.nd && s.image_shaders[d].image) {
+    // GenerateBrush's pixmap branch (sw_canvas.cc:755-786): Scale(1/w, 1/h)
+    // * inverse(local); the canvas translation is applied by the caller
+    const SceneView::ImageShaderRec& r = s.image_shaders[d];
+    const SceneView::ImageRec& im = s.images[r.image - 1];
+    Mat inv = Mat::Identity();  // Matrix::InvertNonIdentity, scale + translate
+    if (r.local[0] != 1.f || r.local[4] != 1.f) {
+      float ix = 1.f / r.local[0], iy = 1.f / r.local[4];
+      inv.e[0][0] = ix;
+      inv.e[1][1] = iy;
+      inv.e[3][0] = -r.local[2] * ix;
+      inv.e[3][1] = -r.local[5] * iy;
+    } else {
+      inv.e[3][0] = -r.local[2];
+      inv.e[3][1] = -r.local[5];
+    }
+    br.kind = 5;
+    br.m = MatMul(MatScale(1.f / (float)im.width, 1.f / (float)im.height), inv);
+    br.img.px = s.image_pixels + im.offset;
+    br.img.w = im.width;
+    br.img.h = im.height;
+    br.img.filter = (int)r.filter;
+    br.img.tile_x = (int)r.tile_x;
+    br.img.tile_y = (int)r.tile_y;
+    br.img.unpremul = im.alpha_type == 3;
+    // SWSpanBrush's global alpha from Paint::GetAlphaF (paint.cc:96-98)
+    br.global_alpha = (uint8_t)(255 * (p.style == 1 ? p.stroke_color[3] : p.fill_color[3]));
+    br.filter = FilterOf(s, p);
+    return br;
+  }
   if (p.gradient >= 0) {
     const GradRec& g = s.grads[p.gradient];
     br.kind = (int)g.type;
@@ -2212,6 +2340,21 @@ static void DrawPath(const SceneView& s, uint32_t d, Target* t, Stats* st,
 // C ABI for the tests and the CPU baseline
 // ---------------------------------------------------------------------------
 extern "C" {
+
+// BitmapSampler::GetColor (+ the pixmap brush's premultiply) of one RGBA8
+// pixmap at unit coordinates (u, v): the checker of the sampler's own tests.
+uint32_t sko_sample(const uint8_t* rgba, uint32_t w, uint32_t h, uint32_t alpha_type,
+                    uint32_t filter, uint32_t tile_x, uint32_t tile_y, float u, float v) {
+  sko::Sampler sm;
+  sm.px = rgba;
+  sm.w = w;
+  sm.h = h;
+  sm.filter = (int)filter;
+  sm.tile_x = (int)tile_x;
+  sm.tile_y = (int)tile_y;
+  sm.unpremul = alpha_type == 3;
+  return sm.Color(u, v);
+}
 
 int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
                uint8_t* out_rgba, sko_stats* stats) {

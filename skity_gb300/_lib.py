@@ -47,13 +47,26 @@ class ColorFilter_(ctypes.Structure):
                 ("color", ctypes.c_uint32), ("matrix", ctypes.c_float * 20)]
 
 
+class Image_(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("alpha_type", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("pixels", ctypes.c_void_p)]
+
+
+class ImageShader_(ctypes.Structure):
+    _fields_ = [("image", ctypes.POINTER(Image_)), ("filter", ctypes.c_uint32),
+                ("tile_x", ctypes.c_uint32), ("tile_y", ctypes.c_uint32),
+                ("local_matrix", ctypes.c_float * 6)]
+
+
 class Paint_(ctypes.Structure):
     _fields_ = [("style", ctypes.c_uint32), ("cap", ctypes.c_uint32), ("join", ctypes.c_uint32),
                 ("blend_mode", ctypes.c_uint32), ("fill_color", ctypes.c_float * 4),
                 ("stroke_color", ctypes.c_float * 4), ("stroke_width", ctypes.c_float),
                 ("miter_limit", ctypes.c_float), ("shader", ctypes.POINTER(Gradient_)),
                 ("blur_style", ctypes.c_uint32), ("blur_radius", ctypes.c_float),
-                ("color_filter", ctypes.POINTER(ColorFilter_))]
+                ("color_filter", ctypes.POINTER(ColorFilter_)),
+                ("image_shader", ctypes.POINTER(ImageShader_))]
 
 
 class ContextInfo_(ctypes.Structure):
@@ -114,6 +127,10 @@ SIGNATURES = {
     "skity_cuda_canvas_clip_rect": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
                                                      ctypes.c_float, ctypes.c_float]),
     "skity_cuda_canvas_clip_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.c_uint32]),
+    "skity_cuda_canvas_draw_image_rect": (ctypes.c_int32, [_vp, ctypes.POINTER(Image_),
+                                                           ctypes.POINTER(ctypes.c_float),
+                                                           ctypes.POINTER(ctypes.c_float),
+                                                           ctypes.c_uint32, ctypes.POINTER(Paint_)]),
     "skity_cuda_render_streams": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
                                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),

@@ -112,7 +112,47 @@ class Path:
         return self
 
 
+class Image:
+    """Image::MakeImage over an RGBA8 Pixmap: (height, width, 4) uint8
+    pixels, AlphaType 2 (premultiplied) or 3 (unpremultiplied, the Pixmap
+    default)."""
+    def __init__(self, pixels, alpha_type=S.ALPHA_UNPREMUL):
+        self.pixels = np.ascontiguousarray(pixels, np.uint8)
+        assert self.pixels.ndim == 3 and self.pixels.shape[2] == 4
+        self.alpha_type = alpha_type
+
+    @staticmethod
+    def MakeImage(pixels, alpha_type=S.ALPHA_UNPREMUL):
+        return Image(pixels, alpha_type)
+
+    def Width(self): return self.pixels.shape[1]
+
+    def Height(self): return self.pixels.shape[0]
+
+    def _struct(self, keep):
+        im = _lib.Image_(self.Width(), self.Height(), self.alpha_type, 0, self.pixels.ctypes.data)
+        keep += [self.pixels, im]
+        return im
+
+
+class FilterMode:
+    kNearest, kLinear = 0, 1
+
+
+class ImageShader:
+    """Shader::MakeShader(image, sampling, x_tile_mode, y_tile_mode,
+    local_matrix); local = (sx, kx, tx, ky, sy, ty), scale and translate."""
+    def __init__(self, image, filter, tile_x, tile_y, local):
+        self.image, self.filter, self.tile_x, self.tile_y = image, filter, tile_x, tile_y
+        self.local = tuple(float(v) for v in local)
+
+
 class Shader:
+    @staticmethod
+    def MakeShader(image, filter=FilterMode.kNearest, x_tile_mode=TileMode.kClamp,
+                   y_tile_mode=TileMode.kClamp, local_matrix=(1.0, 0.0, 0.0, 0.0, 1.0, 0.0)):
+        return ImageShader(image, filter, x_tile_mode, y_tile_mode, local_matrix)
+
     def __init__(self, kind, p0, p1, radius, colors, pos, tile):
         self.kind, self.p0, self.p1, self.radius = kind, p0, p1, radius
         self.colors = np.asarray(colors, np.float32).reshape(-1, 4)
@@ -392,6 +432,32 @@ class Canvas:
         cp = _lib.Path_(verbs.ctypes.data if len(verbs) else None, len(verbs),
                         pts.ctypes.data if len(pts) else None, len(pts),
                         wts.ctypes.data if len(wts) else None, len(wts), path.fill_type)
+        keep = []
+        cpaint = self._paint_struct(paint, keep)
+        _lib.check(self.lib.skity_cuda_canvas_draw_path(self.handle, ctypes.byref(cp),
+                                                        ctypes.byref(cpaint)),
+                   "skity_cuda_canvas_draw_path")
+
+    def DrawImageRect(self, image, src, dst, filter=FilterMode.kNearest, paint=None):
+        """Canvas::DrawImageRect(image, src, dst, sampling, paint); src and
+        dst are (left, top, right, bottom)."""
+        keep = []
+        im = image._struct(keep) if image is not None else None
+        s4 = (ctypes.c_float * 4)(*[float(v) for v in src])
+        d4 = (ctypes.c_float * 4)(*[float(v) for v in dst])
+        cpaint = self._paint_struct(paint, keep) if paint is not None else None
+        _lib.check(self.lib.skity_cuda_canvas_draw_image_rect(
+            self.handle, ctypes.byref(im) if im is not None else None, s4, d4, int(filter),
+            ctypes.byref(cpaint) if cpaint is not None else None),
+            "skity_cuda_canvas_draw_image_rect")
+
+    def DrawImage(self, image, left, top, filter=FilterMode.kNearest, paint=None):
+        """Canvas::DrawImage(image, x, y, sampling, paint): the whole image
+        at (x, y)."""
+        w, h = image.Width(), image.Height()
+        self.DrawImageRect(image, (0, 0, w, h), (left, top, left + w, top + h), filter, paint)
+
+    def _paint_struct(self, paint, keep):
         r = paint.rec
         cpaint = _lib.Paint_()
         cpaint.style, cpaint.cap, cpaint.join, cpaint.blend_mode = (int(r["style"]), int(r["cap"]),
@@ -400,8 +466,15 @@ class Canvas:
         cpaint.stroke_color[:] = [float(v) for v in r["stroke_color"]]
         cpaint.stroke_width = float(r["stroke_width"])
         cpaint.miter_limit = float(r["miter"])
-        keep = []
-        if paint.shader is not None:
+        if isinstance(paint.shader, ImageShader):
+            sh = paint.shader
+            ish = _lib.ImageShader_()
+            ish.image = ctypes.pointer(sh.image._struct(keep))
+            ish.filter, ish.tile_x, ish.tile_y = sh.filter, sh.tile_x, sh.tile_y
+            ish.local_matrix[:] = list(sh.local)
+            keep.append(ish)
+            cpaint.image_shader = ctypes.pointer(ish)
+        elif paint.shader is not None:
             s = paint.shader
             colors = np.ascontiguousarray(s.colors, np.float32)
             offs = None if s.pos is None else np.ascontiguousarray(s.pos, np.float32)
@@ -427,9 +500,7 @@ class Canvas:
                 cf.matrix[:] = paint.color_filter.matrix
             keep.append(cf)
             cpaint.color_filter = ctypes.pointer(cf)
-        _lib.check(self.lib.skity_cuda_canvas_draw_path(self.handle, ctypes.byref(cp),
-                                                        ctypes.byref(cpaint)),
-                   "skity_cuda_canvas_draw_path")
+        return cpaint
 
     def Save(self):
         _lib.check(self.lib.skity_cuda_canvas_save(self.handle), "skity_cuda_canvas_save")

@@ -50,6 +50,25 @@ struct ColorFilterRec {
 };
 static_assert(sizeof(ColorFilterRec) == 96, "colour filter layout");
 
+// An image of the stream (header flag 8): size, AlphaType (2 premultiplied,
+// 3 unpremultiplied) and the byte offset of its RGBA8 rows in the pixel blob.
+struct ImageRec {
+  uint32_t width, height, alpha_type, pad;
+  uint64_t offset;
+};
+static_assert(sizeof(ImageRec) == 24, "image layout");
+// A draw's image shader: Shader::MakeShader(image, sampling, tile_x, tile_y,
+// local) (image 1-based, 0: none; filter 0 nearest, 1 linear, 2 cubic; local
+// in MapPoint form, scale and translate only); rect = 1: the draw is
+// DrawImageRect(image, src, dst), its path the dst rectangle.
+struct ImageShaderRec {
+  uint32_t image, filter, tile_x, tile_y;
+  float local[6];
+  uint32_t rect, pad;
+  float src[4], dst[4];
+};
+static_assert(sizeof(ImageShaderRec) == 80, "image shader layout");
+
 struct StreamView {
   uint32_t width, height, has_clear;
   float clear[4];
@@ -68,6 +87,12 @@ struct StreamView {
   const uint8_t* clip_verbs;
   const float *clip_pts, *clip_wts;
   const uint32_t* draw_clip_state;  // per draw, 1-based (0: none)
+  // images and per-draw image shaders when the stream has them
+  uint32_t n_images;
+  const ImageRec* images;
+  const uint8_t* image_pixels;
+  uint64_t image_bytes;
+  const ImageShaderRec* image_shaders;
 };
 
 // A ClipPath call of the stream: its parent state (1-based, 0: none), the
@@ -181,7 +206,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   // 1: per-draw clip bounds follow the stops; 2: then per-draw colour
   // filters; 4: then the path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~7u) return false;
+  if (flags & ~15u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -255,6 +280,45 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
     }
     for (uint32_t d = 0; d < s->nd; ++d)
       if (s->draw_clip_state[d] > s->n_clip_states) return false;
+  }
+  s->n_images = 0;
+  s->images = nullptr;
+  s->image_pixels = nullptr;
+  s->image_bytes = 0;
+  s->image_shaders = nullptr;
+  if (flags & 8) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_images, buf + o, 4);
+    o += 4;
+    if (s->n_images > (1u << 20)) return false;
+    s->images = (const ImageRec*)at(sizeof(ImageRec) * (size_t)s->n_images);
+    if (o + 8 > len) return false;
+    std::memcpy(&s->image_bytes, buf + o, 8);
+    o += 8;
+    if (s->image_bytes > len) return false;
+    s->image_pixels = at(s->image_bytes);
+    o += (4 - s->image_bytes % 4) % 4;
+    s->image_shaders = (const ImageShaderRec*)at(sizeof(ImageShaderRec) * (size_t)s->nd);
+    if (o > len) return false;
+    for (uint32_t i = 0; i < s->n_images; ++i) {
+      const ImageRec& r = s->images[i];
+      if (r.width == 0 || r.height == 0 || r.width > 16384 || r.height > 16384 ||
+          (r.alpha_type != 2 && r.alpha_type != 3) || r.offset % 4 != 0 ||
+          r.offset + (uint64_t)r.width * r.height * 4 > s->image_bytes)
+        return false;
+    }
+    for (uint32_t d = 0; d < s->nd; ++d) {
+      const ImageShaderRec& r = s->image_shaders[d];
+      if (r.image == 0) continue;
+      // scale and translate local matrices only, invertible
+      const float* m = r.local;
+      if (r.image > s->n_images || r.filter > 2 || r.tile_x > 3 || r.tile_y > 3 || r.rect > 1 ||
+          m[1] != 0.f || m[3] != 0.f || !(std::fabs(m[0]) >= 1e-30f) ||
+          !(std::fabs(m[4]) >= 1e-30f) || !(std::fabs(m[0]) <= 1e30f) ||
+          !(std::fabs(m[4]) <= 1e30f) || !(std::fabs(m[2]) <= 1e30f) ||
+          !(std::fabs(m[5]) <= 1e30f) || s->paints[d].gradient >= 0)
+        return false;
+    }
   }
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
@@ -415,6 +479,15 @@ struct HostBatch {
   uint64_t draw_count = 0;
   uint32_t max_temp_w = 0, max_temp_h = 0;
 
+  // the images of the stream being added: their byte offsets in the pixel
+  // buffer, and the uploads that put them there (offset, first byte, bytes)
+  std::vector<uint64_t> image_off;
+  struct ImageUpload {
+    uint64_t off;
+    std::vector<uint8_t> bytes;
+  };
+  std::vector<ImageUpload> image_uploads;
+
   uint64_t AllocPixels(uint64_t bytes) {
     uint64_t o = (pixel_bytes + 255) & ~uint64_t(255);
     pixel_bytes = o + bytes;
@@ -535,7 +608,41 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
               g->type > 4)) {
       g = nullptr;
     }
-    if (g) {
+    const ImageShaderRec* is =
+        s.image_shaders && s.image_shaders[d].image ? &s.image_shaders[d] : nullptr;
+    if (is) {
+      // PixmapBrush (sw_canvas.cc:755-786, sw_span_brush.cc:555-579): unit
+      // coordinates = Scale(1/w, 1/h) * inverse(local) * inverse(CTM)
+      const ImageRec& im = s.images[is->image - 1];
+      Mat4 inv;  // Matrix::InvertNonIdentity, scale-and-translate form (matrix.cc:242-268)
+      inv.identity();
+      const float lsx = is->local[0], lsy = is->local[4], ltx = is->local[2], lty = is->local[5];
+      if (lsx != 1.f || lsy != 1.f) {
+        const float ix = 1.f / lsx, iy = 1.f / lsy;
+        inv.e[0][0] = ix;
+        inv.e[1][1] = iy;
+        inv.e[3][0] = -ltx * ix;
+        inv.e[3][1] = -lty * iy;
+      } else {
+        inv.e[3][0] = -ltx;
+        inv.e[3][1] = -lty;
+      }
+      Mat4 m = MatMul(MatMul(MatScale(1.f / (float)im.width, 1.f / (float)im.height), inv),
+                      InvertTranslate(tx, ty));
+      br.kind = 6;
+      br.m[0] = m.e[0][0];
+      br.m[1] = m.e[1][0];
+      br.m[2] = m.e[3][0];
+      br.m[3] = m.e[0][1];
+      br.m[4] = m.e[1][1];
+      br.m[5] = m.e[3][1];
+      br.img_w = im.width;
+      br.img_h = im.height;
+      br.img_off = hb.image_off[is->image - 1];
+      br.tile = ImageMode(is->tile_x, is->tile_y, is->filter != 0, im.alpha_type == 3);
+      // Paint::GetAlphaF (paint.cc:96-98) as SWSpanBrush's global alpha
+      br.global_alpha = (uint8_t)(255 * (pr.style == 1 ? pr.stroke_color[3] : pr.fill_color[3]));
+    } else if (g) {
       // brush kinds: 1 linear, 2 radial, 4 sweep, 5 conical (3 is the image brush)
       br.kind = g->type <= 2 ? g->type : g->type + 1;
       Mat4 dev_to_local = MatMul(MatTranslate(0, 0), InvertTranslate(tx, ty));
@@ -630,6 +737,14 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   cd.clear_pm = s.has_clear ? SolidPM(s.clear) : 0;
   hb.canvases.push_back(cd);
   hb.main_canvases.push_back(cidx);
+  hb.image_off.assign(s.n_images, 0);
+  for (uint32_t i = 0; i < s.n_images; ++i) {
+    const ImageRec& r = s.images[i];
+    const uint64_t bytes = (uint64_t)r.width * r.height * 4;
+    hb.image_off[i] = hb.AllocPixels(bytes);
+    hb.image_uploads.push_back({hb.image_off[i], std::vector<uint8_t>(s.image_pixels + r.offset,
+                                                                     s.image_pixels + r.offset + bytes)});
+  }
   std::vector<PassDesc> main_passes;
   std::vector<std::pair<uint32_t, std::vector<PassDesc>>> temps;
   // Path clips: one pass rasterising each ClipPath path (RastePath with the

@@ -11,7 +11,8 @@ namespace skc {
 // Per-pass brush, prepared on the host the way SWCanvas::GenerateBrush
 // (sw_canvas.cc:727-795) prepares the reference's SWSpanBrush.
 struct Brush {
-  uint32_t kind;          // 0 solid, 1 linear, 2 radial, 3 image (blur mask), 4 sweep, 5 conical
+  uint32_t kind;          // 0 solid, 1 linear, 2 radial, 3 image (blur mask), 4 sweep, 5 conical,
+                          // 6 image shader (tile: ImageMode)
   uint32_t blend;         // BlendMode
   uint32_t solid;         // premultiplied ARGB (kind 0)
   uint32_t global_alpha;  // SWSpanBrush::global_alpha_ (255 except image)
@@ -420,6 +421,77 @@ SKC_HDN uint32_t OtherGradientColor(uint32_t kind, uint32_t tile, uint32_t stop_
   return GradientColor(g, t, colors, offsets);
 }
 
+// Image shader mode word: tile modes, bilinear filter, unpremultiplied pixels.
+SKC_HD uint32_t ImageMode(uint32_t tile_x, uint32_t tile_y, bool linear, bool unpremul) {
+  return tile_x | (tile_y << 4) | ((linear ? 1u : 0u) << 8) | ((unpremul ? 1u : 0u) << 12);
+}
+
+// RemapFloatTile (bitmap_sampler.cc:12-23): 0 clamp, 1 repeat, 2 mirror
+// (its floor in double), 3 decal (left as is).
+SKC_HD float RemapTile(float t, uint32_t mode) {
+  if (mode == 0) return t < 0.0f ? 0.0f : (1.0f < t ? 1.0f : t);
+  if (mode == 1) return t - floorf(t);
+  if (mode == 2) {
+    const float t1 = t - 1;
+    const float t2 = (float)((double)t1 - 2 * floor((double)t1 * 0.5) - 1);
+    return fabsf(t2);
+  }
+  return t;
+}
+
+// glm::clamp<uint32_t>(v, 0, n - 1) of a float coordinate
+// (BitmapSampler::SampleXY, bitmap_sampler.cc:26-34).  The float converts
+// to uint32_t as x86-64 compilers do it (through a 64-bit signed integer),
+// so a coordinate of -1 wraps to the last column, as the reference's own
+// build computes it.
+SKC_HD uint32_t SampleIndex(float v, uint32_t n) {
+  const uint32_t u = (uint32_t)(long long)v;
+  return u < n - 1 ? u : n - 1;
+}
+
+SKC_HD float4 SampleTexel(const uint8_t* img, uint32_t w, uint32_t h, float x, float y) {
+  const uint8_t* px = img + ((size_t)SampleIndex(y, h) * w + SampleIndex(x, w)) * 4;
+  // Color4fFromColor (color.cc:44-51)
+  return make_float4(px[0] / 255.f, px[1] / 255.f, px[2] / 255.f, px[3] / 255.f);
+}
+
+// PixmapBrush::CalculateColor (sw_span_brush.cc:568-579) through
+// BitmapSampler::GetColor (bitmap_sampler.cc:36-108), at unit coordinates
+// (u, v).
+SKC_HDN uint32_t ImageShaderColor(float u, float v, uint32_t mode, uint32_t w, uint32_t h,
+                                  const uint8_t* img) {
+  const uint32_t tx = mode & 15, ty = (mode >> 4) & 15;
+  if ((tx == 3 && (u < 0.0f || u >= 1.0f)) || (ty == 3 && (v < 0.0f || v >= 1.0f))) return 0;
+  u = RemapTile(u, tx);
+  v = RemapTile(v, ty);
+  const float fw = (float)w, fh = (float)h;
+  float4 c;
+  if (mode & 256) {  // SampleUnitLinear
+    const float x = u * fw, y = v * fh;
+    float i0 = floorf(x - 0.5f), j0 = floorf(y - 0.5f);
+    if (tx == 1) i0 = i0 - fw * floorf(i0 / fw);  // glm::mod
+    if (ty == 1) j0 = j0 - fh * floorf(j0 / fh);
+    float i1 = i0 + 1.0f, j1 = j0 + 1.0f;
+    if (tx == 1) i1 = i1 - fw * floorf(i1 / fw);
+    if (ty == 1) j1 = j1 - fh * floorf(j1 / fh);
+    const float xa = x - 0.5f, yb = y - 0.5f;
+    const float a = xa - floorf(xa), b = yb - floorf(yb);  // glm::fract
+    const float4 t00 = SampleTexel(img, w, h, i0, j0), t10 = SampleTexel(img, w, h, i1, j0);
+    const float4 t01 = SampleTexel(img, w, h, i0, j1), t11 = SampleTexel(img, w, h, i1, j1);
+    const float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
+    c.x = w00 * t00.x + w10 * t10.x + w01 * t01.x + w11 * t11.x;
+    c.y = w00 * t00.y + w10 * t10.y + w01 * t01.y + w11 * t11.y;
+    c.z = w00 * t00.z + w10 * t10.z + w01 * t01.z + w11 * t11.z;
+    c.w = w00 * t00.w + w10 * t10.w + w01 * t01.w + w11 * t11.w;
+  } else {  // SampleUnitNearest
+    c = SampleTexel(img, w, h, u * fw, v * fh);
+  }
+  // Color4fToColor, then ColorToPMColor for unpremultiplied pixels
+  const uint32_t col =
+      ARGB(ChannelToByte(c.w), ChannelToByte(c.x), ChannelToByte(c.y), ChannelToByte(c.z));
+  return (mode & 4096) ? ColorToPMColor(col) : col;
+}
+
 // BrushColor for the solid, linear, radial and image brushes.
 SKC_HD uint32_t BrushColorCommon(const Brush& b, int x, int y, const float4* colors,
                                  const float* offsets, const uint8_t* images,
@@ -447,6 +519,7 @@ SKC_HD uint32_t BrushColor(const Brush& b, int x, int y, const float4* colors, c
   float my = sx * b.m[3] + sy * b.m[4] + b.m[5];
   if (b.kind == 1) return GradientColor(b, mx, colors, offsets);
   if (b.kind == 2) return GradientColor(b, sqrt_(mx * mx + my * my), colors, offsets);
+  if (b.kind == 6) return ImageShaderColor(mx, my, b.tile, b.img_w, b.img_h, images + b.img_off);
   if (b.kind >= 4)
     return OtherGradientColor(b.kind, b.tile, b.stop_count, b.has_offsets, b.stop0, b.bias, b.scale,
                               b.conical, mx, my, x, y, colors, offsets, conicals);

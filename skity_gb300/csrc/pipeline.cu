@@ -91,6 +91,9 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
   SKC_TRY(Upload(db.roundtrip, rtab, s));
   SKC_TRY(db.pixels.ensure(std::max<uint64_t>(hb.pixel_bytes, 16)));
+  for (const HostBatch::ImageUpload& u : hb.image_uploads)  // the draws' images
+    SKC_TRY(cudaMemcpyAsync(db.pixels.as<uint8_t>() + u.off, u.bytes.data(), u.bytes.size(),
+                            cudaMemcpyHostToDevice, s));
   SKC_TRY(db.task_next.ensure(32));
   db.uploaded = true;
   return SKITY_CUDA_SUCCESS;
@@ -575,6 +578,10 @@ struct skity_cuda_canvas_s {
   std::vector<uint8_t> clip_verbs;
   std::vector<float> clip_pts, clip_wts;
   std::vector<uint32_t> draw_clip_state;
+  // images of the recorded draws (copied) and the per-draw image shaders
+  std::vector<skc::ImageRec> images;
+  std::vector<uint8_t> image_blob;
+  std::vector<skc::ImageShaderRec> image_shaders;
   skc::DeviceBatch db;
 };
 
@@ -834,6 +841,9 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
   canvas->filters.clear();
   canvas->any_filter = false;
   canvas->draw_clip_state.clear();
+  canvas->images.clear();
+  canvas->image_blob.clear();
+  canvas->image_shaders.clear();
   canvas->dirty = true;
   return SKITY_CUDA_SUCCESS;
 }
@@ -861,6 +871,20 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   if (need_p != path->point_count || need_w != path->conic_weight_count)
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
+  const skity_cuda_image_shader* is = paint->image_shader;
+  if (is) {
+    const skity_cuda_image* im = is->image;
+    if (!im || !im->pixels || im->width == 0 || im->height == 0 || im->width > 16384 ||
+        im->height > 16384 || (im->alpha_type != 2 && im->alpha_type != 3) || is->filter > 2 ||
+        is->tile_x > 3 || is->tile_y > 3 || paint->shader)
+      return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    const float* m = is->local_matrix;
+    for (int i : {0, 2, 4, 5})
+      if (!(std::fabs(m[i]) <= 1e30f)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!(std::fabs(m[0]) >= 1e-30f) || !(std::fabs(m[4]) >= 1e-30f))
+      return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // not invertible
+    if (m[1] != 0.f || m[3] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;  // rotated / skewed
+  }
   if (paint->color_filter) {
     skc::ColorFilterRec fr;
     std::memset(&fr, 0, sizeof fr);
@@ -941,7 +965,86 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   }
   canvas->filters.push_back(fr);
   canvas->draw_clip_state.push_back(canvas->st.path_clip);
+  skc::ImageShaderRec ir;
+  std::memset(&ir, 0, sizeof ir);
+  if (is) {
+    const skity_cuda_image* im = is->image;
+    const uint64_t bytes = (uint64_t)im->width * im->height * 4;
+    skc::ImageRec rec;
+    std::memset(&rec, 0, sizeof rec);
+    rec.width = im->width;
+    rec.height = im->height;
+    rec.alpha_type = im->alpha_type;
+    rec.offset = canvas->image_blob.size();
+    const uint8_t* px = (const uint8_t*)im->pixels;
+    canvas->image_blob.insert(canvas->image_blob.end(), px, px + bytes);
+    canvas->images.push_back(rec);
+    ir.image = (uint32_t)canvas->images.size();
+    ir.filter = is->filter;
+    ir.tile_x = is->tile_x;
+    ir.tile_y = is->tile_y;
+    std::memcpy(ir.local, is->local_matrix, sizeof ir.local);
+  }
+  canvas->image_shaders.push_back(ir);
   canvas->dirty = true;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canvas,
+                                                         const skity_cuda_image* image,
+                                                         const float src[4], const float dst[4],
+                                                         uint32_t filter,
+                                                         const skity_cuda_paint* paint) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!image) return SKITY_CUDA_SUCCESS;
+  if (!src || !dst || filter > 2) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  // Rect::Width / Height; an empty src or dst draws nothing
+  const float sw = src[2] - src[0], sh = src[3] - src[1];
+  const float dw = dst[2] - dst[0], dh = dst[3] - dst[1];
+  if (sw == 0 || sh == 0 || dw == 0 || dh == 0) return SKITY_CUDA_SUCCESS;
+  // Translate(dst.L, dst.T) * Scale(dw / sw, dh / sh) * Translate(-src.L, -src.T)
+  const skc::Mat4 local = skc::MatMul(
+      skc::MatMul(skc::MatTranslate(dst[0], dst[1]), skc::MatScale(dw / sw, dh / sh)),
+      skc::MatTranslate(-src[0], -src[1]));
+  skity_cuda_image_shader is;
+  std::memset(&is, 0, sizeof is);
+  is.image = image;
+  is.filter = filter;
+  is.tile_x = is.tile_y = 3;  // TileMode::kDecal
+  is.local_matrix[0] = local.e[0][0];
+  is.local_matrix[1] = local.e[1][0];
+  is.local_matrix[2] = local.e[3][0];
+  is.local_matrix[3] = local.e[0][1];
+  is.local_matrix[4] = local.e[1][1];
+  is.local_matrix[5] = local.e[3][1];
+  skity_cuda_paint p;
+  if (paint) {
+    p = *paint;
+  } else {  // Paint()
+    std::memset(&p, 0, sizeof p);
+    p.blend_mode = 3;
+    p.fill_color[3] = p.stroke_color[3] = 1.f;
+    p.stroke_width = 1.f;
+    p.miter_limit = 4.f;
+  }
+  p.style = 0;  // work_paint.SetStyle(kFill_Style)
+  p.shader = nullptr;
+  p.image_shader = &is;
+  const uint8_t verbs[5] = {SKITY_CUDA_VERB_MOVE, SKITY_CUDA_VERB_LINE, SKITY_CUDA_VERB_LINE,
+                            SKITY_CUDA_VERB_LINE, SKITY_CUDA_VERB_CLOSE};
+  const float pts[8] = {dst[0], dst[1], dst[2], dst[1], dst[2], dst[3], dst[0], dst[3]};
+  skity_cuda_path path;
+  std::memset(&path, 0, sizeof path);
+  path.verbs = verbs;
+  path.verb_count = 5;
+  path.points = pts;
+  path.point_count = 4;
+  const int32_t rc = skity_cuda_canvas_draw_path(canvas, &path, &p);
+  if (rc) return rc;
+  skc::ImageShaderRec& ir = canvas->image_shaders.back();
+  ir.rect = 1;
+  std::memcpy(ir.src, src, 16);
+  std::memcpy(ir.dst, dst, 16);
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -1102,6 +1205,13 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
     sv.clip_wts = canvas->clip_wts.data();
     sv.draw_clip_state = canvas->draw_clip_state.data();
   }
+  if (!canvas->images.empty()) {
+    sv.n_images = (uint32_t)canvas->images.size();
+    sv.images = canvas->images.data();
+    sv.image_pixels = canvas->image_blob.data();
+    sv.image_bytes = canvas->image_blob.size();
+    sv.image_shaders = canvas->image_shaders.data();
+  }
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
   int32_t rc = skc::AddStreamCanvas(db.hb, sv);
@@ -1141,6 +1251,9 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->filters.clear();
   canvas->any_filter = false;
   canvas->draw_clip_state.clear();
+  canvas->images.clear();
+  canvas->image_blob.clear();
+  canvas->image_shaders.clear();
   canvas->dirty = false;
   return SKITY_CUDA_SUCCESS;
 }

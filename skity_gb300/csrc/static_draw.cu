@@ -329,7 +329,7 @@ extern "C" SKITY_CUDA_API int32_t skity_cuda_draw_path_static(
                   paint->miter_limit, 0.f))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   // solid colours only: no shader, no mask filter (MakeBlur(r <= 0) is null)
-  if (paint->blend_mode > 28 || paint->shader || paint->color_filter ||
+  if (paint->blend_mode > 28 || paint->shader || paint->color_filter || paint->image_shader ||
       (paint->blur_style != 0 && paint->blur_radius > 0.f))
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
 

@@ -63,6 +63,7 @@ VERSION = 1
 FLAG_CLIPS = 1    # header flags: the per-draw clip section is present
 FLAG_FILTERS = 2  # the per-draw colour-filter section is present
 FLAG_PATH_CLIPS = 4  # the clip-state table and per-draw clip states are present
+FLAG_IMAGES = 8  # the image table, its pixels and the per-draw image shaders are present
 CLIP_DIFFERENCE, CLIP_INTERSECT = 0, 1  # Canvas::ClipOp
 # clip state record: parent state (1-based, 0: none), ClipOp, the path's
 # fill type, its verb / point / weight counts, the canvas translation and
@@ -91,6 +92,24 @@ FILTER_NONE, FILTER_BLEND, FILTER_MATRIX, FILTER_LINEAR_TO_SRGB, FILTER_SRGB_TO_
 FILTER_DTYPE = np.dtype([("type", "<u4"), ("mode", "<u4"), ("color", "<u4"), ("pad", "<u4"),
                          ("matrix", "<f4", 20)])
 assert FILTER_DTYPE.itemsize == 96
+
+# image record: size, AlphaType (2 premultiplied, 3 unpremultiplied) and the
+# byte offset of its RGBA8 rows (width * 4 bytes each) in the pixel blob
+ALPHA_PREMUL, ALPHA_UNPREMUL = 2, 3
+IMAGE_DTYPE = np.dtype([("width", "<u4"), ("height", "<u4"), ("alpha_type", "<u4"),
+                        ("pad", "<u4"), ("offset", "<u8")])
+assert IMAGE_DTYPE.itemsize == 24
+# per-draw image shader (Shader::MakeShader(image, sampling, tile_x, tile_y,
+# local)): the image (1-based, 0: none), FilterMode (0 nearest, 1 linear, 2
+# cubic, which the software backend samples bilinearly), the tile modes, the
+# local matrix in MapPoint form (sx, kx, tx, ky, sy, ty; scale and translate
+# only); rect = 1: the draw is DrawImageRect(image, src, dst) (its path is
+# the dst rectangle)
+FILTER_NEAREST, FILTER_LINEAR, FILTER_CUBIC = 0, 1, 2
+IMAGE_SHADER_DTYPE = np.dtype([("image", "<u4"), ("filter", "<u4"), ("tile_x", "<u4"),
+                               ("tile_y", "<u4"), ("local", "<f4", 6), ("rect", "<u4"),
+                               ("pad", "<u4"), ("src", "<f4", 4), ("dst", "<f4", 4)])
+assert IMAGE_SHADER_DTYPE.itemsize == 80
 
 GRADIENT_DTYPE = np.dtype([
     ("type", "<u4"), ("tile_mode", "<u4"), ("stop_count", "<u4"),
@@ -132,6 +151,8 @@ class Scene:
     # path clips: (states CLIP_STATE_DTYPE, verbs u8, points (n, 2) f32, weights f32,
     # per-draw state u32), or None
     path_clips: tuple | None = None
+    # images: (IMAGE_DTYPE records, pixel blob u8, per-draw IMAGE_SHADER_DTYPE), or None
+    images: tuple | None = None
 
     @property
     def n_draws(self) -> int:
@@ -141,7 +162,8 @@ class Scene:
         nd = self.n_draws
         flags = (FLAG_CLIPS if self.clips is not None else 0) | \
             (FLAG_FILTERS if self.filters is not None else 0) | \
-            (FLAG_PATH_CLIPS if self.path_clips is not None else 0)
+            (FLAG_PATH_CLIPS if self.path_clips is not None else 0) | \
+            (FLAG_IMAGES if self.images is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -179,6 +201,17 @@ class Scene:
             pd = np.ascontiguousarray(per_draw, np.uint32)
             assert len(pd) == nd
             out.append(pd.tobytes())
+        if self.images is not None:
+            recs, blob, shaders = self.images
+            recs = np.ascontiguousarray(recs, IMAGE_DTYPE)
+            blob = np.ascontiguousarray(blob, np.uint8).tobytes()
+            out.append(struct.pack("<I", len(recs)))
+            out.append(recs.tobytes())
+            out.append(struct.pack("<Q", len(blob)))
+            out.append(blob + b"\0" * ((-len(blob)) % 4))
+            sh = np.ascontiguousarray(shaders, IMAGE_SHADER_DTYPE)
+            assert len(sh) == nd
+            out.append(sh.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -218,8 +251,15 @@ class Scene:
             cwts = take(np.float32, tw)
             per_draw = take(np.uint32, nd)
             path_clips = (states, cverbs, cpts, cwts, per_draw)
+        images = None
+        if flags & FLAG_IMAGES:
+            (n_images,) = struct.unpack_from("<I", buf, o); o += 4
+            recs = take(IMAGE_DTYPE, n_images)
+            (nb,) = struct.unpack_from("<Q", buf, o); o += 8
+            blob = take(np.uint8, nb); o += (-nb) % 4
+            images = (recs, blob, take(IMAGE_SHADER_DTYPE, nd))
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so, clips, filters, path_clips)
+                     paints, grads, sc, so, clips, filters, path_clips, images)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -251,7 +291,9 @@ class Scene:
                      None if self.clips is None else self.clips[first:last].copy(),
                      None if self.filters is None else self.filters[first:last].copy(),
                      None if self.path_clips is None else
-                     self.path_clips[:4] + (self.path_clips[4][first:last].copy(),))
+                     self.path_clips[:4] + (self.path_clips[4][first:last].copy(),),
+                     None if self.images is None else
+                     self.images[:2] + (self.images[2][first:last].copy(),))
 
 
 def map_clip(clip, rect, tx=0.0, ty=0.0):
@@ -287,6 +329,7 @@ class SceneBuilder:
         # the save stack of it (Canvas::Save / Restore)
         self._cstates, self._cverbs, self._cpts, self._cwts = [], [], [], []
         self._cstate, self._csaved, self._draw_cstate = 0, [], []
+        self._images, self._blobs, self._nblob, self._shaders = [], [], 0, []
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
                      tile_mode=TILE_CLAMP) -> int:
@@ -303,10 +346,48 @@ class SceneBuilder:
                                    else np.zeros(len(colors)), np.float32))
         return len(self._grads) - 1
 
-    def draw_path(self, verbs, points, paint, weights=(), clip=None, color_filter=None):
+    def add_image(self, pixels, alpha_type=ALPHA_PREMUL) -> int:
+        """An image of (height, width, 4) RGBA8 pixels; returns its 1-based
+        index for image_shader()."""
+        px = np.ascontiguousarray(pixels, np.uint8)
+        assert px.ndim == 3 and px.shape[2] == 4
+        r = np.zeros((), IMAGE_DTYPE)
+        r["width"], r["height"], r["alpha_type"], r["offset"] = \
+            px.shape[1], px.shape[0], alpha_type, self._nblob
+        self._images.append(r)
+        self._blobs.append(px.reshape(-1))
+        self._nblob += px.size
+        return len(self._images)
+
+    def draw_image_rect(self, image, src, dst, paint, filter=FILTER_NEAREST, clip=None,
+                        color_filter=None):
+        """Canvas::DrawImageRect(image, src, dst, sampling, &paint)
+        (sw_canvas.cc:641-677): a fill of the dst rectangle with a decal image
+        shader whose local matrix maps src onto dst.  An empty src or dst
+        draws nothing."""
+        f32 = np.float32
+        sl, st, sr, sb = (f32(v) for v in src)
+        dl, dt, dr, db = (f32(v) for v in dst)
+        sw, sh, dw, dh = sr - sl, sb - st, dr - dl, db - dt
+        if sw == 0 or sh == 0 or dw == 0 or dh == 0:
+            return
+        sx, sy = dw / sw, dh / sh
+        # Translate(dst.L, dst.T) * Scale(sx, sy) * Translate(-src.L, -src.T)
+        local = (sx, 0.0, sx * -sl + dl, 0.0, sy, sy * -st + dt)
+        rec = image_shader(image, filter, TILE_DECAL, TILE_DECAL, local)
+        rec["rect"], rec["src"], rec["dst"] = 1, (sl, st, sr, sb), (dl, dt, dr, db)
+        p = paint.copy()
+        p["style"], p["gradient"] = FILL, -1
+        self.draw_path([MOVE, LINE, LINE, LINE, CLOSE],
+                       [(dl, dt), (dr, dt), (dr, db), (dl, db)], p, clip=clip,
+                       color_filter=color_filter, image_shader=rec)
+
+    def draw_path(self, verbs, points, paint, weights=(), clip=None, color_filter=None,
+                  image_shader=None):
         """`clip`: device-space clip bounds (l, t, r, b) in effect for the
         draw (see map_clip); None: the canvas's initial bounds.
-        `color_filter`: a FILTER_DTYPE record, or None."""
+        `color_filter`: a FILTER_DTYPE record, or None.
+        `image_shader`: an IMAGE_SHADER_DTYPE record (image_shader()), or None."""
         verbs = np.asarray(verbs, np.uint8)
         points = np.asarray(points, np.float32).reshape(-1, 2)
         self._verbs.append(verbs); self._pts.append(points)
@@ -317,6 +398,8 @@ class SceneBuilder:
         self._clips.append(NO_CLIP if clip is None else tuple(clip))
         self._filters.append(np.zeros((), FILTER_DTYPE) if color_filter is None else color_filter)
         self._draw_cstate.append(self._cstate)
+        self._shaders.append(np.zeros((), IMAGE_SHADER_DTYPE) if image_shader is None
+                             else image_shader)
 
     def save(self):
         """Canvas::Save for the path-clip state."""
@@ -361,7 +444,20 @@ class SceneBuilder:
                      ((np.array(self._cstates, CLIP_STATE_DTYPE), cat(self._cverbs, np.uint8, 0),
                        cat(self._cpts, np.float32, (0, 2)), cat(self._cwts, np.float32, 0),
                        np.asarray(self._draw_cstate, np.uint32))
-                      if self._cstates else None))
+                      if self._cstates else None),
+                     ((np.array(self._images, IMAGE_DTYPE), cat(self._blobs, np.uint8, 0),
+                       np.array(self._shaders, IMAGE_SHADER_DTYPE))
+                      if self._images else None))
+
+
+def image_shader(image, filter=FILTER_NEAREST, tile_x=TILE_CLAMP, tile_y=TILE_CLAMP,
+                 local=(1.0, 0.0, 0.0, 0.0, 1.0, 0.0)):
+    """An IMAGE_SHADER_DTYPE record: Shader::MakeShader(image, sampling,
+    tile_x, tile_y, local) with local = (sx, kx, tx, ky, sy, ty)."""
+    r = np.zeros((), IMAGE_SHADER_DTYPE)
+    r["image"], r["filter"], r["tile_x"], r["tile_y"] = image, filter, tile_x, tile_y
+    r["local"] = local
+    return r
 
 
 def filter_record(kind, mode=0, color=0, matrix=None):

@@ -33,6 +33,8 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     hb.stop_offsets.push_back(0);
   }
   std::vector<uint8_t> pixels(hb.pixel_bytes + 16, 0);
+  for (const HostBatch::ImageUpload& u : hb.image_uploads)  // the draws' images
+    std::memcpy(pixels.data() + u.off, u.bytes.data(), u.bytes.size());
   std::vector<uint8_t> rtab(256);
   for (int v = 0; v < 256; ++v) rtab[v] = ChannelToByte(v / 255.f);
 
