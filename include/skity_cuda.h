@@ -177,6 +177,9 @@ typedef struct skity_cuda_stats {
   uint64_t fragments_by_brush[4]; /* fragments shaded by solid, linear, radial
                                      (sweep and two-point conical included)
                                      and image (blur composite) brushes */
+  double plan_ms;         /* device planning after the geometry: sweep buffers,
+                             row tables, pass bins, sweep and tile orders */
+  uint64_t host_syncs;    /* host waits on the device inside the render */
 } skity_cuda_stats;
 
 /* Launch shape of the compositor and the granularity of its pass bins; no
@@ -353,14 +356,18 @@ SKITY_CUDA_API void skity_cuda_server_destroy(skity_cuda_server server);
  * host that cannot afford the device-wide synchronisation that freeing
  * device memory implies.
  *
- * Limits: inputs whose path copy, geometry, sweep memory, row table and spans
- * together need more than the static scratch are rejected with
- * SKITY_CUDA_ERROR_SCRATCH_LIMIT before the canvas is touched.
+ * Limits: inputs whose path copy, geometry, sweep memory, row tables and
+ * spans together need more than the static scratch are rejected with
+ * SKITY_CUDA_ERROR_SCRATCH_LIMIT before the canvas is touched.  Both passes
+ * of a stroke-and-fill or stroke-then-fill paint are sized and swept before
+ * either is blended, so a draw is applied whole or not at all; a device
+ * self-check failure (SKITY_CUDA_ERROR_DEVICE) likewise leaves the canvas
+ * as it was.  A blend mode past kLuminosity is an invalid argument.
  *
  * The scratch is one per device, not one per call: calls that overlap on the
  * same device race on it, so callers on several host threads must serialise
- * them.  The call runs on `stream` (NULL: the default stream) and returns
- * once the draw is complete.  The first call on a device does a one-time
+ * them.  The call runs on `stream` (NULL: the default stream), waits on it
+ * between its stages and returns once the draw is complete.  The first call on a device does a one-time
  * set-up (it looks up the scratch's device address with that device
  * current); make that first call -- an empty path is enough -- before any
  * stream capture begins. */

@@ -83,7 +83,8 @@ class Stats_(ctypes.Structure):
                 ("sweep_count_ms", ctypes.c_double), ("sweep_emit_ms", ctypes.c_double),
                 ("composite_ms", ctypes.c_double), ("blur_ms", ctypes.c_double),
                 ("fragments", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
-                ("fragments_by_brush", ctypes.c_uint64 * 4)]
+                ("fragments_by_brush", ctypes.c_uint64 * 4), ("plan_ms", ctypes.c_double),
+                ("host_syncs", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -1,5 +1,6 @@
 """skity_cuda_draw_path_static -- the entry point that draws without
-allocating -- against skity_cuda_render_streams on the same draws.
+allocating -- against skity_cuda_render_streams on the same draws, and
+against the oracle.
 
 Each static call draws one path onto a canvas held in a device tensor; after
 every call the canvas must match render_streams of the draws so far (bar:
@@ -20,10 +21,16 @@ TOL_LSB, MIN_EXACT = 1, 0.999
 SCRATCH_LIMIT = -9
 
 
+# BlendMode values (include/skity/graphic/blend_mode.hpp): the Porter-Duff
+# general path (kDstIn, kXor), a separable mode (kMultiply) and SoftLight
+RARE_BLENDS = (6, 11, 24, 21)
+
+
 def _scene():
     """Solid-colour paths over and around a 384x320 canvas: 30% even-odd, 40%
-    stroked; some strokes turned into stroke-and-fill / stroke-then-fill and
-    a few draws using kSrc, so every pass kind and blend path is exercised."""
+    stroked; some strokes turned into stroke-and-fill / stroke-then-fill, a
+    few draws using kSrc and a few the rarer blend modes, so every pass kind
+    and blend path is exercised."""
     sc = S.random_paths_scene(S.SEED_BASE + 77, 384, 320, 24, 3, 20,
                               coord_lo=(-32.0, -32.0), coord_hi=(416.0, 352.0),
                               evenodd_frac=0.3, stroke_frac=0.4)
@@ -35,6 +42,8 @@ def _scene():
             p["style"] = S.STROKE_THEN_FILL
         if d % 7 == 5:
             p["blend"] = S.BLEND_SRC
+        elif d % 5 == 3:
+            p["blend"] = RARE_BLENDS[(d // 5) % len(RARE_BLENDS)]
     return sc
 
 
@@ -95,8 +104,49 @@ def test_static_draw_matches_render_streams(gpu_ctx):
     for d in range(2, sc.n_draws):
         assert _static_draw(lib, canvas, sc, d, stream) == 0
     torch.cuda.synchronize()
+    got = canvas.cpu().numpy()
     want = gpu_ctx.render_streams([sc])[0]
-    assert _check(canvas.cpu().numpy(), want) == 1.0
+    assert _check(got, want) == 1.0
+    # and against the oracle (the CPU restatement of the reference path)
+    from oracle import oracle
+    ref, _ = oracle.render(sc)
+    _check(got, ref)
+
+
+def test_static_draw_stroke_and_fill_is_all_or_nothing(gpu_ctx):
+    """A stroke-and-fill draw whose fill fits the scratch but whose stroke
+    does not: the call fails with the scratch limit and the canvas keeps
+    every pixel it had (the fill pass is not blended on its own)."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    canvas = _white_canvas(torch, 64, 64)
+    stream = torch.cuda.current_stream().cuda_stream
+    # a zig-zag of 20k lines: its fill's edges fit, the stroke's outline
+    # (several times the path) does not
+    n = 20_000
+    verbs = np.full(n, S.LINE, np.uint8)
+    verbs[0] = S.MOVE
+    pts = np.zeros((n, 2), np.float32)
+    pts[:, 0] = (np.arange(n) % 2) * 60 + 2
+    pts[:, 1] = np.linspace(2, 62, n, dtype=np.float32)
+    path = _lib.Path_(verbs.ctypes.data, n, pts.ctypes.data, n, None, 0, 0)
+    r = S.default_paint()
+    r["fill_color"] = (0.2, 0.4, 0.6, 1.0)
+    r["stroke_color"] = (0.9, 0.1, 0.1, 1.0)
+    r["stroke_width"] = 3.0
+    fill_only = _paint(r)
+    assert lib.skity_cuda_draw_path_static(0, canvas.data_ptr(), 64, 64, 256, ctypes.byref(path),
+                                           ctypes.byref(fill_only), stream) == 0
+    torch.cuda.synchronize()
+    assert not bool((canvas == 255).all())  # the fill alone fits and draws
+    canvas.fill_(255)
+    r["style"] = S.STROKE_AND_FILL
+    both = _paint(r)
+    rc = lib.skity_cuda_draw_path_static(0, canvas.data_ptr(), 64, 64, 256, ctypes.byref(path),
+                                         ctypes.byref(both), stream)
+    torch.cuda.synchronize()
+    assert rc == SCRATCH_LIMIT
+    assert bool((canvas == 255).all())
 
 
 def test_static_draw_rejects_oversized_inputs(gpu_ctx):
@@ -133,4 +183,7 @@ def test_static_draw_rejects_oversized_inputs(gpu_ctx):
     assert lib.skity_cuda_draw_path_static(0, None, 64, 64, 256, ctypes.byref(small),
                                            ctypes.byref(paint), stream) == -2
     assert lib.skity_cuda_draw_path_static(0, canvas.data_ptr(), 64, 64, 100, ctypes.byref(small),
+                                           ctypes.byref(paint), stream) == -2
+    paint.blend_mode = 29  # past kLuminosity
+    assert lib.skity_cuda_draw_path_static(0, canvas.data_ptr(), 64, 64, 256, ctypes.byref(small),
                                            ctypes.byref(paint), stream) == -2
