@@ -1,15 +1,26 @@
-"""Benchmark of the GB300 raster backend on the single-large-scene workload:
-a 2048x2048 premultiplied RGBA8 canvas cleared to white, 20,000 seeded
-synthetic paths of 3-64 verbs (50% lines / 25% quads / 25% cubics,
-coordinates uniform in [-64, 2112]^2), 30% even-odd, 50% solid / 25% linear
-/ 25% radial gradients, 20% stroked (width 1-8, all caps and joins), one
-DrawPath per path, one Flush (skity_gb300.scene.config2).
+"""Benchmark of the GB300 raster backend on the batching workload: 256
+independent canvases with log-uniform sides in [64, 1024] px (non-square),
+each cleared to white with a log-uniform 50-2,000 seeded paths of 3-32
+verbs (50% lines / 25% quads / 25% cubics, control points uniform over the
+canvas, nonzero fill, solid colours with alpha in [0.3, 1]), one DrawPath per
+path and one Flush per canvas (skity_gb300.scene.config3).
 
-One step = rendering the whole scene (every DrawPath + Flush).
-  value: paths/s with the scene resident in device memory (CUDA events
+One step = rendering all 256 canvases.
+  value: paths/s of the batched form with the batch resident in device
+         memory (its planned launches replayed from CUDA graphs; CUDA events
          around each render on the library's stream), summed over ranks;
   e2e:   the same through skity_cuda_render_streams with host buffers: the
-         scene stream uploaded and the pixels read back inside every step.
+         scene streams uploaded, planned and rendered, and every canvas read
+         back inside every step;
+  per_draw: the plain per-draw form of the same canvases (every DrawPath
+         rasterised and blended on its own, skity_cuda_batch_render_per_draw);
+  parity: the pixels of the last timed render against the oracle (the CPU
+         restatement of the reference's software backend), every canvas;
+  cpu_baseline: that oracle run, timed on all host cores (a pool of one
+         thread per core, canvases dealt largest first).
+The other workloads (the 512x512 and 2048x2048 scenes, the glyph-dense
+4096x4096 scene with blur) and the serving runs are reported beside it, each
+checked against the oracle's committed pixel digests.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
@@ -19,6 +30,7 @@ collective on the data path); the timing is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -29,10 +41,11 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-METRIC = ("Mpix/s & paths/s, batched vs per-draw GPU vs CPU, ≤1 LSB; p50/p99 ms")
-WORKLOAD = ("config2: 2048x2048 RGBA8 canvas, 20,000 seeded paths (3-64 verbs line/quad/cubic, "
-            "coords U[-64,2112]^2, 30% even-odd, 25% linear + 25% radial gradients 2-8 stops, "
-            "20% stroked w U[1,8] all caps x joins), one DrawPath per path, one Flush")
+METRIC = "Mpix/s & paths/s, batched vs per-draw GPU vs CPU, ≤1 LSB; p50/p99 ms"
+WORKLOAD = ("256 canvases, sides log-uniform [64,1024] px, 50-2,000 seeded paths each (3-32 verbs "
+            "line/quad/cubic, nonzero, solid colours, alpha U[0.3,1]), one DrawPath per path, "
+            "one Flush per canvas")
+TOL_LSB, MIN_EXACT = 1, 0.999
 
 
 def dist_env():
@@ -40,6 +53,15 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", str(rank)))
     return rank, world, local
+
+
+def bench_config(scenes, world: int) -> dict:
+    """The `config` of both arms' lines (identical by construction)."""
+    return {"workload": WORKLOAD, "canvases": len(scenes),
+            "paths": sum(sc.n_draws for sc in scenes),
+            "mpix": round(sum(sc.width * sc.height for sc in scenes) / 1e6, 3),
+            "l2": "flushed between GPU steps (256 MiB device write)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
 
 
 def measured_peaks():
@@ -105,6 +127,8 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+
+
 # Integer ops per fragment, counted from the reference's formulas: coverage
 # AlphaMulQ 9 + PMSrcOver 14 (color_priv.hpp:62-72) for every fragment; a
 # linear gradient adds the mapping 4, stop search and lerp ~26, Color4fToColor
@@ -114,39 +138,62 @@ class ClockSampler:
 OPS_PER_FRAGMENT = (23, 93, 101, 35)  # solid, linear, radial, image
 
 
-def issue_roofline(st, frame_ms, composite_ms, clk):
-    """Fragment work against the int32 issue peak (152 SMs x 128 lanes x the
-    SM clock sampled during the timed region): over the whole frame and over
-    the compositing stage, where the fragments are shaded and blended."""
+def issue_roofline(st, frame_ms, composite_ms, clk, sms):
+    """Fragment work against the int32 issue peak (SMs x 128 lanes x the SM
+    clock sampled during the timed region): over the whole frame and over the
+    compositing stage, where the fragments are shaded and blended."""
     frags = st.get("fragments_by_brush") or [st["fragments"], 0, 0, 0]
     ops = sum(o * f for o, f in zip(OPS_PER_FRAGMENT, frags))
     mhz = clk.get("sm_mhz") or 2070.0
-    peak = 152 * 128 * mhz * 1e6
-    return {"ops_per_frame": ops, "peak_ops_per_s": peak, "sm_mhz": mhz,
+    peak = sms * 128 * mhz * 1e6
+    return {"ops_per_frame": ops, "peak_ops_per_s": peak, "sm_mhz": mhz, "sms": sms,
             "frac_frame": ops / (frame_ms / 1e3) / peak if frame_ms else None,
             "frac_composite": ops / (composite_ms / 1e3) / peak if composite_ms else None,
             "fragments_by_brush": dict(zip(("solid", "linear", "radial", "image"), frags))}
 
 
-def load_scene():
-    from skity_gb300 import scene as S
-    cache = os.path.join("/tmp", "skity_config2_v1.bin")
-    try:
-        with open(cache, "rb") as f:
-            return S.Scene.from_bytes(f.read())
-    except Exception:
-        sc = S.config2()
-        try:
-            with open(cache, "wb") as f:
-                f.write(sc.to_bytes())
-        except Exception:
-            pass
-        return sc
+# The sweep stage's counters per emitted span, from an ncu capture of the
+# 256-canvas workload's first 64 canvases (profiles/k_sweep_reg_config3_64canvases.md):
+# warp instructions executed and DRAM bytes (read + write) of the sweep
+# kernels per span they emit.  Multiplied by the spans of the timed render
+# (the units one launch processes) they give the per-render figures.
+SWEEP_PER_SPAN = {"warp_inst": None, "dram_bytes": None}
 
 
-def load_config3():
+def sweep_roofline(st, sweep_ms, clk, sms, hbm_peak, hbm_kind):
+    """Roofline of the dominant kernel, the AAA sweep.  It is neither
+    HBM- nor tensor-bound: one warp per path walks the path's rows in order,
+    so its bound is instruction issue (SMs x 4 schedulers x 1 warp
+    instruction per cycle at the sampled SM clock).  achieved = the sweep's
+    warp instructions per render (ncu count per span x the render's spans)
+    / the sweep stage's CUDA-event time; traffic = its DRAM bytes per render
+    (ncu, scaled the same way).  Beside it, the HBM view: the sweep's
+    algorithmic bytes (84-byte edges read and written, 8-byte spans
+    written) over the same time against the measured copy bandwidth."""
+    mhz = clk.get("sm_mhz") or 2070.0
+    spans, edges = st["spans"], st["edges"]
+    alg = spans * 8 + edges * 84 * 2
+    hbm = {"algorithmic_bytes": alg, "achieved_gbs": alg / (sweep_ms / 1e3) / 1e9,
+           "peak_gbs": hbm_peak, "peak_source": hbm_kind}
+    hbm["frac"] = hbm["achieved_gbs"] / hbm_peak
+    out = {"kernel": "sweep (k_sweep_reg<32/64/128>, k_sweep)", "sweep_ms": sweep_ms, "hbm": hbm}
+    if SWEEP_PER_SPAN["warp_inst"]:
+        inst = SWEEP_PER_SPAN["warp_inst"] * spans
+        peak = sms * 4 * mhz * 1e6 / 1e9
+        ach = inst / (sweep_ms / 1e3) / 1e9
+        out.update({"bound": "issue", "achieved": ach, "peak": peak, "unit": "Gwarp-inst/s",
+                    "frac": ach / peak, "peak_source": f"{sms} SMs x 4 issue slots x {mhz:.0f} MHz",
+                    "traffic": SWEEP_PER_SPAN["dram_bytes"] * spans
+                    if SWEEP_PER_SPAN["dram_bytes"] else None})
+    else:
+        out.update({"bound": "hbm", "achieved": hbm["achieved_gbs"], "peak": hbm_peak,
+                    "unit": "GB/s", "frac": hbm["frac"], "peak_source": hbm_kind, "traffic": None})
+    return out
+
+
+def _cached_scenes(name, make):
     from skity_gb300 import scene as S
-    cache = os.path.join("/tmp", "skity_config3_v1.bin")
+    cache = os.path.join("/tmp", f"skity_{name}_v1.bin")
     try:
         with open(cache, "rb") as f:
             buf = f.read()
@@ -155,11 +202,11 @@ def load_config3():
             n = int.from_bytes(buf[o:o + 8], "little")
             scenes.append(S.Scene.from_bytes(buf[o + 8:o + 8 + n]))
             o += 8 + n
-        if len(scenes) == 256:
+        if scenes:
             return scenes
     except Exception:
         pass
-    scenes = S.config3()
+    scenes = make()
     try:
         with open(cache, "wb") as f:
             for sc in scenes:
@@ -170,95 +217,76 @@ def load_config3():
     return scenes
 
 
-def batch_forms(ctx, steps: int, warmup: int, sample: int, cpu_sample: int = 64):
-    """The 256-canvas batching workload (log-uniform sides in [64,1024],
-    log-uniform 50-2,000 paths each, drawn as in the 512x512 scene) in three
-    forms: the batched form (one planned batch, re-rendered by CUDA graph
-    replay), the plain per-draw form (one launch sequence per DrawPath onto a
-    device canvas, skity_cuda_draw_path_static) on the first `sample`
-    canvases, and the CPU oracle on all host cores over the first
-    `cpu_sample` canvases, dealt largest first to a pool of one thread per
-    core (each thread takes the next canvas when it finishes one), so that
-    every core stays busy to the end.  The per-draw result is compared with
-    the batched one on its sample."""
-    import numpy as np
-    import torch
+def load_config3():
+    from skity_gb300 import scene as S
+    return _cached_scenes("config3", S.config3)
+
+
+def load_config2():
+    from skity_gb300 import scene as S
+    return _cached_scenes("config2", lambda: [S.config2()])[0]
+
+
+def load_config4():
+    from skity_gb300 import scene as S
+    return _cached_scenes("config4", lambda: [S.config4()])[0]
+
+
+def committed_digests() -> dict:
+    try:
+        with open(os.path.join(HERE, "tests", "golden", "full_digests.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def digest(px) -> str:
+    return hashlib.sha256(px.tobytes()).hexdigest()
+
+
+def oracle_pool(scenes, threads: int):
+    """The oracle on `threads` host threads, one canvas per thread at a time,
+    canvases dealt largest first: pixels per canvas and the wall time."""
     from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle
-    from skity_gb300.canvas import Batch, DeviceCanvas
-
-    scenes = load_config3()
-    pix = sum(sc.width * sc.height for sc in scenes)
-    paths = sum(sc.n_draws for sc in scenes)
-    batch = Batch(ctx, scenes)
-    from skity_gb300 import autotune
-    tuned = autotune.tune(batch, autotune.signature(scenes, "GB300"), reps=2)
-    for _ in range(max(warmup, 1)):
-        batch.render()
-    ms = []
-    for _ in range(steps):
-        st = batch.render()
-        ms.append(st["device_ms"])
-    bms = statistics.mean(ms)
-    stage = {k: st[k] for k in ("geometry_ms", "sweep_emit_ms", "composite_ms", "blur_ms")}
-    out = {"workload": "256 canvases, sides log-uniform [64,1024], 50-2,000 paths each "
-                       "(3-32 verbs line/quad/cubic, nonzero, solid colours)",
-           "canvases": len(scenes), "paths": paths, "mpix": pix / 1e6,
-           "batched": {"ms": bms, "mpix_per_s": pix / 1e3 / bms, "paths_per_s": paths * 1e3 / bms,
-                       "graph_replays": int(st["graph_replays"]), "stage_ms": stage,
-                       "raster_config": tuned["config"], "autotune_cached": tuned["cached"],
-                       "autotune_trials": len(tuned.get("trials", [])),
-                       "spans": st["spans"], "fragments": st["fragments"],
-                       "form": "one planned batch, "
-                       "CUDA-graph replay (geometry, sweeps, composites)"}}
-    # per-draw form on a sample of canvases
-    sub = scenes[:sample]
-    spix = sum(sc.width * sc.height for sc in sub)
-    spaths = sum(sc.n_draws for sc in sub)
-    stream = torch.cuda.current_stream()
-    canv = [torch.full((sc.height, sc.width, 4), 255, dtype=torch.uint8, device="cuda")
-            for sc in sub]
-    dcs = [DeviceCanvas(c.data_ptr(), sc.width, sc.height, device=torch.cuda.current_device(),
-                        stream=stream.cuda_stream) for c, sc in zip(canv, sub)]
-    dcs[0].draw_scene(sub[0].subset(0, 8))  # first call: one-time set-up
-    for c in canv:
-        c.fill_(255)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for dc, sc in zip(dcs, sub):
-        dc.draw_scene(sc)
-    torch.cuda.synchronize()
-    pd_s = time.perf_counter() - t0
-    exact = all(np.array_equal(c.cpu().numpy(), batch.read(i)) for i, c in enumerate(canv))
-    out["per_draw"] = {"ms_per_canvas": 1e3 * pd_s / len(sub), "mpix_per_s": spix / 1e6 / pd_s,
-                       "paths_per_s": spaths / pd_s, "sample": f"first {len(sub)} canvases, "
-                       f"{spaths} paths", "matches_batched": exact,
-                       "form": "skity_cuda_draw_path_static per DrawPath on a device canvas"}
-    # CPU oracle on all host cores: a pool of one thread per core, canvases
-    # dealt largest first (paths x rows), each thread taking the next canvas
-    threads = os.cpu_count() or 1
     oracle.build()
-    csub = sorted(scenes[:cpu_sample], key=lambda sc: -sc.n_draws * sc.height)
-    cpix = sum(sc.width * sc.height for sc in csub)
-    cpaths = sum(sc.n_draws for sc in csub)
+    order = sorted(range(len(scenes)), key=lambda i: -scenes[i].n_draws * scenes[i].height)
+    out = [None] * len(scenes)
 
-    def one(sc):
-        t = time.perf_counter()
-        oracle.render(sc)
-        return time.perf_counter() - t
+    def one(i):
+        out[i] = oracle.render(scenes[i])[0]
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(threads) as ex:
-        busy = sum(ex.map(one, csub))
-    cpu_s = time.perf_counter() - t0
-    out["cpu"] = {"mpix_per_s": cpix / 1e6 / cpu_s, "paths_per_s": cpaths / cpu_s, "cores": threads,
-                  "kind": "port", "seconds": cpu_s, "core_busy": busy / (threads * cpu_s),
-                  "sample": f"first {len(csub)} canvases ({cpaths} paths), largest first on a "
-                            f"{threads}-thread pool"}
-    out["batched_over_per_draw"] = out["batched"]["paths_per_s"] / out["per_draw"]["paths_per_s"]
-    out["batched_over_cpu"] = out["batched"]["paths_per_s"] / out["cpu"]["paths_per_s"]
-    batch.close()
-    return out
+        list(ex.map(one, order))
+    return out, time.perf_counter() - t0
+
+
+def parity(got: list, want: list) -> dict:
+    from oracle import oracle
+    worst, bad, px = 0, 0, 0
+    for g, w in zip(got, want):
+        c = oracle.compare(g, w)
+        worst = max(worst, c["max_abs_diff"])
+        bad += c["bad_pixels"]
+        px += g.shape[0] * g.shape[1]
+    exact = 1.0 - bad / max(px, 1)
+    return {"max_abs_diff": worst, "exact_frac": exact, "bad_pixels": bad, "pixels": px,
+            "pass": worst <= TOL_LSB and exact >= MIN_EXACT, "against": "oracle pixels"}
+
+
+def parity_by_digest(name: str, got: list, scenes, threads: int) -> dict:
+    """Pixels against the committed oracle digests of the workload; on a
+    mismatch the oracle renders the canvases and the difference is
+    measured."""
+    want = committed_digests().get(name)
+    if want and len(want) == len(got) and all(digest(g) == w for g, w in zip(got, want)):
+        return {"max_abs_diff": 0, "exact_frac": 1.0, "bad_pixels": 0,
+                "pixels": sum(g.shape[0] * g.shape[1] for g in got), "pass": True,
+                "against": "committed oracle digests (tests/golden/full_digests.json)"}
+    from oracle import oracle
+    ref = [oracle.render_mt(sc, threads)[0] for sc in scenes]
+    return parity(got, ref)
 
 
 def serving_pool(n: int = 64):
@@ -389,91 +417,99 @@ def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512)
             "offline_batched": offline, "rates": results}
 
 
-def load_config4():
-    from skity_gb300 import scene as S
-    cache = os.path.join("/tmp", "skity_config4_v1.bin")
-    try:
-        with open(cache, "rb") as f:
-            return S.Scene.from_bytes(f.read())
-    except Exception:
-        sc = S.config4()
-        try:
-            with open(cache, "wb") as f:
-                f.write(sc.to_bytes())
-        except Exception:
-            pass
-        return sc
 
 
-def other_workloads(ctx, steps: int):
-    """The 512x512 scene (1,000 fills) and the glyph-dense scene (4096x4096,
-    100,000 small even-odd outlines, a tenth with a kNormal blur): resident
-    batch renders (CUDA-graph replays) against the CPU oracle on one core
-    over the whole scene (a single canvas has no parallelism in the
-    reference)."""
+def other_workloads(ctx, steps: int, threads: int):
+    """The 512x512 scene (1,000 fills), the single large scene (2048x2048,
+    20,000 paths with gradients, strokes and both fill rules) and the
+    glyph-dense scene (4096x4096, 100,000 small even-odd outlines, a tenth
+    with a kNormal blur): resident batch renders (CUDA-graph replays), their
+    pixels checked against the committed oracle digests, and the oracle
+    timed on one core (a single canvas has no parallelism in the reference)
+    -- over the whole scene, or the first paths of the 2048x2048 one."""
     from oracle import oracle
     from skity_gb300 import scene as S
     from skity_gb300.canvas import Batch
     out = {}
-    for name, sc, desc in [
-            ("config1", S.config1(), "512x512, 1,000 fills of 3-32 verbs, nonzero, solid"),
+    for name, sc, desc, cpu_paths in [
+            ("config1", S.config1(), "512x512, 1,000 fills of 3-32 verbs, nonzero, solid", None),
+            ("config2", load_config2(), "2048x2048, 20,000 paths of 3-64 verbs over [-64,2112]^2, "
+             "30% even-odd, 25% linear + 25% radial gradients, 20% stroked", 400),
             ("config4", load_config4(), "4096x4096, 100,000 outlines (1-3 contours, 8-48 px), "
-                                        "even-odd, 10% kNormal blur sigma 2-20")]:
+                                        "even-odd, 10% kNormal blur sigma 2-20", None)]:
         b = Batch(ctx, [sc])
         for _ in range(3):
             b.render()
-        ms = [b.render()["device_ms"] for _ in range(steps)]
-        st = ctx.stats()
+        sts = [b.render() for _ in range(steps)]
+        st = sts[-1]
+        pix = b.read(0)
         b.close()
-        gms = statistics.mean(ms)
-        _, cst = oracle.render(sc)
+        gms = statistics.mean(s["device_ms"] for s in sts)
+        n = sc.n_draws if cpu_paths is None else cpu_paths
+        _, cst = oracle.render(sc, 0, n)
+        cpu_ps = n / cst.seconds
         px = sc.width * sc.height
         out[name] = {"workload": desc, "paths": sc.n_draws,
                      "gpu": {"ms": gms, "paths_per_s": sc.n_draws * 1e3 / gms,
                              "mpix_per_s": px / 1e3 / gms,
-                             "stage_ms": {k: st[k] for k in ("geometry_ms", "sweep_emit_ms",
-                                                             "composite_ms", "blur_ms")}},
-                     "cpu": {"s": cst.seconds, "paths_per_s": sc.n_draws / cst.seconds,
-                             "cores": 1, "kind": "port", "sample": "whole scene"},
-                     "gpu_over_cpu": (sc.n_draws * 1e3 / gms) / (sc.n_draws / cst.seconds)}
+                             "stage_ms": {k: st[k] for k in ("geometry_ms", "plan_ms",
+                                                             "sweep_emit_ms", "composite_ms",
+                                                             "blur_ms")},
+                             "spans": st["spans"], "fragments": st["fragments"]},
+                     "cpu": {"paths_per_s": cpu_ps, "cores": 1, "kind": "port",
+                             "sample": "whole scene" if cpu_paths is None
+                             else f"first {n} of {sc.n_draws} paths, {cst.seconds:.1f} s"},
+                     "gpu_over_cpu": (sc.n_draws * 1e3 / gms) / cpu_ps,
+                     "parity": parity_by_digest(name, [pix], [sc], threads),
+                     "coverage": coverage_report(ctx, sc, 16)}
     return out
 
 
-def cpu_baseline(scene, threads: int, sample_paths: int, steps: int = 1):
-    """The oracle (CPU restatement of the reference path) on the first
-    `sample_paths` draws; paths/s over `steps` repetitions."""
+def coverage_report(ctx, scene, n_draws: int) -> dict:
+    """The FP64 exact-area coverage report (oracle/exact_area.cc) of the
+    first `n_draws` fill draws of a workload: each fill rendered alone (opaque
+    white on transparent) by the GPU and by the oracle, its alpha against the
+    path's true area -- max and mean error in 1/255 units over the pixels
+    either touches."""
     from oracle import oracle
-    oracle.build()
-    secs = []
-    for _ in range(steps):
-        if threads == 1:
-            _, st = oracle.render(scene, 0, sample_paths)
-        else:
-            _, st = oracle.render_mt(scene, threads, 0, sample_paths)
-        secs.append(st.seconds)
-    return sample_paths / statistics.mean(secs), secs
+    cs = oracle.coverage_scenes(scene.subset(0, min(scene.n_draws, 4 * n_draws)))[:n_draws]
+    gpu = ctx.render_streams([s for _, s in cs])
+    ref = [oracle.render(s)[0] for _, s in cs]
+    sub = scene.subset(0, min(scene.n_draws, 4 * n_draws))
+    rg = oracle.coverage_error(sub, [g[..., 3] for g in gpu])
+    rr = oracle.coverage_error(sub, [r[..., 3] for r in ref])
+    return {"draws": len(cs), "gpu": rg, "reference": rr,
+            "same_pixels": all(bool((g == r).all()) for g, r in zip(gpu, ref))}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU software path -- its restatement
+    in oracle/, pinned pixel for pixel to the reference's own build -- on the
+    same 256 canvases, on every host core (a pool of one thread per core,
+    canvases largest first).  Each step renders every canvas."""
     if rank != 0:
         return 0
-    scene = load_scene()
+    scenes = load_config3()
+    if args.ref_canvases:
+        scenes = scenes[:args.ref_canvases]
     threads = os.cpu_count() or 1
-    sample = args.ref_sample_paths
-    # warm-up (untimed), then timed steps, each a bounded sample of the scene
+    paths = sum(sc.n_draws for sc in scenes)
     for _ in range(args.warmup):
-        cpu_baseline(scene, threads, min(sample, 50))
-    value, secs = cpu_baseline(scene, threads, sample, steps=args.steps)
+        oracle_pool(scenes, threads)
+    secs = [oracle_pool(scenes, threads)[1] for _ in range(args.steps)]
+    ms = 1e3 * statistics.mean(secs)
+    value = paths / (ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs) * scene.n_draws / sample,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32/f32",
-        "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": WORKLOAD, "canvas": "2048x2048", "paths": scene.n_draws},
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/int32/f32", "data": "synthetic (seeded)",
+        "impl": "reference", "config": bench_config(scenes, world),
+        "mpix_per_s": sum(sc.width * sc.height for sc in scenes) / 1e6 / (ms / 1e3),
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} of {scene.n_draws} paths per step, banded rows "
-                                   f"on {threads} threads (identical pixels)"},
-        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                         "sample": f"every step: all {len(scenes)} canvases ({paths} paths) on a "
+                                   f"{threads}-thread pool, largest first"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
@@ -485,13 +521,20 @@ def run_gpu(args, rank, world, local):
     torch.cuda.set_device(local)
     if world > 1 and not dist.is_initialized():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from skity_gb300 import autotune
     from skity_gb300.canvas import Batch, Context
 
-    scene = load_scene()
-    if args.paths:
-        scene = scene.subset(0, args.paths)
+    scenes = load_config3()
+    if args.canvases:
+        scenes = scenes[:args.canvases]
+    paths = sum(sc.n_draws for sc in scenes)
+    pix = sum(sc.width * sc.height for sc in scenes)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    threads = os.cpu_count() or 1
     ctx = Context(local)
-    batch = Batch(ctx, [scene])
+    batch = Batch(ctx, scenes)
+    tuned = (autotune.tune(batch, autotune.signature(scenes, "GB300"), reps=2)
+             if not args.no_tune else {"config": batch.config(), "cached": False, "trials": []})
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     for _ in range(max(args.warmup, 1)):
@@ -518,71 +561,85 @@ def run_gpu(args, rank, world, local):
     if world > 1:
         dist.all_reduce(total_ms, op=dist.ReduceOp.MAX)
     ms_per_step = total_ms.item() / args.steps
-    paths = scene.n_draws
     value = world * paths / (ms_per_step / 1e3)
-    mpix = world * scene.width * scene.height / (ms_per_step / 1e3) / 1e6
     last = stages[-1]
+    got = [batch.read(i) for i in range(len(scenes))]
 
-    # end to end through the C ABI with host buffers (upload + render + readback)
+    # end to end through the C ABI with host buffers: every step uploads the
+    # scene streams, plans and renders on the device, and reads every canvas back
     e2e_ms = []
     if not args.no_e2e:
-        ctx.render_streams([scene])  # warm
-        for _ in range(max(1, min(args.steps, 3))):
-            ctx.render_streams([scene])
+        ctx.render_streams(scenes)  # warm
+        for _ in range(max(1, min(args.steps, 5))):
+            e2e_out = ctx.render_streams(scenes)
             e2e_ms.append(ctx.stats()["total_ms"])
+        e2e_same = all(bool((a == b).all()) for a, b in zip(e2e_out, got))
     e2e_ms_mean = statistics.mean(e2e_ms) if e2e_ms else None
 
-    # roofline of the dominant stage
     stage_ms = {k: statistics.mean(s[k] for s in stages)
-                for k in ("geometry_ms", "sweep_count_ms", "sweep_emit_ms", "composite_ms", "blur_ms")}
-    dom = max(stage_ms, key=stage_ms.get)
+                for k in ("geometry_ms", "plan_ms", "sweep_count_ms", "sweep_emit_ms",
+                          "composite_ms", "blur_ms")}
     peak, peak_kind = measured_peaks()
-    spans, frags, pixels, edges = last["spans"], last["fragments"], last["pixels"], last["edges"]
-    # algorithmic bytes per launch of each stage (measurement section)
-    alg = {
-        "composite_ms": spans * 8 + pixels * 4 * 2 + last["passes"] * 24,
-        "sweep_emit_ms": spans * 8 + edges * 84 * 2,
-        "sweep_count_ms": edges * 84 * 2,
-        "geometry_ms": edges * 84 * 2,
-        "blur_ms": 0,
-    }[dom]
-    achieved = alg / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32/f32",
-        "data": "synthetic (seeded, skity_gb300.scene.config2)",
-        "config": {"workload": WORKLOAD, "canvas": "2048x2048", "paths": paths,
-                   "l2": "flushed between steps (256 MiB device write)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-        "mpix_per_s": mpix,
+        "data": "synthetic (seeded, skity_gb300.scene.config3)",
+        "config": bench_config(scenes, world),
+        "mpix_per_s": world * pix / 1e6 / (ms_per_step / 1e3),
         "stage_ms": stage_ms,
-        "work": {"passes": last["passes"], "edges": edges, "spans": spans, "fragments": frags,
-                 "fragments_per_s": world * frags / (ms_per_step / 1e3)},
+        "raster_config": tuned["config"], "autotune_cached": tuned.get("cached"),
+        "work": {"passes": last["passes"], "edges": last["edges"], "spans": last["spans"],
+                 "fragments": last["fragments"],
+                 "fragments_per_s": world * last["fragments"] / (ms_per_step / 1e3)},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stages)),
+        "host_syncs_per_step": int(last["host_syncs"]),
         "clocks": clk,
-        "roofline": {"kernel": dom.replace("_ms", ""), "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else None,
-                     "peak_source": peak_kind, "traffic": None},
-        "issue_roofline": issue_roofline(last, ms_per_step, stage_ms["composite_ms"], clk),
+        "roofline": sweep_roofline(last, stage_ms["sweep_emit_ms"], clk, sms, peak, peak_kind),
+        "issue_roofline": issue_roofline(last, ms_per_step, stage_ms["composite_ms"], clk, sms),
         "e2e": {"value": (world * paths / (e2e_ms_mean / 1e3)) if e2e_ms_mean else None,
-                "unit": "paths/s", "h2d_bytes_per_step": len(scene.to_bytes()),
-                "d2h_bytes_per_step": scene.width * scene.height * 4,
-                "ms_per_step": e2e_ms_mean},
+                "unit": "paths/s",
+                "h2d_bytes_per_step": sum(len(sc.to_bytes()) for sc in scenes),
+                "d2h_bytes_per_step": pix * 4, "ms_per_step": e2e_ms_mean,
+                "same_pixels": e2e_same if e2e_ms else None},
         "wall_s": wall,
     }
+    if rank == 0 and not args.no_per_draw:
+        # the per-draw form runs each path's sequential work alone (about
+        # 1.6 ms a draw), so it is timed on the first canvases only
+        sub = scenes[:args.per_draw_canvases]
+        spaths = sum(sc.n_draws for sc in sub)
+        spix = sum(sc.width * sc.height for sc in sub)
+        pb = Batch(ctx, sub)
+        pst = pb.render_per_draw()  # capacities found on the way (its time: the last attempt)
+        pd_same = all(bool((pb.read(i) == g).all()) for i, g in enumerate(got[:len(sub)]))
+        pb.close()
+        line["per_draw"] = {"ms": pst["device_ms"], "paths_per_s": spaths * 1e3 / pst["device_ms"],
+                            "mpix_per_s": spix / 1e3 / pst["device_ms"],
+                            "ms_per_draw": pst["device_ms"] / spaths,
+                            "kernel_launches": int(pst["kernel_launches"]),
+                            "host_syncs": int(pst["host_syncs"]), "same_pixels": pd_same,
+                            "sample": f"first {len(sub)} canvases ({spaths} paths)",
+                            "form": "skity_cuda_batch_render_per_draw: geometry, plan, sweep and "
+                                    "composite launches per DrawPath, one stream, no host sync "
+                                    "until the end"}
+        line["batched_over_per_draw"] = value / world / line["per_draw"]["paths_per_s"]
+    if rank == 0 and not args.no_cpu:
+        ref, cpu_s = oracle_pool(scenes, threads)
+        line["parity"] = parity(got, ref)
+        line["cpu_baseline"] = {"value": paths / cpu_s, "unit": "paths/s", "cores": threads,
+                                "kind": "port", "seconds": cpu_s,
+                                "sample": f"all {len(scenes)} canvases ({paths} paths) on a "
+                                          f"{threads}-thread pool, largest first"}
+        line["batched_over_cpu"] = value / world / (paths / cpu_s)
+        line["coverage"] = coverage_report(ctx, scenes[0], 32)
+        if e2e_ms_mean:
+            line["e2e_over_cpu"] = (paths / (e2e_ms_mean / 1e3)) / (paths / cpu_s)
     if rank == 0 and not args.no_others:
-        line["other_workloads"] = other_workloads(ctx, max(1, min(args.steps, 5)))
+        line["other_workloads"] = other_workloads(ctx, max(1, min(args.steps, 5)), threads)
     if rank == 0 and args.serve_seconds > 0:
         line["serving"] = serving(ctx, [float(r) for r in args.serve_rates.split(",")],
                                   args.serve_seconds, local)
-    if rank == 0 and not args.no_forms:
-        line["batching"] = batch_forms(ctx, max(1, min(args.steps, 5)), 3, args.per_draw_sample)
-    if rank == 0 and not args.no_cpu:
-        v, secs = cpu_baseline(scene, 1, args.cpu_sample_paths)
-        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": 1, "kind": "port",
-                                "sample": f"first {args.cpu_sample_paths} of {paths} paths, "
-                                          f"{secs[0]:.1f} s single-threaded"}
     batch.close()
     ctx.close()
     if rank == 0:
@@ -598,20 +655,21 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--cpu-sample-paths", type=int, default=400)
-    ap.add_argument("--ref-sample-paths", type=int, default=800)
-    ap.add_argument("--paths", type=int, default=0,
-                    help="render only the first N paths of the scene (small profiling case)")
+    ap.add_argument("--canvases", type=int, default=0,
+                    help="render only the first N canvases (small profiling case)")
+    ap.add_argument("--ref-canvases", type=int, default=0,
+                    help="reference arm: the first N canvases per step (default all)")
+    ap.add_argument("--no-tune", action="store_true", help="default raster config, no autotuning")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-forms", action="store_true",
-                    help="skip the 256-canvas batched / per-draw / CPU comparison")
-    ap.add_argument("--per-draw-sample", type=int, default=16)
+    ap.add_argument("--no-per-draw", action="store_true")
+    ap.add_argument("--per-draw-canvases", type=int, default=8,
+                    help="canvases the per-draw form is timed on")
     ap.add_argument("--no-others", action="store_true",
-                    help="skip the 512x512 and glyph-dense scenes")
+                    help="skip the 512x512, 2048x2048 and glyph-dense scenes")
     ap.add_argument("--serve-rates", default="200,1000,5000",
                     help="Poisson request rates (requests/s) of the serving runs")
-    ap.add_argument("--serve-seconds", type=float, default=5.0,
-                    help="arrival window per rate (the serving workload specifies 60 s); 0 skips")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="arrival window per rate (the serving workload's 60 s); 0 skips")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()

@@ -289,6 +289,14 @@ SKITY_CUDA_API int32_t skity_cuda_batch_create(skity_cuda_context ctx, uint32_t 
                                                const size_t* stream_bytes,
                                                skity_cuda_batch* out);
 SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch);
+/* The plain per-draw form of the same render: every DrawPath of every
+ * canvas rasterised and blended on its own, in order (geometry, sweep and
+ * composite launches per draw, queued with no host round trip), as the
+ * software canvas draws (SWCanvas::OnDrawPath, src/render/sw/
+ * sw_canvas.cc:357-411).  Same pixels as skity_cuda_batch_render; it is the
+ * baseline that batching is measured against.  Batches with blur mask
+ * filters or path clips: SKITY_CUDA_ERROR_NOT_SUPPORTED. */
+SKITY_CUDA_API int32_t skity_cuda_batch_render_per_draw(skity_cuda_batch batch);
 SKITY_CUDA_API int32_t skity_cuda_batch_read(skity_cuda_batch batch, uint32_t index,
                                              uint8_t* out_pixels);
 SKITY_CUDA_API void skity_cuda_batch_destroy(skity_cuda_batch batch);

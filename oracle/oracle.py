@@ -13,7 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libskity_oracle.so")
 REF_RENDER = os.path.join(HERE, "_ref", "ref_render")
-REFERENCE_SRC = "/root/reference"
+# the reference checkout the pinning build compiles from
+REFERENCE_SRC = os.environ.get("SKITY_REFERENCE", "/root/reference")
 
 
 class Stats(ctypes.Structure):

@@ -137,6 +137,7 @@ SIGNATURES = {
     "skity_cuda_batch_create": (ctypes.c_int32, [_vp, ctypes.c_uint32, ctypes.POINTER(_vp),
                                                  ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
+    "skity_cuda_batch_render_per_draw": (ctypes.c_int32, [_vp]),
     "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
     "skity_cuda_batch_destroy": (None, [_vp]),
     "skity_cuda_context_set_config": (ctypes.c_int32, [_vp, ctypes.POINTER(RasterConfig_)]),

@@ -22,7 +22,7 @@ LIB = os.path.join(BUILD, "libskity_cuda.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden"]
-SOURCES = ["kernels.cu", "pipeline.cu", "static_draw.cu", "server.cu"]
+SOURCES = ["kernels.cu", "plan.cu", "pipeline.cu", "per_draw.cu", "static_draw.cu", "server.cu"]
 
 
 def nvcc() -> str:

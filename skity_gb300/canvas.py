@@ -364,6 +364,13 @@ class Batch:
         _lib.check(self.lib.skity_cuda_batch_render(self.handle), "skity_cuda_batch_render")
         return self.ctx.stats()
 
+    def render_per_draw(self) -> dict:
+        """skity_cuda_batch_render_per_draw: the same canvases rendered one
+        DrawPath at a time (the plain per-draw form)."""
+        _lib.check(self.lib.skity_cuda_batch_render_per_draw(self.handle),
+                   "skity_cuda_batch_render_per_draw")
+        return self.ctx.stats()
+
     def set_config(self, tile_width: int = 256, ctas_per_sm: int = 4, band_rows: int = 16):
         """skity_cuda_batch_set_config: the compositor's launch shape and bin
         granularity (the pixels do not change); the next render replans."""

@@ -984,6 +984,27 @@ inline void OrderRowTasks(const HostBatch& hb, const std::vector<uint32_t>& band
   tasks.swap(out);
 }
 
+// Pass-bin segments of the device planner: for every band of every canvas,
+// in band order, runs of at most kSegPasses of the canvas's passes (a band
+// of a canvas without passes gets one empty segment, so every band has one).
+constexpr uint32_t kSegPasses = 1024;
+inline void BuildBandSegs(const HostBatch& hb, int shift, std::vector<BandSeg>& segs) {
+  segs.clear();
+  for (const CanvasDesc& cd : hb.canvases) {
+    const uint32_t nb = (cd.h + (1u << shift) - 1) >> shift;
+    for (uint32_t k = 0; k < nb; ++k) {
+      uint32_t p0 = cd.pass0;
+      bool first = true;
+      do {
+        const uint32_t p1 = std::min<uint32_t>(cd.pass1, p0 + kSegPasses);
+        segs.push_back(BandSeg{cd.band0 + k, p0, p1, first ? 1u : 0u});
+        first = false;
+        p0 = p1;
+      } while (p0 < cd.pass1);
+    }
+  }
+}
+
 inline void BuildRowTasks(const HostBatch& hb, const std::vector<uint32_t>& canv, uint32_t chunk,
                           std::vector<RowTask>& out) {
   out.clear();
@@ -1006,15 +1027,6 @@ struct SweepPlan {
 inline int32_t RegDiffCap(const SweepPlan& pl) {
   int32_t c = (pl.max_acc + 3) & ~3;
   return std::max<int32_t>(4, std::min<int32_t>(c, kRegDiffMax));
-}
-// Spans per pool chunk for a pass: a power of two holding any one row of it.
-// A row has at most one direct span per pixel plus one per interval end and
-// one accumulated run per pixel: 2 * width + 2 * edges + 64 bounds it.
-inline uint32_t SpanChunk(uint32_t width, int32_t edges) {
-  uint64_t need = 2ull * width + 2ull * (uint64_t)std::max(edges, 0) + 64;
-  uint64_t c = 4096;
-  while (c < need) c <<= 1;
-  return (uint32_t)std::min<uint64_t>(c, 1ull << 31);
 }
 inline SweepPlan PlanSweep(const HostBatch& hb, const std::vector<PassGeom>& geom,
                            std::vector<PassSweep>& sw) {

@@ -68,6 +68,19 @@ struct DeviceBatch {
   RasterConfig cfg;
   DevBuf task_next;  // persistent compositor's counters
   DevBuf clip_states, clip_flags, clip_rows, clip_items;  // path clips
+  // device planning (batches without path clips): status, per-pass scan
+  // arrays and band ranges, bin segments, the tiles (main then temp) and
+  // their sorted copy; capacities of the plan's buffers
+  DevBuf plan_st, plan_a, plan_r, pband, segs, seg_cnt, tasks_in, tasks_sorted;
+  DevBuf sort_keys, sort_hist;
+  std::vector<BandSeg> h_segs;
+  bool slices_dirty = true;   // pass capacities changed: slice offsets and passes re-uploaded
+  uint64_t cap_sweep = 0, cap_rows = 0, cap_bins = 0;
+  uint64_t cap_scratch = 0;
+  // the launch parameters the replay graphs were recorded with
+  DevBatch graph_b{};
+  DevPlan graph_q{};
+  int graph_launches = 0;
   // true when the caller has loaded the canvases' current pixels (a canvas
   // flush without a clear); otherwise a canvas without a clear colour starts
   // from transparent black, as a fresh Bitmap does
@@ -79,7 +92,7 @@ struct DeviceBatch {
   // same launches on the same buffers without host round trips.
   bool want_graph = false;
   bool graph_ok = false;
-  cudaGraphExec_t graphs[5] = {};
+  cudaGraphExec_t graphs[6] = {};
   DevBatch planned{};
   uint64_t planned_rows = 0;
   const void* planned_pool = nullptr;  // the context span pool the plan used
@@ -87,6 +100,27 @@ struct DeviceBatch {
   ~DeviceBatch() {
     for (auto g : graphs)
       if (g) cudaGraphExecDestroy(g);
+  }
+  // Forgets the batch's canvases and draws but keeps its device buffers, so
+  // the next batch built in it reuses their memory.
+  void Reset() {
+    for (auto& g : graphs) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+    graph_ok = false;
+    hb = HostBatch{};
+    h_tasks_main.clear();
+    h_tasks_temp.clear();
+    h_band_off.clear();
+    h_bins.clear();
+    h_segs.clear();
+    h_geom.clear();
+    keep_pixels = false;
+    uploaded = false;
+    slices_dirty = true;
+    cap_sweep = cap_rows = cap_bins = 0;
+    stats = skity_cuda_stats{};
   }
   std::vector<PassGeom> h_geom;
   skity_cuda_stats stats{};
@@ -102,7 +136,14 @@ struct skity_cuda_context_s {
   skc::DevBuf span_pool, span_next;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t stage[10] = {};
+  cudaEvent_t stage[12] = {};
+  // largest plan needs seen by the context's device-planned renders (sweep
+  // bytes, row entries, bin entries): first capacities of new batches
+  uint64_t hint_sweep = 0, hint_rows = 0, hint_bins = 0;
+  // the batch skity_cuda_render_streams builds each call in (its device
+  // buffers are reused from call to call)
+  skc::DeviceBatch* streams_batch = nullptr;
+  ~skity_cuda_context_s() { delete streams_batch; }
   skc::RasterConfig cfg;  // default launch shape of new batches and canvases
   uint32_t num_sms = 0;
   skity_cuda_stats last{};
@@ -126,5 +167,12 @@ int32_t ApplyConfig(skity_cuda_context_s* ctx, DeviceBatch& db, const RasterConf
 // Copies canvas `index` of the batch to host memory (row_bytes 0: packed).
 int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,
                    size_t row_bytes);
+// Renders the batch's main canvases one DrawPath at a time (per_draw.cu);
+// batches with blur mask filters or path clips are not taken.
+int32_t RenderPerDraw(skity_cuda_context_s* ctx, DeviceBatch& db);
+// Queues the copies of canvases [0, count) to out[i] (packed rows) on the
+// context stream; the caller waits for the stream.
+int32_t QueueReadCanvases(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t count,
+                          uint8_t* const* out);
 
 }  // namespace skc

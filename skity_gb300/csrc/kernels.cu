@@ -196,6 +196,9 @@ __global__ void __launch_bounds__(32 * kCompWarps, kCompMinBlocks)
     k_composite(DevBatch b, const RowTask* __restrict__ tasks, uint32_t n_tasks, uint32_t chunk,
                 unsigned int* counter) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
+  // a device plan that fell short: the host grows its buffers and renders
+  // again, so nothing is composited from it
+  if (b.plan && b.plan->flags) return;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   uint8_t* mine = reg_smem + (size_t)wib * CompWarpSmem(chunk);
@@ -413,12 +416,36 @@ int LaunchPathClips(const DevBatch& b, const ClipStateDesc* states, uint32_t n_s
 // the one crossing the centre is pixel(min(i + 1, n - 1)).  Horizontal pass:
 // canvas -> blur scratch; vertical pass: blur scratch -> canvas.
 // ---------------------------------------------------------------------------
+// Staged StackBlur: a block copies a run of whole rows (horizontal pass) or
+// a 32-column strip of every row (vertical pass) of one temp canvas into
+// shared memory with coalesced 4-byte loads -- the rows are contiguous in
+// memory, and 32 lanes cover 128 contiguous bytes of a strip row -- blurs
+// each line there with one thread per line (BlurLine, the same arithmetic
+// as the direct kernels above), and writes the result back coalesced.
+// Lines are stored an odd number of words apart, so the threads, each
+// walking its own line, hit distinct banks.  Temp canvases whose lines do
+// not fit the shared-memory budget take the direct kernels (they return at
+// once for the staged ones, and the staged ones for them).
+constexpr int kBlurThreads = 64;
+constexpr uint32_t kBlurSmemWords = 12 * 1024;  // 48 KiB: input and output lines
+
+__host__ __device__ inline uint32_t OddStride(uint32_t n) { return n | 1u; }
+// Rows per block of the staged horizontal pass (0: the row does not fit).
+__host__ __device__ inline uint32_t BlurRowsPerBlock(uint32_t w) {
+  const uint32_t r = kBlurSmemWords / (2 * OddStride(w));
+  return r < (uint32_t)kBlurThreads ? r : (uint32_t)kBlurThreads;
+}
+// The staged vertical pass takes canvases whose 32-column strip fits.
+__host__ __device__ inline bool BlurStripFits(uint32_t h) {
+  return 2ull * OddStride(32) * h <= kBlurSmemWords;
+}
+
 __global__ void k_blur_h(DevBatch b, const uint32_t* temps, uint32_t n_temp, uint32_t max_h) {
   uint32_t t = blockIdx.y;
   uint32_t yrow = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
-  if (yrow >= cd.h) return;
+  if (yrow >= cd.h || BlurRowsPerBlock(cd.w) != 0) return;  // staged
   const uint8_t* src = b.pixels + cd.px_off + (size_t)yrow * cd.w * 4;
   uint8_t* dst = b.pixels + cd.blur_off + (size_t)yrow * cd.w * 4;
   int r = min(cd.blur_radius, 254);
@@ -434,7 +461,7 @@ __global__ void k_blur_v(DevBatch b, const uint32_t* temps, uint32_t n_temp, uin
   uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
-  if (x >= cd.w) return;
+  if (x >= cd.w || BlurStripFits(cd.h)) return;  // staged
   int r = min(cd.blur_radius, 254);
   const uint8_t* src = b.pixels + cd.blur_off + (size_t)x * 4;
   uint8_t* dst = b.pixels + cd.out_off + (size_t)x * 4;
@@ -463,17 +490,99 @@ __global__ void k_blur_style(DevBatch b, const uint32_t* temps, uint32_t n_temp)
     out[i] = ARGBtoRGBA(BlurStylePixel(cd.blur_style, RGBAtoARGB(raw[i]), RGBAtoARGB(out[i])));
 }
 
+__global__ void __launch_bounds__(kBlurThreads)
+    k_blur_h_staged(DevBatch b, const uint32_t* temps, uint32_t n_temp) {
+  extern __shared__ uint32_t bsm[];
+  const uint32_t t = blockIdx.y;
+  if (t >= n_temp) return;
+  const CanvasDesc cd = b.canvases[temps[t]];
+  const uint32_t rows = BlurRowsPerBlock(cd.w);
+  if (rows == 0) return;
+  const uint32_t y0 = blockIdx.x * rows;
+  if (y0 >= cd.h) return;
+  const uint32_t nr = min(rows, cd.h - y0);
+  const uint32_t ws = OddStride(cd.w);
+  uint32_t* in = bsm;
+  uint32_t* out = bsm + rows * ws;
+  const uint32_t* src = (const uint32_t*)(b.pixels + cd.px_off) + (size_t)y0 * cd.w;
+  uint32_t* dst = (uint32_t*)(b.pixels + cd.blur_off) + (size_t)y0 * cd.w;
+  const uint32_t n = nr * cd.w;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) in[(i / cd.w) * ws + i % cd.w] = src[i];
+  __syncthreads();
+  const int r = min(cd.blur_radius, 254);
+  if (threadIdx.x < nr) {
+    const uint32_t* li = in + threadIdx.x * ws;
+    uint32_t* lo = out + threadIdx.x * ws;
+    if (r <= 1) {
+      for (uint32_t x = 0; x < cd.w; ++x) lo[x] = li[x];
+    } else {
+      BlurLine((const uint8_t*)li, (uint8_t*)lo, (int)cd.w, 1, r, false);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = out[(i / cd.w) * ws + i % cd.w];
+}
+
+__global__ void __launch_bounds__(32)
+    k_blur_v_staged(DevBatch b, const uint32_t* temps, uint32_t n_temp) {
+  extern __shared__ uint32_t bsm[];
+  const uint32_t t = blockIdx.y;
+  if (t >= n_temp) return;
+  const CanvasDesc cd = b.canvases[temps[t]];
+  if (!BlurStripFits(cd.h)) return;
+  const uint32_t x0 = blockIdx.x * 32;
+  if (x0 >= cd.w) return;
+  const uint32_t nc = min(32u, cd.w - x0);
+  const uint32_t ws = OddStride(32);
+  uint32_t* in = bsm;
+  uint32_t* out = bsm + cd.h * ws;
+  const uint32_t* src = (const uint32_t*)(b.pixels + cd.blur_off) + x0;
+  uint32_t* dst = (uint32_t*)(b.pixels + cd.out_off) + x0;
+  const uint32_t lane = threadIdx.x;
+  for (uint32_t y = 0; y < cd.h; ++y)
+    if (lane < nc) in[y * ws + lane] = src[(size_t)y * cd.w + lane];
+  __syncwarp();
+  const int r = min(cd.blur_radius, 254);
+  if (lane < nc) {
+    if (r <= 1) {
+      for (uint32_t y = 0; y < cd.h; ++y) out[y * ws + lane] = in[y * ws + lane];
+    } else {
+      BlurLine((const uint8_t*)(in + lane), (uint8_t*)(out + lane), (int)cd.h, ws, r, true);
+    }
+  }
+  __syncwarp();
+  for (uint32_t y = 0; y < cd.h; ++y)
+    if (lane < nc) dst[(size_t)y * cd.w + lane] = out[y * ws + lane];
+}
+
 int LaunchBlur(const DevBatch& b, const uint32_t* temps, uint32_t n_temp, uint32_t max_h,
                uint32_t max_w, cudaStream_t stream) {
   if (n_temp == 0) return 0;
-  dim3 gh((max_h + 63) / 64, n_temp);
-  k_blur_h<<<gh, 64, 0, stream>>>(b, temps, n_temp, max_h);
-  dim3 gv((max_w + 63) / 64, n_temp);
-  k_blur_v<<<gv, 64, 0, stream>>>(b, temps, n_temp, max_w);
+  // staged passes (their blocks for canvases that do not fit return at once)
+  const uint32_t min_rows = std::max<uint32_t>(BlurRowsPerBlock(max_w), 1);
+  dim3 gsh((max_h + min_rows - 1) / min_rows, n_temp);
+  const uint32_t smem_h = std::min<uint32_t>(2u * kBlurThreads * OddStride(max_w), kBlurSmemWords);
+  k_blur_h_staged<<<gsh, kBlurThreads, smem_h * 4, stream>>>(b, temps, n_temp);
+  // direct passes for the canvases the staged ones do not take
+  int n = 1;
+  if (BlurRowsPerBlock(max_w) == 0) {
+    dim3 gh((max_h + 63) / 64, n_temp);
+    k_blur_h<<<gh, 64, 0, stream>>>(b, temps, n_temp, max_h);
+    n++;
+  }
+  dim3 gsv((max_w + 31) / 32, n_temp);
+  const uint32_t smem_v = (uint32_t)std::min<uint64_t>(2ull * OddStride(32) * max_h, kBlurSmemWords);
+  k_blur_v_staged<<<gsv, 32, smem_v * 4, stream>>>(b, temps, n_temp);
+  n++;
+  if (!BlurStripFits(max_h)) {
+    dim3 gv((max_w + 63) / 64, n_temp);
+    k_blur_v<<<gv, 64, 0, stream>>>(b, temps, n_temp, max_w);
+    n++;
+  }
   const uint64_t px = (uint64_t)max_w * max_h;
   dim3 gs((unsigned)std::min<uint64_t>((px + 255) / 256, 1024), n_temp);
   k_blur_style<<<gs, 256, 0, stream>>>(b, temps, n_temp);
-  return 3;
+  return n + 1;
 }
 
 }  // namespace skc

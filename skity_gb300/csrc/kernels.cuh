@@ -177,7 +177,82 @@ struct DevBatch {
   // a canvas is general (CanvasDesc::general): the compositor's general
   // form runs for the whole batch
   uint32_t any_general;
+  // device-planned renders: the plan's status (null for host-planned
+  // ones); the compositor writes nothing when a plan buffer fell short
+  const struct PlanStatus* plan;
 };
+
+// Spans per pool chunk for a pass: a power of two holding any one row of it.
+// A row has at most one direct span per pixel plus one per interval end and
+// one accumulated run per pixel: 2 * width + 2 * edges + 64 bounds it.
+SKC_HD uint32_t SpanChunk(uint32_t width, int32_t edges) {
+  uint64_t need = 2ull * width + 2ull * (uint64_t)(edges > 0 ? edges : 0) + 64;
+  uint64_t c = 4096;
+  while (c < need) c <<= 1;
+  return (uint32_t)(c < (1ull << 31) ? c : (1ull << 31));
+}
+
+// ---------------------------------------------------------------------------
+// Device planning (plan.cu): after the geometry stage, the per-pass sweep
+// buffers, row tables, pass bins, sweep order and compositor tile order are
+// computed on the device from the passes' geometry -- prefix sums over the
+// passes, bins by warp-ballot compaction -- so a render needs no host round
+// trip between its stages.  Buffers have host-chosen capacities; a plan that
+// does not fit flags what fell short (and by how much) in its PlanStatus,
+// the stages after it skip the work that would not fit, and the host grows
+// the buffers and renders again.
+// ---------------------------------------------------------------------------
+enum : uint32_t {
+  kPlanGeomOverflow = 1,  // a pass's geometry scratch overflowed (PassGeom::status)
+  kPlanSweepMem = 2,      // sweep memory short
+  kPlanRows = 4,          // row-span table short
+  kPlanBins = 8,          // pass bins short
+};
+// pass_class of a pass no sweep form takes (nothing to sweep, or no room)
+constexpr uint8_t kSweepSkip = 4;
+
+struct PlanStatus {  // zeroed before each render, read back after it
+  uint32_t flags;
+  uint32_t geom_overflows;
+  unsigned long long sweep_need;  // sweep-memory bytes the passes need
+  unsigned long long rows_need;   // row-span entries
+  unsigned long long bins_need;   // pass-bin entries
+  // work of the render
+  unsigned long long spans, edges;
+  unsigned long long frags_by_brush[4];
+  unsigned long long sort_total[2];  // items of the sweep and tile sorts
+};
+
+struct BandSeg {   // a pass-bin segment: the passes [p0, p1) of the band's canvas
+  uint32_t band;   // global band index
+  uint32_t p0, p1;
+  uint32_t first;  // 1: the first segment of its band
+};
+
+struct DevPlan {
+  PlanStatus* st;
+  unsigned long long* a;  // per pass: sweep bytes, then their exclusive prefix sums
+  unsigned long long* r;  // per pass: rows, then their exclusive prefix sums
+  uint2* pband;           // per pass: first and last global band (x > y: none)
+  const BandSeg* segs;
+  uint32_t n_segs;
+  unsigned long long* seg_cnt;  // per segment: bin entries, then their prefix sums
+  uint32_t* band_off;
+  uint32_t n_bands;
+  uint32_t* bins;
+  uint64_t sweep_cap, rows_cap, bins_cap;  // capacities: bytes, entries, entries
+  uint32_t* sweep_order;
+  const RowTask* tasks_in;  // main canvases' tiles, then the temp canvases'
+  RowTask* tasks_out;       // the same, each list most work first
+  uint32_t n_main, n_temp;
+  // bucket-sort scratch: per item its key; per (key, block) counts, then
+  // their prefix sums
+  uint16_t* sort_keys;
+  unsigned long long* sort_hist;
+};
+int LaunchPlan(const DevBatch& b, const DevPlan& q, cudaStream_t stream);
+// Work totals of the render into the plan status.
+int LaunchPlanStats(const DevBatch& b, const DevPlan& q, cudaStream_t stream);
 
 // Shared memory of one register-sweep warp: its RegSharedT block, then an
 // accumulator of reg_diff_cap entries (passes with wider accumulators keep

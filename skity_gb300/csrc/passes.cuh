@@ -710,6 +710,10 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
     EmptyPass(b, p, lanes);
     return;
   }
+  // rows the sweep leaves without spans read as empty
+  uint2* rows = b.rowspan + b.sweep[p].rbase;
+  for (int r = lanes.lane; r < g.row1 - g.row0; r += Lanes::n) rows[r] = make_uint2(0, 0);
+  lanes.sync();
   PoolSinkReg sink;
   InitPoolSink(b, p, g, &sink);
   if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {

@@ -48,6 +48,19 @@ static cudaError_t Upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
   return cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
 }
 
+// Inputs of the device planner that depend only on the canvases, their
+// passes and the raster config: the compositor's tiles (main canvases, then
+// the temp canvases) and the pass-bin segments.
+static int32_t UploadDevicePlanInputs(skity_cuda_context_s* ctx, DeviceBatch& db) {
+  cudaStream_t s = ctx->stream;
+  std::vector<RowTask> all(db.h_tasks_main);
+  all.insert(all.end(), db.h_tasks_temp.begin(), db.h_tasks_temp.end());
+  SKC_TRY(Upload(db.tasks_in, all, s));
+  BuildBandSegs(db.hb, db.cfg.band_shift, db.h_segs);
+  SKC_TRY(Upload(db.segs, db.h_segs, s));
+  return SKITY_CUDA_SUCCESS;
+}
+
 int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   cudaStream_t s = ctx->stream;
   HostBatch& hb = db.hb;
@@ -85,6 +98,7 @@ int32_t UploadBatch(skity_cuda_context_s* ctx, DeviceBatch& db) {
   BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
   SKC_TRY(Upload(db.tasks_main, db.h_tasks_main, s));
   SKC_TRY(Upload(db.tasks_temp, db.h_tasks_temp, s));
+  if (int32_t rc = UploadDevicePlanInputs(ctx, db)) return rc;
   // PixmapBrush colour round trip per channel value (Color4fFromColor then
   // Color4fToColor, bitmap_sampler.cc:21-29, color.cc:44-59)
   std::vector<uint8_t> rtab(256);
@@ -110,6 +124,7 @@ int32_t ApplyConfig(skity_cuda_context_s* ctx, DeviceBatch& db, const RasterConf
   db.chunk = std::min<uint32_t>(maxw, std::max<uint32_t>(32, std::min<uint32_t>(cfg.tile_w, 2048)));
   BuildRowTasks(hb, hb.main_canvases, db.chunk, db.h_tasks_main);
   BuildRowTasks(hb, hb.temp_canvases, db.chunk, db.h_tasks_temp);
+  if (int32_t rc = UploadDevicePlanInputs(ctx, db)) return rc;
   for (auto& g : db.graphs) {
     if (g) cudaGraphExecDestroy(g);
     g = nullptr;
@@ -225,11 +240,344 @@ static void CaptureReplay(skity_cuda_context_s* ctx, DeviceBatch& db) {
 
 static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed);
 
+// ---------------------------------------------------------------------------
+// Device-planned render (batches without path clips): geometry -> device
+// plan -> sweeps -> composite of the temp canvases -> StackBlur -> composite
+// of the main canvases, all queued on the stream with no host round trip;
+// the host waits once, at the end, for the plan's status and the device
+// self-checks.  A plan that fell short (geometry scratch, sweep memory, row
+// table, pass bins, span pool) is rendered again with the buffers grown to
+// what the status reports.
+// ---------------------------------------------------------------------------
+static uint64_t GuessSweepBytes(const HostBatch& hb) {
+  uint64_t t = 0;
+  for (const PassDesc& pd : hb.passes) {
+    const uint32_t w = std::min<uint32_t>(hb.canvases[pd.canvas].w, 2048);
+    t += (SweepMemBytes(pd.cap[12], (int)w + 2) + 255) & ~uint64_t(255);
+  }
+  return t;
+}
+static uint64_t GuessRows(const HostBatch& hb) {
+  uint64_t t = 0;
+  for (const PassDesc& pd : hb.passes) t += hb.canvases[pd.canvas].h;
+  return std::min<uint64_t>(t, 64ull << 20);
+}
+static uint64_t GuessBins(const HostBatch& hb, int shift) {
+  uint64_t t = 0;
+  for (const CanvasDesc& cd : hb.canvases)
+    t += (uint64_t)((cd.h + (1u << shift) - 1) >> shift) * (cd.pass1 - cd.pass0);
+  return std::min<uint64_t>(std::max<uint64_t>(t, 1), 64ull << 20);
+}
+
+// Buffers of a device-planned render at the batch's current capacities, and
+// the launch parameters over them.
+static int32_t PrepareDevice(skity_cuda_context_s* ctx, DeviceBatch& db, DevBatch& b, DevPlan& q) {
+  HostBatch& hb = db.hb;
+  cudaStream_t s = ctx->stream;
+  const uint32_t np = (uint32_t)hb.passes.size();
+  const size_t npm = std::max<size_t>(np, 1);
+  if (db.slices_dirty) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < np; ++i) {
+      SliceLayout L;
+      L.compute(hb.passes[i].cap, sizeof(Edge));
+      hb.passes[i].slice_off = total;
+      total += L.bytes;
+    }
+    if (ctx->budget && total > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+    SKC_TRY(db.scratch.ensure(std::max<uint64_t>(total, 16)));
+    SKC_TRY(Upload(db.passes, hb.passes, s));
+    db.slices_dirty = false;
+  }
+  SKC_TRY(db.geom.ensure(npm * sizeof(PassGeom)));
+  SKC_TRY(db.sweep.ensure(npm * sizeof(PassSweep)));
+  SKC_TRY(db.comp.ensure(npm * sizeof(PassComp)));
+  SKC_TRY(db.pass_spans.ensure(npm * 4));
+  SKC_TRY(db.pass_frags.ensure(npm * 8));
+  SKC_TRY(db.pass_class.ensure(npm));
+  SKC_TRY(db.err.ensure(16));
+  SKC_TRY(db.plan_st.ensure(sizeof(PlanStatus)));
+  SKC_TRY(db.plan_a.ensure(npm * 8));
+  SKC_TRY(db.plan_r.ensure(npm * 8));
+  SKC_TRY(db.pband.ensure(npm * 8));
+  SKC_TRY(db.sweep_order.ensure(npm * 4));
+  SKC_TRY(db.seg_cnt.ensure(std::max<size_t>(db.h_segs.size(), 1) * 8));
+  SKC_TRY(db.band_off.ensure(((size_t)db.n_bands + 1) * 4));
+  const size_t nt = db.h_tasks_main.size() + db.h_tasks_temp.size();
+  SKC_TRY(db.tasks_sorted.ensure(std::max<size_t>(nt, 1) * sizeof(RowTask)));
+  SKC_TRY(db.task_next.ensure(32));
+  SKC_TRY(ctx->span_next.ensure(8));
+  {
+    // bucket sorts: a key per item, 1024 counts per block of 2048 items
+    const size_t items = std::max<size_t>(np, nt);
+    SKC_TRY(db.sort_keys.ensure(std::max<size_t>(items, 1) * 2));
+    SKC_TRY(db.sort_hist.ensure(((items + 2047) / 2048 + 1) * 1024 * 8));
+  }
+  if (!db.cap_sweep) db.cap_sweep = std::max(ctx->hint_sweep, GuessSweepBytes(hb));
+  if (!db.cap_rows) db.cap_rows = std::max(ctx->hint_rows, GuessRows(hb));
+  if (!db.cap_bins) db.cap_bins = std::max(ctx->hint_bins, GuessBins(hb, db.cfg.band_shift));
+  if (ctx->budget && (db.cap_sweep > ctx->budget || db.cap_rows * 8 > ctx->budget ||
+                      db.cap_bins * 4 > ctx->budget))
+    return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+  SKC_TRY(db.sweepmem.ensure(std::max<uint64_t>(db.cap_sweep, 16)));
+  SKC_TRY(db.rowspan.ensure(std::max<uint64_t>(db.cap_rows, 1) * sizeof(uint2)));
+  SKC_TRY(db.bins.ensure(std::max<uint64_t>(db.cap_bins, 1) * 4));
+  if (!ctx->span_pool.p) SKC_TRY(ctx->span_pool.ensure((uint64_t)(1 << 20) * sizeof(uint2)));
+
+  // zeroed bytewise (padding included): the replay test compares the bytes
+  std::memset(&b, 0, sizeof b);
+  std::memset(&q, 0, sizeof q);
+  b.verbs = db.verbs.as<uint8_t>();
+  b.pts = db.pts.as<P>();
+  b.weights = db.weights.as<float>();
+  b.draws = db.draws.as<DrawDesc>();
+  b.passes = db.passes.as<PassDesc>();
+  b.n_passes = np;
+  b.n_list = np;
+  b.canvases = db.canvases.as<CanvasDesc>();
+  b.scratch = db.scratch.as<uint8_t>();
+  b.geom = db.geom.as<PassGeom>();
+  b.sweep = db.sweep.as<PassSweep>();
+  b.sweepmem = db.sweepmem.as<uint8_t>();
+  b.rowspan = db.rowspan.as<uint2>();
+  b.pass_spans = db.pass_spans.as<uint32_t>();
+  b.pass_frags = db.pass_frags.as<unsigned long long>();
+  b.err = db.err.as<uint32_t>();
+  b.pass_class = db.pass_class.as<uint8_t>();
+  uint32_t maxw = 1;
+  for (const CanvasDesc& cd : hb.canvases) maxw = std::max(maxw, cd.w);
+  // accumulator entries of a register-sweep warp in shared memory: a path
+  // about as wide as its canvas fits (wider ones use their sweep memory)
+  b.reg_diff_cap = std::max<int32_t>(4, std::min<int32_t>(((int32_t)maxw + 132 + 3) & ~3, kRegDiffMax));
+  b.comp = db.comp.as<PassComp>();
+  b.band_off = db.band_off.as<uint32_t>();
+  b.bins = db.bins.as<uint32_t>();
+  b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
+  b.band_shift = db.cfg.band_shift;
+  b.task_next = db.task_next.as<unsigned int>();
+  b.sweep_done = db.task_next.as<unsigned int>() + 2;
+  b.spans = ctx->span_pool.as<uint2>();
+  b.span_cap = ctx->span_pool.cap / sizeof(uint2);
+  b.span_next = ctx->span_next.as<unsigned long long>();
+  b.any_general = 0;
+  for (const CanvasDesc& cd : hb.canvases) b.any_general |= cd.general;
+  b.brushes = db.brushes.as<Brush>();
+  b.conicals = db.conicals.as<ConicalParams>();
+  b.srgb_tables = db.srgb_tables.as<uint8_t>();
+  b.cf_matrices = db.cf_matrices.as<int16_t>();
+  b.stop_colors = db.stop_colors.as<float4>();
+  b.stop_offsets = db.stop_offsets.as<float>();
+  b.pixels = db.pixels.as<uint8_t>();
+  b.roundtrip = db.roundtrip.as<uint8_t>();
+  b.plan = db.plan_st.as<PlanStatus>();
+
+  q.st = db.plan_st.as<PlanStatus>();
+  q.a = db.plan_a.as<unsigned long long>();
+  q.r = db.plan_r.as<unsigned long long>();
+  q.pband = db.pband.as<uint2>();
+  q.segs = db.segs.as<BandSeg>();
+  q.n_segs = (uint32_t)db.h_segs.size();
+  q.seg_cnt = db.seg_cnt.as<unsigned long long>();
+  q.band_off = db.band_off.as<uint32_t>();
+  q.n_bands = db.n_bands;
+  q.bins = db.bins.as<uint32_t>();
+  q.sweep_cap = db.cap_sweep;
+  q.rows_cap = db.cap_rows;
+  q.bins_cap = db.cap_bins;
+  q.sweep_order = b.sweep_order ? db.sweep_order.as<uint32_t>() : nullptr;
+  q.tasks_in = db.tasks_in.as<RowTask>();
+  q.tasks_out = db.tasks_sorted.as<RowTask>();
+  q.n_main = (uint32_t)db.h_tasks_main.size();
+  q.n_temp = (uint32_t)db.h_tasks_temp.size();
+  q.sort_keys = db.sort_keys.as<uint16_t>();
+  q.sort_hist = db.sort_hist.as<unsigned long long>();
+  return SKITY_CUDA_SUCCESS;
+}
+
+// The launches of one device-planned render, in six parts (timed apart):
+// 0 clears, status reset and geometry; 1 the device plan; 2 the sweeps;
+// 3 composite of the blur temp canvases; 4 StackBlur; 5 composite of the
+// main canvases and the work totals.  Returns the number of kernel launches.
+static int EnqueueDevice(DeviceBatch& db, const DevBatch& b, const DevPlan& q, uint32_t num_sms,
+                         cudaStream_t s, int part) {
+  HostBatch& hb = db.hb;
+  switch (part) {
+    case 0:
+      if (!db.keep_pixels) {
+        for (uint32_t c : hb.main_canvases) {
+          const CanvasDesc& cd = hb.canvases[c];
+          if (!cd.has_clear)
+            cudaMemsetAsync(db.pixels.as<uint8_t>() + cd.px_off, 0, (size_t)cd.w * cd.h * 4, s);
+        }
+      }
+      cudaMemsetAsync(q.st, 0, sizeof(PlanStatus), s);
+      cudaMemsetAsync(b.err, 0, 16, s);
+      return LaunchGeometry(b, s);
+    case 1:
+      return LaunchPlan(b, q, s);
+    case 2:
+      cudaMemsetAsync(b.span_next, 0, 8, s);
+      cudaMemsetAsync(b.sweep_done, 0, 16, s);
+      return LaunchSweep(b, s);
+    case 3:
+      if (!q.n_temp) return 0;
+      cudaMemsetAsync(b.task_next, 0, 4, s);
+      return LaunchComposite(b, q.tasks_out + q.n_main, q.n_temp, db.chunk, db.cfg.ctas_per_sm,
+                             num_sms, b.task_next, s);
+    case 4:
+      if (!q.n_temp) return 0;
+      return LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
+                        hb.max_temp_h, hb.max_temp_w, s);
+    default: {
+      cudaMemsetAsync(b.task_next + 1, 0, 4, s);
+      int n = LaunchComposite(b, q.tasks_out, q.n_main, db.chunk, db.cfg.ctas_per_sm, num_sms,
+                              b.task_next + 1, s);
+      return n + LaunchPlanStats(b, q, s);
+    }
+  }
+}
+
+static void DropReplay(DeviceBatch& db);
+
+// Records the six parts of a device-planned render as replay graphs.
+static void CaptureDevice(skity_cuda_context_s* ctx, DeviceBatch& db, const DevBatch& b,
+                          const DevPlan& q) {
+  DropReplay(db);
+  cudaStream_t s = ctx->stream;
+  bool ok = true;
+  int launches = 0;
+  for (int part = 0; part < 6 && ok; ++part) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      ok = false;
+      break;
+    }
+    launches += EnqueueDevice(db, b, q, ctx->num_sms, s, part);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    size_t nodes = 0;
+    if (e != cudaSuccess || !g) {
+      ok = false;
+    } else if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess && nodes > 0) {
+      if (cudaGraphInstantiate(&db.graphs[part], g, 0) != cudaSuccess) {
+        db.graphs[part] = nullptr;
+        ok = false;
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+  }
+  cudaGetLastError();
+  if (!ok) {
+    DropReplay(db);
+    return;
+  }
+  db.graph_ok = true;
+  std::memcpy(&db.graph_b, &b, sizeof b);
+  std::memcpy(&db.graph_q, &q, sizeof q);
+  db.graph_launches = launches;
+}
+
+static double ElapsedMs(cudaEvent_t a, cudaEvent_t b);
+
+static int32_t DeviceRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
+  (void)timed;
+  cudaStream_t s = ctx->stream;
+  HostBatch& hb = db.hb;
+  const uint32_t np = (uint32_t)hb.passes.size();
+  skity_cuda_stats st{};
+  st.draws = hb.draw_count;
+  st.passes = np;
+  const uint64_t kMaxPool = 0xFFFFFFFFull;  // span indices are 32-bit
+  double discarded_ms = 0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    DevBatch b;
+    DevPlan q;
+    int32_t rc = PrepareDevice(ctx, db, b, q);
+    if (rc) return rc;
+    const bool replay = db.graph_ok && std::memcmp(&b, &db.graph_b, sizeof b) == 0 &&
+                        std::memcmp(&q, &db.graph_q, sizeof q) == 0;
+    int launches = 0;
+    SKC_TRY(cudaEventRecord(ctx->ev0, s));
+    for (int part = 0; part < 6; ++part) {
+      SKC_TRY(cudaEventRecord(ctx->stage[2 * part], s));
+      if (replay) {
+        if (db.graphs[part]) SKC_TRY(cudaGraphLaunch(db.graphs[part], s));
+      } else {
+        launches += EnqueueDevice(db, b, q, ctx->num_sms, s, part);
+      }
+      SKC_TRY(cudaEventRecord(ctx->stage[2 * part + 1], s));
+    }
+    SKC_TRY(cudaEventRecord(ctx->ev1, s));
+    SKC_TRY(cudaGetLastError());
+    PlanStatus ps;
+    uint32_t err = 0;
+    unsigned long long used = 0;
+    SKC_TRY(cudaMemcpyAsync(&ps, q.st, sizeof ps, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaMemcpyAsync(&err, b.err, 4, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaMemcpyAsync(&used, b.span_next, 8, cudaMemcpyDeviceToHost, s));
+    SKC_TRY(cudaStreamSynchronize(s));
+    st.host_syncs++;
+    if (err) {
+      std::fprintf(stderr, "skity_cuda: device self-check failed (code %u)\n", err);
+      return SKITY_CUDA_ERROR_DEVICE;
+    }
+    if (ps.flags == 0 && used <= b.span_cap) {
+      st.device_ms = ElapsedMs(ctx->ev0, ctx->ev1);
+      st.geometry_ms = ElapsedMs(ctx->stage[0], ctx->stage[1]);
+      st.plan_ms = ElapsedMs(ctx->stage[2], ctx->stage[3]);
+      st.sweep_emit_ms = ElapsedMs(ctx->stage[4], ctx->stage[5]);
+      st.composite_ms = ElapsedMs(ctx->stage[6], ctx->stage[7]) + ElapsedMs(ctx->stage[10], ctx->stage[11]);
+      st.blur_ms = ElapsedMs(ctx->stage[8], ctx->stage[9]);
+      st.sweep_count_ms = discarded_ms;
+      st.edges = ps.edges;
+      st.spans = ps.spans;
+      st.fragments = 0;
+      for (int k = 0; k < 4; ++k) {
+        st.fragments_by_brush[k] = ps.frags_by_brush[k];
+        st.fragments += ps.frags_by_brush[k];
+      }
+      for (uint32_t c : hb.main_canvases) st.pixels += (uint64_t)hb.canvases[c].w * hb.canvases[c].h;
+      st.graph_replays = replay ? 1 : 0;
+      st.kernel_launches = replay ? (uint64_t)db.graph_launches : (uint64_t)launches;
+      ctx->hint_sweep = std::max<uint64_t>(ctx->hint_sweep, ps.sweep_need);
+      ctx->hint_rows = std::max<uint64_t>(ctx->hint_rows, ps.rows_need);
+      ctx->hint_bins = std::max<uint64_t>(ctx->hint_bins, ps.bins_need);
+      db.stats = st;
+      if (!replay && db.want_graph) CaptureDevice(ctx, db, b, q);
+      return SKITY_CUDA_SUCCESS;
+    }
+    // grow what fell short and render again
+    DropReplay(db);
+    discarded_ms += ElapsedMs(ctx->ev0, ctx->ev1);
+    st.retries++;
+    if (ps.flags & kPlanGeomOverflow) {
+      db.h_geom.resize(np);
+      SKC_TRY(cudaMemcpy(db.h_geom.data(), db.geom.p, (size_t)np * sizeof(PassGeom),
+                         cudaMemcpyDeviceToHost));
+      for (uint32_t p = 0; p < np; ++p)
+        if (db.h_geom[p].status) GrowCaps(hb.passes[p], db.h_geom[p]);
+      db.slices_dirty = true;
+    }
+    if (ps.sweep_need > db.cap_sweep) db.cap_sweep = ps.sweep_need + ps.sweep_need / 8;
+    if (ps.rows_need > db.cap_rows) db.cap_rows = ps.rows_need + ps.rows_need / 8;
+    if (ps.bins_need > db.cap_bins) db.cap_bins = ps.bins_need + ps.bins_need / 8;
+    if (used > b.span_cap) {
+      if (used > kMaxPool) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+      const uint64_t grow = std::min<uint64_t>(used + used / 16, kMaxPool);
+      if (ctx->budget && grow * sizeof(uint2) > ctx->budget) return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+      ctx->span_pool.release();
+      SKC_TRY(ctx->span_pool.ensure(grow * sizeof(uint2)));
+    }
+  }
+  return SKITY_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+}
+
 // Render of a resident batch; pixels stay on the device.  A batch whose
 // replay graph is current re-renders with one graph launch; the graph's
 // device self-checks (error word, span pool use) are read back, and any
 // surprise falls back to a full planned render.
 int32_t RenderBatch(skity_cuda_context_s* ctx, DeviceBatch& db, bool timed) {
+  // batches without path clips are planned on the device
+  if (db.hb.clip_states.empty()) return DeviceRender(ctx, db, timed);
   if (db.graph_ok && db.planned_pool == ctx->span_pool.p) {
     cudaStream_t s = ctx->stream;
     static const int kStageEv[5][2] = {{0, 1}, {4, 5}, {6, 7}, {7, 8}, {8, 9}};
@@ -536,6 +884,17 @@ int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, u
   return SKITY_CUDA_SUCCESS;
 }
 
+int32_t QueueReadCanvases(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t count,
+                          uint8_t* const* out) {
+  if (count > db.hb.main_canvases.size()) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < count; ++i) {
+    const CanvasDesc& cd = db.hb.canvases[db.hb.main_canvases[i]];
+    SKC_TRY(cudaMemcpyAsync(out[i], db.pixels.as<uint8_t>() + cd.px_off, (size_t)cd.w * cd.h * 4,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  return SKITY_CUDA_SUCCESS;
+}
+
 }  // namespace skc
 
 // ---------------------------------------------------------------------------
@@ -677,17 +1036,20 @@ SKITY_CUDA_API int32_t skity_cuda_render_streams(skity_cuda_context ctx, uint32_
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
   auto t0 = std::chrono::steady_clock::now();
-  skc::DeviceBatch db;
+  if (!ctx->streams_batch) ctx->streams_batch = new (std::nothrow) skc::DeviceBatch();
+  if (!ctx->streams_batch) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  skc::DeviceBatch& db = *ctx->streams_batch;
+  db.Reset();
   int32_t rc = skc::BuildFromStreams(db, count, streams, stream_bytes);
   if (rc) return rc;
   rc = skc::UploadBatch(ctx, db);
   if (rc) return rc;
   rc = skc::RenderBatch(ctx, db, true);
   if (rc) return rc;
-  for (uint32_t i = 0; i < count; ++i) {
-    rc = skc::ReadCanvas(ctx, db, i, out_pixels[i], 0);
-    if (rc) return rc;
-  }
+  rc = skc::QueueReadCanvases(ctx, db, count, out_pixels);
+  if (rc) return rc;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return SKITY_CUDA_ERROR_DEVICE;
+  db.stats.host_syncs++;
   db.stats.total_ms =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   ctx->last = db.stats;
@@ -722,6 +1084,18 @@ SKITY_CUDA_API int32_t skity_cuda_batch_render(skity_cuda_batch batch) {
   cudaSetDevice(batch->ctx->device);
   auto t0 = std::chrono::steady_clock::now();
   int32_t rc = skc::RenderBatch(batch->ctx, batch->db, true);
+  batch->db.stats.total_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  batch->ctx->last = batch->db.stats;
+  return rc;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_batch_render_per_draw(skity_cuda_batch batch) {
+  if (!batch) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  std::lock_guard<std::mutex> lock(batch->ctx->mu);
+  cudaSetDevice(batch->ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  int32_t rc = skc::RenderPerDraw(batch->ctx, batch->db);
   batch->db.stats.total_ms =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   batch->ctx->last = batch->db.stats;

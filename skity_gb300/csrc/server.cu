@@ -6,8 +6,9 @@
 //
 // No counterpart in the reference (its software canvas renders one canvas
 // per host thread).  The pipeline per batch is the batch pipeline of
-// pipeline.cu: parse + upload (path and paint buffers resident on the device
-// for the batch's lifetime), planned render, pixel readback per request.
+// pipeline.cu: parse + upload into the worker's resident buffers, a render
+// planned on the device (one wait on the device per batch, at the end), the
+// pixels of every request read back together.
 //
 // Admission: a request's footprint is estimated when it is submitted
 // (RequestFootprint below); a batch takes requests in arrival order while
@@ -75,6 +76,11 @@ namespace skc {
 namespace {
 
 void WorkerLoop(skity_cuda_server_s* sv, skity_cuda_context ctx) {
+  // The worker's batch: rebuilt for every batch of requests, its device
+  // buffers (paths, paints, geometry scratch, sweep memory, row tables,
+  // bins, canvases) kept resident and reused, so a batch allocates only
+  // when it outgrows every batch before it.
+  DeviceBatch db;
   for (;;) {
     std::vector<std::shared_ptr<Request>> batch;
     uint64_t fp = 0;
@@ -98,20 +104,21 @@ void WorkerLoop(skity_cuda_server_s* sv, skity_cuda_context ctx) {
     {
       std::lock_guard<std::mutex> clk(ctx->mu);
       cudaSetDevice(ctx->device);
-      DeviceBatch db;
+      db.Reset();
       std::vector<const uint8_t*> ptrs;
       std::vector<size_t> lens;
+      std::vector<uint8_t*> outs;
       for (auto& r : batch) {
         ptrs.push_back(r->stream.data());
         lens.push_back(r->stream.size());
+        r->pixels.resize((size_t)r->w * r->h * 4);
+        outs.push_back(r->pixels.data());
       }
       rc = BuildFromStreams(db, (uint32_t)batch.size(), ptrs.data(), lens.data());
       if (!rc) rc = UploadBatch(ctx, db);
       if (!rc) rc = RenderBatch(ctx, db, true);
-      for (size_t i = 0; i < batch.size() && !rc; ++i) {
-        batch[i]->pixels.resize((size_t)batch[i]->w * batch[i]->h * 4);
-        rc = ReadCanvas(ctx, db, (uint32_t)i, batch[i]->pixels.data(), 0);
-      }
+      if (!rc) rc = QueueReadCanvases(ctx, db, (uint32_t)batch.size(), outs.data());
+      if (!rc && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = SKITY_CUDA_ERROR_DEVICE;
       if (!rc) ctx->last = db.stats;
     }
     const double t1 = NowS();

@@ -10,7 +10,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("SKITY_REFERENCE", "/root/reference")
 
 
 @pytest.fixture(scope="module")
