@@ -515,6 +515,18 @@ def run_reference(args, rank, world):
     return 0
 
 
+def workload_scenes(args):
+    """The timed workload: the 256-canvas batch (or its first --canvases);
+    --workload picks one of the single-canvas scenes instead, cut to its
+    first --paths draws -- small cases for profiling single kernels."""
+    if args.workload == "config3":
+        scenes = load_config3()
+        return scenes[:args.canvases] if args.canvases else scenes
+    from skity_gb300 import scene as S
+    sc = {"config1": S.config1, "config2": load_config2, "config4": load_config4}[args.workload]()
+    return [sc.subset(0, args.paths) if args.paths else sc]
+
+
 def run_gpu(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -524,9 +536,7 @@ def run_gpu(args, rank, world, local):
     from skity_gb300 import autotune
     from skity_gb300.canvas import Batch, Context
 
-    scenes = load_config3()
-    if args.canvases:
-        scenes = scenes[:args.canvases]
+    scenes = workload_scenes(args)
     paths = sum(sc.n_draws for sc in scenes)
     pix = sum(sc.width * sc.height for sc in scenes)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -657,6 +667,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--canvases", type=int, default=0,
                     help="render only the first N canvases (small profiling case)")
+    ap.add_argument("--workload", default="config3",
+                    choices=["config3", "config1", "config2", "config4"],
+                    help="profiling: time one of the single-canvas scenes instead of the batch")
+    ap.add_argument("--paths", type=int, default=0,
+                    help="profiling: the first N draws of a single-canvas --workload")
     ap.add_argument("--ref-canvases", type=int, default=0,
                     help="reference arm: the first N canvases per step (default all)")
     ap.add_argument("--no-tune", action="store_true", help="default raster config, no autotuning")

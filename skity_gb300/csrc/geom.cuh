@@ -91,8 +91,30 @@ SKC_HD Fixed FixedMul(Fixed a, Fixed b) { return (Fixed)(((int64_t)a * b) >> 16)
 SKC_HD Fixed FDot6ToFixed(FDot6 x) { return (Fixed)((uint32_t)x << 10); }
 SKC_HD int32_t LShift(int32_t v, int s) { return (int32_t)((uint32_t)v << s); }
 SKC_HD Fixed FDot6ToFixedDiv2(FDot6 v) { return LShift(v, 16 - 6 - 1); }
-SKC_HD Fixed FixedDiv(int32_t numer, int32_t denom) {
+// (numer << 16) / denom in 64 bits, truncated toward zero, clamped to
+// [kMinS32, kMaxS32] (the reference's SkFixed-style FixedDiv).
+SKC_HD Fixed FixedDivWide(int32_t numer, int32_t denom) {
   int64_t q = (int64_t)((uint64_t)(int64_t)numer << 16) / denom;
+  if (q < kMinS32) q = kMinS32;
+  if (q > kMaxS32) q = kMaxS32;
+  return (Fixed)q;
+}
+// The same quotient without a 64-bit division (which the GPU runs as a long
+// called routine): for |denom| < 2^24, floor(|numer| 2^16 / |denom|) is
+// built from three 32-bit divisions giving 16 + 8 + 8 quotient bits
+// (a = q1 b + r1, 2^8 r1 = q2 b + r2, 2^8 r2 = q3 b + r3, so the quotient
+// is q1 2^16 + q2 2^8 + q3 and every partial dividend stays below 2^32),
+// then signed as C's division truncates; larger divisors take the 64-bit
+// path.  Equal to FixedDivWide for every input with denom != 0.
+SKC_HD Fixed FixedDiv(int32_t numer, int32_t denom) {
+  const uint32_t a = numer < 0 ? 0u - (uint32_t)numer : (uint32_t)numer;
+  const uint32_t b = denom < 0 ? 0u - (uint32_t)denom : (uint32_t)denom;
+  if (b >= (1u << 24)) return FixedDivWide(numer, denom);
+  const uint32_t q1 = a / b, r1 = a - q1 * b;
+  const uint32_t t2 = r1 << 8, q2 = t2 / b, r2 = t2 - q2 * b;
+  const uint32_t q3 = (r2 << 8) / b;
+  const uint64_t u = ((uint64_t)q1 << 16) + ((uint64_t)q2 << 8) + q3;
+  int64_t q = ((numer < 0) != (denom < 0)) ? -(int64_t)u : (int64_t)u;
   if (q < kMinS32) q = kMinS32;
   if (q > kMaxS32) q = kMaxS32;
   return (Fixed)q;

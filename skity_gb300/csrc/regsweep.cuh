@@ -5,8 +5,9 @@
 // arrays lives on chip:
 //   * list position p of the active list is slot p / 32 of lane p % 32; a
 //     slot holds the edge's index, x, dx, dy, lower_y, winding and curve
-//     count in registers (the quad-piece state stays in the pass's edge
-//     copy in global memory and is touched only when a piece ends);
+//     count in registers, and in the 32-edge form its quad-piece state too
+//     (the larger forms keep that in the pass's edge copy in global memory,
+//     touched only when a piece ends);
 //   * the per-position values an interval reads (x before the step, after
 //     GoY and after the update, dx, dy) and the interval endpoints are
 //     exchanged through a per-warp shared-memory block;
@@ -56,6 +57,40 @@ struct TrapRowSoA {
   }
 };
 
+// The quad-piece state of an active edge that UpdateQuad reads besides the
+// edge's line (x, dx, dy, lower_y, winding, curve count): forward-difference
+// position, steps and second differences, the last point, the shift.  The
+// 32-edge form holds it in registers beside the rest of the edge (one slot
+// per lane), so a piece change is a register update; the larger forms, with
+// two or four slots per lane, keep it in the pass's edge copy in memory.
+constexpr int kRegQuadWords = 9;
+SKC_HD constexpr bool RegQuadHeld(int M) { return M == 32; }
+struct RegQuad {
+  int32_t w[kRegQuadWords];  // qx, qy, qdx, qdy, qddx, qddy, q_last_x, q_last_y, curve_shift
+  SKC_HD void load(const Edge& e) {
+    w[0] = e.qx;
+    w[1] = e.qy;
+    w[2] = e.qdx;
+    w[3] = e.qdy;
+    w[4] = e.qddx;
+    w[5] = e.qddy;
+    w[6] = e.q_last_x;
+    w[7] = e.q_last_y;
+    w[8] = e.curve_shift;
+  }
+  SKC_HD void put(Edge& e) const {
+    e.qx = w[0];
+    e.qy = w[1];
+    e.qdx = w[2];
+    e.qdy = w[3];
+    e.qddx = w[4];
+    e.qddy = w[5];
+    e.q_last_x = w[6];
+    e.q_last_y = w[7];
+    e.curve_shift = (uint8_t)w[8];
+  }
+};
+
 // Per-warp shared block of the register sweep for active lists of up to
 // M edges.
 template <int M>
@@ -74,6 +109,9 @@ struct RegSharedT {
   // edge state by new list position (reorder and insertion)
   int32_t p_idx[M], p_x[M], p_dx[M], p_dy[M];
   int32_t p_low[M], p_wc[M];
+  // the quad-piece state of the edges (RegQuad) by new list position, for
+  // the forms that keep it in registers
+  int32_t p_q[RegQuadHeld(M) ? kRegQuadWords : 1][M];
   union {
     struct {
       // the step's intervals (blit_trapezoid_row set-ups) and their first span
@@ -310,6 +348,8 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
   constexpr unsigned kFull = NL == 32 ? 0xffffffffu : 1u;
   const int winding_mask = even_odd ? 1 : -1;
   int32_t r_idx[S], r_x[S], r_dx[S], r_dy[S], r_low[S], r_wc[S];
+  constexpr bool kQ = RegQuadHeld(M);
+  RegQuad r_q[kQ ? S : 1];
 
   BlitPending pend;
   pend.n = pend.total = 0;
@@ -335,6 +375,7 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
       if (p < m) {
         Edge e = W[p];
         GoY(&e, y);
+        if (kQ) r_q[s].load(e);
         r_idx[s] = p;
         r_x[s] = e.x;
         r_dx[s] = e.dx;
@@ -387,7 +428,12 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           int32_t x = wadd(xo, dxo >> y_shift);  // GoYShift
           const int32_t xg = x;
           if (SKC_COLD(r_low[s] <= next_y && WcCount(r_wc[s]) > 0)) {
-            Edge e = W[r_idx[s]];
+            Edge e;
+            if (kQ) {
+              r_q[s].put(e);
+            } else {
+              e = W[r_idx[s]];
+            }
             e.x = x;
             e.y = next_y;
             e.dx = dxo;
@@ -400,7 +446,11 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
               e.snapped_y = e.y;
               if (!UpdateQuad(&e)) break;
             }
-            W[r_idx[s]] = e;
+            if (kQ) {
+              r_q[s].load(e);
+            } else {
+              W[r_idx[s]] = e;
+            }
             x = e.x;
             r_dx[s] = e.dx;
             r_dy[s] = e.dy;
@@ -568,6 +618,10 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           sh.p_dy[r] = r_dy[s];
           sh.p_low[r] = r_low[s];
           sh.p_wc[r] = r_wc[s];
+          if (kQ) {
+#pragma unroll
+            for (int j = 0; j < kRegQuadWords; ++j) sh.p_q[j][r] = r_q[s].w[j];
+          }
         }
       }
       L.sync();
@@ -581,6 +635,10 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           r_dy[s] = sh.p_dy[p];
           r_low[s] = sh.p_low[p];
           r_wc[s] = sh.p_wc[p];
+          if (kQ) {
+#pragma unroll
+            for (int j = 0; j < kRegQuadWords; ++j) r_q[s].w[j] = sh.p_q[j][p];
+          }
         }
       }
       L.sync();
@@ -622,6 +680,10 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           sh.p_dy[np] = r_dy[s];
           sh.p_low[np] = r_low[s];
           sh.p_wc[np] = r_wc[s];
+          if (kQ) {
+#pragma unroll
+            for (int j = 0; j < kRegQuadWords; ++j) sh.p_q[j][np] = r_q[s].w[j];
+          }
         }
       }
       L.sync();
@@ -643,6 +705,12 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           sh.p_dy[np] = e.dy;
           sh.p_low[np] = e.lower_y;
           sh.p_wc[np] = MakeWc(e.winding, e.curve_count);
+          if (kQ) {
+            RegQuad q;
+            q.load(e);
+#pragma unroll
+            for (int j = 0; j < kRegQuadWords; ++j) sh.p_q[j][np] = q.w[j];
+          }
           if (e.lower_y > y) lmin2 = min_(lmin2, e.lower_y);
         }
       }
@@ -659,6 +727,10 @@ SKC_HD int RegWalk(const Lanes& L, RegSharedT<M>& sh, Edge* W, int n, Sink* sink
           r_dy[s] = sh.p_dy[p];
           r_low[s] = sh.p_low[p];
           r_wc[s] = sh.p_wc[p];
+          if (kQ) {
+#pragma unroll
+            for (int j = 0; j < kRegQuadWords; ++j) r_q[s].w[j] = sh.p_q[j][p];
+          }
           if (r_idx[s] >= k && p > 0 &&
               wadd(sh.p_x[p - 1], sh.p_dx[p - 1]) > wadd(r_x[s], r_dx[s]))
             cross2 = true;

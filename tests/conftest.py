@@ -46,6 +46,8 @@ def cpu_pipeline():
                                         ctypes.c_uint64]
     lib.skc_cpu_introsort.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     lib.skc_std_sort.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    lib.skc_cpu_fixed_div_check.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    lib.skc_cpu_fixed_div_check.restype = ctypes.c_int64
     return lib
 
 

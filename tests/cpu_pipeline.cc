@@ -252,3 +252,12 @@ extern "C" void skc_std_sort(const int32_t* keys, int32_t* idx, int n) {
   for (int i = 0; i < n; ++i) idx[i] = i;
   std::sort(idx, idx + n, [&](int32_t a, int32_t b) { return keys[a] < keys[b]; });
 }
+
+// FixedDiv (three 32-bit divisions) against the 64-bit quotient on n
+// numerator / denominator pairs; returns the number of mismatches.
+extern "C" int64_t skc_cpu_fixed_div_check(const int32_t* numer, const int32_t* denom, int64_t n) {
+  int64_t bad = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (denom[i] != 0 && FixedDiv(numer[i], denom[i]) != FixedDivWide(numer[i], denom[i])) ++bad;
+  return bad;
+}

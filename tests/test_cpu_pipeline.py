@@ -212,3 +212,23 @@ def test_clip_path_cases_bit_exact(cpu_pipeline, oracle_lib):
     ref, _ = oracle_lib.render(sc)
     c = oracle_lib.compare(got, ref)
     assert c["bad_pixels"] == 0, c
+
+
+def test_fixed_div_matches_64bit_quotient(cpu_pipeline):
+    """The device FixedDiv (three 32-bit divisions for divisors below 2^24)
+    against the 64-bit truncated quotient: random pairs over every magnitude,
+    the extremes, and the small FDot6 values the raster divides most."""
+    rng = np.random.default_rng(7)
+    n = 2_000_000
+    mags = rng.integers(0, 32, size=n)
+    numer = (rng.integers(0, 2**31, size=n, dtype=np.int64) >> (31 - mags)).astype(np.int64)
+    numer *= np.where(rng.random(n) < 0.5, -1, 1)
+    dm = rng.integers(0, 32, size=n)
+    denom = (rng.integers(1, 2**31, size=n, dtype=np.int64) >> (31 - dm)).astype(np.int64)
+    denom = np.maximum(denom, 1) * np.where(rng.random(n) < 0.5, -1, 1)
+    edge = np.array([-2**31, 2**31 - 1, 0, 1, -1, 2**24 - 1, 2**24, -(2**24) + 1], np.int64)
+    en, ed = np.meshgrid(edge, np.array([1, -1, 2, 3, 2**24 - 1, -(2**24 - 1), 2**24, 2**31 - 1,
+                                         -2**31, 16, -64], np.int64))
+    numer = np.concatenate([numer, en.ravel()]).astype(np.int32)
+    denom = np.concatenate([denom, ed.ravel()]).astype(np.int32)
+    assert cpu_pipeline.skc_cpu_fixed_div_check(numer.ctypes.data, denom.ctypes.data, len(numer)) == 0
