@@ -258,6 +258,19 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canva
  * clip returns SKITY_CUDA_ERROR_NOT_SUPPORTED at flush. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
                                                    const skity_cuda_path* path, uint32_t op);
+/* Canvas::SaveLayer(bounds, paint) (canvas.hpp; canvas.cc:255-276;
+ * SWCanvas::OnSaveLayer / OnLayerRestore, sw_canvas.cc:441-484, 891-902):
+ * a Save whose matching Restore draws the layer -- every draw made in
+ * between, rendered into a transparent bitmap over the layer's device
+ * bounds -- onto the canvas with the paint's alpha and blend mode (paint
+ * NULL: Paint()).  `bounds` is (left, top, right, bottom) in local
+ * coordinates; empty bounds, or bounds outside the global clip bounds, save
+ * no layer (a Save with an empty clip, as the reference does).  One level of
+ * layers: a SaveLayer inside a layer, a layer paint with a mask or colour
+ * filter, a blurred draw or a path clip inside a layer, and a flush while a
+ * layer is open return SKITY_CUDA_ERROR_NOT_SUPPORTED. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, const float bounds[4],
+                                                    const skity_cuda_paint* paint);
 /* Canvas::Flush: renders the recorded draws on the GPU and writes the
  * bitmap's pixels. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas);
@@ -386,6 +399,35 @@ SKITY_CUDA_API int32_t skity_cuda_draw_path_static(int32_t device, uint8_t* devi
                                                    const skity_cuda_path* path,
                                                    const skity_cuda_paint* paint,
                                                    void* stream);
+
+/* ---- PictureRecorder / DisplayList -------------------------------------------
+ * The reference's recorder (include/skity/recorder/picture_recorder.hpp,
+ * display_list.hpp; C API module/capi/include/skity_c/skity_recorder.h):
+ * skity_cuda_recorder_begin returns a canvas (of the recording's size) whose
+ * calls -- clear, draw_path, draw_image_rect, save, restore, save_layer,
+ * translate, clip_rect, clip_path -- are recorded instead of drawn, with
+ * their paths, paints, shaders and images copied; flush on it does nothing.
+ * skity_cuda_recorder_finish hands the recorded ops to a display list and
+ * leaves the recorder empty (destroy it with skity_cuda_canvas_destroy).
+ * skity_cuda_display_list_draw replays the ops, in order, through a canvas's
+ * own calls (DisplayList::Draw, src/recorder/display_list.cc:330-343): the
+ * canvas's current matrix and clips apply, and the first failing call's
+ * code is returned after every op has been replayed.
+ * skity_cuda_display_list_to_stream writes the display list as a scene
+ * stream, the input of skity_cuda_render_streams, skity_cuda_batch_create
+ * and skity_cuda_server_submit (out NULL: *size receives the byte count). */
+typedef struct skity_cuda_display_list_s* skity_cuda_display_list;
+
+SKITY_CUDA_API int32_t skity_cuda_recorder_begin(uint32_t width, uint32_t height,
+                                                 skity_cuda_canvas* out);
+SKITY_CUDA_API int32_t skity_cuda_recorder_finish(skity_cuda_canvas recorder,
+                                                  skity_cuda_display_list* out);
+SKITY_CUDA_API void skity_cuda_display_list_destroy(skity_cuda_display_list list);
+SKITY_CUDA_API uint32_t skity_cuda_display_list_op_count(skity_cuda_display_list list);
+SKITY_CUDA_API int32_t skity_cuda_display_list_draw(skity_cuda_display_list list,
+                                                    skity_cuda_canvas canvas);
+SKITY_CUDA_API int32_t skity_cuda_display_list_to_stream(skity_cuda_display_list list, uint8_t* out,
+                                                         size_t* size);
 
 /* Library version string. */
 SKITY_CUDA_API const char* skity_cuda_version(void);

@@ -70,6 +70,13 @@ struct Scene {
   std::vector<uint8_t> clip_verbs;
   std::vector<float> clip_pts, clip_wts;
   std::vector<uint32_t> draw_clip_state;  // per draw, 1-based (0: none)
+  struct Layer {  // Canvas::SaveLayer ... Restore around draws [start, restore)
+    float bounds[4], translate[2], clip[4];
+    uint32_t start, restore;
+    float alpha;
+    uint32_t blend, pad[2];
+  };
+  std::vector<Layer> layers;
 };
 
 template <typename T>
@@ -130,6 +137,23 @@ bool Load(const char* path, Scene* s) {
     Take(buf, o, s->clip_pts, 2 * tp);
     Take(buf, o, s->clip_wts, tw);
     Take(buf, o, s->draw_clip_state, nd);
+  }
+  if (flags & 8) {  // images: not replayed here, skipped
+    uint32_t n_images = 0;
+    if (o + 4 > buf.size()) return false;
+    std::memcpy(&n_images, buf.data() + o, 4);
+    o += 4 + 24 * size_t(n_images);
+    uint64_t nb = 0;
+    if (o + 8 > buf.size()) return false;
+    std::memcpy(&nb, buf.data() + o, 8);
+    o += 8 + nb + (4 - nb % 4) % 4 + 80 * size_t(nd);
+  }
+  if (flags & 16) {
+    uint32_t n_layers = 0;
+    if (o + 4 > buf.size()) return false;
+    std::memcpy(&n_layers, buf.data() + o, 4);
+    o += 4;
+    Take(buf, o, s->layers, n_layers);
   }
   return o <= buf.size();
 }
@@ -307,7 +331,42 @@ int main(int argc, char** argv) {
   if (s.has_clear) {
     canvas->Clear(skity::Color4f{s.clear[0], s.clear[1], s.clear[2], s.clear[3]});
   }
+  // Layers: SaveLayer under the translation and clip bounds recorded for
+  // it, the translation then undone, so the draws inside replay as outside;
+  // Restore composites the layer.
+  size_t li = 0;
+  while (li < s.layers.size() && s.layers[li].start < first) ++li;
+  const Scene::Layer* open_layer = nullptr;
+  auto layer_events = [&](uint32_t d) {
+    if (open_layer && open_layer->restore == d) {
+      canvas->Restore();  // the layer
+      canvas->Restore();  // the Save around it
+      open_layer = nullptr;
+    }
+    while (!open_layer && li < s.layers.size() && s.layers[li].start == d) {
+      const Scene::Layer& L = s.layers[li++];
+      canvas->Save();
+      const bool lclipped = !(L.clip[0] == -1e9f && L.clip[1] == -1e9f && L.clip[2] == 1e9f &&
+                              L.clip[3] == 1e9f);
+      if (lclipped) canvas->ClipRect(skity::Rect::MakeLTRB(L.clip[0], L.clip[1], L.clip[2], L.clip[3]));
+      const bool lmoved = L.translate[0] != 0.f || L.translate[1] != 0.f;
+      if (lmoved) canvas->Translate(L.translate[0], L.translate[1]);
+      skity::Paint lp;
+      lp.SetAlphaF(L.alpha);
+      lp.SetBlendMode(static_cast<skity::BlendMode>(L.blend));
+      canvas->SaveLayer(skity::Rect::MakeLTRB(L.bounds[0], L.bounds[1], L.bounds[2], L.bounds[3]),
+                        lp);
+      if (lmoved) canvas->Translate(-L.translate[0], -L.translate[1]);
+      open_layer = &L;
+      if (L.restore == d) {
+        canvas->Restore();
+        canvas->Restore();
+        open_layer = nullptr;
+      }
+    }
+  };
   for (size_t i = 0; i < paths.size(); ++i) {
+    layer_events(first + uint32_t(i));
     const PaintRec& pr = s.paints[first + i];
     const bool moved = pr.translate[0] != 0.f || pr.translate[1] != 0.f;
     const float* c = s.clips.empty() ? nullptr : s.clips.data() + 4 * (first + i);
@@ -323,6 +382,7 @@ int main(int argc, char** argv) {
     canvas->DrawPath(paths[i], paints[i]);
     if (moved || clipped || cstate) canvas->Restore();
   }
+  layer_events(last);
   canvas->Flush();
   auto t1 = std::chrono::steady_clock::now();
   if (timed) {

@@ -1927,6 +1927,16 @@ struct SceneView {
   const ImageRec* images = nullptr;
   const uint8_t* image_pixels = nullptr;
   const ImageShaderRec* image_shaders = nullptr;
+  // layers (header flag 16): Canvas::SaveLayer ... Restore, draws
+  // [start, restore) inside (restore 0xFFFFFFFF: never restored)
+  struct LayerRec {
+    float bounds[4], translate[2], clip[4];
+    uint32_t start, restore;
+    float alpha;
+    uint32_t blend, pad[2];
+  };
+  uint32_t n_layers = 0;
+  const LayerRec* layers = nullptr;
 };
 
 // The colour filter of the draw whose paint record is `p` (a record of s).
@@ -1957,7 +1967,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->has_clear = hdr[3];
   // 1: per-draw clip bounds, 2: per-draw colour filters, 4: path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~15u) return false;
+  if (flags & ~31u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -2017,6 +2027,20 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
     s->image_shaders =
         (const SceneView::ImageShaderRec*)at(sizeof(SceneView::ImageShaderRec) * (size_t)s->nd);
   }
+  if (flags & 16) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_layers, buf + o, 4);
+    o += 4;
+    s->layers = (const SceneView::LayerRec*)at(sizeof(SceneView::LayerRec) * (size_t)s->n_layers);
+    if (o > len) return false;
+    // one level: in start order, each restored before the next starts
+    for (uint32_t i = 0; i < s->n_layers; ++i) {
+      const SceneView::LayerRec& L = s->layers[i];
+      const bool open = L.restore == 0xFFFFFFFFu;
+      if (L.start > s->nd || (!open && (L.restore < L.start || L.restore > s->nd))) return false;
+      if (i + 1 < s->n_layers && (open || s->layers[i + 1].start < L.restore)) return false;
+    }
+  }
   return o <= len;
 }
 
@@ -2024,6 +2048,13 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
 // image draw under a clip are not restated here (the GPU path refuses the
 // same draws).
 static bool BlurUnderClip(const SceneView& s) {
+  for (uint32_t i = 0; i < s.n_layers; ++i) {
+    const uint32_t end = s.layers[i].restore == 0xFFFFFFFFu ? s.nd : s.layers[i].restore;
+    for (uint32_t d = s.layers[i].start; d < end; ++d)
+      if ((s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f) ||
+          (s.draw_clip_state && s.draw_clip_state[d] != 0))
+        return true;
+  }
   for (uint32_t d = 0; d < s.nd && s.clips; ++d) {
     const Clip c = ClipOf(s, d);
     const bool narrowed = !(c.l == -1e9f && c.t == -1e9f && c.r == 1e9f && c.b == 1e9f);
@@ -2377,19 +2408,8 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
     std::memset(out_rgba, 0, (size_t)t.w * t.h * 4);
   }
   Stats st;
-  std::vector<Span> spans;
   uint32_t last = std::min<uint32_t>(s.nd, first + count);
-  for (uint32_t d = first; d < last; ++d) {
-    if (s.paints[d].blur_style != 0) {
-      HandleBlurFilter(s, d, &t, &st);
-    } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
-      // Canvas::Translate then DrawPath: the CTM reaches RastePath and the brush
-      DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
-                         s.paints[d].translate[1], ClipOf(s, d), &t, &st);
-    } else {
-      DrawPath(s, d, &t, &st, &spans);
-    }
-  }
+  ReplayDraws(s, first, last, &t, &st);
   auto t1 = std::chrono::steady_clock::now();
   if (stats) {
     stats->fragments = st.fragments;
@@ -2429,17 +2449,7 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
       uint32_t c = s.has_clear ? ColorToPMColor(Color4fToColor(s.clear)) : 0;
       for (int y = t.band0; y < t.band1; ++y)
         for (int x = 0; x < t.w; ++x) t.Set(x, y, c);
-      std::vector<Span> spans;
-      for (uint32_t d = first; d < last; ++d) {
-        if (s.paints[d].blur_style != 0) {
-          HandleBlurFilter(s, d, &t, &st[k]);
-        } else if (s.paints[d].translate[0] != 0.f || s.paints[d].translate[1] != 0.f) {
-          DrawPathTranslated(s, BuildPath(s, d), s.paints[d], s.paints[d].translate[0],
-                             s.paints[d].translate[1], ClipOf(s, d), &t, &st[k]);
-        } else {
-          DrawPath(s, d, &t, &st[k], &spans);
-        }
-      }
+      ReplayDraws(s, first, last, &t, &st[k]);
     });
   }
   for (auto& th : pool) th.join();

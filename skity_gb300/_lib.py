@@ -138,6 +138,16 @@ SIGNATURES = {
                                                  ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_vp)]),
     "skity_cuda_batch_render": (ctypes.c_int32, [_vp]),
     "skity_cuda_batch_render_per_draw": (ctypes.c_int32, [_vp]),
+    "skity_cuda_canvas_save_layer": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float),
+                                                      ctypes.POINTER(Paint_)]),
+    "skity_cuda_recorder_begin": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32,
+                                                   ctypes.POINTER(_vp)]),
+    "skity_cuda_recorder_finish": (ctypes.c_int32, [_vp, ctypes.POINTER(_vp)]),
+    "skity_cuda_display_list_destroy": (None, [_vp]),
+    "skity_cuda_display_list_op_count": (ctypes.c_uint32, [_vp]),
+    "skity_cuda_display_list_draw": (ctypes.c_int32, [_vp, _vp]),
+    "skity_cuda_display_list_to_stream": (ctypes.c_int32, [_vp, _vp,
+                                                           ctypes.POINTER(ctypes.c_size_t)]),
     "skity_cuda_batch_read": (ctypes.c_int32, [_vp, ctypes.c_uint32, _vp]),
     "skity_cuda_batch_destroy": (None, [_vp]),
     "skity_cuda_context_set_config": (ctypes.c_int32, [_vp, ctypes.POINTER(RasterConfig_)]),

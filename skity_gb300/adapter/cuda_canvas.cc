@@ -208,17 +208,105 @@ static void PathStorage(const Path& path, std::vector<uint8_t>* verbs, std::vect
   p->fill_type = path.GetFillType() == Path::PathFillType::kEvenOdd ? 1u : 0u;
 }
 
-void CUDACanvas::OnSaveLayer(const Rect&, const Paint&) {
-  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+// Canvas::SaveLayer has saved the level and narrowed the global clip bounds
+// by the bounds (canvas.cc:255-276); the C-ABI canvas gets a level with
+// those clip bounds and the translation, then the layer, then the
+// translation undone (draws carry their own).  Restore pops both levels:
+// the inner one composites the layer.
+void CUDACanvas::OnSaveLayer(const Rect& bounds, const Paint& paint) {
+  float tx = 0.f, ty = 0.f;
+  bad_clip_.push_back(bad_clip_.back());
+  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+    saves_.push_back(1);
+    skity_cuda_canvas_save(canvas_);
+    bad_clip_.back() = true;
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  skity_cuda_canvas_save(canvas_);
+  const Rect& g = GetGlobalClipBounds();
+  if (!(g.Left() == -1e9f && g.Top() == -1e9f && g.Right() == 1e9f && g.Bottom() == 1e9f))
+    skity_cuda_canvas_clip_rect(canvas_, g.Left(), g.Top(), g.Right(), g.Bottom());
+  const bool moved = tx != 0.f || ty != 0.f;
+  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  skity_cuda_paint q{};
+  q.style = static_cast<uint32_t>(paint.GetStyle());
+  q.blend_mode = static_cast<uint32_t>(paint.GetBlendMode());
+  const Vector fc = paint.GetFillColor(), sc = paint.GetStrokeColor();
+  const float fill[4] = {fc.x, fc.y, fc.z, fc.w}, stroke[4] = {sc.x, sc.y, sc.z, sc.w};
+  std::memcpy(q.fill_color, fill, sizeof fill);
+  std::memcpy(q.stroke_color, stroke, sizeof stroke);
+  q.stroke_width = 1.f;
+  q.miter_limit = 4.f;
+  if (paint.GetMaskFilter() || paint.GetColorFilter()) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    bad_clip_.back() = true;
+  } else {
+    const float b[4] = {bounds.Left(), bounds.Top(), bounds.Right(), bounds.Bottom()};
+    status_ = skity_cuda_canvas_save_layer(canvas_, b, &q);
+  }
+  if (status_ != SKITY_CUDA_SUCCESS) {
+    if (moved) skity_cuda_canvas_translate(canvas_, -tx, -ty);
+    saves_.push_back(1);
+    bad_clip_.back() = true;
+    return;
+  }
+  if (moved) skity_cuda_canvas_translate(canvas_, -tx, -ty);
+  saves_.push_back(2);
 }
 
 void CUDACanvas::OnDrawBlob(const TextBlob*, float, float, Paint const&) {
   status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
 }
 
-void CUDACanvas::OnDrawImageRect(std::shared_ptr<Image>, const Rect&, const Rect&,
-                                 const SamplingOptions&, Paint const*) {
-  status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+// Canvas::DrawImageRect / DrawImage of a pixmap image (SWCanvas::
+// OnDrawImageRect, sw_canvas.cc:641-677) under a translation: the pixels,
+// src / dst and the paint's alpha and blend mode go to the C-ABI canvas.
+void CUDACanvas::OnDrawImageRect(std::shared_ptr<Image> image, const Rect& src, const Rect& dst,
+                                 const SamplingOptions& sampling, Paint const* paint) {
+  float tx = 0.f, ty = 0.f;
+  if (bad_clip_.back() || !TranslationOf(GetTotalMatrix(), &tx, &ty) || !image) {
+    status_ = image ? SKITY_CUDA_ERROR_NOT_SUPPORTED : SKITY_CUDA_SUCCESS;
+    return;
+  }
+  const std::shared_ptr<Pixmap>* pm = image->GetPixmap();
+  if (!pm || !*pm || (paint && (paint->GetShader() || paint->GetMaskFilter() ||
+                                paint->GetColorFilter()))) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    return;
+  }
+  const Pixmap& px = **pm;
+  skity_cuda_image im{};
+  im.width = static_cast<uint32_t>(px.Width());
+  im.height = static_cast<uint32_t>(px.Height());
+  im.alpha_type = static_cast<uint32_t>(px.GetAlphaType());
+  im.pixels = px.Addr();
+  skity_cuda_paint q{};
+  q.blend_mode = 3;
+  q.fill_color[3] = q.stroke_color[3] = 1.f;
+  q.stroke_width = 1.f;
+  q.miter_limit = 4.f;
+  if (paint) {
+    q.style = static_cast<uint32_t>(paint->GetStyle());
+    q.blend_mode = static_cast<uint32_t>(paint->GetBlendMode());
+    const Vector fc = paint->GetFillColor(), sc = paint->GetStrokeColor();
+    const float fill[4] = {fc.x, fc.y, fc.z, fc.w}, stroke[4] = {sc.x, sc.y, sc.z, sc.w};
+    std::memcpy(q.fill_color, fill, sizeof fill);
+    std::memcpy(q.stroke_color, stroke, sizeof stroke);
+  }
+  const float s4[4] = {src.Left(), src.Top(), src.Right(), src.Bottom()};
+  const float d4[4] = {dst.Left(), dst.Top(), dst.Right(), dst.Bottom()};
+  const uint32_t filter = sampling.UseCubic() ? 2u : sampling.filter == FilterMode::kLinear ? 1u : 0u;
+  const Rect& clip = GetGlobalClipBounds();
+  const bool clipped = !(clip.Left() == -1e9f && clip.Top() == -1e9f && clip.Right() == 1e9f &&
+                         clip.Bottom() == 1e9f);
+  const bool moved = tx != 0.f || ty != 0.f;
+  if (moved || clipped) skity_cuda_canvas_save(canvas_);
+  if (clipped)
+    skity_cuda_canvas_clip_rect(canvas_, clip.Left(), clip.Top(), clip.Right(), clip.Bottom());
+  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  status_ = skity_cuda_canvas_draw_image_rect(canvas_, &im, s4, d4, filter, &q);
+  if (moved || clipped) skity_cuda_canvas_restore(canvas_);
 }
 
 void CUDACanvas::OnDrawGlyphs(uint32_t, const GlyphID[], const float[], const float[],
@@ -243,6 +331,15 @@ void CUDACanvas::OnFlush() { status_ = skity_cuda_canvas_flush(canvas_); }
 uint32_t CUDACanvas::OnGetWidth() const { return bitmap_->Width(); }
 
 uint32_t CUDACanvas::OnGetHeight() const { return bitmap_->Height(); }
+
+std::unique_ptr<CUDACanvas> MakeCUDACanvas(Bitmap* bitmap) {
+  static skity_cuda_context ctx = [] {
+    skity_cuda_context c = nullptr;
+    return skity_cuda_context_create(nullptr, &c) == SKITY_CUDA_SUCCESS ? c : nullptr;
+  }();
+  if (!ctx) return nullptr;
+  return MakeCUDACanvas(ctx, bitmap);
+}
 
 std::unique_ptr<CUDACanvas> MakeCUDACanvas(skity_cuda_context ctx, Bitmap* bitmap) {
   if (!bitmap || bitmap->Width() == 0 || bitmap->Height() == 0) return nullptr;

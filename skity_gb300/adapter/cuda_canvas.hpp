@@ -11,9 +11,11 @@
 // taken (the global clip bounds the base class keeps bound each draw's scan,
 // as SWCanvas::OnClipRect relies on, sw_canvas.cc:279-295), and so are
 // ClipPath, ClipRRect and ClipRect(kDifference) under a translation (path
-// clips the C ABI canvas keeps per save level, as SWCanvas does).  Operations
-// outside the GPU raster path -- clips under other matrices, layers, text,
-// images, canvas matrices other than translations, shader local matrices --
+// clips the C ABI canvas keeps per save level, as SWCanvas does), SaveLayer
+// (one level, a layer paint's alpha and blend mode) and DrawImageRect /
+// DrawImage under a translation.  Operations outside the GPU raster path --
+// clips under other matrices, nested layers, text, canvas matrices other
+// than translations, shader local matrices --
 // draw nothing and leave
 // SKITY_CUDA_ERROR_NOT_SUPPORTED in LastStatus(); draws under a clip this
 // canvas did not take draw nothing either, until the Restore that drops it.
@@ -51,11 +53,18 @@ class CUDACanvas : public Canvas {
   void OnDrawPaint(Paint const& paint) override;
   void OnSave() override {
     bad_clip_.push_back(bad_clip_.back());
+    saves_.push_back(1);
     skity_cuda_canvas_save(canvas_);
   }
   void OnRestore() override {
     if (bad_clip_.size() > 1) bad_clip_.pop_back();
-    skity_cuda_canvas_restore(canvas_);
+    // a SaveLayer level holds two C-ABI levels (the clip and the layer)
+    int n = 1;
+    if (!saves_.empty()) {
+      n = saves_.back();
+      saves_.pop_back();
+    }
+    for (int i = 0; i < n; ++i) skity_cuda_canvas_restore(canvas_);
   }
   void OnRestoreToCount(int) override {}
   void OnFlush() override;
@@ -68,12 +77,17 @@ class CUDACanvas : public Canvas {
   int32_t status_ = SKITY_CUDA_SUCCESS;
   // per save level: a clip this canvas does not take is in effect
   std::vector<bool> bad_clip_{false};
+  // per save level: the C-ABI canvas levels it pushed (1, or 2 for a SaveLayer)
+  std::vector<int> saves_;
 };
 
 // Same null / empty semantics as MakeSoftwareCanvas: nullptr for a null
 // bitmap or a zero width or height.  The bitmap must be kPremul_AlphaType,
 // kRGBA, and outlive the canvas.
 std::unique_ptr<CUDACanvas> MakeCUDACanvas(skity_cuda_context ctx, Bitmap* bitmap);
+// The same over a process-wide context on CUDA device 0, created at the
+// first call: the drop-in for Canvas::MakeSoftwareCanvas(Bitmap*).
+std::unique_ptr<CUDACanvas> MakeCUDACanvas(Bitmap* bitmap);
 
 }  // namespace cuda
 }  // namespace skity

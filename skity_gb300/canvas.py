@@ -515,6 +515,17 @@ class Canvas:
     def Restore(self):
         _lib.check(self.lib.skity_cuda_canvas_restore(self.handle), "skity_cuda_canvas_restore")
 
+    def SaveLayer(self, bounds, paint: "Paint | None" = None):
+        """Canvas::SaveLayer(bounds, paint): the draws until the matching
+        Restore go to a layer, composited at the Restore with the paint's
+        alpha and blend mode."""
+        b = (ctypes.c_float * 4)(*[float(v) for v in bounds])
+        keep = []
+        cp = self._paint_struct(paint, keep) if paint is not None else None
+        _lib.check(self.lib.skity_cuda_canvas_save_layer(
+            self.handle, b, ctypes.byref(cp) if cp is not None else None),
+            "skity_cuda_canvas_save_layer")
+
     def Translate(self, dx, dy):
         _lib.check(self.lib.skity_cuda_canvas_translate(self.handle, float(dx), float(dy)),
                    "skity_cuda_canvas_translate")
@@ -543,6 +554,85 @@ class Canvas:
     def close(self):
         if self.handle:
             self.lib.skity_cuda_canvas_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PictureRecorder:
+    """PictureRecorder (include/skity/recorder/picture_recorder.hpp):
+    BeginRecording returns a canvas whose calls are recorded, and
+    FinishRecording the DisplayList holding them.  Needs no GPU."""
+
+    def __init__(self):
+        self.lib = _lib.load()
+        self.canvas = None
+
+    def BeginRecording(self, bounds):
+        """bounds: (left, top, right, bottom) of the recording, as the
+        reference takes it; the recorded canvas is right x bottom pixels."""
+        w, h = int(round(bounds[2])), int(round(bounds[3]))
+        hdl = ctypes.c_void_p()
+        _lib.check(self.lib.skity_cuda_recorder_begin(w, h, ctypes.byref(hdl)),
+                   "skity_cuda_recorder_begin")
+        self.canvas = Canvas(_RecorderContext(self.lib), hdl, None)
+        self.size = (w, h)
+        return self.canvas
+
+    def GetRecordingCanvas(self):
+        return self.canvas
+
+    def FinishRecording(self) -> "DisplayList":
+        dl = ctypes.c_void_p()
+        _lib.check(self.lib.skity_cuda_recorder_finish(self.canvas.handle, ctypes.byref(dl)),
+                   "skity_cuda_recorder_finish")
+        self.canvas.close()
+        self.canvas = None
+        return DisplayList(self.lib, dl, self.size)
+
+
+class _RecorderContext:
+    """Stands in for a Context for a recorder's canvas (it draws nothing)."""
+
+    def __init__(self, lib):
+        self.lib, self.handle = lib, None
+
+
+class DisplayList:
+    """DisplayList (include/skity/recorder/display_list.hpp): Draw(canvas)
+    replays the recorded calls on a canvas; to_stream() / to_scene() give
+    the scene stream the batched and serving forms take."""
+
+    def __init__(self, lib, handle, size):
+        self.lib, self.handle, self.size = lib, handle, size
+
+    def GetOpCount(self) -> int:
+        return int(self.lib.skity_cuda_display_list_op_count(self.handle))
+
+    def Draw(self, canvas: "Canvas"):
+        _lib.check(self.lib.skity_cuda_display_list_draw(self.handle, canvas.handle),
+                   "skity_cuda_display_list_draw")
+
+    def to_stream(self) -> bytes:
+        n = ctypes.c_size_t(0)
+        _lib.check(self.lib.skity_cuda_display_list_to_stream(self.handle, None, ctypes.byref(n)),
+                   "skity_cuda_display_list_to_stream")
+        buf = ctypes.create_string_buffer(n.value)
+        _lib.check(self.lib.skity_cuda_display_list_to_stream(self.handle, buf, ctypes.byref(n)),
+                   "skity_cuda_display_list_to_stream")
+        return buf.raw[:n.value]
+
+    def to_scene(self):
+        from . import scene as S
+        return S.Scene.from_bytes(self.to_stream())
+
+    def close(self):
+        if self.handle:
+            self.lib.skity_cuda_display_list_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

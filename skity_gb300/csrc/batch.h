@@ -69,6 +69,19 @@ struct ImageShaderRec {
 };
 static_assert(sizeof(ImageShaderRec) == 80, "image shader layout");
 
+// Canvas::SaveLayer(bounds, paint) ... Restore around draws [start,
+// restore) (restore kLayerOpen: not restored), with the canvas translation
+// and global clip bounds in effect before the SaveLayer and the layer
+// paint's alpha (Paint::GetAlphaF) and blend mode.  Layers do not nest.
+struct LayerRec {
+  float bounds[4], translate[2], clip[4];
+  uint32_t start, restore;
+  float alpha;
+  uint32_t blend, pad[2];
+};
+static_assert(sizeof(LayerRec) == 64, "layer layout");
+constexpr uint32_t kLayerOpen = 0xFFFFFFFFu;
+
 struct StreamView {
   uint32_t width, height, has_clear;
   float clear[4];
@@ -93,6 +106,9 @@ struct StreamView {
   const uint8_t* image_pixels;
   uint64_t image_bytes;
   const ImageShaderRec* image_shaders;
+  // layers when the stream has them
+  uint32_t n_layers;
+  const LayerRec* layers;
 };
 
 // A ClipPath call of the stream: its parent state (1-based, 0: none), the
@@ -206,7 +222,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   // 1: per-draw clip bounds follow the stops; 2: then per-draw colour
   // filters; 4: then the path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~15u) return false;
+  if (flags & ~31u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -317,6 +333,27 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
           !(std::fabs(m[4]) >= 1e-30f) || !(std::fabs(m[0]) <= 1e30f) ||
           !(std::fabs(m[4]) <= 1e30f) || !(std::fabs(m[2]) <= 1e30f) ||
           !(std::fabs(m[5]) <= 1e30f) || s->paints[d].gradient >= 0)
+        return false;
+    }
+  }
+  s->n_layers = 0;
+  s->layers = nullptr;
+  if (flags & 16) {
+    if (o + 4 > len) return false;
+    std::memcpy(&s->n_layers, buf + o, 4);
+    o += 4;
+    if (s->n_layers > (1u << 20)) return false;
+    s->layers = (const LayerRec*)at(sizeof(LayerRec) * (size_t)s->n_layers);
+    if (o > len) return false;
+    for (uint32_t i = 0; i < s->n_layers; ++i) {
+      const LayerRec& L = s->layers[i];
+      const bool open = L.restore == kLayerOpen;
+      // one level, in draw order, each restored before the next starts
+      if (L.start > s->nd || (!open && (L.restore < L.start || L.restore > s->nd))) return false;
+      if (i + 1 < s->n_layers && (open || s->layers[i + 1].start < L.restore)) return false;
+      if (!ValidClip(L.bounds) || !ValidClip(L.clip) || L.blend > 28 ||
+          !(L.alpha >= 0.f && L.alpha <= 1.f) || !(std::fabs(L.translate[0]) <= kMaxCoord) ||
+          !(std::fabs(L.translate[1]) <= kMaxCoord))
         return false;
     }
   }
@@ -478,6 +515,7 @@ struct HostBatch {
   uint64_t pixel_bytes = 0;
   uint64_t draw_count = 0;
   uint32_t max_temp_w = 0, max_temp_h = 0;
+  uint32_t max_temp_style = 0;  // largest BlurStyle of the temp canvases (1: kNormal only)
 
   // the images of the stream being added: their byte offsets in the pixel
   // buffer, and the uploads that put them there (offset, first byte, bytes)
@@ -590,8 +628,12 @@ inline bool FiltersColor(const StreamView& s, uint32_t d) {
 }
 
 // Appends the passes of one DrawPath (fill/stroke in paint order) to `out`.
+// clip_shift: the draw's clip bounds moved by (dx, dy) -- a draw inside a
+// layer, whose sub-canvas clips with the global clip bounds offset by the
+// layer's origin (SWCanvas::GetScanClipBounds, sw_canvas.hpp:157-161).
 inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
-                          uint32_t canvas, float tx, float ty, std::vector<PassDesc>& out) {
+                          uint32_t canvas, float tx, float ty, std::vector<PassDesc>& out,
+                          const float* clip_shift = nullptr) {
   const PaintRec& pr = s.paints[d];
   const uint8_t* verbs = s.verbs + s.vo[d];
   uint32_t nv = s.vo[d + 1] - s.vo[d];
@@ -706,6 +748,12 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
       pd.clipped = 1;
       std::memcpy(pd.clip, s.clips + 4 * (size_t)d, sizeof pd.clip);
+      if (clip_shift) {  // Rect::Offset
+        pd.clip[0] = pd.clip[0] + clip_shift[0];
+        pd.clip[1] = pd.clip[1] + clip_shift[1];
+        pd.clip[2] = pd.clip[2] + clip_shift[0];
+        pd.clip[3] = pd.clip[3] + clip_shift[1];
+      }
     }
     pd.stroke_width = pr.stroke_width;
     pd.miter = pr.miter;
@@ -723,6 +771,62 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     if (need_fill) add(false);
     if (need_stroke) add(true);
   }
+}
+
+// Layers (Canvas::SaveLayer, canvas.cc:255-276 -> SWCanvas::OnSaveLayer,
+// sw_canvas.cc:441-484, on the canvas itself): the layer's bounds in local
+// coordinates (log_bounds), the origin of its sub-canvas (rel_bounds'
+// left/top) and its bitmap size.
+struct LayerGeom {
+  float log[4];
+  float off[2];
+  uint32_t w = 0, h = 0;
+};
+inline bool RectIntersect(float* a, const float* b) {  // Rect::Intersect (rect.cc:160-172)
+  const float l = std::max(a[0], b[0]), r = std::min(a[2], b[2]);
+  const float t = std::max(a[1], b[1]), bt = std::min(a[3], b[3]);
+  if (!(l < r && t < bt)) return false;
+  a[0] = l;
+  a[1] = t;
+  a[2] = r;
+  a[3] = bt;
+  return true;
+}
+// Matrix::MapRect of a translation (matrix.cc:306-337): corners x + tx, min/max.
+inline void MapRectTranslate(const float* src, float tx, float ty, float* dst) {
+  const float x0 = src[0] + tx, x1 = src[2] + tx, y0 = src[1] + ty, y1 = src[3] + ty;
+  dst[0] = std::min(x0, x1);
+  dst[2] = std::max(x0, x1);
+  dst[1] = std::min(y0, y1);
+  dst[3] = std::max(y0, y1);
+}
+inline LayerGeom LayerGeometry(const StreamView& s, const LayerRec& L) {
+  LayerGeom g;
+  const float tx = L.translate[0], ty = L.translate[1];
+  // Canvas::SaveLayer narrows the global clip bounds by the mapped bounds
+  // (CalculateGlobalClipBounds) before OnSaveLayer reads them
+  float clip[4] = {L.clip[0], L.clip[1], L.clip[2], L.clip[3]};
+  float mapped[4];
+  MapRectTranslate(L.bounds, tx, ty, mapped);
+  if (!RectIntersect(clip, mapped)) clip[0] = clip[1] = clip[2] = clip[3] = 0.f;
+  // ComputeFastBounds of a fill paint without a mask filter: the bounds
+  float layer[4] = {L.bounds[0] - 0.f, L.bounds[1] - 0.f, L.bounds[2] + 0.f, L.bounds[3] + 0.f};
+  float device[4] = {0.f, 0.f, (float)s.width, (float)s.height};
+  const float scan[4] = {clip[0] + -0.f, clip[1] + -0.f, clip[2] + -0.f, clip[3] + -0.f};
+  if (!RectIntersect(device, scan)) device[0] = device[1] = device[2] = device[3] = 0.f;
+  // device_to_local: the inverse translation (identity for none)
+  const bool ident = tx == 0.f && ty == 0.f;
+  float local_clip[4];
+  MapRectTranslate(device, ident ? 0.f : -tx, ident ? 0.f : -ty, local_clip);
+  if (!RectIntersect(layer, local_clip)) layer[0] = layer[1] = layer[2] = layer[3] = 0.f;
+  float rel[4];
+  MapRectTranslate(layer, tx, ty, rel);
+  std::memcpy(g.log, layer, sizeof layer);
+  g.off[0] = 0.f + rel[0];
+  g.off[1] = 0.f + rel[1];
+  g.w = (uint32_t)std::ceil(rel[2] - rel[0]);
+  g.h = (uint32_t)std::ceil(rel[3] - rel[1]);
+  return g;
 }
 
 // One canvas of a stream into the batch; returns false on invalid input.
@@ -788,14 +892,151 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       w += c.nw;
     }
   }
+  // Layers: each saved layer is a temp canvas (a zeroed bitmap over its
+  // device bounds) holding the passes of its draws, and at its restore an
+  // image pass draws it onto the canvas (SWCanvas::OnLayerRestore,
+  // sw_canvas.cc:891-902).
+  uint32_t li = 0;                 // next layer of the stream
+  const LayerRec* layer = nullptr; // the open layer
+  LayerGeom lg;
+  uint32_t ltemp = 0;              // its temp canvas (0: none, the bitmap is empty)
+  size_t ltemp_slot = 0;           // its entry in `temps`
+  auto restore_layer = [&]() {
+    if (ltemp) {
+      // DrawImage(layer bitmap, log_bounds, &paint) with drawing_layer set:
+      // a rect path with a decal / nearest pixmap brush whose unit
+      // coordinates are Scale(1/w, 1/h) * inverse(local) * Scale(1/B.W,
+      // 1/B.H) * Translate(-B.L, -B.T), local = Scale(1/w, 1/h) and B the
+      // drawn rect's device bounds rounded out (OnDrawImageRect
+      // sw_canvas.cc:659-662, GenerateBrush :772-784, SWRaster bounds_
+      // sw_raster.cc:742-744)
+      const LayerRec& L = *layer;
+      const float tx = L.translate[0], ty = L.translate[1];
+      const uint8_t rv[5] = {kMove, kLine, kLine, kLine, kClose};
+      const float rp[8] = {lg.log[0], lg.log[1], lg.log[2], lg.log[1],
+                           lg.log[2], lg.log[3], lg.log[0], lg.log[3]};
+      float bl = 0, bt = 0, br = 0, bb = 0;
+      for (int i = 0; i < 4; ++i) {
+        // CopyWithMatrix(Translate(tx, ty)): (1*x + 0*y) + (0*0 + tx*1)
+        const float x = (1.f * rp[2 * i] + 0.f * rp[2 * i + 1]) + (0.f * 0.f + tx * 1.f);
+        const float y = (0.f * rp[2 * i] + 1.f * rp[2 * i + 1]) + (0.f * 0.f + ty * 1.f);
+        if (i == 0) {
+          bl = br = x;
+          bt = bb = y;
+        }
+        bl = std::min(bl, x);
+        br = std::max(br, x);
+        bt = std::min(bt, y);
+        bb = std::max(bb, y);
+      }
+      bl = std::floor(bl);
+      bt = std::floor(bt);
+      br = std::ceil(br);
+      bb = std::ceil(bb);
+      const float fw = (float)lg.w, fh = (float)lg.h;
+      const Mat4 local = MatMul(MatScale(1.f / fw, 1.f / fh), MatTranslate(-0.f, -0.f));
+      Mat4 inv;  // Matrix::Invert (matrix.cc:134-142, 242-266)
+      inv.identity();
+      if (!local.is_identity()) {
+        const float sx = local.e[0][0], sy = local.e[1][1];
+        if (sx != 1.f || sy != 1.f) {
+          const float ix = 1.f / sx, iy = 1.f / sy;
+          inv.e[0][0] = ix;
+          inv.e[1][1] = iy;
+          inv.e[3][0] = -local.e[3][0] * ix;
+          inv.e[3][1] = -local.e[3][1] * iy;
+        } else {
+          inv.e[3][0] = -local.e[3][0];
+          inv.e[3][1] = -local.e[3][1];
+        }
+      }
+      const Mat4 m = MatMul(MatMul(MatMul(MatScale(1.f / fw, 1.f / fh), inv),
+                                   MatScale(1.0f / (br - bl), 1.0f / (bb - bt))),
+                            MatTranslate(-bl, -bt));
+      const uint32_t rect = hb.AddDraw(rv, 5, rp, 4, nullptr, 0);
+      Brush b;
+      std::memset(&b, 0, sizeof b);
+      b.kind = 3;
+      b.blend = L.blend;
+      b.global_alpha = (uint8_t)(255 * L.alpha);
+      b.m[0] = m.e[0][0];
+      b.m[1] = m.e[1][0];
+      b.m[2] = m.e[3][0];
+      b.m[3] = m.e[0][1];
+      b.m[4] = m.e[1][1];
+      b.m[5] = m.e[3][1];
+      b.img_w = lg.w;
+      b.img_h = lg.h;
+      b.img_off = hb.canvases[ltemp].px_off;
+      hb.brushes.push_back(b);
+      PassDesc pd;
+      std::memset(&pd, 0, sizeof pd);
+      pd.draw = rect;
+      pd.canvas = cidx;
+      pd.flags = L.blend == 3 ? kPassSrcOver : 0;
+      pd.brush = (uint32_t)hb.brushes.size() - 1;
+      pd.ga = b.global_alpha;
+      pd.tx = tx;
+      pd.ty = ty;
+      if (!IsNoClip(L.clip)) {  // the global clip bounds after the restore
+        pd.clipped = 1;
+        std::memcpy(pd.clip, L.clip, sizeof pd.clip);
+      }
+      pd.stroke_width = 1.f;
+      pd.miter = 4.f;
+      InitialCaps(rv, 5, rp, false, pd.cap);
+      DerivedCaps(pd.cap, false);
+      main_passes.push_back(pd);
+    }
+    layer = nullptr;
+    ltemp = 0;
+  };
+  auto layer_events = [&](uint32_t d) -> int {
+    if (layer && layer->restore == d) restore_layer();
+    while (!layer && li < s.n_layers && s.layers[li].start == d) {
+      layer = &s.layers[li++];
+      lg = LayerGeometry(s, *layer);
+      if (lg.w > 0 && lg.h > 0) {
+        if (lg.w > 65535 || lg.h > 65535) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+        ltemp = (uint32_t)hb.canvases.size();
+        CanvasDesc tc;
+        std::memset(&tc, 0, sizeof tc);
+        tc.w = lg.w;
+        tc.h = lg.h;
+        tc.px_off = hb.AllocPixels((uint64_t)lg.w * lg.h * 4);
+        tc.blur_off = tc.out_off = tc.px_off;
+        tc.has_clear = 1;  // a zeroed premultiplied bitmap (LayerState::Init)
+        tc.clear_pm = 0;
+        tc.blur_style = 0;  // a layer, not a blur: the blur stage passes it by
+        hb.canvases.push_back(tc);
+        hb.temp_canvases.push_back(ltemp);
+        ltemp_slot = temps.size();
+        temps.emplace_back(ltemp, std::vector<PassDesc>());
+      }
+      if (layer->restore == d) restore_layer();
+    }
+    return SKITY_CUDA_SUCCESS;
+  };
   for (uint32_t d = 0; d < s.nd; ++d) {
     const PaintRec& pr = s.paints[d];
     const uint32_t path_clip = s.draw_clip_state ? s.draw_clip_state[d] : 0u;
     if (pr.blend > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
+    if (int rc = layer_events(d)) return rc;
     uint32_t draw = hb.AddDraw(s.verbs + s.vo[d], s.vo[d + 1] - s.vo[d], s.pts + 2 * (size_t)s.po[d],
                                s.po[d + 1] - s.po[d], s.wts + s.wo[d], s.wo[d + 1] - s.wo[d]);
     hb.draw_count++;
     bool blur = pr.blur_style != 0 && pr.blur_radius > 0;  // MakeBlur(r <= 0) is null
+    if (layer) {
+      // a draw inside the layer: the sub-canvas's transform
+      // Translate(-origin) * CTM (sw_canvas.hpp:179-182), its clip moved by
+      // -origin; blurs and path clips inside layers are not taken
+      if (blur || path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+      if (!ltemp) continue;  // an empty layer bitmap: nothing lands
+      const float shift[2] = {-lg.off[0], -lg.off[1]};
+      AddDrawPasses(hb, s, d, draw, ltemp, pr.translate[0] + shift[0], pr.translate[1] + shift[1],
+                    temps[ltemp_slot].second, shift);
+      continue;
+    }
     if (!blur) {
       // the canvas translation goes where the reference's CopyWithMatrix
       // and device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
@@ -860,6 +1101,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     hb.temp_canvases.push_back(tidx);
     hb.max_temp_w = std::max(hb.max_temp_w, fw);
     hb.max_temp_h = std::max(hb.max_temp_h, fh);
+    hb.max_temp_style = std::max<uint32_t>(hb.max_temp_style, pr.blur_style);
     std::vector<PassDesc> tp;
     AddDrawPasses(hb, s, d, draw, tidx, -fl, -ft, tp);
     temps.emplace_back(tidx, std::move(tp));
@@ -907,6 +1149,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     DerivedCaps(pd.cap, false);
     main_passes.push_back(pd);
   }
+  if (int rc = layer_events(s.nd)) return rc;
   // canvases with passes the compositor's common form does not take
   auto general = [&](const std::vector<PassDesc>& ps) {
     for (const PassDesc& pd : ps) {

@@ -445,7 +445,8 @@ __global__ void k_blur_h(DevBatch b, const uint32_t* temps, uint32_t n_temp, uin
   uint32_t yrow = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
-  if (yrow >= cd.h || BlurRowsPerBlock(cd.w) != 0) return;  // staged
+  // staged, or a layer's temp canvas (no blur)
+  if (yrow >= cd.h || BlurRowsPerBlock(cd.w) != 0 || cd.blur_style == 0) return;
   const uint8_t* src = b.pixels + cd.px_off + (size_t)yrow * cd.w * 4;
   uint8_t* dst = b.pixels + cd.blur_off + (size_t)yrow * cd.w * 4;
   int r = min(cd.blur_radius, 254);
@@ -461,7 +462,7 @@ __global__ void k_blur_v(DevBatch b, const uint32_t* temps, uint32_t n_temp, uin
   uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
-  if (x >= cd.w || BlurStripFits(cd.h)) return;  // staged
+  if (x >= cd.w || BlurStripFits(cd.h) || cd.blur_style == 0) return;  // staged, or a layer
   int r = min(cd.blur_radius, 254);
   const uint8_t* src = b.pixels + cd.blur_off + (size_t)x * 4;
   uint8_t* dst = b.pixels + cd.out_off + (size_t)x * 4;
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(kBlurThreads)
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
   const uint32_t rows = BlurRowsPerBlock(cd.w);
-  if (rows == 0) return;
+  if (rows == 0 || cd.blur_style == 0) return;  // direct pass, or a layer (no blur)
   const uint32_t y0 = blockIdx.x * rows;
   if (y0 >= cd.h) return;
   const uint32_t nr = min(rows, cd.h - y0);
@@ -529,7 +530,7 @@ __global__ void __launch_bounds__(32)
   const uint32_t t = blockIdx.y;
   if (t >= n_temp) return;
   const CanvasDesc cd = b.canvases[temps[t]];
-  if (!BlurStripFits(cd.h)) return;
+  if (!BlurStripFits(cd.h) || cd.blur_style == 0) return;  // direct pass, or a layer
   const uint32_t x0 = blockIdx.x * 32;
   if (x0 >= cd.w) return;
   const uint32_t nc = min(32u, cd.w - x0);
@@ -556,8 +557,9 @@ __global__ void __launch_bounds__(32)
 }
 
 int LaunchBlur(const DevBatch& b, const uint32_t* temps, uint32_t n_temp, uint32_t max_h,
-               uint32_t max_w, cudaStream_t stream) {
-  if (n_temp == 0) return 0;
+               uint32_t max_w, uint32_t max_style, cudaStream_t stream) {
+  // no blurred temp canvases (the temps are layers): nothing to blur
+  if (n_temp == 0 || max_w == 0 || max_h == 0) return 0;
   // staged passes (their blocks for canvases that do not fit return at once)
   const uint32_t min_rows = std::max<uint32_t>(BlurRowsPerBlock(max_w), 1);
   dim3 gsh((max_h + min_rows - 1) / min_rows, n_temp);
@@ -579,6 +581,7 @@ int LaunchBlur(const DevBatch& b, const uint32_t* temps, uint32_t n_temp, uint32
     k_blur_v<<<gv, 64, 0, stream>>>(b, temps, n_temp, max_w);
     n++;
   }
+  if (max_style <= 1) return n;  // kNormal blurs in place: nothing to combine
   const uint64_t px = (uint64_t)max_w * max_h;
   dim3 gs((unsigned)std::min<uint64_t>((px + 255) / 256, 1024), n_temp);
   k_blur_style<<<gs, 256, 0, stream>>>(b, temps, n_temp);

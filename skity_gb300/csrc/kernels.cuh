@@ -271,8 +271,10 @@ int LaunchPathClips(const DevBatch& b, const ClipStateDesc* states, uint32_t n_s
 int LaunchComposite(const DevBatch& b, const RowTask* tasks, uint32_t n_tasks, uint32_t chunk,
                     uint32_t ctas_per_sm, uint32_t num_sms, unsigned int* counter,
                     cudaStream_t stream);
+// max_style: the largest BlurStyle of the temp canvases (the style pass
+// runs only when one is not kNormal)
 int LaunchBlur(const DevBatch& b, const uint32_t* temp_canvases, uint32_t n_temp,
-               uint32_t max_h, uint32_t max_w, cudaStream_t stream);
+               uint32_t max_h, uint32_t max_w, uint32_t max_style, cudaStream_t stream);
 int LaunchClearCanvases(const DevBatch& b, const uint32_t* canvases, uint32_t n, cudaStream_t stream);
 
 }  // namespace skc

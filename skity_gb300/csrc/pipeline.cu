@@ -177,7 +177,7 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
     case 3:
       if (db.h_tasks_temp.empty()) return 0;
       return LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
-                        hb.max_temp_h, hb.max_temp_w, s);
+                        hb.max_temp_h, hb.max_temp_w, hb.max_temp_style, s);
     default:
       cudaMemsetAsync(b.task_next + 1, 0, 4, s);
       return LaunchComposite(b, db.tasks_main.as<RowTask>(), (uint32_t)db.h_tasks_main.size(),
@@ -427,7 +427,7 @@ static int EnqueueDevice(DeviceBatch& db, const DevBatch& b, const DevPlan& q, u
     case 4:
       if (!q.n_temp) return 0;
       return LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
-                        hb.max_temp_h, hb.max_temp_w, s);
+                        hb.max_temp_h, hb.max_temp_w, hb.max_temp_style, s);
     default: {
       cudaMemsetAsync(b.task_next + 1, 0, 4, s);
       int n = LaunchComposite(b, q.tasks_out, q.n_main, db.chunk, db.cfg.ctas_per_sm, num_sms,
@@ -819,7 +819,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   SKC_TRY(cudaEventRecord(ctx->stage[7], s));
   if (!db.h_tasks_temp.empty()) {
     st.kernel_launches += LaunchBlur(b, db.temps.as<uint32_t>(), (uint32_t)hb.temp_canvases.size(),
-                                     hb.max_temp_h, hb.max_temp_w, s);
+                                     hb.max_temp_h, hb.max_temp_w, hb.max_temp_style, s);
   }
   SKC_TRY(cudaEventRecord(ctx->stage[8], s));
   st.kernel_launches += LaunchComposite(b, db.tasks_main.as<RowTask>(),
@@ -905,8 +905,122 @@ struct skity_cuda_batch_s {
   skc::DeviceBatch db;
 };
 
+namespace skc {
+
+// One recorded canvas call of a display list (the reference's RecordedOp,
+// src/recorder/recorded_op.hpp): the call's arguments, with the path,
+// paint, shader, colour filter and image copied so the list owns them.
+struct RecordedOp {
+  enum Type : uint32_t {
+    kClear, kDrawPath, kDrawImageRect, kSave, kRestore, kSaveLayer, kTranslate, kClipRect,
+    kClipPath
+  };
+  Type type = kSave;
+  float f[8] = {};  // colour / bounds / translation / rect / src + dst
+  uint32_t u = 0;   // ClipOp / image filter
+  bool has_path = false;
+  std::vector<uint8_t> verbs;
+  std::vector<float> pts, wts;
+  uint32_t fill_type = 0;
+  bool has_paint = false;
+  skity_cuda_paint paint{};
+  bool has_grad = false;
+  skity_cuda_gradient grad{};
+  std::vector<float> grad_colors, grad_offsets;
+  bool has_cf = false;
+  skity_cuda_color_filter cf{};
+  bool has_ish = false;
+  skity_cuda_image_shader ish{};
+  bool has_img = false;  // the image of the image shader or of DrawImageRect
+  skity_cuda_image img{};
+  std::vector<uint8_t> img_px;
+
+  void CopyPath(const skity_cuda_path* p) {
+    has_path = true;
+    verbs.assign(p->verbs, p->verbs + p->verb_count);
+    pts.assign(p->points, p->points + 2 * (size_t)p->point_count);
+    wts.assign(p->conic_weights, p->conic_weights + p->conic_weight_count);
+    fill_type = p->fill_type;
+  }
+  void CopyImage(const skity_cuda_image* im) {
+    has_img = true;
+    img = *im;
+    const uint8_t* px = (const uint8_t*)im->pixels;
+    img_px.assign(px, px + (size_t)im->width * im->height * 4);
+  }
+  void CopyPaint(const skity_cuda_paint* q) {
+    if (!q) return;
+    has_paint = true;
+    paint = *q;
+    if (q->shader) {
+      has_grad = true;
+      grad = *q->shader;
+      grad_colors.assign(q->shader->colors, q->shader->colors + 4 * (size_t)q->shader->stop_count);
+      if (q->shader->has_offsets && q->shader->offsets)
+        grad_offsets.assign(q->shader->offsets, q->shader->offsets + q->shader->stop_count);
+    }
+    if (q->color_filter) {
+      has_cf = true;
+      cf = *q->color_filter;
+    }
+    if (q->image_shader) {
+      has_ish = true;
+      ish = *q->image_shader;
+      if (q->image_shader->image) CopyImage(q->image_shader->image);
+    }
+  }
+  // views of the copies (valid while the op is not moved)
+  skity_cuda_path PathView() const {
+    skity_cuda_path p{};
+    p.verbs = verbs.data();
+    p.verb_count = (uint32_t)verbs.size();
+    p.points = pts.data();
+    p.point_count = (uint32_t)(pts.size() / 2);
+    p.conic_weights = wts.data();
+    p.conic_weight_count = (uint32_t)wts.size();
+    p.fill_type = fill_type;
+    return p;
+  }
+  skity_cuda_image ImageView() const {
+    skity_cuda_image im = img;
+    im.pixels = img_px.data();
+    return im;
+  }
+  // q (and the shader records it points to) over the copies
+  void PaintView(skity_cuda_paint* q, skity_cuda_gradient* g, skity_cuda_image_shader* is,
+                 skity_cuda_image* im) const {
+    *q = paint;
+    q->shader = nullptr;
+    q->color_filter = has_cf ? &cf : nullptr;
+    q->image_shader = nullptr;
+    if (has_grad) {
+      *g = grad;
+      g->colors = grad_colors.data();
+      g->offsets = grad_offsets.empty() ? nullptr : grad_offsets.data();
+      q->shader = g;
+    }
+    if (has_ish) {
+      *is = ish;
+      *im = ImageView();
+      is->image = has_img ? im : nullptr;
+      q->image_shader = is;
+    }
+  }
+};
+
+}  // namespace skc
+
+struct skity_cuda_display_list_s {
+  uint32_t width = 0, height = 0;
+  std::vector<skc::RecordedOp> ops;
+};
+
 struct skity_cuda_canvas_s {
   skity_cuda_context ctx;
+  // a recorder's canvas (skity_cuda_recorder_begin): calls are recorded as
+  // ops of a display list instead of being drawn
+  bool recording = false;
+  std::vector<skc::RecordedOp> ops;
   uint32_t width, height;
   uint8_t* pixels;
   size_t row_bytes;
@@ -928,6 +1042,9 @@ struct skity_cuda_canvas_s {
   };
   State st;
   std::vector<State> saved;
+  // per saved level: the layer its Restore composites (1-based in `layers`; 0: none)
+  std::vector<uint32_t> saved_layer;
+  std::vector<skc::LayerRec> layers;
   std::vector<float> clips;  // per recorded draw: its clip bounds
   bool any_clip = false;
   std::vector<skc::ColorFilterRec> filters;  // per recorded draw: its colour filter
@@ -1170,6 +1287,13 @@ SKITY_CUDA_API void skity_cuda_canvas_destroy(skity_cuda_canvas canvas) { delete
 SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const float color[4]) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!color) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kClear;
+    std::memcpy(op.f, color, 16);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   if (canvas->st.path_clip) {
     // SWCanvas::OnDrawPaint under a path clip (sw_canvas.cc:413-439): the
     // canvas rect, rasterised with no matrix and no clip bounds, clipped by
@@ -1197,7 +1321,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
     canvas->st = keep;
     return rc;
   }
+  // a Clear inside a layer clears the layer's bitmap in the reference (the
+  // sub-canvas takes the DrawPaint); not taken here
+  for (uint32_t l : canvas->saved_layer)
+    if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   // a kSrc fill of the whole canvas overwrites everything drawn before
+  canvas->layers.clear();
   canvas->has_clear = true;
   std::memcpy(canvas->clear, color, 16);
   canvas->verbs.clear();
@@ -1245,6 +1374,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   if (need_p != path->point_count || need_w != path->conic_weight_count)
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past kLuminosity
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kDrawPath;
+    op.CopyPath(path);
+    op.CopyPaint(paint);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   const skity_cuda_image_shader* is = paint->image_shader;
   if (is) {
     const skity_cuda_image* im = is->image;
@@ -1372,6 +1509,17 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canva
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!image) return SKITY_CUDA_SUCCESS;
   if (!src || !dst || filter > 2) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kDrawImageRect;
+    std::memcpy(op.f, src, 16);
+    std::memcpy(op.f + 4, dst, 16);
+    op.u = filter;
+    op.CopyImage(image);
+    op.CopyPaint(paint);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   // Rect::Width / Height; an empty src or dst draws nothing
   const float sw = src[2] - src[0], sh = src[3] - src[1];
   const float dw = dst[2] - dst[0], dh = dst[3] - dst[1];
@@ -1424,18 +1572,99 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canva
 
 SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kSave;
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   canvas->saved.push_back(canvas->st);
+  canvas->saved_layer.push_back(0);
   return SKITY_CUDA_SUCCESS;
 }
 
-// Canvas::Restore with nothing saved leaves the matrix as it is.
+// Canvas::Restore with nothing saved leaves the matrix as it is.  Restoring
+// the level a SaveLayer made composites the layer before the next draw.
 SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kRestore;
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   if (!canvas->saved.empty()) {
     canvas->st = canvas->saved.back();
     canvas->saved.pop_back();
+    const uint32_t layer = canvas->saved_layer.back();
+    canvas->saved_layer.pop_back();
+    if (layer) {
+      canvas->layers[layer - 1].restore = (uint32_t)canvas->paints.size();
+      canvas->dirty = true;
+    }
   }
   return SKITY_CUDA_SUCCESS;
+}
+
+// Canvas::SaveLayer(bounds, paint) (canvas.cc:255-276): empty bounds, or
+// bounds the global clip bounds reject (QuickReject, canvas.cc:478-486),
+// save no layer -- a Save and an empty clip instead; otherwise a Save, the
+// global clip bounds narrowed by the bounds, and a layer whose draws are
+// composited at the matching Restore (SWCanvas::OnSaveLayer / OnLayerRestore,
+// sw_canvas.cc:441-484, 891-902).
+SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, const float bounds[4],
+                                                    const skity_cuda_paint* paint) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!bounds || !std::isfinite(bounds[0]) || !std::isfinite(bounds[1]) ||
+      !std::isfinite(bounds[2]) || !std::isfinite(bounds[3]))
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (paint && paint->blend_mode > 28) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kSaveLayer;
+    std::memcpy(op.f, bounds, 16);
+    op.CopyPaint(paint);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
+  // one level of layers; no mask or colour filter on the layer paint
+  for (uint32_t l : canvas->saved_layer)
+    if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (paint && ((paint->blur_style != 0 && paint->blur_radius > 0.f) || paint->color_filter))
+    return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  const bool empty = !(bounds[0] < bounds[2] && bounds[1] < bounds[3]);
+  bool reject = empty;
+  if (!empty) {  // QuickReject: the mapped bounds against the global clip bounds
+    const float x0 = bounds[0] + canvas->st.tx, x1 = bounds[2] + canvas->st.tx;
+    const float y0 = bounds[1] + canvas->st.ty, y1 = bounds[3] + canvas->st.ty;
+    const float* c = canvas->st.clip;
+    const float l = std::max(c[0], std::min(x0, x1)), r = std::min(c[2], std::max(x0, x1));
+    const float t = std::max(c[1], std::min(y0, y1)), b = std::min(c[3], std::max(y0, y1));
+    reject = !(l < r && t < b);
+  }
+  canvas->saved.push_back(canvas->st);
+  if (reject) {
+    canvas->saved_layer.push_back(0);
+    float* c = canvas->st.clip;
+    c[0] = c[1] = c[2] = c[3] = 0.f;
+    return SKITY_CUDA_SUCCESS;
+  }
+  skc::LayerRec L;
+  std::memset(&L, 0, sizeof L);
+  std::memcpy(L.bounds, bounds, sizeof L.bounds);
+  L.translate[0] = canvas->st.tx;
+  L.translate[1] = canvas->st.ty;
+  std::memcpy(L.clip, canvas->st.clip, sizeof L.clip);
+  L.start = (uint32_t)canvas->paints.size();
+  L.restore = skc::kLayerOpen;
+  // the image draw's alpha: Paint::GetAlphaF (paint.cc:96-98)
+  L.alpha = paint ? (paint->style == 1 ? paint->stroke_color[3] : paint->fill_color[3]) : 1.f;
+  L.alpha = std::min(std::max(L.alpha, 0.f), 1.f);
+  L.blend = paint ? paint->blend_mode : 3u;
+  canvas->layers.push_back(L);
+  canvas->saved_layer.push_back((uint32_t)canvas->layers.size());
+  canvas->dirty = true;
+  return skity_cuda_canvas_clip_rect(canvas, bounds[0], bounds[1], bounds[2], bounds[3]);
 }
 
 // The product of two translations: Translate(tx, ty) * Translate(dx, dy)
@@ -1443,6 +1672,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas) {
 SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!std::isfinite(dx) || !std::isfinite(dy)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kTranslate;
+    op.f[0] = dx;
+    op.f[1] = dy;
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   canvas->st.tx = canvas->st.tx + dx;
   canvas->st.ty = canvas->st.ty + dy;
   return SKITY_CUDA_SUCCESS;
@@ -1475,6 +1712,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
   if (!skc::ValidPath(path->verbs, path->verb_count, path->points, path->point_count,
                       path->conic_weights, path->conic_weight_count))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp rop;
+    rop.type = skc::RecordedOp::kClipPath;
+    rop.CopyPath(path);
+    rop.u = op;
+    canvas->ops.push_back(std::move(rop));
+    return SKITY_CUDA_SUCCESS;
+  }
   float t[2] = {canvas->st.tx, canvas->st.ty};
   if (!skc::ValidTranslate(t, path->points, path->point_count)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (op == 1) {
@@ -1528,6 +1773,16 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, flo
   if (!std::isfinite(left) || !std::isfinite(top) || !std::isfinite(right) ||
       !std::isfinite(bottom))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kClipRect;
+    op.f[0] = left;
+    op.f[1] = top;
+    op.f[2] = right;
+    op.f[3] = bottom;
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
   float* c = canvas->st.clip;
   const float x0 = left + canvas->st.tx, x1 = right + canvas->st.tx;
   const float y0 = top + canvas->st.ty, y1 = bottom + canvas->st.ty;
@@ -1546,7 +1801,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, flo
 
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (canvas->recording || !canvas->ctx) return SKITY_CUDA_SUCCESS;  // a recorder draws nothing
   if (!canvas->dirty) return SKITY_CUDA_SUCCESS;  // OnFlush with nothing recorded
+  // a layer still open holds draws the bitmap does not show yet; this
+  // canvas does not carry them across a flush
+  for (uint32_t l : canvas->saved_layer)
+    if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   skity_cuda_context ctx = canvas->ctx;
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1585,6 +1845,10 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
     sv.image_pixels = canvas->image_blob.data();
     sv.image_bytes = canvas->image_blob.size();
     sv.image_shaders = canvas->image_shaders.data();
+  }
+  if (!canvas->layers.empty()) {
+    sv.n_layers = (uint32_t)canvas->layers.size();
+    sv.layers = canvas->layers.data();
   }
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
@@ -1628,7 +1892,206 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->images.clear();
   canvas->image_blob.clear();
   canvas->image_shaders.clear();
+  canvas->layers.clear();
   canvas->dirty = false;
+  return SKITY_CUDA_SUCCESS;
+}
+
+
+// ---------------------------------------------------------------------------
+// PictureRecorder / DisplayList (src/recorder/picture_recorder.cc,
+// display_list.cc; C API module/capi/include/skity_c/skity_recorder.h)
+// ---------------------------------------------------------------------------
+SKITY_CUDA_API int32_t skity_cuda_recorder_begin(uint32_t width, uint32_t height,
+                                                 skity_cuda_canvas* out) {
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (width == 0 || height == 0) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (width > 65535 || height > 65535) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  auto* c = new (std::nothrow) skity_cuda_canvas_s();
+  if (!c) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  c->ctx = nullptr;
+  c->recording = true;
+  c->width = width;
+  c->height = height;
+  c->pixels = nullptr;
+  c->row_bytes = (size_t)width * 4;
+  *out = c;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_recorder_finish(skity_cuda_canvas recorder,
+                                                  skity_cuda_display_list* out) {
+  if (!recorder || !recorder->recording) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!out) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  auto* dl = new (std::nothrow) skity_cuda_display_list_s();
+  if (!dl) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  dl->width = recorder->width;
+  dl->height = recorder->height;
+  dl->ops.swap(recorder->ops);
+  *out = dl;
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API void skity_cuda_display_list_destroy(skity_cuda_display_list list) { delete list; }
+
+SKITY_CUDA_API uint32_t skity_cuda_display_list_op_count(skity_cuda_display_list list) {
+  return list ? (uint32_t)list->ops.size() : 0u;
+}
+
+// DisplayList::Draw (display_list.cc:330-343, ReplayRecordedOp :69-): every
+// op replayed, in order, through the canvas's own calls -- so the canvas's
+// current matrix and clips apply, and a recorder's canvas records them again.
+SKITY_CUDA_API int32_t skity_cuda_display_list_draw(skity_cuda_display_list list,
+                                                    skity_cuda_canvas canvas) {
+  if (!list || !canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  int32_t first_error = SKITY_CUDA_SUCCESS;
+  for (const skc::RecordedOp& op : list->ops) {
+    int32_t rc = SKITY_CUDA_SUCCESS;
+    skity_cuda_paint q{};
+    skity_cuda_gradient g{};
+    skity_cuda_image_shader is{};
+    skity_cuda_image im{};
+    if (op.has_paint) op.PaintView(&q, &g, &is, &im);
+    switch (op.type) {
+      case skc::RecordedOp::kClear:
+        rc = skity_cuda_canvas_clear(canvas, op.f);
+        break;
+      case skc::RecordedOp::kDrawPath: {
+        const skity_cuda_path p = op.PathView();
+        rc = skity_cuda_canvas_draw_path(canvas, &p, &q);
+      } break;
+      case skc::RecordedOp::kDrawImageRect: {
+        const skity_cuda_image img = op.ImageView();
+        rc = skity_cuda_canvas_draw_image_rect(canvas, &img, op.f, op.f + 4, op.u,
+                                               op.has_paint ? &q : nullptr);
+      } break;
+      case skc::RecordedOp::kSave:
+        rc = skity_cuda_canvas_save(canvas);
+        break;
+      case skc::RecordedOp::kRestore:
+        rc = skity_cuda_canvas_restore(canvas);
+        break;
+      case skc::RecordedOp::kSaveLayer:
+        rc = skity_cuda_canvas_save_layer(canvas, op.f, op.has_paint ? &q : nullptr);
+        break;
+      case skc::RecordedOp::kTranslate:
+        rc = skity_cuda_canvas_translate(canvas, op.f[0], op.f[1]);
+        break;
+      case skc::RecordedOp::kClipRect:
+        rc = skity_cuda_canvas_clip_rect(canvas, op.f[0], op.f[1], op.f[2], op.f[3]);
+        break;
+      case skc::RecordedOp::kClipPath: {
+        const skity_cuda_path p = op.PathView();
+        rc = skity_cuda_canvas_clip_path(canvas, &p, op.u);
+      } break;
+    }
+    if (rc != SKITY_CUDA_SUCCESS && first_error == SKITY_CUDA_SUCCESS) first_error = rc;
+  }
+  return first_error;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+void Put(std::vector<uint8_t>& out, const T* p, size_t n) {
+  const uint8_t* b = (const uint8_t*)p;
+  out.insert(out.end(), b, b + n * sizeof(T));
+}
+void Pad4(std::vector<uint8_t>& out, size_t n) { out.insert(out.end(), (4 - n % 4) % 4, 0); }
+
+// The recorded scene of a canvas as a scene stream (the layout ParseStream
+// reads; skity_gb300/scene.py writes the same).
+void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
+  const uint32_t nd = (uint32_t)c.paints.size();
+  const uint32_t flags = (c.any_clip ? 1u : 0u) | (c.any_filter ? 2u : 0u) |
+                         (!c.clip_states.empty() ? 4u : 0u) | (!c.images.empty() ? 8u : 0u) |
+                         (!c.layers.empty() ? 16u : 0u);
+  out.clear();
+  out.insert(out.end(), {'S', 'K', 'S', 'C'});
+  const uint32_t hdr[7] = {1u, c.width, c.height, c.has_clear ? 1u : 0u, flags, 0u, 0u};
+  Put(out, hdr, 7);
+  Put(out, c.clear, 4);
+  const uint32_t cnt[6] = {nd, (uint32_t)c.verbs.size(), (uint32_t)(c.pts.size() / 2),
+                           (uint32_t)c.wts.size(), (uint32_t)c.grads.size(),
+                           (uint32_t)c.stop_offsets.size()};
+  Put(out, cnt, 6);
+  Put(out, c.vo.data(), c.vo.size());
+  Put(out, c.po.data(), c.po.size());
+  Put(out, c.wo.data(), c.wo.size());
+  Put(out, c.verbs.data(), c.verbs.size());
+  Pad4(out, c.verbs.size());
+  Put(out, c.pts.data(), c.pts.size());
+  Put(out, c.wts.data(), c.wts.size());
+  Put(out, c.paints.data(), c.paints.size());
+  Put(out, c.grads.data(), c.grads.size());
+  Put(out, c.stop_colors.data(), c.stop_colors.size());
+  Put(out, c.stop_offsets.data(), c.stop_offsets.size());
+  if (flags & 1) Put(out, c.clips.data(), c.clips.size());
+  if (flags & 2) Put(out, c.filters.data(), c.filters.size());
+  if (flags & 4) {
+    const uint32_t n = (uint32_t)c.clip_states.size();
+    Put(out, &n, 1);
+    Put(out, c.clip_states.data(), c.clip_states.size());
+    Put(out, c.clip_verbs.data(), c.clip_verbs.size());
+    Pad4(out, c.clip_verbs.size());
+    Put(out, c.clip_pts.data(), c.clip_pts.size());
+    Put(out, c.clip_wts.data(), c.clip_wts.size());
+    Put(out, c.draw_clip_state.data(), c.draw_clip_state.size());
+  }
+  if (flags & 8) {
+    const uint32_t n = (uint32_t)c.images.size();
+    Put(out, &n, 1);
+    Put(out, c.images.data(), c.images.size());
+    const uint64_t nb = c.image_blob.size();
+    Put(out, &nb, 1);
+    Put(out, c.image_blob.data(), c.image_blob.size());
+    Pad4(out, c.image_blob.size());
+    Put(out, c.image_shaders.data(), c.image_shaders.size());
+  }
+  if (flags & 16) {
+    const uint32_t n = (uint32_t)c.layers.size();
+    Put(out, &n, 1);
+    Put(out, c.layers.data(), c.layers.size());
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// The display list as a scene stream: its ops replayed onto a fresh canvas
+// of the recording's size, whose recorded scene is written out -- the input
+// of skity_cuda_render_streams, skity_cuda_batch_create and
+// skity_cuda_server_submit.  out NULL: *size receives the byte count.
+SKITY_CUDA_API int32_t skity_cuda_display_list_to_stream(skity_cuda_display_list list, uint8_t* out,
+                                                         size_t* size) {
+  if (!list) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!size) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  skity_cuda_canvas_s c;
+  c.ctx = nullptr;
+  c.width = list->width;
+  c.height = list->height;
+  c.pixels = nullptr;
+  c.row_bytes = (size_t)list->width * 4;
+  int32_t rc = skity_cuda_display_list_draw(list, &c);
+  if (rc) return rc;
+  for (uint32_t l : c.saved_layer)
+    if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a layer left open
+  std::vector<uint8_t> bytes;
+  SerializeCanvas(c, bytes);
+  if (!out) {
+    *size = bytes.size();
+    return SKITY_CUDA_SUCCESS;
+  }
+  if (*size < bytes.size()) {
+    *size = bytes.size();
+    return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  }
+  std::memcpy(out, bytes.data(), bytes.size());
+  *size = bytes.size();
   return SKITY_CUDA_SUCCESS;
 }
 

@@ -64,6 +64,17 @@ FLAG_CLIPS = 1    # header flags: the per-draw clip section is present
 FLAG_FILTERS = 2  # the per-draw colour-filter section is present
 FLAG_PATH_CLIPS = 4  # the clip-state table and per-draw clip states are present
 FLAG_IMAGES = 8  # the image table, its pixels and the per-draw image shaders are present
+FLAG_LAYERS = 16  # the layer table (Canvas::SaveLayer ... Restore) is present
+# layer record: Canvas::SaveLayer(bounds, paint) under the canvas translation
+# and global clip bounds in effect before the call; draws [start, restore)
+# are drawn into the layer, which is composited onto the canvas (DrawImage of
+# the layer with the layer paint's alpha and blend mode) just before draw
+# `restore` (LAYER_OPEN: not restored, never composited).  Layers do not nest.
+LAYER_OPEN = 0xFFFFFFFF
+LAYER_DTYPE = np.dtype([("bounds", "<f4", 4), ("translate", "<f4", 2), ("clip", "<f4", 4),
+                        ("start", "<u4"), ("restore", "<u4"), ("alpha", "<f4"),
+                        ("blend", "<u4"), ("pad", "<u4", 2)])
+assert LAYER_DTYPE.itemsize == 64
 CLIP_DIFFERENCE, CLIP_INTERSECT = 0, 1  # Canvas::ClipOp
 # clip state record: parent state (1-based, 0: none), ClipOp, the path's
 # fill type, its verb / point / weight counts, the canvas translation and
@@ -153,6 +164,7 @@ class Scene:
     path_clips: tuple | None = None
     # images: (IMAGE_DTYPE records, pixel blob u8, per-draw IMAGE_SHADER_DTYPE), or None
     images: tuple | None = None
+    layers: np.ndarray | None = None  # LAYER_DTYPE records, or None
 
     @property
     def n_draws(self) -> int:
@@ -163,7 +175,8 @@ class Scene:
         flags = (FLAG_CLIPS if self.clips is not None else 0) | \
             (FLAG_FILTERS if self.filters is not None else 0) | \
             (FLAG_PATH_CLIPS if self.path_clips is not None else 0) | \
-            (FLAG_IMAGES if self.images is not None else 0)
+            (FLAG_IMAGES if self.images is not None else 0) | \
+            (FLAG_LAYERS if self.layers is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -212,6 +225,10 @@ class Scene:
             sh = np.ascontiguousarray(shaders, IMAGE_SHADER_DTYPE)
             assert len(sh) == nd
             out.append(sh.tobytes())
+        if self.layers is not None:
+            lay = np.ascontiguousarray(self.layers, LAYER_DTYPE)
+            out.append(struct.pack("<I", len(lay)))
+            out.append(lay.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -258,8 +275,12 @@ class Scene:
             (nb,) = struct.unpack_from("<Q", buf, o); o += 8
             blob = take(np.uint8, nb); o += (-nb) % 4
             images = (recs, blob, take(IMAGE_SHADER_DTYPE, nd))
+        layers = None
+        if flags & FLAG_LAYERS:
+            (n_layers,) = struct.unpack_from("<I", buf, o); o += 4
+            layers = take(LAYER_DTYPE, n_layers)
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so, clips, filters, path_clips, images)
+                     paints, grads, sc, so, clips, filters, path_clips, images, layers)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -293,7 +314,27 @@ class Scene:
                      None if self.path_clips is None else
                      self.path_clips[:4] + (self.path_clips[4][first:last].copy(),),
                      None if self.images is None else
-                     self.images[:2] + (self.images[2][first:last].copy(),))
+                     self.images[:2] + (self.images[2][first:last].copy(),),
+                     self._subset_layers(first, last))
+
+    def _subset_layers(self, first: int, last: int):
+        """The layers of draws [first, last): those restored before `first`
+        are gone; one restored past `last` is not restored in the subset."""
+        if self.layers is None:
+            return None
+        out = []
+        for rec in self.layers:
+            start, restore = int(rec["start"]), int(rec["restore"])
+            if restore != LAYER_OPEN and restore < first:
+                continue
+            if start > last:
+                continue
+            r = rec.copy()
+            r["start"] = max(start, first) - first
+            r["restore"] = (restore - first) if restore != LAYER_OPEN and restore <= last \
+                else LAYER_OPEN
+            out.append(r)
+        return np.array(out, LAYER_DTYPE) if out else None
 
 
 def map_clip(clip, rect, tx=0.0, ty=0.0):
@@ -330,6 +371,7 @@ class SceneBuilder:
         self._cstates, self._cverbs, self._cpts, self._cwts = [], [], [], []
         self._cstate, self._csaved, self._draw_cstate = 0, [], []
         self._images, self._blobs, self._nblob, self._shaders = [], [], 0, []
+        self._layers = []
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
                      tile_mode=TILE_CLAMP) -> int:
@@ -427,6 +469,36 @@ class SceneBuilder:
         self._cstate = len(self._cstates)
         return self._cstate
 
+    def save_layer(self, bounds, alpha=1.0, blend=BLEND_SRC_OVER, translate=(0.0, 0.0),
+                   clip=NO_CLIP):
+        """Canvas::SaveLayer(bounds, paint) under the canvas translation and
+        global clip bounds `clip` in effect before the call.  Returns the clip
+        bounds of the draws inside the layer (Canvas::SaveLayer narrows them
+        by the bounds, src/render/canvas.cc:255-276), or None when the
+        reference saves no layer (empty bounds, or bounds outside the clip:
+        a Save with an empty clip instead)."""
+        f = np.float32
+        b = tuple(float(f(v)) for v in bounds)
+        if not (b[0] < b[2] and b[1] < b[3]):
+            return None
+        narrowed = map_clip(clip, b, translate[0], translate[1])
+        if narrowed == (0.0, 0.0, 0.0, 0.0):
+            return None
+        r = np.zeros((), LAYER_DTYPE)
+        r["bounds"], r["translate"], r["clip"] = b, translate, clip
+        r["start"], r["restore"] = len(self._paints), LAYER_OPEN
+        r["alpha"], r["blend"] = alpha, blend
+        self._layers.append(r)
+        return narrowed
+
+    def restore_layer(self):
+        """Canvas::Restore of the innermost open layer: it is composited
+        before the next draw."""
+        for r in reversed(self._layers):
+            if int(r["restore"]) == LAYER_OPEN:
+                r["restore"] = len(self._paints)
+                return
+
     def build(self) -> Scene:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
         return Scene(self.width, self.height, self.clear,
@@ -447,7 +519,8 @@ class SceneBuilder:
                       if self._cstates else None),
                      ((np.array(self._images, IMAGE_DTYPE), cat(self._blobs, np.uint8, 0),
                        np.array(self._shaders, IMAGE_SHADER_DTYPE))
-                      if self._images else None))
+                      if self._images else None),
+                     np.array(self._layers, LAYER_DTYPE) if self._layers else None)
 
 
 def image_shader(image, filter=FILTER_NEAREST, tile_x=TILE_CLAMP, tile_y=TILE_CLAMP,
@@ -614,6 +687,71 @@ def random_paths_scene(seed, width, height, n_paths, verbs_lo, verbs_hi,
             p["gradient"] = gi
         b.draw_path(verbs, pts, p)
     return b.build()
+
+
+def with_layers(sc: Scene, specs) -> Scene:
+    """`sc` with layers around runs of its draws.  specs: (start, restore,
+    bounds, alpha, blend, translate, clip) per layer, in draw order, not
+    overlapping; `clip` is the canvas's global clip bounds before the
+    SaveLayer.  Draws inside a layer get their clip bounds narrowed by the
+    layer's bounds, as Canvas::SaveLayer narrows them (src/render/canvas.cc:
+    255-276); a layer the reference would not save (empty bounds, or bounds
+    outside the clip) becomes an empty clip for its draws instead."""
+    out = Scene(**{k: getattr(sc, k) for k in sc.__dataclass_fields__})
+    clips = (np.array(sc.clips, np.float32) if sc.clips is not None
+             else np.tile(np.array(NO_CLIP, np.float32), (sc.n_draws, 1)))
+    recs = []
+    for start, restore, bounds, alpha, blend, translate, clip in specs:
+        b = SceneBuilder(sc.width, sc.height)
+        narrowed = b.save_layer(bounds, alpha, blend, translate, clip)
+        end = sc.n_draws if restore == LAYER_OPEN else restore
+        for d in range(start, end):
+            clips[d] = (0.0, 0.0, 0.0, 0.0) if narrowed is None else \
+                map_clip(narrowed, tuple(float(v) for v in clips[d]))
+        if narrowed is None:
+            continue
+        r = b._layers[0]
+        r["start"], r["restore"] = start, restore
+        recs.append(r)
+    out.clips = clips
+    out.layers = np.array(recs, LAYER_DTYPE) if recs else None
+    return out
+
+
+def layered_scene(seed, width, height, n_paths, n_layers, gradient_frac=0.3, stroke_frac=0.2,
+                  blends=(BLEND_SRC_OVER,)) -> Scene:
+    """Random paths (line/quad/cubic, both fill rules, gradients, strokes)
+    with `n_layers` layers around runs of them: bounds over and past the
+    canvas with fractional edges, alpha in [0.2, 1], blend modes from
+    `blends`, some under a canvas translation and a narrowed clip."""
+    sc = random_paths_scene(seed, width, height, n_paths, 2, 16,
+                            coord_lo=(-16.0, -16.0), coord_hi=(width + 16.0, height + 16.0),
+                            evenodd_frac=0.4, gradient_frac=gradient_frac,
+                            stroke_frac=stroke_frac)
+    R = random_streams(seed ^ 0x9E3779B97F4A7C15, max(n_layers, 1), 16)
+    cuts = sorted(set(int(v) for v in randint(R[:, 0], 0, n_paths)))
+    specs, prev = [], 0
+    for i in range(n_layers):
+        start = min(n_paths, prev + int(randint(R[i, 1:2], 0, max(1, n_paths // n_layers // 2))[0]))
+        restore = min(n_paths, start + int(randint(R[i, 2:3], 0, max(1, n_paths // n_layers))[0]))
+        prev = restore
+        x0 = float(uniform(R[i, 3:4], -0.3 * width, 0.8 * width)[0])
+        y0 = float(uniform(R[i, 4:5], -0.3 * height, 0.8 * height)[0])
+        x1 = x0 + float(uniform(R[i, 5:6], 0.1 * width, 0.9 * width)[0])
+        y1 = y0 + float(uniform(R[i, 6:7], 0.1 * height, 0.9 * height)[0])
+        alpha = float(uniform(R[i, 7:8], 0.2, 1.0)[0])
+        blend = blends[int(randint(R[i, 8:9], 0, len(blends) - 1)[0])]
+        moved = u01(R[i, 9:10])[0] < 0.4
+        tx = float(uniform(R[i, 10:11], -0.25 * width, 0.25 * width)[0]) if moved else 0.0
+        ty = float(uniform(R[i, 11:12], -0.25 * height, 0.25 * height)[0]) if moved else 0.0
+        clipped = u01(R[i, 12:13])[0] < 0.4
+        clip = NO_CLIP if not clipped else (
+            float(uniform(R[i, 13:14], -8.0, 0.4 * width)[0]),
+            float(uniform(R[i, 14:15], -8.0, 0.4 * height)[0]),
+            float(uniform(R[i, 15:16], 0.6 * width, width + 8.0)[0]), float(height) * 0.9)
+        specs.append((start, restore, (x0, y0, x1, y1), alpha, blend, (tx, ty), clip))
+    del cuts
+    return with_layers(sc, specs)
 
 
 def config1(seed=SEED_BASE + 1, n_paths=1000) -> Scene:

@@ -10,7 +10,9 @@
 #include <skity/graphic/bitmap.hpp>
 #include <skity/graphic/color.hpp>
 #include <skity/graphic/paint.hpp>
+#include <skity/graphic/image.hpp>
 #include <skity/graphic/path.hpp>
+#include <skity/io/pixmap.hpp>
 
 #include "../skity_gb300/adapter/cuda_canvas.hpp"
 
@@ -85,6 +87,25 @@ int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas, float l, float t, float r
 }
 int32_t skity_cuda_canvas_flush(skity_cuda_canvas) {
   std::printf("flush\n");
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas, const float b[4],
+                                     const skity_cuda_paint* q) {
+  std::printf("save_layer %g %g %g %g alpha=%g blend=%u\n", b[0], b[1], b[2], b[3],
+              q ? q->fill_color[3] : 1.f, q ? q->blend_mode : 3u);
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas, const skity_cuda_image* im,
+                                          const float s[4], const float d[4], uint32_t filter,
+                                          const skity_cuda_paint* q) {
+  std::printf("image %ux%u alpha_type=%u src=%g,%g,%g,%g dst=%g,%g,%g,%g filter=%u alpha=%g "
+              "blend=%u\n",
+              im->width, im->height, im->alpha_type, s[0], s[1], s[2], s[3], d[0], d[1], d[2],
+              d[3], filter, q ? q->fill_color[3] : 1.f, q ? q->blend_mode : 3u);
+  return SKITY_CUDA_SUCCESS;
+}
+int32_t skity_cuda_context_create(const skity_cuda_context_create_info*, skity_cuda_context* out) {
+  *out = reinterpret_cast<skity_cuda_context>(0x30);
   return SKITY_CUDA_SUCCESS;
 }
 }
@@ -169,6 +190,29 @@ int main() {
   std::printf("status=%d\n", canvas->LastStatus());
   canvas->Flush();
   std::printf("status=%d\n", canvas->LastStatus());
+  // SaveLayer under a translation and a clip: the C-ABI canvas gets a level
+  // with the narrowed clip bounds and the translation, the layer, then the
+  // translation undone; Restore pops both levels
+  paint.SetColorFilter(nullptr);
+  canvas->Save();
+  canvas->Translate(3, 2);
+  Paint lp;
+  lp.SetAlphaF(0.25f);
+  lp.SetBlendMode(BlendMode::kMultiply);
+  canvas->SaveLayer(Rect::MakeLTRB(1, 1, 21, 11), lp);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->DrawPath(path, paint);
+  canvas->Restore();
+  canvas->Restore();
+  // DrawImageRect / DrawImage of a pixmap image reach the C ABI
+  auto pixmap = std::make_shared<Pixmap>(4, 3, AlphaType::kPremul_AlphaType);
+  auto image = Image::MakeImage(pixmap);
+  Paint ip;
+  ip.SetAlphaF(0.5f);
+  canvas->DrawImageRect(image, Rect::MakeLTRB(0, 0, 4, 3), Rect::MakeLTRB(5, 6, 13, 12),
+                        SamplingOptions{FilterMode::kLinear, MipmapMode::kNone}, &ip);
+  std::printf("status=%d\n", canvas->LastStatus());
+  std::printf("default_ctx=%d\n", cuda::MakeCUDACanvas(&bm) != nullptr);
   canvas.reset();
   return 0;
 }

@@ -189,6 +189,7 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   for (const RowTask& t : tasks) CompositeRowScalar(b, t, row.data());
   for (uint32_t c : hb.temp_canvases) {
     const CanvasDesc& cd = hb.canvases[c];
+    if (cd.blur_style == 0) continue;  // a layer: no blur
     int r = std::min(cd.blur_radius, 254);
     for (uint32_t y = 0; y < cd.h; ++y) {
       const uint8_t* src = pixels.data() + cd.px_off + (size_t)y * cd.w * 4;

@@ -105,4 +105,27 @@ def test_color_filters_forwarded(driver_output):
     assert " filter=1 mode=14 color=80102030 " in blend
     assert " filter=2 mode=0 color=00000000 m=0,1,0,0,0.25,1,0,0,0,0,0,0,1,0,0,0,0,0,0.5,0," in matrix
     assert " filter=4 " in gamma
-    assert driver_output[45:] == ["status=0", "flush", "status=0", "destroy 0x10"]
+    assert driver_output[45:48] == ["status=0", "flush", "status=0"]
+
+
+def test_save_layer_forwarded(driver_output):
+    # Save; Translate(3, 2); SaveLayer((1, 1, 21, 11), alpha 0.25, kMultiply):
+    # the global clip bounds narrowed to the mapped bounds (4, 3, 24, 13)
+    i = driver_output.index("save_layer 1 1 21 11 alpha=0.25 blend=24")
+    assert driver_output[i - 4:i] == ["save", "save", "clip 4 3 24 13", "translate 3 2"]
+    assert driver_output[i + 1:i + 3] == ["translate -3 -2", "status=0"]
+    # the draw inside carries its clip and translation; Restore of the
+    # layer level pops both C-ABI levels, then the outer Save's
+    assert driver_output[i + 3:i + 6] == ["save", "clip 4 3 24 13", "translate 3 2"]
+    assert driver_output[i + 6].startswith("draw verbs=0,1,2,3,4,5,")
+    assert driver_output[i + 7:i + 11] == ["restore", "restore", "restore", "restore"]
+
+
+def test_draw_image_rect_forwarded(driver_output):
+    line = [l for l in driver_output if l.startswith("image ")]
+    assert line == ["image 4x3 alpha_type=2 src=0,0,4,3 dst=5,6,13,12 filter=1 alpha=0.5 blend=3"]
+    i = driver_output.index(line[0])
+    assert driver_output[i + 1] == "status=0"
+    # MakeCUDACanvas(Bitmap*): a canvas over the process-wide context
+    assert driver_output[i + 2] == "create ctx=0x30 w=40 h=30 pixels=1 row_bytes=160"
+    assert driver_output[i + 3:] == ["default_ctx=1", "destroy 0x10", "destroy 0x10"]

@@ -232,3 +232,15 @@ def test_fixed_div_matches_64bit_quotient(cpu_pipeline):
     numer = np.concatenate([numer, en.ravel()]).astype(np.int32)
     denom = np.concatenate([denom, ed.ravel()]).astype(np.int32)
     assert cpu_pipeline.skc_cpu_fixed_div_check(numer.ctypes.data, denom.ctypes.data, len(numer)) == 0
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_layers_bit_exact(cpu_pipeline, oracle_lib, seed):
+    """Canvas::SaveLayer / Restore: layer temp canvases and their restore
+    image passes (alpha, blend modes, translations, clips, fractional
+    bounds) against the oracle."""
+    sc = S.layered_scene(S.SEED_BASE + 700 + seed, 120 + 8 * seed, 96 + 4 * seed, 30, 3,
+                         blends=(3, 1, 24, 6, 11))
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0

@@ -404,3 +404,13 @@ def clip_path_cases_scene():
 
 def test_clip_path_cases(ref):
     _pin(ref, clip_path_cases_scene())
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_layers(ref, seed):
+    """Canvas::SaveLayer / Restore: layers over and past the canvas with
+    fractional bounds, alpha, several blend modes, under translations and
+    narrowed clips, with fills, strokes and gradients inside and outside."""
+    sc = S.layered_scene(S.SEED_BASE + 700 + seed, 120 + 8 * seed, 96 + 4 * seed, 30, 3,
+                         blends=(3, 1, 24, 6, 11, 21))
+    _pin(ref, sc)
