@@ -577,12 +577,14 @@ def run_gpu(args, rank, world, local):
 
     # end to end through the C ABI with host buffers: every step uploads the
     # scene streams, plans and renders on the device, and reads every canvas back
-    e2e_ms = []
+    e2e_ms, e2e_parts = [], []
     if not args.no_e2e:
         ctx.render_streams(scenes)  # warm
         for _ in range(max(1, min(args.steps, 5))):
             e2e_out = ctx.render_streams(scenes)
-            e2e_ms.append(ctx.stats()["total_ms"])
+            est = ctx.stats()
+            e2e_ms.append(est["total_ms"])
+            e2e_parts.append(est)
         e2e_same = all(bool((a == b).all()) for a, b in zip(e2e_out, got))
     e2e_ms_mean = statistics.mean(e2e_ms) if e2e_ms else None
 
@@ -611,6 +613,9 @@ def run_gpu(args, rank, world, local):
                 "unit": "paths/s",
                 "h2d_bytes_per_step": sum(len(sc.to_bytes()) for sc in scenes),
                 "d2h_bytes_per_step": pix * 4, "ms_per_step": e2e_ms_mean,
+                "stage_ms": ({k: statistics.mean(p[k] for p in e2e_parts)
+                              for k in ("parse_ms", "upload_ms", "device_ms", "readback_ms")}
+                             if e2e_parts else None),
                 "same_pixels": e2e_same if e2e_ms else None},
         "wall_s": wall,
     }

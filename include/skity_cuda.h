@@ -180,6 +180,10 @@ typedef struct skity_cuda_stats {
   double plan_ms;         /* device planning after the geometry: sweep buffers,
                              row tables, pass bins, sweep and tile orders */
   uint64_t host_syncs;    /* host waits on the device inside the render */
+  /* skity_cuda_render_streams: wall time of its host stages */
+  double parse_ms;        /* streams parsed into the batch (passes, brushes, caps) */
+  double upload_ms;       /* inputs copied to the device */
+  double readback_ms;     /* pixels copied back to the host */
 } skity_cuda_stats;
 
 /* Launch shape of the compositor and the granularity of its pass bins; no

@@ -84,7 +84,8 @@ class Stats_(ctypes.Structure):
                 ("composite_ms", ctypes.c_double), ("blur_ms", ctypes.c_double),
                 ("fragments", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
                 ("fragments_by_brush", ctypes.c_uint64 * 4), ("plan_ms", ctypes.c_double),
-                ("host_syncs", ctypes.c_uint64)]
+                ("host_syncs", ctypes.c_uint64), ("parse_ms", ctypes.c_double),
+                ("upload_ms", ctypes.c_double), ("readback_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -221,7 +221,7 @@ struct SinkBase {
 };
 
 SKC_HD unsigned long long LaneBcast64(const Lanes& L, unsigned long long v, int src) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   return __shfl_sync(0xffffffffu, v, src);
 #else
   return v;

@@ -1157,16 +1157,27 @@ SKITY_CUDA_API int32_t skity_cuda_render_streams(skity_cuda_context ctx, uint32_
   if (!ctx->streams_batch) return SKITY_CUDA_ERROR_OUT_OF_HOST_MEMORY;
   skc::DeviceBatch& db = *ctx->streams_batch;
   db.Reset();
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
   int32_t rc = skc::BuildFromStreams(db, count, streams, stream_bytes);
   if (rc) return rc;
+  const double parse_ms = ms_since(t0);
+  auto t1 = std::chrono::steady_clock::now();
   rc = skc::UploadBatch(ctx, db);
   if (rc) return rc;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return SKITY_CUDA_ERROR_DEVICE;
+  const double upload_ms = ms_since(t1);
   rc = skc::RenderBatch(ctx, db, true);
   if (rc) return rc;
+  auto t2 = std::chrono::steady_clock::now();
   rc = skc::QueueReadCanvases(ctx, db, count, out_pixels);
   if (rc) return rc;
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return SKITY_CUDA_ERROR_DEVICE;
-  db.stats.host_syncs++;
+  db.stats.host_syncs += 2;
+  db.stats.parse_ms = parse_ms;
+  db.stats.upload_ms = upload_ms;
+  db.stats.readback_ms = ms_since(t2);
   db.stats.total_ms =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   ctx->last = db.stats;

@@ -481,8 +481,14 @@ SKC_HDN void introsort(int32_t* a, int n, Less less) {
 // logic runs warp-uniformly -- every lane computes the same values -- and the
 // per-pixel loops are split across lanes), one thread on the CPU.
 // ---------------------------------------------------------------------------
+// SKC_WARP_LANES: the lanes of a sweep are the 32 threads of a warp.  A
+// translation unit that defines SKC_SOLO_LANES before its includes compiles
+// the sweep for one thread per pass instead (the form the CPU runs).
+#if defined(__CUDA_ARCH__) && !defined(SKC_SOLO_LANES)
+#define SKC_WARP_LANES 1
+#endif
 struct Lanes {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   static constexpr int n = 32;
   int lane;
   __device__ unsigned ballot(bool p) const { return __ballot_sync(0xffffffffu, p); }
@@ -494,12 +500,17 @@ struct Lanes {
 #else
   static constexpr int n = 1;
   int lane = 0;
-  unsigned ballot(bool p) const { return p ? 1u : 0u; }
-  void sync() const {}
-  uint32_t shfl(uint32_t v, int) const { return v; }
-  unsigned lt_mask() const { return 0u; }
+  SKC_HD unsigned ballot(bool p) const { return p ? 1u : 0u; }
+  SKC_HD void sync() const {}
+  SKC_HD uint32_t shfl(uint32_t v, int) const { return v; }
+  SKC_HD unsigned lt_mask() const { return 0u; }
+#ifdef __CUDA_ARCH__
+  __device__ static int popc(unsigned m) { return __popc(m); }
+  __device__ static int ffs(unsigned m) { return __ffs((int)m); }
+#else
   static int popc(unsigned m) { return __builtin_popcount(m); }
   static int ffs(unsigned m) { return __builtin_ffs((int)m); }
+#endif
 #endif
   SKC_HD bool leader() const { return lane == 0; }
 };

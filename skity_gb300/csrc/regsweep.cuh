@@ -133,7 +133,7 @@ SKC_HD int WcWinding(int32_t wc) { return (int8_t)(wc & 0xFF); }
 SKC_HD int WcCount(int32_t wc) { return (int8_t)((wc >> 8) & 0xFF); }
 
 SKC_HD long long LaneMax64(const Lanes& L, long long v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   for (int o = 16; o > 0; o >>= 1) {
     long long t = __shfl_xor_sync(0xffffffffu, v, o);
     v = t > v ? t : v;

@@ -29,7 +29,7 @@ namespace skc {
 
 // ---- warp-level helpers -----------------------------------------------------
 SKC_HD int32_t LaneScanIncl(const Lanes& L, int32_t v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   for (int o = 1; o < 32; o <<= 1) {
     int32_t t = __shfl_up_sync(0xffffffffu, v, o);
     if (L.lane >= o) v += t;
@@ -38,26 +38,26 @@ SKC_HD int32_t LaneScanIncl(const Lanes& L, int32_t v) {
   return v;
 }
 SKC_HD int32_t LaneBcast(const Lanes& L, int32_t v, int src) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   return __shfl_sync(0xffffffffu, v, src);
 #else
   return v;
 #endif
 }
 SKC_HD int32_t LaneMin(const Lanes& L, int32_t v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
 #endif
   return v;
 }
 SKC_HD int32_t LaneMax(const Lanes& L, int32_t v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
 #endif
   return v;
 }
 SKC_HD unsigned long long LaneSum64(const Lanes& L, unsigned long long v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
 #endif
   return v;
@@ -70,8 +70,9 @@ SKC_HD void FlagError(uint32_t* err, uint32_t code) {
   *err |= code;
 #endif
 }
+// An add to the row accumulator, which the lanes of a warp share.
 SKC_HD void AtomicAddI32(int32_t* p, int32_t v) {
-#ifdef __CUDA_ARCH__
+#ifdef SKC_WARP_LANES
   atomicAdd(p, v);
 #else
   *p += v;
