@@ -154,10 +154,11 @@ def issue_roofline(st, frame_ms, composite_ms, clk, sms):
 
 # The sweep stage's counters per emitted span, from an ncu capture of the
 # 256-canvas workload's first 64 canvases (profiles/k_sweep_reg_config3_64canvases.md):
-# warp instructions executed and DRAM bytes (read + write) of the sweep
-# kernels per span they emit.  Multiplied by the spans of the timed render
+# warp instructions executed and DRAM bytes (read + write) of the four sweep
+# launches of one render (17.285 G instructions, 1.816 GB) over the
+# 165,827,810 spans they emit.  Multiplied by the spans of the timed render
 # (the units one launch processes) they give the per-render figures.
-SWEEP_PER_SPAN = {"warp_inst": None, "dram_bytes": None}
+SWEEP_PER_SPAN = {"warp_inst": 104.24, "dram_bytes": 10.95}
 
 
 def sweep_roofline(st, sweep_ms, clk, sms, hbm_peak, hbm_kind):
@@ -579,9 +580,13 @@ def run_gpu(args, rank, world, local):
     # scene streams, plans and renders on the device, and reads every canvas back
     e2e_ms, e2e_parts = [], []
     if not args.no_e2e:
-        ctx.render_streams(scenes)  # warm
+        # the canvases land in page-locked host memory, as a renderer handing
+        # frames to a compositor or an encoder would keep them
+        pinned = [torch.empty((sc.height, sc.width, 4), dtype=torch.uint8,
+                              pin_memory=True).numpy() for sc in scenes]
+        ctx.render_streams(scenes, pinned)  # warm
         for _ in range(max(1, min(args.steps, 5))):
-            e2e_out = ctx.render_streams(scenes)
+            e2e_out = ctx.render_streams(scenes, pinned)
             est = ctx.stats()
             e2e_ms.append(est["total_ms"])
             e2e_parts.append(est)

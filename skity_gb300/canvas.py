@@ -331,9 +331,21 @@ class Context:
             pass
 
     # ---- batched form over scene streams
-    def render_streams(self, scenes: list) -> list:
+    def render_streams(self, scenes: list, out: list | None = None) -> list:
+        """skity_cuda_render_streams: the scenes parsed, rendered and read
+        back in one call.  `out`: the canvases' pixel arrays to fill
+        ((height, width, 4) uint8, C-contiguous -- page-locked host memory
+        makes the read-back a direct copy); new arrays when None."""
         bufs = [s.to_bytes() for s in scenes]
-        outs = [np.zeros((s.height, s.width, 4), np.uint8) for s in scenes]
+        if out is None:
+            outs = [np.zeros((s.height, s.width, 4), np.uint8) for s in scenes]
+        else:
+            outs = list(out)
+            if len(outs) != len(scenes) or any(
+                    o.shape != (s.height, s.width, 4) or o.dtype != np.uint8 or
+                    not o.flags["C_CONTIGUOUS"] for o, s in zip(outs, scenes)):
+                raise ValueError("render_streams: out must hold one (height, width, 4) uint8 "
+                                 "C-contiguous array per scene")
         n = len(bufs)
         cbufs = [ctypes.create_string_buffer(b, len(b)) for b in bufs]
         ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(c) for c in cbufs])

@@ -10,8 +10,10 @@
 // (ImageFilterBase::BlurBitmapToCanvas, src/effect/image_filter.cc:184-194).
 #pragma once
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -1171,6 +1173,178 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     hb.passes.insert(hb.passes.end(), tpp.second.begin(), tpp.second.end());
     hb.canvases[tpp.first].pass1 = (uint32_t)hb.passes.size();
   }
+  return SKITY_CUDA_SUCCESS;
+}
+
+// Where a batch of canvases (built into an empty HostBatch) lands in a
+// larger one: the sizes of the larger batch's arrays before it, and its
+// first pixel byte.
+struct BatchBase {
+  size_t verbs = 0, pts = 0, weights = 0, draws = 0, passes = 0, brushes = 0, conicals = 0,
+         cf = 0, clip_states = 0, canvases = 0, stops = 0, temps = 0, mains = 0;
+  uint64_t px = 0;
+  // the base of the batch after `l`
+  BatchBase after(const HostBatch& l) const {
+    BatchBase n;
+    n.verbs = verbs + l.verbs.size();
+    n.pts = pts + l.pts.size();
+    n.weights = weights + l.weights.size();
+    n.draws = draws + l.draws.size();
+    n.passes = passes + l.passes.size();
+    n.brushes = brushes + l.brushes.size();
+    n.conicals = conicals + l.conicals.size();
+    n.cf = cf + l.cf_matrices.size();
+    n.clip_states = clip_states + l.clip_states.size();
+    n.canvases = canvases + l.canvases.size();
+    n.stops = stops + l.stop_colors.size();
+    n.temps = temps + l.temp_canvases.size();
+    n.mains = mains + l.main_canvases.size();
+    n.px = px + l.pixel_bytes;
+    return n;
+  }
+};
+
+// Copies batch `l` into `g` (arrays already sized for it) at base `b`,
+// moving every index and byte offset of `l` by the base: the result is the
+// batch AddStreamCanvas builds by adding l's canvases to g one after the
+// other.  b.px is 256-byte aligned, as AllocPixels places a canvas.
+inline void PlaceBatch(HostBatch& g, const HostBatch& l, const BatchBase& b) {
+  std::copy(l.verbs.begin(), l.verbs.end(), g.verbs.begin() + b.verbs);
+  std::copy(l.pts.begin(), l.pts.end(), g.pts.begin() + b.pts);
+  std::copy(l.weights.begin(), l.weights.end(), g.weights.begin() + b.weights);
+  std::copy(l.conicals.begin(), l.conicals.end(), g.conicals.begin() + b.conicals);
+  std::copy(l.cf_matrices.begin(), l.cf_matrices.end(), g.cf_matrices.begin() + b.cf);
+  std::copy(l.stop_colors.begin(), l.stop_colors.end(), g.stop_colors.begin() + b.stops);
+  std::copy(l.stop_offsets.begin(), l.stop_offsets.end(), g.stop_offsets.begin() + b.stops);
+  for (size_t i = 0; i < l.draws.size(); ++i) {
+    DrawDesc d = l.draws[i];
+    d.v0 += (uint32_t)b.verbs;
+    d.p0 += (uint32_t)b.pts;
+    d.w0 += (uint32_t)b.weights;
+    g.draws[b.draws + i] = d;
+  }
+  for (size_t i = 0; i < l.passes.size(); ++i) {
+    PassDesc p = l.passes[i];
+    p.draw += (uint32_t)b.draws;
+    p.canvas += (uint32_t)b.canvases;
+    if (!(p.flags & kPassClipPath)) p.brush += (uint32_t)b.brushes;  // a clip path's pass has none
+    if (p.path_clip) p.path_clip += (uint32_t)b.clip_states;
+    g.passes[b.passes + i] = p;
+  }
+  for (size_t i = 0; i < l.brushes.size(); ++i) {
+    Brush r = l.brushes[i];
+    if (r.kind == 1 || r.kind == 2 || r.kind == 4 || r.kind == 5) r.stop0 += (uint32_t)b.stops;
+    if (r.kind == 5) r.conical += (uint32_t)b.conicals;
+    if (r.kind == 3 || r.kind == 6) r.img_off += b.px;
+    if (r.cf_type == 2) r.cf_index += (uint32_t)b.cf;
+    g.brushes[b.brushes + i] = r;
+  }
+  for (size_t i = 0; i < l.clip_states.size(); ++i) {
+    ClipStateDesc c = l.clip_states[i];
+    if (c.parent) c.parent += (uint32_t)b.clip_states;
+    c.pass += (uint32_t)b.passes;
+    g.clip_states[b.clip_states + i] = c;
+  }
+  for (size_t i = 0; i < l.canvases.size(); ++i) {
+    CanvasDesc c = l.canvases[i];
+    c.px_off += b.px;
+    c.pass0 += (uint32_t)b.passes;
+    c.pass1 += (uint32_t)b.passes;
+    g.canvases[b.canvases + i] = c;
+  }
+  for (size_t i = 0; i < l.temp_canvases.size(); ++i) {  // temp canvases own all three buffers
+    const uint32_t t = l.temp_canvases[i];
+    CanvasDesc& c = g.canvases[b.canvases + t];
+    c.blur_off += b.px;
+    c.out_off += b.px;
+    g.temp_canvases[b.temps + i] = t + (uint32_t)b.canvases;
+  }
+  for (size_t i = 0; i < l.main_canvases.size(); ++i)
+    g.main_canvases[b.mains + i] = l.main_canvases[i] + (uint32_t)b.canvases;
+}
+
+// Parses `count` scene streams into `hb` (empty on entry), the canvases in
+// stream order.  The streams are cut into runs of consecutive canvases of
+// about equal bytes; host threads (up to `threads`) build the runs into
+// batches of their own, then copy them into `hb` at the places a one-thread
+// loop over AddStreamCanvas gives them, so `hb` is the batch that loop
+// builds.  Returns the first failing stream's status (in stream order), or
+// success.
+inline int32_t BuildStreams(HostBatch& hb, uint32_t count, const uint8_t* const* streams,
+                            const size_t* bytes, unsigned threads) {
+  auto add_range = [&](HostBatch& b, uint32_t i0, uint32_t i1) -> int32_t {
+    for (uint32_t i = i0; i < i1; ++i) {
+      StreamView sv;
+      if (!ParseStream(streams[i], bytes[i], &sv)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+      const int32_t rc = AddStreamCanvas(b, sv);
+      if (rc != SKITY_CUDA_SUCCESS) return rc;
+    }
+    return SKITY_CUDA_SUCCESS;
+  };
+  if (threads > count / 4) threads = count / 4;
+  if (threads < 2) return add_range(hb, 0, count);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < count; ++i) total += bytes[i] + 64;
+  // runs of about total / (4 * threads) bytes: the threads take them in
+  // order from a counter, so a heavy run does not hold the others up
+  const uint64_t target = total / (4 * (uint64_t)threads) + 1;
+  std::vector<uint32_t> cut{0};
+  uint64_t acc = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    acc += bytes[i] + 64;
+    if (acc >= target && i + 1 < count) {
+      cut.push_back(i + 1);
+      acc = 0;
+    }
+  }
+  cut.push_back(count);
+  const uint32_t runs = (uint32_t)cut.size() - 1;
+  std::vector<HostBatch> part(runs);
+  std::vector<int32_t> rc(runs, SKITY_CUDA_SUCCESS);
+  std::vector<BatchBase> base(runs);
+  auto parallel = [&](auto&& body) {
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+      for (uint32_t r; (r = next.fetch_add(1)) < runs;) body(r);
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+  };
+  parallel([&](uint32_t r) { rc[r] = add_range(part[r], cut[r], cut[r + 1]); });
+  for (uint32_t r = 0; r < runs; ++r)
+    if (rc[r] != SKITY_CUDA_SUCCESS) return rc[r];
+  BatchBase end;
+  for (uint32_t r = 0; r < runs; ++r) {
+    end.px = (end.px + 255) & ~uint64_t(255);  // every run starts with a canvas
+    base[r] = end;
+    end = end.after(part[r]);
+  }
+  hb.verbs.resize(end.verbs);
+  hb.pts.resize(end.pts);
+  hb.weights.resize(end.weights);
+  hb.draws.resize(end.draws);
+  hb.passes.resize(end.passes);
+  hb.brushes.resize(end.brushes);
+  hb.conicals.resize(end.conicals);
+  hb.cf_matrices.resize(end.cf);
+  hb.clip_states.resize(end.clip_states);
+  hb.canvases.resize(end.canvases);
+  hb.stop_colors.resize(end.stops);
+  hb.stop_offsets.resize(end.stops);
+  hb.temp_canvases.resize(end.temps);
+  hb.main_canvases.resize(end.mains);
+  parallel([&](uint32_t r) { PlaceBatch(hb, part[r], base[r]); });
+  for (uint32_t r = 0; r < runs; ++r) {
+    for (auto& u : part[r].image_uploads)
+      hb.image_uploads.push_back({u.off + base[r].px, std::move(u.bytes)});
+    hb.draw_count += part[r].draw_count;
+    hb.max_temp_w = std::max(hb.max_temp_w, part[r].max_temp_w);
+    hb.max_temp_h = std::max(hb.max_temp_h, part[r].max_temp_h);
+    hb.max_temp_style = std::max(hb.max_temp_style, part[r].max_temp_style);
+  }
+  hb.pixel_bytes = end.px;
   return SKITY_CUDA_SUCCESS;
 }
 

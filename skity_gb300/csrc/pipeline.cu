@@ -24,6 +24,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "device.h"
@@ -439,32 +440,31 @@ static int EnqueueDevice(DeviceBatch& db, const DevBatch& b, const DevPlan& q, u
 
 static void DropReplay(DeviceBatch& db);
 
-// Records the six parts of a device-planned render as replay graphs.
+// Records a device-planned render -- its six parts, every kernel of the
+// batch -- as one replay graph.  The stage events are event-record nodes of
+// the graph (recorded as the graph runs), so a replay keeps its per-stage
+// timings.
 static void CaptureDevice(skity_cuda_context_s* ctx, DeviceBatch& db, const DevBatch& b,
                           const DevPlan& q) {
   DropReplay(db);
   cudaStream_t s = ctx->stream;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
   bool ok = true;
   int launches = 0;
-  for (int part = 0; part < 6 && ok; ++part) {
-    cudaGraph_t g = nullptr;
-    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-      ok = false;
-      break;
-    }
+  for (int part = 0; part < 6; ++part) {
+    ok = ok && cudaEventRecordWithFlags(ctx->stage[2 * part], s, cudaEventRecordExternal) ==
+                   cudaSuccess;
     launches += EnqueueDevice(db, b, q, ctx->num_sms, s, part);
-    cudaError_t e = cudaStreamEndCapture(s, &g);
-    size_t nodes = 0;
-    if (e != cudaSuccess || !g) {
-      ok = false;
-    } else if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess && nodes > 0) {
-      if (cudaGraphInstantiate(&db.graphs[part], g, 0) != cudaSuccess) {
-        db.graphs[part] = nullptr;
-        ok = false;
-      }
-    }
-    if (g) cudaGraphDestroy(g);
+    ok = ok && cudaEventRecordWithFlags(ctx->stage[2 * part + 1], s, cudaEventRecordExternal) ==
+                   cudaSuccess;
   }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  ok = ok && e == cudaSuccess && g && cudaGraphInstantiate(&db.graphs[0], g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
   cudaGetLastError();
   if (!ok) {
     DropReplay(db);
@@ -497,14 +497,14 @@ static int32_t DeviceRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool tim
                         std::memcmp(&q, &db.graph_q, sizeof q) == 0;
     int launches = 0;
     SKC_TRY(cudaEventRecord(ctx->ev0, s));
-    for (int part = 0; part < 6; ++part) {
-      SKC_TRY(cudaEventRecord(ctx->stage[2 * part], s));
-      if (replay) {
-        if (db.graphs[part]) SKC_TRY(cudaGraphLaunch(db.graphs[part], s));
-      } else {
+    if (replay) {
+      SKC_TRY(cudaGraphLaunch(db.graphs[0], s));  // the stage events are nodes of the graph
+    } else {
+      for (int part = 0; part < 6; ++part) {
+        SKC_TRY(cudaEventRecord(ctx->stage[2 * part], s));
         launches += EnqueueDevice(db, b, q, ctx->num_sms, s, part);
+        SKC_TRY(cudaEventRecord(ctx->stage[2 * part + 1], s));
       }
-      SKC_TRY(cudaEventRecord(ctx->stage[2 * part + 1], s));
     }
     SKC_TRY(cudaEventRecord(ctx->ev1, s));
     SKC_TRY(cudaGetLastError());
@@ -861,15 +861,11 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   return SKITY_CUDA_SUCCESS;
 }
 
+// The streams are parsed on the host's threads (BuildStreams), at most 32.
 int32_t BuildFromStreams(DeviceBatch& db, uint32_t count, const uint8_t* const* streams,
                                 const size_t* bytes) {
-  for (uint32_t i = 0; i < count; ++i) {
-    StreamView sv;
-    if (!ParseStream(streams[i], bytes[i], &sv)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
-    int32_t rc = AddStreamCanvas(db.hb, sv);
-    if (rc != SKITY_CUDA_SUCCESS) return rc;
-  }
-  return SKITY_CUDA_SUCCESS;
+  const unsigned hw = std::thread::hardware_concurrency();
+  return BuildStreams(db.hb, count, streams, bytes, std::min(hw ? hw : 1u, 32u));
 }
 
 int32_t ReadCanvas(skity_cuda_context_s* ctx, DeviceBatch& db, uint32_t index, uint8_t* out,

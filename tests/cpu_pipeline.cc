@@ -262,3 +262,44 @@ extern "C" int64_t skc_cpu_fixed_div_check(const int32_t* numer, const int32_t* 
     if (denom[i] != 0 && FixedDiv(numer[i], denom[i]) != FixedDivWide(numer[i], denom[i])) ++bad;
   return bad;
 }
+
+// The threaded stream build (BuildStreams) against the one-thread loop on
+// the same streams: 0 when every array and counter of the two batches is
+// byte-identical, else the number of the first one that differs; negative:
+// the status of a failing build.
+template <typename T>
+static bool SameBytes(const std::vector<T>& a, const std::vector<T>& b) {
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+extern "C" int skc_build_streams_compare(uint32_t count, const uint8_t* const* streams,
+                                         const size_t* bytes, unsigned threads) {
+  HostBatch one, many;
+  int32_t rc1 = BuildStreams(one, count, streams, bytes, 1);
+  int32_t rc2 = BuildStreams(many, count, streams, bytes, threads);
+  if (rc1 != rc2) return 100;
+  if (rc1) return rc1;
+  if (!SameBytes(one.verbs, many.verbs)) return 1;
+  if (!SameBytes(one.pts, many.pts)) return 2;
+  if (!SameBytes(one.weights, many.weights)) return 3;
+  if (!SameBytes(one.draws, many.draws)) return 4;
+  if (!SameBytes(one.passes, many.passes)) return 5;
+  if (!SameBytes(one.brushes, many.brushes)) return 6;
+  if (!SameBytes(one.conicals, many.conicals)) return 7;
+  if (!SameBytes(one.cf_matrices, many.cf_matrices)) return 8;
+  if (!SameBytes(one.clip_states, many.clip_states)) return 9;
+  if (!SameBytes(one.canvases, many.canvases)) return 10;
+  if (!SameBytes(one.stop_colors, many.stop_colors)) return 11;
+  if (!SameBytes(one.stop_offsets, many.stop_offsets)) return 12;
+  if (!SameBytes(one.main_canvases, many.main_canvases)) return 13;
+  if (!SameBytes(one.temp_canvases, many.temp_canvases)) return 14;
+  if (one.pixel_bytes != many.pixel_bytes || one.draw_count != many.draw_count) return 15;
+  if (one.max_temp_w != many.max_temp_w || one.max_temp_h != many.max_temp_h ||
+      one.max_temp_style != many.max_temp_style)
+    return 16;
+  if (one.image_uploads.size() != many.image_uploads.size()) return 17;
+  for (size_t i = 0; i < one.image_uploads.size(); ++i)
+    if (one.image_uploads[i].off != many.image_uploads[i].off ||
+        !SameBytes(one.image_uploads[i].bytes, many.image_uploads[i].bytes))
+      return 18;
+  return 0;
+}
