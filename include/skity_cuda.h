@@ -226,20 +226,40 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas,
 SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
                                                    const skity_cuda_path* path,
                                                    const skity_cuda_paint* paint);
-/* Canvas::Save / Restore / Translate (include/skity/render/canvas.hpp):
- * the canvas matrix as a translation; later draws are recorded with it.
- * Other matrices (scale, rotation, skew) are not taken by this canvas. */
+/* Canvas::Save / Restore / Translate / Scale / Rotate / Skew / Concat /
+ * SetMatrix (include/skity/render/canvas.hpp:51-122; canvas.cc:70-123 ->
+ * LayerState, canvas_state.cc:18-46): the canvas matrix times the call's
+ * matrix (Matrix::operator*, matrix.cc:452-460), later draws recorded under
+ * it.  Rotation is about (px, py), in degrees (Matrix::RotateDeg,
+ * matrix.cc:28-53); Concat / SetMatrix take a row-major 3x3 as
+ * Matrix::Set9 does (scale x, skew x, translate x, skew y, scale y,
+ * translate y, perspective 0, 1, 2).  Paths are mapped by any affine
+ * matrix (fills and strokes, solid colours); shaders are taken under scale
+ * and translation; blurs, layers and path clips under a translation.
+ * Draws past those limits (and draws under perspective) return
+ * SKITY_CUDA_ERROR_NOT_SUPPORTED and draw nothing. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas);
 SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas);
 SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy);
+SKITY_CUDA_API int32_t skity_cuda_canvas_scale(skity_cuda_canvas canvas, float sx, float sy);
+SKITY_CUDA_API int32_t skity_cuda_canvas_rotate(skity_cuda_canvas canvas, float degrees, float px,
+                                                float py);
+SKITY_CUDA_API int32_t skity_cuda_canvas_skew(skity_cuda_canvas canvas, float sx, float sy);
+SKITY_CUDA_API int32_t skity_cuda_canvas_concat(skity_cuda_canvas canvas, const float m[9]);
+SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas canvas, const float m[9]);
+/* Canvas::GetTotalMatrix as Matrix::Get9 (matrix.cc:106-116) gives it. */
+SKITY_CUDA_API int32_t skity_cuda_canvas_get_matrix(skity_cuda_canvas canvas, float m[9]);
 /* Canvas::ClipRect(rect, ClipOp::kIntersect) (canvas.hpp; canvas.cc:130-135,
- * 463-476): the rect, mapped by the current translation, narrows the
- * canvas's global clip bounds (kept and restored by Save / Restore); later
- * DrawPath calls rasterise only inside them, as SWCanvas does for a
- * scale/translate matrix (sw_canvas.cc:279-295).  Clear is not clipped
- * (SWCanvas::OnDrawPaint rasterises the whole canvas).  kDifference and
- * ClipPath are not taken by this canvas; a blurred draw under a clip
- * returns SKITY_CUDA_ERROR_NOT_SUPPORTED. */
+ * 463-476): the rect, mapped by the canvas matrix (Matrix::MapRect, matrix.cc:
+ * 306-337), narrows the canvas's global clip bounds (kept and restored by
+ * Save / Restore); later DrawPath calls rasterise only inside them, as
+ * SWCanvas does for a scale/translate matrix (sw_canvas.cc:279-295).  Under
+ * a rotation or skew the reference also clips by the rect as a path, which
+ * is not taken: the call returns SKITY_CUDA_ERROR_NOT_SUPPORTED and the
+ * draws under it are refused.  Clear is not clipped (SWCanvas::OnDrawPaint
+ * rasterises the whole canvas); kDifference is a path clip of the rect
+ * (skity_cuda_canvas_clip_path); a blurred draw under a clip returns
+ * SKITY_CUDA_ERROR_NOT_SUPPORTED. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
                                                    float right, float bottom);
 /* Canvas::DrawImageRect(image, src, dst, sampling, paint) (canvas.hpp:342;

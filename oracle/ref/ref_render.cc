@@ -77,6 +77,7 @@ struct Scene {
     uint32_t blend, pad[2];
   };
   std::vector<Layer> layers;
+  std::vector<float> matrices;  // per draw (sx, kx, tx, ky, sy, ty), or empty
 };
 
 template <typename T>
@@ -155,6 +156,7 @@ bool Load(const char* path, Scene* s) {
     o += 4;
     Take(buf, o, s->layers, n_layers);
   }
+  if (flags & 32) Take(buf, o, s->matrices, 6 * size_t(nd));
   return o <= buf.size();
 }
 
@@ -368,7 +370,10 @@ int main(int argc, char** argv) {
   for (size_t i = 0; i < paths.size(); ++i) {
     layer_events(first + uint32_t(i));
     const PaintRec& pr = s.paints[first + i];
-    const bool moved = pr.translate[0] != 0.f || pr.translate[1] != 0.f;
+    const float* mx = s.matrices.empty() ? nullptr : s.matrices.data() + 6 * (first + i);
+    const bool concat = mx && !(mx[0] == 1.f && mx[1] == 0.f && mx[2] == 0.f && mx[3] == 0.f &&
+                                mx[4] == 1.f && mx[5] == 0.f);
+    const bool moved = concat || pr.translate[0] != 0.f || pr.translate[1] != 0.f;
     const float* c = s.clips.empty() ? nullptr : s.clips.data() + 4 * (first + i);
     const bool clipped =
         c && !(c[0] == -1e9f && c[1] == -1e9f && c[2] == 1e9f && c[3] == 1e9f);
@@ -378,7 +383,15 @@ int main(int argc, char** argv) {
     // the stored clip is already in device space: ClipRect before the
     // translation leaves exactly these global clip bounds
     if (clipped) canvas->ClipRect(skity::Rect::MakeLTRB(c[0], c[1], c[2], c[3]));
-    if (moved) canvas->Translate(pr.translate[0], pr.translate[1]);
+    if (concat) {
+      // Canvas::Concat onto the identity: the CTM becomes the matrix itself
+      const float nine[9] = {mx[0], mx[1], mx[2], mx[3], mx[4], mx[5], 0.f, 0.f, 1.f};
+      skity::Matrix m;
+      m.Set9(nine);
+      canvas->Concat(m);
+    } else if (moved) {
+      canvas->Translate(pr.translate[0], pr.translate[1]);
+    }
     canvas->DrawPath(paths[i], paints[i]);
     if (moved || clipped || cstate) canvas->Restore();
   }

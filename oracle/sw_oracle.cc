@@ -1937,6 +1937,9 @@ struct SceneView {
   };
   uint32_t n_layers = 0;
   const LayerRec* layers = nullptr;
+  // per-draw canvas matrices (sx, kx, tx, ky, sy, ty), or null: the paints'
+  // translations
+  const float* matrices = nullptr;
 };
 
 // The colour filter of the draw whose paint record is `p` (a record of s).
@@ -1967,7 +1970,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->has_clear = hdr[3];
   // 1: per-draw clip bounds, 2: per-draw colour filters, 4: path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~31u) return false;
+  if (flags & ~63u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -2041,7 +2044,50 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
       if (i + 1 < s->n_layers && (open || s->layers[i + 1].start < L.restore)) return false;
     }
   }
+  if (flags & 32) {
+    s->matrices = (const float*)at(24 * (size_t)s->nd);
+    for (uint32_t d = 0; d < s->nd && o <= len; ++d)
+      if (s->paints[d].translate[0] != 0.f || s->paints[d].translate[1] != 0.f) return false;
+  }
   return o <= len;
+}
+
+// The canvas matrix of draw d as (sx, kx, tx, ky, sy, ty).
+static void MatrixOf(const SceneView& s, uint32_t d, float m[6]) {
+  if (s.matrices) {
+    std::memcpy(m, s.matrices + 6 * (size_t)d, 24);
+  } else {
+    const float t[6] = {1.f, 0.f, s.paints[d].translate[0], 0.f, 1.f, s.paints[d].translate[1]};
+    std::memcpy(m, t, 24);
+  }
+}
+static bool IsTranslation(const float m[6]) {
+  return m[0] == 1.f && m[1] == 0.f && m[3] == 0.f && m[4] == 1.f;
+}
+
+// Draws this restatement does not take under a canvas matrix that is more
+// than a translation: blurs, layers, path clips, and shaders under a matrix
+// with rotation or skew (their device_to_local needs the general 4x4
+// inverse).  The GPU path refuses the same draws.
+static bool UnsupportedUnderMatrix(const SceneView& s) {
+  if (!s.matrices) return false;
+  for (uint32_t d = 0; d < s.nd; ++d) {
+    const float* m = s.matrices + 6 * (size_t)d;
+    const PaintRec& bp = s.paints[d];
+    if (bp.blur_style != 0 && bp.blur_radius > 0.f &&
+        !(IsTranslation(m) && m[2] == 0.f && m[5] == 0.f))
+      return true;  // a blur under any canvas matrix (as under a translation)
+    if (IsTranslation(m)) continue;
+    const PaintRec& p = s.paints[d];
+    if (s.draw_clip_state && s.draw_clip_state[d]) return true;
+    for (uint32_t i = 0; i < s.n_layers; ++i) {
+      const uint32_t end = s.layers[i].restore == 0xFFFFFFFFu ? s.nd : s.layers[i].restore;
+      if (d >= s.layers[i].start && d < end) return true;
+    }
+    const bool shaded = p.gradient >= 0 || (s.image_shaders && s.image_shaders[d].image);
+    if (shaded && (m[1] != 0.f || m[3] != 0.f)) return true;
+  }
+  return false;
 }
 
 // A blurred draw under a narrowed clip: the blur's temp canvas and its
@@ -2393,6 +2439,7 @@ int sko_render(const uint8_t* scene, size_t len, uint32_t first, uint32_t count,
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
   if (BlurUnderClip(s)) return -3;
+  if (UnsupportedUnderMatrix(s)) return -4;
   ClipStates clip_states;
   ComputeClipStates(s, &clip_states);
   s.clip_cache = &clip_states;
@@ -2432,6 +2479,7 @@ int sko_render_mt(const uint8_t* scene, size_t len, uint32_t first, uint32_t cou
   SceneView s;
   if (!ParseScene(scene, len, &s)) return -2;
   if (BlurUnderClip(s)) return -3;
+  if (UnsupportedUnderMatrix(s)) return -4;
   ClipStates clip_states;
   ComputeClipStates(s, &clip_states);
   s.clip_cache = &clip_states;

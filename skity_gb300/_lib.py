@@ -126,6 +126,13 @@ SIGNATURES = {
     "skity_cuda_canvas_save": (ctypes.c_int32, [_vp]),
     "skity_cuda_canvas_restore": (ctypes.c_int32, [_vp]),
     "skity_cuda_canvas_translate": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
+    "skity_cuda_canvas_scale": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
+    "skity_cuda_canvas_rotate": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
+                                                  ctypes.c_float]),
+    "skity_cuda_canvas_skew": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float]),
+    "skity_cuda_canvas_concat": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "skity_cuda_canvas_set_matrix": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "skity_cuda_canvas_get_matrix": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "skity_cuda_canvas_clip_rect": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
                                                      ctypes.c_float, ctypes.c_float]),
     "skity_cuda_canvas_clip_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.c_uint32]),

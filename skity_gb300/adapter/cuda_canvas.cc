@@ -32,15 +32,26 @@ static bool TranslationOf(const Matrix& m, float* tx, float* ty) {
 static void PathStorage(const Path& path, std::vector<uint8_t>* verbs, std::vector<float>* pts,
                         std::vector<float>* weights, skity_cuda_path* p);
 
+// The canvas matrix as Matrix::Get9 gives it, or false under perspective
+// (the C ABI canvas maps paths by affine matrices; the z terms meet z = 0).
+static bool AffineOf(const Matrix& m, float nine[9]) {
+  if (m.Get(3, 0) != 0.f || m.Get(3, 1) != 0.f || m.Get(3, 3) != 1.f) return false;
+  m.Get9(nine);
+  return true;
+}
+static bool IsIdentity9(const float n[9]) {
+  return n[0] == 1.f && n[1] == 0.f && n[2] == 0.f && n[3] == 0.f && n[4] == 1.f && n[5] == 0.f;
+}
+
 // Canvas::ClipRect has already narrowed the global clip bounds
-// (canvas.cc:130-135,463-476); for kIntersect under a translation that is
+// (canvas.cc:130-135,463-476); for kIntersect under scale and translation that is
 // all SWCanvas does too (sw_canvas.cc:279-295).  kDifference goes on as a
 // path clip of the rect (Canvas::OnClipRect, canvas.cc:144-150).
 void CUDACanvas::OnClipRect(Rect const& rect, ClipOp op) {
-  float tx = 0.f, ty = 0.f;
-  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
-    bad_clip_.back() = true;
-    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (!GetTotalMatrix().OnlyScaleAndTranslate()) {
+    // SWCanvas::OnClipRect clips by the rect as a path under any other
+    // matrix (sw_canvas.cc:305-309): OnClipPath takes it (or refuses it)
+    Canvas::OnClipRect(rect, op);
     return;
   }
   if (op != ClipOp::kIntersect) {
@@ -74,8 +85,8 @@ void CUDACanvas::OnClipPath(Path const& path, ClipOp op) {
 }
 
 void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
-  float tx = 0.f, ty = 0.f;
-  if (bad_clip_.back() || !TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+  float nine[9];
+  if (bad_clip_.back() || !AffineOf(GetTotalMatrix(), nine)) {
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     return;
   }
@@ -169,16 +180,21 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
     q.blur_radius = mf->GetBlurRadius();
   }
   // the C-ABI canvas holds no state between draws: each draw carries its
-  // device-space clip bounds (set before the translation, so they stay as
-  // they are) and its translation
+  // device-space clip bounds (set before the matrix, so they stay as they
+  // are) and the canvas matrix this canvas computed
   const Rect& clip = GetGlobalClipBounds();
   const bool clipped = !(clip.Left() == -1e9f && clip.Top() == -1e9f && clip.Right() == 1e9f &&
                          clip.Bottom() == 1e9f);
-  const bool moved = tx != 0.f || ty != 0.f;
+  const bool moved = !IsIdentity9(nine);
   if (moved || clipped) skity_cuda_canvas_save(canvas_);
   if (clipped)
     skity_cuda_canvas_clip_rect(canvas_, clip.Left(), clip.Top(), clip.Right(), clip.Bottom());
-  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  if (moved) skity_cuda_canvas_set_matrix(canvas_, nine);
+  if ((q.shader || q.image_shader) && !GetTotalMatrix().OnlyScaleAndTranslate()) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a shader's inverse past scale and translation
+    if (moved || clipped) skity_cuda_canvas_restore(canvas_);
+    return;
+  }
   status_ = skity_cuda_canvas_draw_path(canvas_, &p, &q);
   if (moved || clipped) skity_cuda_canvas_restore(canvas_);
 }
@@ -260,12 +276,12 @@ void CUDACanvas::OnDrawBlob(const TextBlob*, float, float, Paint const&) {
 }
 
 // Canvas::DrawImageRect / DrawImage of a pixmap image (SWCanvas::
-// OnDrawImageRect, sw_canvas.cc:641-677) under a translation: the pixels,
+// OnDrawImageRect, sw_canvas.cc:641-677) under the canvas matrix: the pixels,
 // src / dst and the paint's alpha and blend mode go to the C-ABI canvas.
 void CUDACanvas::OnDrawImageRect(std::shared_ptr<Image> image, const Rect& src, const Rect& dst,
                                  const SamplingOptions& sampling, Paint const* paint) {
-  float tx = 0.f, ty = 0.f;
-  if (bad_clip_.back() || !TranslationOf(GetTotalMatrix(), &tx, &ty) || !image) {
+  float nine[9];
+  if (bad_clip_.back() || !AffineOf(GetTotalMatrix(), nine) || !image) {
     status_ = image ? SKITY_CUDA_ERROR_NOT_SUPPORTED : SKITY_CUDA_SUCCESS;
     return;
   }
@@ -300,11 +316,16 @@ void CUDACanvas::OnDrawImageRect(std::shared_ptr<Image> image, const Rect& src, 
   const Rect& clip = GetGlobalClipBounds();
   const bool clipped = !(clip.Left() == -1e9f && clip.Top() == -1e9f && clip.Right() == 1e9f &&
                          clip.Bottom() == 1e9f);
-  const bool moved = tx != 0.f || ty != 0.f;
+  const bool moved = !IsIdentity9(nine);
   if (moved || clipped) skity_cuda_canvas_save(canvas_);
   if (clipped)
     skity_cuda_canvas_clip_rect(canvas_, clip.Left(), clip.Top(), clip.Right(), clip.Bottom());
-  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  if (moved) skity_cuda_canvas_set_matrix(canvas_, nine);
+  if (!GetTotalMatrix().OnlyScaleAndTranslate()) {
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;  // the pixmap brush's inverse past scale and translation
+    if (moved || clipped) skity_cuda_canvas_restore(canvas_);
+    return;
+  }
   status_ = skity_cuda_canvas_draw_image_rect(canvas_, &im, s4, d4, filter, &q);
   if (moved || clipped) skity_cuda_canvas_restore(canvas_);
 }

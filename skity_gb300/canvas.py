@@ -542,6 +542,36 @@ class Canvas:
         _lib.check(self.lib.skity_cuda_canvas_translate(self.handle, float(dx), float(dy)),
                    "skity_cuda_canvas_translate")
 
+    def Scale(self, sx, sy):
+        _lib.check(self.lib.skity_cuda_canvas_scale(self.handle, float(sx), float(sy)),
+                   "skity_cuda_canvas_scale")
+
+    def Rotate(self, degrees, px=0.0, py=0.0):
+        """Canvas::Rotate(degrees) / Rotate(degrees, px, py)."""
+        _lib.check(self.lib.skity_cuda_canvas_rotate(self.handle, float(degrees), float(px),
+                                                     float(py)), "skity_cuda_canvas_rotate")
+
+    def Skew(self, sx, sy):
+        _lib.check(self.lib.skity_cuda_canvas_skew(self.handle, float(sx), float(sy)),
+                   "skity_cuda_canvas_skew")
+
+    def Concat(self, m9):
+        """Canvas::Concat(matrix); m9 row-major as Matrix::Set9 takes it."""
+        m = (ctypes.c_float * 9)(*[float(v) for v in m9])
+        _lib.check(self.lib.skity_cuda_canvas_concat(self.handle, m), "skity_cuda_canvas_concat")
+
+    def SetMatrix(self, m9):
+        m = (ctypes.c_float * 9)(*[float(v) for v in m9])
+        _lib.check(self.lib.skity_cuda_canvas_set_matrix(self.handle, m),
+                   "skity_cuda_canvas_set_matrix")
+
+    def GetTotalMatrix(self):
+        """The canvas matrix as Matrix::Get9 gives it (row-major 3x3)."""
+        m = (ctypes.c_float * 9)()
+        _lib.check(self.lib.skity_cuda_canvas_get_matrix(self.handle, m),
+                   "skity_cuda_canvas_get_matrix")
+        return tuple(float(v) for v in m)
+
     def ClipPath(self, path: Path, op=1):
         """Canvas::ClipPath(path, op): op 0 kDifference, 1 kIntersect."""
         verbs = np.asarray(path.verbs, np.uint8)

@@ -111,6 +111,9 @@ struct StreamView {
   // layers when the stream has them
   uint32_t n_layers;
   const LayerRec* layers;
+  // per-draw canvas matrices (sx, kx, tx, ky, sy, ty) when the stream has
+  // them (the paints' translations are then zero), else null
+  const float* matrices;
 };
 
 // A ClipPath call of the stream: its parent state (1-based, 0: none), the
@@ -178,6 +181,25 @@ inline bool ValidTranslate(const float t[2], const float* pts, uint32_t np) {
   return true;
 }
 
+// A canvas matrix keeps the draw's points inside the coordinate range
+// ValidPath allows (points mapped as RastePath maps them; curves stay in
+// their control points' hull).
+inline bool ValidMatrix(const float m[6], const float* pts, uint32_t np) {
+  Xform xf;
+  xf.tx = m[2];
+  xf.ty = m[5];
+  xf.sx = m[0];
+  xf.kx = m[1];
+  xf.ky = m[3];
+  xf.sy = m[4];
+  xf.lin = true;
+  for (uint32_t i = 0; i < np; ++i) {
+    const P q = xf.map(mkP(pts[2 * i], pts[2 * i + 1]));
+    if (!(std::fabs(q.x) <= kMaxCoord && std::fabs(q.y) <= kMaxCoord)) return false;
+  }
+  return true;
+}
+
 // Clip bounds: finite floats (the empty rect (0, 0, 0, 0) included).
 inline bool ValidClip(const float c[4]) {
   return std::isfinite(c[0]) && std::isfinite(c[1]) && std::isfinite(c[2]) && std::isfinite(c[3]);
@@ -224,7 +246,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   // 1: per-draw clip bounds follow the stops; 2: then per-draw colour
   // filters; 4: then the path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~31u) return false;
+  if (flags & ~63u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -359,6 +381,14 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
         return false;
     }
   }
+  s->matrices = nullptr;
+  if (flags & 32) {
+    s->matrices = (const float*)at(24 * (size_t)s->nd);
+    if (o > len) return false;
+    for (uint32_t d = 0; d < s->nd; ++d)
+      for (int k = 0; k < 6; ++k)
+        if (!std::isfinite(s->matrices[6 * (size_t)d + k])) return false;
+  }
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
   for (uint32_t d = 0; d < s->nd; ++d) {
@@ -371,6 +401,12 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
       return false;
     if (!ValidTranslate(pr.translate, s->pts + 2 * (size_t)s->po[d], s->po[d + 1] - s->po[d]))
       return false;
+    if (s->matrices) {
+      if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return false;
+      if (!ValidMatrix(s->matrices + 6 * (size_t)d, s->pts + 2 * (size_t)s->po[d],
+                       s->po[d + 1] - s->po[d]))
+        return false;
+    }
     if (s->clips && !ValidClip(s->clips + 4 * (size_t)d)) return false;
     if (s->filters && !ValidColorFilter(s->filters[d])) return false;
     if (!ValidPath(s->verbs + s->vo[d], s->vo[d + 1] - s->vo[d], s->pts + 2 * (size_t)s->po[d],
@@ -483,18 +519,33 @@ inline ConicalParams ConicalSetup(const GradRec& g, const Mat4& device_to_local)
   return c;
 }
 
-// Matrix::Invert of a translate-only CTM (matrix.cc:134-142, 242-266)
-inline Mat4 InvertTranslate(float tx, float ty) {
-  Mat4 m = MatTranslate(tx, ty);
-  if (m.is_identity()) {
-    m.identity();
-    return m;
-  }
+// Matrix::Invert of a scale-and-translate canvas matrix m = (sx, 0, tx, 0,
+// sy, ty) (matrix.cc:134-142, 242-266): the identity for a matrix within
+// FLT_EPSILON of it; else the reciprocal scales (an infinite one leaves the
+// identity: Invert fails after Reset) and the translation times them.
+inline Mat4 InvertScaleTranslate(const float m[6]) {
+  Mat4 ctm = MatScale(m[0], m[4]);
+  ctm.e[3][0] = m[2];
+  ctm.e[3][1] = m[5];
   Mat4 inv;
   inv.identity();
-  inv.e[3][0] = -tx;
-  inv.e[3][1] = -ty;
+  if (ctm.is_identity()) return inv;
+  if (m[0] != 1.f || m[4] != 1.f) {
+    const float ix = 1.f / m[0], iy = 1.f / m[4];
+    if (ix == INFINITY || iy == INFINITY) return inv;
+    inv.e[0][0] = ix;
+    inv.e[1][1] = iy;
+    inv.e[3][0] = -m[2] * ix;
+    inv.e[3][1] = -m[5] * iy;
+  } else {
+    inv.e[3][0] = -m[2];
+    inv.e[3][1] = -m[5];
+  }
   return inv;
+}
+// The canvas matrix has a linear part (anything but a translation).
+inline bool HasLinear(const float m[6]) {
+  return !(m[0] == 1.f && m[1] == 0.f && m[3] == 0.f && m[4] == 1.f);
 }
 inline uint32_t SolidPM(const float c[4]) {
   return ColorToPMColor(Color4fToColor(c[0], c[1], c[2], c[3]));
@@ -633,9 +684,13 @@ inline bool FiltersColor(const StreamView& s, uint32_t d) {
 // clip_shift: the draw's clip bounds moved by (dx, dy) -- a draw inside a
 // layer, whose sub-canvas clips with the global clip bounds offset by the
 // layer's origin (SWCanvas::GetScanClipBounds, sw_canvas.hpp:157-161).
-inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
-                          uint32_t canvas, float tx, float ty, std::vector<PassDesc>& out,
-                          const float* clip_shift = nullptr) {
+// ctm: the canvas matrix (sx, kx, tx, ky, sy, ty); shaders are taken under
+// scale and translation (NOT_SUPPORTED under rotation or skew).
+inline int AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
+                         uint32_t canvas, const float ctm[6], std::vector<PassDesc>& out,
+                         const float* clip_shift = nullptr) {
+  const float tx = ctm[2], ty = ctm[5];
+  const bool lin = HasLinear(ctm);
   const PaintRec& pr = s.paints[d];
   const uint8_t* verbs = s.verbs + s.vo[d];
   uint32_t nv = s.vo[d + 1] - s.vo[d];
@@ -672,7 +727,7 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
         inv.e[3][1] = -lty;
       }
       Mat4 m = MatMul(MatMul(MatScale(1.f / (float)im.width, 1.f / (float)im.height), inv),
-                      InvertTranslate(tx, ty));
+                      InvertScaleTranslate(ctm));
       br.kind = 6;
       br.m[0] = m.e[0][0];
       br.m[1] = m.e[1][0];
@@ -689,7 +744,7 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     } else if (g) {
       // brush kinds: 1 linear, 2 radial, 4 sweep, 5 conical (3 is the image brush)
       br.kind = g->type <= 2 ? g->type : g->type + 1;
-      Mat4 dev_to_local = MatMul(MatTranslate(0, 0), InvertTranslate(tx, ty));
+      Mat4 dev_to_local = MatMul(MatTranslate(0, 0), InvertScaleTranslate(ctm));
       // PointsToUnit (sw_span_brush.cc:164-194): the sweep's is a translation
       // to its centre; the conical brush maps device_to_local and its own
       // transforms one after the other
@@ -747,6 +802,13 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     pd.cap_join = (pr.cap & 0xFF) | ((pr.join & 0xFF) << 8);
     pd.tx = tx;
     pd.ty = ty;
+    if (lin) {
+      pd.flags |= kPassMatrix;
+      pd.lin[0] = ctm[0];
+      pd.lin[1] = ctm[1];
+      pd.lin[2] = ctm[3];
+      pd.lin[3] = ctm[4];
+    }
     if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
       pd.clipped = 1;
       std::memcpy(pd.clip, s.clips + 4 * (size_t)d, sizeof pd.clip);
@@ -765,6 +827,8 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     DerivedCaps(pd.cap, stroke);
     out.push_back(pd);
   };
+  const bool shaded = (pr.gradient >= 0) || (s.image_shaders && s.image_shaders[d].image);
+  if (shaded && (ctm[1] != 0.f || ctm[3] != 0.f)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   bool need_fill = pr.style != 1, need_stroke = pr.style != 0;
   if (pr.style == 3) {
     if (need_stroke) add(true);
@@ -773,6 +837,7 @@ inline void AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32
     if (need_fill) add(false);
     if (need_stroke) add(true);
   }
+  return SKITY_CUDA_SUCCESS;
 }
 
 // Layers (Canvas::SaveLayer, canvas.cc:255-276 -> SWCanvas::OnSaveLayer,
@@ -1028,22 +1093,29 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
                                s.po[d + 1] - s.po[d], s.wts + s.wo[d], s.wo[d + 1] - s.wo[d]);
     hb.draw_count++;
     bool blur = pr.blur_style != 0 && pr.blur_radius > 0;  // MakeBlur(r <= 0) is null
+    // the draw's canvas matrix: the stream's, or the paint's translation
+    float ctm[6] = {1.f, 0.f, pr.translate[0], 0.f, 1.f, pr.translate[1]};
+    if (s.matrices) std::memcpy(ctm, s.matrices + 6 * (size_t)d, sizeof ctm);
+    const bool lin = HasLinear(ctm);
     if (layer) {
       // a draw inside the layer: the sub-canvas's transform
       // Translate(-origin) * CTM (sw_canvas.hpp:179-182), its clip moved by
-      // -origin; blurs and path clips inside layers are not taken
-      if (blur || path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+      // -origin; blurs, path clips and matrices past a translation inside
+      // layers are not taken
+      if (blur || path_clip || lin) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
       if (!ltemp) continue;  // an empty layer bitmap: nothing lands
       const float shift[2] = {-lg.off[0], -lg.off[1]};
-      AddDrawPasses(hb, s, d, draw, ltemp, pr.translate[0] + shift[0], pr.translate[1] + shift[1],
-                    temps[ltemp_slot].second, shift);
+      const float moved[6] = {1.f, 0.f, ctm[2] + shift[0], 0.f, 1.f, ctm[5] + shift[1]};
+      if (int rc = AddDrawPasses(hb, s, d, draw, ltemp, moved, temps[ltemp_slot].second, shift))
+        return rc;
       continue;
     }
     if (!blur) {
-      // the canvas translation goes where the reference's CopyWithMatrix
-      // and device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
+      // the canvas matrix goes where the reference's CopyWithMatrix and
+      // device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
+      if (path_clip && lin) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
       const size_t first_pass = main_passes.size();
-      AddDrawPasses(hb, s, d, draw, cidx, pr.translate[0], pr.translate[1], main_passes);
+      if (int rc = AddDrawPasses(hb, s, d, draw, cidx, ctm, main_passes)) return rc;
       if (path_clip) {  // DoBrush clips the raster's spans by the state (sw_canvas.cc:338-353)
         for (size_t q = first_pass; q < main_passes.size(); ++q) {
           main_passes[q].path_clip = state_base + path_clip;
@@ -1053,7 +1125,7 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       continue;
     }
     if (path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a blur under a path clip
-    if (pr.translate[0] != 0.f || pr.translate[1] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    if (lin || ctm[2] != 0.f || ctm[5] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (pr.blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
     // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
@@ -1105,7 +1177,8 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     hb.max_temp_h = std::max(hb.max_temp_h, fh);
     hb.max_temp_style = std::max<uint32_t>(hb.max_temp_style, pr.blur_style);
     std::vector<PassDesc> tp;
-    AddDrawPasses(hb, s, d, draw, tidx, -fl, -ft, tp);
+    const float to_temp[6] = {1.f, 0.f, -fl, 0.f, 1.f, -ft};
+    if (int rc = AddDrawPasses(hb, s, d, draw, tidx, to_temp, tp)) return rc;
     temps.emplace_back(tidx, std::move(tp));
     // DrawImage(blurred, filter_bounds, &paint) (sw_canvas.cc:641-677):
     // a rect path with a decal/nearest pixmap brush, alpha = paint alpha

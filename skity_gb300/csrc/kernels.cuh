@@ -16,7 +16,7 @@ struct PassDesc {
   uint32_t canvas;      // index into CanvasDesc
   uint32_t flags;       // kPassStroke | kPassEvenOdd | kPassSrcOver
   uint32_t cap_join;    // Paint::Cap | Paint::Join << 8
-  float tx, ty;         // translate applied to the path (blur temp canvases)
+  float tx, ty;         // translation of the canvas matrix the path is mapped by
   float stroke_width, miter;
   uint32_t ga;          // brush global alpha (spans with cover & ga == 0 are dropped)
   uint32_t brush;       // index into Brush
@@ -26,6 +26,7 @@ struct PassDesc {
   float clip[4];
   uint32_t path_clip;   // the path-clip state the draw is under (1-based; 0: none)
   uint32_t pad2;
+  float lin[4];         // kPassMatrix: sx, kx, ky, sy of the canvas matrix (tx, ty above)
 };
 // kPassRawSpans: the sweep stores the raster's spans as they are (any x,
 // zero coverage kept; ClipSpanRaw format) for the path-clip stages;
@@ -36,8 +37,22 @@ enum : uint32_t {
   kPassEvenOdd = 2,
   kPassSrcOver = 4,
   kPassRawSpans = 8,
-  kPassClipPath = 16
+  kPassClipPath = 16,
+  kPassMatrix = 32  // the canvas matrix has a linear part (PassDesc::lin)
 };
+
+// The canvas matrix a pass's path is mapped by.
+SKC_HD Xform PassXform(const PassDesc& pd) {
+  Xform x;
+  x.tx = pd.tx;
+  x.ty = pd.ty;
+  x.lin = (pd.flags & kPassMatrix) != 0;
+  x.sx = pd.lin[0];
+  x.kx = pd.lin[1];
+  x.ky = pd.lin[2];
+  x.sy = pd.lin[3];
+  return x;
+}
 
 // One Canvas::ClipPath call (SWCanvas::OnClipPath, sw_canvas.cc:317-336) on
 // top of its parent state; its span rows are computed on the device.

@@ -84,15 +84,16 @@ SKC_HDN void GeometryPass(const DevBatch& b, uint32_t p) {
     }
     quad = q2.view();
   }
+  const Xform xf = PassXform(pd);
   RasterBounds rb = pd.clipped
-                        ? ComputeBounds(quad, pd.tx, pd.ty, pd.clip[0], pd.clip[1], pd.clip[2], pd.clip[3])
-                        : ComputeBounds(quad, pd.tx, pd.ty);
+                        ? ComputeBounds(quad, xf, pd.clip[0], pd.clip[1], pd.clip[2], pd.clip[3])
+                        : ComputeBounds(quad, xf);
   if (rb.empty) {
     b.geom[p] = g;
     return;
   }
   Edge* edges = (Edge*)(base + L.off[12]);
-  int n = BuildEdges(quad, pd.tx, pd.ty, rb.st, rb.sb, edges, pd.cap[12]);
+  int n = BuildEdges(quad, xf, rb.st, rb.sb, edges, pd.cap[12]);
   g.need[12] = n;
   if (n > pd.cap[12]) {
     g.status = 1;

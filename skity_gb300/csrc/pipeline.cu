@@ -909,10 +909,10 @@ namespace skc {
 struct RecordedOp {
   enum Type : uint32_t {
     kClear, kDrawPath, kDrawImageRect, kSave, kRestore, kSaveLayer, kTranslate, kClipRect,
-    kClipPath
+    kClipPath, kScale, kRotate, kSkew, kConcat, kSetMatrix
   };
   Type type = kSave;
-  float f[8] = {};  // colour / bounds / translation / rect / src + dst
+  float f[9] = {};  // colour / bounds / translation / rect / src + dst / matrix
   uint32_t u = 0;   // ClipOp / image filter
   bool has_path = false;
   std::vector<uint8_t> verbs;
@@ -1030,11 +1030,38 @@ struct skity_cuda_canvas_s {
   std::vector<skc::PaintRec> paints;
   std::vector<skc::GradRec> grads;
   std::vector<float> stop_colors, stop_offsets;
-  // canvas matrix (a translation), global clip bounds and their save stack
+  // canvas matrix, global clip bounds and their save stack
   struct State {
-    float tx = 0.f, ty = 0.f;
+    skc::Mat4 m;  // the canvas matrix (LayerState::CurrentMatrix), column-major
     float clip[4] = {-1e9f, -1e9f, 1e9f, 1e9f};  // kMaxCullRect
     uint32_t path_clip = 0;  // the path-clip state (1-based in clip_states; 0: none)
+    // a ClipRect under a rotation or skew (a path clip of the rect in the
+    // reference, not taken here): draws under it are refused
+    bool bad_clip = false;
+    State() { m.identity(); }
+    float tx() const { return m.e[3][0]; }
+    float ty() const { return m.e[3][1]; }
+    // no perspective: CopyWithMatrix and MapRect then map points by
+    // (sx, kx, tx, ky, sy, ty) alone (the z terms meet z = 0)
+    bool affine() const { return m.e[0][3] == 0.f && m.e[1][3] == 0.f && m.e[3][3] == 1.f; }
+    void six(float out[6]) const {
+      out[0] = m.e[0][0];
+      out[1] = m.e[1][0];
+      out[2] = m.e[3][0];
+      out[3] = m.e[0][1];
+      out[4] = m.e[1][1];
+      out[5] = m.e[3][1];
+    }
+    bool translation() const {
+      return affine() && m.e[0][0] == 1.f && m.e[1][0] == 0.f && m.e[0][1] == 0.f &&
+             m.e[1][1] == 1.f;
+    }
+    // Matrix::OnlyScaleAndTranslate (matrix.cc:171-187), every term checked
+    bool scale_translate() const {
+      return affine() && m.e[0][2] == 0.f && m.e[1][2] == 0.f && m.e[2][2] == 1.f &&
+             m.e[3][2] == 0.f && m.e[2][0] == 0.f && m.e[2][1] == 0.f && m.e[2][3] == 0.f &&
+             m.e[1][0] == 0.f && m.e[0][1] == 0.f;
+    }
   };
   State st;
   std::vector<State> saved;
@@ -1054,6 +1081,10 @@ struct skity_cuda_canvas_s {
   std::vector<skc::ImageRec> images;
   std::vector<uint8_t> image_blob;
   std::vector<skc::ImageShaderRec> image_shaders;
+  // per recorded draw: its canvas matrix (sx, kx, tx, ky, sy, ty); written
+  // to the scene when a draw's matrix is more than a translation
+  std::vector<float> matrices;
+  bool any_matrix = false;
   skc::DeviceBatch db;
 };
 
@@ -1321,7 +1352,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
     paint.stroke_width = 1.f;
     paint.miter_limit = 4.f;
     const skity_cuda_canvas_s::State keep = canvas->st;
-    canvas->st.tx = canvas->st.ty = 0.f;
+    canvas->st.m.identity();
     canvas->st.clip[0] = canvas->st.clip[1] = -1e9f;
     canvas->st.clip[2] = canvas->st.clip[3] = 1e9f;
     const int32_t rc = skity_cuda_canvas_draw_path(canvas, &path, &paint);
@@ -1350,6 +1381,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
   canvas->any_clip = false;
   canvas->filters.clear();
   canvas->any_filter = false;
+  canvas->matrices.clear();
+  canvas->any_matrix = false;
   canvas->draw_clip_state.clear();
   canvas->images.clear();
   canvas->image_blob.clear();
@@ -1434,14 +1467,31 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   std::memcpy(pr.stroke_color, paint->stroke_color, 16);
   pr.stroke_width = paint->stroke_width;
   pr.miter = paint->miter_limit;
-  pr.translate[0] = canvas->st.tx;
-  pr.translate[1] = canvas->st.ty;
-  if (!skc::ValidTranslate(pr.translate, path->points, path->point_count))
+  // the canvas matrix: a translation goes in the paint record; anything
+  // more in the draw's matrix record
+  if (!canvas->st.affine() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  float ctm[6];
+  canvas->st.six(ctm);
+  const bool lin = !canvas->st.translation();
+  pr.translate[0] = lin ? 0.f : ctm[2];
+  pr.translate[1] = lin ? 0.f : ctm[5];
+  if (lin ? !skc::ValidMatrix(ctm, path->points, path->point_count)
+          : !skc::ValidTranslate(pr.translate, path->points, path->point_count))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   const bool clipped = !skc::IsNoClip(canvas->st.clip);
-  if ((canvas->st.tx != 0.f || canvas->st.ty != 0.f || clipped) && paint->blur_style != 0 &&
+  if ((lin || ctm[2] != 0.f || ctm[5] != 0.f || clipped) && paint->blur_style != 0 &&
       paint->blur_radius > 0.f)
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  // shaders under scale and translation only (their device_to_local is
+  // then the short inverse); no layers or path clips under more than a
+  // translation
+  if ((paint->shader || paint->image_shader) && !canvas->st.scale_translate())
+    return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (lin) {
+    if (canvas->st.path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    for (uint32_t l : canvas->saved_layer)
+      if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  }
   if (paint->shader) {
     const skity_cuda_gradient* g = paint->shader;
     if (!g->colors || (g->has_offsets && !g->offsets)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
@@ -1470,6 +1520,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   canvas->po.push_back((uint32_t)(canvas->pts.size() / 2));
   canvas->wo.push_back((uint32_t)canvas->wts.size());
   canvas->paints.push_back(pr);
+  canvas->matrices.insert(canvas->matrices.end(), ctm, ctm + 6);
+  canvas->any_matrix = canvas->any_matrix || lin;
   canvas->clips.insert(canvas->clips.end(), canvas->st.clip, canvas->st.clip + 4);
   canvas->any_clip = canvas->any_clip || clipped;
   skc::ColorFilterRec fr;
@@ -1639,11 +1691,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, co
     if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (paint && ((paint->blur_style != 0 && paint->blur_radius > 0.f) || paint->color_filter))
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (!canvas->st.translation() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   const bool empty = !(bounds[0] < bounds[2] && bounds[1] < bounds[3]);
   bool reject = empty;
   if (!empty) {  // QuickReject: the mapped bounds against the global clip bounds
-    const float x0 = bounds[0] + canvas->st.tx, x1 = bounds[2] + canvas->st.tx;
-    const float y0 = bounds[1] + canvas->st.ty, y1 = bounds[3] + canvas->st.ty;
+    const float x0 = bounds[0] + canvas->st.tx(), x1 = bounds[2] + canvas->st.tx();
+    const float y0 = bounds[1] + canvas->st.ty(), y1 = bounds[3] + canvas->st.ty();
     const float* c = canvas->st.clip;
     const float l = std::max(c[0], std::min(x0, x1)), r = std::min(c[2], std::max(x0, x1));
     const float t = std::max(c[1], std::min(y0, y1)), b = std::min(c[3], std::max(y0, y1));
@@ -1659,8 +1712,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, co
   skc::LayerRec L;
   std::memset(&L, 0, sizeof L);
   std::memcpy(L.bounds, bounds, sizeof L.bounds);
-  L.translate[0] = canvas->st.tx;
-  L.translate[1] = canvas->st.ty;
+  L.translate[0] = canvas->st.tx();
+  L.translate[1] = canvas->st.ty();
   std::memcpy(L.clip, canvas->st.clip, sizeof L.clip);
   L.start = (uint32_t)canvas->paints.size();
   L.restore = skc::kLayerOpen;
@@ -1674,21 +1727,84 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, co
   return skity_cuda_canvas_clip_rect(canvas, bounds[0], bounds[1], bounds[2], bounds[3]);
 }
 
-// The product of two translations: Translate(tx, ty) * Translate(dx, dy)
-// holds tx + dx in float (matrix.cc:452-460 with the zero terms exact).
-SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy) {
-  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
-  if (!std::isfinite(dx) || !std::isfinite(dy)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+// The canvas matrix times another (LayerState::Translate / Scale / Rotate
+// / Skew / Concat, canvas_state.cc:18-42: CurrentMatrix() * m through
+// Matrix::operator*, matrix.cc:452-460), or recorded as an op of a display
+// list.
+static int32_t CanvasConcat(skity_cuda_canvas canvas, skc::RecordedOp::Type type,
+                            const float* args, int nargs, const skc::Mat4& m) {
+  for (int i = 0; i < nargs; ++i)
+    if (!std::isfinite(args[i])) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (canvas->recording) {
     skc::RecordedOp op;
-    op.type = skc::RecordedOp::kTranslate;
-    op.f[0] = dx;
-    op.f[1] = dy;
+    op.type = type;
+    std::memcpy(op.f, args, sizeof(float) * nargs);
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
-  canvas->st.tx = canvas->st.tx + dx;
-  canvas->st.ty = canvas->st.ty + dy;
+  canvas->st.m = skc::MatMul(canvas->st.m, m);
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_translate(skity_cuda_canvas canvas, float dx, float dy) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  const float a[2] = {dx, dy};
+  return CanvasConcat(canvas, skc::RecordedOp::kTranslate, a, 2, skc::MatTranslate(dx, dy));
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_scale(skity_cuda_canvas canvas, float sx, float sy) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  const float a[2] = {sx, sy};
+  return CanvasConcat(canvas, skc::RecordedOp::kScale, a, 2, skc::MatScale(sx, sy));
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_rotate(skity_cuda_canvas canvas, float degrees, float px,
+                                                float py) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  const float a[3] = {degrees, px, py};
+  for (float v : a)
+    if (!std::isfinite(v)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  return CanvasConcat(canvas, skc::RecordedOp::kRotate, a, 3, skc::MatRotateDeg(degrees, px, py));
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_skew(skity_cuda_canvas canvas, float sx, float sy) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  const float a[2] = {sx, sy};
+  return CanvasConcat(canvas, skc::RecordedOp::kSkew, a, 2, skc::MatSkew(sx, sy));
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_concat(skity_cuda_canvas canvas, const float m[9]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  for (int i = 0; i < 9; ++i)
+    if (!std::isfinite(m[i])) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  return CanvasConcat(canvas, skc::RecordedOp::kConcat, m, 9, skc::MatFrom9(m));
+}
+
+// Canvas::SetMatrix (LayerState::SetMatrix: the matrix replaces the current one).
+SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas canvas, const float m[9]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  for (int i = 0; i < 9; ++i)
+    if (!std::isfinite(m[i])) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kSetMatrix;
+    std::memcpy(op.f, m, sizeof(float) * 9);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
+  canvas->st.m = skc::MatFrom9(m);
+  return SKITY_CUDA_SUCCESS;
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_get_matrix(skity_cuda_canvas canvas, float m[9]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  const skc::Mat4& a = canvas->st.m;  // Matrix::Get9 (matrix.cc:106-116)
+  const float v[9] = {a.e[0][0], a.e[1][0], a.e[3][0], a.e[0][1], a.e[1][1],
+                      a.e[3][1], a.e[0][3], a.e[1][3], a.e[3][3]};
+  std::memcpy(m, v, sizeof v);
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -1727,7 +1843,9 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
     canvas->ops.push_back(std::move(rop));
     return SKITY_CUDA_SUCCESS;
   }
-  float t[2] = {canvas->st.tx, canvas->st.ty};
+  // path clips under a translation only
+  if (!canvas->st.translation() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  float t[2] = {canvas->st.tx(), canvas->st.ty()};
   if (!skc::ValidTranslate(t, path->points, path->point_count)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   if (op == 1) {
     // the path's bounds: its points but a trailing move
@@ -1757,8 +1875,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
   c.nv = path->verb_count;
   c.np = path->point_count;
   c.nw = path->conic_weight_count;
-  c.translate[0] = canvas->st.tx;
-  c.translate[1] = canvas->st.ty;
+  c.translate[0] = canvas->st.tx();
+  c.translate[1] = canvas->st.ty();
   std::memcpy(c.bounds, canvas->st.clip, sizeof c.bounds);
   canvas->clip_states.push_back(c);
   canvas->clip_verbs.insert(canvas->clip_verbs.end(), path->verbs, path->verbs + path->verb_count);
@@ -1790,11 +1908,37 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, flo
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
+  // the global clip bounds narrowed by the mapped rect (Canvas::
+  // CalculateGlobalClipBounds, canvas.cc:463-476; Matrix::MapRect,
+  // matrix.cc:306-337: the corners mapped, w = 1, their min and max).  Under
+  // a rotation or skew SWCanvas::OnClipRect clips by the rect as a path
+  // (sw_canvas.cc:297-313), which is not taken: later draws are refused.
+  if (!canvas->st.affine()) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  const bool st_ok = canvas->st.scale_translate();
+  float m6[6];
+  canvas->st.six(m6);
+  skc::Xform xf;
+  xf.sx = m6[0];
+  xf.kx = m6[1];
+  xf.tx = m6[2];
+  xf.ky = m6[3];
+  xf.sy = m6[4];
+  xf.ty = m6[5];
+  xf.lin = !canvas->st.translation();
+  const skc::P q[4] = {xf.map(skc::mkP(left, top)), xf.map(skc::mkP(right, top)),
+                       xf.map(skc::mkP(right, bottom)), xf.map(skc::mkP(left, bottom))};
+  float ml = q[0].x, mr = q[0].x, mt = q[0].y, mb = q[0].y;
+  for (int i = 1; i < 4; ++i) {
+    ml = std::min(q[i].x, ml);
+    mr = std::max(q[i].x, mr);
+    mt = std::min(q[i].y, mt);
+    mb = std::max(q[i].y, mb);
+  }
   float* c = canvas->st.clip;
-  const float x0 = left + canvas->st.tx, x1 = right + canvas->st.tx;
-  const float y0 = top + canvas->st.ty, y1 = bottom + canvas->st.ty;
-  const float l = std::max(c[0], std::min(x0, x1)), r = std::min(c[2], std::max(x0, x1));
-  const float t = std::max(c[1], std::min(y0, y1)), b = std::min(c[3], std::max(y0, y1));
+  // Rect::Intersect (rect.cc:160-172)
+  const float l = std::max(c[0], ml), r = std::min(c[2], mr);
+  const float t = std::max(c[1], mt), b = std::min(c[3], mb);
+  if (!st_ok) canvas->st.bad_clip = true;
   if (!(l < r && t < b)) {
     c[0] = c[1] = c[2] = c[3] = 0.f;
   } else {
@@ -1803,7 +1947,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, flo
     c[2] = r;
     c[3] = b;
   }
-  return SKITY_CUDA_SUCCESS;
+  return st_ok ? SKITY_CUDA_SUCCESS : SKITY_CUDA_ERROR_NOT_SUPPORTED;
 }
 
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
@@ -1857,6 +2001,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
     sv.n_layers = (uint32_t)canvas->layers.size();
     sv.layers = canvas->layers.data();
   }
+  sv.matrices = canvas->any_matrix ? canvas->matrices.data() : nullptr;
   skc::DeviceBatch& db = canvas->db;
   db.hb = skc::HostBatch();
   int32_t rc = skc::AddStreamCanvas(db.hb, sv);
@@ -1895,6 +2040,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
   canvas->any_clip = false;
   canvas->filters.clear();
   canvas->any_filter = false;
+  canvas->matrices.clear();
+  canvas->any_matrix = false;
   canvas->draw_clip_state.clear();
   canvas->images.clear();
   canvas->image_blob.clear();
@@ -1985,6 +2132,21 @@ SKITY_CUDA_API int32_t skity_cuda_display_list_draw(skity_cuda_display_list list
       case skc::RecordedOp::kTranslate:
         rc = skity_cuda_canvas_translate(canvas, op.f[0], op.f[1]);
         break;
+      case skc::RecordedOp::kScale:
+        rc = skity_cuda_canvas_scale(canvas, op.f[0], op.f[1]);
+        break;
+      case skc::RecordedOp::kRotate:
+        rc = skity_cuda_canvas_rotate(canvas, op.f[0], op.f[1], op.f[2]);
+        break;
+      case skc::RecordedOp::kSkew:
+        rc = skity_cuda_canvas_skew(canvas, op.f[0], op.f[1]);
+        break;
+      case skc::RecordedOp::kConcat:
+        rc = skity_cuda_canvas_concat(canvas, op.f);
+        break;
+      case skc::RecordedOp::kSetMatrix:
+        rc = skity_cuda_canvas_set_matrix(canvas, op.f);
+        break;
       case skc::RecordedOp::kClipRect:
         rc = skity_cuda_canvas_clip_rect(canvas, op.f[0], op.f[1], op.f[2], op.f[3]);
         break;
@@ -2015,7 +2177,7 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
   const uint32_t nd = (uint32_t)c.paints.size();
   const uint32_t flags = (c.any_clip ? 1u : 0u) | (c.any_filter ? 2u : 0u) |
                          (!c.clip_states.empty() ? 4u : 0u) | (!c.images.empty() ? 8u : 0u) |
-                         (!c.layers.empty() ? 16u : 0u);
+                         (!c.layers.empty() ? 16u : 0u) | (c.any_matrix ? 32u : 0u);
   out.clear();
   out.insert(out.end(), {'S', 'K', 'S', 'C'});
   const uint32_t hdr[7] = {1u, c.width, c.height, c.has_clear ? 1u : 0u, flags, 0u, 0u};
@@ -2032,7 +2194,14 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
   Pad4(out, c.verbs.size());
   Put(out, c.pts.data(), c.pts.size());
   Put(out, c.wts.data(), c.wts.size());
-  Put(out, c.paints.data(), c.paints.size());
+  if (flags & 32) {  // the translations are in the matrix records
+    for (skc::PaintRec pr : c.paints) {
+      pr.translate[0] = pr.translate[1] = 0.f;
+      Put(out, &pr, 1);
+    }
+  } else {
+    Put(out, c.paints.data(), c.paints.size());
+  }
   Put(out, c.grads.data(), c.grads.size());
   Put(out, c.stop_colors.data(), c.stop_colors.size());
   Put(out, c.stop_offsets.data(), c.stop_offsets.size());
@@ -2063,6 +2232,7 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
     Put(out, &n, 1);
     Put(out, c.layers.data(), c.layers.size());
   }
+  if (flags & 32) Put(out, c.matrices.data(), c.matrices.size());
 }
 
 }  // namespace

@@ -214,10 +214,25 @@ struct RasterBounds {
   float l, t, r, b;      // floor/ceil of the path bounds (bounds_)
   float sl, st, sr, sb;  // scan bounds
 };
+// The canvas matrix RastePath maps the quadified path by
+// (Path::CopyWithMatrix, path.cc:1274-1294, sw_raster.cc:740): glm's
+// mat4 * vec4 sums the columns as (m0 x + m1 y) + (m2 0 + m3 1), which is
+// (sx x + kx y) + tx in each row.  A translation (lin false) maps
+// x -> x + tx: its (1 x + 0 y) is x exactly.
+struct Xform {
+  float tx, ty;
+  float sx, kx, ky, sy;  // the linear part (lin)
+  bool lin;
+  SKC_HD P map(P p) const {
+    if (!lin) return mkP(p.x + tx, p.y + ty);
+    return mkP((sx * p.x + kx * p.y) + tx, (ky * p.x + sy * p.y) + ty);
+  }
+};
+
 // The clip bounds (cl, ct, cr, cb) are the canvas's global clip bounds:
 // kMaxCullRect (+-1e9, include/skity/render/canvas.hpp:26) unless a
 // ClipRect narrowed them.
-SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty, float cl = -1e9f,
+SKC_HD RasterBounds ComputeBounds(const PathView& q, const Xform& xf, float cl = -1e9f,
                                   float ct = -1e9f, float cr = 1e9f, float cb = 1e9f) {
   RasterBounds rb;
   rb.empty = true;
@@ -225,9 +240,11 @@ SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty, float c
   int n = q.np;
   if (q.nv > 1 && q.verbs[q.nv - 1] == kMove) n--;
   if (n <= 0) return rb;
-  float l = q.pts[0].x + tx, t = q.pts[0].y + ty, r = l, b = t;
+  const P p0 = xf.map(q.pts[0]);
+  float l = p0.x, t = p0.y, r = l, b = t;
   for (int i = 1; i < n; ++i) {
-    float x = q.pts[i].x + tx, y = q.pts[i].y + ty;
+    const P pi = xf.map(q.pts[i]);
+    const float x = pi.x, y = pi.y;
     l = min_(l, x);
     r = max_(r, x);
     t = min_(t, y);
@@ -254,16 +271,15 @@ SKC_HD RasterBounds ComputeBounds(const PathView& q, float tx, float ty, float c
 }
 
 // SWEdgeBuilder::BuildEdges over PathEdgeIter (sw_edge.cc:299-336,
-// src/graphic/path_priv.hpp:75-170).  Points are translated by (tx, ty)
-// first: Path::CopyWithMatrix(Translate) computes (1*x + 0*y) + (0*0 + tx*1),
-// which is x + tx exactly.  Returns the number of edges (may exceed cap:
-// only cap are stored).
-SKC_HDN int BuildEdges(const PathView& q, float tx, float ty, float top, float bottom,
+// src/graphic/path_priv.hpp:75-170).  Points are mapped by the canvas
+// matrix first (Xform).  Returns the number of edges (may exceed cap: only
+// cap are stored).
+SKC_HDN int BuildEdges(const PathView& q, const Xform& xf, float top, float bottom,
                        Edge* out, int cap) {
   int n = 0;
   int vi = 0, pi = 0, move_to = 0;
   bool needs_close = false;
-  auto T = [&](int i) { return mkP(q.pts[i].x + tx, q.pts[i].y + ty); };
+  auto T = [&](int i) { return xf.map(q.pts[i]); };
   auto add_line = [&](P a, P b) {
     Edge e;
     if (SetLine(&e, a, b) && !CanBeIgnored(top, bottom, e.upper_y, e.lower_y)) {

@@ -80,6 +80,74 @@ SKC_HD Mat4 MatTranslate(float tx, float ty) {
   m.e[3][1] = ty;
   return m;
 }
+// Matrix::Skew(sx, sy) (include/skity/geometry/matrix.hpp:30-35)
+SKC_HD Mat4 MatSkew(float kx, float ky) {
+  Mat4 m;
+  m.identity();
+  m.e[1][0] = kx;
+  m.e[0][1] = ky;
+  return m;
+}
+// Matrix::Set9 (matrix.cc:96-104): a row-major 3x3 (scale x, skew x,
+// translate x, skew y, scale y, translate y, perspective 0, 1, 2) into the
+// column-major 4x4.
+SKC_HD Mat4 MatFrom9(const float b[9]) {
+  Mat4 m;
+  m.identity();
+  m.e[0][0] = b[0];
+  m.e[0][1] = b[3];
+  m.e[0][3] = b[6];
+  m.e[1][0] = b[1];
+  m.e[1][1] = b[4];
+  m.e[1][3] = b[7];
+  m.e[3][0] = b[2];
+  m.e[3][1] = b[5];
+  m.e[3][3] = b[8];
+  return m;
+}
+// glm's mat4 product with no identity shortcut (what glm::rotate(...) * d1
+// computes: columns summed left to right).
+SKC_HD Mat4 MatMulPlain(const Mat4& a, const Mat4& b) {
+  Mat4 r;
+  for (int j = 0; j < 4; ++j)
+    for (int k = 0; k < 4; ++k) {
+      float v = a.e[0][k] * b.e[j][0];
+      v = v + a.e[1][k] * b.e[j][1];
+      v = v + a.e[2][k] * b.e[j][2];
+      v = v + a.e[3][k] * b.e[j][3];
+      r.e[j][k] = v;
+    }
+  return r;
+}
+// Matrix::RotateDeg(deg, (px, py)) (matrix.cc:28-53): radians = deg times
+// pi / 180 in float (FloatDegreesToRadians, scalar.hpp:101-103), then
+// glm::rotate(Translate(px, py), rad, (0, 0, 1)) * Translate(-px, -py).
+// glm::rotate builds the rotation about the normalised axis from cos and
+// sin and right-multiplies its upper 3x3 into the matrix's first three
+// columns, keeping the fourth.
+SKC_HD Mat4 MatRotateDeg(float deg, float px, float py) {
+  const float rad = deg * (float)0.01745329251994329576923690768489;
+  const float c = cosf(rad), s = sinf(rad);
+  const float ax[3] = {0.f, 0.f, 1.f};  // (0, 0, 1) normalised is itself
+  const float tmp[3] = {(1.f - c) * ax[0], (1.f - c) * ax[1], (1.f - c) * ax[2]};
+  float rot[3][3];
+  rot[0][0] = c + tmp[0] * ax[0];
+  rot[0][1] = tmp[0] * ax[1] + s * ax[2];
+  rot[0][2] = tmp[0] * ax[2] - s * ax[1];
+  rot[1][0] = tmp[1] * ax[0] - s * ax[2];
+  rot[1][1] = c + tmp[1] * ax[1];
+  rot[1][2] = tmp[1] * ax[2] + s * ax[0];
+  rot[2][0] = tmp[2] * ax[0] + s * ax[1];
+  rot[2][1] = tmp[2] * ax[1] - s * ax[0];
+  rot[2][2] = c + tmp[2] * ax[2];
+  const Mat4 d2 = MatTranslate(px, py);
+  Mat4 r;
+  for (int j = 0; j < 3; ++j)
+    for (int k = 0; k < 4; ++k)
+      r.e[j][k] = (d2.e[0][k] * rot[j][0] + d2.e[1][k] * rot[j][1]) + d2.e[2][k] * rot[j][2];
+  for (int k = 0; k < 4; ++k) r.e[3][k] = d2.e[3][k];
+  return MatMulPlain(r, MatTranslate(-px, -py));
+}
 SKC_HD P MatMapPoint(const Mat4& m, P p) {  // mat4 * (x, y, 0, 1)
   float rx = (m.e[0][0] * p.x + m.e[1][0] * p.y) + (m.e[2][0] * 0.f + m.e[3][0] * 1.f);
   float ry = (m.e[0][1] * p.x + m.e[1][1] * p.y) + (m.e[2][1] * 0.f + m.e[3][1] * 1.f);

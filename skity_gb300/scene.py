@@ -65,6 +65,8 @@ FLAG_FILTERS = 2  # the per-draw colour-filter section is present
 FLAG_PATH_CLIPS = 4  # the clip-state table and per-draw clip states are present
 FLAG_IMAGES = 8  # the image table, its pixels and the per-draw image shaders are present
 FLAG_LAYERS = 16  # the layer table (Canvas::SaveLayer ... Restore) is present
+FLAG_MATRICES = 32  # the per-draw canvas matrix section is present
+IDENTITY6 = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0)  # (sx, kx, tx, ky, sy, ty)
 # layer record: Canvas::SaveLayer(bounds, paint) under the canvas translation
 # and global clip bounds in effect before the call; draws [start, restore)
 # are drawn into the layer, which is composited onto the canvas (DrawImage of
@@ -165,6 +167,10 @@ class Scene:
     # images: (IMAGE_DTYPE records, pixel blob u8, per-draw IMAGE_SHADER_DTYPE), or None
     images: tuple | None = None
     layers: np.ndarray | None = None  # LAYER_DTYPE records, or None
+    # (n_draws, 6) float32 canvas matrices (sx, kx, tx, ky, sy, ty: the
+    # Matrix::Get9 order without the perspective row), or None: each draw's
+    # matrix is its paint's translation
+    matrices: np.ndarray | None = None
 
     @property
     def n_draws(self) -> int:
@@ -176,7 +182,8 @@ class Scene:
             (FLAG_FILTERS if self.filters is not None else 0) | \
             (FLAG_PATH_CLIPS if self.path_clips is not None else 0) | \
             (FLAG_IMAGES if self.images is not None else 0) | \
-            (FLAG_LAYERS if self.layers is not None else 0)
+            (FLAG_LAYERS if self.layers is not None else 0) | \
+            (FLAG_MATRICES if self.matrices is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -229,6 +236,10 @@ class Scene:
             lay = np.ascontiguousarray(self.layers, LAYER_DTYPE)
             out.append(struct.pack("<I", len(lay)))
             out.append(lay.tobytes())
+        if self.matrices is not None:
+            m = np.ascontiguousarray(self.matrices, np.float32).reshape(-1, 6)
+            assert len(m) == nd
+            out.append(m.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -279,8 +290,10 @@ class Scene:
         if flags & FLAG_LAYERS:
             (n_layers,) = struct.unpack_from("<I", buf, o); o += 4
             layers = take(LAYER_DTYPE, n_layers)
+        matrices = take(np.float32, 6 * nd, (nd, 6)) if flags & FLAG_MATRICES else None
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
-                     paints, grads, sc, so, clips, filters, path_clips, images, layers)
+                     paints, grads, sc, so, clips, filters, path_clips, images, layers,
+                     matrices)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -315,7 +328,8 @@ class Scene:
                      self.path_clips[:4] + (self.path_clips[4][first:last].copy(),),
                      None if self.images is None else
                      self.images[:2] + (self.images[2][first:last].copy(),),
-                     self._subset_layers(first, last))
+                     self._subset_layers(first, last),
+                     None if self.matrices is None else self.matrices[first:last].copy())
 
     def _subset_layers(self, first: int, last: int):
         """The layers of draws [first, last): those restored before `first`
@@ -372,6 +386,7 @@ class SceneBuilder:
         self._cstate, self._csaved, self._draw_cstate = 0, [], []
         self._images, self._blobs, self._nblob, self._shaders = [], [], 0, []
         self._layers = []
+        self._matrices = []
 
     def add_gradient(self, kind, p0, p1, radius, colors, offsets=None,
                      tile_mode=TILE_CLAMP) -> int:
@@ -425,11 +440,17 @@ class SceneBuilder:
                        color_filter=color_filter, image_shader=rec)
 
     def draw_path(self, verbs, points, paint, weights=(), clip=None, color_filter=None,
-                  image_shader=None):
+                  image_shader=None, matrix=None):
         """`clip`: device-space clip bounds (l, t, r, b) in effect for the
         draw (see map_clip); None: the canvas's initial bounds.
         `color_filter`: a FILTER_DTYPE record, or None.
-        `image_shader`: an IMAGE_SHADER_DTYPE record (image_shader()), or None."""
+        `image_shader`: an IMAGE_SHADER_DTYPE record (image_shader()), or None.
+        `matrix`: the canvas matrix of the draw (sx, kx, tx, ky, sy, ty), in
+        place of the paint's translation (which must then be zero); None: the
+        translation."""
+        if matrix is not None:
+            assert tuple(paint["translate"]) == (0.0, 0.0)
+        self._matrices.append(None if matrix is None else tuple(float(np.float32(v)) for v in matrix))
         verbs = np.asarray(verbs, np.uint8)
         points = np.asarray(points, np.float32).reshape(-1, 2)
         self._verbs.append(verbs); self._pts.append(points)
@@ -501,12 +522,22 @@ class SceneBuilder:
 
     def build(self) -> Scene:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
+        paints = (np.array(self._paints, PAINT_DTYPE) if self._paints
+                  else np.zeros(0, PAINT_DTYPE))
+        matrices = None
+        if any(m is not None for m in self._matrices):
+            # every draw's matrix in the section; the paints' translations move there
+            matrices = np.array([m if m is not None else
+                                 (1.0, 0.0, float(p["translate"][0]), 0.0, 1.0,
+                                  float(p["translate"][1]))
+                                 for m, p in zip(self._matrices, paints)], np.float32)
+            paints["translate"] = 0.0
         return Scene(self.width, self.height, self.clear,
                      cat(self._verbs, np.uint8, 0), cat(self._pts, np.float32, (0, 2)),
                      cat(self._wts, np.float32, 0),
                      np.asarray(self._vo, np.uint32), np.asarray(self._po, np.uint32),
                      np.asarray(self._wo, np.uint32),
-                     np.array(self._paints, PAINT_DTYPE) if self._paints else np.zeros(0, PAINT_DTYPE),
+                     paints,
                      np.array(self._grads, GRADIENT_DTYPE) if self._grads else np.zeros(0, GRADIENT_DTYPE),
                      cat(self._sc, np.float32, (0, 4)), cat(self._so, np.float32, 0),
                      (np.array(self._clips, np.float32).reshape(-1, 4)
@@ -520,7 +551,8 @@ class SceneBuilder:
                      ((np.array(self._images, IMAGE_DTYPE), cat(self._blobs, np.uint8, 0),
                        np.array(self._shaders, IMAGE_SHADER_DTYPE))
                       if self._images else None),
-                     np.array(self._layers, LAYER_DTYPE) if self._layers else None)
+                     np.array(self._layers, LAYER_DTYPE) if self._layers else None,
+                     matrices)
 
 
 def image_shader(image, filter=FILTER_NEAREST, tile_x=TILE_CLAMP, tile_y=TILE_CLAMP,

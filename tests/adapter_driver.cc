@@ -73,6 +73,12 @@ int32_t skity_cuda_canvas_translate(skity_cuda_canvas, float dx, float dy) {
   std::printf("translate %g %g\n", dx, dy);
   return SKITY_CUDA_SUCCESS;
 }
+int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas, const float m[9]) {
+  std::printf("set_matrix");
+  for (int i = 0; i < 9; ++i) std::printf(" %a", m[i]);
+  std::printf("\n");
+  return SKITY_CUDA_SUCCESS;
+}
 int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas, const skity_cuda_path* p, uint32_t op) {
   std::printf("clip_path op=%u fill=%u verbs=", op, p->fill_type);
   for (uint32_t i = 0; i < p->verb_count; ++i) std::printf("%u,", p->verbs[i]);
@@ -152,7 +158,11 @@ int main() {
   canvas->Translate(0.5f, -2);
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
-  canvas->Scale(2, 2);
+  // a perspective matrix is outside the GPU path
+  Matrix persp;
+  const float p9[9] = {1, 0, 0, 0, 1, 0, 0.001f, 0, 1};
+  persp.Set9(p9);
+  canvas->Concat(persp);
   canvas->DrawPath(path, paint);
   std::printf("status=%d\n", canvas->LastStatus());
   canvas->Restore();
@@ -213,6 +223,34 @@ int main() {
                         SamplingOptions{FilterMode::kLinear, MipmapMode::kNone}, &ip);
   std::printf("status=%d\n", canvas->LastStatus());
   std::printf("default_ctx=%d\n", cuda::MakeCUDACanvas(&bm) != nullptr);
+  // Scale / Rotate / Skew: the canvas matrix this canvas computed reaches
+  // the C ABI as Get9 gives it (printed beside it by the reference's
+  // GetTotalMatrix); a gradient under a rotation is refused, and a ClipRect
+  // under a rotation becomes a path clip of the rect (refused)
+  Paint solid;
+  solid.SetColor(ColorSetARGB(255, 10, 20, 30));
+  paint.SetShader(Shader::MakeRadial(Point{20, 15, 0, 1}, 12.f, colors, nullptr, 3, TileMode::kClamp));
+  canvas->Save();
+  canvas->Translate(3, 2);
+  canvas->Scale(2, 0.5f);
+  canvas->DrawPath(path, paint);  // the radial shader under scale and translation
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Rotate(30, 4, 5);
+  canvas->Skew(0.25f, 0);
+  float m9[9];
+  canvas->GetTotalMatrix().Get9(m9);
+  std::printf("total");
+  for (float v : m9) std::printf(" %a", v);
+  std::printf("\n");
+  canvas->DrawPath(path, solid);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->DrawPath(path, paint);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->ClipRect(Rect::MakeLTRB(0, 0, 10, 10));
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->DrawPath(path, solid);
+  std::printf("status=%d\n", canvas->LastStatus());
+  canvas->Restore();
   canvas.reset();
   return 0;
 }

@@ -303,3 +303,26 @@ extern "C" int skc_build_streams_compare(uint32_t count, const uint8_t* const* s
       return 18;
   return 0;
 }
+
+// The canvas matrix the C ABI canvas keeps (skity_cuda_canvas_translate /
+// scale / rotate / skew / concat / set_matrix: the current matrix times the
+// call's, skc::MatMul) for a sequence of calls: op 0 translate (2 args),
+// 1 scale (2), 2 rotate (3), 3 skew (2), 4 concat (9), 5 set matrix (9);
+// out: Matrix::Get9.
+extern "C" void skc_canvas_matrix(const int* ops, int n, const float* args, float out[9]) {
+  Mat4 m;
+  m.identity();
+  for (int i = 0; i < n; ++i) {
+    switch (ops[i]) {
+      case 0: m = MatMul(m, MatTranslate(args[0], args[1])); args += 2; break;
+      case 1: m = MatMul(m, MatScale(args[0], args[1])); args += 2; break;
+      case 2: m = MatMul(m, MatRotateDeg(args[0], args[1], args[2])); args += 3; break;
+      case 3: m = MatMul(m, MatSkew(args[0], args[1])); args += 2; break;
+      case 4: m = MatMul(m, MatFrom9(args)); args += 9; break;
+      case 5: m = MatFrom9(args); args += 9; break;
+    }
+  }
+  const float v[9] = {m.e[0][0], m.e[1][0], m.e[3][0], m.e[0][1], m.e[1][1],
+                      m.e[3][1], m.e[0][3], m.e[1][3], m.e[3][3]};
+  std::memcpy(out, v, sizeof v);
+}

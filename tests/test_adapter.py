@@ -56,11 +56,13 @@ def test_shaders_and_mask_filter(driver_output):
     assert "shader=2 tile=0 stops=3 offsets=0 p0=20,15" in rad and "r=12" in rad
 
 
-def test_translation_forwarded_other_matrices_refused(driver_output):
+def test_matrix_forwarded_perspective_refused(driver_output):
     # Canvas::Save reaches the C ABI (its save level keeps the path clips);
-    # Translate(5, 0) then Translate(0.5, -2): one translation of (5.5, -2)
-    # around the draw; a scaled matrix is outside the GPU path (-5)
-    assert driver_output[9:12] == ["save", "save", "translate 5.5 -2"]
+    # Translate(5, 0) then Translate(0.5, -2): the canvas matrix (a
+    # translation of (5.5, -2)) set around the draw; a perspective matrix is
+    # outside the GPU path (-5)
+    assert driver_output[9:12] == ["save", "save", "set_matrix 0x1p+0 0x0p+0 0x1.6p+2 0x0p+0 "
+                                   "0x1p+0 -0x1p+1 0x0p+0 0x0p+0 0x1p+0"]
     assert driver_output[12].startswith("draw verbs=0,1,2,3,4,5,")
     assert driver_output[13:16] == ["restore", "status=0", "status=-5"]
     assert driver_output[16] == "restore"
@@ -70,7 +72,7 @@ def test_clip_rect_forwarded(driver_output):
     # Translate(2, 1); ClipRect(1.5, 0, 30, 20) -> device (3.5, 1, 32, 21);
     # ClipRect(-5, 2, 25, 40) -> (-3, 3, 27, 41); the global clip bounds are
     # their intersection (3.5, 3, 27, 21), set before the translation
-    assert driver_output[17:21] == ["save", "save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[17:21] == ["save", "save", "clip 3.5 3 27 21", "set_matrix 0x1p+0 0x0p+0 0x1p+1 0x0p+0 0x1p+0 0x1p+0 0x0p+0 0x0p+0 0x1p+0"]
     assert driver_output[21].startswith("draw verbs=0,1,2,3,4,5,")
     assert driver_output[22:24] == ["restore", "status=0"]
 
@@ -83,7 +85,7 @@ def test_difference_clip_rect_is_a_path_clip(driver_output):
     assert driver_output[27] == "clip_path op=0 fill=0 verbs=0,1,1,1,5, points=0,0,10,0,10,10,0,10,"
     assert driver_output[28] == "translate -2 -1"
     # the draw under it is taken (the path clip is recorded on the state)
-    assert driver_output[29:32] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
+    assert driver_output[29:32] == ["save", "clip 3.5 3 27 21", "set_matrix 0x1p+0 0x0p+0 0x1p+1 0x0p+0 0x1p+0 0x1p+0 0x0p+0 0x0p+0 0x1p+0"]
     assert driver_output[32].startswith("draw verbs=0,1,2,3,4,5,")
     assert driver_output[33:37] == ["restore", "status=0", "restore", "restore"]
     # after the Restores the canvas is unclipped and untranslated again
@@ -114,9 +116,10 @@ def test_save_layer_forwarded(driver_output):
     i = driver_output.index("save_layer 1 1 21 11 alpha=0.25 blend=24")
     assert driver_output[i - 4:i] == ["save", "save", "clip 4 3 24 13", "translate 3 2"]
     assert driver_output[i + 1:i + 3] == ["translate -3 -2", "status=0"]
-    # the draw inside carries its clip and translation; Restore of the
-    # layer level pops both C-ABI levels, then the outer Save's
-    assert driver_output[i + 3:i + 6] == ["save", "clip 4 3 24 13", "translate 3 2"]
+    # the draw inside carries its clip and matrix; Restore of the layer
+    # level pops both C-ABI levels, then the outer Save's
+    assert driver_output[i + 3:i + 6] == ["save", "clip 4 3 24 13", "set_matrix 0x1p+0 0x0p+0 "
+                                          "0x1.8p+1 0x0p+0 0x1p+0 0x1p+1 0x0p+0 0x0p+0 0x1p+0"]
     assert driver_output[i + 6].startswith("draw verbs=0,1,2,3,4,5,")
     assert driver_output[i + 7:i + 11] == ["restore", "restore", "restore", "restore"]
 
@@ -128,4 +131,26 @@ def test_draw_image_rect_forwarded(driver_output):
     assert driver_output[i + 1] == "status=0"
     # MakeCUDACanvas(Bitmap*): a canvas over the process-wide context
     assert driver_output[i + 2] == "create ctx=0x30 w=40 h=30 pixels=1 row_bytes=160"
-    assert driver_output[i + 3:] == ["default_ctx=1", "destroy 0x10", "destroy 0x10"]
+    assert driver_output[i + 3:i + 5] == ["default_ctx=1", "destroy 0x10"]
+    assert driver_output[-1] == "destroy 0x10"
+
+
+def test_scale_rotate_skew_forwarded(driver_output):
+    # Translate(3, 2) * Scale(2, 0.5): a radial shader under scale and
+    # translation is taken
+    i = driver_output.index("default_ctx=1") + 2
+    assert driver_output[i:i + 3] == ["save", "save", "set_matrix 0x1p+1 0x0p+0 0x1.8p+1 0x0p+0 "
+                                      "0x1p-1 0x1p+1 0x0p+0 0x0p+0 0x1p+0"]
+    assert "shader=2" in driver_output[i + 3]
+    assert driver_output[i + 4:i + 6] == ["restore", "status=0"]
+    # then Rotate(30, 4, 5) and Skew(0.25, 0): the matrix reaching the C ABI
+    # is the reference canvas's own GetTotalMatrix, bit for bit
+    total = driver_output[i + 6]
+    assert total.startswith("total ")
+    assert driver_output[i + 7:i + 9] == ["save", "set_matrix " + total[6:]]
+    assert driver_output[i + 9].startswith("draw ") and driver_output[i + 10:i + 12] == \
+        ["restore", "status=0"]
+    # a gradient under the rotation is refused; a ClipRect under it is a
+    # path clip of the rect (refused), and so are the draws under it
+    assert driver_output[i + 12:i + 15] == ["save", "set_matrix " + total[6:], "restore"]
+    assert driver_output[i + 15:i + 19] == ["status=-5", "status=-5", "status=-5", "restore"]

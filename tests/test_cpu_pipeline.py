@@ -137,6 +137,43 @@ def test_canvas_translate_bit_exact(cpu_pipeline, oracle_lib):
 
 
 @pytest.mark.parametrize("seed", range(3))
+def test_canvas_matrices_bit_exact(cpu_pipeline, oracle_lib, seed):
+    """Canvas::Scale / Rotate / Skew / Concat: fills and strokes under every
+    kind of affine canvas matrix, gradients under scale and translation."""
+    from test_oracle_pin import matrix_scene
+    sc = matrix_scene(S.SEED_BASE + 365 + seed)
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+
+
+def test_matrix_limits_refused(cpu_pipeline, oracle_lib):
+    """Under a rotation or skew a gradient is refused (its device_to_local
+    needs the general inverse), as is a blur under any canvas matrix; the
+    oracle refuses the same draws."""
+    from test_oracle_pin import matrix_scene
+    sc = matrix_scene(S.SEED_BASE + 365, shaded=False)
+    g = S.SceneBuilder(sc.width, sc.height)
+    gi = g.add_gradient(S.GRAD_LINEAR, (0.0, 0.0), (50.0, 20.0), (0.0, 0.0),
+                        [(1, 0, 0, 1), (0, 0, 1, 1)])
+    p = S.default_paint()
+    p["gradient"] = gi
+    tri = ([S.MOVE, S.LINE, S.LINE, S.CLOSE], [(5, 5), (60, 10), (20, 50)])
+    g.draw_path(*tri, p, matrix=(0.9, 0.3, 4.0, -0.3, 0.9, 6.0))
+    blur = S.default_paint()
+    blur["blur_style"], blur["blur_radius"] = 1, 3.0
+    h = S.SceneBuilder(sc.width, sc.height)
+    h.draw_path(*tri, blur, matrix=(2.0, 0.0, 0.0, 0.0, 2.0, 0.0))
+    for bad in (g.build(), h.build()):
+        b = bad.to_bytes()
+        out = np.zeros((bad.height, bad.width, 4), np.uint8)
+        st = (ctypes.c_uint64 * 6)()
+        assert cpu_pipeline.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, 0, 0) == -5
+        with pytest.raises(RuntimeError):
+            oracle_lib.render(bad)
+
+
+@pytest.mark.parametrize("seed", range(3))
 def test_clip_rect_bit_exact(cpu_pipeline, oracle_lib, seed):
     """Canvas::ClipRect bounds the scan of every later draw (fills, strokes,
     gradients, under translations, empty clips included)."""

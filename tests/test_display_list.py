@@ -72,3 +72,42 @@ def test_stream_matches_reference(oracle_lib):
     want = oracle_lib.render_reference(sc)
     got, _ = oracle_lib.render(sc)
     assert oracle_lib.compare(got, want)["bad_pixels"] == 0
+
+
+def test_recorded_transforms_write_matrices(oracle_lib):
+    """Scale / Rotate / Skew / Concat / SetMatrix are recorded and replayed:
+    the scene gets each draw's canvas matrix, the one the reference's own
+    Canvas computes for the same calls (oracle/_ref/ref_matrix, where the
+    reference build exists)."""
+    import os
+    import subprocess
+    from skity_gb300.canvas import Paint, Path
+    tri = Path().MoveTo(10, 10).LineTo(60, 20).LineTo(20, 70).Close()
+    calls = [("t", (12.0, 7.5)), ("s", (1.25, 0.8)), ("r", (33.0, 20.0, 10.0)),
+             ("k", (0.2, -0.15)), ("c", (0.9, 0.1, 5.0, -0.2, 1.1, -3.0, 0.0, 0.0, 1.0))]
+
+    def ops(cv):
+        cv.Clear((1.0, 1.0, 1.0, 1.0))
+        for name, a in calls:
+            {"t": cv.Translate, "s": cv.Scale, "r": cv.Rotate, "k": cv.Skew}.get(
+                name, lambda *v: cv.Concat(v))(*a)
+            cv.DrawPath(tri, Paint().SetColor(0xFF3060C0).SetAlphaF(0.7))
+        cv.SetMatrix((2.0, 0.0, 1.0, 0.0, 2.0, 1.0, 0.0, 0.0, 1.0))
+        cv.DrawPath(tri, Paint().SetColor(0xFF20A040))
+    dl = _record(ops)
+    sc = dl.to_scene()
+    assert sc.matrices is not None and sc.matrices.shape == (6, 6)
+    assert (sc.paints["translate"] == 0).all()
+    assert tuple(sc.matrices[5]) == (2.0, 0.0, 1.0, 0.0, 2.0, 1.0)
+    got, _ = oracle_lib.render(sc)
+    assert len(np.unique(got.reshape(-1, 4), axis=0)) > 20
+    ref_matrix = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                              "oracle", "_ref", "ref_matrix")
+    if not os.path.exists(ref_matrix):
+        return
+    args = []
+    for k, (name, a) in enumerate(calls):
+        args += [name] + [float(np.float32(v)).hex() for v in a]
+        out = subprocess.check_output([ref_matrix] + args, text=True).split()
+        want = np.array([float.fromhex(v) for v in out], np.float32)
+        assert want[[0, 1, 2, 3, 4, 5]].tobytes() == sc.matrices[k].tobytes(), k

@@ -1,0 +1,119 @@
+"""Canvas matrices on the GPU (Canvas::Scale / Rotate / Skew / Concat /
+SetMatrix; RastePath's CopyWithMatrix and GenerateBrush's inverse) through
+the C ABI against the oracle, pinned to the reference's software canvas.
+Bit-exact expected (tolerance: <= 1 LSB per channel, >= 99.9% exact)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from skity_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+TOL_LSB, MIN_EXACT = 1, 0.999
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+
+def check(oracle_lib, got, sc):
+    ref, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, ref)
+    assert c["max_abs_diff"] <= TOL_LSB and c["exact_frac"] >= MIN_EXACT, c
+    return c
+
+
+def test_matrix_scenes_match_oracle(gpu_ctx, oracle_lib):
+    """Fills and strokes under scales, flips, rotations, skews and general
+    affine maps; gradients under scale and translation; one batch."""
+    from test_oracle_pin import matrix_scene
+    scenes = [matrix_scene(S.SEED_BASE + 365 + k) for k in range(4)]
+    scenes.append(matrix_scene(S.SEED_BASE + 369, 640, 480))
+    for got, sc in zip(gpu_ctx.render_streams(scenes), scenes):
+        assert check(oracle_lib, got, sc)["bad_pixels"] == 0
+
+
+def _shapes():
+    from skity_gb300.canvas import Path
+    tri = Path().MoveTo(2, 2).LineTo(30, 6).LineTo(8, 28).Close()
+    blob = (Path().MoveTo(5, 5).QuadTo(40, 0, 35, 20).CubicTo(30, 40, 10, 45, 3, 30)
+            .ConicTo(0, 20, 5, 5, 0.7).Close())
+    return tri, blob
+
+
+def test_canvas_transforms_match_oracle(gpu_ctx, oracle_lib):
+    """The canvas API: Translate, Scale, Rotate (about a point), Skew and
+    Concat between Save / Restore; each draw's matrix (GetTotalMatrix, the
+    reference Canvas's own product, pinned on the CPU) replayed by the
+    oracle."""
+    from skity_gb300.canvas import Canvas, Paint, Shader
+    tri, blob = _shapes()
+    W, H = 96, 80
+    bitmap = np.zeros((H, W, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    sb = S.SceneBuilder(W, H)
+    colors = [(1, 0, 0, 1), (0, 0.5, 1, 1), (0.2, 0.9, 0.1, 0.8)]
+
+    def draw(path, paint, shader=None):
+        canvas.DrawPath(path, paint)
+        m9 = canvas.GetTotalMatrix()
+        p = paint.rec.copy()
+        if shader is not None:
+            p["gradient"] = sb.add_gradient(shader.kind, shader.p0, shader.p1, shader.radius,
+                                            shader.colors, shader.pos, shader.tile)
+        sb.draw_path(path.verbs, path.points, p, path.weights,
+                     matrix=(m9[0], m9[1], m9[2], m9[3], m9[4], m9[5]))
+
+    red = Paint().SetFillColor(0.9, 0.1, 0.1, 0.8)
+    blue = Paint().SetFillColor(0.1, 0.2, 0.9, 0.6)
+    stroke = Paint().SetStyle(1).SetStrokeWidth(2.5).SetStrokeJoin(1).SetFillColor(0, 0, 0, 1)
+    stroke.SetStrokeColor(0.1, 0.6, 0.2, 0.9)
+    draw(tri, red)
+    canvas.Save()
+    canvas.Translate(20, 10)
+    canvas.Scale(1.5, 0.75)
+    grad = Shader.MakeLinear([(0, 0), (30, 20)], colors, None, 3)
+    draw(blob, Paint().SetShader(grad).SetFillColor(0, 0, 0, 1), grad)
+    canvas.Rotate(25, 10, 10)
+    draw(blob, blue)
+    draw(tri, stroke)
+    canvas.Skew(0.3, -0.1)
+    draw(tri, red)
+    canvas.Restore()
+    canvas.Save()
+    canvas.Concat((0.8, -0.4, 50, 0.3, 1.1, 20, 0, 0, 1))
+    draw(blob, stroke)
+    canvas.Rotate(-60)
+    draw(tri, blue)
+    canvas.Restore()
+    draw(tri, blue)
+    canvas.Flush()
+    check(oracle_lib, bitmap, sb.build())
+
+
+def test_canvas_transform_limits(gpu_ctx):
+    """A gradient under a rotation, a ClipRect under a rotation and the
+    draws under it, and draws under perspective return NOT_SUPPORTED and
+    draw nothing."""
+    from skity_gb300 import _lib
+    from skity_gb300.canvas import Canvas, Paint, Shader
+    tri, _ = _shapes()
+    bitmap = np.full((40, 48, 4), 7, np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    grad = Shader.MakeLinear([(0, 0), (30, 20)], [(1, 0, 0, 1), (0, 0, 1, 1)], None, 2)
+    canvas.Rotate(30)
+    with pytest.raises(_lib.SkityCudaError) as e:
+        canvas.DrawPath(tri, Paint().SetShader(grad))
+    assert e.value.code == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
+    canvas.Save()
+    with pytest.raises(_lib.SkityCudaError) as e:
+        canvas.ClipRect(0, 0, 10, 10)
+    assert e.value.code == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
+    with pytest.raises(_lib.SkityCudaError):
+        canvas.DrawPath(tri, Paint())
+    canvas.Restore()
+    canvas.SetMatrix((1, 0, 0, 0, 1, 0, 0.01, 0, 1))
+    with pytest.raises(_lib.SkityCudaError):
+        canvas.DrawPath(tri, Paint())
+    canvas.Flush()
+    assert (bitmap == 7).all()

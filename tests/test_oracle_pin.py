@@ -104,6 +104,65 @@ def test_canvas_translate(ref):
     _pin(ref, translated_scene())
 
 
+def matrix_scene(seed=S.SEED_BASE + 365, width=180, height=140, shaded=True):
+    """Draws under canvas matrices (Canvas::Scale / Rotate / Skew / Concat):
+    fills (both fill rules) and strokes under scales (non-uniform, flipped,
+    fractional), rotations, skews and their products, plus translations and
+    the identity; gradients under the scale-and-translate matrices only
+    (`shaded`)."""
+    base = S.random_paths_scene(seed, width, height, 36, 2, 20, coord_lo=(-20.0, -20.0),
+                                coord_hi=(width - 20.0, height - 20.0), evenodd_frac=0.4,
+                                gradient_frac=0.5 if shaded else 0.0, stroke_frac=0.3)
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height)
+    gi = {}
+    for d in range(base.n_draws):
+        v0, v1 = int(base.verb_off[d]), int(base.verb_off[d + 1])
+        p0, p1 = int(base.point_off[d]), int(base.point_off[d + 1])
+        p = base.paints[d].copy()
+        kind = d % 6
+        f = np.float32
+        if kind == 0:    # scale and translate
+            sx, sy = rng.uniform(0.3, 1.8), rng.uniform(0.3, 1.8)
+            m = (sx, 0.0, rng.uniform(-30, 60), 0.0, sy, rng.uniform(-30, 50))
+        elif kind == 1:  # flip and scale
+            m = (-rng.uniform(0.5, 1.5), 0.0, width * 0.9, 0.0, rng.uniform(0.5, 1.5), 5.5)
+        elif kind == 2:  # rotation about a point
+            a = f(rng.uniform(-3.1, 3.1))
+            c, s_ = np.cos(a), np.sin(a)
+            cx, cy = f(width / 2), f(height / 2)
+            m = (c, -s_, f(cx - (c * cx - s_ * cy)), s_, c, f(cy - (s_ * cx + c * cy)))
+        elif kind == 3:  # skew
+            m = (1.0, rng.uniform(-0.6, 0.6), rng.uniform(-20, 20), rng.uniform(-0.4, 0.4), 1.0,
+                 rng.uniform(-20, 20))
+        elif kind == 4:  # a general affine map
+            m = tuple(rng.uniform(-1.2, 1.2, 6) * (1, 1, 80, 1, 1, 60) + (0.2, 0, 60, 0, 0.2, 50))
+        else:            # translation or identity
+            m = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0) if d % 12 == 5 else \
+                (1.0, 0.0, rng.uniform(-40, 40), 0.0, 1.0, rng.uniform(-40, 40))
+        m = tuple(float(f(v)) for v in m)
+        g = int(p["gradient"])
+        if g >= 0 and (m[1] != 0.0 or m[3] != 0.0):
+            g = -1  # shaders are taken under scale and translation only
+        if g >= 0:
+            if g not in gi:
+                gr = base.gradients[g]
+                s0, n = int(gr["stop_start"]), int(gr["stop_count"])
+                gi[g] = b.add_gradient(int(gr["type"]), tuple(gr["p0"]), tuple(gr["p1"]),
+                                       tuple(gr["radius"]), base.stop_colors[s0:s0 + n],
+                                       base.stop_offsets[s0:s0 + n] if gr["has_offsets"] else None,
+                                       int(gr["tile_mode"]))
+            g = gi[g]
+        p["gradient"] = g
+        b.draw_path(base.verbs[v0:v1], base.points[p0:p1], p, matrix=m)
+    return b.build()
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_canvas_matrices(ref, seed):
+    _pin(ref, matrix_scene(S.SEED_BASE + 365 + seed))
+
+
 def clipped_scene(seed=S.SEED_BASE + 380, width=180, height=140):
     """Draws under Canvas::ClipRect (kIntersect) and Translate, as a canvas
     sees them between Save and Restore: one or two nested clip rects per
