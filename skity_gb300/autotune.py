@@ -6,7 +6,7 @@ only the time does.  The searched space:
 * row-tile width in pixels {128, 256, 512, 1024, 2048} -- the compositor gives each
   warp one canvas row segment, so a tile is (width x 1 row) and its width,
   a multiple of the 32 lanes, is the shape parameter;
-* persistent CTAs per SM {4, 6, 8} (the grid is that many CTAs per SM,
+* persistent CTAs per SM {1, 2, 4, 6, 8} (the grid is that many CTAs per SM,
   pulling tiles from a work counter in most-work-first order);
 * pass-bin granularity: bands of {8, 16, 32} rows.
 
@@ -22,7 +22,7 @@ import json
 import os
 
 TILE_WIDTHS = (128, 256, 512, 1024, 2048)
-CTAS_PER_SM = (4, 6, 8)
+CTAS_PER_SM = (1, 2, 4, 6, 8)
 BAND_ROWS = (8, 16, 32)
 
 
