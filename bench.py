@@ -422,9 +422,10 @@ def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512)
 
 def other_workloads(ctx, steps: int, threads: int):
     """The 512x512 scene (1,000 fills), the single large scene (2048x2048,
-    20,000 paths with gradients, strokes and both fill rules) and the
+    20,000 paths with gradients, strokes and both fill rules), the
     glyph-dense scene (4096x4096, 100,000 small even-odd outlines, a tenth
-    with a kNormal blur): resident batch renders (CUDA-graph replays), their
+    with a kNormal blur) and the imported tiger picture: resident batch
+    renders (CUDA-graph replays), their
     pixels checked against the committed oracle digests, and the oracle
     timed on one core (a single canvas has no parallelism in the reference)
     -- over the whole scene, or the first paths of the 2048x2048 one."""
@@ -437,7 +438,10 @@ def other_workloads(ctx, steps: int, threads: int):
             ("config2", load_config2(), "2048x2048, 20,000 paths of 3-64 verbs over [-64,2112]^2, "
              "30% even-odd, 25% linear + 25% radial gradients, 20% stroked", 400),
             ("config4", load_config4(), "4096x4096, 100,000 outlines (1-3 contours, 8-48 px), "
-                                        "even-odd, 10% kNormal blur sigma 2-20", None)]:
+                                        "even-odd, 10% kNormal blur sigma 2-20", None),
+            ("skp_tiger", load_tiger(), "the reference's resources/skp/tiger.skp imported "
+             "(skity_gb300/skp.py): 2560x1920, 305 fills and strokes under a canvas matrix",
+             None)]:
         b = Batch(ctx, [sc])
         for _ in range(3):
             b.render()
@@ -461,9 +465,31 @@ def other_workloads(ctx, steps: int, threads: int):
                              "sample": "whole scene" if cpu_paths is None
                              else f"first {n} of {sc.n_draws} paths, {cst.seconds:.1f} s"},
                      "gpu_over_cpu": (sc.n_draws * 1e3 / gms) / cpu_ps,
-                     "parity": parity_by_digest(name, [pix], [sc], threads),
-                     "coverage": coverage_report(ctx, sc, 16)}
+                     "parity": (parity_by_digest(name, [pix], [sc], threads)
+                                if name != "skp_tiger" else tiger_parity(pix, sc, threads)),
+                     "coverage": coverage_report(ctx, sc, 16) if name != "skp_tiger" else None}
     return out
+
+
+def load_tiger():
+    """The tiger picture as the SKP importer wrote it (tests/golden/tiger_scene.bin.gz)."""
+    import gzip
+    from skity_gb300 import scene as S
+    with gzip.open(os.path.join(HERE, "tests", "golden", "tiger_scene.bin.gz"), "rb") as f:
+        return S.Scene.from_bytes(f.read())
+
+
+def tiger_parity(pix, sc, threads: int) -> dict:
+    """The tiger's pixels against the digest of the reference IO module's own
+    playback of the SKP (tests/golden/skp_digests.json)."""
+    with open(os.path.join(HERE, "tests", "golden", "skp_digests.json")) as f:
+        want = json.load(f)["tiger"]["pixels_sha256"]
+    if digest(pix) == want:
+        return {"max_abs_diff": 0, "exact_frac": 1.0, "bad_pixels": 0,
+                "pixels": pix.shape[0] * pix.shape[1], "pass": True,
+                "against": "the reference's playback of the SKP (tests/golden/skp_digests.json)"}
+    from oracle import oracle
+    return parity([pix], [oracle.render_mt(sc, threads)[0]])
 
 
 def coverage_report(ctx, scene, n_draws: int) -> dict:

@@ -247,6 +247,11 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_rotate(skity_cuda_canvas canvas, float 
 SKITY_CUDA_API int32_t skity_cuda_canvas_skew(skity_cuda_canvas canvas, float sx, float sy);
 SKITY_CUDA_API int32_t skity_cuda_canvas_concat(skity_cuda_canvas canvas, const float m[9]);
 SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas canvas, const float m[9]);
+/* Canvas::Concat / SetMatrix of a full 4x4 Matrix, its 16 floats in
+ * column-major order (the Matrix(16 floats) constructor; pictures' CONCAT44
+ * and SET_M44 records, module/io/src/picture.cc:431-460,991-1011). */
+SKITY_CUDA_API int32_t skity_cuda_canvas_concat44(skity_cuda_canvas canvas, const float m[16]);
+SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix44(skity_cuda_canvas canvas, const float m[16]);
 /* Canvas::GetTotalMatrix as Matrix::Get9 (matrix.cc:106-116) gives it. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_get_matrix(skity_cuda_canvas canvas, float m[9]);
 /* Canvas::ClipRect(rect, ClipOp::kIntersect) (canvas.hpp; canvas.cc:130-135,

@@ -175,6 +175,19 @@ def reference_available() -> bool:
     return os.path.exists(REF_RENDER)
 
 
+def render_reference_skp(skp_path: str):
+    """An SKP file played back by the reference's own IO module onto its
+    software canvas, cleared to opaque white (oracle/_ref/ref_skp)."""
+    exe = os.path.join(os.path.dirname(REF_RENDER), "ref_skp")
+    with tempfile.TemporaryDirectory() as d:
+        op = os.path.join(d, "o.rgba")
+        r = subprocess.run([exe, skp_path, op], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("ref_skp failed: " + r.stderr)
+        w, h = (int(v) for v in r.stdout.split())
+        return np.fromfile(op, np.uint8).reshape(h, w, 4)
+
+
 def render_reference(scene, first: int = 0, count: int | None = None):
     """Pixels from the reference's own software backend (oracle/_ref)."""
     count = scene.n_draws if count is None else count

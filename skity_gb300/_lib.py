@@ -133,6 +133,8 @@ SIGNATURES = {
     "skity_cuda_canvas_concat": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "skity_cuda_canvas_set_matrix": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "skity_cuda_canvas_get_matrix": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "skity_cuda_canvas_concat44": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "skity_cuda_canvas_set_matrix44": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "skity_cuda_canvas_clip_rect": (ctypes.c_int32, [_vp, ctypes.c_float, ctypes.c_float,
                                                      ctypes.c_float, ctypes.c_float]),
     "skity_cuda_canvas_clip_path": (ctypes.c_int32, [_vp, ctypes.POINTER(Path_), ctypes.c_uint32]),

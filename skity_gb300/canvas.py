@@ -565,6 +565,17 @@ class Canvas:
         _lib.check(self.lib.skity_cuda_canvas_set_matrix(self.handle, m),
                    "skity_cuda_canvas_set_matrix")
 
+    def Concat44(self, m16):
+        """Canvas::Concat of a 4x4 Matrix given column-major."""
+        m = (ctypes.c_float * 16)(*[float(v) for v in m16])
+        _lib.check(self.lib.skity_cuda_canvas_concat44(self.handle, m),
+                   "skity_cuda_canvas_concat44")
+
+    def SetMatrix44(self, m16):
+        m = (ctypes.c_float * 16)(*[float(v) for v in m16])
+        _lib.check(self.lib.skity_cuda_canvas_set_matrix44(self.handle, m),
+                   "skity_cuda_canvas_set_matrix44")
+
     def GetTotalMatrix(self):
         """The canvas matrix as Matrix::Get9 gives it (row-major 3x3)."""
         m = (ctypes.c_float * 9)()

@@ -909,10 +909,10 @@ namespace skc {
 struct RecordedOp {
   enum Type : uint32_t {
     kClear, kDrawPath, kDrawImageRect, kSave, kRestore, kSaveLayer, kTranslate, kClipRect,
-    kClipPath, kScale, kRotate, kSkew, kConcat, kSetMatrix
+    kClipPath, kScale, kRotate, kSkew, kConcat, kSetMatrix, kConcat44, kSetMatrix44
   };
   Type type = kSave;
-  float f[9] = {};  // colour / bounds / translation / rect / src + dst / matrix
+  float f[16] = {};  // colour / bounds / translation / rect / src + dst / matrix
   uint32_t u = 0;   // ClipOp / image filter
   bool has_path = false;
   std::vector<uint8_t> verbs;
@@ -1798,6 +1798,30 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas canvas, co
   return SKITY_CUDA_SUCCESS;
 }
 
+SKITY_CUDA_API int32_t skity_cuda_canvas_concat44(skity_cuda_canvas canvas, const float m[16]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  for (int i = 0; i < 16; ++i)
+    if (!std::isfinite(m[i])) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  return CanvasConcat(canvas, skc::RecordedOp::kConcat44, m, 16, skc::MatFrom16(m));
+}
+
+SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix44(skity_cuda_canvas canvas, const float m[16]) {
+  if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
+  if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  for (int i = 0; i < 16; ++i)
+    if (!std::isfinite(m[i])) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  if (canvas->recording) {
+    skc::RecordedOp op;
+    op.type = skc::RecordedOp::kSetMatrix44;
+    std::memcpy(op.f, m, sizeof(float) * 16);
+    canvas->ops.push_back(std::move(op));
+    return SKITY_CUDA_SUCCESS;
+  }
+  canvas->st.m = skc::MatFrom16(m);
+  return SKITY_CUDA_SUCCESS;
+}
+
 SKITY_CUDA_API int32_t skity_cuda_canvas_get_matrix(skity_cuda_canvas canvas, float m[9]) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
   if (!m) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
@@ -2146,6 +2170,12 @@ SKITY_CUDA_API int32_t skity_cuda_display_list_draw(skity_cuda_display_list list
         break;
       case skc::RecordedOp::kSetMatrix:
         rc = skity_cuda_canvas_set_matrix(canvas, op.f);
+        break;
+      case skc::RecordedOp::kConcat44:
+        rc = skity_cuda_canvas_concat44(canvas, op.f);
+        break;
+      case skc::RecordedOp::kSetMatrix44:
+        rc = skity_cuda_canvas_set_matrix44(canvas, op.f);
         break;
       case skc::RecordedOp::kClipRect:
         rc = skity_cuda_canvas_clip_rect(canvas, op.f[0], op.f[1], op.f[2], op.f[3]);

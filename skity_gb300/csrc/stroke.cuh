@@ -105,6 +105,14 @@ SKC_HD Mat4 MatFrom9(const float b[9]) {
   m.e[3][3] = b[8];
   return m;
 }
+// Matrix(16 floats), column-major: e[c][r] = m[4c + r] (the CONCAT44 /
+// SET_M44 records of a picture, module/io/src/picture.cc:431-460,991-1011).
+SKC_HD Mat4 MatFrom16(const float m[16]) {
+  Mat4 r;
+  for (int c = 0; c < 4; ++c)
+    for (int k = 0; k < 4; ++k) r.e[c][k] = m[4 * c + k];
+  return r;
+}
 // glm's mat4 product with no identity shortcut (what glm::rotate(...) * d1
 // computes: columns summed left to right).
 SKC_HD Mat4 MatMulPlain(const Mat4& a, const Mat4& b) {
