@@ -467,7 +467,7 @@ def other_workloads(ctx, steps: int, threads: int):
                      "gpu_over_cpu": (sc.n_draws * 1e3 / gms) / cpu_ps,
                      "parity": (parity_by_digest(name, [pix], [sc], threads)
                                 if name != "skp_tiger" else tiger_parity(pix, sc, threads)),
-                     "coverage": coverage_report(ctx, sc, 16) if name != "skp_tiger" else None}
+                     "coverage": coverage_report(ctx, sc, 16)}
     return out
 
 

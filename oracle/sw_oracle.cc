@@ -2539,6 +2539,14 @@ int sko_fill_quads(const uint8_t* scene, size_t len, uint32_t draw, uint8_t* ver
   Path path = BuildPath(s, draw);
   Path quad;
   QuadPath(path, &quad);
+  // mapped by the draw's canvas matrix, as RastePath's CopyWithMatrix maps them
+  float m[6];
+  MatrixOf(s, draw, m);
+  for (auto& q : quad.pts) {
+    const float x = q.x, y = q.y;
+    q.x = (m[0] * x + m[1] * y) + (0.f * 0.f + m[2] * 1.f);
+    q.y = (m[3] * x + m[4] * y) + (0.f * 0.f + m[5] * 1.f);
+  }
   counts[0] = (uint32_t)quad.verbs.size();
   counts[1] = (uint32_t)quad.pts.size();
   for (uint32_t i = 0; i < counts[0] && i < vcap; ++i) verbs[i] = (uint8_t)quad.verbs[i];
