@@ -550,7 +550,8 @@ def workload_scenes(args):
         scenes = load_config3()
         return scenes[:args.canvases] if args.canvases else scenes
     from skity_gb300 import scene as S
-    sc = {"config1": S.config1, "config2": load_config2, "config4": load_config4}[args.workload]()
+    sc = {"config1": S.config1, "config2": load_config2, "config4": load_config4,
+          "tiger": load_tiger}[args.workload]()
     return [sc.subset(0, args.paths) if args.paths else sc]
 
 
@@ -704,7 +705,7 @@ def main():
     ap.add_argument("--canvases", type=int, default=0,
                     help="render only the first N canvases (small profiling case)")
     ap.add_argument("--workload", default="config3",
-                    choices=["config3", "config1", "config2", "config4"],
+                    choices=["config3", "config1", "config2", "config4", "tiger"],
                     help="profiling: time one of the single-canvas scenes instead of the batch")
     ap.add_argument("--paths", type=int, default=0,
                     help="profiling: the first N draws of a single-canvas --workload")
