@@ -195,6 +195,9 @@ typedef struct skity_cuda_raster_config {
   uint32_t ctas_per_sm;   /* persistent compositor CTAs per SM, 0: one warp per
                              tile, no work queue (default 6) */
   uint32_t band_rows;     /* rows per pass-bin band: 8, 16, 32 or 64 (default 16) */
+  uint32_t sweep_warps;   /* warps (one pass each) per CTA of the register-resident
+                             sweeps: 1, 2 or 4 (default 2). A struct_size that ends
+                             before this field keeps the default. */
 } skity_cuda_raster_config;
 
 /* ---- context ------------------------------------------------------------ */

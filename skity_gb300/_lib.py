@@ -107,7 +107,8 @@ class RequestInfo_(ctypes.Structure):
 
 class RasterConfig_(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("tile_width", ctypes.c_uint32),
-                ("ctas_per_sm", ctypes.c_uint32), ("band_rows", ctypes.c_uint32)]
+                ("ctas_per_sm", ctypes.c_uint32), ("band_rows", ctypes.c_uint32),
+                ("sweep_warps", ctypes.c_uint32)]
 
 
 # every entry point declared in include/skity_cuda.h: name -> (restype, argtypes)

@@ -383,11 +383,13 @@ class Batch:
                    "skity_cuda_batch_render_per_draw")
         return self.ctx.stats()
 
-    def set_config(self, tile_width: int = 256, ctas_per_sm: int = 4, band_rows: int = 16):
-        """skity_cuda_batch_set_config: the compositor's launch shape and bin
-        granularity (the pixels do not change); the next render replans."""
+    def set_config(self, tile_width: int = 256, ctas_per_sm: int = 4, band_rows: int = 16,
+                   sweep_warps: int = 2):
+        """skity_cuda_batch_set_config: the compositor's launch shape, bin
+        granularity and the register sweeps' warps per CTA (the pixels do not
+        change); the next render replans."""
         c = _lib.RasterConfig_(ctypes.sizeof(_lib.RasterConfig_), tile_width, ctas_per_sm,
-                               band_rows)
+                               band_rows, sweep_warps)
         _lib.check(self.lib.skity_cuda_batch_set_config(self.handle, ctypes.byref(c)),
                    "skity_cuda_batch_set_config")
 
@@ -395,7 +397,8 @@ class Batch:
         c = _lib.RasterConfig_()
         _lib.check(self.lib.skity_cuda_batch_get_config(self.handle, ctypes.byref(c)),
                    "skity_cuda_batch_get_config")
-        return {"tile_width": c.tile_width, "ctas_per_sm": c.ctas_per_sm, "band_rows": c.band_rows}
+        return {"tile_width": c.tile_width, "ctas_per_sm": c.ctas_per_sm, "band_rows": c.band_rows,
+                "sweep_warps": c.sweep_warps}
 
     def read(self, i: int, out: np.ndarray | None = None) -> np.ndarray:
         h, w = self.sizes[i]

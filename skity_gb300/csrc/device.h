@@ -49,6 +49,7 @@ struct RasterConfig {
   uint32_t tile_w = 1024;    // row-tile width in pixels
   uint32_t ctas_per_sm = 6;  // persistent compositor CTAs per SM (0: one warp per tile)
   int32_t band_shift = 4;    // pass-bin bands of 1 << band_shift rows
+  uint32_t sweep_warps = 2;  // warps per CTA of the register sweeps (1, 2 or 4)
 };
 
 // A batch resident on the device: inputs uploaded once, re-rendered on

@@ -74,7 +74,7 @@ int LaunchGeometry(const DevBatch& b, cudaStream_t stream) {
 // memory), then the generic sweep (4 warps per block, state in global
 // memory) for longer lists.
 constexpr int kSweepWarps = 4;
-constexpr int kRegWarps = 2;
+constexpr int kRegWarpsMax = 4;  // warps per CTA of the register sweeps: DevBatch::reg_warps
 
 __device__ __forceinline__ uint32_t DynamicSmemBytes() {
   uint32_t v;
@@ -106,15 +106,16 @@ __device__ __forceinline__ void FinishOverlapped(unsigned int* done) {
 }
 
 template <int M, int kForm>
-__global__ void __launch_bounds__(32 * kRegWarps) k_sweep_reg(DevBatch b) {
+__global__ void __launch_bounds__(32 * kRegWarpsMax) k_sweep_reg(DevBatch b) {
   extern __shared__ __align__(16) uint8_t reg_smem[];
   AllowNextLaunch();
   const int w = threadIdx.x >> 5;
-  const uint32_t i = blockIdx.x * kRegWarps + w;
+  const uint32_t nw = blockDim.x >> 5;
+  const uint32_t i = blockIdx.x * nw + w;
   if (i < b.n_passes) {
     const uint32_t p = SweepPassAt(b, i);
     if (SweepForm(b.geom[p], b.pass_class[p]) == kForm) {
-      if (DynamicSmemBytes() < kRegWarps * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
+      if (DynamicSmemBytes() < nw * RegSmemBytes<M>(b.reg_diff_cap)) {  // self-check
         FlagError(b.err, 16);
       } else {
         Lanes L;
@@ -163,12 +164,13 @@ static void LaunchOverlapped(void (*kernel)(Args...), dim3 grid, dim3 block, siz
 
 template <int M, int kForm>
 static void LaunchRegForm(const DevBatch& b, cudaStream_t stream, bool overlap) {
-  const size_t smem = kRegWarps * RegSmemBytes<M>(b.reg_diff_cap);
+  const uint32_t nw = b.reg_warps == 1 || b.reg_warps == 4 ? b.reg_warps : 2;
+  const size_t smem = nw * RegSmemBytes<M>(b.reg_diff_cap);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_sweep_reg<M, kForm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-  LaunchOverlapped(k_sweep_reg<M, kForm>, dim3((b.n_passes + kRegWarps - 1) / kRegWarps),
-                   dim3(32 * kRegWarps), smem, stream, overlap, b);
+  LaunchOverlapped(k_sweep_reg<M, kForm>, dim3((b.n_passes + nw - 1) / nw), dim3(32 * nw), smem,
+                   stream, overlap, b);
 }
 
 // With b.sweep_done (four zeroed counters) the later forms overlap the

@@ -179,6 +179,7 @@ struct DevBatch {
   const uint32_t* bins;      // pass indices, per band in draw order
   const uint32_t* sweep_order;  // passes in the order the sweeps take them (null: index order)
   int32_t band_shift;        // rows per pass-bin band: 1 << band_shift
+  uint32_t reg_warps;        // warps per CTA of the register sweeps (1, 2 or 4)
   unsigned int* task_next;   // persistent compositor's work counters (temp, main)
   unsigned int* sweep_done;  // per sweep form, CTAs finished (zeroed before the sweeps);
                              // null: the forms' launches do not overlap

@@ -19,6 +19,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -355,6 +356,7 @@ static int32_t PrepareDevice(skity_cuda_context_s* ctx, DeviceBatch& db, DevBatc
   b.bins = db.bins.as<uint32_t>();
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.band_shift = db.cfg.band_shift;
+  b.reg_warps = db.cfg.sweep_warps;
   b.task_next = db.task_next.as<unsigned int>();
   b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.spans = ctx->span_pool.as<uint2>();
@@ -751,6 +753,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.bins = db.bins.as<uint32_t>();
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.band_shift = db.cfg.band_shift;
+  b.reg_warps = db.cfg.sweep_warps;
   b.task_next = db.task_next.as<unsigned int>();
   b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.span_next = ctx->span_next.as<unsigned long long>();
@@ -1141,16 +1144,24 @@ SKITY_CUDA_API void skity_cuda_context_destroy(skity_cuda_context ctx) {
   delete ctx;
 }
 
+// A config of the first layout (no sweep_warps) keeps the default of 2.
 static bool ToConfig(const skity_cuda_raster_config* c, skc::RasterConfig* out) {
-  if (!c || c->struct_size < sizeof(skity_cuda_raster_config)) return false;
+  const size_t v1 = offsetof(skity_cuda_raster_config, sweep_warps);
+  if (!c || c->struct_size < v1) return false;
   if (c->tile_width < 32 || c->tile_width > 2048 || c->ctas_per_sm > 64) return false;
   int shift = -1;
   for (int k = 3; k <= 6; ++k)
     if (c->band_rows == (1u << k)) shift = k;
   if (shift < 0) return false;
+  uint32_t warps = 2;
+  if (c->struct_size >= sizeof(skity_cuda_raster_config)) {
+    warps = c->sweep_warps;
+    if (warps != 1 && warps != 2 && warps != 4) return false;
+  }
   out->tile_w = c->tile_width;
   out->ctas_per_sm = c->ctas_per_sm;
   out->band_shift = shift;
+  out->sweep_warps = warps;
   return true;
 }
 
@@ -1284,6 +1295,7 @@ SKITY_CUDA_API int32_t skity_cuda_batch_get_config(skity_cuda_batch batch,
   out->tile_width = batch->db.cfg.tile_w;
   out->ctas_per_sm = batch->db.cfg.ctas_per_sm;
   out->band_rows = 1u << batch->db.cfg.band_shift;
+  out->sweep_warps = batch->db.cfg.sweep_warps;
   return SKITY_CUDA_SUCCESS;
 }
 
