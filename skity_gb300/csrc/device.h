@@ -68,6 +68,7 @@ struct DeviceBatch {
   uint32_t n_bands = 0;
   RasterConfig cfg;
   DevBuf task_next;  // persistent compositor's counters
+  DevBuf retry;      // DevBatch::sweep_retry
   DevBuf clip_states, clip_flags, clip_rows, clip_items;  // path clips
   // device planning (batches without path clips): status, per-pass scan
   // arrays and band ranges, bin segments, the tiles (main then temp) and

@@ -121,12 +121,33 @@ __global__ void __launch_bounds__(32 * kRegWarpsMax) k_sweep_reg(DevBatch b) {
         Lanes L;
         L.lane = threadIdx.x & 31;
         uint8_t* mine = reg_smem + (size_t)w * RegSmemBytes<M>(b.reg_diff_cap);
-        SweepPassReg<M>(b, p, L, (RegSharedT<M>*)mine,
-                        (int32_t*)(mine + sizeof(RegSharedT<M>)), b.reg_diff_cap);
+        if (!SweepPassReg<M>(b, p, L, (RegSharedT<M>*)mine,
+                             (int32_t*)(mine + sizeof(RegSharedT<M>)), b.reg_diff_cap) &&
+            L.leader()) {
+          // each pass is taken by one form, so the list holds at most n_passes
+          const uint32_t at = b.sweep_retry ? atomicAdd(b.sweep_retry, 1u) : b.n_passes;
+          if (at < b.n_passes) {
+            b.sweep_retry[1 + at] = p;
+          } else {
+            FlagError(b.err, 32);  // no list: the pass stays unswept, the render fails
+          }
+        }
       }
     }
   }
   FinishOverlapped(b.sweep_done ? b.sweep_done + (kForm & 3) : nullptr);
+}
+
+// The passes the register forms gave up on, swept with the generic form after
+// every register form has finished (a plain launch after them).
+__global__ void __launch_bounds__(32 * kSweepWarps) k_sweep_retry(DevBatch b) {
+  if (!b.sweep_retry) return;
+  const uint32_t n = min(b.sweep_retry[0], b.n_passes);
+  const uint32_t nw = gridDim.x * kSweepWarps;
+  Lanes L;
+  L.lane = threadIdx.x & 31;
+  for (uint32_t i = blockIdx.x * kSweepWarps + (threadIdx.x >> 5); i < n; i += nw)
+    SweepPass(b, b.sweep_retry[1 + i], L);
 }
 
 template <bool kRaw>
@@ -187,7 +208,8 @@ int LaunchSweep(const DevBatch& b, cudaStream_t stream) {
   LaunchRegForm<kRegMaxM, kSweepReg128>(b, stream, overlap);
   LaunchRegForm<64, kSweepReg64>(b, stream, overlap);
   LaunchRegForm<32, kSweepReg32>(b, stream, overlap);
-  return 4;
+  k_sweep_retry<<<64, 32 * kSweepWarps, 0, stream>>>(b);
+  return 5;
 }
 
 // ---------------------------------------------------------------------------

@@ -180,6 +180,8 @@ struct DevBatch {
   const uint32_t* sweep_order;  // passes in the order the sweeps take them (null: index order)
   int32_t band_shift;        // rows per pass-bin band: 1 << band_shift
   uint32_t reg_warps;        // warps per CTA of the register sweeps (1, 2 or 4)
+  uint32_t* sweep_retry;     // [0]: passes the register sweeps gave up on (zeroed before the
+                             // sweeps), [1, n_passes]: their indices
   unsigned int* task_next;   // persistent compositor's work counters (temp, main)
   unsigned int* sweep_done;  // per sweep form, CTAs finished (zeroed before the sweeps);
                              // null: the forms' launches do not overlap

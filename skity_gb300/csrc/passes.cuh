@@ -700,16 +700,17 @@ SKC_HD int SweepForm(const PassGeom& g, uint8_t pass_class) {
                                                         : kSweepGeneric;
 }
 
-// Sweep of pass p through the register form of size M; should its active
-// list outgrow M after all, the same warp sweeps the pass again with the
-// generic form (which clears the rows the attempt wrote).
+// Sweep of pass p through the register form of size M.  Returns false when
+// its active list outgrows M after all: the caller then sweeps the pass with
+// the generic form (SweepPass, which clears the rows the attempt wrote).
+// The generic form is not inlined here, so the register kernels stay small.
 template <int M>
-SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegSharedT<M>* sh,
+SKC_HD bool SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegSharedT<M>* sh,
                          int32_t* sdiff, int32_t sdiff_cap) {
   const PassGeom g = b.geom[p];
   if (g.n_edges <= 0 || g.row1 <= g.row0) {
     EmptyPass(b, p, lanes);
-    return;
+    return true;
   }
   // rows the sweep leaves without spans read as empty
   uint2* rows = b.rowspan + b.sweep[p].rbase;
@@ -719,10 +720,10 @@ SKC_HD void SweepPassReg(const DevBatch& b, uint32_t p, const Lanes& lanes, RegS
   InitPoolSink(b, p, g, &sink);
   if (!RunRegSweep<M>(b, p, g, &sink, lanes, sh, sdiff, sdiff_cap)) {
     lanes.sync();
-    SweepPass(b, p, lanes);
-    return;
+    return false;
   }
   FinishPass(b, p, &sink, lanes);
+  return true;
 }
 
 

@@ -82,6 +82,7 @@ __global__ void k_draw_plan(DevBatch b, uint32_t npass, uint64_t sweep_cap, uint
   atomicMax(&st->sweep_need, off);
   atomicMax(&st->rows_need, rb);
   *b.span_next = 0;
+  b.sweep_retry[0] = 0;
 }
 
 // One warp per canvas row: the spans of the draw's passes on that row,
@@ -197,6 +198,7 @@ int32_t RenderPerDraw(skity_cuda_context_s* ctx, DeviceBatch& db) {
     SKC_TRY_RC(db.pass_spans.ensure(npm * 4));
     SKC_TRY_RC(db.pass_frags.ensure(npm * 8));
     SKC_TRY_RC(db.pass_class.ensure(npm));
+    SKC_TRY_RC(db.retry.ensure((npm + 1) * 4));
     SKC_TRY_RC(db.err.ensure(16));
     SKC_TRY_RC(status.ensure(sizeof(DrawStatus)));
     SKC_TRY_RC(sweepmem.ensure(std::max<uint64_t>(cap_sweep, 16)));
@@ -215,6 +217,7 @@ int32_t RenderPerDraw(skity_cuda_context_s* ctx, DeviceBatch& db) {
     b.sweepmem = sweepmem.as<uint8_t>();
     b.rowspan = rowspan.as<uint2>();
     b.err = db.err.as<uint32_t>();
+    b.sweep_retry = db.retry.as<uint32_t>();  // zeroed by each draw's k_draw_plan
     b.reg_diff_cap = std::max<int32_t>(4, std::min<int32_t>(((int32_t)maxw + 132 + 3) & ~3, kRegDiffMax));
     b.spans = ctx->span_pool.as<uint2>();
     b.span_cap = ctx->span_pool.cap / sizeof(uint2);

@@ -163,6 +163,7 @@ static int EnqueuePlanned(skity_cuda_context_s* ctx, DeviceBatch& db, cudaStream
       cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s);
       cudaMemsetAsync(ctx->span_next.p, 0, 8, s);
       cudaMemsetAsync(b.sweep_done, 0, 16, s);
+      cudaMemsetAsync(b.sweep_retry, 0, 4, s);
       {
         int n = LaunchSweep(b, s);
         if (b.n_clip_states || b.n_clip_items) {
@@ -297,6 +298,7 @@ static int32_t PrepareDevice(skity_cuda_context_s* ctx, DeviceBatch& db, DevBatc
   SKC_TRY(db.pass_spans.ensure(npm * 4));
   SKC_TRY(db.pass_frags.ensure(npm * 8));
   SKC_TRY(db.pass_class.ensure(npm));
+  SKC_TRY(db.retry.ensure((npm + 1) * 4));
   SKC_TRY(db.err.ensure(16));
   SKC_TRY(db.plan_st.ensure(sizeof(PlanStatus)));
   SKC_TRY(db.plan_a.ensure(npm * 8));
@@ -357,6 +359,7 @@ static int32_t PrepareDevice(skity_cuda_context_s* ctx, DeviceBatch& db, DevBatc
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.band_shift = db.cfg.band_shift;
   b.reg_warps = db.cfg.sweep_warps;
+  b.sweep_retry = db.retry.as<uint32_t>();
   b.task_next = db.task_next.as<unsigned int>();
   b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.spans = ctx->span_pool.as<uint2>();
@@ -421,6 +424,7 @@ static int EnqueueDevice(DeviceBatch& db, const DevBatch& b, const DevPlan& q, u
     case 2:
       cudaMemsetAsync(b.span_next, 0, 8, s);
       cudaMemsetAsync(b.sweep_done, 0, 16, s);
+      cudaMemsetAsync(b.sweep_retry, 0, 4, s);
       return LaunchSweep(b, s);
     case 3:
       if (!q.n_temp) return 0;
@@ -699,6 +703,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   SKC_TRY(db.pass_frags.ensure(std::max<size_t>(np, 1) * 8));
   SKC_TRY(db.err.ensure(16));
   SKC_TRY(db.pass_class.ensure(std::max<size_t>(np, 1)));
+  SKC_TRY(db.retry.ensure((std::max<size_t>(np, 1) + 1) * 4));
   SKC_TRY(ctx->span_next.ensure(8));
   std::vector<PassComp> comp;
   PlanComp(hb, db.h_geom, sw, comp);
@@ -754,6 +759,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
   b.sweep_order = np ? db.sweep_order.as<uint32_t>() : nullptr;
   b.band_shift = db.cfg.band_shift;
   b.reg_warps = db.cfg.sweep_warps;
+  b.sweep_retry = db.retry.as<uint32_t>();
   b.task_next = db.task_next.as<unsigned int>();
   b.sweep_done = db.task_next.as<unsigned int>() + 2;
   b.span_next = ctx->span_next.as<unsigned long long>();
@@ -776,6 +782,7 @@ static int32_t PlanAndRender(skity_cuda_context_s* ctx, DeviceBatch& db, bool ti
     SKC_TRY(cudaMemsetAsync(db.pass_class.p, 0, std::max<size_t>(np, 1), s));
     SKC_TRY(cudaMemsetAsync(ctx->span_next.p, 0, 8, s));
     SKC_TRY(cudaMemsetAsync(b.sweep_done, 0, 16, s));
+    SKC_TRY(cudaMemsetAsync(b.sweep_retry, 0, 4, s));
     SKC_TRY(cudaEventRecord(ctx->stage[4], s));
     st.kernel_launches += LaunchSweep(b, s);
     if (b.n_clip_states || b.n_clip_items) {  // the path-clip stages use the span pool too

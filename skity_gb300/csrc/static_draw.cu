@@ -63,6 +63,7 @@ struct StaticDesc {  // the descriptor block at the start of the scratch
   uint8_t pass_class[8];
   unsigned long long pass_frags[2];
   unsigned long long span_next;
+  uint32_t sweep_retry[3];  // DevBatch::sweep_retry: a count, then at most two passes
 };
 static_assert(sizeof(StaticDesc) <= kDescBytes, "descriptor block");
 static_assert(sizeof(P) == 8, "points are copied as float pairs");
@@ -156,6 +157,7 @@ int32_t StaticDraw(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   b.comp = dev->comp;
   b.brushes = dev->brush;
   b.pass_class = dev->pass_class;
+  b.sweep_retry = dev->sweep_retry;
   b.pixels = pixels;
   b.n_list = npass;
   {
@@ -255,6 +257,7 @@ int32_t StaticDraw(uint8_t* base, uint64_t path_off, uint64_t slice_off0, PassDe
   if (e == cudaSuccess) e = cudaMemsetAsync(&dev->err, 0, sizeof(uint32_t), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(dev->pass_class, 0, sizeof dev->pass_class, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(&dev->span_next, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dev->sweep_retry, 0, sizeof dev->sweep_retry, st);
   if (e != cudaSuccess) return Err(e);
   LaunchSweep(b, st);
   // the sweeps' self-check word and pool use, both read before any pixel is

@@ -16,7 +16,9 @@
 using namespace skc;
 
 // mode 0: register sweep with the generic sweep for passes it gives up on
-// (the GPU pipeline's choice); mode 1: generic sweep for every pass.
+// (the GPU pipeline's choice); mode 1: generic sweep for every pass; mode 2:
+// every pass through the 32-edge register form, so that the passes with more
+// active edges take the give-up path (swept again after the register forms).
 extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* out_rgba,
                                    uint64_t stats[6], int mode, uint64_t pool_hint) {
   StreamView sv;
@@ -132,6 +134,10 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
   for (int attempt = 0; attempt < attempts; ++attempt) {
     std::fill(rowspan.begin(), rowspan.end(), make_uint2(0, 0));
     std::fill(pclass.begin(), pclass.end(), (uint8_t)(mode == 1 ? 1 : 0));
+    if (mode == 2)  // every pass of plain spans through the 32-edge form
+      for (uint32_t p = 0; p < np; ++p)
+        if (!geom[p].raw_spans) pclass[p] = (uint8_t)kSweepReg32;
+    std::vector<uint32_t> retry;
     next = 0;
     b.spans = pool.data();
     b.span_cap = pool.size();
@@ -149,18 +155,21 @@ extern "C" int skc_cpu_render_mode(const uint8_t* stream, size_t len, uint8_t* o
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
       if (SweepForm(geom[p], pclass[p]) == kSweepReg128)
-        SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap);
+        if (!SweepPassReg<kRegMaxM>(b, p, lanes, sh, sdiff, b.reg_diff_cap)) retry.push_back(p);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
       if (SweepForm(geom[p], pclass[p]) == kSweepReg64)
-        SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap);
+        if (!SweepPassReg<64>(b, p, lanes, sh64, sdiff64, b.reg_diff_cap)) retry.push_back(p);
     }
     for (uint32_t i = 0; i < np; ++i) {
       const uint32_t p = order[i];
       if (SweepForm(geom[p], pclass[p]) == kSweepReg32)
-        SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap);
+        if (!SweepPassReg<32>(b, p, lanes, sh32, sdiff32, b.reg_diff_cap)) retry.push_back(p);
     }
+    // the passes the register forms gave up on, after them (k_sweep_retry)
+    for (uint32_t p : retry) SweepPass(b, p, lanes);
+    generic += retry.size();
     std::fill(clip_flags.begin(), clip_flags.end(), 0u);
     for (uint32_t k = 1; k <= b.n_clip_states; ++k) {
       const ClipStateDesc& st = hb.clip_states[k - 1];

@@ -11,7 +11,9 @@ from skity_gb300 import scene as S
 
 def cpu_render(lib, sc, mode=0):
     """mode 0: register sweep (generic sweep for passes it gives up on), as
-    the GPU pipeline runs it; mode 1: generic sweep for every pass."""
+    the GPU pipeline runs it; mode 1: generic sweep for every pass; mode 2:
+    every pass forced through the 32-edge register form (the wider ones give
+    up and are swept again after the register forms, as k_sweep_retry does)."""
     b = sc.to_bytes()
     out = np.zeros((sc.height, sc.width, 4), np.uint8)
     st = (ctypes.c_uint64 * 6)()
@@ -119,6 +121,19 @@ def test_long_active_lists_fall_back_to_generic_sweep(cpu_pipeline, oracle_lib):
     generic, st1 = cpu_render(cpu_pipeline, sc, mode=1)
     assert st1[5] == 3
     assert np.array_equal(got, generic)
+
+
+def test_register_give_up_path(cpu_pipeline, oracle_lib):
+    """Passes whose active list outgrows the register form they were given
+    are swept again by the generic form after every register form; the
+    pixels do not change."""
+    sc = S.config2(n_paths=80, width=384, height=384)
+    a, st0 = cpu_render(cpu_pipeline, sc, 0)
+    f, st2 = cpu_render(cpu_pipeline, sc, 2)
+    assert st2[5] > st0[5], (st0, st2)  # some passes gave up
+    assert np.array_equal(a, f)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(f, ref)["bad_pixels"] == 0
 
 
 def test_register_and_generic_sweeps_agree(cpu_pipeline):
