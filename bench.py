@@ -154,11 +154,11 @@ def issue_roofline(st, frame_ms, composite_ms, clk, sms):
 
 # The sweep stage's counters per emitted span, from an ncu capture of the
 # 256-canvas workload's first 64 canvases (profiles/k_sweep_reg_config3_64canvases.md):
-# warp instructions executed and DRAM bytes (read + write) of the four sweep
-# launches of one render (17.285 G instructions, 1.816 GB) over the
+# warp instructions executed and DRAM bytes (read + write) of the five sweep
+# launches of one render (17.440 G instructions, 1.854 GB) over the
 # 165,827,810 spans they emit.  Multiplied by the spans of the timed render
 # (the units one launch processes) they give the per-render figures.
-SWEEP_PER_SPAN = {"warp_inst": 104.24, "dram_bytes": 10.95}
+SWEEP_PER_SPAN = {"warp_inst": 105.17, "dram_bytes": 11.18}
 
 
 def sweep_roofline(st, sweep_ms, clk, sms, hbm_peak, hbm_kind):
@@ -177,7 +177,7 @@ def sweep_roofline(st, sweep_ms, clk, sms, hbm_peak, hbm_kind):
     hbm = {"algorithmic_bytes": alg, "achieved_gbs": alg / (sweep_ms / 1e3) / 1e9,
            "peak_gbs": hbm_peak, "peak_source": hbm_kind}
     hbm["frac"] = hbm["achieved_gbs"] / hbm_peak
-    out = {"kernel": "sweep (k_sweep_reg<32/64/128>, k_sweep)", "sweep_ms": sweep_ms, "hbm": hbm}
+    out = {"kernel": "sweep (k_sweep_reg<32/64/128>, k_sweep, k_sweep_retry)", "sweep_ms": sweep_ms, "hbm": hbm}
     if SWEEP_PER_SPAN["warp_inst"]:
         inst = SWEEP_PER_SPAN["warp_inst"] * spans
         peak = sms * 4 * mhz * 1e6 / 1e9
