@@ -236,10 +236,11 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
  * it.  Rotation is about (px, py), in degrees (Matrix::RotateDeg,
  * matrix.cc:28-53); Concat / SetMatrix take a row-major 3x3 as
  * Matrix::Set9 does (scale x, skew x, translate x, skew y, scale y,
- * translate y, perspective 0, 1, 2).  Paths are mapped by any affine
- * matrix (fills and strokes, solid colours); shaders are taken under scale
- * and translation; blurs, layers and path clips under a translation.
- * Draws past those limits (and draws under perspective) return
+ * translate y, perspective 0, 1, 2).  Paths and clip paths are mapped by
+ * any affine matrix (fills and strokes, solid colours, path clips);
+ * shaders and blurs (whose filtered bitmap is drawn as an image) are taken
+ * under scale and translation, layers under a translation.  Draws past
+ * those limits (and draws under perspective) return
  * SKITY_CUDA_ERROR_NOT_SUPPORTED and draw nothing. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_save(skity_cuda_canvas canvas);
 SKITY_CUDA_API int32_t skity_cuda_canvas_restore(skity_cuda_canvas canvas);
@@ -262,12 +263,11 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_get_matrix(skity_cuda_canvas canvas, fl
  * 306-337), narrows the canvas's global clip bounds (kept and restored by
  * Save / Restore); later DrawPath calls rasterise only inside them, as
  * SWCanvas does for a scale/translate matrix (sw_canvas.cc:279-295).  Under
- * a rotation or skew the reference also clips by the rect as a path, which
- * is not taken: the call returns SKITY_CUDA_ERROR_NOT_SUPPORTED and the
- * draws under it are refused.  Clear is not clipped (SWCanvas::OnDrawPaint
- * rasterises the whole canvas); kDifference is a path clip of the rect
- * (skity_cuda_canvas_clip_path); a blurred draw under a clip returns
- * SKITY_CUDA_ERROR_NOT_SUPPORTED. */
+ * a rotation or skew the canvas also clips by the rect as a path (Path::
+ * AddRect under that matrix, Canvas::OnClipRect, canvas.cc:144-150), as the
+ * reference does.  Clear is not clipped (SWCanvas::OnDrawPaint rasterises
+ * the whole canvas); kDifference is a path clip of the rect
+ * (skity_cuda_canvas_clip_path). */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
                                                    float right, float bottom);
 /* Canvas::DrawImageRect(image, src, dst, sampling, paint) (canvas.hpp:342;
@@ -285,9 +285,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_image_rect(skity_cuda_canvas canva
  * Clear) are clipped by the path's spans the way the software canvas clips
  * them, nested clips combined as it combines them; Save / Restore keep and
  * restore the clip.  A kIntersect clip also narrows the global clip bounds
- * by the path's bounds.  ClipRRect and ClipRect with kDifference are path
- * clips of the rounded rect's / rect's path.  A blurred draw under a path
- * clip returns SKITY_CUDA_ERROR_NOT_SUPPORTED at flush. */
+ * by the path's mapped bounds.  The path is rasterised under the canvas
+ * matrix of the call (any affine matrix; perspective returns
+ * SKITY_CUDA_ERROR_NOT_SUPPORTED).  ClipRRect and ClipRect with kDifference
+ * are path clips of the rounded rect's / rect's path.  A blurred draw under
+ * a clip keeps its temp canvas unclipped and clips the filtered bitmap's
+ * image draw, as the reference does. */
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
                                                    const skity_cuda_path* path, uint32_t op);
 /* Canvas::SaveLayer(bounds, paint) (canvas.hpp; canvas.cc:255-276;

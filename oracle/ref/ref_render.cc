@@ -78,6 +78,7 @@ struct Scene {
   };
   std::vector<Layer> layers;
   std::vector<float> matrices;  // per draw (sx, kx, tx, ky, sy, ty), or empty
+  std::vector<float> clip_matrices;  // per clip state, or empty: their translations
 };
 
 template <typename T>
@@ -157,6 +158,7 @@ bool Load(const char* path, Scene* s) {
     Take(buf, o, s->layers, n_layers);
   }
   if (flags & 32) Take(buf, o, s->matrices, 6 * size_t(nd));
+  if (flags & 64) Take(buf, o, s->clip_matrices, 6 * s->clip_states.size());
   return o <= buf.size();
 }
 
@@ -193,6 +195,18 @@ void ReplayClipState(const Scene& s, skity::Canvas* canvas, uint32_t k) {
                                    s.clip_wts.data() + w0);
   if (c.fill_type == 1) path.SetFillType(skity::Path::PathFillType::kEvenOdd);
   canvas->ClipRect(skity::Rect::MakeLTRB(c.bounds[0], c.bounds[1], c.bounds[2], c.bounds[3]));
+  if (!s.clip_matrices.empty()) {
+    // the canvas matrix of the call, then back to the identity the draw's
+    // replay starts from (a Restore would drop the clip as well)
+    const float* mx = s.clip_matrices.data() + 6 * (k - 1);
+    const float nine[9] = {mx[0], mx[1], mx[2], mx[3], mx[4], mx[5], 0.f, 0.f, 1.f};
+    skity::Matrix m;
+    m.Set9(nine);
+    canvas->SetMatrix(m);
+    canvas->ClipPath(path, static_cast<skity::Canvas::ClipOp>(c.op));
+    canvas->ResetMatrix();
+    return;
+  }
   canvas->Translate(c.translate[0], c.translate[1]);
   canvas->ClipPath(path, static_cast<skity::Canvas::ClipOp>(c.op));
   canvas->Translate(-c.translate[0], -c.translate[1]);

@@ -1940,6 +1940,8 @@ struct SceneView {
   // per-draw canvas matrices (sx, kx, tx, ky, sy, ty), or null: the paints'
   // translations
   const float* matrices = nullptr;
+  // per-clip-state canvas matrices, or null: the states' translations
+  const float* clip_matrices = nullptr;
 };
 
 // The colour filter of the draw whose paint record is `p` (a record of s).
@@ -1970,7 +1972,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
   s->has_clear = hdr[3];
   // 1: per-draw clip bounds, 2: per-draw colour filters, 4: path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~63u) return false;
+  if (flags & ~127u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -2049,6 +2051,7 @@ static bool ParseScene(const uint8_t* buf, size_t len, SceneView* s) {
     for (uint32_t d = 0; d < s->nd && o <= len; ++d)
       if (s->paints[d].translate[0] != 0.f || s->paints[d].translate[1] != 0.f) return false;
   }
+  if (flags & 64) s->clip_matrices = (const float*)at(24 * (size_t)s->n_clip_states);
   return o <= len;
 }
 
@@ -2066,20 +2069,18 @@ static bool IsTranslation(const float m[6]) {
 }
 
 // Draws this restatement does not take under a canvas matrix that is more
-// than a translation: blurs, layers, path clips, and shaders under a matrix
-// with rotation or skew (their device_to_local needs the general 4x4
-// inverse).  The GPU path refuses the same draws.
+// than a translation: layers, and shaders (a blur's filtered bitmap
+// included) under a matrix with rotation or skew (their device_to_local
+// needs the general 4x4 inverse).  The GPU path refuses the same draws.
 static bool UnsupportedUnderMatrix(const SceneView& s) {
   if (!s.matrices) return false;
   for (uint32_t d = 0; d < s.nd; ++d) {
     const float* m = s.matrices + 6 * (size_t)d;
     const PaintRec& bp = s.paints[d];
-    if (bp.blur_style != 0 && bp.blur_radius > 0.f &&
-        !(IsTranslation(m) && m[2] == 0.f && m[5] == 0.f))
-      return true;  // a blur under any canvas matrix (as under a translation)
+    if (bp.blur_style != 0 && bp.blur_radius > 0.f && (m[1] != 0.f || m[3] != 0.f))
+      return true;  // the blur's image draw under a rotation or skew
     if (IsTranslation(m)) continue;
     const PaintRec& p = s.paints[d];
-    if (s.draw_clip_state && s.draw_clip_state[d]) return true;
     for (uint32_t i = 0; i < s.n_layers; ++i) {
       const uint32_t end = s.layers[i].restore == 0xFFFFFFFFu ? s.nd : s.layers[i].restore;
       if (d >= s.layers[i].start && d < end) return true;
@@ -2090,9 +2091,8 @@ static bool UnsupportedUnderMatrix(const SceneView& s) {
   return false;
 }
 
-// A blurred draw under a narrowed clip: the blur's temp canvas and its
-// image draw under a clip are not restated here (the GPU path refuses the
-// same draws).
+// A blurred or path-clipped draw inside a layer: not restated here (the GPU
+// path refuses the same draws).
 static bool BlurUnderClip(const SceneView& s) {
   for (uint32_t i = 0; i < s.n_layers; ++i) {
     const uint32_t end = s.layers[i].restore == 0xFFFFFFFFu ? s.nd : s.layers[i].restore;
@@ -2100,15 +2100,6 @@ static bool BlurUnderClip(const SceneView& s) {
       if ((s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f) ||
           (s.draw_clip_state && s.draw_clip_state[d] != 0))
         return true;
-  }
-  for (uint32_t d = 0; d < s.nd && s.clips; ++d) {
-    const Clip c = ClipOf(s, d);
-    const bool narrowed = !(c.l == -1e9f && c.t == -1e9f && c.r == 1e9f && c.b == 1e9f);
-    if (narrowed && s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f) return true;
-  }
-  for (uint32_t d = 0; d < s.nd && s.draw_clip_state; ++d) {
-    if (s.draw_clip_state[d] != 0 && s.paints[d].blur_style != 0 && s.paints[d].blur_radius > 0.f)
-      return true;
   }
   return false;
 }
@@ -2323,13 +2314,17 @@ static void ComputeClipStates(const SceneView& s, ClipStates* cs) {
     v += r.nv;
     p += 2 * (size_t)r.np;
     w += r.nw;
-    // RastePath(path, CurrentTransform(), GetScanClipBounds())
+    // RastePath(path, CurrentTransform(), GetScanClipBounds()); the points
+    // mapped as CopyWithMatrix maps them (see DrawPathMatrix)
+    const float* cm = s.clip_matrices ? s.clip_matrices + 6 * (size_t)i : nullptr;
+    const float m[6] = {cm ? cm[0] : 1.f, cm ? cm[1] : 0.f, cm ? cm[2] : r.translate[0],
+                        cm ? cm[3] : 0.f, cm ? cm[4] : 1.f, cm ? cm[5] : r.translate[1]};
     Path quad;
     QuadPath(path, &quad);
     for (auto& q : quad.pts) {
       const float x = q.x, y = q.y;
-      q.x = (1.f * x + 0.f * y) + (0.f * 0.f + r.translate[0] * 1.f);
-      q.y = (0.f * x + 1.f * y) + (0.f * 0.f + r.translate[1] * 1.f);
+      q.x = (m[0] * x + m[1] * y) + (0.f * 0.f + m[2] * 1.f);
+      q.y = (m[3] * x + m[4] * y) + (0.f * 0.f + m[5] * 1.f);
     }
     Clip bounds;
     bounds.l = r.bounds[0];

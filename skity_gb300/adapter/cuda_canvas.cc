@@ -62,11 +62,11 @@ void CUDACanvas::OnClipRect(Rect const& rect, ClipOp op) {
 }
 
 // SWCanvas::OnClipPath (sw_canvas.cc:317-336): the C ABI canvas records the
-// clip on its state for this save level, with the translation and the
+// clip on its state for this save level, with the canvas matrix and the
 // global clip bounds in effect (the base class has already narrowed them).
 void CUDACanvas::OnClipPath(Path const& path, ClipOp op) {
-  float tx = 0.f, ty = 0.f;
-  if (!TranslationOf(GetTotalMatrix(), &tx, &ty)) {
+  float nine[9];
+  if (!AffineOf(GetTotalMatrix(), nine)) {
     bad_clip_.back() = true;
     status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     return;
@@ -78,10 +78,14 @@ void CUDACanvas::OnClipPath(Path const& path, ClipOp op) {
   const Rect& g = GetGlobalClipBounds();
   if (!(g.Left() == -1e9f && g.Top() == -1e9f && g.Right() == 1e9f && g.Bottom() == 1e9f))
     skity_cuda_canvas_clip_rect(canvas_, g.Left(), g.Top(), g.Right(), g.Bottom());
-  const bool moved = tx != 0.f || ty != 0.f;
-  if (moved) skity_cuda_canvas_translate(canvas_, tx, ty);
+  // the matrix for this call only (a Restore would drop the clip too)
+  const bool moved = !IsIdentity9(nine);
+  if (moved) skity_cuda_canvas_set_matrix(canvas_, nine);
   status_ = skity_cuda_canvas_clip_path(canvas_, &p, op == ClipOp::kIntersect ? 1u : 0u);
-  if (moved) skity_cuda_canvas_translate(canvas_, -tx, -ty);
+  if (moved) {
+    static const float kIdentity[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    skity_cuda_canvas_set_matrix(canvas_, kIdentity);
+  }
 }
 
 void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
@@ -190,8 +194,9 @@ void CUDACanvas::OnDrawPath(Path const& path, Paint const& paint) {
   if (clipped)
     skity_cuda_canvas_clip_rect(canvas_, clip.Left(), clip.Top(), clip.Right(), clip.Bottom());
   if (moved) skity_cuda_canvas_set_matrix(canvas_, nine);
-  if ((q.shader || q.image_shader) && !GetTotalMatrix().OnlyScaleAndTranslate()) {
-    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a shader's inverse past scale and translation
+  if ((q.shader || q.image_shader || q.blur_style) && !GetTotalMatrix().OnlyScaleAndTranslate()) {
+    // a shader's (or a blur's image draw's) inverse past scale and translation
+    status_ = SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (moved || clipped) skity_cuda_canvas_restore(canvas_);
     return;
   }

@@ -114,6 +114,9 @@ struct StreamView {
   // per-draw canvas matrices (sx, kx, tx, ky, sy, ty) when the stream has
   // them (the paints' translations are then zero), else null
   const float* matrices;
+  // per-clip-state canvas matrices of the ClipPath calls when the stream has
+  // them (the states' translations are then zero), else null
+  const float* clip_matrices;
 };
 
 // A ClipPath call of the stream: its parent state (1-based, 0: none), the
@@ -246,7 +249,7 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
   // 1: per-draw clip bounds follow the stops; 2: then per-draw colour
   // filters; 4: then the path clips
   const uint32_t flags = hdr[4];
-  if (flags & ~63u) return false;
+  if (flags & ~127u) return false;
   size_t o = 32;
   std::memcpy(s->clear, buf + o, 16);
   o += 16;
@@ -388,6 +391,21 @@ inline bool ParseStream(const uint8_t* buf, size_t len, StreamView* s) {
     for (uint32_t d = 0; d < s->nd; ++d)
       for (int k = 0; k < 6; ++k)
         if (!std::isfinite(s->matrices[6 * (size_t)d + k])) return false;
+  }
+  s->clip_matrices = nullptr;
+  if (flags & 64) {
+    if (!(flags & 4)) return false;  // matrices of clip states the stream does not have
+    s->clip_matrices = (const float*)at(24 * (size_t)s->n_clip_states);
+    if (o > len) return false;
+    const float* p = s->clip_pts;
+    for (uint32_t i = 0; i < s->n_clip_states; ++i) {
+      const ClipStateRec& c = s->clip_states[i];
+      const float* m = s->clip_matrices + 6 * (size_t)i;
+      for (int k = 0; k < 6; ++k)
+        if (!std::isfinite(m[k])) return false;
+      if (c.translate[0] != 0.f || c.translate[1] != 0.f || !ValidMatrix(m, p, c.np)) return false;
+      p += 2 * (size_t)c.np;
+    }
   }
   if (o > len) return false;
   if (s->width == 0 || s->height == 0 || s->width > 65535 || s->height > 65535) return false;
@@ -688,7 +706,7 @@ inline bool FiltersColor(const StreamView& s, uint32_t d) {
 // scale and translation (NOT_SUPPORTED under rotation or skew).
 inline int AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_t draw_index,
                          uint32_t canvas, const float ctm[6], std::vector<PassDesc>& out,
-                         const float* clip_shift = nullptr) {
+                         const float* clip_shift = nullptr, bool draw_clip = true) {
   const float tx = ctm[2], ty = ctm[5];
   const bool lin = HasLinear(ctm);
   const PaintRec& pr = s.paints[d];
@@ -809,7 +827,7 @@ inline int AddDrawPasses(HostBatch& hb, const StreamView& s, uint32_t d, uint32_
       pd.lin[2] = ctm[3];
       pd.lin[3] = ctm[4];
     }
-    if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
+    if (draw_clip && s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
       pd.clipped = 1;
       std::memcpy(pd.clip, s.clips + 4 * (size_t)d, sizeof pd.clip);
       if (clip_shift) {  // Rect::Offset
@@ -919,9 +937,9 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
   std::vector<PassDesc> main_passes;
   std::vector<std::pair<uint32_t, std::vector<PassDesc>>> temps;
   // Path clips: one pass rasterising each ClipPath path (RastePath with the
-  // canvas translation and global clip bounds of the call, sw_canvas.cc:
-  // 317-324), its spans kept raw for the clip stages; states numbered
-  // across the batch.
+  // canvas matrix and global clip bounds of the call, sw_canvas.cc:317-324),
+  // its spans kept raw for the clip stages; states numbered across the
+  // batch.
   const uint32_t state_base = (uint32_t)hb.clip_states.size();
   std::vector<uint32_t> clip_pass_pos;
   {
@@ -938,6 +956,18 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       pd.flags = kPassClipPath | kPassRawSpans | (c.fill_type == 1 ? kPassEvenOdd : 0);
       pd.tx = c.translate[0];
       pd.ty = c.translate[1];
+      if (s.clip_matrices) {
+        const float* m = s.clip_matrices + 6 * (size_t)i;
+        pd.tx = m[2];
+        pd.ty = m[5];
+        if (HasLinear(m)) {
+          pd.flags |= kPassMatrix;
+          pd.lin[0] = m[0];
+          pd.lin[1] = m[1];
+          pd.lin[2] = m[3];
+          pd.lin[3] = m[4];
+        }
+      }
       if (!IsNoClip(c.bounds)) {
         pd.clipped = 1;
         std::memcpy(pd.clip, c.bounds, sizeof pd.clip);
@@ -1113,7 +1143,6 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     if (!blur) {
       // the canvas matrix goes where the reference's CopyWithMatrix and
       // device_to_local put it (sw_raster.cc:736-754, sw_canvas.cc:727-795)
-      if (path_clip && lin) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
       const size_t first_pass = main_passes.size();
       if (int rc = AddDrawPasses(hb, s, d, draw, cidx, ctm, main_passes)) return rc;
       if (path_clip) {  // DoBrush clips the raster's spans by the state (sw_canvas.cc:338-353)
@@ -1124,9 +1153,9 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       }
       continue;
     }
-    if (path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;  // a blur under a path clip
-    if (lin || ctm[2] != 0.f || ctm[5] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
-    if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+    // the filtered bitmap's image draw inverts the canvas matrix: scale and
+    // translate only (the short inverse, matrix.cc:242-268)
+    if (ctm[1] != 0.f || ctm[3] != 0.f) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     if (pr.blur_style > 4) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;  // past BlurStyle::kInner
     // SWCanvas::HandleFilter: bounds of the source path (path.cc:1341-1360)
     const float* p = s.pts + 2 * (size_t)s.po[d];
@@ -1177,11 +1206,14 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     hb.max_temp_h = std::max(hb.max_temp_h, fh);
     hb.max_temp_style = std::max<uint32_t>(hb.max_temp_style, pr.blur_style);
     std::vector<PassDesc> tp;
+    // a fresh software canvas: no clip of the main canvas applies there
     const float to_temp[6] = {1.f, 0.f, -fl, 0.f, 1.f, -ft};
-    if (int rc = AddDrawPasses(hb, s, d, draw, tidx, to_temp, tp)) return rc;
+    if (int rc = AddDrawPasses(hb, s, d, draw, tidx, to_temp, tp, nullptr, false)) return rc;
     temps.emplace_back(tidx, std::move(tp));
-    // DrawImage(blurred, filter_bounds, &paint) (sw_canvas.cc:641-677):
-    // a rect path with a decal/nearest pixmap brush, alpha = paint alpha
+    // DrawImage(blurred, filter_bounds, &paint) (sw_canvas.cc:641-677): a
+    // rect path with a decal/nearest pixmap brush, alpha = paint alpha, drawn
+    // under the canvas matrix, the global clip bounds and the path clip of
+    // the draw (the temp canvas had none of them)
     const uint8_t rv[5] = {kMove, kLine, kLine, kLine, kClose};
     const float rp[8] = {fl, ft, fr, ft, fr, fb, fl, fb};
     uint32_t rect = hb.AddDraw(rv, 5, rp, 4, nullptr, 0);
@@ -1199,7 +1231,9 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
       inv.e[3][0] = -local.e[3][0];
       inv.e[3][1] = -local.e[3][1];
     }
-    Mat4 m = MatMul(MatScale(1.f / fw, 1.f / fh), inv);
+    // GenerateBrush: Scale(1/w, 1/h) * inverse(local) * inverse(CTM)
+    // (sw_canvas.cc:762-777)
+    Mat4 m = MatMul(MatMul(MatScale(1.f / fw, 1.f / fh), inv), InvertScaleTranslate(ctm));
     br.m[0] = m.e[0][0];
     br.m[1] = m.e[1][0];
     br.m[2] = m.e[3][0];
@@ -1220,6 +1254,23 @@ inline int AddStreamCanvas(HostBatch& hb, const StreamView& s) {
     pd.ga = br.global_alpha;
     pd.stroke_width = 1.f;
     pd.miter = 4.f;
+    pd.tx = ctm[2];
+    pd.ty = ctm[5];
+    if (lin) {
+      pd.flags |= kPassMatrix;
+      pd.lin[0] = ctm[0];
+      pd.lin[1] = ctm[1];
+      pd.lin[2] = ctm[3];
+      pd.lin[3] = ctm[4];
+    }
+    if (s.clips && !IsNoClip(s.clips + 4 * (size_t)d)) {
+      pd.clipped = 1;
+      std::memcpy(pd.clip, s.clips + 4 * (size_t)d, sizeof pd.clip);
+    }
+    if (path_clip) {  // DoBrush clips the rect's spans by the state (sw_canvas.cc:338-353)
+      pd.path_clip = state_base + path_clip;
+      pd.flags |= kPassRawSpans;
+    }
     InitialCaps(rv, 5, rp, false, pd.cap);
     DerivedCaps(pd.cap, false);
     main_passes.push_back(pd);

@@ -1045,9 +1045,6 @@ struct skity_cuda_canvas_s {
     skc::Mat4 m;  // the canvas matrix (LayerState::CurrentMatrix), column-major
     float clip[4] = {-1e9f, -1e9f, 1e9f, 1e9f};  // kMaxCullRect
     uint32_t path_clip = 0;  // the path-clip state (1-based in clip_states; 0: none)
-    // a ClipRect under a rotation or skew (a path clip of the rect in the
-    // reference, not taken here): draws under it are refused
-    bool bad_clip = false;
     State() { m.identity(); }
     float tx() const { return m.e[3][0]; }
     float ty() const { return m.e[3][1]; }
@@ -1087,6 +1084,10 @@ struct skity_cuda_canvas_s {
   std::vector<uint8_t> clip_verbs;
   std::vector<float> clip_pts, clip_wts;
   std::vector<uint32_t> draw_clip_state;
+  // per clip state: the canvas matrix of the call (sx, kx, tx, ky, sy, ty);
+  // written to the scene when one of them is more than a translation
+  std::vector<float> clip_matrices;
+  bool any_clip_matrix = false;
   // images of the recorded draws (copied) and the per-draw image shaders
   std::vector<skc::ImageRec> images;
   std::vector<uint8_t> image_blob;
@@ -1097,6 +1098,76 @@ struct skity_cuda_canvas_s {
   bool any_matrix = false;
   skc::DeviceBatch db;
 };
+
+namespace {
+
+// Canvas::CalculateGlobalClipBounds for kIntersect (canvas.cc:463-476): the
+// rect mapped by the canvas matrix (Matrix::MapRect, matrix.cc:306-337: the
+// corners mapped, w = 1, their min and max), intersected with the bounds
+// (Rect::Intersect, rect.cc:160-172), or the empty rect.
+void NarrowClipBounds(skity_cuda_canvas_s* canvas, float left, float top, float right,
+                      float bottom) {
+  float m6[6];
+  canvas->st.six(m6);
+  skc::Xform xf;
+  xf.sx = m6[0];
+  xf.kx = m6[1];
+  xf.tx = m6[2];
+  xf.ky = m6[3];
+  xf.sy = m6[4];
+  xf.ty = m6[5];
+  xf.lin = !canvas->st.translation();
+  const skc::P q[4] = {xf.map(skc::mkP(left, top)), xf.map(skc::mkP(right, top)),
+                       xf.map(skc::mkP(right, bottom)), xf.map(skc::mkP(left, bottom))};
+  float ml = q[0].x, mr = q[0].x, mt = q[0].y, mb = q[0].y;
+  for (int i = 1; i < 4; ++i) {
+    ml = std::min(q[i].x, ml);
+    mr = std::max(q[i].x, mr);
+    mt = std::min(q[i].y, mt);
+    mb = std::max(q[i].y, mb);
+  }
+  float* c = canvas->st.clip;
+  const float l = std::max(c[0], ml), r = std::min(c[2], mr);
+  const float t = std::max(c[1], mt), b = std::min(c[3], mb);
+  if (!(l < r && t < b)) {
+    c[0] = c[1] = c[2] = c[3] = 0.f;
+  } else {
+    c[0] = l;
+    c[1] = t;
+    c[2] = r;
+    c[3] = b;
+  }
+}
+
+// SWCanvas::OnClipPath (sw_canvas.cc:317-335): a new clip state over the
+// current one, with the canvas matrix and global clip bounds of the call.
+void AddClipState(skity_cuda_canvas_s* canvas, const uint8_t* verbs, uint32_t nv,
+                  const float* pts, uint32_t np, const float* wts, uint32_t nw, uint32_t op,
+                  uint32_t fill_type) {
+  skc::ClipStateRec c;
+  std::memset(&c, 0, sizeof c);
+  c.parent = canvas->st.path_clip;
+  c.op = op;
+  c.fill_type = fill_type;
+  c.nv = nv;
+  c.np = np;
+  c.nw = nw;
+  c.translate[0] = canvas->st.tx();
+  c.translate[1] = canvas->st.ty();
+  std::memcpy(c.bounds, canvas->st.clip, sizeof c.bounds);
+  canvas->clip_states.push_back(c);
+  canvas->clip_verbs.insert(canvas->clip_verbs.end(), verbs, verbs + nv);
+  canvas->clip_pts.insert(canvas->clip_pts.end(), pts, pts + 2 * (size_t)np);
+  if (nw) canvas->clip_wts.insert(canvas->clip_wts.end(), wts, wts + nw);
+  float m6[6];
+  canvas->st.six(m6);
+  canvas->clip_matrices.insert(canvas->clip_matrices.end(), m6, m6 + 6);
+  canvas->any_clip_matrix = canvas->any_clip_matrix || !canvas->st.translation();
+  canvas->st.path_clip = (uint32_t)canvas->clip_states.size();
+  canvas->dirty = true;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1488,7 +1559,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   pr.miter = paint->miter_limit;
   // the canvas matrix: a translation goes in the paint record; anything
   // more in the draw's matrix record
-  if (!canvas->st.affine() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (!canvas->st.affine()) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   float ctm[6];
   canvas->st.six(ctm);
   const bool lin = !canvas->st.translation();
@@ -1497,17 +1568,14 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   if (lin ? !skc::ValidMatrix(ctm, path->points, path->point_count)
           : !skc::ValidTranslate(pr.translate, path->points, path->point_count))
     return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
-  const bool clipped = !skc::IsNoClip(canvas->st.clip);
-  if ((lin || ctm[2] != 0.f || ctm[5] != 0.f || clipped) && paint->blur_style != 0 &&
-      paint->blur_radius > 0.f)
-    return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   // shaders under scale and translation only (their device_to_local is
-  // then the short inverse); no layers or path clips under more than a
-  // translation
-  if ((paint->shader || paint->image_shader) && !canvas->st.scale_translate())
+  // then the short inverse), a blur's filtered bitmap included; no layers
+  // under more than a translation
+  if ((paint->shader || paint->image_shader ||
+       (paint->blur_style != 0 && paint->blur_radius > 0.f)) &&
+      !canvas->st.scale_translate())
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (lin) {
-    if (canvas->st.path_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
     for (uint32_t l : canvas->saved_layer)
       if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   }
@@ -1542,7 +1610,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_draw_path(skity_cuda_canvas canvas,
   canvas->matrices.insert(canvas->matrices.end(), ctm, ctm + 6);
   canvas->any_matrix = canvas->any_matrix || lin;
   canvas->clips.insert(canvas->clips.end(), canvas->st.clip, canvas->st.clip + 4);
-  canvas->any_clip = canvas->any_clip || clipped;
+  canvas->any_clip = canvas->any_clip || !skc::IsNoClip(canvas->st.clip);
   skc::ColorFilterRec fr;
   std::memset(&fr, 0, sizeof fr);
   if (paint->color_filter) {
@@ -1710,7 +1778,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, co
     if (l) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   if (paint && ((paint->blur_style != 0 && paint->blur_radius > 0.f) || paint->color_filter))
     return SKITY_CUDA_ERROR_NOT_SUPPORTED;
-  if (!canvas->st.translation() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  if (!canvas->st.translation()) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
   const bool empty = !(bounds[0] < bounds[2] && bounds[1] < bounds[3]);
   bool reject = empty;
   if (!empty) {  // QuickReject: the mapped bounds against the global clip bounds
@@ -1886,12 +1954,22 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
     canvas->ops.push_back(std::move(rop));
     return SKITY_CUDA_SUCCESS;
   }
-  // path clips under a translation only
-  if (!canvas->st.translation() || canvas->st.bad_clip) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
-  float t[2] = {canvas->st.tx(), canvas->st.ty()};
-  if (!skc::ValidTranslate(t, path->points, path->point_count)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  // the path under the canvas matrix (any affine map), as RastePath takes
+  // CurrentTransform() (sw_canvas.cc:317-324)
+  if (!canvas->st.affine()) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  float m6[6];
+  canvas->st.six(m6);
+  if (!canvas->st.translation()) {
+    if (!skc::ValidMatrix(m6, path->points, path->point_count))
+      return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  } else {
+    float t[2] = {m6[2], m6[5]};
+    if (!skc::ValidTranslate(t, path->points, path->point_count))
+      return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
+  }
   if (op == 1) {
-    // the path's bounds: its points but a trailing move
+    // Canvas::ClipPath narrows the global clip bounds by the path's bounds
+    // (canvas.cc:159-164): its points but a trailing move
     uint32_t n = path->point_count;
     if (path->verb_count > 1 && path->verbs[path->verb_count - 1] == SKITY_CUDA_VERB_MOVE) n--;
     float l = 0.f, tp = 0.f, r = 0.f, b = 0.f;
@@ -1907,34 +1985,18 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_path(skity_cuda_canvas canvas,
         b = std::max(b, y);
       }
     }
-    const int32_t rc = skity_cuda_canvas_clip_rect(canvas, l, tp, r, b);
-    if (rc) return rc;
+    NarrowClipBounds(canvas, l, tp, r, b);
   }
-  skc::ClipStateRec c;
-  std::memset(&c, 0, sizeof c);
-  c.parent = canvas->st.path_clip;
-  c.op = op;
-  c.fill_type = path->fill_type ? 1u : 0u;
-  c.nv = path->verb_count;
-  c.np = path->point_count;
-  c.nw = path->conic_weight_count;
-  c.translate[0] = canvas->st.tx();
-  c.translate[1] = canvas->st.ty();
-  std::memcpy(c.bounds, canvas->st.clip, sizeof c.bounds);
-  canvas->clip_states.push_back(c);
-  canvas->clip_verbs.insert(canvas->clip_verbs.end(), path->verbs, path->verbs + path->verb_count);
-  canvas->clip_pts.insert(canvas->clip_pts.end(), path->points, path->points + 2 * (size_t)path->point_count);
-  canvas->clip_wts.insert(canvas->clip_wts.end(), path->conic_weights,
-                          path->conic_weights + path->conic_weight_count);
-  canvas->st.path_clip = (uint32_t)canvas->clip_states.size();
-  canvas->dirty = true;
+  AddClipState(canvas, path->verbs, path->verb_count, path->points, path->point_count,
+               path->conic_weights, path->conic_weight_count, op, path->fill_type ? 1u : 0u);
   return SKITY_CUDA_SUCCESS;
 }
 
-// Canvas::CalculateGlobalClipBounds (canvas.cc:463-476) for kIntersect
-// under a translation: Matrix::MapRect (matrix.cc:306-337) gives the
-// corners x + tx, y + ty, ordered by min/max; Rect::Intersect (rect.cc:
-// 160-172) keeps the overlap, or the bounds become the empty rect.
+// Canvas::ClipRect (canvas.cc:130-150): the global clip bounds narrowed by
+// the mapped rect (Canvas::CalculateGlobalClipBounds, canvas.cc:463-476;
+// Matrix::MapRect, matrix.cc:306-337: the corners mapped, w = 1, their min
+// and max); under a rotation or skew SWCanvas::OnClipRect then clips by the
+// rect as a path (Path::AddRect, sw_canvas.cc:297-313, canvas.cc:144-150).
 SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, float left, float top,
                                                    float right, float bottom) {
   if (!canvas) return SKITY_CUDA_ERROR_INVALID_HANDLE;
@@ -1951,46 +2013,21 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clip_rect(skity_cuda_canvas canvas, flo
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
-  // the global clip bounds narrowed by the mapped rect (Canvas::
-  // CalculateGlobalClipBounds, canvas.cc:463-476; Matrix::MapRect,
-  // matrix.cc:306-337: the corners mapped, w = 1, their min and max).  Under
-  // a rotation or skew SWCanvas::OnClipRect clips by the rect as a path
-  // (sw_canvas.cc:297-313), which is not taken: later draws are refused.
   if (!canvas->st.affine()) return SKITY_CUDA_ERROR_NOT_SUPPORTED;
-  const bool st_ok = canvas->st.scale_translate();
-  float m6[6];
-  canvas->st.six(m6);
-  skc::Xform xf;
-  xf.sx = m6[0];
-  xf.kx = m6[1];
-  xf.tx = m6[2];
-  xf.ky = m6[3];
-  xf.sy = m6[4];
-  xf.ty = m6[5];
-  xf.lin = !canvas->st.translation();
-  const skc::P q[4] = {xf.map(skc::mkP(left, top)), xf.map(skc::mkP(right, top)),
-                       xf.map(skc::mkP(right, bottom)), xf.map(skc::mkP(left, bottom))};
-  float ml = q[0].x, mr = q[0].x, mt = q[0].y, mb = q[0].y;
-  for (int i = 1; i < 4; ++i) {
-    ml = std::min(q[i].x, ml);
-    mr = std::max(q[i].x, mr);
-    mt = std::min(q[i].y, mt);
-    mb = std::max(q[i].y, mb);
+  const float pts[8] = {left, top, right, top, right, bottom, left, bottom};
+  if (!canvas->st.scale_translate()) {
+    float m6[6];
+    canvas->st.six(m6);
+    if (!skc::ValidMatrix(m6, pts, 4)) return SKITY_CUDA_ERROR_INVALID_ARGUMENT;
   }
-  float* c = canvas->st.clip;
-  // Rect::Intersect (rect.cc:160-172)
-  const float l = std::max(c[0], ml), r = std::min(c[2], mr);
-  const float t = std::max(c[1], mt), b = std::min(c[3], mb);
-  if (!st_ok) canvas->st.bad_clip = true;
-  if (!(l < r && t < b)) {
-    c[0] = c[1] = c[2] = c[3] = 0.f;
-  } else {
-    c[0] = l;
-    c[1] = t;
-    c[2] = r;
-    c[3] = b;
+  NarrowClipBounds(canvas, left, top, right, bottom);
+  if (!canvas->st.scale_translate()) {
+    static const uint8_t kRectVerbs[5] = {SKITY_CUDA_VERB_MOVE, SKITY_CUDA_VERB_LINE,
+                                          SKITY_CUDA_VERB_LINE, SKITY_CUDA_VERB_LINE,
+                                          SKITY_CUDA_VERB_CLOSE};
+    AddClipState(canvas, kRectVerbs, 5, pts, 4, nullptr, 0, 1u /* kIntersect */, 0u);
   }
-  return st_ok ? SKITY_CUDA_SUCCESS : SKITY_CUDA_ERROR_NOT_SUPPORTED;
+  return SKITY_CUDA_SUCCESS;
 }
 
 SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
@@ -2032,6 +2069,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_flush(skity_cuda_canvas canvas) {
     sv.clip_pts = canvas->clip_pts.data();
     sv.clip_wts = canvas->clip_wts.data();
     sv.draw_clip_state = canvas->draw_clip_state.data();
+    if (canvas->any_clip_matrix) sv.clip_matrices = canvas->clip_matrices.data();
   }
   if (!canvas->images.empty()) {
     sv.n_images = (uint32_t)canvas->images.size();
@@ -2226,7 +2264,8 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
   const uint32_t nd = (uint32_t)c.paints.size();
   const uint32_t flags = (c.any_clip ? 1u : 0u) | (c.any_filter ? 2u : 0u) |
                          (!c.clip_states.empty() ? 4u : 0u) | (!c.images.empty() ? 8u : 0u) |
-                         (!c.layers.empty() ? 16u : 0u) | (c.any_matrix ? 32u : 0u);
+                         (!c.layers.empty() ? 16u : 0u) | (c.any_matrix ? 32u : 0u) |
+                         (!c.clip_states.empty() && c.any_clip_matrix ? 64u : 0u);
   out.clear();
   out.insert(out.end(), {'S', 'K', 'S', 'C'});
   const uint32_t hdr[7] = {1u, c.width, c.height, c.has_clear ? 1u : 0u, flags, 0u, 0u};
@@ -2259,7 +2298,14 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
   if (flags & 4) {
     const uint32_t n = (uint32_t)c.clip_states.size();
     Put(out, &n, 1);
-    Put(out, c.clip_states.data(), c.clip_states.size());
+    if (flags & 64) {  // the translations are in the matrix records
+      for (skc::ClipStateRec r : c.clip_states) {
+        r.translate[0] = r.translate[1] = 0.f;
+        Put(out, &r, 1);
+      }
+    } else {
+      Put(out, c.clip_states.data(), c.clip_states.size());
+    }
     Put(out, c.clip_verbs.data(), c.clip_verbs.size());
     Pad4(out, c.clip_verbs.size());
     Put(out, c.clip_pts.data(), c.clip_pts.size());
@@ -2282,6 +2328,7 @@ void SerializeCanvas(const skity_cuda_canvas_s& c, std::vector<uint8_t>& out) {
     Put(out, c.layers.data(), c.layers.size());
   }
   if (flags & 32) Put(out, c.matrices.data(), c.matrices.size());
+  if (flags & 64) Put(out, c.clip_matrices.data(), c.clip_matrices.size());
 }
 
 }  // namespace

@@ -66,6 +66,7 @@ FLAG_PATH_CLIPS = 4  # the clip-state table and per-draw clip states are present
 FLAG_IMAGES = 8  # the image table, its pixels and the per-draw image shaders are present
 FLAG_LAYERS = 16  # the layer table (Canvas::SaveLayer ... Restore) is present
 FLAG_MATRICES = 32  # the per-draw canvas matrix section is present
+FLAG_CLIP_MATRICES = 64  # the per-clip-state canvas matrix section is present
 IDENTITY6 = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0)  # (sx, kx, tx, ky, sy, ty)
 # layer record: Canvas::SaveLayer(bounds, paint) under the canvas translation
 # and global clip bounds in effect before the call; draws [start, restore)
@@ -171,6 +172,10 @@ class Scene:
     # Matrix::Get9 order without the perspective row), or None: each draw's
     # matrix is its paint's translation
     matrices: np.ndarray | None = None
+    # (n_clip_states, 6) float32 canvas matrices of the ClipPath calls (the
+    # states' translations are then zero), or None: each state's matrix is
+    # its translation
+    clip_matrices: np.ndarray | None = None
 
     @property
     def n_draws(self) -> int:
@@ -183,7 +188,8 @@ class Scene:
             (FLAG_PATH_CLIPS if self.path_clips is not None else 0) | \
             (FLAG_IMAGES if self.images is not None else 0) | \
             (FLAG_LAYERS if self.layers is not None else 0) | \
-            (FLAG_MATRICES if self.matrices is not None else 0)
+            (FLAG_MATRICES if self.matrices is not None else 0) | \
+            (FLAG_CLIP_MATRICES if self.clip_matrices is not None else 0)
         out = [MAGIC, struct.pack("<7I", VERSION, self.width, self.height,
                                   1 if self.clear is not None else 0, flags, 0, 0)]
         out.append(np.asarray(self.clear if self.clear is not None else (0, 0, 0, 0),
@@ -240,6 +246,11 @@ class Scene:
             m = np.ascontiguousarray(self.matrices, np.float32).reshape(-1, 6)
             assert len(m) == nd
             out.append(m.tobytes())
+        if self.clip_matrices is not None:
+            assert self.path_clips is not None
+            m = np.ascontiguousarray(self.clip_matrices, np.float32).reshape(-1, 6)
+            assert len(m) == len(self.path_clips[0])
+            out.append(m.tobytes())
         return b"".join(out)
 
     @staticmethod
@@ -291,9 +302,13 @@ class Scene:
             (n_layers,) = struct.unpack_from("<I", buf, o); o += 4
             layers = take(LAYER_DTYPE, n_layers)
         matrices = take(np.float32, 6 * nd, (nd, 6)) if flags & FLAG_MATRICES else None
+        clip_matrices = None
+        if flags & FLAG_CLIP_MATRICES:
+            n = len(path_clips[0]) if path_clips is not None else 0
+            clip_matrices = take(np.float32, 6 * n, (n, 6))
         return Scene(w, h, clear if has_clear else None, verbs, pts, wts, vo, po, wo,
                      paints, grads, sc, so, clips, filters, path_clips, images, layers,
-                     matrices)
+                     matrices, clip_matrices)
 
     def subset(self, first: int, count: int) -> "Scene":
         """Draws [first, first+count) of this scene, same canvas and clear."""
@@ -329,7 +344,8 @@ class Scene:
                      None if self.images is None else
                      self.images[:2] + (self.images[2][first:last].copy(),),
                      self._subset_layers(first, last),
-                     None if self.matrices is None else self.matrices[first:last].copy())
+                     None if self.matrices is None else self.matrices[first:last].copy(),
+                     None if self.clip_matrices is None else self.clip_matrices.copy())
 
     def _subset_layers(self, first: int, last: int):
         """The layers of draws [first, last): those restored before `first`
@@ -369,6 +385,41 @@ def map_clip(clip, rect, tx=0.0, ty=0.0):
     return (float(l), float(t), float(r), float(b))
 
 
+def map_clip_matrix(clip, rect, m):
+    """Canvas::ClipRect / ClipPath(kIntersect) under the canvas matrix `m`
+    (sx, kx, tx, ky, sy, ty): the global clip bounds after the call -- the
+    rect's corners mapped as Matrix::MapRect maps them ((sx x + kx y) + tx,
+    in float32), their min and max, intersected with `clip`, or the empty
+    rect (0, 0, 0, 0)."""
+    f = np.float32
+    sx, kx, tx, ky, sy, ty = (f(v) for v in m)
+    xs, ys = [], []
+    for x, y in ((rect[0], rect[1]), (rect[2], rect[1]), (rect[2], rect[3]),
+                 (rect[0], rect[3])):
+        x, y = f(x), f(y)
+        xs.append(f(f(sx * x) + f(kx * y)) + tx)
+        ys.append(f(f(ky * x) + f(sy * y)) + ty)
+    ml, mr, mt, mb = xs[0], xs[0], ys[0], ys[0]
+    for i in range(1, 4):
+        ml, mr = min(xs[i], ml), max(xs[i], mr)
+        mt, mb = min(ys[i], mt), max(ys[i], mb)
+    l, r = max(f(clip[0]), ml), min(f(clip[2]), mr)
+    t, b = max(f(clip[1]), mt), min(f(clip[3]), mb)
+    if not (l < r and t < b):
+        return (0.0, 0.0, 0.0, 0.0)
+    return (float(l), float(t), float(r), float(b))
+
+
+RECT_VERBS = [MOVE, LINE, LINE, LINE, CLOSE]
+
+
+def rect_points(rect):
+    """Path::AddRect(rect) (src/graphic/path.cc:815-835): clockwise from the
+    top-left corner."""
+    l, t, r, b = rect
+    return [(l, t), (r, t), (r, b), (l, b)]
+
+
 class SceneBuilder:
     """Appends Canvas::DrawPath calls to a Scene, the way skity::Path builds
     its verb/point arrays (src/graphic/path.cc:494-569, 837-860)."""
@@ -383,6 +434,7 @@ class SceneBuilder:
         # path clips: state records and their paths; the current state and
         # the save stack of it (Canvas::Save / Restore)
         self._cstates, self._cverbs, self._cpts, self._cwts = [], [], [], []
+        self._cmatrices = []
         self._cstate, self._csaved, self._draw_cstate = 0, [], []
         self._images, self._blobs, self._nblob, self._shaders = [], [], 0, []
         self._layers = []
@@ -473,9 +525,15 @@ class SceneBuilder:
             self._cstate = self._csaved.pop()
 
     def clip_path(self, verbs, points, op, fill_type=WINDING, weights=(), translate=(0.0, 0.0),
-                  bounds=NO_CLIP):
+                  bounds=NO_CLIP, matrix=None):
         """Canvas::ClipPath(path, op) on the current state, with the canvas
-        translation and the global clip bounds in effect at the call."""
+        translation (or the whole canvas matrix `matrix`, sx, kx, tx, ky, sy,
+        ty, with `translate` zero) and the global clip bounds in effect at the
+        call."""
+        if matrix is not None:
+            assert tuple(translate) == (0.0, 0.0)
+        self._cmatrices.append(None if matrix is None
+                               else tuple(float(np.float32(v)) for v in matrix))
         st = np.zeros((), CLIP_STATE_DTYPE)
         verbs = np.asarray(verbs, np.uint8)
         points = np.asarray(points, np.float32).reshape(-1, 2)
@@ -524,6 +582,15 @@ class SceneBuilder:
         cat = lambda xs, dt, shp: (np.concatenate(xs).astype(dt) if xs else np.zeros(shp, dt))
         paints = (np.array(self._paints, PAINT_DTYPE) if self._paints
                   else np.zeros(0, PAINT_DTYPE))
+        cstates = np.array(self._cstates, CLIP_STATE_DTYPE) if self._cstates else None
+        clip_matrices = None
+        if any(m is not None for m in self._cmatrices):
+            # every state's matrix in the section; the translations move there
+            clip_matrices = np.array([m if m is not None else
+                                      (1.0, 0.0, float(c["translate"][0]), 0.0, 1.0,
+                                       float(c["translate"][1]))
+                                      for m, c in zip(self._cmatrices, cstates)], np.float32)
+            cstates["translate"] = 0.0
         matrices = None
         if any(m is not None for m in self._matrices):
             # every draw's matrix in the section; the paints' translations move there
@@ -544,7 +611,7 @@ class SceneBuilder:
                       if any(c != NO_CLIP for c in self._clips) else None),
                      (np.array(self._filters, FILTER_DTYPE)
                       if any(int(f["type"]) != FILTER_NONE for f in self._filters) else None),
-                     ((np.array(self._cstates, CLIP_STATE_DTYPE), cat(self._cverbs, np.uint8, 0),
+                     ((cstates, cat(self._cverbs, np.uint8, 0),
                        cat(self._cpts, np.float32, (0, 2)), cat(self._cwts, np.float32, 0),
                        np.asarray(self._draw_cstate, np.uint32))
                       if self._cstates else None),
@@ -552,7 +619,7 @@ class SceneBuilder:
                        np.array(self._shaders, IMAGE_SHADER_DTYPE))
                       if self._images else None),
                      np.array(self._layers, LAYER_DTYPE) if self._layers else None,
-                     matrices)
+                     matrices, clip_matrices)
 
 
 def image_shader(image, filter=FILTER_NEAREST, tile_x=TILE_CLAMP, tile_y=TILE_CLAMP,

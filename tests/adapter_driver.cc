@@ -226,7 +226,7 @@ int main() {
   // Scale / Rotate / Skew: the canvas matrix this canvas computed reaches
   // the C ABI as Get9 gives it (printed beside it by the reference's
   // GetTotalMatrix); a gradient under a rotation is refused, and a ClipRect
-  // under a rotation becomes a path clip of the rect (refused)
+  // under a rotation becomes a path clip of the rect under that matrix
   Paint solid;
   solid.SetColor(ColorSetARGB(255, 10, 20, 30));
   paint.SetShader(Shader::MakeRadial(Point{20, 15, 0, 1}, 12.f, colors, nullptr, 3, TileMode::kClamp));

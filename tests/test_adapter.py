@@ -11,6 +11,9 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.environ.get("SKITY_REFERENCE", "/root/reference")
+# set_matrix arguments as the driver's stub prints them (%a)
+T21 = "0x1p+0 0x0p+0 0x1p+1 0x0p+0 0x1p+0 0x1p+0 0x0p+0 0x0p+0 0x1p+0"
+IDENTITY = "0x1p+0 0x0p+0 0x0p+0 0x0p+0 0x1p+0 0x0p+0 0x0p+0 0x0p+0 0x1p+0"
 
 
 @pytest.fixture(scope="module")
@@ -80,10 +83,11 @@ def test_clip_rect_forwarded(driver_output):
 def test_difference_clip_rect_is_a_path_clip(driver_output):
     # ClipRect(0, 0, 10, 10, kDifference) under Translate(2, 1): the rect's
     # path (Canvas::OnClipRect) clipped on the C ABI canvas at this save
-    # level, with the global clip bounds and the translation of the call
-    assert driver_output[24:27] == ["save", "clip 3.5 3 27 21", "translate 2 1"]
+    # level, with the global clip bounds and the canvas matrix of the call
+    # (set for the call, then the identity again)
+    assert driver_output[24:27] == ["save", "clip 3.5 3 27 21", "set_matrix " + T21]
     assert driver_output[27] == "clip_path op=0 fill=0 verbs=0,1,1,1,5, points=0,0,10,0,10,10,0,10,"
-    assert driver_output[28] == "translate -2 -1"
+    assert driver_output[28] == "set_matrix " + IDENTITY
     # the draw under it is taken (the path clip is recorded on the state)
     assert driver_output[29:32] == ["save", "clip 3.5 3 27 21", "set_matrix 0x1p+0 0x0p+0 0x1p+1 0x0p+0 0x1p+0 0x1p+0 0x0p+0 0x0p+0 0x1p+0"]
     assert driver_output[32].startswith("draw verbs=0,1,2,3,4,5,")
@@ -151,6 +155,16 @@ def test_scale_rotate_skew_forwarded(driver_output):
     assert driver_output[i + 9].startswith("draw ") and driver_output[i + 10:i + 12] == \
         ["restore", "status=0"]
     # a gradient under the rotation is refused; a ClipRect under it is a
-    # path clip of the rect (refused), and so are the draws under it
-    assert driver_output[i + 12:i + 15] == ["save", "set_matrix " + total[6:], "restore"]
-    assert driver_output[i + 15:i + 19] == ["status=-5", "status=-5", "status=-5", "restore"]
+    # path clip of the rect under the rotation (the global clip bounds
+    # narrowed by the rotated rect's bounds first), and a draw under it is
+    # taken
+    assert driver_output[i + 12:i + 16] == ["save", "set_matrix " + total[6:], "restore",
+                                            "status=-5"]
+    clip = "clip 3.40192 1.33494 26.3923 8.79006"
+    assert driver_output[i + 16:i + 21] == [
+        clip, "set_matrix " + total[6:],
+        "clip_path op=1 fill=0 verbs=0,1,1,1,5, points=0,0,10,0,10,10,0,10,",
+        "set_matrix " + IDENTITY, "status=0"]
+    assert driver_output[i + 21:i + 24] == ["save", clip, "set_matrix " + total[6:]]
+    assert driver_output[i + 24].startswith("draw ")
+    assert driver_output[i + 25:i + 28] == ["restore", "status=0", "restore"]

@@ -164,8 +164,9 @@ def test_canvas_matrices_bit_exact(cpu_pipeline, oracle_lib, seed):
 
 def test_matrix_limits_refused(cpu_pipeline, oracle_lib):
     """Under a rotation or skew a gradient is refused (its device_to_local
-    needs the general inverse), as is a blur under any canvas matrix; the
-    oracle refuses the same draws."""
+    needs the general inverse), as is a blur (its filtered bitmap's image
+    draw inverts the matrix the same way); the oracle refuses the same
+    draws."""
     from test_oracle_pin import matrix_scene
     sc = matrix_scene(S.SEED_BASE + 365, shaded=False)
     g = S.SceneBuilder(sc.width, sc.height)
@@ -178,7 +179,7 @@ def test_matrix_limits_refused(cpu_pipeline, oracle_lib):
     blur = S.default_paint()
     blur["blur_style"], blur["blur_radius"] = 1, 3.0
     h = S.SceneBuilder(sc.width, sc.height)
-    h.draw_path(*tri, blur, matrix=(2.0, 0.0, 0.0, 0.0, 2.0, 0.0))
+    h.draw_path(*tri, blur, matrix=(0.9, 0.3, 4.0, -0.3, 0.9, 6.0))
     for bad in (g.build(), h.build()):
         b = bad.to_bytes()
         out = np.zeros((bad.height, bad.width, 4), np.uint8)
@@ -199,16 +200,27 @@ def test_clip_rect_bit_exact(cpu_pipeline, oracle_lib, seed):
     assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
 
 
-def test_blur_under_clip_refused(cpu_pipeline, oracle_lib):
-    """A blurred draw under a narrowed clip is refused by the batch builder
-    (not supported) rather than drawn unclipped."""
+def test_blur_under_clip_bit_exact(cpu_pipeline, oracle_lib):
+    """A blurred draw under a narrowed clip: the temp canvas is unclipped,
+    the filtered bitmap's image draw is clipped."""
     sc = S.config4(seed=S.SEED_BASE + 390, n_outlines=20, width=96, height=96, blur_frac=1.0)
     sc.clips = np.tile(np.array([[4, 4, 60, 60]], np.float32), (sc.n_draws, 1))
-    b = sc.to_bytes()
-    out = np.zeros((sc.height, sc.width, 4), np.uint8)
-    st = (ctypes.c_uint64 * 6)()
-    rc = cpu_pipeline.skc_cpu_render_mode(b, len(b), out.ctypes.data, st, 0, 0)
-    assert rc == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    assert oracle_lib.compare(got, ref)["bad_pixels"] == 0
+    assert (got[61:] == got[95, 95]).all()  # nothing below the clip
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_clips_and_blurs_under_matrices_bit_exact(cpu_pipeline, oracle_lib, seed):
+    """ClipPath and rotated ClipRect under canvas matrices, rotated draws
+    under path clips, blurs under scales, clip rects and path clips."""
+    from test_oracle_pin import matrix_clips_scene
+    sc = matrix_clips_scene(S.SEED_BASE + 470 + seed)
+    got, _ = cpu_render(cpu_pipeline, sc)
+    ref, _ = oracle_lib.render(sc)
+    c = oracle_lib.compare(got, ref)
+    assert c["bad_pixels"] == 0, c
 
 
 def test_every_blend_mode_bit_exact(cpu_pipeline, oracle_lib):

@@ -111,3 +111,54 @@ def test_recorded_transforms_write_matrices(oracle_lib):
         out = subprocess.check_output([ref_matrix] + args, text=True).split()
         want = np.array([float.fromhex(v) for v in out], np.float32)
         assert want[[0, 1, 2, 3, 4, 5]].tobytes() == sc.matrices[k].tobytes(), k
+
+
+def test_recorded_clips_under_matrices(oracle_lib):
+    """ClipRect under a rotation becomes a kIntersect path clip of the rect
+    (Path::AddRect) under that matrix, after the global clip bounds narrow
+    to the rotated rect's bounds; ClipPath under a scale keeps its matrix;
+    the draws carry the narrowed bounds.  The recorded scene renders as the
+    same calls made on a scene builder (the oracle is pinned to the
+    reference for these cases)."""
+    from skity_gb300.canvas import Paint, Path
+    blob = Path().MoveTo(5, 5).QuadTo(40, 0, 35, 20).CubicTo(30, 40, 10, 45, 3, 30).Close()
+
+    def ops(cv):
+        cv.Clear((1.0, 1.0, 1.0, 1.0))
+        cv.Save()
+        cv.Rotate(20, 60, 48)
+        cv.ClipRect(20, 15, 100, 80)
+        cv.DrawPath(blob, Paint().SetColor(0xFFC03060))
+        cv.Restore()
+        cv.Scale(2.0, 1.5)
+        cv.ClipPath(blob, S.CLIP_INTERSECT)
+        cv.DrawPath(blob, Paint().SetColor(0xFF3060C0).SetAlphaF(0.7))
+    sc = _record(ops).to_scene()
+    states, _, _, _, per_draw = sc.path_clips
+    assert sc.clip_matrices is not None and len(states) == 2
+    rot = tuple(float(v) for v in sc.matrices[0])
+    assert tuple(float(v) for v in sc.clip_matrices[0]) == rot
+    assert int(states[0]["op"]) == S.CLIP_INTERSECT and int(states[0]["nv"]) == 5
+    glob = S.map_clip_matrix(S.NO_CLIP, (20.0, 15.0, 100.0, 80.0), rot)
+    assert tuple(float(v) for v in states[0]["bounds"]) == glob
+    assert tuple(float(v) for v in sc.clips[0]) == glob
+    sm = (2.0, 0.0, 0.0, 0.0, 1.5, 0.0)
+    assert tuple(float(v) for v in sc.clip_matrices[1]) == sm
+    pts = np.asarray(blob.points, np.float32).reshape(-1, 2)
+    g2 = S.map_clip_matrix(S.NO_CLIP, (pts[:, 0].min(), pts[:, 1].min(), pts[:, 0].max(),
+                                       pts[:, 1].max()), sm)
+    assert tuple(float(v) for v in states[1]["bounds"]) == g2 and g2[0] == 6.0
+    assert list(per_draw) == [1, 2]
+    b = S.SceneBuilder(sc.width, sc.height)
+    b.save()
+    b.clip_path(S.RECT_VERBS, S.rect_points((20.0, 15.0, 100.0, 80.0)), S.CLIP_INTERSECT,
+                bounds=glob, matrix=rot)
+    b.draw_path(blob.verbs, blob.points, Paint().SetColor(0xFFC03060).rec, clip=glob,
+                matrix=rot)
+    b.restore()
+    b.clip_path(blob.verbs, blob.points, S.CLIP_INTERSECT, bounds=g2, matrix=sm)
+    b.draw_path(blob.verbs, blob.points, Paint().SetColor(0xFF3060C0).SetAlphaF(0.7).rec,
+                clip=g2, matrix=sm)
+    got, _ = oracle_lib.render(sc)
+    want, _ = oracle_lib.render(b.build())
+    assert np.array_equal(got, want)

@@ -92,11 +92,10 @@ def test_canvas_transforms_match_oracle(gpu_ctx, oracle_lib):
 
 
 def test_canvas_transform_limits(gpu_ctx):
-    """A gradient under a rotation, a ClipRect under a rotation and the
-    draws under it, and draws under perspective return NOT_SUPPORTED and
-    draw nothing."""
+    """A gradient or a blur under a rotation, and draws under perspective,
+    return NOT_SUPPORTED and draw nothing."""
     from skity_gb300 import _lib
-    from skity_gb300.canvas import Canvas, Paint, Shader
+    from skity_gb300.canvas import Canvas, MaskFilter, Paint, Shader
     tri, _ = _shapes()
     bitmap = np.full((40, 48, 4), 7, np.uint8)
     canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
@@ -105,15 +104,108 @@ def test_canvas_transform_limits(gpu_ctx):
     with pytest.raises(_lib.SkityCudaError) as e:
         canvas.DrawPath(tri, Paint().SetShader(grad))
     assert e.value.code == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
-    canvas.Save()
     with pytest.raises(_lib.SkityCudaError) as e:
-        canvas.ClipRect(0, 0, 10, 10)
-    assert e.value.code == -5  # SKITY_CUDA_ERROR_NOT_SUPPORTED
-    with pytest.raises(_lib.SkityCudaError):
-        canvas.DrawPath(tri, Paint())
-    canvas.Restore()
+        canvas.DrawPath(tri, Paint().SetMaskFilter(MaskFilter.MakeBlur(1, 3.0)))
+    assert e.value.code == -5
     canvas.SetMatrix((1, 0, 0, 0, 1, 0, 0.01, 0, 1))
     with pytest.raises(_lib.SkityCudaError):
         canvas.DrawPath(tri, Paint())
     canvas.Flush()
     assert (bitmap == 7).all()
+
+
+def test_clips_and_blurs_under_matrices(gpu_ctx, oracle_lib):
+    """ClipPath and rotated ClipRect under canvas matrices, rotated draws
+    under path clips, blurs under scales, clip rects and path clips; one
+    batch."""
+    from test_oracle_pin import matrix_clips_scene
+    scenes = [matrix_clips_scene(S.SEED_BASE + 470 + k) for k in range(6)]
+    scenes.append(matrix_clips_scene(S.SEED_BASE + 476, 512, 384, 120))
+    for got, sc in zip(gpu_ctx.render_streams(scenes), scenes):
+        assert check(oracle_lib, got, sc)["bad_pixels"] == 0
+
+
+def test_canvas_clips_under_matrices(gpu_ctx, oracle_lib):
+    """The canvas API: ClipRect under a rotation (a rect path clip),
+    ClipPath under a scale and a skew, a blur under a scale, a clip rect and
+    a path clip; the expected scene built with the reference's rules
+    (global clip bounds by the mapped bounds, Path::AddRect) and rendered by
+    the oracle."""
+    from skity_gb300.canvas import Canvas, MaskFilter, Paint
+    tri, blob = _shapes()
+    W, H = 120, 96
+    bitmap = np.zeros((H, W, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    sb = S.SceneBuilder(W, H)
+    state = {"glob": S.NO_CLIP, "stack": []}
+
+    def m6():
+        m9 = canvas.GetTotalMatrix()
+        return (m9[0], m9[1], m9[2], m9[3], m9[4], m9[5])
+
+    def draw(path, paint):
+        canvas.DrawPath(path, paint)
+        p = paint.rec.copy()
+        if paint.mask_filter is not None:
+            p["blur_style"], p["blur_radius"] = paint.mask_filter.style, paint.mask_filter.radius
+        sb.draw_path(path.verbs, path.points, p, path.weights, clip=state["glob"], matrix=m6())
+
+    def save():
+        canvas.Save()
+        sb.save()
+        state["stack"].append(state["glob"])
+
+    def restore():
+        canvas.Restore()
+        sb.restore()
+        state["glob"] = state["stack"].pop()
+
+    def clip_rect(rect):
+        canvas.ClipRect(*rect)
+        m = m6()
+        state["glob"] = S.map_clip_matrix(state["glob"], rect, m)
+        if m[1] != 0.0 or m[3] != 0.0:
+            sb.clip_path(S.RECT_VERBS, S.rect_points(rect), S.CLIP_INTERSECT, S.WINDING,
+                         bounds=state["glob"], matrix=m)
+
+    def clip_path(path, op):
+        canvas.ClipPath(path, op)
+        m = m6()
+        pts = np.asarray(path.points, np.float32).reshape(-1, 2)
+        if op == S.CLIP_INTERSECT:
+            pb = (pts[:, 0].min(), pts[:, 1].min(), pts[:, 0].max(), pts[:, 1].max())
+            state["glob"] = S.map_clip_matrix(state["glob"], pb, m)
+        sb.clip_path(path.verbs, pts, op, path.fill_type, path.weights, bounds=state["glob"],
+                     matrix=m)
+
+    red = Paint().SetFillColor(0.9, 0.1, 0.1, 0.8)
+    blue = Paint().SetFillColor(0.1, 0.2, 0.9, 0.6)
+    stroke = Paint().SetStyle(1).SetStrokeWidth(3.0).SetFillColor(0, 0, 0, 1)
+    stroke.SetStrokeColor(0.1, 0.6, 0.2, 0.9)
+    blur = Paint().SetFillColor(0.2, 0.2, 0.7, 0.9).SetMaskFilter(MaskFilter.MakeBlur(1, 4.0))
+    save()
+    canvas.Rotate(20, 60, 48)
+    clip_rect((20.0, 15.0, 100.0, 80.0))
+    canvas.Translate(30, 20)
+    draw(blob, red)
+    canvas.Skew(0.25, 0.0)
+    draw(tri, stroke)
+    restore()
+    save()
+    canvas.Scale(2.0, 1.5)
+    clip_path(blob, S.CLIP_INTERSECT)
+    draw(tri, blue)
+    canvas.Translate(3, 4)
+    draw(blob, blur)
+    canvas.Skew(0.3, -0.2)
+    clip_path(tri, S.CLIP_DIFFERENCE)
+    draw(blob, stroke)
+    restore()
+    clip_rect((5.0, 5.0, 70.0, 60.0))
+    canvas.Scale(1.25, 1.25)
+    draw(blob, Paint().SetFillColor(0.8, 0.5, 0.1, 0.9).SetMaskFilter(MaskFilter.MakeBlur(3, 2.5)))
+    canvas.Flush()
+    sc = sb.build()
+    assert sc.clip_matrices is not None
+    check(oracle_lib, bitmap, sc)

@@ -465,6 +465,101 @@ def test_clip_path_cases(ref):
     _pin(ref, clip_path_cases_scene())
 
 
+def _random_matrix(rng, width, height, kind):
+    """A canvas matrix (sx, kx, tx, ky, sy, ty) of one of five kinds:
+    0 translation, 1 scale and translate, 2 rotation about the centre,
+    3 skew, 4 general affine."""
+    f = np.float32
+    if kind == 0:
+        m = (1.0, 0.0, rng.uniform(-20, 20), 0.0, 1.0, rng.uniform(-20, 20))
+    elif kind == 1:
+        m = (rng.uniform(0.5, 1.6) * rng.choice([-1, 1]), 0.0, rng.uniform(-20, 40), 0.0,
+             rng.uniform(0.5, 1.6), rng.uniform(-20, 40))
+        if m[0] < 0:
+            m = (m[0], 0.0, m[2] + width, 0.0, m[4], m[5])
+    elif kind == 2:
+        a = f(rng.uniform(-3.1, 3.1))
+        c, s_ = np.cos(a), np.sin(a)
+        cx, cy = f(width / 2), f(height / 2)
+        m = (c, -s_, f(cx - (c * cx - s_ * cy)), s_, c, f(cy - (s_ * cx + c * cy)))
+    elif kind == 3:
+        m = (1.0, rng.uniform(-0.5, 0.5), rng.uniform(-15, 15), rng.uniform(-0.4, 0.4), 1.0,
+             rng.uniform(-15, 15))
+    else:
+        m = tuple(rng.uniform(-1.1, 1.1, 6) * (1, 1, 60, 1, 1, 50) + (0.3, 0, width / 2, 0, 0.3,
+                                                                   height / 2))
+    return tuple(float(f(v)) for v in m)
+
+
+def matrix_clips_scene(seed=S.SEED_BASE + 470, width=150, height=110, n_ops=70):
+    """ClipPath under canvas matrices of every kind, ClipRect under them (a
+    rect path clip under a rotation or skew, Canvas::OnClipRect), nested
+    under Save / Restore; fills and strokes under any matrix beneath those
+    clips; blurs (every style) under scale-and-translate matrices, clip
+    rects and path clips."""
+    rng = np.random.default_rng(seed & 0xFFFF)
+    b = S.SceneBuilder(width, height, clear=(1.0, 1.0, 1.0, 1.0))
+    glob, m = S.NO_CLIP, (1.0, 0.0, 0.0, 0.0, 1.0, 0.0)
+    stack = []
+    for i in range(n_ops):
+        r = rng.random()
+        st = m[1] == 0.0 and m[3] == 0.0
+        if r < 0.07 and stack:
+            b.restore()
+            glob, m = stack.pop()
+        elif r < 0.14:
+            b.save()
+            stack.append((glob, m))
+        elif r < 0.24:
+            m = _random_matrix(rng, width, height, int(rng.integers(0, 5)))
+        elif r < 0.34:
+            op = S.CLIP_INTERSECT if rng.random() < 0.7 else S.CLIP_DIFFERENCE
+            verbs, pts = _random_closed_path(rng, [-10, -10], [width + 10, height + 10],
+                                             int(rng.integers(3, 8)))
+            if op == S.CLIP_INTERSECT:  # Canvas::ClipPath narrows the bounds first
+                pb = (pts[:, 0].min(), pts[:, 1].min(), pts[:, 0].max(), pts[:, 1].max())
+                glob = S.map_clip_matrix(glob, pb, m)
+            fill = S.EVEN_ODD if rng.random() < 0.3 else S.WINDING
+            b.clip_path(verbs, pts, op, fill, bounds=glob, matrix=m)
+        elif r < 0.42:
+            x0, y0 = rng.uniform(-10, [width * 0.7, height * 0.7])
+            rect = tuple(float(np.float32(v)) for v in
+                         (x0, y0, x0 + rng.uniform(30, 120), y0 + rng.uniform(25, 90)))
+            glob = S.map_clip_matrix(glob, rect, m)
+            if not st:  # SWCanvas::OnClipRect -> Canvas::OnClipRect: the rect as a path
+                b.clip_path(S.RECT_VERBS, S.rect_points(rect), S.CLIP_INTERSECT, S.WINDING,
+                            bounds=glob, matrix=m)
+        else:
+            verbs, pts = _random_closed_path(rng, [-10, -10], [width + 10, height + 10],
+                                             int(rng.integers(2, 10)))
+            p = S.default_paint()
+            p["style"] = S.STROKE if rng.random() < 0.2 else S.FILL
+            p["stroke_width"] = float(rng.uniform(1, 6))
+            p["fill_type"] = S.EVEN_ODD if rng.random() < 0.3 else S.WINDING
+            p["fill_color"] = tuple(np.append(rng.uniform(0, 1, 3),
+                                              rng.uniform(0.3, 1)).astype(np.float32))
+            p["stroke_color"] = p["fill_color"]
+            if st and rng.random() < 0.35:
+                p["blur_style"] = int(rng.integers(1, 5))
+                p["blur_radius"] = float(np.float32(rng.uniform(1.0, 6.0)))
+            elif st and rng.random() < 0.2:
+                cols = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+                p["gradient"] = b.add_gradient(S.GRAD_LINEAR,
+                                               (float(pts[0, 0]), float(pts[0, 1])),
+                                               (float(pts[1, 0]), float(pts[1, 1])), (0.0, 0.0),
+                                               cols)
+            b.draw_path(verbs, pts, p, clip=glob, matrix=m)
+    return b.build()
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_clips_and_blurs_under_matrices(ref, seed):
+    sc = matrix_clips_scene(S.SEED_BASE + 470 + seed)
+    assert sc.clip_matrices is not None
+    assert (sc.paints["blur_style"] != 0).any()
+    _pin(ref, sc)
+
+
 @pytest.mark.parametrize("seed", range(8))
 def test_layers(ref, seed):
     """Canvas::SaveLayer / Restore: layers over and past the canvas with
