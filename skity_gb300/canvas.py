@@ -10,6 +10,7 @@ reference's own: ``Path().MoveTo(..).LineTo(..)``, ``Paint().SetColor(..)``,
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -313,6 +314,8 @@ class Context:
         _lib.check(self.lib.skity_cuda_context_create(ctypes.byref(info), ctypes.byref(h)),
                    "skity_cuda_context_create")
         self.handle = h
+        # batches and canvases made on this context: closed before it is
+        self._dependents = weakref.WeakSet()
 
     def stats(self) -> dict:
         st = _lib.Stats_()
@@ -321,6 +324,8 @@ class Context:
 
     def close(self):
         if self.handle:
+            for d in list(self._dependents):
+                d.close()
             self.lib.skity_cuda_context_destroy(self.handle)
             self.handle = None
 
@@ -371,6 +376,7 @@ class Batch:
         _lib.check(self.lib.skity_cuda_batch_create(ctx.handle, n, ptrs, lens, ctypes.byref(h)),
                    "skity_cuda_batch_create")
         self.handle = h
+        ctx._dependents.add(self)
 
     def render(self) -> dict:
         _lib.check(self.lib.skity_cuda_batch_render(self.handle), "skity_cuda_batch_render")
@@ -426,6 +432,9 @@ class Canvas:
 
     def __init__(self, ctx: Context, handle, bitmap: np.ndarray):
         self.ctx, self.lib, self.handle, self.bitmap = ctx, ctx.lib, handle, bitmap
+        deps = getattr(ctx, "_dependents", None)  # a recorder's canvas has no context
+        if deps is not None:
+            deps.add(self)
 
     @staticmethod
     def MakeCUDACanvas(ctx: Context, bitmap: np.ndarray | None):
