@@ -324,7 +324,8 @@ def serving_pool(n: int = 64):
     return out
 
 
-def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512):
+def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512,
+            workers: int = 2):
     """Poisson request streams against the serving loop: for each rate,
     arrivals for `seconds` seconds (seeded exponential gaps), requests
     drawn in turn from the pool; latency = submit -> pixels on the host.
@@ -347,7 +348,7 @@ def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512)
                "requests_per_s": len(pool) * 1e3 / st["device_ms"], "ms": st["device_ms"]}
     results = []
     for rate in rates:
-        srv = Server(device, workers=2, max_batch=64)
+        srv = Server(device, workers=workers, max_batch=64)
         rng = random.Random(0x5EED0005 + int(rate))
         tickets = []
         lock = threading.Lock()
@@ -414,7 +415,7 @@ def serving(ctx, rates, seconds: float, device: int, max_outstanding: int = 512)
                         "vs_offline_paths": (npaths / wall) / offline["paths_per_s"]})
     return {"workload": "Poisson arrivals; requests cycle through 64 seeded canvases (sides "
                         "log-uniform [128,2048], 10-5,000 paths, solid fills); admission budget "
-                        "40 GiB; 2 workers, up to 64 requests per batch",
+                        f"40 GiB; {workers} workers, up to 64 requests per batch",
             "offline_batched": offline, "rates": results}
 
 
@@ -686,7 +687,7 @@ def run_gpu(args, rank, world, local):
         line["other_workloads"] = other_workloads(ctx, max(1, min(args.steps, 5)), threads)
     if rank == 0 and args.serve_seconds > 0:
         line["serving"] = serving(ctx, [float(r) for r in args.serve_rates.split(",")],
-                                  args.serve_seconds, local)
+                                  args.serve_seconds, local, workers=args.serve_workers)
     batch.close()
     ctx.close()
     if rank == 0:
@@ -720,6 +721,8 @@ def main():
                     help="skip the 512x512, 2048x2048 and glyph-dense scenes")
     ap.add_argument("--serve-rates", default="200,1000,5000",
                     help="Poisson request rates (requests/s) of the serving runs")
+    ap.add_argument("--serve-workers", type=int, default=2,
+                    help="serving loop workers (concurrent batches, each its own stream)")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window per rate (the serving workload's 60 s); 0 skips")
     ap.add_argument("--no-cpu", action="store_true")
