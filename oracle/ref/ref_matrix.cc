@@ -2,11 +2,13 @@
 // a sequence of transform calls (Canvas::Translate / Scale / Rotate / Skew /
 // Concat / SetMatrix on a software canvas), printed as Matrix::Get9 gives it
 // (nine %a floats).  Usage: ref_matrix op args... ; ops:
-//   t dx dy | s sx sy | r deg px py | k kx ky | c m0..m8 | m m0..m8
+//   t dx dy | s sx sy | r deg px py | k kx ky | c m0..m8 | m m0..m8 |
+//   S (Save) | R (Restore) | L l t r b (SaveLayer with a default paint)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <skity/graphic/bitmap.hpp>
+#include <skity/graphic/paint.hpp>
 #include <skity/render/canvas.hpp>
 
 int main(int argc, char** argv) {
@@ -35,6 +37,13 @@ int main(int argc, char** argv) {
       m.Set9(b);
       if (op == 'c') canvas->Concat(m);
       else canvas->SetMatrix(m);
+    } else if (op == 'S') {
+      canvas->Save();
+    } else if (op == 'R') {
+      canvas->Restore();
+    } else if (op == 'L') {
+      const float l = f(), t = f(), r = f(), b = f();
+      canvas->SaveLayer(skity::Rect::MakeLTRB(l, t, r, b), skity::Paint());
     } else {
       return 2;
     }

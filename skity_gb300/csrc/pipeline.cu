@@ -1042,10 +1042,25 @@ struct skity_cuda_canvas_s {
   std::vector<float> stop_colors, stop_offsets;
   // canvas matrix, global clip bounds and their save stack
   struct State {
-    skc::Mat4 m;  // the canvas matrix (LayerState::CurrentMatrix), column-major
+    // the canvas matrix as the reference's CanvasState keeps it (canvas_state
+    // .hpp:41,55,89-95): a SaveLayer starts a layer state whose world matrix
+    // is the total matrix at the call and whose own matrix starts at the
+    // identity; the calls after it multiply the layer's own matrix, and the
+    // total is world * own (Matrix::operator*).  Column-major.
+    skc::Mat4 m;      // the total matrix (GetTotalMatrix)
+    skc::Mat4 world;  // the layer state's world matrix (the identity outside layers)
+    skc::Mat4 own;    // the layer state's CurrentMatrix
+    void set_own(const skc::Mat4& o) {
+      own = o;
+      m = skc::MatMul(world, own);
+    }
     float clip[4] = {-1e9f, -1e9f, 1e9f, 1e9f};  // kMaxCullRect
     uint32_t path_clip = 0;  // the path-clip state (1-based in clip_states; 0: none)
-    State() { m.identity(); }
+    State() {
+      m.identity();
+      world.identity();
+      own.identity();
+    }
     float tx() const { return m.e[3][0]; }
     float ty() const { return m.e[3][1]; }
     // no perspective: CopyWithMatrix and MapRect then map points by
@@ -1443,6 +1458,8 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_clear(skity_cuda_canvas canvas, const f
     paint.miter_limit = 4.f;
     const skity_cuda_canvas_s::State keep = canvas->st;
     canvas->st.m.identity();
+    canvas->st.world.identity();
+    canvas->st.own.identity();
     canvas->st.clip[0] = canvas->st.clip[1] = -1e9f;
     canvas->st.clip[2] = canvas->st.clip[3] = 1e9f;
     const int32_t rc = skity_cuda_canvas_draw_path(canvas, &path, &paint);
@@ -1811,7 +1828,12 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_save_layer(skity_cuda_canvas canvas, co
   canvas->layers.push_back(L);
   canvas->saved_layer.push_back((uint32_t)canvas->layers.size());
   canvas->dirty = true;
-  return skity_cuda_canvas_clip_rect(canvas, bounds[0], bounds[1], bounds[2], bounds[3]);
+  const int32_t rc = skity_cuda_canvas_clip_rect(canvas, bounds[0], bounds[1], bounds[2], bounds[3]);
+  // CanvasState::SaveLayer -> PushLayer: a layer state over the total matrix
+  canvas->st.world = canvas->st.m;
+  canvas->st.own.identity();
+  canvas->st.m = skc::MatMul(canvas->st.world, canvas->st.own);
+  return rc;
 }
 
 // The canvas matrix times another (LayerState::Translate / Scale / Rotate
@@ -1829,7 +1851,7 @@ static int32_t CanvasConcat(skity_cuda_canvas canvas, skc::RecordedOp::Type type
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
-  canvas->st.m = skc::MatMul(canvas->st.m, m);
+  canvas->st.set_own(skc::MatMul(canvas->st.own, m));
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -1881,7 +1903,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix(skity_cuda_canvas canvas, co
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
-  canvas->st.m = skc::MatFrom9(m);
+  canvas->st.set_own(skc::MatFrom9(m));
   return SKITY_CUDA_SUCCESS;
 }
 
@@ -1905,7 +1927,7 @@ SKITY_CUDA_API int32_t skity_cuda_canvas_set_matrix44(skity_cuda_canvas canvas, 
     canvas->ops.push_back(std::move(op));
     return SKITY_CUDA_SUCCESS;
   }
-  canvas->st.m = skc::MatFrom16(m);
+  canvas->st.set_own(skc::MatFrom16(m));
   return SKITY_CUDA_SUCCESS;
 }
 

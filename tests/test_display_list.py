@@ -162,3 +162,63 @@ def test_recorded_clips_under_matrices(oracle_lib):
     got, _ = oracle_lib.render(sc)
     want, _ = oracle_lib.render(b.build())
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_recorded_matrices_inside_layers_match_reference(seed):
+    """Translations, Save / Restore and SaveLayer in random order: the matrix
+    of a draw inside a layer is the layer's world matrix times the matrix
+    the calls after SaveLayer built (the reference's CanvasState layer
+    states), bit for bit the reference Canvas's GetTotalMatrix
+    (oracle/_ref/ref_matrix) -- not the product taken call by call."""
+    import os
+    import subprocess
+    from skity_gb300.canvas import Paint, Path
+    ref_matrix = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                              "oracle", "_ref", "ref_matrix")
+    if not os.path.exists(ref_matrix):
+        pytest.skip("reference build not present")
+    rng = np.random.default_rng(0x1A7E + seed)
+    f = np.float32
+    seq, depth_layers, depth = [], 0, 0
+    for _ in range(24):
+        r = rng.random()
+        if r < 0.45:
+            seq.append(("t", (f(rng.uniform(-9, 9)), f(rng.uniform(-9, 9)))))
+        elif r < 0.6:
+            seq.append(("S", ()))
+            depth += 1
+        elif r < 0.75 and depth_layers == 0:
+            seq.append(("L", (f(-50), f(-50), f(200), f(200))))
+            depth += 1
+            depth_layers = depth
+        elif depth > 0:
+            seq.append(("R", ()))
+            if depth == depth_layers:
+                depth_layers = 0
+            depth -= 1
+    tri = Path().MoveTo(10, 10).LineTo(60, 20).LineTo(20, 70).Close()
+
+    def ops(cv):
+        cv.Clear((1.0, 1.0, 1.0, 1.0))
+        for name, a in seq:
+            if name == "t":
+                cv.Translate(float(a[0]), float(a[1]))
+            elif name == "S":
+                cv.Save()
+            elif name == "L":
+                cv.SaveLayer(tuple(float(v) for v in a), Paint())
+            else:
+                cv.Restore()
+            cv.DrawPath(tri, Paint().SetColor(0xFF3060C0))
+        for _ in range(depth):  # close what is open (a layer is drawn at its restore)
+            cv.Restore()
+    sc = _record(ops).to_scene()
+    m = sc.matrices if sc.matrices is not None else None
+    args = []
+    for k, (name, a) in enumerate(seq):
+        args += [name] + [float(v).hex() for v in a]
+        out = subprocess.check_output([ref_matrix] + args, text=True).split()
+        want = np.array([float.fromhex(v) for v in out], np.float32)
+        got = (m[k][[2, 5]] if m is not None else sc.paints[k]["translate"]).astype(np.float32)
+        assert want[[2, 5]].tobytes() == got.tobytes(), (k, seq[:k + 1], want, got)
