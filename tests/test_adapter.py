@@ -168,3 +168,17 @@ def test_scale_rotate_skew_forwarded(driver_output):
     assert driver_output[i + 21:i + 24] == ["save", clip, "set_matrix " + total[6:]]
     assert driver_output[i + 24].startswith("draw ")
     assert driver_output[i + 25:i + 28] == ["restore", "status=0", "restore"]
+
+
+def test_capi_binding_compiles(tmp_path):
+    """The module/capi binding of INTEGRATION.md (a skity_canvas handle over
+    the CUDA canvas) compiles against the reference's C API headers."""
+    if not os.path.isdir(os.path.join(REF, "module", "capi")):
+        pytest.skip("reference checkout not present")
+    cmd = ["g++", "-std=c++17", "-c", "-w", "-DSKITY_CPU", "-I" + ROOT,
+           "-I" + os.path.join(ROOT, "oracle", "ref", "glm_shim"), "-I" + REF + "/include",
+           "-I" + REF, "-I" + REF + "/src", "-I" + REF + "/module/capi/include",
+           "-I" + REF + "/module/capi/src", os.path.join(ROOT, "tests", "capi_binding.cc"),
+           "-o", str(tmp_path / "capi_binding.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
