@@ -108,6 +108,28 @@ class Path:
         """Path::AddRect(rect) with the default direction (CW, start 0)."""
         return self.MoveTo(l, t).LineTo(r, t).LineTo(r, b).LineTo(l, b).Close()
 
+    def AddOvalRRect(self, l, t, r, b):
+        """Path::AddRRect of RRect::SetOval(rect) (src/geometry/rrect.cc:
+        214-233, 353-367; src/graphic/path.cc:881-900, 1010-1040), the path
+        Canvas::DrawOval and DrawCircle draw: the rect sorted; an empty one
+        (or one with a zero half side) a rect path from its bottom-left
+        corner (Path::AddRect, start index 3); otherwise four conics of
+        weight FloatRoot2Over2, from (left, centre y) clockwise."""
+        f = np.float32
+        l, t, r, b = f(l), f(t), f(r), f(b)
+        if not all(np.isfinite(v) for v in (l, t, r, b)):
+            return self
+        l, r = min(l, r), max(l, r)
+        t, b = min(t, b), max(t, b)
+        empty = not (l < r and t < b)
+        half = f(0.5)
+        if empty or f(r * half) - f(l * half) == 0 or f(b * half) - f(t * half) == 0:
+            return self.MoveTo(l, b).LineTo(l, t).LineTo(r, t).LineTo(r, b).Close()
+        cx, cy = f(half * f(r + l)), f(half * f(t + b))
+        w = float(f(0.707106781))
+        return (self.MoveTo(l, cy).ConicTo(l, t, cx, t, w).ConicTo(r, t, r, cy, w)
+                .ConicTo(r, b, cx, b, w).ConicTo(l, b, l, cy, w).Close())
+
     def SetFillType(self, ft):
         self.fill_type = ft
         return self
@@ -455,6 +477,24 @@ class Canvas:
         c4 = Color4fFromColor(color) if isinstance(color, int) else tuple(color)
         arr = (ctypes.c_float * 4)(*c4)
         _lib.check(self.lib.skity_cuda_canvas_clear(self.handle, arr), "skity_cuda_canvas_clear")
+
+    def DrawOval(self, left, top, right, bottom, paint: Paint):
+        """Canvas::DrawOval(rect, paint) (canvas.cc:202-204, 418-430): the
+        oval's RRect path (Path.AddOvalRRect), drawn as DrawPath."""
+        self.DrawPath(Path().AddOvalRRect(left, top, right, bottom), paint)
+
+    def DrawCircle(self, cx, cy, radius, paint: Paint):
+        """Canvas::DrawCircle (canvas.cc:178-180, 407-416): a negative radius
+        is 0; the oval of the circle's bounds."""
+        f = np.float32
+        cx, cy, radius = f(cx), f(cy), f(radius)
+        if radius < 0:
+            radius = f(0)
+        self.DrawOval(cx - radius, cy - radius, cx + radius, cy + radius, paint)
+
+    def DrawRect(self, left, top, right, bottom, paint: Paint):
+        """Canvas::DrawRect (canvas.cc:206-208, 432-437): Path::AddRect."""
+        self.DrawPath(Path().AddRect(left, top, right, bottom), paint)
 
     def DrawPath(self, path: Path, paint: Paint):
         verbs = np.asarray(path.verbs, np.uint8)
