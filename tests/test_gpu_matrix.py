@@ -209,3 +209,43 @@ def test_canvas_clips_under_matrices(gpu_ctx, oracle_lib):
     sc = sb.build()
     assert sc.clip_matrices is not None
     check(oracle_lib, bitmap, sc)
+
+
+def test_canvas_shapes_match_oracle(gpu_ctx, oracle_lib):
+    """Canvas::DrawOval / DrawCircle / DrawRect on the CUDA canvas (fills and
+    strokes, under a scale and a rotation) against the oracle rendering the
+    same paths (the reference's RRect and rect paths, tests/test_shapes.py)."""
+    from skity_gb300.canvas import Canvas, Paint, Path
+    W, H = 128, 96
+    bitmap = np.zeros((H, W, 4), np.uint8)
+    canvas = Canvas.MakeCUDACanvas(gpu_ctx, bitmap)
+    canvas.Clear((1.0, 1.0, 1.0, 1.0))
+    sb = S.SceneBuilder(W, H)
+
+    def m6():
+        m9 = canvas.GetTotalMatrix()
+        return (m9[0], m9[1], m9[2], m9[3], m9[4], m9[5])
+
+    fill = Paint().SetFillColor(0.8, 0.2, 0.3, 0.8)
+    stroke = Paint().SetStyle(1).SetStrokeWidth(2.5).SetFillColor(0, 0, 0, 1)
+    stroke.SetStrokeColor(0.1, 0.4, 0.9, 0.9)
+    calls = [("oval", (8.0, 6.0, 60.5, 40.0), fill), ("circle", (90.0, 30.0, 18.25), stroke),
+             ("rect", (10.0, 50.0, 50.0, 90.0), fill), ("circle", (70.0, 70.0, 0.0), stroke)]
+    for k, (kind, a, paint) in enumerate(calls):
+        if k == 2:
+            canvas.Scale(1.2, 0.9)
+        if k == 3:
+            canvas.Rotate(15, 64, 48)
+        if kind == "oval":
+            canvas.DrawOval(*a, paint)
+            path = Path().AddOvalRRect(*a)
+        elif kind == "circle":
+            canvas.DrawCircle(*a, paint)
+            cx, cy, r = (np.float32(v) for v in a)
+            path = Path().AddOvalRRect(cx - r, cy - r, cx + r, cy + r)
+        else:
+            canvas.DrawRect(*a, paint)
+            path = Path().AddRect(*a)
+        sb.draw_path(path.verbs, path.points, paint.rec, path.weights, matrix=m6())
+    canvas.Flush()
+    check(oracle_lib, bitmap, sb.build())
